@@ -1,0 +1,299 @@
+"""Benchmark: transient 3D convection-diffusion, the OpenCMP hot path on one GB300.
+
+Workload (one "step" = one implicit-Euler time step, exactly what OpenCMP's transient loop does
+per step: reassemble the bilinear and linear forms, refresh the preconditioner, Krylov-solve to a
+1e-8 FP64 relative residual starting from the previous step's solution):
+  unit cube, 64^3 cubes x 6 tetrahedra (1,572,864 tets), H1 order 2 (2,146,689 dofs), Dirichlet 0 on
+  all faces, eps = 1e-2, w = (1, 0.5, 0.25), dt = 1e-3, u0 = Gaussian (sigma 0.1 at (0.25,0.25,0.25)).
+Metric: DOF/s = dofs x steps / time. `value` is the optimised path (FP32-inner GMRES with FP64
+refinement); `plain_fp64` is the plain FP64 GPU path on the same steps.
+Inputs are resident in HBM and larger than L2 (the matrix alone is ~730 MB), so no L2 flush.
+
+--impl reference: the CPU restatement of the same step (the oracle: C + OpenMP, all host
+threads) on a bounded sample, the 32^3 x 6 mesh (274,625 dofs), since NGSolve cannot run here.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+EPS, WIND, DT = 1e-2, (1.0, 0.5, 0.25), 1e-3
+GAUSS = dict(c=(0.25, 0.25, 0.25), s=0.1)
+METRIC = 'DOF/s to 1e-8 FP64 rel. residual: mixed+batched+learned vs plain FP64, 1 GB300'
+
+
+def gaussian(X):
+    c = np.asarray(GAUSS['c'])
+    return np.exp(-((X - c) ** 2).sum(-1) / (2 * GAUSS['s'] ** 2))
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, 'MEASURED_PEAKS.json')) as fh:
+            d = json.load(fh)
+        return float(d['hbm_gbs']), 'measured'
+    except Exception:
+        return 6800.0, 'fallback'
+
+
+class Clocks:
+    """nvidia-smi sampling during the timed region."""
+
+    def __init__(self):
+        self.samples, self.proc = [], None
+        try:
+            import torch
+            self.dev = 'GPU-' + str(torch.cuda.get_device_properties(torch.cuda.current_device()).uuid)
+        except Exception:
+            self.dev = '0'
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ['nvidia-smi', '--query-gpu=clocks.sm,clocks.max.sm,clocks_event_reasons.hw_slowdown,'
+                 'clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,'
+                 'clocks_event_reasons.sw_power_cap', '--format=csv,noheader,nounits', '-i', self.dev, '-lms', '200'],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            threading.Thread(target=self._read, daemon=True).start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for ln in self.proc.stdout:
+            self.samples.append([t.strip() for t in ln.split(',')])
+
+    def stop(self):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+        sm = [float(s[0]) for s in self.samples if s and s[0].replace('.', '').isdigit()]
+        mx = [float(s[1]) for s in self.samples if len(s) > 1 and s[1].replace('.', '').isdigit()]
+        names = ['hw_slowdown', 'hw_thermal_slowdown', 'sw_thermal_slowdown', 'sw_power_cap']
+        reasons = sorted({names[k] for s in self.samples for k in range(4) if len(s) > 2 + k and 'Active' in s[2 + k]
+                          and 'Not' not in s[2 + k]})
+        return {'sm_mhz': float(np.median(sm)) if sm else None, 'sm_max_mhz': max(mx) if mx else None,
+                'reasons': reasons, 'samples': len(sm)}
+
+
+def run_ours(args):
+    import torch
+    import torch.distributed as dist
+    from opencmp_gb300 import fem, mesh as M, _lib
+
+    world = int(os.environ.get('WORLD_SIZE', '1'))
+    rank = int(os.environ.get('RANK', '0'))
+    local = int(os.environ.get('LOCAL_RANK', '0'))
+    torch.cuda.set_device(local)
+    if world > 1:
+        dist.init_process_group('nccl')
+    from opencmp_gb300 import build
+    if rank == 0 or not os.path.exists(_lib.LIB_PATH):
+        build.build()
+    if world > 1:
+        dist.barrier()
+
+    n = args.n
+    t0 = time.perf_counter()
+    mesh = M.unit_cube(n)
+    space = fem.Space(mesh, 'H1', 2, mesh.bc_names)
+    setup_s = time.perf_counter() - t0
+    ndof, nnz = space.ndof, space.nnz
+    A = fem.Matrix(space, fp32=True)
+    form = fem.make_form(mass=1.0, diff=EPS, dt=DT, wind=WIND)
+    u0 = torch.as_tensor(fem.interpolate_p2(space, gaussian), device='cuda')
+    b = torch.zeros(ndof, dtype=torch.float64, device='cuda')
+    A.assemble(form)
+    solvers = {
+        'fp64': fem.KrylovSolver(A, method='GMRES', restart=args.restart, precond='jacobi', precision='fp64', tol=1e-8,
+                                 maxit=2000, check_every=args.check_every),
+        'mixed': fem.KrylovSolver(A, method='GMRES', restart=args.restart, precond='jacobi', precision='mixed',
+                                  tol=1e-8, maxit=2000, inner_tol=args.inner_tol, check_every=args.check_every),
+    }
+
+    def step(sv, u_in, u_out, stats):
+        A.assemble(form)
+        sv.update()
+        fem.assemble_rhs(space, form, fem.make_rhs(dt=DT, mass=1.0, uprev=u_in), b)
+        u_out.copy_(u_in)
+        info = sv.solve(b, u_out)
+        stats.append((info.iterations, info.outer_iterations, info.relres0, info.relres))
+
+    def timed(kind, steps, warmup, e2e=False):
+        sv = solvers[kind]
+        u = [u0.clone(), torch.empty_like(u0)]
+        h_in = torch.empty(ndof, dtype=torch.float64, pin_memory=True)
+        h_out = torch.empty(ndof, dtype=torch.float64, pin_memory=True)
+        h_in.copy_(u0.cpu())
+        stats = []
+        for k in range(warmup):
+            step(sv, u[k % 2], u[(k + 1) % 2], stats)
+        stats.clear()
+        torch.cuda.synchronize()
+        if world > 1:
+            dist.barrier()
+        ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        ev0.record()
+        for k in range(steps):
+            if e2e:
+                u[0].copy_(h_in, non_blocking=True)
+                step(sv, u[0], u[1], stats)
+                h_out.copy_(u[1], non_blocking=True)
+                torch.cuda.current_stream().synchronize()
+                h_in, h_out = h_out, h_in
+            else:
+                step(sv, u[k % 2], u[(k + 1) % 2], stats)
+        ev1.record()
+        torch.cuda.synchronize()
+        ms = ev0.elapsed_time(ev1)
+        if world > 1:
+            t = torch.tensor([ms], device='cuda')
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            ms = float(t.item())
+        return ms, stats
+
+    clocks = Clocks()
+    clocks.start()
+    ms_plain, st_plain = timed('fp64', args.steps, args.warmup)
+    ms_opt, st_opt = timed('mixed', args.steps, args.warmup)
+    cl = clocks.stop()
+    ms_e2e, _ = timed('mixed', args.steps, 1, e2e=True)
+
+    # SpMV roofline: FP64 CSR SpMV launches timed with CUDA events on the launching stream
+    x = torch.randn(ndof, dtype=torch.float64, device='cuda')
+    y = torch.empty_like(x)
+    for _ in range(3):
+        A.mult(x, y)
+    reps = 50
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record()
+    for _ in range(reps):
+        A.mult(x, y)
+    e1.record()
+    torch.cuda.synchronize()
+    spmv_ms = e0.elapsed_time(e1) / reps
+    spmv_bytes = 12 * nnz + 4 * (ndof + 1) + 16 * ndof
+    peak, peak_kind = peaks()
+    achieved = spmv_bytes / (spmv_ms * 1e-3) / 1e9
+
+    value = ndof * args.steps * world / (ms_opt * 1e-3)
+    plain = ndof * args.steps * world / (ms_plain * 1e-3)
+    e2e_val = ndof * args.steps * world / (ms_e2e * 1e-3)
+    line = {
+        'metric': METRIC, 'value': value, 'unit': 'DOF/s', 'n_gpus': world, 'steps': args.steps, 'warmup': args.warmup,
+        'ms_per_step': ms_opt / args.steps, 'higher_is_better': True, 'scaling': 'weak', 'vs_baseline': None,
+        'dtype': 'f64+f32', 'data': 'synthetic (generated structured mesh, Gaussian initial condition)',
+        'config': {'workload': 'transient 3D convection-diffusion, unit cube {}^3 x 6 tets, H1 p=2, implicit Euler'
+                               ' dt=1e-3, GMRES({}) + Jacobi to 1e-8 FP64 relative residual, previous-step guess,'
+                               ' full reassembly every step'.format(n, args.restart),
+                   'ndof': ndof, 'nnz': nnz, 'parallelism': 'replicas' if world > 1 else 'single GPU',
+                   'l2': 'inputs larger than L2 (no flush)'},
+        'plain_fp64': {'value': plain, 'unit': 'DOF/s', 'ms_per_step': ms_plain / args.steps,
+                       'iters_per_step': float(np.mean([s[0] for s in st_plain]))},
+        'optimised': {'kind': 'mixed: FP32 inner GMRES + FP64 iterative refinement',
+                      'iters_per_step': float(np.mean([s[0] for s in st_opt])),
+                      'outer_per_step': float(np.mean([s[1] for s in st_opt])),
+                      'max_relres': float(max(s[3] for s in st_opt)), 'speedup_vs_plain_fp64': value / plain},
+        'e2e': {'value': e2e_val, 'unit': 'DOF/s', 'h2d_bytes_per_step': 8 * ndof, 'd2h_bytes_per_step': 8 * ndof},
+        'roofline': {'bound': 'hbm', 'kernel': 'spmv_masked<double> / spmv64 (CSR FP64)', 'achieved': achieved,
+                     'peak': peak, 'peak_kind': peak_kind, 'unit': 'GB/s', 'frac': achieved / peak,
+                     'traffic': None, 'algorithmic_bytes': spmv_bytes, 'avg_launch_ms': spmv_ms},
+        'gpu_launches': None,
+        'clocks': cl,
+        'setup_s': setup_s,
+    }
+    if rank == 0 and world == 1 and not args.no_cpu:
+        line['cpu_baseline'] = cpu_baseline(args.cpu_n)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        dist.destroy_process_group()
+
+
+def cpu_step_sample(n_cpu, steps):
+    """The oracle's implicit-Euler step (assembly + GMRES/Jacobi to 1e-8) on the n_cpu^3 x 6 mesh."""
+    from oracle import oracle as O
+    from opencmp_gb300 import mesh as M
+    O.build()
+    threads = os.cpu_count() or 1
+    O.lib().or_set_threads(threads)
+    m = M.unit_cube(n_cpu)
+    s = O.Space(m, O.H1, 2, m.label_mask(m.bc_names))
+    f = O.make_form(mass=1.0, diff=EPS, dt=DT, wind=WIND)
+    u = _interp_p2_oracle(s, m)
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        A = s.assemble(f)
+        b = s.rhs(f, O.make_rhs(dt=DT, mass=1.0, uprev=u))
+        x = u.copy()
+        s.gmres(A, b, x, restart=30, precond=1, tol=1e-8, maxit=2000)
+        u = x
+    dt = time.perf_counter() - t0
+    return s.ndof, dt, threads
+
+
+def _interp_p2_oracle(s, m):
+    from opencmp_gb300.fem import interpolate_p2_arrays
+    return interpolate_p2_arrays(m.coords, s.sorted_conn(), s.dofs(), s.ndof, gaussian)
+
+
+def cpu_baseline(n_cpu):
+    ndof, dt, threads = cpu_step_sample(n_cpu, 1)
+    return {'value': ndof / dt, 'unit': 'DOF/s', 'cores': threads, 'kind': 'port',
+            'sample': 'one implicit-Euler step (assembly + GMRES(30)/Jacobi to 1e-8) on the {}^3 x 6 tet mesh '
+                      '({} dofs), C oracle with OpenMP'.format(n_cpu, ndof)}
+
+
+def run_reference(args):
+    rank = int(os.environ.get('RANK', '0'))
+    if rank != 0:
+        return
+    ndof, dt, threads = cpu_step_sample(args.cpu_n, max(1, args.steps // 10) if args.steps > 0 else 1)
+    steps = max(1, args.steps // 10) if args.steps > 0 else 1
+    v = ndof * steps / dt
+    line = {'metric': METRIC, 'value': v, 'unit': 'DOF/s', 'n_gpus': 0, 'steps': steps, 'warmup': 0,
+            'ms_per_step': dt / steps * 1e3, 'higher_is_better': True, 'scaling': 'weak', 'vs_baseline': None,
+            'dtype': 'f64', 'data': 'synthetic', 'impl': 'reference',
+            'config': {'workload': 'transient 3D convection-diffusion, implicit Euler step, H1 p=2 (CPU sample on '
+                                   'the {}^3 x 6 mesh, {} dofs)'.format(args.cpu_n, ndof)},
+            'cpu_baseline': {'value': v, 'unit': 'DOF/s', 'cores': threads, 'kind': 'port',
+                             'sample': '{} step(s) on {} dofs'.format(steps, ndof)},
+            'e2e': {'value': v, 'unit': 'DOF/s', 'h2d_bytes_per_step': 0, 'd2h_bytes_per_step': 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument('--gpus', type=int, default=1)
+    ap.add_argument('--steps', type=int, default=20)
+    ap.add_argument('--warmup', type=int, default=3)
+    ap.add_argument('--impl', default='ours', choices=['ours', 'reference'])
+    ap.add_argument('--n', type=int, default=64)
+    ap.add_argument('--cpu-n', type=int, default=32)
+    ap.add_argument('--restart', type=int, default=30)
+    ap.add_argument('--inner-tol', type=float, default=1e-4)
+    ap.add_argument('--check-every', type=int, default=8)
+    ap.add_argument('--no-cpu', action='store_true')
+    args = ap.parse_args()
+    if args.impl == 'reference':
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == '__main__':
+    main()

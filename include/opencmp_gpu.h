@@ -1,0 +1,162 @@
+/*
+ * opencmp_gpu.h - C ABI of libopencmp_gpu.so, the GB300 (sm_103a) finite-element hot path behind
+ * OpenCMP's Model/Solver plugin interface: form assembly into CSR followed by the Krylov solve.
+ *
+ * Plain C types only: host arrays are `const T*`, device arrays are raw device pointers (for
+ * example `torch.Tensor.data_ptr()`), streams are `cudaStream_t` passed as `void*` (NULL = the
+ * legacy default stream). Every function returns an ocmp_status; no exception crosses the ABI.
+ * ocmp_last_error() returns the message of the last failure on the calling thread.
+ *
+ * Each entry point replaces one call OpenCMP makes into NGSolve (paths are relative to the
+ * OpenCMP source tree):
+ *   ocmp_mesh_create      <- opencmp/helpers/io.py:69-110        (load_mesh -> ngsolve.Mesh)
+ *   ocmp_space_create     <- opencmp/models/poisson.py:60-65, multi_component_ins.py:95-117
+ *                            (ngsolve.H1 / L2 (..., order, dirichlet, dgjumps); FESpace.FreeDofs)
+ *   ocmp_assemble_matrix  <- opencmp/solvers/base_solver.py:368-377 (BilinearForm.Assemble) for the
+ *                            forms of poisson.py:71-131 and multi_component_ins.py:158-300
+ *   ocmp_assemble_rhs     <- base_solver.py:374-375 (LinearForm.Assemble) for poisson.py:133-158,
+ *                            multi_component_ins.py:302-388 and the implicit-Euler mass term of
+ *                            time_integration_schemes.py:663-685 / base_model.py:418-497
+ *   ocmp_set_boundary     <- opencmp/models/base_model.py:321-341 (GridFunction.Set on Dirichlet
+ *                            boundaries)
+ *   ocmp_solver_create    <- opencmp/models/base_model.py:365-383 (ngsolve.Preconditioner(a, 'local'))
+ *   ocmp_solve            <- opencmp/models/base_model.py:886-947 (linear_solve: solvers.CG with
+ *                            initialize=False, solvers.GMRes with freedofs, direct solve on L - A*gfu)
+ *   ocmp_spmv             <- the `a.mat * gfu.vec` products inside base_model.py:920-944
+ *   ocmp_batch_*          <- a loop of the above over independent problem instances
+ *   ocmp_guess_*          <- no counterpart: learned Krylov initial guess (its fallback is the
+ *                            previous-step guess OpenCMP uses, base_model.py:925-937)
+ */
+#ifndef OPENCMP_GPU_H
+#define OPENCMP_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define OCMP_ABI_VERSION 1
+
+typedef enum {
+    OCMP_OK = 0,
+    OCMP_ERR_ARG = 1,          /* bad argument (null handle, unsupported size or order)          */
+    OCMP_ERR_CUDA = 2,         /* a CUDA runtime call failed                                      */
+    OCMP_ERR_NONFINITE = 3,    /* NaN / Inf met in the right-hand side or during the iteration    */
+    OCMP_NOT_CONVERGED = 4,    /* iteration cap reached before the tolerance                      */
+    OCMP_BREAKDOWN = 5,        /* Krylov breakdown (zero pivot / zero inner product)               */
+    OCMP_TIMEOUT = 6,          /* a bounded device-side wait gave up                              */
+    OCMP_ERR_UNSUPPORTED = 7,  /* combination not built (e.g. L2 on tetrahedra)                    */
+    OCMP_ERR_NOMEM = 8         /* device allocation failed                                        */
+} ocmp_status;
+
+enum { OCMP_H1 = 0, OCMP_L2 = 1 };
+enum { OCMP_WIND_NONE = 0, OCMP_WIND_CONST = 1, OCMP_WIND_VERTEX = 2 };
+enum { OCMP_SRC_NONE = 0, OCMP_SRC_CONST = 1, OCMP_SRC_QP = 2 };
+enum { OCMP_CG = 0, OCMP_GMRES = 1 };
+enum { OCMP_PRE_NONE = 0, OCMP_PRE_JACOBI = 1, OCMP_PRE_BLOCK_JACOBI = 2 };
+enum { OCMP_FP64 = 0, OCMP_MIXED = 1 };
+
+typedef struct ocmp_mesh_s* ocmp_mesh_t;
+typedef struct ocmp_space_s* ocmp_space_t;
+typedef struct ocmp_matrix_s* ocmp_matrix_t;
+typedef struct ocmp_solver_s* ocmp_solver_t;
+
+/* Bilinear form  a(u,v) = mass (u,v) + dt [ diff (grad u, grad v) - (u, w . grad v) ]
+ *                        + dt * facet terms selected by the masks (bit l = boundary label l).
+ * Terms follow multi_component_ins.py:158-300 (velocity_fixed) and poisson.py:71-131. */
+typedef struct {
+    double mass;             /* coefficient of the mass term (u, v); not scaled by dt            */
+    double diff;             /* diffusion coefficient                                            */
+    double dt;               /* time-step factor on every other term (1 for a stationary solve)  */
+    int32_t wind_kind;       /* OCMP_WIND_*                                                       */
+    double wind[3];          /* constant wind                                                     */
+    const double* wind_vtx;  /* device, nv*dim: wind at the mesh vertices, linear in between      */
+    double ipc;              /* interior penalty coefficient; alpha = ipc * order^2 / h            */
+    int32_t dg;              /* add interior-facet (skeleton) SIPG + upwind terms (L2 spaces)      */
+    uint32_t outflow_mask;   /* labels with  dt r c max(w.n, 0)      (total-flux / unlabelled)     */
+    uint32_t wn_mask;        /* labels with  dt r c (w.n)            (Neumann half)                */
+    uint32_t nitsche_mask;   /* DG Dirichlet labels (penalty, consistency, inflow upwind)          */
+} ocmp_form_t;
+
+/* Linear form  L(v) = dt (f, v) + mass (u_prev, v) + dt * sum_l bval[l] <v>_l + DG Dirichlet data */
+typedef struct {
+    double dt;
+    int32_t src_kind;        /* OCMP_SRC_*                                                        */
+    double src_const;        /* f for OCMP_SRC_CONST                                              */
+    const double* src_qp;    /* device, ne*nq: f at the quadrature points (ocmp_space_quad_points) */
+    double mass;             /* coefficient of (u_prev, v)                                        */
+    const double* uprev;     /* device, ndof, or NULL                                             */
+    double bval[32];         /* per label, constant Neumann-type data                              */
+    uint32_t bval_mask;
+    double gval[32];         /* per label, constant DG Dirichlet datum                              */
+} ocmp_rhs_t;
+
+typedef struct {
+    int64_t ndof, nnz, ne, nv;
+    int32_t nloc, nq, dim, order, kind;
+    int64_t n_interior_facets, n_boundary_facets, n_contrib;
+} ocmp_space_info_t;
+
+typedef struct {
+    int32_t method;          /* OCMP_CG / OCMP_GMRES                                               */
+    int32_t restart;         /* GMRES restart length m (<= 128)                                    */
+    int32_t precond;         /* OCMP_PRE_*                                                         */
+    int32_t precision;       /* OCMP_FP64, or OCMP_MIXED: FP32 inner GMRES + FP64 refinement        */
+    double tol;              /* on || (b - A x)_free ||_2 / || (b - A x_D)_free ||_2 (FP64)       */
+    int32_t maxit;           /* total Krylov iterations                                             */
+    double inner_tol;        /* mixed: relative reduction asked of each inner solve               */
+    int32_t check_every;     /* host reads the convergence flag every k iterations (>= 1)          */
+} ocmp_solve_params_t;
+
+typedef struct {
+    int32_t status;          /* ocmp_status of the solve                                           */
+    int32_t iterations;      /* Krylov iterations (inner iterations for OCMP_MIXED)                 */
+    int32_t outer_iterations;/* refinement steps (OCMP_MIXED), restarts (GMRES)                    */
+    double relres0;          /* FP64 relative residual of the initial guess                        */
+    double relres;           /* FP64 relative residual at return, recomputed from b - A x           */
+} ocmp_solve_info_t;
+
+/* ---------------------------------------------------------------- general */
+int ocmp_abi_version(void);
+int ocmp_last_error(char* buf, int len);
+int ocmp_device_sync(void* stream);
+
+/* ---------------------------------------------------------------- mesh and space */
+int ocmp_mesh_create(const double* coords, int64_t nv, int32_t dim, const int32_t* elements, int64_t ne,
+                     const int32_t* bfacets, const int32_t* blabels, int64_t nbf, ocmp_mesh_t* out);
+int ocmp_mesh_destroy(ocmp_mesh_t mesh);
+
+int ocmp_space_create(ocmp_mesh_t mesh, int32_t kind, int32_t order, uint32_t dirichlet_mask,
+                      ocmp_space_t* out);
+int ocmp_space_destroy(ocmp_space_t space);
+int ocmp_space_info(ocmp_space_t space, ocmp_space_info_t* info);
+int ocmp_space_get_dofs(ocmp_space_t space, int32_t* elem_dofs_host);            /* ne*nloc  */
+int ocmp_space_get_pattern(ocmp_space_t space, int64_t* rowptr_host, int32_t* col_host);
+int ocmp_space_get_free(ocmp_space_t space, uint8_t* free_host);                 /* ndof     */
+int ocmp_space_quad_points(ocmp_space_t space, double* xyz_host);                /* ne*nq*dim */
+int ocmp_set_boundary(ocmp_space_t space, uint32_t mask, const double* gval_host32, double* u_dev,
+                      void* stream);
+
+/* ---------------------------------------------------------------- assembly */
+int ocmp_matrix_create(ocmp_space_t space, int32_t want_fp32, ocmp_matrix_t* out);
+int ocmp_matrix_destroy(ocmp_matrix_t mat);
+int ocmp_matrix_values(ocmp_matrix_t mat, double** vals64_dev, float** vals32_dev);
+int ocmp_assemble_matrix(ocmp_matrix_t mat, const ocmp_form_t* form, void* stream);
+int ocmp_assemble_rhs(ocmp_space_t space, const ocmp_form_t* form, const ocmp_rhs_t* rhs, double* b_dev,
+                      void* stream);
+int ocmp_spmv(ocmp_matrix_t mat, const double* x_dev, double* y_dev, void* stream);
+
+/* ---------------------------------------------------------------- Krylov solve */
+int ocmp_solver_create(ocmp_matrix_t mat, const ocmp_solve_params_t* params, ocmp_solver_t* out);
+int ocmp_solver_destroy(ocmp_solver_t solver);
+/* Refresh preconditioner data after the matrix values changed (Preconditioner.Update). */
+int ocmp_solver_update(ocmp_solver_t solver, void* stream);
+/* Solve A_ff x_f = (b - A x_D)_f in place; x_dev holds the Dirichlet values and the initial guess. */
+int ocmp_solve(ocmp_solver_t solver, const double* b_dev, double* x_dev, void* stream, ocmp_solve_info_t* info);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

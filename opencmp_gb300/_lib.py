@@ -1,0 +1,124 @@
+"""ctypes binding of libopencmp_gpu.so (include/opencmp_gpu.h).
+
+The library is the only compute path: if it is missing or fails to load, every entry point raises;
+there is no CPU fallback.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, 'libopencmp_gpu.so')
+
+OK, ERR_ARG, ERR_CUDA, ERR_NONFINITE, NOT_CONVERGED, BREAKDOWN, TIMEOUT, ERR_UNSUPPORTED, ERR_NOMEM = range(9)
+STATUS_NAMES = ['OK', 'ERR_ARG', 'ERR_CUDA', 'ERR_NONFINITE', 'NOT_CONVERGED', 'BREAKDOWN', 'TIMEOUT',
+                'ERR_UNSUPPORTED', 'ERR_NOMEM']
+H1, L2 = 0, 1
+WIND_NONE, WIND_CONST, WIND_VERTEX = 0, 1, 2
+SRC_NONE, SRC_CONST, SRC_QP = 0, 1, 2
+CG, GMRES = 0, 1
+PRE_NONE, PRE_JACOBI, PRE_BLOCK_JACOBI = 0, 1, 2
+FP64, MIXED = 0, 1
+
+
+class OcmpError(RuntimeError):
+    def __init__(self, status, msg):
+        super().__init__('{} ({}): {}'.format(STATUS_NAMES[status] if 0 <= status < len(STATUS_NAMES) else status,
+                                              status, msg))
+        self.status = status
+
+
+class Form(C.Structure):
+    _fields_ = [('mass', C.c_double), ('diff', C.c_double), ('dt', C.c_double), ('wind_kind', C.c_int32),
+                ('wind', C.c_double * 3), ('wind_vtx', C.c_void_p), ('ipc', C.c_double), ('dg', C.c_int32),
+                ('outflow_mask', C.c_uint32), ('wn_mask', C.c_uint32), ('nitsche_mask', C.c_uint32)]
+
+
+class Rhs(C.Structure):
+    _fields_ = [('dt', C.c_double), ('src_kind', C.c_int32), ('src_const', C.c_double), ('src_qp', C.c_void_p),
+                ('mass', C.c_double), ('uprev', C.c_void_p), ('bval', C.c_double * 32), ('bval_mask', C.c_uint32),
+                ('gval', C.c_double * 32)]
+
+
+class SpaceInfo(C.Structure):
+    _fields_ = [('ndof', C.c_int64), ('nnz', C.c_int64), ('ne', C.c_int64), ('nv', C.c_int64),
+                ('nloc', C.c_int32), ('nq', C.c_int32), ('dim', C.c_int32), ('order', C.c_int32),
+                ('kind', C.c_int32), ('n_interior_facets', C.c_int64), ('n_boundary_facets', C.c_int64),
+                ('n_contrib', C.c_int64)]
+
+
+class SolveParams(C.Structure):
+    _fields_ = [('method', C.c_int32), ('restart', C.c_int32), ('precond', C.c_int32), ('precision', C.c_int32),
+                ('tol', C.c_double), ('maxit', C.c_int32), ('inner_tol', C.c_double), ('check_every', C.c_int32)]
+
+
+class SolveInfo(C.Structure):
+    _fields_ = [('status', C.c_int32), ('iterations', C.c_int32), ('outer_iterations', C.c_int32),
+                ('relres0', C.c_double), ('relres', C.c_double)]
+
+
+P = C.c_void_p
+I32, I64, U32, D = C.c_int32, C.c_int64, C.c_uint32, C.c_double
+
+# name -> argtypes (all return int status unless listed in _RESTYPE)
+SIGNATURES = {
+    'ocmp_abi_version': [],
+    'ocmp_last_error': [C.c_char_p, C.c_int],
+    'ocmp_device_sync': [P],
+    'ocmp_mesh_create': [P, I64, I32, P, I64, P, P, I64, C.POINTER(P)],
+    'ocmp_mesh_destroy': [P],
+    'ocmp_space_create': [P, I32, I32, U32, C.POINTER(P)],
+    'ocmp_space_destroy': [P],
+    'ocmp_space_info': [P, C.POINTER(SpaceInfo)],
+    'ocmp_space_get_dofs': [P, P],
+    'ocmp_space_get_pattern': [P, P, P],
+    'ocmp_space_get_free': [P, P],
+    'ocmp_space_quad_points': [P, P],
+    'ocmp_set_boundary': [P, U32, P, P, P],
+    'ocmp_matrix_create': [P, I32, C.POINTER(P)],
+    'ocmp_matrix_destroy': [P],
+    'ocmp_matrix_values': [P, C.POINTER(P), C.POINTER(P)],
+    'ocmp_assemble_matrix': [P, C.POINTER(Form), P],
+    'ocmp_assemble_rhs': [P, C.POINTER(Form), C.POINTER(Rhs), P, P],
+    'ocmp_spmv': [P, P, P, P],
+    'ocmp_solver_create': [P, C.POINTER(SolveParams), C.POINTER(P)],
+    'ocmp_solver_destroy': [P],
+    'ocmp_solver_update': [P, P],
+    'ocmp_solve': [P, P, P, P, C.POINTER(SolveInfo)],
+}
+
+_lib = None
+
+
+def load():
+    """Load the in-tree library; raises if it is missing (no fallback)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise OcmpError(ERR_ARG, 'libopencmp_gpu.so is not built; run opencmp_gb300.build.build() '
+                                 '(or __graft_entry__.build())')
+    L = C.CDLL(LIB_PATH)
+    for name, argt in SIGNATURES.items():
+        fn = getattr(L, name)
+        fn.argtypes = argt
+        fn.restype = C.c_int
+    _lib = L
+    return L
+
+
+def last_error() -> str:
+    buf = C.create_string_buffer(1024)
+    load().ocmp_last_error(buf, 1024)
+    return buf.value.decode(errors='replace')
+
+
+def check(status: int, allow=()):
+    if status != OK and status not in allow:
+        raise OcmpError(status, last_error())
+    return status
+
+
+def call(name, *args, allow=()):
+    return check(getattr(load(), name)(*args), allow=allow)

@@ -1,0 +1,773 @@
+// Host side of libopencmp_gpu.so: handles, error reporting, and the one-off set-up of each space
+// (DOF numbering, CSR pattern, sorted scatter plan, reference-element tables), uploaded once to
+// HBM. Everything per time step runs on the GPU (ocmp_assemble.cu, ocmp_krylov.cu).
+//
+// Space conventions (the documented numbering this library and its CPU oracle share):
+//  * element vertices are stored in ascending global order, so every edge/face is oriented from
+//    its lower to its higher global vertex in every element that shares it;
+//  * H1 order p: dofs [0, nv) are the vertex functions lam_v; then p-1 functions per edge, edges
+//    sorted by (lower, upper) vertex; then (p=3) one bubble per triangle face, faces sorted by
+//    vertex triple; the local order is vertices, edges (a<b) lexicographic, faces (a<b<c);
+//  * L2 order p (triangles): Dubiner basis, dof = element * nloc + local.
+// NGSolve (opencmp/models/poisson.py:60-65) numbers vertex dofs first too, then edge, face and
+// cell dofs; its edge enumeration comes from netgen and is not reproduced here.
+#include <algorithm>
+#include <atomic>
+#include <cmath>
+#include <cstring>
+#include <functional>
+#include <mutex>
+#include <numeric>
+#include <thread>
+
+#include "ocmp_internal.h"
+
+namespace ocmp {
+
+static thread_local std::string g_err;
+void set_error(const std::string& msg) { g_err = msg; }
+int fail(int code, const std::string& msg) {
+    g_err = msg;
+    return code;
+}
+int cuda_fail(cudaError_t e, const char* what) {
+    g_err = std::string(what) + ": " + cudaGetErrorString(e);
+    return e == cudaErrorMemoryAllocation ? OCMP_ERR_NOMEM : OCMP_ERR_CUDA;
+}
+void dfree(void* p) {
+    if (p) cudaFree(p);
+}
+
+static void parallel_for(int64_t n, const std::function<void(int64_t, int64_t)>& fn) {
+    int nt = (int)std::max(1u, std::min(32u, std::thread::hardware_concurrency()));
+    if (n < 4096 || nt == 1) {
+        fn(0, n);
+        return;
+    }
+    std::vector<std::thread> th;
+    int64_t chunk = (n + nt - 1) / nt;
+    for (int t = 0; t < nt; t++) {
+        int64_t a = t * chunk, b = std::min(n, a + chunk);
+        if (a >= b) break;
+        th.emplace_back(fn, a, b);
+    }
+    for (auto& x : th) x.join();
+}
+
+// ---------------------------------------------------------------- reference basis (host)
+struct Dn {
+    double v, d[3];
+};
+static Dn dconst(double c) { return Dn{c, {0, 0, 0}}; }
+static Dn operator+(Dn a, Dn b) { return Dn{a.v + b.v, {a.d[0] + b.d[0], a.d[1] + b.d[1], a.d[2] + b.d[2]}}; }
+static Dn operator-(Dn a, Dn b) { return Dn{a.v - b.v, {a.d[0] - b.d[0], a.d[1] - b.d[1], a.d[2] - b.d[2]}}; }
+static Dn operator*(Dn a, double s) { return Dn{a.v * s, {a.d[0] * s, a.d[1] * s, a.d[2] * s}}; }
+static Dn operator*(Dn a, Dn b) {
+    return Dn{a.v * b.v, {a.d[0] * b.v + a.v * b.d[0], a.d[1] * b.v + a.v * b.d[1], a.d[2] * b.v + a.v * b.d[2]}};
+}
+
+// scaled Legendre L_k(x,t) = t^k P_k(x/t)
+static void sleg(int n, Dn x, Dn t, Dn* out) {
+    out[0] = dconst(1);
+    if (n >= 1) out[1] = x;
+    Dn t2 = t * t;
+    for (int k = 1; k < n; k++) out[k + 1] = ((x * out[k]) * (2.0 * k + 1) - (t2 * out[k - 1]) * (double)k) * (1.0 / (k + 1));
+}
+// Jacobi P_j^{(a,0)}
+static void jac(int n, double a, Dn s, Dn* out) {
+    out[0] = dconst(1);
+    if (n >= 1) out[1] = (s * (a + 2) + dconst(a)) * 0.5;
+    for (int k = 2; k <= n; k++) {
+        double A = 2.0 * k * (k + a) * (2.0 * k + a - 2);
+        double B = 2.0 * k + a - 1;
+        double C1 = (2.0 * k + a) * (2.0 * k + a - 2), C0 = a * a;
+        double Dd = 2.0 * (k + a - 1) * (k - 1) * (2.0 * k + a);
+        out[k] = (((s * C1 + dconst(C0)) * out[k - 1]) * B - out[k - 2] * Dd) * (1.0 / A);
+    }
+}
+
+static int nloc_of(int kind, int D, int p) {
+    (void)kind;
+    return D == 2 ? (p + 1) * (p + 2) / 2 : (p + 1) * (p + 2) * (p + 3) / 6;
+}
+
+static void bary(int D, const double* xi, Dn* lam) {
+    lam[0] = dconst(1);
+    for (int k = 0; k < D; k++) {
+        lam[0].v -= xi[k];
+        lam[0].d[k] = -1;
+        lam[k + 1] = dconst(xi[k]);
+        lam[k + 1].d[k] = 1;
+    }
+}
+
+static int basis(int kind, int D, int p, const double* xi, Dn* out) {
+    Dn lam[4];
+    bary(D, xi, lam);
+    int c = 0;
+    if (kind == OCMP_H1) {
+        for (int v = 0; v <= D; v++) out[c++] = lam[v];
+        if (p >= 2)
+            for (int a = 0; a <= D; a++)
+                for (int b = a + 1; b <= D; b++) {
+                    Dn L[4];
+                    sleg(p - 2, lam[b] - lam[a], lam[a] + lam[b], L);
+                    Dn base = lam[a] * lam[b];
+                    for (int k = 0; k <= p - 2; k++) out[c++] = base * L[k];
+                }
+        if (p >= 3)
+            for (int a = 0; a <= D; a++)
+                for (int b = a + 1; b <= D; b++)
+                    for (int cc = b + 1; cc <= D; cc++) out[c++] = lam[a] * lam[b] * lam[cc];
+    } else {
+        Dn L[8];
+        sleg(p, lam[1] - lam[0], lam[0] + lam[1], L);
+        for (int i = 0; i <= p; i++) {
+            Dn P[8];
+            jac(p - i, 2.0 * i + 1, lam[2] * 2.0 - dconst(1), P);
+            for (int j = 0; j <= p - i; j++) out[c++] = L[i] * P[j];
+        }
+    }
+    return c;
+}
+
+// Gauss-Legendre on [0,1] and the collapsed simplex rule with n points per direction.
+static void gauss01(int n, double* x, double* w) {
+    for (int i = 0; i < n; i++) {
+        double z = std::cos(M_PI * (i + 0.75) / (n + 0.5)), pp = 0;
+        for (int it = 0; it < 100; it++) {
+            double p0 = 1, p1 = 0;
+            for (int k = 1; k <= n; k++) {
+                double p2 = p1;
+                p1 = p0;
+                p0 = ((2.0 * k - 1) * z * p1 - (k - 1.0) * p2) / k;
+            }
+            pp = n * (z * p0 - p1) / (z * z - 1);
+            double dz = p0 / pp;
+            z -= dz;
+            if (std::fabs(dz) < 1e-16) break;
+        }
+        x[i] = 0.5 * (1 - z);
+        w[i] = 1.0 / ((1 - z * z) * pp * pp);
+    }
+}
+static int simplex_rule(int D, int n, std::vector<double>& pts, std::vector<double>& wts) {
+    double x[32], w[32];
+    gauss01(n, x, w);
+    pts.clear();
+    wts.clear();
+    if (D == 1) {
+        for (int i = 0; i < n; i++) { pts.push_back(x[i]); wts.push_back(w[i]); }
+    } else if (D == 2) {
+        for (int i = 0; i < n; i++)
+            for (int j = 0; j < n; j++) {
+                pts.push_back(x[i]);
+                pts.push_back(x[j] * (1 - x[i]));
+                wts.push_back(w[i] * w[j] * (1 - x[i]));
+            }
+    } else {
+        for (int i = 0; i < n; i++)
+            for (int j = 0; j < n; j++)
+                for (int k = 0; k < n; k++) {
+                    pts.push_back(x[i]);
+                    pts.push_back(x[j] * (1 - x[i]));
+                    pts.push_back(x[k] * (1 - x[i]) * (1 - x[j]));
+                    wts.push_back(w[i] * w[j] * w[k] * (1 - x[i]) * (1 - x[i]) * (1 - x[j]));
+                }
+    }
+    return (int)wts.size();
+}
+
+static void build_tables(int kind, int D, int p, ocmp_tables& T) {
+    int L = nloc_of(kind, D, p);
+    T.nloc = L;
+    std::vector<double> qp, qw;
+    T.nq = simplex_rule(D, p + 2, qp, qw);
+    T.qw = qw;
+    T.qxi = qp;
+    int S = D * (D + 1) / 2;
+    T.ng_const = 1 + S + D;
+    T.ng_vtx = 1 + S + D * (D + 1);
+    T.R_const.assign((size_t)T.ng_const * L * L, 0.0);
+    T.R_vtx.assign((size_t)T.ng_vtx * L * L, 0.0);
+    T.qphi.assign((size_t)T.nq * L, 0.0);
+    T.mvec.assign(L, 0.0);
+    Dn b[kMaxLoc];
+    for (int q = 0; q < T.nq; q++) {
+        const double* xi = &qp[q * D];
+        basis(kind, D, p, xi, b);
+        double lam[4];
+        lam[0] = 1;
+        for (int k = 0; k < D; k++) { lam[k + 1] = xi[k]; lam[0] -= xi[k]; }
+        double w = qw[q];
+        for (int i = 0; i < L; i++) {
+            T.qphi[q * L + i] = b[i].v;
+            T.mvec[i] += w * b[i].v;
+            for (int j = 0; j < L; j++) {
+                size_t ij = (size_t)i * L + j;
+                double m = w * b[i].v * b[j].v;
+                T.R_const[ij] += m;
+                T.R_vtx[ij] += m;
+                int g = 1;
+                for (int k = 0; k < D; k++)
+                    for (int l = k; l < D; l++, g++) {
+                        double s = w * b[i].d[k] * b[j].d[l];
+                        if (k != l) s += w * b[i].d[l] * b[j].d[k];
+                        T.R_const[(size_t)g * L * L + ij] += s;
+                        T.R_vtx[(size_t)g * L * L + ij] += s;
+                    }
+                for (int k = 0; k < D; k++) T.R_const[(size_t)(1 + S + k) * L * L + ij] += w * b[i].d[k] * b[j].v;
+                for (int k = 0; k < D; k++)
+                    for (int v = 0; v <= D; v++)
+                        T.R_vtx[(size_t)(1 + S + k * (D + 1) + v) * L * L + ij] += w * lam[v] * b[i].d[k] * b[j].v;
+            }
+        }
+    }
+    // facet tables: local facet f = the facet opposite local vertex f; its vertices in ascending
+    // local order a0 < a1 (< a2) with lam_{a0} = 1 - s (- t), lam_{a1} = s, lam_{a2} = t.
+    std::vector<double> fp, fw;
+    T.nfq = simplex_rule(D - 1, p + 2, fp, fw);
+    T.fw = fw;
+    int nf = D + 1;
+    T.fphi.assign((size_t)nf * T.nfq * L, 0.0);
+    T.fdphi.assign((size_t)nf * T.nfq * L * D, 0.0);
+    T.flam.assign((size_t)nf * T.nfq * (D + 1), 0.0);
+    for (int f = 0; f < nf; f++) {
+        int av[3], c = 0;
+        for (int v = 0; v <= D; v++)
+            if (v != f) av[c++] = v;
+        for (int q = 0; q < T.nfq; q++) {
+            double lam[4] = {0, 0, 0, 0};
+            if (D == 2) {
+                lam[av[0]] = 1 - fp[q];
+                lam[av[1]] = fp[q];
+            } else {
+                lam[av[0]] = 1 - fp[2 * q] - fp[2 * q + 1];
+                lam[av[1]] = fp[2 * q];
+                lam[av[2]] = fp[2 * q + 1];
+            }
+            double xi[3];
+            for (int k = 0; k < D; k++) xi[k] = lam[k + 1];
+            basis(kind, D, p, xi, b);
+            for (int v = 0; v <= D; v++) T.flam[((size_t)f * T.nfq + q) * (D + 1) + v] = lam[v];
+            for (int i = 0; i < L; i++) {
+                T.fphi[((size_t)f * T.nfq + q) * L + i] = b[i].v;
+                for (int k = 0; k < D; k++) T.fdphi[(((size_t)f * T.nfq + q) * L + i) * D + k] = b[i].d[k];
+            }
+        }
+    }
+}
+
+}  // namespace ocmp
+
+using namespace ocmp;
+
+extern "C" {
+
+int ocmp_abi_version(void) { return OCMP_ABI_VERSION; }
+
+int ocmp_last_error(char* buf, int len) {
+    if (!buf || len <= 0) return OCMP_ERR_ARG;
+    std::strncpy(buf, g_err.c_str(), (size_t)len - 1);
+    buf[len - 1] = 0;
+    return OCMP_OK;
+}
+
+int ocmp_device_sync(void* stream) {
+    OCMP_CUDA(cudaStreamSynchronize((cudaStream_t)stream));
+    return OCMP_OK;
+}
+
+int ocmp_mesh_create(const double* coords, int64_t nv, int32_t dim, const int32_t* elements, int64_t ne,
+                     const int32_t* bfacets, const int32_t* blabels, int64_t nbf, ocmp_mesh_t* out) {
+    if (!out || !coords || !elements || (dim != 2 && dim != 3) || nv <= 0 || ne <= 0 || nbf < 0 ||
+        (nbf > 0 && (!bfacets || !blabels)))
+        return fail(OCMP_ERR_ARG, "ocmp_mesh_create: bad arguments");
+    if (nv >= (int64_t)1 << 31 || ne * (dim + 1) >= (int64_t)1 << 31)
+        return fail(OCMP_ERR_ARG, "ocmp_mesh_create: mesh too large for 32-bit indices");
+    auto* m = new ocmp_mesh_s();
+    m->dim = dim;
+    m->nv = nv;
+    m->ne = ne;
+    m->nbf = nbf;
+    m->X.assign(coords, coords + nv * dim);
+    m->conn.assign(elements, elements + ne * (dim + 1));
+    for (int64_t i = 0; i < ne * (dim + 1); i++)
+        if (m->conn[i] < 0 || m->conn[i] >= nv) {
+            delete m;
+            return fail(OCMP_ERR_ARG, "ocmp_mesh_create: element vertex index out of range");
+        }
+    for (int64_t e = 0; e < ne; e++) std::sort(m->conn.begin() + e * (dim + 1), m->conn.begin() + (e + 1) * (dim + 1));
+    if (nbf) {
+        m->bfac.assign(bfacets, bfacets + nbf * dim);
+        m->blab.assign(blabels, blabels + nbf);
+    }
+    int st = upload(&m->dX, m->X.data(), m->X.size());
+    if (!st) st = upload(&m->dconn, m->conn.data(), m->conn.size());
+    if (st) {
+        dfree(m->dX);
+        dfree(m->dconn);
+        delete m;
+        return st;
+    }
+    *out = m;
+    return OCMP_OK;
+}
+
+int ocmp_mesh_destroy(ocmp_mesh_t m) {
+    if (!m) return OCMP_OK;
+    dfree(m->dX);
+    dfree(m->dconn);
+    delete m;
+    return OCMP_OK;
+}
+
+static void free_space_device(ocmp_space_s* s) {
+    void* ps[] = {s->d_dofs, s->d_rowptr, s->d_col,  s->d_free, s->d_diag, s->d_seg,  s->d_contrib, s->d_inc_ptr,
+                  s->d_inc,  s->d_ifac,   s->d_bfac, s->d_ebf_ptr, s->d_ebf, s->d_Rc, s->d_Rv,      s->d_qw,
+                  s->d_qphi, s->d_mvec,   s->d_fw,   s->d_fphi, s->d_fdphi, s->d_flam, s->d_F,      s->d_facetK,
+                  s->d_Fe};
+    for (void* p : ps) dfree(p);
+}
+
+int ocmp_space_create(ocmp_mesh_t mesh, int32_t kind, int32_t order, uint32_t dirichlet_mask, ocmp_space_t* out) {
+    if (!mesh || !out) return fail(OCMP_ERR_ARG, "ocmp_space_create: null argument");
+    const int D = mesh->dim, nvp = D + 1, p = order;
+    if (kind != OCMP_H1 && kind != OCMP_L2) return fail(OCMP_ERR_ARG, "ocmp_space_create: kind must be H1 or L2");
+    if (p < 1 || p > 3) return fail(OCMP_ERR_UNSUPPORTED, "ocmp_space_create: order must be 1..3");
+    if (kind == OCMP_L2 && D != 2) return fail(OCMP_ERR_UNSUPPORTED, "ocmp_space_create: L2 is built for triangles only");
+    auto* s = new ocmp_space_s();
+    s->mesh = mesh;
+    s->kind = kind;
+    s->order = p;
+    s->dim = D;
+    s->dirichlet_mask = dirichlet_mask;
+    const int L = s->nloc = nloc_of(kind, D, p);
+    const int64_t ne = mesh->ne, nv = mesh->nv;
+    const int32_t* conn = mesh->conn.data();
+    build_tables(kind, D, p, s->T);
+
+    // ---- dof map
+    s->dofs.resize((size_t)ne * L);
+    if (kind == OCMP_L2) {
+        s->ndof = ne * L;
+        for (int64_t i = 0; i < ne * L; i++) s->dofs[i] = (int32_t)i;
+    } else {
+        const int nel = D == 2 ? 3 : 6, nfl = D == 2 ? 1 : 4;
+        std::vector<int64_t> ek, fk;
+        if (p >= 2) {
+            ek.resize((size_t)ne * nel);
+            parallel_for(ne, [&](int64_t a, int64_t b) {
+                for (int64_t e = a; e < b; e++) {
+                    int c = 0;
+                    for (int x = 0; x < nvp; x++)
+                        for (int y = x + 1; y < nvp; y++) ek[e * nel + c++] = (int64_t)conn[e * nvp + x] * nv + conn[e * nvp + y];
+                }
+            });
+            std::sort(ek.begin(), ek.end());
+            ek.erase(std::unique(ek.begin(), ek.end()), ek.end());
+        }
+        if (p >= 3) {
+            fk.resize((size_t)ne * nfl);
+            for (int64_t e = 0; e < ne; e++) {
+                int c = 0;
+                for (int x = 0; x < nvp; x++)
+                    for (int y = x + 1; y < nvp; y++)
+                        for (int z = y + 1; z < nvp; z++)
+                            fk[e * nfl + c++] = ((int64_t)conn[e * nvp + x] * nv + conn[e * nvp + y]) * nv + conn[e * nvp + z];
+            }
+            std::sort(fk.begin(), fk.end());
+            fk.erase(std::unique(fk.begin(), fk.end()), fk.end());
+        }
+        const int64_t ned = (int64_t)ek.size(), nfc = (int64_t)fk.size();
+        const int epd = p - 1;
+        s->ndof = nv + ned * epd + nfc * (p >= 3 ? 1 : 0);
+        if (s->ndof >= (int64_t)1 << 31) {
+            delete s;
+            return fail(OCMP_ERR_ARG, "ocmp_space_create: too many dofs for 32-bit indices");
+        }
+        parallel_for(ne, [&](int64_t a, int64_t b) {
+            for (int64_t e = a; e < b; e++) {
+                const int32_t* v = conn + e * nvp;
+                int c = 0;
+                int32_t* d = &s->dofs[e * L];
+                for (int x = 0; x < nvp; x++) d[c++] = v[x];
+                if (p >= 2)
+                    for (int x = 0; x < nvp; x++)
+                        for (int y = x + 1; y < nvp; y++) {
+                            int64_t id = std::lower_bound(ek.begin(), ek.end(), (int64_t)v[x] * nv + v[y]) - ek.begin();
+                            for (int k = 0; k < epd; k++) d[c++] = (int32_t)(nv + id * epd + k);
+                        }
+                if (p >= 3)
+                    for (int x = 0; x < nvp; x++)
+                        for (int y = x + 1; y < nvp; y++)
+                            for (int z = y + 1; z < nvp; z++) {
+                                int64_t key = ((int64_t)v[x] * nv + v[y]) * nv + v[z];
+                                int64_t id = std::lower_bound(fk.begin(), fk.end(), key) - fk.begin();
+                                d[c++] = (int32_t)(nv + ned * epd + id);
+                            }
+            }
+        });
+    }
+    const int64_t nd = s->ndof;
+
+    // ---- facets
+    {
+        std::vector<std::pair<int64_t, int64_t>> fkeys((size_t)ne * nvp);
+        parallel_for(ne, [&](int64_t a, int64_t b) {
+            for (int64_t e = a; e < b; e++)
+                for (int f = 0; f < nvp; f++) {
+                    int64_t k = 0;
+                    for (int v = 0; v < nvp; v++)
+                        if (v != f) k = k * nv + conn[e * nvp + v];
+                    fkeys[e * nvp + f] = {k, e * nvp + f};
+                }
+        });
+        std::sort(fkeys.begin(), fkeys.end());
+        for (size_t i = 0; i + 1 < fkeys.size(); i++)
+            if (fkeys[i].first == fkeys[i + 1].first) {
+                int64_t a = fkeys[i].second, b = fkeys[i + 1].second;
+                s->ifac.push_back((int32_t)(a / nvp));
+                s->ifac.push_back((int32_t)(a % nvp));
+                s->ifac.push_back((int32_t)(b / nvp));
+                s->ifac.push_back((int32_t)(b % nvp));
+                i++;
+            }
+        s->nif = (int64_t)s->ifac.size() / 4;
+        for (int64_t b = 0; b < mesh->nbf; b++) {
+            int32_t vv[3];
+            for (int k = 0; k < D; k++) vv[k] = mesh->bfac[b * D + k];
+            std::sort(vv, vv + D);
+            int64_t key = 0;
+            for (int k = 0; k < D; k++) key = key * nv + vv[k];
+            auto it = std::lower_bound(fkeys.begin(), fkeys.end(), std::make_pair(key, (int64_t)-1));
+            if (it == fkeys.end() || it->first != key) continue;  // facet not on any element: ignored
+            s->bfac.push_back((int32_t)(it->second / nvp));
+            s->bfac.push_back((int32_t)(it->second % nvp));
+            s->bfac.push_back(mesh->blab[b]);
+        }
+        s->nbf = (int64_t)s->bfac.size() / 3;
+    }
+
+    // ---- free dofs (H1): every function living on a Dirichlet-labelled facet is constrained
+    s->freed.assign(nd, 1);
+    if (kind == OCMP_H1)
+        for (int64_t b = 0; b < s->nbf; b++) {
+            int lab = s->bfac[3 * b + 2];
+            if (lab < 0 || lab >= 32 || !((dirichlet_mask >> lab) & 1u)) continue;
+            int64_t e = s->bfac[3 * b];
+            int f = s->bfac[3 * b + 1];
+            int c = 0;
+            const int32_t* d = &s->dofs[e * L];
+            for (int a = 0; a < nvp; a++, c++)
+                if (a != f) s->freed[d[c]] = 0;
+            if (p >= 2)
+                for (int a = 0; a < nvp; a++)
+                    for (int bb = a + 1; bb < nvp; bb++)
+                        for (int k = 0; k < p - 1; k++, c++)
+                            if (a != f && bb != f) s->freed[d[c]] = 0;
+            if (p >= 3)
+                for (int a = 0; a < nvp; a++)
+                    for (int bb = a + 1; bb < nvp; bb++)
+                        for (int cc = bb + 1; cc < nvp; cc++, c++)
+                            if (a != f && bb != f && cc != f) s->freed[d[c]] = 0;
+        }
+
+    // ---- dof -> (element, local) incidence
+    std::vector<int32_t> inc_ptr(nd + 1, 0), inc((size_t)ne * L);
+    for (int64_t i = 0; i < ne * L; i++) inc_ptr[s->dofs[i] + 1]++;
+    for (int64_t i = 0; i < nd; i++) inc_ptr[i + 1] += inc_ptr[i];
+    {
+        std::vector<int32_t> fill(inc_ptr.begin(), inc_ptr.end() - 1);
+        for (int64_t i = 0; i < ne * L; i++) inc[fill[s->dofs[i]]++] = (int32_t)i;
+    }
+    // element -> interior facets (L2) and element -> boundary facets
+    std::vector<int32_t> enb((size_t)ne * nvp, -1);  // facet index of local facet f (interior), or -1
+    for (int64_t fi = 0; fi < s->nif; fi++) {
+        enb[(int64_t)s->ifac[4 * fi] * nvp + s->ifac[4 * fi + 1]] = (int32_t)fi;
+        enb[(int64_t)s->ifac[4 * fi + 2] * nvp + s->ifac[4 * fi + 3]] = (int32_t)fi;
+    }
+    std::vector<int32_t> ebf_ptr(ne + 1, 0), ebf((size_t)s->nbf);
+    for (int64_t b = 0; b < s->nbf; b++) ebf_ptr[s->bfac[3 * b] + 1]++;
+    for (int64_t e = 0; e < ne; e++) ebf_ptr[e + 1] += ebf_ptr[e];
+    {
+        std::vector<int32_t> fill(ebf_ptr.begin(), ebf_ptr.end() - 1);
+        for (int64_t b = 0; b < s->nbf; b++) ebf[fill[s->bfac[3 * b]]++] = (int32_t)b;
+    }
+    const bool dgj = kind == OCMP_L2;
+
+    // ---- CSR pattern (row-parallel sort/unique of the incident elements' dofs)
+    std::vector<std::vector<int32_t>> rows(nd);
+    std::vector<int64_t> rl(nd + 1, 0);
+    parallel_for(nd, [&](int64_t a, int64_t b) {
+        std::vector<int32_t> buf;
+        for (int64_t r = a; r < b; r++) {
+            buf.clear();
+            for (int32_t k = inc_ptr[r]; k < inc_ptr[r + 1]; k++) {
+                int64_t e = inc[k] / L;
+                buf.insert(buf.end(), &s->dofs[e * L], &s->dofs[e * L] + L);
+                if (dgj)
+                    for (int f = 0; f < nvp; f++) {
+                        int32_t fi = enb[e * nvp + f];
+                        if (fi < 0) continue;
+                        int64_t o = s->ifac[4 * fi] == e ? s->ifac[4 * fi + 2] : s->ifac[4 * fi];
+                        buf.insert(buf.end(), &s->dofs[o * L], &s->dofs[o * L] + L);
+                    }
+            }
+            std::sort(buf.begin(), buf.end());
+            buf.erase(std::unique(buf.begin(), buf.end()), buf.end());
+            rows[r] = buf;
+            rl[r + 1] = (int64_t)buf.size();
+        }
+    });
+    for (int64_t r = 0; r < nd; r++) rl[r + 1] += rl[r];
+    s->nnz = rl[nd];
+    if (s->nnz >= (int64_t)1 << 31) {
+        delete s;
+        return fail(OCMP_ERR_ARG, "ocmp_space_create: nnz too large for 32-bit row pointers");
+    }
+    s->rowptr = rl;
+    s->col.resize(s->nnz);
+    parallel_for(nd, [&](int64_t a, int64_t b) {
+        for (int64_t r = a; r < b; r++) {
+            std::copy(rows[r].begin(), rows[r].end(), s->col.begin() + rl[r]);
+            std::vector<int32_t>().swap(rows[r]);
+        }
+    });
+    std::vector<std::vector<int32_t>>().swap(rows);
+
+    // ---- sorted scatter plan: for each CSR entry, the local-matrix entries that sum into it.
+    // Contribution index space: [0, ne L^2) element entries e*L^2 + i*L + j; then interior facet
+    // entries (2L x 2L per facet); then boundary facet entries (L x L per facet).
+    const uint64_t E = (uint64_t)ne * L * L;
+    const uint64_t FI = E, FB = E + (uint64_t)s->nif * 4 * L * L;
+    const uint64_t total_space = FB + (uint64_t)s->nbf * L * L;
+    s->elem_entries = E;
+    if (total_space >= ((uint64_t)1 << 32)) {
+        delete s;
+        return fail(OCMP_ERR_ARG, "ocmp_space_create: local-matrix entries exceed 32-bit plan indices");
+    }
+    std::vector<int64_t> rc(nd + 1, 0);
+    auto row_contribs = [&](int64_t r, std::vector<std::pair<int32_t, uint32_t>>& out) {
+        out.clear();
+        const int32_t* c0 = s->col.data() + rl[r];
+        const int64_t rn = rl[r + 1] - rl[r];
+        auto pos_of = [&](int32_t dof) { return (int32_t)(std::lower_bound(c0, c0 + rn, dof) - c0); };
+        for (int32_t k = inc_ptr[r]; k < inc_ptr[r + 1]; k++) {
+            int64_t e = inc[k] / L;
+            int i = inc[k] % L;
+            for (int j = 0; j < L; j++)
+                out.push_back({pos_of(s->dofs[e * L + j]), (uint32_t)(e * L * L + i * L + j)});
+            if (dgj)
+                for (int f = 0; f < nvp; f++) {
+                    int32_t fi = enb[e * nvp + f];
+                    if (fi < 0) continue;
+                    bool left = s->ifac[4 * fi] == e;
+                    int ri = left ? i : L + i;
+                    int64_t eL = s->ifac[4 * fi], eR = s->ifac[4 * fi + 2];
+                    for (int j = 0; j < 2 * L; j++) {
+                        int32_t cd = j < L ? s->dofs[eL * L + j] : s->dofs[eR * L + j - L];
+                        out.push_back({pos_of(cd), (uint32_t)(FI + (uint64_t)fi * 4 * L * L + ri * 2 * L + j)});
+                    }
+                }
+            for (int32_t q = ebf_ptr[e]; q < ebf_ptr[e + 1]; q++) {
+                int32_t bf = ebf[q];
+                for (int j = 0; j < L; j++)
+                    out.push_back({pos_of(s->dofs[e * L + j]), (uint32_t)(FB + (uint64_t)bf * L * L + i * L + j)});
+            }
+        }
+        std::sort(out.begin(), out.end());
+    };
+    parallel_for(nd, [&](int64_t a, int64_t b) {
+        std::vector<std::pair<int32_t, uint32_t>> tmp;
+        for (int64_t r = a; r < b; r++) {
+            row_contribs(r, tmp);
+            rc[r + 1] = (int64_t)tmp.size();
+        }
+    });
+    for (int64_t r = 0; r < nd; r++) rc[r + 1] += rc[r];
+    s->ncontrib = rc[nd];
+    if (s->ncontrib >= ((int64_t)1 << 32)) {
+        delete s;
+        return fail(OCMP_ERR_ARG, "ocmp_space_create: scatter plan exceeds 32-bit offsets");
+    }
+    std::vector<uint32_t> seg(s->nnz + 1), contrib(s->ncontrib);
+    std::vector<int32_t> diag(nd);
+    parallel_for(nd, [&](int64_t a, int64_t b) {
+        std::vector<std::pair<int32_t, uint32_t>> tmp;
+        for (int64_t r = a; r < b; r++) {
+            row_contribs(r, tmp);
+            int64_t base = rc[r];
+            int64_t rn = rl[r + 1] - rl[r];
+            size_t t = 0;
+            for (int64_t k = 0; k < rn; k++) {
+                seg[rl[r] + k] = (uint32_t)(base + (int64_t)t);
+                while (t < tmp.size() && tmp[t].first == k) {
+                    contrib[base + t] = tmp[t].second;
+                    t++;
+                }
+            }
+            const int32_t* c0 = s->col.data() + rl[r];
+            diag[r] = (int32_t)(rl[r] + (std::lower_bound(c0, c0 + rn, (int32_t)r) - c0));
+        }
+    });
+    seg[s->nnz] = (uint32_t)s->ncontrib;
+
+    // ---- upload
+    std::vector<int32_t> rp32(nd + 1);
+    for (int64_t i = 0; i <= nd; i++) rp32[i] = (int32_t)rl[i];
+    int st = OCMP_OK;
+    auto U = [&](auto** dst, const auto& v) {
+        if (!st) st = upload(dst, v.data(), v.size());
+    };
+    U(&s->d_dofs, s->dofs);
+    U(&s->d_rowptr, rp32);
+    U(&s->d_col, s->col);
+    U(&s->d_free, s->freed);
+    U(&s->d_diag, diag);
+    U(&s->d_seg, seg);
+    U(&s->d_contrib, contrib);
+    U(&s->d_inc_ptr, inc_ptr);
+    U(&s->d_inc, inc);
+    U(&s->d_ifac, s->ifac);
+    U(&s->d_bfac, s->bfac);
+    U(&s->d_ebf_ptr, ebf_ptr);
+    U(&s->d_ebf, ebf);
+    U(&s->d_Rc, s->T.R_const);
+    U(&s->d_Rv, s->T.R_vtx);
+    U(&s->d_qw, s->T.qw);
+    U(&s->d_qphi, s->T.qphi);
+    U(&s->d_mvec, s->T.mvec);
+    U(&s->d_fw, s->T.fw);
+    U(&s->d_fphi, s->T.fphi);
+    U(&s->d_fdphi, s->T.fdphi);
+    U(&s->d_flam, s->T.flam);
+    if (!st) st = dalloc(&s->d_F, (size_t)kMaxNg * ne);
+    if (!st) st = dalloc(&s->d_facetK, (size_t)(total_space - E));
+    if (!st) st = dalloc(&s->d_Fe, (size_t)ne * L);
+    if (st) {
+        free_space_device(s);
+        delete s;
+        return st;
+    }
+    *out = s;
+    return OCMP_OK;
+}
+
+int ocmp_space_destroy(ocmp_space_t s) {
+    if (!s) return OCMP_OK;
+    free_space_device(s);
+    delete s;
+    return OCMP_OK;
+}
+
+int ocmp_space_info(ocmp_space_t s, ocmp_space_info_t* info) {
+    if (!s || !info) return fail(OCMP_ERR_ARG, "ocmp_space_info: null argument");
+    info->ndof = s->ndof;
+    info->nnz = s->nnz;
+    info->ne = s->mesh->ne;
+    info->nv = s->mesh->nv;
+    info->nloc = s->nloc;
+    info->nq = s->T.nq;
+    info->dim = s->dim;
+    info->order = s->order;
+    info->kind = s->kind;
+    info->n_interior_facets = s->nif;
+    info->n_boundary_facets = s->nbf;
+    info->n_contrib = s->ncontrib;
+    return OCMP_OK;
+}
+
+int ocmp_space_get_dofs(ocmp_space_t s, int32_t* d) {
+    if (!s || !d) return fail(OCMP_ERR_ARG, "ocmp_space_get_dofs: null argument");
+    std::memcpy(d, s->dofs.data(), s->dofs.size() * sizeof(int32_t));
+    return OCMP_OK;
+}
+
+int ocmp_space_get_pattern(ocmp_space_t s, int64_t* rp, int32_t* col) {
+    if (!s || !rp || !col) return fail(OCMP_ERR_ARG, "ocmp_space_get_pattern: null argument");
+    std::memcpy(rp, s->rowptr.data(), s->rowptr.size() * sizeof(int64_t));
+    std::memcpy(col, s->col.data(), s->col.size() * sizeof(int32_t));
+    return OCMP_OK;
+}
+
+int ocmp_space_get_free(ocmp_space_t s, uint8_t* f) {
+    if (!s || !f) return fail(OCMP_ERR_ARG, "ocmp_space_get_free: null argument");
+    std::memcpy(f, s->freed.data(), s->freed.size());
+    return OCMP_OK;
+}
+
+int ocmp_space_quad_points(ocmp_space_t s, double* xyz) {
+    if (!s || !xyz) return fail(OCMP_ERR_ARG, "ocmp_space_quad_points: null argument");
+    const int D = s->dim, nvp = D + 1, nq = s->T.nq;
+    const ocmp_mesh_s* m = s->mesh;
+    parallel_for(m->ne, [&](int64_t a, int64_t b) {
+        for (int64_t e = a; e < b; e++) {
+            const int32_t* v = &m->conn[e * nvp];
+            for (int q = 0; q < nq; q++)
+                for (int r = 0; r < D; r++) {
+                    double x0 = m->X[(int64_t)v[0] * D + r], acc = x0;
+                    for (int c = 0; c < D; c++) acc += (m->X[(int64_t)v[c + 1] * D + r] - x0) * s->T.qxi[q * D + c];
+                    xyz[(e * nq + q) * D + r] = acc;
+                }
+        }
+    });
+    return OCMP_OK;
+}
+
+int ocmp_set_boundary(ocmp_space_t s, uint32_t mask, const double* gval, double* u, void* stream) {
+    if (!s || !gval || !u) return fail(OCMP_ERR_ARG, "ocmp_set_boundary: null argument");
+    return launch_set_boundary(s, mask, gval, u, (cudaStream_t)stream);
+}
+
+int ocmp_matrix_create(ocmp_space_t s, int32_t want_fp32, ocmp_matrix_t* out) {
+    if (!s || !out) return fail(OCMP_ERR_ARG, "ocmp_matrix_create: null argument");
+    auto* m = new ocmp_matrix_s();
+    m->space = s;
+    int st = dalloc(&m->vals, (size_t)s->nnz);
+    if (!st && want_fp32) st = dalloc(&m->vals32, (size_t)s->nnz);
+    if (!st) st = cudaMemset(m->vals, 0, sizeof(double) * s->nnz) == cudaSuccess ? 0 : OCMP_ERR_CUDA;
+    if (st) {
+        dfree(m->vals);
+        dfree(m->vals32);
+        delete m;
+        return st;
+    }
+    *out = m;
+    return OCMP_OK;
+}
+
+int ocmp_matrix_destroy(ocmp_matrix_t m) {
+    if (!m) return OCMP_OK;
+    dfree(m->vals);
+    dfree(m->vals32);
+    delete m;
+    return OCMP_OK;
+}
+
+int ocmp_matrix_values(ocmp_matrix_t m, double** v64, float** v32) {
+    if (!m) return fail(OCMP_ERR_ARG, "ocmp_matrix_values: null argument");
+    if (v64) *v64 = m->vals;
+    if (v32) *v32 = m->vals32;
+    return OCMP_OK;
+}
+
+int ocmp_assemble_matrix(ocmp_matrix_t m, const ocmp_form_t* f, void* stream) {
+    if (!m || !f) return fail(OCMP_ERR_ARG, "ocmp_assemble_matrix: null argument");
+    if (f->wind_kind == OCMP_WIND_VERTEX && !f->wind_vtx)
+        return fail(OCMP_ERR_ARG, "ocmp_assemble_matrix: per-vertex wind needs wind_vtx");
+    return launch_assemble_matrix(m, f, (cudaStream_t)stream);
+}
+
+int ocmp_assemble_rhs(ocmp_space_t s, const ocmp_form_t* f, const ocmp_rhs_t* r, double* b, void* stream) {
+    if (!s || !f || !r || !b) return fail(OCMP_ERR_ARG, "ocmp_assemble_rhs: null argument");
+    if (r->src_kind == OCMP_SRC_QP && !r->src_qp) return fail(OCMP_ERR_ARG, "ocmp_assemble_rhs: src_qp is null");
+    return launch_assemble_rhs(s, f, r, b, (cudaStream_t)stream);
+}
+
+int ocmp_spmv(ocmp_matrix_t m, const double* x, double* y, void* stream) {
+    if (!m || !x || !y) return fail(OCMP_ERR_ARG, "ocmp_spmv: null argument");
+    return launch_spmv64(m->space, m->vals, x, y, (cudaStream_t)stream);
+}
+
+}  // extern "C"

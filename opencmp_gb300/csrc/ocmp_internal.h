@@ -1,0 +1,127 @@
+// Internal declarations shared by the host setup (ocmp_host.cpp) and the CUDA kernels (*.cu).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "../../include/opencmp_gpu.h"
+
+namespace ocmp {
+
+constexpr int kMaxLoc = 20;     // largest nloc built: H1 order 3 on tetrahedra
+constexpr int kMaxNg = 19;      // volume factors: 1 mass + 6 stiffness + 12 per-vertex wind (3D)
+constexpr int kMaxFq = 25;      // facet quadrature points
+
+void set_error(const std::string& msg);
+int fail(int code, const std::string& msg);
+int cuda_fail(cudaError_t e, const char* what);
+
+#define OCMP_CUDA(call)                                         \
+    do {                                                        \
+        cudaError_t _e = (call);                                \
+        if (_e != cudaSuccess) return ::ocmp::cuda_fail(_e, #call); \
+    } while (0)
+
+template <class T>
+int dalloc(T** p, size_t n) {
+    *p = nullptr;
+    if (n == 0) n = 1;
+    cudaError_t e = cudaMalloc((void**)p, n * sizeof(T));
+    if (e != cudaSuccess) return cuda_fail(e, "cudaMalloc");
+    return OCMP_OK;
+}
+template <class T>
+int upload(T** p, const T* h, size_t n) {
+    int st = dalloc(p, n);
+    if (st) return st;
+    if (n) OCMP_CUDA(cudaMemcpy(*p, h, n * sizeof(T), cudaMemcpyHostToDevice));
+    return OCMP_OK;
+}
+void dfree(void* p);
+
+}  // namespace ocmp
+
+struct ocmp_mesh_s {
+    int dim = 0;
+    int64_t nv = 0, ne = 0, nbf = 0;
+    std::vector<double> X;          // nv*dim
+    std::vector<int32_t> conn;      // ne*(dim+1), vertices ascending per element
+    std::vector<int32_t> bfac;      // nbf*dim
+    std::vector<int32_t> blab;      // nbf
+    double* dX = nullptr;
+    int32_t* dconn = nullptr;
+};
+
+// Reference-element tables of one space (host copies; device copies in ocmp_space_s).
+struct ocmp_tables {
+    int nloc = 0, nq = 0, nfq = 0, ng_const = 0, ng_vtx = 0;
+    std::vector<double> R_const;    // ng_const * nloc^2 : mass, stiffness (k<=l), wind (k)
+    std::vector<double> R_vtx;      // ng_vtx * nloc^2   : mass, stiffness, wind (k, vertex v)
+    std::vector<double> qw;         // nq
+    std::vector<double> qphi;       // nq * nloc  basis values at element quadrature points
+    std::vector<double> qxi;        // nq * dim   reference quadrature points
+    std::vector<double> mvec;       // nloc       integral of each basis function on the reference element
+    std::vector<double> fw;         // nfq        facet rule weights (sum 1 in 2D, 1/2 in 3D)
+    std::vector<double> fphi;       // (dim+1) * nfq * nloc       basis values on local facet f
+    std::vector<double> fdphi;      // (dim+1) * nfq * nloc * dim reference gradients on local facet f
+    std::vector<double> flam;       // (dim+1) * nfq * (dim+1)    barycentrics on local facet f
+};
+
+struct ocmp_space_s {
+    ocmp_mesh_s* mesh = nullptr;
+    int kind = 0, order = 0, nloc = 0, dim = 0;
+    uint32_t dirichlet_mask = 0;
+    int64_t ndof = 0, nnz = 0, nif = 0, nbf = 0, ncontrib = 0;
+    std::vector<int32_t> dofs;      // ne*nloc
+    std::vector<int64_t> rowptr;    // ndof+1
+    std::vector<int32_t> col;       // nnz
+    std::vector<uint8_t> freed;     // ndof
+    std::vector<int32_t> ifac;      // nif*4 : eL, fL, eR, fR
+    std::vector<int32_t> bfac;      // nbf*3 : e, f, label  (only facets matched to an element)
+    ocmp_tables T;
+    // device
+    int32_t* d_dofs = nullptr;
+    int32_t* d_rowptr = nullptr;
+    int32_t* d_col = nullptr;
+    uint8_t* d_free = nullptr;
+    int32_t* d_diag = nullptr;      // ndof: position of the diagonal entry in each row
+    uint32_t* d_seg = nullptr;      // nnz+1: segment start of each CSR entry in d_contrib
+    uint32_t* d_contrib = nullptr;  // ncontrib: local-matrix entry feeding that CSR entry
+    int32_t* d_inc_ptr = nullptr;   // ndof+1: dof -> (element, local) incidence
+    int32_t* d_inc = nullptr;       // ne*nloc: e*nloc + i
+    int32_t* d_ifac = nullptr;
+    int32_t* d_bfac = nullptr;
+    int32_t* d_ebf_ptr = nullptr;   // ne+1: element -> boundary facets
+    int32_t* d_ebf = nullptr;
+    double* d_Rc = nullptr;         // R_const
+    double* d_Rv = nullptr;         // R_vtx
+    double* d_qw = nullptr;
+    double* d_qphi = nullptr;
+    double* d_mvec = nullptr;
+    double* d_fw = nullptr;
+    double* d_fphi = nullptr;
+    double* d_fdphi = nullptr;
+    double* d_flam = nullptr;
+    // scratch owned by the space
+    double* d_F = nullptr;          // kMaxNg * ne element factors
+    double* d_facetK = nullptr;     // nif*(2 nloc)^2 + nbf*nloc^2 facet matrices
+    double* d_Fe = nullptr;         // ne*nloc element right-hand sides
+    uint64_t elem_entries = 0;      // ne * nloc^2: contributions below this index are volume entries
+};
+
+struct ocmp_matrix_s {
+    ocmp_space_s* space = nullptr;
+    double* vals = nullptr;
+    float* vals32 = nullptr;
+};
+
+namespace ocmp {
+// kernels (ocmp_assemble.cu)
+int launch_assemble_matrix(ocmp_matrix_s* m, const ocmp_form_t* f, cudaStream_t st);
+int launch_assemble_rhs(ocmp_space_s* s, const ocmp_form_t* f, const ocmp_rhs_t* r, double* b, cudaStream_t st);
+int launch_set_boundary(ocmp_space_s* s, uint32_t mask, const double* gval, double* u, cudaStream_t st);
+int launch_spmv64(const ocmp_space_s* s, const double* vals, const double* x, double* y, cudaStream_t st);
+}  // namespace ocmp

@@ -1,0 +1,914 @@
+// Krylov solvers of libopencmp_gpu.so (sm_103a): the GPU counterpart of the linear solve in
+// opencmp/models/base_model.py:886-947 (solvers.CG with the 'local' = point-Jacobi preconditioner
+// restricted to free dofs, solvers.GMRes with freedofs).
+//
+// The whole iteration stays on the device: Hessenberg matrix, Givens rotations, residual
+// estimate and convergence/breakdown flags live in device memory and are updated by one-thread
+// kernels; the host only reads the flags every `check_every` iterations. Every reduction is a
+// fixed two-stage tree (per-block partials, then one block per value), so results are
+// bit-reproducible run to run.
+//
+// Precision: OCMP_FP64 runs everything in FP64. OCMP_MIXED runs an outer FP64 iterative
+// refinement (r = b - A x with the FP64 matrix, x += correction) around an inner GMRES/CG whose
+// matrix values, vectors and preconditioner are FP32 and whose dot products are accumulated per
+// thread in FP32 and across threads in FP64; the Hessenberg matrix and rotations stay FP64.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+
+#include "ocmp_internal.h"
+
+struct ocmp_solver_s {
+    ocmp_matrix_s* mat = nullptr;
+    ocmp_space_s* s = nullptr;
+    ocmp_solve_params_t prm{};
+    int64_t n = 0;
+    int nb = 0;                 // reduction blocks
+    int m = 0;                  // GMRES restart
+    // FP64 path
+    double* dinv = nullptr;     // Jacobi (0 on constrained rows)
+    double* Binv = nullptr;     // block Jacobi (L2 element blocks)
+    double* V = nullptr;        // (m+1) x n
+    double* w = nullptr;
+    double* z = nullptr;
+    double* r = nullptr;
+    double* p = nullptr;
+    // FP32 inner path (OCMP_MIXED)
+    float* dinv32 = nullptr;
+    float* Binv32 = nullptr;
+    float* V32 = nullptr;
+    float* w32 = nullptr;
+    float* z32 = nullptr;
+    float* r32 = nullptr;
+    float* p32 = nullptr;
+    float* d32 = nullptr;       // inner correction
+    // reductions and small state
+    double* part = nullptr;     // (m+4) x nb
+    double* pspmv = nullptr;    // one partial per SpMV block (CG p . Ap)
+    double* red = nullptr;      // m+2 reduced values
+    double* st = nullptr;       // small state, see enum below
+    double* H = nullptr;        // (m+1) x m
+    int* flags = nullptr;       // device flags
+    int* hflags = nullptr;      // pinned host mirror
+};
+
+namespace ocmp {
+namespace {
+
+// small-state slots (doubles)
+enum { S_BETA = 0, S_NB, S_INV, S_RES, S_HN2, S_NW2, S_ALPHA, S_RZ, S_TOL, S_SCALE, S_G0, S_NSLOT = 16 };
+// flags
+enum { F_CONV = 0, F_REORTH, F_BREAK, F_NONFIN, F_JDONE, F_ITERS, F_NFLAG = 8 };
+
+constexpr int kThreads = 256;
+inline unsigned nblk(int64_t n, int t) { return (unsigned)((n + t - 1) / t); }
+
+template <class T>
+__device__ __forceinline__ double block_sum(T v) {
+    __shared__ double sh[kThreads / 32];
+    double d = (double)v;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) d += __shfl_down_sync(0xffffffffu, d, o);
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    __syncthreads();
+    if (lane == 0) sh[wid] = d;
+    __syncthreads();
+    double t = 0;
+    if (wid == 0) {
+        t = lane < (int)(blockDim.x >> 5) ? sh[lane] : 0.0;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) t += __shfl_down_sync(0xffffffffu, t, o);
+    }
+    return t;  // valid in thread 0
+}
+
+// out[k] = sum_b part[k * nb + b]; one block per k
+__global__ void reduce_kernel(int nb, int nk, const double* __restrict__ part, double* __restrict__ out,
+                              const int* __restrict__ flags, int gate) {
+    if (gate >= 0 && flags[gate] == 0) return;
+    const int k = blockIdx.x;
+    if (k >= nk) return;
+    double acc = 0;
+    for (int b = threadIdx.x; b < nb; b += blockDim.x) acc += part[(int64_t)k * nb + b];
+    double t = block_sum(acc);
+    if (threadIdx.x == 0) out[k] = t;
+}
+
+// y = free ? A x : 0, optional partial of dot(x, y) (CG: p . A p).
+template <class TM, class TV, int TPR>
+__global__ void __launch_bounds__(kThreads) spmv_masked(int64_t n, const int32_t* __restrict__ rp,
+                                                        const int32_t* __restrict__ col, const TM* __restrict__ val,
+                                                        const uint8_t* __restrict__ freed, const TV* __restrict__ x,
+                                                        TV* __restrict__ y, double* __restrict__ part,
+                                                        const int* __restrict__ flags) {
+    if (flags && flags[F_CONV]) return;
+    const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    const int64_t r = t / TPR;
+    const int lane = threadIdx.x % TPR;
+    TV acc = 0;
+    if (r < n) {
+        const int32_t a = rp[r], b = rp[r + 1];
+        for (int32_t k = a + lane; k < b; k += TPR) acc += (TV)__ldg(val + k) * __ldg(x + __ldg(col + k));
+    }
+#pragma unroll
+    for (int o = TPR / 2; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o, TPR);
+    TV dv = 0;
+    if (r < n && lane == 0) {
+        const TV yv = freed[r] ? acc : (TV)0;
+        y[r] = yv;
+        dv = yv * x[r];
+    }
+    if (part) {
+        double s = block_sum(dv);
+        if (threadIdx.x == 0) part[blockIdx.x] = s;
+    }
+}
+
+// r = free ? b - Ax : 0 ; partial of |r|^2.  Also used with Ax = A x_D to get the rhs norm.
+template <class T>
+__global__ void resid_kernel(int64_t n, const double* __restrict__ b, const double* __restrict__ Ax,
+                             const uint8_t* __restrict__ freed, T* __restrict__ r, double* __restrict__ part,
+                             int nparts) {
+    double acc = 0;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        double v = freed[i] ? b[i] - Ax[i] : 0.0;
+        if (r) r[i] = (T)v;
+        acc += v * v;
+    }
+    double s = block_sum(acc);
+    if (threadIdx.x == 0) part[blockIdx.x] = s;
+    (void)nparts;
+}
+
+__global__ void zero_free(int64_t n, const uint8_t* __restrict__ freed, const double* __restrict__ x,
+                          double* __restrict__ xd) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        xd[i] = freed[i] ? 0.0 : x[i];
+}
+
+template <class T>
+__global__ void jacobi_setup(int64_t n, const int32_t* __restrict__ diag, const double* __restrict__ vals,
+                             const uint8_t* __restrict__ freed, T* __restrict__ dinv) {
+    int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    double d = vals[diag[i]];
+    dinv[i] = (T)((freed[i] && d != 0.0) ? 1.0 / d : 0.0);
+}
+
+// block-Jacobi inverse of each element block (L2 spaces), Gauss-Jordan with partial pivoting, FP64
+template <int L>
+__global__ void block_jacobi_setup(int64_t ne, const int32_t* __restrict__ rp, const int32_t* __restrict__ col,
+                                   const double* __restrict__ vals, double* __restrict__ Binv,
+                                   float* __restrict__ Binv32) {
+    int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (e >= ne) return;
+    double A[L][2 * L];
+    for (int i = 0; i < L; i++) {
+        const int64_t r = e * L + i;
+        const int32_t a = rp[r], b = rp[r + 1];
+        for (int j = 0; j < L; j++) {
+            A[i][j] = 0;
+            A[i][L + j] = (i == j) ? 1.0 : 0.0;
+        }
+        for (int32_t k = a; k < b; k++) {
+            const int32_t c = col[k];
+            if (c >= e * L && c < (e + 1) * L) A[i][c - e * L] = vals[k];
+        }
+    }
+    for (int c = 0; c < L; c++) {
+        int pr = c;
+        for (int i = c + 1; i < L; i++)
+            if (fabs(A[i][c]) > fabs(A[pr][c])) pr = i;
+        if (pr != c)
+            for (int j = 0; j < 2 * L; j++) {
+                double t = A[c][j];
+                A[c][j] = A[pr][j];
+                A[pr][j] = t;
+            }
+        const double d = A[c][c];
+        const double id = d != 0.0 ? 1.0 / d : 0.0;
+        for (int j = 0; j < 2 * L; j++) A[c][j] *= id;
+        for (int i = 0; i < L; i++)
+            if (i != c) {
+                const double mm = A[i][c];
+                for (int j = 0; j < 2 * L; j++) A[i][j] -= mm * A[c][j];
+            }
+    }
+    for (int i = 0; i < L; i++)
+        for (int j = 0; j < L; j++) {
+            Binv[(e * L + i) * L + j] = A[i][L + j];
+            if (Binv32) Binv32[(e * L + i) * L + j] = (float)A[i][L + j];
+        }
+}
+
+// v_j = w * inv ; z = P v_j (Jacobi fused; block-Jacobi done by block_prec afterwards)
+template <class T>
+__global__ void scale_prec(int64_t n, const T* __restrict__ w, const double* __restrict__ st, T* __restrict__ v,
+                           const T* __restrict__ dinv, T* __restrict__ z, const int* __restrict__ flags) {
+    if (flags[F_CONV]) return;
+    const T inv = (T)st[S_INV];
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const T vi = w[i] * inv;
+        v[i] = vi;
+        if (dinv) z[i] = dinv[i] * vi;
+        else if (z != v) z[i] = vi;
+    }
+}
+
+template <class T, int L>
+__global__ void block_prec(int64_t ne, const T* __restrict__ Binv, const T* __restrict__ v, T* __restrict__ z,
+                           const int* __restrict__ flags) {
+    if (flags && flags[F_CONV]) return;
+    const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (t >= ne * L) return;
+    const int64_t e = t / L;
+    const int i = (int)(t % L);
+    T acc = 0;
+#pragma unroll
+    for (int j = 0; j < L; j++) acc += Binv[(e * L + i) * L + j] * v[e * L + j];
+    z[t] = acc;
+}
+
+// partials of  V_k . w  for k in [k0, k0 + 8) (k <= j) and, in chunk 0, w . w
+template <class T>
+__global__ void mdot_kernel(int64_t n, int j, const T* __restrict__ V, const T* __restrict__ w,
+                            double* __restrict__ part, int nb, const int* __restrict__ flags, int gate) {
+    if (flags[F_CONV] || (gate >= 0 && flags[gate] == 0)) return;
+    const int k0 = blockIdx.y * 8;
+    T acc[9];
+#pragma unroll
+    for (int k = 0; k < 9; k++) acc[k] = 0;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const T wi = w[i];
+#pragma unroll
+        for (int k = 0; k < 8; k++)
+            if (k0 + k <= j) acc[k] += V[(int64_t)(k0 + k) * n + i] * wi;
+        if (k0 == 0) acc[8] += wi * wi;
+    }
+#pragma unroll
+    for (int k = 0; k < 8; k++)
+        if (k0 + k <= j) {
+            double s = block_sum(acc[k]);
+            if (threadIdx.x == 0) part[(int64_t)(k0 + k) * nb + blockIdx.x] = s;
+        }
+    if (k0 == 0) {
+        double s = block_sum(acc[8]);
+        if (threadIdx.x == 0) part[(int64_t)(j + 1) * nb + blockIdx.x] = s;
+    }
+}
+
+// w -= sum_k h[k] V_k (k <= j); partial of |w|^2 into slot 0
+template <class T>
+__global__ void axpy_norm_kernel(int64_t n, int j, const T* __restrict__ V, const double* __restrict__ h,
+                                 T* __restrict__ w, double* __restrict__ part, const int* __restrict__ flags,
+                                 int gate) {
+    if (flags[F_CONV] || (gate >= 0 && flags[gate] == 0)) return;
+    __shared__ T hs[130];
+    for (int k = threadIdx.x; k <= j; k += blockDim.x) hs[k] = (T)h[k];
+    __syncthreads();
+    T acc = 0;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        T wi = w[i];
+        for (int k = 0; k <= j; k++) wi -= hs[k] * V[(int64_t)k * n + i];
+        w[i] = wi;
+        acc += wi * wi;
+    }
+    double s = block_sum(acc);
+    if (threadIdx.x == 0) part[blockIdx.x] = s;
+}
+
+// after the first orthogonalisation: decide on a second pass ("twice is enough" test)
+__global__ void reorth_check(const double* __restrict__ red, int j, double* st, int* flags) {
+    if (flags[F_CONV]) return;
+    const double nw2 = red[j + 1];  // |w|^2 before orthogonalisation
+    st[S_NW2] = nw2;
+    flags[F_REORTH] = 0;
+}
+__global__ void reorth_decide(const double* __restrict__ hn2, double* st, int* flags) {
+    if (flags[F_CONV]) return;
+    st[S_HN2] = hn2[0];
+    flags[F_REORTH] = (hn2[0] < 0.49 * st[S_NW2]) ? 1 : 0;
+}
+
+// Hessenberg column j from h (first pass) and h2 (second pass, gated), Givens rotations,
+// residual estimate, flags.
+__global__ void givens_kernel(int m, int j, double* __restrict__ H, const double* __restrict__ h,
+                              const double* __restrict__ h2, const double* __restrict__ hn2b, double* st, int* flags,
+                              double* __restrict__ cs_sn_g) {
+    if (flags[F_CONV]) return;
+    double* cs = cs_sn_g;
+    double* sn = cs_sn_g + m;
+    double* g = cs_sn_g + 2 * m;
+    const bool re = flags[F_REORTH] != 0;
+    double hn2 = re ? hn2b[0] : st[S_HN2];
+    for (int k = 0; k <= j; k++) H[k * m + j] = h[k] + (re ? h2[k] : 0.0);
+    double hn = sqrt(fmax(hn2, 0.0));
+    H[(j + 1) * m + j] = hn;
+    for (int k = 0; k < j; k++) {
+        const double a = H[k * m + j], b = H[(k + 1) * m + j];
+        H[k * m + j] = cs[k] * a + sn[k] * b;
+        H[(k + 1) * m + j] = -sn[k] * a + cs[k] * b;
+    }
+    const double a = H[j * m + j], b = H[(j + 1) * m + j];
+    const double d = sqrt(a * a + b * b);
+    flags[F_ITERS] += 1;
+    flags[F_JDONE] = j + 1;
+    if (!isfinite(d) || !isfinite(hn)) {
+        flags[F_NONFIN] = 1;
+        flags[F_CONV] = 1;
+        flags[F_JDONE] = j;  // drop the bad column
+        return;
+    }
+    if (d == 0.0) {
+        flags[F_BREAK] = 1;
+        flags[F_CONV] = 1;
+        flags[F_JDONE] = j;
+        return;
+    }
+    cs[j] = a / d;
+    sn[j] = b / d;
+    H[j * m + j] = d;
+    H[(j + 1) * m + j] = 0;
+    g[j + 1] = -sn[j] * g[j];
+    g[j] = cs[j] * g[j];
+    const double res = fabs(g[j + 1]) / st[S_NB];
+    st[S_RES] = res;
+    st[S_INV] = hn > 0 ? 1.0 / hn : 0.0;
+    if (res <= st[S_TOL] || hn == 0.0) flags[F_CONV] = 1;
+}
+
+// start of a cycle: beta = |r|, g = beta e1, inv = 1/beta; converged if beta/nb <= tol
+__global__ void cycle_start(const double* __restrict__ red, double* st, int* flags, double* __restrict__ cs_sn_g,
+                            int m) {
+    const double beta = sqrt(fmax(red[0], 0.0));
+    st[S_BETA] = beta;
+    double* g = cs_sn_g + 2 * m;
+    for (int k = 0; k <= m; k++) g[k] = 0;
+    g[0] = beta;
+    st[S_INV] = beta > 0 ? 1.0 / beta : 0.0;
+    st[S_RES] = beta / st[S_NB];
+    flags[F_JDONE] = 0;
+    flags[F_REORTH] = 0;
+    if (!isfinite(beta)) {
+        flags[F_NONFIN] = 1;
+        flags[F_CONV] = 1;
+    } else
+        flags[F_CONV] = (beta / st[S_NB] <= st[S_TOL]) ? 1 : 0;
+}
+
+// y = H^-1 g over the completed columns, then coefficients stored in y
+__global__ void trisolve_kernel(int m, const double* __restrict__ H, const double* __restrict__ cs_sn_g,
+                                double* __restrict__ y, const int* flags) {
+    const int jd = flags[F_JDONE];
+    const double* g = cs_sn_g + 2 * m;
+    for (int k = jd - 1; k >= 0; k--) {
+        double acc = g[k];
+        for (int l = k + 1; l < jd; l++) acc -= H[k * m + l] * y[l];
+        y[k] = acc / H[k * m + k];
+    }
+}
+
+// u = sum_k y_k V_k  (k < jdone)
+template <class T>
+__global__ void combine_kernel(int64_t n, const T* __restrict__ V, const double* __restrict__ y,
+                               const int* __restrict__ flags, T* __restrict__ u) {
+    __shared__ T ys[130];
+    const int jd = flags[F_JDONE];
+    for (int k = threadIdx.x; k < jd; k += blockDim.x) ys[k] = (T)y[k];
+    __syncthreads();
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        T acc = 0;
+        for (int k = 0; k < jd; k++) acc += ys[k] * V[(int64_t)k * n + i];
+        u[i] = acc;
+    }
+}
+
+// x += P u  (Jacobi fused; for block-Jacobi the caller applied the blocks into z already)
+template <class TX, class T>
+__global__ void xupdate_kernel(int64_t n, const T* __restrict__ u, const T* __restrict__ dinv, TX* __restrict__ x) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const T z = dinv ? dinv[i] * u[i] : u[i];
+        x[i] += (TX)z;
+    }
+}
+
+// ---- CG pieces
+template <class T>
+__global__ void cg_update(int64_t n, const double* __restrict__ st, T* __restrict__ x, T* __restrict__ r,
+                          const T* __restrict__ p, const T* __restrict__ q, const T* __restrict__ dinv,
+                          T* __restrict__ z, double* __restrict__ part, int nb, const int* __restrict__ flags) {
+    if (flags[F_CONV]) return;
+    const T alpha = (T)st[S_ALPHA];
+    T rz = 0, rr = 0;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        x[i] += alpha * p[i];
+        const T ri = r[i] - alpha * q[i];
+        r[i] = ri;
+        const T zi = dinv[i] * ri;
+        z[i] = zi;
+        rz += ri * zi;
+        rr += ri * ri;
+    }
+    double s1 = block_sum(rz);
+    if (threadIdx.x == 0) part[blockIdx.x] = s1;
+    double s2 = block_sum(rr);
+    if (threadIdx.x == 0) part[nb + blockIdx.x] = s2;
+}
+
+template <class T>
+__global__ void cg_pupdate(int64_t n, const double* __restrict__ st, const T* __restrict__ z, T* __restrict__ p,
+                           const int* __restrict__ flags) {
+    if (flags[F_CONV]) return;
+    const T beta = (T)st[S_SCALE];
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        p[i] = z[i] + beta * p[i];
+}
+
+template <class T>
+__global__ void cg_init(int64_t n, const T* __restrict__ r, const T* __restrict__ dinv, T* __restrict__ z,
+                        T* __restrict__ p, double* __restrict__ part, int nb) {
+    T rz = 0, rr = 0;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const T zi = dinv[i] * r[i];
+        z[i] = zi;
+        p[i] = zi;
+        rz += r[i] * zi;
+        rr += r[i] * r[i];
+    }
+    double s1 = block_sum(rz);
+    if (threadIdx.x == 0) part[blockIdx.x] = s1;
+    double s2 = block_sum(rr);
+    if (threadIdx.x == 0) part[nb + blockIdx.x] = s2;
+}
+
+__global__ void cg_scalars_init(const double* __restrict__ red, double* st, int* flags) {
+    st[S_RZ] = red[0];
+    const double res = sqrt(fmax(red[1], 0.0)) / st[S_NB];
+    st[S_RES] = res;
+    flags[F_CONV] = res <= st[S_TOL] ? 1 : 0;
+    if (!isfinite(res)) {
+        flags[F_NONFIN] = 1;
+        flags[F_CONV] = 1;
+    }
+}
+__global__ void cg_alpha(const double* __restrict__ red, double* st, int* flags) {
+    if (flags[F_CONV]) return;
+    const double pq = red[0];
+    if (pq == 0.0 || !isfinite(pq)) {
+        flags[pq == 0.0 ? F_BREAK : F_NONFIN] = 1;
+        flags[F_CONV] = 1;
+        st[S_ALPHA] = 0;
+        return;
+    }
+    st[S_ALPHA] = st[S_RZ] / pq;
+}
+__global__ void cg_beta(const double* __restrict__ red, double* st, int* flags) {
+    if (flags[F_CONV]) return;
+    const double rz1 = red[0];
+    st[S_SCALE] = st[S_RZ] != 0.0 ? rz1 / st[S_RZ] : 0.0;
+    st[S_RZ] = rz1;
+    const double res = sqrt(fmax(red[1], 0.0)) / st[S_NB];
+    st[S_RES] = res;
+    flags[F_ITERS] += 1;
+    if (!isfinite(res)) {
+        flags[F_NONFIN] = 1;
+        flags[F_CONV] = 1;
+    } else if (res <= st[S_TOL])
+        flags[F_CONV] = 1;
+}
+
+__global__ void set_state(double* st, int slot, double v) { st[slot] = v; }
+__global__ void set_nb_from(const double* __restrict__ red, double* st) {
+    const double nb = sqrt(fmax(red[0], 0.0));
+    st[S_NB] = nb > 0 ? nb : 1.0;
+}
+__global__ void scale_to_float(int64_t n, const double* __restrict__ r, const double* __restrict__ st,
+                               float* __restrict__ r32) {
+    const double inv = st[S_BETA] > 0 ? 1.0 / st[S_BETA] : 0.0;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        r32[i] = (float)(r[i] * inv);
+}
+__global__ void add_scaled_float(int64_t n, const float* __restrict__ d, const double* __restrict__ st,
+                                 double* __restrict__ x) {
+    const double s = st[S_BETA];
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        x[i] += s * (double)d[i];
+}
+
+// ------------------------------------------------------------------ host-side drivers
+struct Ctx {
+    ocmp_solver_s* sv;
+    cudaStream_t st;
+    int tpr;
+    int grid;  // grid-stride vector kernels
+};
+
+int pick_tpr(const ocmp_space_s* s) {
+    const double avg = (double)s->nnz / (double)s->ndof;
+    if (avg <= 6) return 2;
+    if (avg <= 14) return 4;
+    if (avg <= 40) return 8;
+    return 16;
+}
+
+template <class TM, class TV>
+void launch_spmv_masked(const Ctx& c, const TM* vals, const TV* x, TV* y, double* part, const int* flags) {
+    const ocmp_space_s* s = c.sv->s;
+    const int64_t n = s->ndof;
+    switch (c.tpr) {
+    case 2: spmv_masked<TM, TV, 2><<<nblk(n * 2, kThreads), kThreads, 0, c.st>>>(n, s->d_rowptr, s->d_col, vals, s->d_free, x, y, part, flags); break;
+    case 4: spmv_masked<TM, TV, 4><<<nblk(n * 4, kThreads), kThreads, 0, c.st>>>(n, s->d_rowptr, s->d_col, vals, s->d_free, x, y, part, flags); break;
+    case 8: spmv_masked<TM, TV, 8><<<nblk(n * 8, kThreads), kThreads, 0, c.st>>>(n, s->d_rowptr, s->d_col, vals, s->d_free, x, y, part, flags); break;
+    default: spmv_masked<TM, TV, 16><<<nblk(n * 16, kThreads), kThreads, 0, c.st>>>(n, s->d_rowptr, s->d_col, vals, s->d_free, x, y, part, flags); break;
+    }
+}
+inline int spmv_blocks(const Ctx& c) { return (int)nblk(c.sv->s->ndof * c.tpr, kThreads); }
+
+template <class T>
+void launch_block_prec(const Ctx& c, const T* Binv, const T* v, T* z, const int* flags) {
+    const ocmp_space_s* s = c.sv->s;
+    const int64_t ne = s->mesh->ne;
+    switch (s->nloc) {
+    case 3: block_prec<T, 3><<<nblk(ne * 3, kThreads), kThreads, 0, c.st>>>(ne, Binv, v, z, flags); break;
+    case 6: block_prec<T, 6><<<nblk(ne * 6, kThreads), kThreads, 0, c.st>>>(ne, Binv, v, z, flags); break;
+    case 10: block_prec<T, 10><<<nblk(ne * 10, kThreads), kThreads, 0, c.st>>>(ne, Binv, v, z, flags); break;
+    default: break;
+    }
+}
+
+// ||(b - A x_D)_free||: the norm the relative residual is measured against
+int rhs_norm(const Ctx& c, const double* b, const double* x) {
+    ocmp_solver_s* sv = c.sv;
+    const int64_t n = sv->n;
+    zero_free<<<c.grid, kThreads, 0, c.st>>>(n, sv->s->d_free, x, sv->z);
+    launch_spmv64(sv->s, sv->mat->vals, sv->z, sv->w, c.st);
+    resid_kernel<double><<<sv->nb, kThreads, 0, c.st>>>(n, b, sv->w, sv->s->d_free, (double*)nullptr, sv->part, sv->nb);
+    reduce_kernel<<<1, kThreads, 0, c.st>>>(sv->nb, 1, sv->part, sv->red, nullptr, -1);
+    set_nb_from<<<1, 1, 0, c.st>>>(sv->red, sv->st);
+    OCMP_CUDA(cudaGetLastError());
+    return OCMP_OK;
+}
+
+// FP64 residual r = (b - A x)_free into dst (double or float-scaled), |r|^2 into red[0]
+int residual64(const Ctx& c, const double* b, const double* x, double* dst) {
+    ocmp_solver_s* sv = c.sv;
+    launch_spmv64(sv->s, sv->mat->vals, x, sv->w, c.st);
+    resid_kernel<double><<<sv->nb, kThreads, 0, c.st>>>(sv->n, b, sv->w, sv->s->d_free, dst, sv->part, sv->nb);
+    reduce_kernel<<<1, kThreads, 0, c.st>>>(sv->nb, 1, sv->part, sv->red, nullptr, -1);
+    OCMP_CUDA(cudaGetLastError());
+    return OCMP_OK;
+}
+
+int read_flags(const Ctx& c) {
+    OCMP_CUDA(cudaMemcpyAsync(c.sv->hflags, c.sv->flags, sizeof(int) * F_NFLAG, cudaMemcpyDeviceToHost, c.st));
+    OCMP_CUDA(cudaStreamSynchronize(c.st));
+    return OCMP_OK;
+}
+
+// One GMRES(m) solve on vectors of type T (double: the FP64 solve; float: the inner solve of
+// OCMP_MIXED). Solves A z = r0 where r0 is the (free-masked) residual already stored in V[0..n)
+// unnormalised with |r0|^2 in red[0]; accumulates the correction into xacc.
+template <class T, class TM, class TX>
+int gmres_core(const Ctx& c, const TM* vals, const T* dinv, const T* Binv, T* V, T* w, T* z, TX* xacc,
+               const double* b64, const double* x64, int maxit, double tol, int* iters_out, bool outer64) {
+    ocmp_solver_s* sv = c.sv;
+    const int64_t n = sv->n;
+    const int m = sv->m;
+    double* H = sv->H;
+    double* csg = sv->H + (size_t)(m + 1) * m;  // cs, sn, g
+    double* y = csg + 3 * m + 1;
+    const bool block = sv->prm.precond == OCMP_PRE_BLOCK_JACOBI && Binv;
+    const T* djac = (sv->prm.precond == OCMP_PRE_JACOBI) ? dinv : nullptr;
+    int iters = 0;
+    set_state<<<1, 1, 0, c.st>>>(sv->st, S_TOL, tol);
+    OCMP_CUDA(cudaMemsetAsync(sv->flags, 0, sizeof(int) * F_NFLAG, c.st));
+    bool first = true;
+    while (true) {
+        if (!first) {
+            // recompute the residual of the current iterate for the restart
+            if (outer64) {
+                residual64(c, b64, x64, (double*)V);
+            } else {
+                // inner: residual of the correction system A d = r0 is not needed for restarts of
+                // the FP32 solve; it is rebuilt by the outer refinement instead
+                break;
+            }
+        }
+        first = false;
+        cycle_start<<<1, 1, 0, c.st>>>(sv->red, sv->st, sv->flags, csg, m);
+        if (read_flags(c)) return OCMP_ERR_CUDA;
+        if (sv->hflags[F_CONV] || iters >= maxit) break;
+        // w := r0 for the j = 0 scaling
+        OCMP_CUDA(cudaMemcpyAsync(w, V, sizeof(T) * n, cudaMemcpyDeviceToDevice, c.st));
+        int j = 0;
+        for (; j < m && iters < maxit; j++) {
+            T* vj = V + (int64_t)j * n;
+            scale_prec<T><<<c.grid, kThreads, 0, c.st>>>(n, w, sv->st, vj, djac, z, sv->flags);
+            if (block) launch_block_prec<T>(c, Binv, vj, z, sv->flags);
+            launch_spmv_masked<TM, T>(c, vals, (djac || block) ? z : vj, w, nullptr, sv->flags);
+            const int nch = j / 8 + 1;
+            dim3 g2(sv->nb, nch);
+            mdot_kernel<T><<<g2, kThreads, 0, c.st>>>(n, j, V, w, sv->part, sv->nb, sv->flags, -1);
+            reduce_kernel<<<j + 2, kThreads, 0, c.st>>>(sv->nb, j + 2, sv->part, sv->red, nullptr, -1);
+            reorth_check<<<1, 1, 0, c.st>>>(sv->red, j, sv->st, sv->flags);
+            axpy_norm_kernel<T><<<sv->nb, kThreads, 0, c.st>>>(n, j, V, sv->red, w, sv->part + (size_t)(m + 2) * sv->nb,
+                                                               sv->flags, -1);
+            reduce_kernel<<<1, kThreads, 0, c.st>>>(sv->nb, 1, sv->part + (size_t)(m + 2) * sv->nb,
+                                                    sv->red + (m + 2), nullptr, -1);
+            reorth_decide<<<1, 1, 0, c.st>>>(sv->red + (m + 2), sv->st, sv->flags);
+            // gated second pass
+            mdot_kernel<T><<<g2, kThreads, 0, c.st>>>(n, j, V, w, sv->part + (size_t)(m + 3) * sv->nb, sv->nb,
+                                                      sv->flags, F_REORTH);
+            reduce_kernel<<<j + 1, kThreads, 0, c.st>>>(sv->nb, j + 1, sv->part + (size_t)(m + 3) * sv->nb,
+                                                        sv->red + (m + 3), sv->flags, F_REORTH);
+            axpy_norm_kernel<T><<<sv->nb, kThreads, 0, c.st>>>(n, j, V, sv->red + (m + 3), w,
+                                                               sv->part + (size_t)(m + 2) * sv->nb, sv->flags,
+                                                               F_REORTH);
+            reduce_kernel<<<1, kThreads, 0, c.st>>>(sv->nb, 1, sv->part + (size_t)(m + 2) * sv->nb,
+                                                    sv->red + (2 * m + 5), sv->flags, F_REORTH);
+            givens_kernel<<<1, 1, 0, c.st>>>(m, j, H, sv->red, sv->red + (m + 3), sv->red + (2 * m + 5), sv->st,
+                                             sv->flags, csg);
+            iters++;
+            if ((iters % std::max(1, sv->prm.check_every)) == 0 || j == m - 1 || iters >= maxit) {
+                if (read_flags(c)) return OCMP_ERR_CUDA;
+                if (sv->hflags[F_CONV]) {
+                    j++;
+                    break;
+                }
+            }
+        }
+        // x += P V y
+        trisolve_kernel<<<1, 1, 0, c.st>>>(m, H, csg, y, sv->flags);
+        combine_kernel<T><<<c.grid, kThreads, 0, c.st>>>(n, V, y, sv->flags, w);
+        if (block) {
+            launch_block_prec<T>(c, Binv, w, z, nullptr);
+            xupdate_kernel<TX, T><<<c.grid, kThreads, 0, c.st>>>(n, z, (const T*)nullptr, xacc);
+        } else {
+            xupdate_kernel<TX, T><<<c.grid, kThreads, 0, c.st>>>(n, w, djac, xacc);
+        }
+        OCMP_CUDA(cudaGetLastError());
+        if (read_flags(c)) return OCMP_ERR_CUDA;
+        if (sv->hflags[F_NONFIN] || sv->hflags[F_BREAK]) break;
+        if (!outer64) break;       // the inner solve is one cycle; refinement restarts it
+        if (iters >= maxit) break;
+        // converged estimate: confirm with the true residual at the top of the loop
+    }
+    *iters_out = iters;
+    return OCMP_OK;
+}
+
+template <class T, class TM, class TX>
+int cg_core(const Ctx& c, const TM* vals, const T* dinv, T* r, T* z, T* p, T* q, TX* x, int maxit, double tol,
+            int* iters_out) {
+    ocmp_solver_s* sv = c.sv;
+    const int64_t n = sv->n;
+    set_state<<<1, 1, 0, c.st>>>(sv->st, S_TOL, tol);
+    OCMP_CUDA(cudaMemsetAsync(sv->flags, 0, sizeof(int) * F_NFLAG, c.st));
+    cg_init<T><<<sv->nb, kThreads, 0, c.st>>>(n, r, dinv, z, p, sv->part, sv->nb);
+    reduce_kernel<<<2, kThreads, 0, c.st>>>(sv->nb, 2, sv->part, sv->red, nullptr, -1);
+    cg_scalars_init<<<1, 1, 0, c.st>>>(sv->red, sv->st, sv->flags);
+    int it = 0;
+    if (read_flags(c)) return OCMP_ERR_CUDA;
+    if (!sv->hflags[F_CONV]) {
+        const int nbs = spmv_blocks(c);
+        while (it < maxit) {
+            launch_spmv_masked<TM, T>(c, vals, p, q, sv->pspmv, sv->flags);
+            reduce_kernel<<<1, kThreads, 0, c.st>>>(nbs, 1, sv->pspmv, sv->red, nullptr, -1);
+            cg_alpha<<<1, 1, 0, c.st>>>(sv->red, sv->st, sv->flags);
+            cg_update<T><<<sv->nb, kThreads, 0, c.st>>>(n, sv->st, x, r, p, q, dinv, z, sv->part, sv->nb, sv->flags);
+            reduce_kernel<<<2, kThreads, 0, c.st>>>(sv->nb, 2, sv->part, sv->red, sv->flags, -1);
+            cg_beta<<<1, 1, 0, c.st>>>(sv->red, sv->st, sv->flags);
+            cg_pupdate<T><<<c.grid, kThreads, 0, c.st>>>(n, sv->st, z, p, sv->flags);
+            it++;
+            if ((it % std::max(1, sv->prm.check_every)) == 0 || it >= maxit) {
+                if (read_flags(c)) return OCMP_ERR_CUDA;
+                if (sv->hflags[F_CONV]) break;
+            }
+        }
+    }
+    OCMP_CUDA(cudaGetLastError());
+    if (read_flags(c)) return OCMP_ERR_CUDA;
+    *iters_out = sv->hflags[F_ITERS];
+    return OCMP_OK;
+}
+
+}  // namespace
+}  // namespace ocmp
+
+using namespace ocmp;
+
+static void free_solver(ocmp_solver_s* sv) {
+    void* ps[] = {sv->dinv, sv->Binv, sv->V,   sv->w,     sv->z,   sv->r,     sv->p,    sv->dinv32, sv->Binv32,
+                  sv->V32,  sv->w32,  sv->z32, sv->r32,   sv->p32, sv->d32,   sv->part, sv->pspmv,  sv->red,
+                  sv->st,   sv->H,    sv->flags};
+    for (void* q : ps) dfree(q);
+    if (sv->hflags) cudaFreeHost(sv->hflags);
+}
+
+extern "C" {
+
+int ocmp_solver_create(ocmp_matrix_t mat, const ocmp_solve_params_t* prm, ocmp_solver_t* out) {
+    if (!mat || !prm || !out) return fail(OCMP_ERR_ARG, "ocmp_solver_create: null argument");
+    if (prm->method != OCMP_CG && prm->method != OCMP_GMRES) return fail(OCMP_ERR_ARG, "ocmp_solver_create: method");
+    if (prm->precond < OCMP_PRE_NONE || prm->precond > OCMP_PRE_BLOCK_JACOBI)
+        return fail(OCMP_ERR_ARG, "ocmp_solver_create: precond");
+    if (prm->precision == OCMP_MIXED && !mat->vals32)
+        return fail(OCMP_ERR_ARG, "ocmp_solver_create: mixed precision needs a matrix created with want_fp32");
+    if (prm->method == OCMP_CG && prm->precond != OCMP_PRE_JACOBI)
+        return fail(OCMP_ERR_UNSUPPORTED, "ocmp_solver_create: CG is built with the Jacobi preconditioner");
+    ocmp_space_s* s = mat->space;
+    if (prm->precond == OCMP_PRE_BLOCK_JACOBI && (s->kind != OCMP_L2 || (s->nloc != 3 && s->nloc != 6 && s->nloc != 10)))
+        return fail(OCMP_ERR_UNSUPPORTED, "ocmp_solver_create: block Jacobi is built for L2 element blocks");
+    auto* sv = new ocmp_solver_s();
+    sv->mat = mat;
+    sv->s = s;
+    sv->prm = *prm;
+    if (sv->prm.check_every <= 0) sv->prm.check_every = 8;
+    const int64_t n = sv->n = s->ndof;
+    sv->m = std::max(1, std::min(128, prm->restart > 0 ? prm->restart : 30));
+    const int m = sv->m;
+    sv->nb = (int)std::max<int64_t>(1, std::min<int64_t>(1216, (n + 1023) / 1024));
+    const bool gm = prm->method == OCMP_GMRES, mixed = prm->precision == OCMP_MIXED;
+    const bool blk = prm->precond == OCMP_PRE_BLOCK_JACOBI;
+    const int tpr = pick_tpr(s);
+    const int64_t nbs = (n * tpr + kThreads - 1) / kThreads;
+    int st = OCMP_OK;
+    auto A = [&](auto** p, size_t cnt) {
+        if (!st) st = dalloc(p, cnt);
+    };
+    A(&sv->dinv, n);
+    A(&sv->w, n);
+    A(&sv->z, n);
+    A(&sv->r, n);
+    if (!mixed) {
+        if (gm) A(&sv->V, (size_t)(m + 1) * n);
+        else A(&sv->p, n);
+    }
+    if (blk) A(&sv->Binv, (size_t)s->mesh->ne * s->nloc * s->nloc);
+    if (mixed) {
+        A(&sv->dinv32, n);
+        A(&sv->w32, n);
+        A(&sv->z32, n);
+        A(&sv->d32, n);
+        if (gm) A(&sv->V32, (size_t)(m + 1) * n);
+        else {
+            A(&sv->r32, n);
+            A(&sv->p32, n);
+        }
+        if (blk) A(&sv->Binv32, (size_t)s->mesh->ne * s->nloc * s->nloc);
+    }
+    A(&sv->part, (size_t)(2 * m + 8) * sv->nb);
+    A(&sv->pspmv, (size_t)nbs);
+    A(&sv->red, (size_t)(3 * m + 12));
+    A(&sv->st, (size_t)S_NSLOT);
+    A(&sv->H, (size_t)(m + 1) * m + 4 * m + 2);
+    A(&sv->flags, (size_t)F_NFLAG);
+    if (!st && cudaMallocHost((void**)&sv->hflags, sizeof(int) * F_NFLAG) != cudaSuccess)
+        st = fail(OCMP_ERR_NOMEM, "cudaMallocHost");
+    if (st) {
+        free_solver(sv);
+        delete sv;
+        return st;
+    }
+    st = ocmp_solver_update(sv, nullptr);
+    if (st) {
+        free_solver(sv);
+        delete sv;
+        return st;
+    }
+    OCMP_CUDA(cudaDeviceSynchronize());
+    *out = sv;
+    return OCMP_OK;
+}
+
+int ocmp_solver_destroy(ocmp_solver_t sv) {
+    if (!sv) return OCMP_OK;
+    free_solver(sv);
+    delete sv;
+    return OCMP_OK;
+}
+
+int ocmp_solver_update(ocmp_solver_t sv, void* stream) {
+    if (!sv) return fail(OCMP_ERR_ARG, "ocmp_solver_update: null solver");
+    cudaStream_t st = (cudaStream_t)stream;
+    ocmp_space_s* s = sv->s;
+    const int64_t n = sv->n;
+    jacobi_setup<double><<<nblk(n, kThreads), kThreads, 0, st>>>(n, s->d_diag, sv->mat->vals, s->d_free, sv->dinv);
+    if (sv->dinv32)
+        jacobi_setup<float><<<nblk(n, kThreads), kThreads, 0, st>>>(n, s->d_diag, sv->mat->vals, s->d_free, sv->dinv32);
+    if (sv->Binv) {
+        const int64_t ne = s->mesh->ne;
+        switch (s->nloc) {
+        case 3: block_jacobi_setup<3><<<nblk(ne, 128), 128, 0, st>>>(ne, s->d_rowptr, s->d_col, sv->mat->vals, sv->Binv, sv->Binv32); break;
+        case 6: block_jacobi_setup<6><<<nblk(ne, 128), 128, 0, st>>>(ne, s->d_rowptr, s->d_col, sv->mat->vals, sv->Binv, sv->Binv32); break;
+        case 10: block_jacobi_setup<10><<<nblk(ne, 128), 128, 0, st>>>(ne, s->d_rowptr, s->d_col, sv->mat->vals, sv->Binv, sv->Binv32); break;
+        default: break;
+        }
+    }
+    OCMP_CUDA(cudaGetLastError());
+    return OCMP_OK;
+}
+
+int ocmp_solve(ocmp_solver_t sv, const double* b, double* x, void* stream, ocmp_solve_info_t* info) {
+    if (!sv || !b || !x) return fail(OCMP_ERR_ARG, "ocmp_solve: null argument");
+    Ctx c;
+    c.sv = sv;
+    c.st = (cudaStream_t)stream;
+    c.tpr = pick_tpr(sv->s);
+    c.grid = sv->nb;
+    const int64_t n = sv->n;
+    const ocmp_solve_params_t& P = sv->prm;
+    const bool gm = P.method == OCMP_GMRES, mixed = P.precision == OCMP_MIXED;
+    int st = rhs_norm(c, b, x);
+    if (st) return st;
+    double hst[S_NSLOT];
+    // initial residual
+    st = residual64(c, b, x, gm && !mixed ? sv->V : sv->r);
+    if (st) return st;
+    double red0 = 0;
+    OCMP_CUDA(cudaMemcpyAsync(&red0, sv->red, sizeof(double), cudaMemcpyDeviceToHost, c.st));
+    OCMP_CUDA(cudaMemcpyAsync(hst, sv->st, sizeof(hst), cudaMemcpyDeviceToHost, c.st));
+    OCMP_CUDA(cudaStreamSynchronize(c.st));
+    const double nbv = hst[S_NB];
+    double relres0 = std::sqrt(std::max(red0, 0.0)) / nbv;
+    int iters = 0, outer = 0;
+    bool nonfin = !std::isfinite(relres0), brk = false;
+    if (!nonfin && relres0 > P.tol) {
+        if (!mixed) {
+            if (gm) {
+                st = gmres_core<double, double, double>(c, sv->mat->vals, sv->dinv, sv->Binv, sv->V, sv->w, sv->z, x, b,
+                                                        x, P.maxit, P.tol, &iters, true);
+            } else {
+                st = cg_core<double, double, double>(c, sv->mat->vals, sv->dinv, sv->r, sv->z, sv->p, sv->w, x, P.maxit,
+                                                     P.tol, &iters);
+            }
+            if (st) return st;
+            nonfin = sv->hflags[F_NONFIN] != 0;
+            brk = sv->hflags[F_BREAK] != 0;
+        } else {
+            double beta = std::sqrt(std::max(red0, 0.0));
+            while (iters < P.maxit) {
+                // inner FP32 solve of A d = r / beta
+                set_state<<<1, 1, 0, c.st>>>(sv->st, S_BETA, beta);
+                set_state<<<1, 1, 0, c.st>>>(sv->st, S_NB, 1.0);
+                double itol = std::max(P.inner_tol > 0 ? P.inner_tol : 1e-4, 0.5 * P.tol * nbv / beta);
+                OCMP_CUDA(cudaMemsetAsync(sv->d32, 0, sizeof(float) * n, c.st));
+                int it_in = 0;
+                if (gm) {
+                    scale_to_float<<<c.grid, kThreads, 0, c.st>>>(n, sv->r, sv->st, sv->V32);
+                    set_state<<<1, 1, 0, c.st>>>(sv->red, 0, 1.0);
+                    st = gmres_core<float, float, float>(c, sv->mat->vals32, sv->dinv32, sv->Binv32, sv->V32, sv->w32,
+                                                         sv->z32, sv->d32, b, x, P.maxit - iters, itol, &it_in, false);
+                } else {
+                    scale_to_float<<<c.grid, kThreads, 0, c.st>>>(n, sv->r, sv->st, sv->r32);
+                    st = cg_core<float, float, float>(c, sv->mat->vals32, sv->dinv32, sv->r32, sv->z32, sv->p32,
+                                                      sv->w32, sv->d32, P.maxit - iters, itol, &it_in);
+                }
+                if (st) return st;
+                iters += std::max(it_in, 1);
+                outer++;
+                if (sv->hflags[F_NONFIN]) {
+                    nonfin = true;
+                    break;
+                }
+                set_state<<<1, 1, 0, c.st>>>(sv->st, S_BETA, beta);
+                add_scaled_float<<<c.grid, kThreads, 0, c.st>>>(n, sv->d32, sv->st, x);
+                set_state<<<1, 1, 0, c.st>>>(sv->st, S_NB, nbv);
+                st = residual64(c, b, x, sv->r);
+                if (st) return st;
+                OCMP_CUDA(cudaMemcpyAsync(&red0, sv->red, sizeof(double), cudaMemcpyDeviceToHost, c.st));
+                OCMP_CUDA(cudaStreamSynchronize(c.st));
+                beta = std::sqrt(std::max(red0, 0.0));
+                if (!std::isfinite(beta)) {
+                    nonfin = true;
+                    break;
+                }
+                if (beta / nbv <= P.tol) break;
+            }
+        }
+    }
+    // final FP64 relative residual
+    set_state<<<1, 1, 0, c.st>>>(sv->st, S_NB, nbv);
+    st = residual64(c, b, x, (double*)nullptr);
+    if (st) return st;
+    OCMP_CUDA(cudaMemcpyAsync(&red0, sv->red, sizeof(double), cudaMemcpyDeviceToHost, c.st));
+    OCMP_CUDA(cudaStreamSynchronize(c.st));
+    const double relres = std::sqrt(std::max(red0, 0.0)) / nbv;
+    int status = OCMP_OK;
+    if (nonfin || !std::isfinite(relres)) status = OCMP_ERR_NONFINITE;
+    else if (relres > P.tol) status = brk ? OCMP_BREAKDOWN : OCMP_NOT_CONVERGED;
+    if (info) {
+        info->status = status;
+        info->iterations = iters;
+        info->outer_iterations = outer;
+        info->relres0 = relres0;
+        info->relres = relres;
+    }
+    if (status == OCMP_ERR_NONFINITE) set_error("ocmp_solve: non-finite value in the right-hand side or iteration");
+    else if (status == OCMP_NOT_CONVERGED) set_error("ocmp_solve: iteration cap reached before the tolerance");
+    else if (status == OCMP_BREAKDOWN) set_error("ocmp_solve: Krylov breakdown");
+    return status;
+}
+
+}  // extern "C"

@@ -1,0 +1,264 @@
+"""Host-side handles over libopencmp_gpu.so: the GPU stand-ins for the NGSolve objects OpenCMP passes
+around (mesh, finite-element space with ``FreeDofs``, assembled matrix, linear-form vector,
+preconditioned Krylov solver).
+
+Device arrays are torch tensors (``device='cuda'``); torch only owns memory and streams. All
+arithmetic happens in the library's kernels.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from typing import Dict, Optional, Sequence
+
+import numpy as np
+import torch
+
+from . import _lib as LB
+from .mesh import Mesh
+
+
+def _ptr(a):
+    if a is None:
+        return None
+    if isinstance(a, torch.Tensor):
+        return C.c_void_p(a.data_ptr())
+    return a.ctypes.data_as(C.c_void_p)
+
+
+def _stream(stream):
+    if stream is None:
+        return C.c_void_p(torch.cuda.current_stream().cuda_stream)
+    if isinstance(stream, torch.cuda.Stream):
+        return C.c_void_p(stream.cuda_stream)
+    return C.c_void_p(stream)
+
+
+class GPUMesh:
+    """Device copy of a :class:`Mesh` (``ocmp_mesh_create``)."""
+
+    def __init__(self, mesh: Mesh):
+        self.mesh = mesh
+        self._keep = [np.ascontiguousarray(mesh.coords, np.float64), np.ascontiguousarray(mesh.elements, np.int32),
+                      np.ascontiguousarray(mesh.bfacets, np.int32), np.ascontiguousarray(mesh.blabels, np.int32)]
+        h = C.c_void_p()
+        c, e, bf, bl = self._keep
+        LB.call('ocmp_mesh_create', _ptr(c), mesh.nv, mesh.dim, _ptr(e), mesh.ne, _ptr(bf), _ptr(bl),
+                bf.shape[0], C.byref(h))
+        self.h = h
+
+    def __del__(self):
+        if getattr(self, 'h', None) and LB._lib is not None:
+            LB._lib.ocmp_mesh_destroy(self.h)
+            self.h = None
+
+
+class Space:
+    """H1 (order 1..3, triangles/tetrahedra) or L2 (order 1..3, triangles) space on the GPU.
+
+    ``dirichlet`` names boundary labels whose dofs are constrained (``FreeDofs`` excludes them).
+    """
+
+    def __init__(self, mesh: Mesh, kind: str = 'H1', order: int = 1, dirichlet: Sequence[str] | str = (),
+                 gmesh: Optional[GPUMesh] = None):
+        self.mesh = mesh
+        self.gmesh = gmesh or GPUMesh(mesh)
+        self.kind = LB.H1 if kind in ('H1', LB.H1) else LB.L2
+        self.order = order
+        self.dirichlet_mask = mesh.label_mask(dirichlet) if self.kind == LB.H1 else 0
+        h = C.c_void_p()
+        LB.call('ocmp_space_create', self.gmesh.h, self.kind, order, self.dirichlet_mask, C.byref(h))
+        self.h = h
+        info = LB.SpaceInfo()
+        LB.call('ocmp_space_info', self.h, C.byref(info))
+        self.info = info
+        self.ndof, self.nnz, self.nloc, self.nq = info.ndof, info.nnz, info.nloc, info.nq
+        self._free = None
+
+    def __del__(self):
+        if getattr(self, 'h', None) and LB._lib is not None:
+            LB._lib.ocmp_space_destroy(self.h)
+            self.h = None
+
+    def dofs(self) -> np.ndarray:
+        d = np.empty((self.mesh.ne, self.nloc), np.int32)
+        LB.call('ocmp_space_get_dofs', self.h, _ptr(d))
+        return d
+
+    def pattern(self):
+        rp = np.empty(self.ndof + 1, np.int64)
+        col = np.empty(self.nnz, np.int32)
+        LB.call('ocmp_space_get_pattern', self.h, _ptr(rp), _ptr(col))
+        return rp, col
+
+    def FreeDofs(self) -> np.ndarray:
+        if self._free is None:
+            f = np.empty(self.ndof, np.uint8)
+            LB.call('ocmp_space_get_free', self.h, _ptr(f))
+            self._free = f.astype(bool)
+        return self._free
+
+    def quad_points(self) -> np.ndarray:
+        x = np.empty((self.mesh.ne, self.nq, self.mesh.dim), np.float64)
+        LB.call('ocmp_space_quad_points', self.h, _ptr(x))
+        return x
+
+    def set_boundary(self, labels: Dict[int, float], u: torch.Tensor, mask: Optional[int] = None, stream=None):
+        g = np.zeros(32, np.float64)
+        m = 0
+        for lab, v in labels.items():
+            g[lab] = v
+            m |= 1 << lab
+        if mask is not None:
+            m = mask
+        LB.call('ocmp_set_boundary', self.h, m, _ptr(g), _ptr(u), _stream(stream))
+
+
+def make_form(mass=0.0, diff=0.0, dt=1.0, wind=None, wind_vtx: Optional[torch.Tensor] = None, ipc=10.0, dg=False,
+              outflow_mask=0, wn_mask=0, nitsche_mask=0) -> LB.Form:
+    f = LB.Form()
+    f.mass, f.diff, f.dt, f.ipc, f.dg = mass, diff, dt, ipc, int(dg)
+    f.outflow_mask, f.wn_mask, f.nitsche_mask = outflow_mask, wn_mask, nitsche_mask
+    f.wind_kind = LB.WIND_NONE
+    if wind_vtx is not None:
+        f.wind_kind = LB.WIND_VERTEX
+        f.wind_vtx = wind_vtx.data_ptr()
+    elif wind is not None:
+        f.wind_kind = LB.WIND_CONST
+        for k, w in enumerate(wind):
+            f.wind[k] = w
+    return f
+
+
+def make_rhs(dt=1.0, src_const=None, src_qp: Optional[torch.Tensor] = None, mass=0.0,
+             uprev: Optional[torch.Tensor] = None, bval: Optional[Dict[int, float]] = None,
+             gval: Optional[Dict[int, float]] = None) -> LB.Rhs:
+    r = LB.Rhs()
+    r.dt, r.mass = dt, mass
+    r.src_kind = LB.SRC_NONE
+    if src_qp is not None:
+        r.src_kind, r.src_qp = LB.SRC_QP, src_qp.data_ptr()
+    elif src_const is not None:
+        r.src_kind, r.src_const = LB.SRC_CONST, src_const
+    if uprev is not None:
+        r.uprev = uprev.data_ptr()
+    for lab, v in (bval or {}).items():
+        r.bval[lab] = v
+        r.bval_mask |= 1 << lab
+    for lab, v in (gval or {}).items():
+        r.gval[lab] = v
+    return r
+
+
+class Matrix:
+    """Assembled sparse matrix in the space's CSR pattern (FP64 values, optional FP32 copy)."""
+
+    def __init__(self, space: Space, fp32: bool = False):
+        self.space = space
+        h = C.c_void_p()
+        LB.call('ocmp_matrix_create', space.h, int(fp32), C.byref(h))
+        self.h = h
+        self.fp32 = fp32
+
+    def __del__(self):
+        if getattr(self, 'h', None) and LB._lib is not None:
+            LB._lib.ocmp_matrix_destroy(self.h)
+            self.h = None
+
+    def assemble(self, form: LB.Form, stream=None):
+        LB.call('ocmp_assemble_matrix', self.h, C.byref(form), _stream(stream))
+
+    def device_values(self):
+        """Zero-copy torch views of the FP64 (and FP32, or None) value arrays on the device."""
+        p64, p32 = C.c_void_p(), C.c_void_p()
+        LB.call('ocmp_matrix_values', self.h, C.byref(p64), C.byref(p32))
+        v64 = _dev_view(p64.value, self.space.nnz, '<f8', self)
+        v32 = _dev_view(p32.value, self.space.nnz, '<f4', self) if p32.value else None
+        return v64, v32
+
+    def values(self) -> np.ndarray:
+        """FP64 values copied to the host (for checks)."""
+        torch.cuda.synchronize()
+        return self.device_values()[0].cpu().numpy()
+
+    def values32(self) -> np.ndarray:
+        torch.cuda.synchronize()
+        return self.device_values()[1].cpu().numpy()
+
+    def mult(self, x: torch.Tensor, y: torch.Tensor, stream=None):
+        LB.call('ocmp_spmv', self.h, _ptr(x), _ptr(y), _stream(stream))
+
+
+class _CudaArray:
+    """Minimal __cuda_array_interface__ holder so torch can view library-owned device memory."""
+
+    def __init__(self, ptr, n, typestr, owner):
+        self.__cuda_array_interface__ = {'shape': (n,), 'typestr': typestr, 'data': (ptr, False), 'version': 3,
+                                         'strides': None}
+        self._owner = owner
+
+
+def _dev_view(ptr, n, typestr, owner):
+    return torch.as_tensor(_CudaArray(ptr, n, typestr, owner), device='cuda')
+
+
+def assemble_rhs(space: Space, form: LB.Form, rhs: LB.Rhs, b: torch.Tensor, stream=None):
+    LB.call('ocmp_assemble_rhs', space.h, C.byref(form), C.byref(rhs), _ptr(b), _stream(stream))
+
+
+class KrylovSolver:
+    """Preconditioned CG / GMRES(m) on the free dofs of an assembled matrix (``ocmp_solve``)."""
+
+    def __init__(self, mat: Matrix, method='GMRES', restart=30, precond='jacobi', precision='fp64', tol=1e-8,
+                 maxit=1000, inner_tol=1e-4, check_every=8):
+        self.mat = mat
+        p = LB.SolveParams()
+        p.method = LB.CG if str(method).upper() == 'CG' else LB.GMRES
+        p.restart = restart
+        p.precond = {'none': LB.PRE_NONE, 'jacobi': LB.PRE_JACOBI, 'local': LB.PRE_JACOBI,
+                     'block_jacobi': LB.PRE_BLOCK_JACOBI, 'block': LB.PRE_BLOCK_JACOBI}[str(precond).lower()]
+        p.precision = LB.MIXED if str(precision).lower() == 'mixed' else LB.FP64
+        p.tol, p.maxit, p.inner_tol, p.check_every = tol, maxit, inner_tol, check_every
+        self.params = p
+        h = C.c_void_p()
+        LB.call('ocmp_solver_create', mat.h, C.byref(p), C.byref(h))
+        self.h = h
+
+    def __del__(self):
+        if getattr(self, 'h', None) and LB._lib is not None:
+            LB._lib.ocmp_solver_destroy(self.h)
+            self.h = None
+
+    def update(self, stream=None):
+        LB.call('ocmp_solver_update', self.h, _stream(stream))
+
+    def solve(self, b: torch.Tensor, x: torch.Tensor, stream=None, raise_on_fail=True) -> LB.SolveInfo:
+        info = LB.SolveInfo()
+        st = LB.load().ocmp_solve(self.h, _ptr(b), _ptr(x), _stream(stream), C.byref(info))
+        if raise_on_fail:
+            LB.check(st)
+        return info
+
+
+_EDGES = {2: [(0, 1), (0, 2), (1, 2)], 3: [(0, 1), (0, 2), (0, 3), (1, 2), (1, 3), (2, 3)]}
+
+
+def interpolate_p2_arrays(coords, sorted_conn, dofs, ndof, fn):
+    """P2 Lagrange interpolant of fn in the hierarchical basis (vertex values; edge bubble
+    lam_a lam_b with coefficient 4 (f(mid) - (f(a) + f(b)) / 2)). Host-side, numpy."""
+    D = coords.shape[1]
+    u = np.zeros(ndof, np.float64)
+    nv = coords.shape[0]
+    u[:nv] = fn(coords)
+    for k, (a, b) in enumerate(_EDGES[D]):
+        va, vb = sorted_conn[:, a], sorted_conn[:, b]
+        mid = 0.5 * (coords[va] + coords[vb])
+        u[dofs[:, D + 1 + k]] = 4.0 * (fn(mid) - 0.5 * (u[va] + u[vb]))
+    return u
+
+
+def interpolate_p2(space: 'Space', fn):
+    """Interpolant of fn in an H1 order-2 space (initial conditions of the benchmarks)."""
+    if space.kind != LB.H1 or space.order != 2:
+        raise ValueError('interpolate_p2 needs an H1 order-2 space')
+    m = space.mesh
+    return interpolate_p2_arrays(m.coords, np.sort(m.elements, axis=1), space.dofs(), space.ndof, fn)
