@@ -156,6 +156,23 @@ int ocmp_solver_update(ocmp_solver_t solver, void* stream);
 /* Solve A_ff x_f = (b - A x_D)_f in place; x_dev holds the Dirichlet values and the initial guess. */
 int ocmp_solve(ocmp_solver_t solver, const double* b_dev, double* x_dev, void* stream, ocmp_solve_info_t* info);
 
+/* ---------------------------------------------------------------- allocation-free solve
+ * No counterpart in the reference: an addition for callers that cannot call cudaMalloc when they
+ * solve (a stream being captured into a CUDA graph in global capture mode, a host whose device
+ * memory belongs to another allocator's fixed pool, a loop that cannot take cudaFree's implicit
+ * device synchronisation). Same FP64 Jacobi-preconditioned CG as ocmp_solve with OCMP_CG, on the
+ * free dofs of `mat`, to the same relative-residual definition; it allocates nothing. Its
+ * workspace is a static device array of 41 MiB that every GPU which loads this library holds until
+ * the process exits; systems with more than OCMP_NOALLOC_MAX_NDOF dofs are rejected with
+ * OCMP_ERR_ARG. The first call on each device looks up that array's device address
+ * (cudaGetSymbolAddress) with the device current: make that first call before any stream capture.
+ * All calls share the one workspace and it keeps the last call's contents (the call resets what
+ * must start at zero): calls whose work overlaps on the GPU (different streams or threads) race,
+ * so serialise them. */
+#define OCMP_NOALLOC_MAX_NDOF 1048576
+int ocmp_solve_cg_noalloc(ocmp_matrix_t mat, const double* b_dev, double* x_dev, double tol, int32_t maxit,
+                          void* stream, ocmp_solve_info_t* info);
+
 #ifdef __cplusplus
 }
 #endif

@@ -86,6 +86,7 @@ SIGNATURES = {
     'ocmp_solver_destroy': [P],
     'ocmp_solver_update': [P, P],
     'ocmp_solve': [P, P, P, P, C.POINTER(SolveInfo)],
+    'ocmp_solve_cg_noalloc': [P, P, P, D, I32, P, C.POINTER(SolveInfo)],
 }
 
 _lib = None

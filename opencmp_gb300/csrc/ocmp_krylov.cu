@@ -16,6 +16,8 @@
 
 #include <algorithm>
 #include <cmath>
+#include <mutex>
+#include <string>
 
 #include "ocmp_internal.h"
 
@@ -912,3 +914,138 @@ int ocmp_solve(ocmp_solver_t sv, const double* b, double* x, void* stream, ocmp_
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------------------------
+// Allocation-free CG. Some callers cannot call cudaMalloc at the moment they need a solve: code
+// that runs while a stream is being captured into a CUDA graph in global capture mode, hosts whose
+// device memory belongs to another allocator's fixed pool, and latency-bound loops that cannot
+// afford cudaFree's implicit device synchronisation. ocmp_solve_cg_noalloc serves them: it runs the
+// same FP64 Jacobi-preconditioned CG as ocmp_solve with method OCMP_CG, but its workspace (five
+// n-vectors, reduction partials, scalars and flags) lives in the file-scope device arrays below,
+// which the driver allocates once per device when this library is loaded and keeps until exit.
+// The caller passes only the assembled matrix, the right-hand side and the initial guess/result.
+namespace {
+
+constexpr int64_t kNoAllocMaxN = OCMP_NOALLOC_MAX_NDOF;      // 1,048,576 dofs
+constexpr int64_t kNoAllocRed = int64_t(1) << 17;            // reduction partials
+constexpr int64_t kNoAllocState = 256;                        // reduced values + scalars
+constexpr int64_t kNoAllocDoubles = 5 * kNoAllocMaxN + kNoAllocRed + kNoAllocState;  // 41 MiB
+
+static __device__ __align__(256) double g_noalloc_scratch[kNoAllocDoubles];
+static __device__ __align__(256) int g_noalloc_flags[64];
+
+std::mutex g_noalloc_mu;
+double* g_noalloc_ptr[128] = {};
+int* g_noalloc_fptr[128] = {};
+
+// Device addresses of the scratch arrays for the current device. Host code must not use the
+// arrays' names as pointers (they name host-side shadows); cudaGetSymbolAddress gives the device
+// address. Done once per device, under a lock, with that device current.
+int noalloc_scratch(double** scratch, int** flags) {
+    int dev = 0;
+    OCMP_CUDA(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= 128) return fail(OCMP_ERR_ARG, "ocmp_solve_cg_noalloc: device index out of range");
+    std::lock_guard<std::mutex> lk(g_noalloc_mu);
+    if (!g_noalloc_ptr[dev]) {
+        double* p = nullptr;
+        int* f = nullptr;
+        cudaError_t e = cudaGetSymbolAddress((void**)&p, g_noalloc_scratch);
+        if (e != cudaSuccess) return cuda_fail(e, "cudaGetSymbolAddress(g_noalloc_scratch)");
+        e = cudaGetSymbolAddress((void**)&f, g_noalloc_flags);
+        if (e != cudaSuccess) return cuda_fail(e, "cudaGetSymbolAddress(g_noalloc_flags)");
+        g_noalloc_ptr[dev] = p;
+        g_noalloc_fptr[dev] = f;
+    }
+    *scratch = g_noalloc_ptr[dev];
+    *flags = g_noalloc_fptr[dev];
+    return OCMP_OK;
+}
+
+}  // namespace
+
+extern "C" int ocmp_solve_cg_noalloc(ocmp_matrix_t mat, const double* b, double* x, double tol, int32_t maxit,
+                                     void* stream, ocmp_solve_info_t* info) {
+    if (!mat || !b || !x) return fail(OCMP_ERR_ARG, "ocmp_solve_cg_noalloc: null argument");
+    ocmp_space_s* s = mat->space;
+    const int64_t n = s->ndof;
+    if (n > kNoAllocMaxN)
+        return fail(OCMP_ERR_ARG, "ocmp_solve_cg_noalloc: " + std::to_string(n) + " dofs exceed the " +
+                                      std::to_string(kNoAllocMaxN) + "-dof limit of its static workspace");
+    const int tpr = pick_tpr(s);
+    if ((n * tpr + kThreads - 1) / kThreads > kNoAllocRed)
+        return fail(OCMP_ERR_ARG, "ocmp_solve_cg_noalloc: SpMV partials exceed the static workspace");
+    double* scr = nullptr;
+    int* flg = nullptr;
+    int st = noalloc_scratch(&scr, &flg);
+    if (st) return st;
+    // A solver view over the static workspace: nothing here touches the allocator.
+    ocmp_solver_s sv;
+    sv.mat = mat;
+    sv.s = s;
+    sv.prm.method = OCMP_CG;
+    sv.prm.precond = OCMP_PRE_JACOBI;
+    sv.prm.precision = OCMP_FP64;
+    sv.prm.tol = tol;
+    sv.prm.maxit = maxit;
+    sv.prm.check_every = 8;
+    sv.n = n;
+    sv.m = 1;
+    sv.nb = (int)std::max<int64_t>(1, std::min<int64_t>(1216, (n + 1023) / 1024));
+    sv.dinv = scr;
+    sv.r = scr + n;
+    sv.z = scr + 2 * n;
+    sv.p = scr + 3 * n;
+    sv.w = scr + 4 * n;
+    double* tail = scr + 5 * kNoAllocMaxN;
+    sv.pspmv = tail;
+    sv.part = tail;  // CG partials (2 x nb) never overlap a live SpMV partial
+    sv.red = tail + kNoAllocRed;
+    sv.st = sv.red + 64;
+    sv.flags = flg;
+    int hflags[F_NFLAG] = {0};
+    sv.hflags = hflags;
+    Ctx c;
+    c.sv = &sv;
+    c.st = (cudaStream_t)stream;
+    c.tpr = tpr;
+    c.grid = sv.nb;
+    // the workspace keeps the previous call's contents: reset the flags and scalars
+    OCMP_CUDA(cudaMemsetAsync(flg, 0, sizeof(int) * 64, c.st));
+    OCMP_CUDA(cudaMemsetAsync(sv.red, 0, sizeof(double) * kNoAllocState, c.st));
+    jacobi_setup<double><<<nblk(n, kThreads), kThreads, 0, c.st>>>(n, s->d_diag, mat->vals, s->d_free, sv.dinv);
+    st = rhs_norm(c, b, x);
+    if (st) return st;
+    st = residual64(c, b, x, sv.r);
+    if (st) return st;
+    double red0 = 0, nbv = 1;
+    OCMP_CUDA(cudaMemcpyAsync(&red0, sv.red, sizeof(double), cudaMemcpyDeviceToHost, c.st));
+    OCMP_CUDA(cudaMemcpyAsync(&nbv, sv.st + S_NB, sizeof(double), cudaMemcpyDeviceToHost, c.st));
+    OCMP_CUDA(cudaStreamSynchronize(c.st));
+    const double relres0 = std::sqrt(std::max(red0, 0.0)) / nbv;
+    int iters = 0;
+    bool nonfin = !std::isfinite(relres0), brk = false;
+    if (!nonfin && relres0 > tol) {
+        st = cg_core<double, double, double>(c, mat->vals, sv.dinv, sv.r, sv.z, sv.p, sv.w, x, maxit, tol, &iters);
+        if (st) return st;
+        nonfin = hflags[F_NONFIN] != 0;
+        brk = hflags[F_BREAK] != 0;
+    }
+    st = residual64(c, b, x, (double*)nullptr);
+    if (st) return st;
+    OCMP_CUDA(cudaMemcpyAsync(&red0, sv.red, sizeof(double), cudaMemcpyDeviceToHost, c.st));
+    OCMP_CUDA(cudaStreamSynchronize(c.st));
+    const double relres = std::sqrt(std::max(red0, 0.0)) / nbv;
+    int status = OCMP_OK;
+    if (nonfin || !std::isfinite(relres)) status = OCMP_ERR_NONFINITE;
+    else if (relres > tol) status = brk ? OCMP_BREAKDOWN : OCMP_NOT_CONVERGED;
+    if (info) {
+        info->status = status;
+        info->iterations = iters;
+        info->outer_iterations = 0;
+        info->relres0 = relres0;
+        info->relres = relres;
+    }
+    if (status != OCMP_OK) set_error("ocmp_solve_cg_noalloc: did not reach the tolerance (status " +
+                                     std::to_string(status) + ")");
+    return status;
+}
