@@ -112,20 +112,25 @@ def run_ours(args):
     space = fem.Space(mesh, 'H1', 2, mesh.bc_names)
     setup_s = time.perf_counter() - t0
     ndof, nnz = space.ndof, space.nnz
-    A = fem.Matrix(space, fp32=True)
+    # each path assembles the Krylov matrix it iterates with (A D^-1 in FP64, or in FP32) in the same
+    # pass as the FP64 values used for the residuals
+    mats = {'fp64': fem.Matrix(space, jacobi64=True), 'mixed': fem.Matrix(space, jacobi32=True)}
     form = fem.make_form(mass=1.0, diff=EPS, dt=DT, wind=WIND)
     u0 = torch.as_tensor(fem.interpolate_p2(space, gaussian), device='cuda')
     b = torch.zeros(ndof, dtype=torch.float64, device='cuda')
-    A.assemble(form)
+    for M_ in mats.values():
+        M_.assemble(form)
+    A = mats['fp64']
     solvers = {
-        'fp64': fem.KrylovSolver(A, method='GMRES', restart=args.restart, precond='jacobi', precision='fp64', tol=1e-8,
-                                 maxit=2000, check_every=args.check_every),
-        'mixed': fem.KrylovSolver(A, method='GMRES', restart=args.restart, precond='jacobi', precision='mixed',
-                                  tol=1e-8, maxit=2000, inner_tol=args.inner_tol, check_every=args.check_every),
+        'fp64': fem.KrylovSolver(mats['fp64'], method='GMRES', restart=args.restart, precond='jacobi',
+                                 precision='fp64', tol=1e-8, maxit=2000, check_every=args.check_every),
+        'mixed': fem.KrylovSolver(mats['mixed'], method='GMRES', restart=args.restart, precond='jacobi',
+                                  precision='mixed', tol=1e-8, maxit=2000, inner_tol=args.inner_tol,
+                                  check_every=args.check_every),
     }
 
     def step(sv, u_in, u_out, stats):
-        A.assemble(form)
+        sv.mat.assemble(form)
         sv.update()
         fem.assemble_rhs(space, form, fem.make_rhs(dt=DT, mass=1.0, uprev=u_in), b)
         u_out.copy_(u_in)
@@ -205,6 +210,7 @@ def run_ours(args):
         'plain_fp64': {'value': plain, 'unit': 'DOF/s', 'ms_per_step': ms_plain / args.steps,
                        'iters_per_step': float(np.mean([s[0] for s in st_plain]))},
         'optimised': {'kind': 'mixed: FP32 inner GMRES + FP64 iterative refinement',
+                      'relres0_per_step': float(np.mean([s[2] for s in st_opt])),
                       'iters_per_step': float(np.mean([s[0] for s in st_opt])),
                       'outer_per_step': float(np.mean([s[1] for s in st_opt])),
                       'max_relres': float(max(s[3] for s in st_opt)), 'speedup_vs_plain_fp64': value / plain},

@@ -140,9 +140,15 @@ int ocmp_set_boundary(ocmp_space_t space, uint32_t mask, const double* gval_host
                       void* stream);
 
 /* ---------------------------------------------------------------- assembly */
-int ocmp_matrix_create(ocmp_space_t space, int32_t want_fp32, ocmp_matrix_t* out);
+/* Matrix outputs written by each assembly (flags, OR-able). The FP64 values are always written.
+ * The Jacobi-scaled values A D^-1 (D = diag A on free rows) are the Krylov matrices the GMRES path
+ * uses with the point-Jacobi preconditioner; assembling them in the same pass saves a sweep. */
+enum { OCMP_MAT_FP32 = 1, OCMP_MAT_JACOBI64 = 2, OCMP_MAT_JACOBI32 = 4 };
+int ocmp_matrix_create(ocmp_space_t space, int32_t flags, ocmp_matrix_t* out);
 int ocmp_matrix_destroy(ocmp_matrix_t mat);
 int ocmp_matrix_values(ocmp_matrix_t mat, double** vals64_dev, float** vals32_dev);
+/* Device pointers of the Jacobi-scaled values A D^-1 (FP64, FP32) and of D^-1 (NULL if not built). */
+int ocmp_matrix_scaled_values(ocmp_matrix_t mat, double** svals64_dev, float** svals32_dev, double** dinv_dev);
 int ocmp_assemble_matrix(ocmp_matrix_t mat, const ocmp_form_t* form, void* stream);
 int ocmp_assemble_rhs(ocmp_space_t space, const ocmp_form_t* form, const ocmp_rhs_t* rhs, double* b_dev,
                       void* stream);

@@ -79,6 +79,7 @@ SIGNATURES = {
     'ocmp_matrix_create': [P, I32, C.POINTER(P)],
     'ocmp_matrix_destroy': [P],
     'ocmp_matrix_values': [P, C.POINTER(P), C.POINTER(P)],
+    'ocmp_matrix_scaled_values': [P, C.POINTER(P), C.POINTER(P), C.POINTER(P)],
     'ocmp_assemble_matrix': [P, C.POINTER(Form), P],
     'ocmp_assemble_rhs': [P, C.POINTER(Form), C.POINTER(Rhs), P, P],
     'ocmp_spmv': [P, P, P, P],

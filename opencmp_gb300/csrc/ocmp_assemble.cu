@@ -1,19 +1,23 @@
 // Assembly kernels of libopencmp_gpu.so (sm_103a).
 //
-// Matrix assembly is two launches (plus one for facet terms when the form has any):
-//   1. elem_factors   one thread per element: Jacobian, |det J| and J^-1 in FP64, reduced to the
-//                     ng geometric/coefficient factors F[g][e] of the element matrix
-//                     K_e = sum_g F[g][e] R_g (R_g = reference-element tensors, exact quadrature);
-//   2. scatter        one thread per CSR entry: walks its segment of the precomputed, sorted
-//                     contribution list and sums F[.][e] . R[.][ij] for element entries and the
-//                     precomputed facet-matrix entries for facet contributions. Every CSR value
-//                     is written exactly once, in a fixed order: the result is bit-reproducible
-//                     and needs no atomics and no zeroing pass.
+// Matrix assembly (FP64 throughout; GB300 runs FP64 at 1/58 of its FP32 rate, so the FP64 work
+// per element is kept small and the data movement coalesced):
+//   1. elem_matrix_kernel  one thread per element: Jacobian, |det J|, barycentric gradients, the
+//                     element factors (mass, G_ab = grad lam_a . grad lam_b, wind projections),
+//                     then the sparse barycentric term list K[slot] += F[g] * coef in shared memory
+//                     (symmetric parts for i <= j only), written out coalesced as K[e][i][j];
+//   2. diag_kernel    (only when Jacobi-scaled outputs are requested) the diagonal of each row;
+//   3. row_scatter_kernel  one thread per CSR row: sums the element-matrix row slices K[e][i][:]
+//                     of its incident elements (and facet-matrix rows) into the row through the
+//                     byte-sized slot table, then writes the row once: FP64 values, and optionally
+//                     an FP32 copy and the Jacobi-scaled A D^-1 in FP64 / FP32.
+// Every CSR value is produced by one thread in a fixed order: bit-reproducible, no atomics.
 // Facet matrices (DG skeleton terms, boundary terms) are computed by quadrature because their
 // integrands (max(w.n, 0)) are not polynomial.
 #include <cuda_runtime.h>
 
 #include "ocmp_internal.h"
+#include "ocmp_spmv.cuh"
 
 namespace ocmp {
 namespace {
@@ -70,57 +74,6 @@ struct FormArgs {
     uint32_t outflow, wn, nitsche;
     int dg, order;
 };
-
-// F layout: g-major, F[g * ne + e].  g = 0 mass; 1..S stiffness (k <= l); then wind factors.
-template <int D>
-__global__ void elem_factors(int64_t ne, const double* __restrict__ X, const int32_t* __restrict__ conn,
-                             FormArgs a, double* __restrict__ F) {
-    int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    if (e >= ne) return;
-    Geo g;
-    double x0[3];
-    element_geo<D>(X, conn, e, g, x0);
-    int k = 0;
-    F[(k++) * ne + e] = a.mass * g.adet;
-    const double sd = a.dt * a.diff * g.adet;
-#pragma unroll
-    for (int r = 0; r < D; r++)
-#pragma unroll
-        for (int c = r; c < D; c++) {
-            double m = 0;
-#pragma unroll
-            for (int t = 0; t < D; t++) m += g.Ji[r][t] * g.Ji[c][t];
-            F[(k++) * ne + e] = sd * m;
-        }
-    const double sw = -a.dt * g.adet;
-    if (a.wind_kind == OCMP_WIND_CONST) {
-        const double w[3] = {a.w0, a.w1, a.w2};
-#pragma unroll
-        for (int r = 0; r < D; r++) {
-            double t = 0;
-#pragma unroll
-            for (int c = 0; c < D; c++) t += g.Ji[r][c] * w[c];
-            F[(k++) * ne + e] = sw * t;
-        }
-    } else if (a.wind_kind == OCMP_WIND_VERTEX) {
-        double wv[D + 1][3];
-#pragma unroll
-        for (int v = 0; v <= D; v++) {
-            int32_t gv = conn[e * (D + 1) + v];
-#pragma unroll
-            for (int c = 0; c < D; c++) wv[v][c] = a.wind_vtx[(int64_t)gv * D + c];
-        }
-#pragma unroll
-        for (int r = 0; r < D; r++)
-#pragma unroll
-            for (int v = 0; v <= D; v++) {
-                double t = 0;
-#pragma unroll
-                for (int c = 0; c < D; c++) t += g.Ji[r][c] * wv[v][c];
-                F[(k++) * ne + e] = sw * t;
-            }
-    }
-}
 
 // Facet geometry on local facet lf of element e: outward unit normal, measure factor (length in
 // 2D, |cross| = 2 area in 3D, matching rule weights that sum to 1 and 1/2).
@@ -328,33 +281,206 @@ __global__ void boundary_facet_kernel(int64_t nbf, const double* __restrict__ X,
     for (int j = 0; j < L; j++) out[j] = row[j];
 }
 
-// The sorted segmented reduction. R (ng x L^2) is staged in shared memory.
-template <int L>
-__global__ void __launch_bounds__(256) scatter_kernel(int64_t nnz, int64_t ne, int ng, const uint32_t* __restrict__ seg,
-                                                      const uint32_t* __restrict__ contrib,
-                                                      const double* __restrict__ F, const double* __restrict__ R,
-                                                      const double* __restrict__ facetK, uint64_t E, int use_facets,
-                                                      double* __restrict__ vals, float* __restrict__ vals32) {
-    extern __shared__ double sR[];
-    for (int k = threadIdx.x; k < ng * L * L; k += blockDim.x) sR[k] = R[k];
-    __syncthreads();
-    int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    if (p >= nnz) return;
-    const uint32_t c0 = seg[p], c1 = seg[p + 1];
-    double acc = 0.0;
-    for (uint32_t c = c0; c < c1; c++) {
-        const uint32_t id = __ldg(contrib + c);
-        if (id < E) {
-            const uint32_t e = id / (L * L), ij = id - e * (L * L);
-            double v = 0.0;
-            for (int g = 0; g < ng; g++) v += __ldg(F + (int64_t)g * ne + e) * sR[g * L * L + ij];
-            acc += v;
-        } else if (use_facets) {
-            acc += __ldg(facetK + (id - E));
+struct TermTab {
+    const int32_t* off;   // per symmetric slot: [mass | stiffness | conv (i,j) | conv (j,i)] offsets
+    const uint8_t* g;
+    const double* coef;
+};
+
+// Element matrices K[e][i][j], one thread per element. The factors F[g] live in shared memory (a
+// private column per thread, so no barrier is needed); every entry is accumulated in a register,
+// the symmetric part once per pair (i <= j), and stored straight to K.
+template <int D, int L>
+__global__ void __launch_bounds__(256) elem_matrix_kernel(int64_t ne, const double* __restrict__ X,
+                                                          const int32_t* __restrict__ conn, FormArgs a, TermTab tt,
+                                                          double* __restrict__ K) {
+    constexpr int NP = D + 1, NS = NP * (NP + 1) / 2, LL = L * L;
+    extern __shared__ double Fs[];
+    const int NTP = blockDim.x + 1, tid = threadIdx.x;
+    const int64_t e = blockIdx.x * (int64_t)blockDim.x + tid;
+    if (e >= ne) return;
+    double* F = Fs + tid;
+    Geo g;
+    double x0[3];
+    element_geo<D>(X, conn, e, g, x0);
+    double gl[NP][3];
+#pragma unroll
+    for (int r = 0; r < D; r++) {
+        double s0 = 0;
+#pragma unroll
+        for (int k = 0; k < D; k++) {
+            gl[k + 1][r] = g.Ji[k][r];
+            s0 += g.Ji[k][r];
+        }
+        gl[0][r] = -s0;
+    }
+    F[0] = a.mass * g.adet;
+    const double sd = a.dt * a.diff * g.adet;
+    int pi = 1;
+#pragma unroll
+    for (int p = 0; p < NP; p++)
+#pragma unroll
+        for (int q = p; q < NP; q++, pi++) {
+            double t = 0;
+#pragma unroll
+            for (int r = 0; r < D; r++) t += gl[p][r] * gl[q][r];
+            F[pi * NTP] = sd * t;
+        }
+    const double sw = -a.dt * g.adet;
+    if (a.wind_kind == OCMP_WIND_CONST) {
+        const double w[3] = {a.w0, a.w1, a.w2};
+#pragma unroll
+        for (int p = 0; p < NP; p++) {
+            double t = 0;
+#pragma unroll
+            for (int r = 0; r < D; r++) t += w[r] * gl[p][r];
+            F[(1 + NS + p) * NTP] = sw * t;
+        }
+    } else if (a.wind_kind == OCMP_WIND_VERTEX) {
+#pragma unroll
+        for (int v = 0; v < NP; v++) {
+            const int32_t gv = conn[e * NP + v];
+            double w[3];
+#pragma unroll
+            for (int r = 0; r < D; r++) w[r] = a.wind_vtx[(int64_t)gv * D + r];
+#pragma unroll
+            for (int p = 0; p < NP; p++) {
+                double t = 0;
+#pragma unroll
+                for (int r = 0; r < D; r++) t += w[r] * gl[p][r];
+                F[(1 + NS + p * NP + v) * NTP] = sw * t;
+            }
         }
     }
-    vals[p] = acc;
-    if (vals32) vals32[p] = (float)acc;
+    const bool um = a.mass != 0.0, us = sd != 0.0, uc = a.wind_kind != OCMP_WIND_NONE;
+    double* __restrict__ Ke = K + e * LL;
+    int slot = 0;
+    for (int i = 0; i < L; i++)
+        for (int j = i; j < L; j++, slot++) {
+            const int o0 = __ldg(tt.off + 4 * slot), o1 = __ldg(tt.off + 4 * slot + 1),
+                      o2 = __ldg(tt.off + 4 * slot + 2), o3 = __ldg(tt.off + 4 * slot + 3),
+                      o4 = __ldg(tt.off + 4 * slot + 4);
+            double sv = 0, cij = 0, cji = 0;
+            if (um)
+                for (int t = o0; t < o1; t++) sv += F[__ldg(tt.g + t) * NTP] * __ldg(tt.coef + t);
+            if (us)
+                for (int t = o1; t < o2; t++) sv += F[__ldg(tt.g + t) * NTP] * __ldg(tt.coef + t);
+            if (uc) {
+                for (int t = o2; t < o3; t++) cij += F[__ldg(tt.g + t) * NTP] * __ldg(tt.coef + t);
+                for (int t = o3; t < o4; t++) cji += F[__ldg(tt.g + t) * NTP] * __ldg(tt.coef + t);
+            }
+            Ke[i * L + j] = sv + cij;
+            if (j != i) Ke[j * L + i] = sv + cji;
+        }
+}
+
+// Row diagonal from the element and facet matrices (for the Jacobi-scaled outputs).
+template <int L>
+__global__ void diag_kernel(int64_t nd, const int32_t* __restrict__ inc_ptr, const int32_t* __restrict__ inc,
+                            const double* __restrict__ K, const uint8_t* __restrict__ freed, int use_facets,
+                            const int32_t* __restrict__ efac_ptr, const int32_t* __restrict__ efac,
+                            const int32_t* __restrict__ ebf_ptr, const int32_t* __restrict__ ebf,
+                            const double* __restrict__ Ki, const double* __restrict__ Kb, double* __restrict__ dinv) {
+    const int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (r >= nd) return;
+    double d = 0;
+    for (int32_t k = inc_ptr[r]; k < inc_ptr[r + 1]; k++) {
+        const int64_t flat = inc[k];
+        const int64_t e = flat / L;
+        const int i = (int)(flat % L);
+        d += K[flat * L + i];
+        if (use_facets) {
+            if (efac_ptr)
+                for (int32_t q = efac_ptr[e]; q < efac_ptr[e + 1]; q++) {
+                    const int f = efac[q], side = f & 1;
+                    const int ri = side * L + i;
+                    d += Ki[(int64_t)(f >> 1) * 4 * L * L + ri * 2 * L + ri];
+                }
+            for (int32_t q = ebf_ptr[e]; q < ebf_ptr[e + 1]; q++) d += Kb[(int64_t)ebf[q] * L * L + i * L + i];
+        }
+    }
+    dinv[r] = (freed[r] && d != 0.0) ? 1.0 / d : 0.0;
+}
+
+// Loads of one element-matrix row slice (L doubles) and its slot bytes: 16-byte vector loads.
+template <int L>
+__device__ __forceinline__ void load_slice(const double* __restrict__ Kr, const uint8_t* __restrict__ sr, double* kv,
+                                           int* sv) {
+    if (L % 2 == 0) {
+#pragma unroll
+        for (int j = 0; j < L; j += 2) {
+            const double2 d = __ldg(reinterpret_cast<const double2*>(Kr + j));
+            kv[j] = d.x;
+            kv[j + 1] = d.y;
+        }
+    } else {
+#pragma unroll
+        for (int j = 0; j < L; j++) kv[j] = __ldg(Kr + j);
+    }
+#pragma unroll
+    for (int c = 0; c < (L + 15) / 16; c++) {
+        const uint4 q = __ldg(reinterpret_cast<const uint4*>(sr + 16 * c));
+        const uint32_t w4[4] = {q.x, q.y, q.z, q.w};
+#pragma unroll
+        for (int j = 16 * c; j < L && j < 16 * c + 16; j++) sv[j] = (w4[(j - 16 * c) >> 2] >> (8 * ((j - 16 * c) & 3))) & 0xff;
+    }
+}
+
+// One thread per CSR row of [r0, r1): gathers the element (and facet) matrix rows into the row
+// via the slot table, in a shared-memory stripe of `stripe` doubles, then writes the row once.
+template <int L>
+__global__ void __launch_bounds__(128) row_scatter_kernel(
+    int64_t r0, int64_t r1, const int32_t* __restrict__ rp, const int32_t* __restrict__ col,
+    const int32_t* __restrict__ inc_ptr, const int32_t* __restrict__ inc, const double* __restrict__ K,
+    const uint8_t* __restrict__ slot, int ss, int use_facets, const int32_t* __restrict__ efac_ptr,
+    const int32_t* __restrict__ efac, const uint8_t* __restrict__ fslot, const int32_t* __restrict__ ebf_ptr,
+    const int32_t* __restrict__ ebf, const double* __restrict__ Ki, const double* __restrict__ Kb,
+    const double* __restrict__ dinv, double* __restrict__ vals, float* __restrict__ vals32,
+    double* __restrict__ svals64, float* __restrict__ svals32) {
+    extern __shared__ double acc[];
+    const int NTP = blockDim.x + 1, tid = threadIdx.x;
+    const int64_t r = r0 + blockIdx.x * (int64_t)blockDim.x + tid;
+    if (r >= r1) return;
+    const int32_t base = rp[r], rn = rp[r + 1] - base;
+    double* __restrict__ ac = acc + tid;
+    for (int q = 0; q < rn; q++) ac[q * NTP] = 0.0;
+    const int32_t k0 = inc_ptr[r], k1 = inc_ptr[r + 1];
+    for (int32_t k = k0; k < k1; k++) {
+        const int64_t flat = inc[k];
+        double kv[L];
+        int sv[L];
+        load_slice<L>(K + flat * L, slot + flat * ss, kv, sv);
+#pragma unroll
+        for (int j = 0; j < L; j++) ac[sv[j] * NTP] += kv[j];
+        if (use_facets) {
+            const int64_t e = flat / L;
+            const int i = (int)(flat % L);
+            if (efac_ptr)
+                for (int32_t q = efac_ptr[e]; q < efac_ptr[e + 1]; q++) {
+                    const int f = efac[q], side = f & 1;
+                    const int64_t fi = f >> 1;
+                    const double* __restrict__ Fr = Ki + fi * 4 * L * L + (int64_t)(side * L + i) * 2 * L;
+                    const uint8_t* __restrict__ fs = fslot + ((fi * 2 + side) * L + i) * 2 * L;
+#pragma unroll
+                    for (int jj = 0; jj < 2 * L; jj++) ac[__ldg(fs + jj) * NTP] += __ldg(Fr + jj);
+                }
+            for (int32_t q = ebf_ptr[e]; q < ebf_ptr[e + 1]; q++) {
+                const double* __restrict__ Br = Kb + (int64_t)ebf[q] * L * L + i * L;
+#pragma unroll
+                for (int j = 0; j < L; j++) ac[sv[j] * NTP] += __ldg(Br + j);
+            }
+        }
+    }
+    for (int q = 0; q < rn; q++) {
+        const double v = ac[q * NTP];
+        vals[base + q] = v;
+        if (vals32) vals32[base + q] = (float)v;
+        if (svals64 || svals32) {
+            const double sv = v * dinv[col[base + q]];
+            if (svals64) svals64[base + q] = sv;
+            if (svals32) svals32[base + q] = (float)sv;
+        }
+    }
 }
 
 // Element right-hand sides: dt (f, phi_i) + mass (u_prev, phi_i) + boundary data.
@@ -455,21 +581,19 @@ __global__ void set_values_kernel(int64_t n, const int32_t* __restrict__ idx, co
     if (k < n) u[idx[k]] = v[k];
 }
 
-// CSR SpMV, TPR threads per row (TPR in {2,4,8,16,32}), FP64 values and accumulation.
-template <int TPR>
+// CSR SpMV y = A x, FP64 values and accumulation (ocmp_spmv).
+template <int TPR, int U>
 __global__ void __launch_bounds__(256) spmv64_kernel(int64_t n, const int32_t* __restrict__ rp,
                                                      const int32_t* __restrict__ col, const double* __restrict__ val,
                                                      const double* __restrict__ x, double* __restrict__ y) {
-    int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    int64_t r = t / TPR;
-    int lane = threadIdx.x % TPR;
-    double acc = 0;
+    const int64_t r = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) / TPR;
+    const int lane = threadIdx.x % TPR;
+    int32_t a = 0, b = 0;
     if (r < n) {
-        int32_t a = rp[r], b = rp[r + 1];
-        for (int32_t k = a + lane; k < b; k += TPR) acc += __ldg(val + k) * __ldg(x + __ldg(col + k));
+        a = __ldg(rp + r);
+        b = __ldg(rp + r + 1);
     }
-#pragma unroll
-    for (int o = TPR / 2; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o, TPR);
+    const double acc = row_dot<double, double, TPR, U>(a, b, col, val, x, lane);
     if (r < n && lane == 0) y[r] = acc;
 }
 
@@ -498,43 +622,53 @@ template <int D, int L>
 int assemble_impl(ocmp_matrix_s* m, const ocmp_form_t* f, cudaStream_t st) {
     ocmp_space_s* s = m->space;
     const ocmp_mesh_s* mesh = s->mesh;
-    const int64_t ne = mesh->ne;
+    const int64_t ne = mesh->ne, nd = s->ndof;
     FormArgs a = make_args(s, f);
-    const int S = D * (D + 1) / 2;
-    int ng = 1 + S;
-    const double* R = s->d_Rc;
-    if (f->wind_kind == OCMP_WIND_CONST) ng += D;
-    if (f->wind_kind == OCMP_WIND_VERTEX) {
-        ng += D * (D + 1);
-        R = s->d_Rv;
-    }
-    elem_factors<D><<<nblk(ne, 128), 128, 0, st>>>(ne, mesh->dX, mesh->dconn, a, s->d_F);
+    constexpr int NP = D + 1, NS = NP * (NP + 1) / 2, NG = 1 + NS + NP * NP, LL = L * L;
+    const int var = f->wind_kind == OCMP_WIND_VERTEX ? 1 : 0;
+    TermTab tt{s->d_slot_off[var], s->d_term_g[var], s->d_term_coef[var]};
+    const int nt = 256;
+    const size_t smem = sizeof(double) * (size_t)NG * (nt + 1);
+    OCMP_CUDA(cudaFuncSetAttribute(elem_matrix_kernel<D, L>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    elem_matrix_kernel<D, L><<<nblk(ne, nt), nt, smem, st>>>(ne, mesh->dX, mesh->dconn, a, tt, s->d_K);
+    // facet matrices
     const bool is_l2 = s->kind == OCMP_L2;
     const bool interior = is_l2 && f->dg && s->nif > 0;
     const uint32_t bmask = f->outflow_mask | f->wn_mask | (is_l2 ? f->nitsche_mask : 0u);
     const bool boundary = bmask != 0 && s->nbf > 0;
     const bool use_facets = interior || boundary;
+    double* Ki = s->d_facetK;
+    double* Kb = s->d_facetK + s->nif * 4 * LL;
     if (use_facets) {
-        double* Ki = s->d_facetK;
-        double* Kb = s->d_facetK + s->nif * 4 * L * L;
         if (is_l2 && s->nif > 0) {
             if (interior)
                 interior_facet_kernel<D, L><<<nblk(s->nif * 2 * L, 128), 128, 0, st>>>(
                     s->nif, mesh->dX, mesh->dconn, s->d_ifac, a, s->T.nfq, s->d_fw, s->d_fphi, s->d_fdphi, s->d_flam, Ki);
             else
-                OCMP_CUDA(cudaMemsetAsync(Ki, 0, sizeof(double) * s->nif * 4 * L * L, st));
+                OCMP_CUDA(cudaMemsetAsync(Ki, 0, sizeof(double) * s->nif * 4 * LL, st));
         }
         if (s->nbf > 0)
             boundary_facet_kernel<D, L><<<nblk(s->nbf * L, 128), 128, 0, st>>>(
                 s->nbf, mesh->dX, mesh->dconn, s->d_bfac, a, is_l2, s->T.nfq, s->d_fw, s->d_fphi, s->d_fdphi,
                 s->d_flam, Kb);
     }
-    const size_t smem = sizeof(double) * ng * L * L;
-    if (smem > 48 * 1024)
-        OCMP_CUDA(cudaFuncSetAttribute(scatter_kernel<L>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    scatter_kernel<L><<<nblk(s->nnz, 256), 256, smem, st>>>(s->nnz, ne, ng, s->d_seg, s->d_contrib, s->d_F, R,
-                                                            s->d_facetK, s->elem_entries, use_facets ? 1 : 0, m->vals,
-                                                            m->vals32);
+    const int32_t* efp = is_l2 ? s->d_efac_ptr : nullptr;
+    if (m->dinv)
+        diag_kernel<L><<<nblk(nd, 256), 256, 0, st>>>(nd, s->d_inc_ptr, s->d_inc, s->d_K, s->d_free, use_facets, efp,
+                                                      s->d_efac, s->d_ebf_ptr, s->d_ebf, Ki, Kb, m->dinv);
+    // rows in ranges of similar length (vertex rows, then the rest) so short rows get small stripes
+    const int rt = 128;
+    OCMP_CUDA(cudaFuncSetAttribute(row_scatter_kernel<L>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   (int)(sizeof(double) * (size_t)s->maxrow * (rt + 1))));
+    for (size_t q = 0; q + 1 < s->row_ranges.size(); q++) {
+        const int64_t r0 = s->row_ranges[q], r1 = s->row_ranges[q + 1];
+        if (r1 <= r0) continue;
+        const size_t rsm = sizeof(double) * (size_t)s->range_maxrow[q] * (rt + 1);
+        row_scatter_kernel<L><<<nblk(r1 - r0, rt), rt, rsm, st>>>(
+            r0, r1, s->d_rowptr, s->d_col, s->d_inc_ptr, s->d_inc, s->d_K, s->d_slot, s->slot_stride, use_facets, efp,
+            s->d_efac, s->d_fslot, s->d_ebf_ptr, s->d_ebf, Ki, Kb, m->dinv, m->vals, m->vals32, m->svals64,
+            m->svals32);
+    }
     OCMP_CUDA(cudaGetLastError());
     return OCMP_OK;
 }
@@ -648,16 +782,14 @@ int launch_set_boundary(ocmp_space_s* s, uint32_t mask, const double* gval, doub
 }
 
 int launch_spmv64(const ocmp_space_s* s, const double* vals, const double* x, double* y, cudaStream_t st) {
-    const double avg = (double)s->nnz / (double)s->ndof;
+    const RowCfg rc = row_cfg(s);
     const int64_t n = s->ndof;
-    if (avg <= 6)
-        spmv64_kernel<2><<<nblk(n * 2, 256), 256, 0, st>>>(n, s->d_rowptr, s->d_col, vals, x, y);
-    else if (avg <= 14)
-        spmv64_kernel<4><<<nblk(n * 4, 256), 256, 0, st>>>(n, s->d_rowptr, s->d_col, vals, x, y);
-    else if (avg <= 40)
-        spmv64_kernel<8><<<nblk(n * 8, 256), 256, 0, st>>>(n, s->d_rowptr, s->d_col, vals, x, y);
-    else
-        spmv64_kernel<16><<<nblk(n * 16, 256), 256, 0, st>>>(n, s->d_rowptr, s->d_col, vals, x, y);
+    const unsigned g = nblk(n * rc.tpr, 256);
+    if (rc.tpr == 2) spmv64_kernel<2, 4><<<g, 256, 0, st>>>(n, s->d_rowptr, s->d_col, vals, x, y);
+    else if (rc.tpr == 4 && rc.u == 4) spmv64_kernel<4, 4><<<g, 256, 0, st>>>(n, s->d_rowptr, s->d_col, vals, x, y);
+    else if (rc.tpr == 4) spmv64_kernel<4, 8><<<g, 256, 0, st>>>(n, s->d_rowptr, s->d_col, vals, x, y);
+    else if (rc.tpr == 8) spmv64_kernel<8, 8><<<g, 256, 0, st>>>(n, s->d_rowptr, s->d_col, vals, x, y);
+    else spmv64_kernel<16, 8><<<g, 256, 0, st>>>(n, s->d_rowptr, s->d_col, vals, x, y);
     OCMP_CUDA(cudaGetLastError());
     return OCMP_OK;
 }

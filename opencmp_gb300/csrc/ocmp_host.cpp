@@ -178,6 +178,172 @@ static int simplex_rule(int D, int n, std::vector<double>& pts, std::vector<doub
     return (int)wts.size();
 }
 
+// Basis as polynomials in independent barycentric variables: values and d/d lam_a (a = 0..D).
+// Every function of both spaces is such a polynomial, so grad phi = sum_a dphi/dlam_a grad lam_a.
+struct DL {
+    double v, d[4];
+};
+static DL lc(double c) { return DL{c, {0, 0, 0, 0}}; }
+static DL operator+(DL a, DL b) {
+    DL r{a.v + b.v, {}};
+    for (int k = 0; k < 4; k++) r.d[k] = a.d[k] + b.d[k];
+    return r;
+}
+static DL operator-(DL a, DL b) {
+    DL r{a.v - b.v, {}};
+    for (int k = 0; k < 4; k++) r.d[k] = a.d[k] - b.d[k];
+    return r;
+}
+static DL operator*(DL a, double s) {
+    DL r{a.v * s, {}};
+    for (int k = 0; k < 4; k++) r.d[k] = a.d[k] * s;
+    return r;
+}
+static DL operator*(DL a, DL b) {
+    DL r{a.v * b.v, {}};
+    for (int k = 0; k < 4; k++) r.d[k] = a.d[k] * b.v + a.v * b.d[k];
+    return r;
+}
+static void sleg_l(int n, DL x, DL t, DL* out) {
+    out[0] = lc(1);
+    if (n >= 1) out[1] = x;
+    DL t2 = t * t;
+    for (int k = 1; k < n; k++) out[k + 1] = ((x * out[k]) * (2.0 * k + 1) - (t2 * out[k - 1]) * (double)k) * (1.0 / (k + 1));
+}
+static void jac_l(int n, double a, DL s, DL* out) {
+    out[0] = lc(1);
+    if (n >= 1) out[1] = (s * (a + 2) + lc(a)) * 0.5;
+    for (int k = 2; k <= n; k++) {
+        double A = 2.0 * k * (k + a) * (2.0 * k + a - 2);
+        double B = 2.0 * k + a - 1;
+        double C1 = (2.0 * k + a) * (2.0 * k + a - 2), C0 = a * a;
+        double Dd = 2.0 * (k + a - 1) * (k - 1) * (2.0 * k + a);
+        out[k] = (((s * C1 + lc(C0)) * out[k - 1]) * B - out[k - 2] * Dd) * (1.0 / A);
+    }
+}
+static int basis_lam(int kind, int D, int p, const double* lamv, DL* out) {
+    DL lam[4];
+    for (int a = 0; a <= D; a++) {
+        lam[a] = lc(lamv[a]);
+        lam[a].d[a] = 1;
+    }
+    int c = 0;
+    if (kind == OCMP_H1) {
+        for (int v = 0; v <= D; v++) out[c++] = lam[v];
+        if (p >= 2)
+            for (int a = 0; a <= D; a++)
+                for (int b = a + 1; b <= D; b++) {
+                    DL L[4];
+                    sleg_l(p - 2, lam[b] - lam[a], lam[a] + lam[b], L);
+                    DL base = lam[a] * lam[b];
+                    for (int k = 0; k <= p - 2; k++) out[c++] = base * L[k];
+                }
+        if (p >= 3)
+            for (int a = 0; a <= D; a++)
+                for (int b = a + 1; b <= D; b++)
+                    for (int cc = b + 1; cc <= D; cc++) out[c++] = lam[a] * lam[b] * lam[cc];
+    } else {
+        DL L[8];
+        sleg_l(p, lam[1] - lam[0], lam[0] + lam[1], L);
+        for (int i = 0; i <= p; i++) {
+            DL P[8];
+            jac_l(p - i, 2.0 * i + 1, lam[2] * 2.0 - lc(1), P);
+            for (int j = 0; j <= p - i; j++) out[c++] = L[i] * P[j];
+        }
+    }
+    return c;
+}
+
+// Element-matrix terms. With G_ab = grad lam_a . grad lam_b and wt_a = w . grad lam_a:
+//   mass       K_ij  = (mass |det J|)              * int phi_i phi_j
+//   stiffness  K_ij += (dt diff |det J| G_ab)       * int (d_a phi_i d_b phi_j + d_b phi_i d_a phi_j) / (1 + [a==b])
+//   convection K_ij += (-dt |det J| wt_a)           * int d_a phi_i phi_j          (constant wind)
+//              K_ij += (-dt |det J| w_v . grad lam_a) * int lam_v d_a phi_i phi_j  (per-vertex wind)
+// Integrals over the reference simplex (exact rule); symmetric parts are kept for i <= j only.
+// Terms below 1e-14 of their group's largest are dropped: for the hierarchical P2 tetrahedron the
+// element matrix takes 510 products instead of 1000 for dense Cartesian reference tensors.
+static void build_terms(int kind, int D, int p, ocmp_tables& T) {
+    const int L = T.nloc, NP = D + 1, NS = NP * (NP + 1) / 2;
+    T.nsym = L * (L + 1) / 2;
+    auto sym = [&](int i, int j) { return i * L - i * (i - 1) / 2 + (j - i); };
+    std::vector<double> msum((size_t)L * L, 0.0), ssum((size_t)NS * L * L, 0.0), csum((size_t)NP * L * L, 0.0),
+        vsum((size_t)NP * NP * L * L, 0.0);
+    DL b[kMaxLoc];
+    for (int q = 0; q < T.nq; q++) {
+        double lam[4] = {1, 0, 0, 0};
+        for (int k = 0; k < D; k++) {
+            lam[k + 1] = T.qxi[q * D + k];
+            lam[0] -= lam[k + 1];
+        }
+        basis_lam(kind, D, p, lam, b);
+        const double w = T.qw[q];
+        for (int i = 0; i < L; i++)
+            for (int j = 0; j < L; j++) {
+                msum[i * L + j] += w * b[i].v * b[j].v;
+                int pi = 0;
+                for (int a = 0; a < NP; a++)
+                    for (int c = a; c < NP; c++, pi++) {
+                        double t = b[i].d[a] * b[j].d[c];
+                        if (a != c) t += b[i].d[c] * b[j].d[a];
+                        ssum[((size_t)pi * L + i) * L + j] += w * t;
+                    }
+                for (int a = 0; a < NP; a++) {
+                    csum[((size_t)a * L + i) * L + j] += w * b[i].d[a] * b[j].v;
+                    for (int v = 0; v < NP; v++)
+                        vsum[(((size_t)a * NP + v) * L + i) * L + j] += w * lam[v] * b[i].d[a] * b[j].v;
+                }
+            }
+    }
+    const double mmax = *std::max_element(msum.begin(), msum.end(), [](double x, double y) { return std::fabs(x) < std::fabs(y); });
+    auto absmax = [](const std::vector<double>& v) {
+        double m = 0;
+        for (double x : v) m = std::max(m, std::fabs(x));
+        return m;
+    };
+    const double tol_m = 1e-14 * std::fabs(mmax), tol_s = 1e-14 * absmax(ssum), tol_c = 1e-14 * absmax(csum),
+                 tol_v = 1e-14 * absmax(vsum);
+    for (int var = 0; var < 2; var++) {
+        auto& off = T.slot_off[var];
+        auto& tg = T.term_g[var];
+        auto& tc = T.term_coef[var];
+        off.clear();
+        tg.clear();
+        tc.clear();
+        auto conv = [&](int i, int j) {
+            if (var == 0) {
+                for (int a = 0; a < NP; a++) {
+                    const double v = csum[((size_t)a * L + i) * L + j];
+                    if (std::fabs(v) > tol_c) { tg.push_back((uint8_t)(1 + NS + a)); tc.push_back(v); }
+                }
+            } else {
+                for (int a = 0; a < NP; a++)
+                    for (int vv = 0; vv < NP; vv++) {
+                        const double v = vsum[(((size_t)a * NP + vv) * L + i) * L + j];
+                        if (std::fabs(v) > tol_v) { tg.push_back((uint8_t)(1 + NS + a * NP + vv)); tc.push_back(v); }
+                    }
+            }
+        };
+        for (int i = 0; i < L; i++)
+            for (int j = i; j < L; j++) {
+                off.push_back((int32_t)tc.size());
+                const double mv = msum[i * L + j];
+                if (std::fabs(mv) > tol_m) { tg.push_back(0); tc.push_back(mv); }
+                off.push_back((int32_t)tc.size());
+                for (int f = 0; f < NS; f++) {
+                    const double v = ssum[((size_t)f * L + i) * L + j];
+                    if (std::fabs(v) > tol_s) { tg.push_back((uint8_t)(1 + f)); tc.push_back(v); }
+                }
+                off.push_back((int32_t)tc.size());
+                conv(i, j);
+                off.push_back((int32_t)tc.size());
+                if (j != i) conv(j, i);
+            }
+        off.push_back((int32_t)tc.size());
+        T.nterms[var] = (int)tc.size();
+    }
+    (void)sym;
+}
+
 static void build_tables(int kind, int D, int p, ocmp_tables& T) {
     int L = nloc_of(kind, D, p);
     T.nloc = L;
@@ -323,10 +489,13 @@ int ocmp_mesh_destroy(ocmp_mesh_t m) {
 }
 
 static void free_space_device(ocmp_space_s* s) {
-    void* ps[] = {s->d_dofs, s->d_rowptr, s->d_col,  s->d_free, s->d_diag, s->d_seg,  s->d_contrib, s->d_inc_ptr,
-                  s->d_inc,  s->d_ifac,   s->d_bfac, s->d_ebf_ptr, s->d_ebf, s->d_Rc, s->d_Rv,      s->d_qw,
-                  s->d_qphi, s->d_mvec,   s->d_fw,   s->d_fphi, s->d_fdphi, s->d_flam, s->d_F,      s->d_facetK,
-                  s->d_Fe};
+    void* ps[] = {s->d_dofs,     s->d_rowptr,   s->d_col,       s->d_free,     s->d_diag,      s->d_slot,
+                  s->d_fslot,    s->d_efac_ptr, s->d_efac,      s->d_slot_off[0], s->d_term_g[0], s->d_term_coef[0],
+                  s->d_slot_off[1], s->d_term_g[1], s->d_term_coef[1],
+                  s->d_inc_ptr,  s->d_inc,      s->d_ifac,      s->d_bfac,     s->d_ebf_ptr,   s->d_ebf,
+                  s->d_Rc,       s->d_Rv,       s->d_qw,        s->d_qphi,     s->d_mvec,      s->d_fw,
+                  s->d_fphi,     s->d_fdphi,    s->d_flam,      s->d_K,        s->d_facetK,    s->d_Fe,
+                  s->d_lift_ptr, s->d_lift_pos};
     for (void* p : ps) dfree(p);
 }
 
@@ -346,6 +515,7 @@ int ocmp_space_create(ocmp_mesh_t mesh, int32_t kind, int32_t order, uint32_t di
     const int64_t ne = mesh->ne, nv = mesh->nv;
     const int32_t* conn = mesh->conn.data();
     build_tables(kind, D, p, s->T);
+    build_terms(kind, D, p, s->T);
 
     // ---- dof map
     s->dofs.resize((size_t)ne * L);
@@ -536,82 +706,82 @@ int ocmp_space_create(ocmp_mesh_t mesh, int32_t kind, int32_t order, uint32_t di
     });
     std::vector<std::vector<int32_t>>().swap(rows);
 
-    // ---- sorted scatter plan: for each CSR entry, the local-matrix entries that sum into it.
-    // Contribution index space: [0, ne L^2) element entries e*L^2 + i*L + j; then interior facet
-    // entries (2L x 2L per facet); then boundary facet entries (L x L per facet).
-    const uint64_t E = (uint64_t)ne * L * L;
-    const uint64_t FI = E, FB = E + (uint64_t)s->nif * 4 * L * L;
-    const uint64_t total_space = FB + (uint64_t)s->nbf * L * L;
-    s->elem_entries = E;
-    if (total_space >= ((uint64_t)1 << 32)) {
-        delete s;
-        return fail(OCMP_ERR_ARG, "ocmp_space_create: local-matrix entries exceed 32-bit plan indices");
+    // ---- slot tables: for element e and local row i, the position within CSR row dof(e,i) of
+    // each column dof(e,j); the same for the 2L columns of every interior-facet matrix row (L2).
+    for (int64_t r = 0; r < nd; r++) s->maxrow = std::max<int>(s->maxrow, (int)(rl[r + 1] - rl[r]));
+    s->row_ranges = {0};
+    if (kind == OCMP_H1 && p >= 2 && nv < nd) s->row_ranges.push_back(nv);
+    s->row_ranges.push_back(nd);
+    for (size_t q = 0; q + 1 < s->row_ranges.size(); q++) {
+        int mx = 0;
+        for (int64_t r = s->row_ranges[q]; r < s->row_ranges[q + 1]; r++) mx = std::max<int>(mx, (int)(rl[r + 1] - rl[r]));
+        s->range_maxrow.push_back(mx);
     }
-    std::vector<int64_t> rc(nd + 1, 0);
-    auto row_contribs = [&](int64_t r, std::vector<std::pair<int32_t, uint32_t>>& out) {
-        out.clear();
-        const int32_t* c0 = s->col.data() + rl[r];
-        const int64_t rn = rl[r + 1] - rl[r];
-        auto pos_of = [&](int32_t dof) { return (int32_t)(std::lower_bound(c0, c0 + rn, dof) - c0); };
-        for (int32_t k = inc_ptr[r]; k < inc_ptr[r + 1]; k++) {
-            int64_t e = inc[k] / L;
-            int i = inc[k] % L;
-            for (int j = 0; j < L; j++)
-                out.push_back({pos_of(s->dofs[e * L + j]), (uint32_t)(e * L * L + i * L + j)});
-            if (dgj)
-                for (int f = 0; f < nvp; f++) {
-                    int32_t fi = enb[e * nvp + f];
-                    if (fi < 0) continue;
-                    bool left = s->ifac[4 * fi] == e;
-                    int ri = left ? i : L + i;
-                    int64_t eL = s->ifac[4 * fi], eR = s->ifac[4 * fi + 2];
-                    for (int j = 0; j < 2 * L; j++) {
-                        int32_t cd = j < L ? s->dofs[eL * L + j] : s->dofs[eR * L + j - L];
-                        out.push_back({pos_of(cd), (uint32_t)(FI + (uint64_t)fi * 4 * L * L + ri * 2 * L + j)});
+    if (s->maxrow > 255) {
+        delete s;
+        return fail(OCMP_ERR_UNSUPPORTED, "ocmp_space_create: a CSR row exceeds 255 entries");
+    }
+    const int64_t LL = (int64_t)L * L;
+    const int SS = s->slot_stride = (L + 15) / 16 * 16;   // one 16-byte load per slice for L <= 16
+    std::vector<uint8_t> slot((size_t)(ne * L * SS), 0);
+    parallel_for(ne, [&](int64_t a0, int64_t b0) {
+        for (int64_t e = a0; e < b0; e++)
+            for (int i = 0; i < L; i++) {
+                const int32_t r = s->dofs[e * L + i];
+                const int32_t* c0 = s->col.data() + rl[r];
+                const int64_t rn = rl[r + 1] - rl[r];
+                for (int j = 0; j < L; j++)
+                    slot[(e * L + i) * SS + j] = (uint8_t)(std::lower_bound(c0, c0 + rn, s->dofs[e * L + j]) - c0);
+            }
+    });
+    std::vector<uint8_t> fslot;
+    std::vector<int32_t> efac_ptr(ne + 1, 0), efac;
+    if (dgj) {
+        fslot.resize((size_t)s->nif * 4 * LL);
+        parallel_for(s->nif, [&](int64_t a0, int64_t b0) {
+            for (int64_t fi = a0; fi < b0; fi++) {
+                const int64_t eL = s->ifac[4 * fi], eR = s->ifac[4 * fi + 2];
+                for (int side = 0; side < 2; side++) {
+                    const int64_t e = side ? eR : eL;
+                    for (int i = 0; i < L; i++) {
+                        const int32_t r = s->dofs[e * L + i];
+                        const int32_t* c0 = s->col.data() + rl[r];
+                        const int64_t rn = rl[r + 1] - rl[r];
+                        for (int jj = 0; jj < 2 * L; jj++) {
+                            const int32_t cd = jj < L ? s->dofs[eL * L + jj] : s->dofs[eR * L + jj - L];
+                            fslot[((fi * 2 + side) * L + i) * 2 * L + jj] =
+                                (uint8_t)(std::lower_bound(c0, c0 + rn, cd) - c0);
+                        }
                     }
                 }
-            for (int32_t q = ebf_ptr[e]; q < ebf_ptr[e + 1]; q++) {
-                int32_t bf = ebf[q];
-                for (int j = 0; j < L; j++)
-                    out.push_back({pos_of(s->dofs[e * L + j]), (uint32_t)(FB + (uint64_t)bf * L * L + i * L + j)});
             }
+        });
+        for (int64_t fi = 0; fi < s->nif; fi++) {
+            efac_ptr[s->ifac[4 * fi] + 1]++;
+            efac_ptr[s->ifac[4 * fi + 2] + 1]++;
         }
-        std::sort(out.begin(), out.end());
-    };
-    parallel_for(nd, [&](int64_t a, int64_t b) {
-        std::vector<std::pair<int32_t, uint32_t>> tmp;
-        for (int64_t r = a; r < b; r++) {
-            row_contribs(r, tmp);
-            rc[r + 1] = (int64_t)tmp.size();
+        for (int64_t e = 0; e < ne; e++) efac_ptr[e + 1] += efac_ptr[e];
+        efac.resize(efac_ptr[ne]);
+        std::vector<int32_t> fill(efac_ptr.begin(), efac_ptr.end() - 1);
+        for (int64_t fi = 0; fi < s->nif; fi++) {
+            efac[fill[s->ifac[4 * fi]]++] = (int32_t)(fi * 2);
+            efac[fill[s->ifac[4 * fi + 2]]++] = (int32_t)(fi * 2 + 1);
         }
-    });
-    for (int64_t r = 0; r < nd; r++) rc[r + 1] += rc[r];
-    s->ncontrib = rc[nd];
-    if (s->ncontrib >= ((int64_t)1 << 32)) {
-        delete s;
-        return fail(OCMP_ERR_ARG, "ocmp_space_create: scatter plan exceeds 32-bit offsets");
     }
-    std::vector<uint32_t> seg(s->nnz + 1), contrib(s->ncontrib);
+    s->ncontrib = ne * LL + s->nif * 4 * LL + s->nbf * LL;
     std::vector<int32_t> diag(nd);
-    parallel_for(nd, [&](int64_t a, int64_t b) {
-        std::vector<std::pair<int32_t, uint32_t>> tmp;
-        for (int64_t r = a; r < b; r++) {
-            row_contribs(r, tmp);
-            int64_t base = rc[r];
-            int64_t rn = rl[r + 1] - rl[r];
-            size_t t = 0;
-            for (int64_t k = 0; k < rn; k++) {
-                seg[rl[r] + k] = (uint32_t)(base + (int64_t)t);
-                while (t < tmp.size() && tmp[t].first == k) {
-                    contrib[base + t] = tmp[t].second;
-                    t++;
-                }
-            }
-            const int32_t* c0 = s->col.data() + rl[r];
-            diag[r] = (int32_t)(rl[r] + (std::lower_bound(c0, c0 + rn, (int32_t)r) - c0));
-        }
-    });
-    seg[s->nnz] = (uint32_t)s->ncontrib;
+    for (int64_t r = 0; r < nd; r++) {
+        const int32_t* c0 = s->col.data() + rl[r];
+        diag[r] = (int32_t)(rl[r] + (std::lower_bound(c0, c0 + (rl[r + 1] - rl[r]), (int32_t)r) - c0));
+    }
+    // lift list: entries of free rows in constrained columns (the Dirichlet lift A_fD x_D)
+    std::vector<int32_t> lift_ptr(nd + 1, 0), lift_pos;
+    for (int64_t r = 0; r < nd; r++) {
+        if (s->freed[r])
+            for (int64_t k = rl[r]; k < rl[r + 1]; k++)
+                if (!s->freed[s->col[k]]) lift_pos.push_back((int32_t)k);
+        lift_ptr[r + 1] = (int32_t)lift_pos.size();
+    }
 
     // ---- upload
     std::vector<int32_t> rp32(nd + 1);
@@ -625,14 +795,23 @@ int ocmp_space_create(ocmp_mesh_t mesh, int32_t kind, int32_t order, uint32_t di
     U(&s->d_col, s->col);
     U(&s->d_free, s->freed);
     U(&s->d_diag, diag);
-    U(&s->d_seg, seg);
-    U(&s->d_contrib, contrib);
+    U(&s->d_slot, slot);
+    U(&s->d_fslot, fslot);
+    U(&s->d_efac_ptr, efac_ptr);
+    U(&s->d_efac, efac);
+    for (int var = 0; var < 2; var++) {
+        U(&s->d_slot_off[var], s->T.slot_off[var]);
+        U(&s->d_term_g[var], s->T.term_g[var]);
+        U(&s->d_term_coef[var], s->T.term_coef[var]);
+    }
     U(&s->d_inc_ptr, inc_ptr);
     U(&s->d_inc, inc);
     U(&s->d_ifac, s->ifac);
     U(&s->d_bfac, s->bfac);
     U(&s->d_ebf_ptr, ebf_ptr);
     U(&s->d_ebf, ebf);
+    U(&s->d_lift_ptr, lift_ptr);
+    U(&s->d_lift_pos, lift_pos);
     U(&s->d_Rc, s->T.R_const);
     U(&s->d_Rv, s->T.R_vtx);
     U(&s->d_qw, s->T.qw);
@@ -642,8 +821,8 @@ int ocmp_space_create(ocmp_mesh_t mesh, int32_t kind, int32_t order, uint32_t di
     U(&s->d_fphi, s->T.fphi);
     U(&s->d_fdphi, s->T.fdphi);
     U(&s->d_flam, s->T.flam);
-    if (!st) st = dalloc(&s->d_F, (size_t)kMaxNg * ne);
-    if (!st) st = dalloc(&s->d_facetK, (size_t)(total_space - E));
+    if (!st) st = dalloc(&s->d_K, (size_t)(ne * LL));
+    if (!st) st = dalloc(&s->d_facetK, (size_t)(s->nif * 4 * LL + s->nbf * LL));
     if (!st) st = dalloc(&s->d_Fe, (size_t)ne * L);
     if (st) {
         free_space_device(s);
@@ -720,16 +899,23 @@ int ocmp_set_boundary(ocmp_space_t s, uint32_t mask, const double* gval, double*
     return launch_set_boundary(s, mask, gval, u, (cudaStream_t)stream);
 }
 
-int ocmp_matrix_create(ocmp_space_t s, int32_t want_fp32, ocmp_matrix_t* out) {
+int ocmp_matrix_create(ocmp_space_t s, int32_t flags, ocmp_matrix_t* out) {
     if (!s || !out) return fail(OCMP_ERR_ARG, "ocmp_matrix_create: null argument");
     auto* m = new ocmp_matrix_s();
     m->space = s;
+    m->flags = flags;
     int st = dalloc(&m->vals, (size_t)s->nnz);
-    if (!st && want_fp32) st = dalloc(&m->vals32, (size_t)s->nnz);
+    if (!st && (flags & OCMP_MAT_FP32)) st = dalloc(&m->vals32, (size_t)s->nnz);
+    if (!st && (flags & OCMP_MAT_JACOBI64)) st = dalloc(&m->svals64, (size_t)s->nnz);
+    if (!st && (flags & OCMP_MAT_JACOBI32)) st = dalloc(&m->svals32, (size_t)s->nnz);
+    if (!st && (flags & (OCMP_MAT_JACOBI64 | OCMP_MAT_JACOBI32))) st = dalloc(&m->dinv, (size_t)s->ndof);
     if (!st) st = cudaMemset(m->vals, 0, sizeof(double) * s->nnz) == cudaSuccess ? 0 : OCMP_ERR_CUDA;
     if (st) {
         dfree(m->vals);
         dfree(m->vals32);
+        dfree(m->svals64);
+        dfree(m->svals32);
+        dfree(m->dinv);
         delete m;
         return st;
     }
@@ -741,6 +927,9 @@ int ocmp_matrix_destroy(ocmp_matrix_t m) {
     if (!m) return OCMP_OK;
     dfree(m->vals);
     dfree(m->vals32);
+    dfree(m->svals64);
+    dfree(m->svals32);
+    dfree(m->dinv);
     delete m;
     return OCMP_OK;
 }
@@ -749,6 +938,14 @@ int ocmp_matrix_values(ocmp_matrix_t m, double** v64, float** v32) {
     if (!m) return fail(OCMP_ERR_ARG, "ocmp_matrix_values: null argument");
     if (v64) *v64 = m->vals;
     if (v32) *v32 = m->vals32;
+    return OCMP_OK;
+}
+
+int ocmp_matrix_scaled_values(ocmp_matrix_t m, double** s64, float** s32, double** dinv) {
+    if (!m) return fail(OCMP_ERR_ARG, "ocmp_matrix_scaled_values: null argument");
+    if (s64) *s64 = m->svals64;
+    if (s32) *s32 = m->svals32;
+    if (dinv) *dinv = m->dinv;
     return OCMP_OK;
 }
 

@@ -12,7 +12,7 @@
 namespace ocmp {
 
 constexpr int kMaxLoc = 20;     // largest nloc built: H1 order 3 on tetrahedra
-constexpr int kMaxNg = 19;      // volume factors: 1 mass + 6 stiffness + 12 per-vertex wind (3D)
+constexpr int kMaxNg = 27;      // element factors: 1 mass + 10 stiffness + 16 per-vertex wind (3D)
 constexpr int kMaxFq = 25;      // facet quadrature points
 
 void set_error(const std::string& msg);
@@ -68,6 +68,15 @@ struct ocmp_tables {
     std::vector<double> fphi;       // (dim+1) * nfq * nloc       basis values on local facet f
     std::vector<double> fdphi;      // (dim+1) * nfq * nloc * dim reference gradients on local facet f
     std::vector<double> flam;       // (dim+1) * nfq * (dim+1)    barycentrics on local facet f
+    // Sparse element-matrix terms in barycentric form (build_terms in ocmp_host.cpp), organised by
+    // symmetric slot (i <= j): per slot, offsets into the term arrays of [mass | stiffness |
+    // convection (i,j) | convection (j,i)]; one table for a constant wind, one for a per-vertex wind
+    // (they differ only in the convection terms). K_ij = sym + conv_ij, K_ji = sym + conv_ji.
+    int nsym = 0;
+    std::vector<int32_t> slot_off[2];   // [wind variant] nsym * 5 offsets (+1 sentinel)
+    std::vector<uint8_t> term_g[2];
+    std::vector<double> term_coef[2];
+    int nterms[2] = {0, 0};
 };
 
 struct ocmp_space_s {
@@ -88,14 +97,25 @@ struct ocmp_space_s {
     int32_t* d_col = nullptr;
     uint8_t* d_free = nullptr;
     int32_t* d_diag = nullptr;      // ndof: position of the diagonal entry in each row
-    uint32_t* d_seg = nullptr;      // nnz+1: segment start of each CSR entry in d_contrib
-    uint32_t* d_contrib = nullptr;  // ncontrib: local-matrix entry feeding that CSR entry
+    uint8_t* d_slot = nullptr;      // ne*nloc*slot_stride: column slot of dof(e,j) in row dof(e,i)
+    uint8_t* d_fslot = nullptr;     // nif*2*nloc*2nloc: column slots of interior-facet matrix rows
+    int32_t* d_efac_ptr = nullptr;  // ne+1: element -> interior facets (L2)
+    int32_t* d_efac = nullptr;      // facet*2 + side
+    int32_t* d_slot_off[2] = {nullptr, nullptr};
+    uint8_t* d_term_g[2] = {nullptr, nullptr};
+    double* d_term_coef[2] = {nullptr, nullptr};
+    int slot_stride = 0;            // bytes per (element, local row) in d_slot (nloc rounded to 16)
+    int maxrow = 0;                 // longest CSR row
+    std::vector<int64_t> row_ranges;  // row ranges of similar length (vertex rows, the rest)
+    std::vector<int> range_maxrow;
     int32_t* d_inc_ptr = nullptr;   // ndof+1: dof -> (element, local) incidence
     int32_t* d_inc = nullptr;       // ne*nloc: e*nloc + i
     int32_t* d_ifac = nullptr;
     int32_t* d_bfac = nullptr;
     int32_t* d_ebf_ptr = nullptr;   // ne+1: element -> boundary facets
     int32_t* d_ebf = nullptr;
+    int32_t* d_lift_ptr = nullptr;  // ndof+1: per free row, CSR positions whose column is constrained
+    int32_t* d_lift_pos = nullptr;
     double* d_Rc = nullptr;         // R_const
     double* d_Rv = nullptr;         // R_vtx
     double* d_qw = nullptr;
@@ -106,16 +126,22 @@ struct ocmp_space_s {
     double* d_fdphi = nullptr;
     double* d_flam = nullptr;
     // scratch owned by the space
-    double* d_F = nullptr;          // kMaxNg * ne element factors
+    double* d_K = nullptr;          // ne*nloc^2 element matrices
     double* d_facetK = nullptr;     // nif*(2 nloc)^2 + nbf*nloc^2 facet matrices
     double* d_Fe = nullptr;         // ne*nloc element right-hand sides
-    uint64_t elem_entries = 0;      // ne * nloc^2: contributions below this index are volume entries
 };
 
+// Matrix outputs selected at creation (ocmp_matrix_create's flags): the FP64 values always; an FP32
+// copy; the point-Jacobi right-scaled values A D^-1 in FP64 and/or FP32 (the Krylov matrices of
+// the GMRES path) with D^-1 itself. The scaled outputs are written by the same assembly pass.
 struct ocmp_matrix_s {
     ocmp_space_s* space = nullptr;
+    int flags = 0;
     double* vals = nullptr;
     float* vals32 = nullptr;
+    double* svals64 = nullptr;
+    float* svals32 = nullptr;
+    double* dinv = nullptr;
 };
 
 namespace ocmp {

@@ -20,6 +20,7 @@
 #include <string>
 
 #include "ocmp_internal.h"
+#include "ocmp_spmv.cuh"
 
 struct ocmp_solver_s {
     ocmp_matrix_s* mat = nullptr;
@@ -53,6 +54,15 @@ struct ocmp_solver_s {
     double* H = nullptr;        // (m+1) x m
     int* flags = nullptr;       // device flags
     int* hflags = nullptr;      // pinned host mirror
+    // fused GMRES
+    double* As64 = nullptr;     // A D^-1 (Jacobi folded) or A, FP64 Krylov matrix (owned)
+    float* As32 = nullptr;      // same in FP32 (OCMP_MIXED)
+    const double* K64 = nullptr;  // Krylov matrix in use: As64, or the matrix's own scaled values
+    const float* K32 = nullptr;
+    bool borrow = false;        // Jacobi-scaled values and D^-1 come from the assembly
+    double* scale = nullptr;    // basis scales: v_k = scale[k] * V[k]
+    unsigned* cnt = nullptr;    // last-block counters (zero between launches)
+    int grid = 0;               // persistent grid of the fused kernels
 };
 
 namespace ocmp {
@@ -568,97 +578,7 @@ int read_flags(const Ctx& c) {
     return OCMP_OK;
 }
 
-// One GMRES(m) solve on vectors of type T (double: the FP64 solve; float: the inner solve of
-// OCMP_MIXED). Solves A z = r0 where r0 is the (free-masked) residual already stored in V[0..n)
-// unnormalised with |r0|^2 in red[0]; accumulates the correction into xacc.
-template <class T, class TM, class TX>
-int gmres_core(const Ctx& c, const TM* vals, const T* dinv, const T* Binv, T* V, T* w, T* z, TX* xacc,
-               const double* b64, const double* x64, int maxit, double tol, int* iters_out, bool outer64) {
-    ocmp_solver_s* sv = c.sv;
-    const int64_t n = sv->n;
-    const int m = sv->m;
-    double* H = sv->H;
-    double* csg = sv->H + (size_t)(m + 1) * m;  // cs, sn, g
-    double* y = csg + 3 * m + 1;
-    const bool block = sv->prm.precond == OCMP_PRE_BLOCK_JACOBI && Binv;
-    const T* djac = (sv->prm.precond == OCMP_PRE_JACOBI) ? dinv : nullptr;
-    int iters = 0;
-    set_state<<<1, 1, 0, c.st>>>(sv->st, S_TOL, tol);
-    OCMP_CUDA(cudaMemsetAsync(sv->flags, 0, sizeof(int) * F_NFLAG, c.st));
-    bool first = true;
-    while (true) {
-        if (!first) {
-            // recompute the residual of the current iterate for the restart
-            if (outer64) {
-                residual64(c, b64, x64, (double*)V);
-            } else {
-                // inner: residual of the correction system A d = r0 is not needed for restarts of
-                // the FP32 solve; it is rebuilt by the outer refinement instead
-                break;
-            }
-        }
-        first = false;
-        cycle_start<<<1, 1, 0, c.st>>>(sv->red, sv->st, sv->flags, csg, m);
-        if (read_flags(c)) return OCMP_ERR_CUDA;
-        if (sv->hflags[F_CONV] || iters >= maxit) break;
-        // w := r0 for the j = 0 scaling
-        OCMP_CUDA(cudaMemcpyAsync(w, V, sizeof(T) * n, cudaMemcpyDeviceToDevice, c.st));
-        int j = 0;
-        for (; j < m && iters < maxit; j++) {
-            T* vj = V + (int64_t)j * n;
-            scale_prec<T><<<c.grid, kThreads, 0, c.st>>>(n, w, sv->st, vj, djac, z, sv->flags);
-            if (block) launch_block_prec<T>(c, Binv, vj, z, sv->flags);
-            launch_spmv_masked<TM, T>(c, vals, (djac || block) ? z : vj, w, nullptr, sv->flags);
-            const int nch = j / 8 + 1;
-            dim3 g2(sv->nb, nch);
-            mdot_kernel<T><<<g2, kThreads, 0, c.st>>>(n, j, V, w, sv->part, sv->nb, sv->flags, -1);
-            reduce_kernel<<<j + 2, kThreads, 0, c.st>>>(sv->nb, j + 2, sv->part, sv->red, nullptr, -1);
-            reorth_check<<<1, 1, 0, c.st>>>(sv->red, j, sv->st, sv->flags);
-            axpy_norm_kernel<T><<<sv->nb, kThreads, 0, c.st>>>(n, j, V, sv->red, w, sv->part + (size_t)(m + 2) * sv->nb,
-                                                               sv->flags, -1);
-            reduce_kernel<<<1, kThreads, 0, c.st>>>(sv->nb, 1, sv->part + (size_t)(m + 2) * sv->nb,
-                                                    sv->red + (m + 2), nullptr, -1);
-            reorth_decide<<<1, 1, 0, c.st>>>(sv->red + (m + 2), sv->st, sv->flags);
-            // gated second pass
-            mdot_kernel<T><<<g2, kThreads, 0, c.st>>>(n, j, V, w, sv->part + (size_t)(m + 3) * sv->nb, sv->nb,
-                                                      sv->flags, F_REORTH);
-            reduce_kernel<<<j + 1, kThreads, 0, c.st>>>(sv->nb, j + 1, sv->part + (size_t)(m + 3) * sv->nb,
-                                                        sv->red + (m + 3), sv->flags, F_REORTH);
-            axpy_norm_kernel<T><<<sv->nb, kThreads, 0, c.st>>>(n, j, V, sv->red + (m + 3), w,
-                                                               sv->part + (size_t)(m + 2) * sv->nb, sv->flags,
-                                                               F_REORTH);
-            reduce_kernel<<<1, kThreads, 0, c.st>>>(sv->nb, 1, sv->part + (size_t)(m + 2) * sv->nb,
-                                                    sv->red + (2 * m + 5), sv->flags, F_REORTH);
-            givens_kernel<<<1, 1, 0, c.st>>>(m, j, H, sv->red, sv->red + (m + 3), sv->red + (2 * m + 5), sv->st,
-                                             sv->flags, csg);
-            iters++;
-            if ((iters % std::max(1, sv->prm.check_every)) == 0 || j == m - 1 || iters >= maxit) {
-                if (read_flags(c)) return OCMP_ERR_CUDA;
-                if (sv->hflags[F_CONV]) {
-                    j++;
-                    break;
-                }
-            }
-        }
-        // x += P V y
-        trisolve_kernel<<<1, 1, 0, c.st>>>(m, H, csg, y, sv->flags);
-        combine_kernel<T><<<c.grid, kThreads, 0, c.st>>>(n, V, y, sv->flags, w);
-        if (block) {
-            launch_block_prec<T>(c, Binv, w, z, nullptr);
-            xupdate_kernel<TX, T><<<c.grid, kThreads, 0, c.st>>>(n, z, (const T*)nullptr, xacc);
-        } else {
-            xupdate_kernel<TX, T><<<c.grid, kThreads, 0, c.st>>>(n, w, djac, xacc);
-        }
-        OCMP_CUDA(cudaGetLastError());
-        if (read_flags(c)) return OCMP_ERR_CUDA;
-        if (sv->hflags[F_NONFIN] || sv->hflags[F_BREAK]) break;
-        if (!outer64) break;       // the inner solve is one cycle; refinement restarts it
-        if (iters >= maxit) break;
-        // converged estimate: confirm with the true residual at the top of the loop
-    }
-    *iters_out = iters;
-    return OCMP_OK;
-}
+// GMRES lives in the fused section below (gm_*).
 
 template <class T, class TM, class TX>
 int cg_core(const Ctx& c, const TM* vals, const T* dinv, T* r, T* z, T* p, T* q, TX* x, int maxit, double tol,
@@ -695,6 +615,526 @@ int cg_core(const Ctx& c, const TM* vals, const T* dinv, T* r, T* z, T* p, T* q,
     return OCMP_OK;
 }
 
+// =============================================================================================
+// Fused GMRES(m), right-preconditioned.
+//
+// The Krylov matrix is A D^-1 (point Jacobi folded into the values by gm_scale_matrix, refreshed
+// by ocmp_solver_update) or A itself with an explicit block-Jacobi application. The basis is kept
+// unnormalised: v_k = scale[k] * V[k], so no pass is spent normalising. One iteration is
+//   gm_spmv       : w = A_s v_j, written into V[j+1] (the row-blocked CSR SpMV);
+//   gm_dots       : all dot products V_k . w (k <= j) and |w|^2 in one pass over the basis;
+//   gm_orth       : w -= sum_k h_k v_k, |w|^2, then Hessenberg column, Givens rotation, residual
+//                   estimate, convergence and breakdown flags, scale[j+1] = 1/|w|;
+//   gm_dots / gm_orth pass 2 : a second classical Gram-Schmidt pass, launched always and skipped
+//                   on the device unless the first pass cancelled nearly all of |w|.
+// Reductions end in the last block to finish (a counter taken with atomicAdd after the block's
+// partials are written): that block sums the per-block partials in block order, so every result
+// is deterministic. Cycle start, refinement residual and final residual are one FP64 kernel
+// (gm_resid). FP64 restarts and the mixed-precision refinement share the same host loop.
+// =============================================================================================
+constexpr int kGridCap = 1216;  // 152 SMs x 8 resident blocks of 256 threads
+
+enum { S_TARGET = 11, S_INNER = 12, S_OUTERTOL = 13, S_ETA2 = 14 };
+enum { F_OUTER = 6 };
+
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+// true in every thread of the block that finishes last; resets the counter for the next launch
+__device__ __forceinline__ bool finish_last(unsigned* cnt) {
+    __shared__ bool last;
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) last = atomicAdd(cnt, 1u) == gridDim.x - 1;
+    __syncthreads();
+    if (last) {
+        __threadfence();
+        if (threadIdx.x == 0) *cnt = 0;
+    }
+    return last;
+}
+
+// out[k] = sum over blocks of part[k * nbp + b], k < nk, by the finishing block, warp per k
+__device__ __forceinline__ void finish_sums(const double* __restrict__ part, int nbp, int nblocks, int nk,
+                                            double* __restrict__ out) {
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+    for (int k = warp; k < nk; k += nw) {
+        double s = 0;
+        for (int b = lane; b < nblocks; b += 32) s += __ldcg(part + (int64_t)k * nbp + b);
+        s = warp_sum(s);
+        if (lane == 0) out[k] = s;
+    }
+    __syncthreads();
+}
+
+// One Givens step on Hessenberg column j (thread 0 of the finishing block).
+__device__ void givens_step(int m, int j, double hn, double* __restrict__ H, double* __restrict__ csg,
+                            double* __restrict__ st, int* __restrict__ flags, double* __restrict__ scale) {
+    double* cs = csg;
+    double* sn = csg + m;
+    double* g = csg + 2 * m;
+    H[(j + 1) * m + j] = hn;
+    for (int k = 0; k < j; k++) {
+        const double a = H[k * m + j], b = H[(k + 1) * m + j];
+        H[k * m + j] = cs[k] * a + sn[k] * b;
+        H[(k + 1) * m + j] = -sn[k] * a + cs[k] * b;
+    }
+    const double a = H[j * m + j], b = H[(j + 1) * m + j];
+    const double d = sqrt(a * a + b * b);
+    flags[F_ITERS] += 1;
+    if (!isfinite(d) || !isfinite(hn)) {
+        flags[F_NONFIN] = 1;
+        flags[F_CONV] = 1;
+        return;  // column j is dropped (F_JDONE stays j)
+    }
+    if (d == 0.0) {
+        flags[F_BREAK] = 1;
+        flags[F_CONV] = 1;
+        return;
+    }
+    cs[j] = a / d;
+    sn[j] = b / d;
+    H[j * m + j] = d;
+    H[(j + 1) * m + j] = 0;
+    g[j + 1] = -sn[j] * g[j];
+    g[j] = cs[j] * g[j];
+    flags[F_JDONE] = j + 1;
+    st[S_RES] = fabs(g[j + 1]) / st[S_NB];
+    scale[j + 1] = hn > 0 ? 1.0 / hn : 0.0;
+    if (fabs(g[j + 1]) <= st[S_TARGET] || hn == 0.0 || j + 1 >= m) flags[F_CONV] = 1;
+}
+
+// Cycle start / residual: r = (b - A x)_free with the FP64 matrix; V0 = r (stored in T);
+// mode 0: |(b - A x_D)_free| -> S_NB (x_D = x with free entries zeroed, V0 untouched)
+// mode 1: start a cycle (outer convergence test, g = beta e1, scale[0] = 1/beta, target)
+// mode 2: measure only (S_RES)
+// mode 3: mode 0 and mode 1 in the same pass (the first cycle of a solve); the lift A_fD x_D is
+//         summed over the precomputed lift list only
+template <class T, int TPR, int U>
+__global__ void __launch_bounds__(256) gm_resid(int64_t n, const int32_t* __restrict__ rp,
+                                                const int32_t* __restrict__ col, const double* __restrict__ A,
+                                                const uint8_t* __restrict__ freed, const double* __restrict__ b,
+                                                const double* __restrict__ x, T* __restrict__ V0,
+                                                double* __restrict__ part, unsigned* __restrict__ cnt, double* st,
+                                                int* flags, double* scale, double* csg, int m, int mode,
+                                                const int32_t* __restrict__ lift_ptr,
+                                                const int32_t* __restrict__ lift_pos) {
+    constexpr int RT = 256 / TPR;
+    const int lane = threadIdx.x % TPR;
+    double acc = 0, accd = 0;
+    for (int64_t t0 = (int64_t)blockIdx.x * RT; t0 < n; t0 += (int64_t)gridDim.x * RT) {
+        const int64_t r = t0 + threadIdx.x / TPR;
+        int32_t a = 0, e = 0;
+        if (r < n) {
+            a = __ldg(rp + r);
+            e = __ldg(rp + r + 1);
+        }
+        double ax;
+        if (mode == 0) {
+            // A x_D: gather only constrained entries
+            ax = 0;
+            for (int32_t k = a + lane; k < e; k += TPR) {
+                const int32_t c = __ldg(col + k);
+                if (!freed[c]) ax += __ldg(A + k) * __ldg(x + c);
+            }
+#pragma unroll
+            for (int o = TPR / 2; o > 0; o >>= 1) ax += __shfl_xor_sync(0xffffffffu, ax, o, TPR);
+        } else {
+            ax = row_dot<double, double, TPR, U>(a, e, col, A, x, lane);
+        }
+        if (r < n && lane == 0) {
+            const double v = freed[r] ? b[r] - ax : 0.0;
+            if (mode == 1 || mode == 3) V0[r] = (T)v;
+            acc += v * v;
+            if (mode == 3 && freed[r]) {
+                double lift = 0;
+                for (int32_t q = lift_ptr[r]; q < lift_ptr[r + 1]; q++) {
+                    const int32_t k = lift_pos[q];
+                    lift += A[k] * x[col[k]];
+                }
+                const double vd = b[r] - lift;
+                accd += vd * vd;
+            }
+        }
+    }
+    __shared__ double sh[8], shd[8];
+    {
+        const double s1 = warp_sum(acc), s2 = warp_sum(accd);
+        if ((threadIdx.x & 31) == 0) {
+            sh[threadIdx.x >> 5] = s1;
+            shd[threadIdx.x >> 5] = s2;
+        }
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double t = 0, td = 0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); w++) {
+            t += sh[w];
+            td += shd[w];
+        }
+        part[blockIdx.x] = t;
+        part[gridDim.x + blockIdx.x] = td;
+    }
+    if (!finish_last(cnt)) return;
+    __shared__ double tot, totd;
+    if (threadIdx.x < 32) {
+        double q = 0, qd = 0;
+        for (int bb = threadIdx.x; bb < (int)gridDim.x; bb += 32) {
+            q += __ldcg(part + bb);
+            qd += __ldcg(part + gridDim.x + bb);
+        }
+        q = warp_sum(q);
+        qd = warp_sum(qd);
+        if (threadIdx.x == 0) {
+            tot = q;
+            totd = qd;
+        }
+    }
+    __syncthreads();
+    if (threadIdx.x != 0) return;
+    const double beta = isfinite(tot) ? sqrt(fmax(tot, 0.0)) : (double)NAN;
+    if (mode == 0) {
+        st[S_NB] = beta > 0 ? beta : 1.0;
+        return;
+    }
+    if (mode == 3) {
+        const double nb = isfinite(totd) ? sqrt(fmax(totd, 0.0)) : (double)NAN;
+        st[S_NB] = (nb > 0 || !isfinite(nb)) ? nb : 1.0;
+    }
+    const double res = beta / st[S_NB];
+    st[S_RES] = res;
+    st[S_BETA] = beta;
+    if (mode == 2) return;
+    flags[F_JDONE] = 0;
+    flags[F_REORTH] = 0;
+    if (!isfinite(beta)) {
+        flags[F_NONFIN] = 1;
+        flags[F_CONV] = 1;
+        flags[F_OUTER] = 1;
+        return;
+    }
+    if (res <= st[S_OUTERTOL]) {
+        flags[F_OUTER] = 1;
+        flags[F_CONV] = 1;
+        return;
+    }
+    flags[F_CONV] = 0;
+    double* g = csg + 2 * m;
+    for (int k = 0; k <= m; k++) g[k] = 0;
+    g[0] = beta;
+    scale[0] = beta > 0 ? 1.0 / beta : 0.0;
+    // stop the cycle at the outer tolerance, or at the inner reduction for mixed precision
+    st[S_TARGET] = fmax(0.5 * st[S_OUTERTOL] * st[S_NB], st[S_INNER] * beta);
+}
+
+// d_k = V_k . w for k <= j, and |w|^2 as d_{j+1} when with_norm; w = V[j+1]. The second
+// Gram-Schmidt pass (gated = 1) runs only when F_REORTH is set.
+template <class T>
+__global__ void __launch_bounds__(256) gm_dots(int64_t n, int j, const T* __restrict__ V, double* __restrict__ part,
+                                               int nbp, unsigned* __restrict__ cnt, double* __restrict__ red,
+                                               const int* __restrict__ flags, int gated, int with_norm) {
+    if (flags[F_CONV] || (gated && !flags[F_REORTH])) return;
+    const T* __restrict__ w = V + (int64_t)(j + 1) * n;
+    const int warp = threadIdx.x >> 5, lane32 = threadIdx.x & 31;
+    const int nk = j + 1 + (with_norm ? 1 : 0);
+    // a block sweeps a contiguous slab of rows; warp w owns k = w, w + 8, ...
+    const int64_t slab = ((n + gridDim.x - 1) / gridDim.x + 31) / 32 * 32;
+    const int64_t i0 = (int64_t)blockIdx.x * slab, i1 = min(n, i0 + slab);
+    for (int k = warp; k < nk; k += 8) {
+        const T* __restrict__ vk = k <= j ? V + (int64_t)k * n : w;
+        T s0 = 0, s1 = 0, s2 = 0, s3 = 0;
+        int64_t i = i0 + lane32;
+        for (; i + 96 < i1; i += 128) {
+            s0 += vk[i] * w[i];
+            s1 += vk[i + 32] * w[i + 32];
+            s2 += vk[i + 64] * w[i + 64];
+            s3 += vk[i + 96] * w[i + 96];
+        }
+        for (; i < i1; i += 32) s0 += vk[i] * w[i];
+        const double sm = warp_sum((double)s0 + (double)s1 + (double)s2 + (double)s3);
+        if (lane32 == 0) part[(int64_t)k * nbp + blockIdx.x] = sm;
+    }
+    if (!finish_last(cnt)) return;
+    finish_sums(part, nbp, gridDim.x, nk, red);
+}
+
+// plain masked SpMV of the Krylov matrix into the next basis slot: V[j+1] = sc * (A_s x_in)_free
+template <class T, int TPR, int U>
+__global__ void __launch_bounds__(256) gm_spmv(int64_t n, int j, const int32_t* __restrict__ rp,
+                                               const int32_t* __restrict__ col, const T* __restrict__ A,
+                                               const uint8_t* __restrict__ freed, const T* __restrict__ xin,
+                                               int xin_is_basis, T* __restrict__ V, const double* __restrict__ scale,
+                                               const int* __restrict__ flags) {
+    if (flags[F_CONV]) return;
+    const int64_t r = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) / TPR;
+    const int lane = threadIdx.x % TPR;
+    int32_t a = 0, e = 0;
+    if (r < n) {
+        a = __ldg(rp + r);
+        e = __ldg(rp + r + 1);
+    }
+    const T y = row_dot<T, T, TPR, U>(a, e, col, A, xin, lane);
+    if (r < n && lane == 0) {
+        const T sc = xin_is_basis ? (T)scale[j] : (T)1;
+        V[(int64_t)(j + 1) * n + r] = freed[r] ? y * sc : (T)0;
+    }
+}
+
+// w -= sum_k h_k v_k; |w|^2; then (finishing block) Hessenberg column + Givens, or the request for
+// a second pass. pass 1 reads h from red (d_k = V_k . w, |w|^2 in red[j+1]); pass 2 from red2.
+template <class T>
+__global__ void __launch_bounds__(256) gm_orth(int64_t n, int j, int m, T* __restrict__ V,
+                                               const double* __restrict__ red, double* __restrict__ part,
+                                               unsigned* __restrict__ cnt, double* __restrict__ H,
+                                               double* __restrict__ csg, double* st, int* flags, double* scale,
+                                               int pass) {
+    if (flags[F_CONV] || (pass == 2 && !flags[F_REORTH])) return;
+    __shared__ T coef[130];
+    for (int k = threadIdx.x; k <= j; k += blockDim.x) coef[k] = (T)(red[k] * scale[k] * scale[k]);
+    __syncthreads();
+    T* __restrict__ w = V + (int64_t)(j + 1) * n;
+    double acc = 0;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        T wi = w[i];
+        for (int k = 0; k <= j; k++) wi -= coef[k] * V[(int64_t)k * n + i];
+        w[i] = wi;
+        acc += (double)(wi * wi);
+    }
+    double s = warp_sum(acc);
+    __shared__ double sh[8];
+    if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = s;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double t = 0;
+        for (int q = 0; q < (int)(blockDim.x >> 5); q++) t += sh[q];
+        part[blockIdx.x] = t;
+    }
+    if (!finish_last(cnt)) return;
+    __shared__ double hn2;
+    if (threadIdx.x < 32) {
+        double q = 0;
+        for (int b = threadIdx.x; b < (int)gridDim.x; b += 32) q += __ldcg(part + b);
+        q = warp_sum(q);
+        if (threadIdx.x == 0) hn2 = q;
+    }
+    __syncthreads();
+    if (threadIdx.x != 0) return;
+    for (int k = 0; k <= j; k++) {
+        const double h = red[k] * scale[k];
+        H[k * m + j] = pass == 1 ? h : H[k * m + j] + h;
+    }
+    if (pass == 1) {
+        st[S_NW2] = red[j + 1];
+        if (hn2 < st[S_ETA2] * red[j + 1]) {  // cancellation beyond the threshold: orthogonalise again
+            flags[F_REORTH] = 1;
+            return;
+        }
+    }
+    flags[F_REORTH] = 0;
+    givens_step(m, j, isfinite(hn2) ? sqrt(fmax(hn2, 0.0)) : (double)NAN, H, csg, st, flags, scale);
+}
+
+// x += P (sum_k y_k v_k) with y = H^-1 g over the completed columns (each block solves the small
+// triangular system itself). P = D^-1 (dinv != null), identity, or (u != null) the sum is written
+// to u for a block-Jacobi application by the caller.
+template <class T>
+__global__ void __launch_bounds__(256) gm_combine(int64_t n, int m, const T* __restrict__ V,
+                                                  const double* __restrict__ scale, const double* __restrict__ H,
+                                                  const double* __restrict__ csg, const int* __restrict__ flags,
+                                                  const T* __restrict__ dinv, double* __restrict__ x,
+                                                  T* __restrict__ u) {
+    __shared__ double y[130];
+    __shared__ T c[130];
+    const int jd = flags[F_JDONE];
+    if (jd == 0) return;
+    if (threadIdx.x == 0) {
+        const double* g = csg + 2 * m;
+        for (int k = jd - 1; k >= 0; k--) {
+            double a = g[k];
+            for (int l = k + 1; l < jd; l++) a -= H[k * m + l] * y[l];
+            y[k] = a / H[k * m + k];
+        }
+        for (int k = 0; k < jd; k++) c[k] = (T)(y[k] * scale[k]);
+    }
+    __syncthreads();
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        T acc = 0;
+        for (int k = 0; k < jd; k++) acc += c[k] * V[(int64_t)k * n + i];
+        if (u) u[i] = acc;
+        else x[i] += (double)(dinv ? dinv[i] * acc : acc);
+    }
+}
+
+template <class T, int L>
+__global__ void gm_block_apply(int64_t ne, const T* __restrict__ Binv, const T* __restrict__ v, double sc_const,
+                               const double* __restrict__ scale, int j, T* __restrict__ z, double* __restrict__ x,
+                               const int* __restrict__ flags) {
+    if (flags && flags[F_CONV]) return;
+    const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (t >= ne * L) return;
+    const int64_t e = t / L;
+    const int i = (int)(t % L);
+    const T sc = scale ? (T)scale[j] : (T)sc_const;
+    T acc = 0;
+#pragma unroll
+    for (int k = 0; k < L; k++) acc += Binv[(e * L + i) * L + k] * v[e * L + k];
+    if (x) x[t] += (double)(acc * sc);
+    else z[t] = acc * sc;
+}
+
+// A_s = A D^-1 (Jacobi) or A, cast to T
+template <class T>
+__global__ void gm_scale_matrix(int64_t n, const int32_t* __restrict__ rp, const int32_t* __restrict__ col,
+                                const double* __restrict__ A, const double* __restrict__ dinv64, T* __restrict__ As) {
+    const int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (r >= n) return;
+    for (int32_t k = rp[r]; k < rp[r + 1]; k++) {
+        const double d = dinv64 ? dinv64[col[k]] : 1.0;
+        As[k] = (T)(A[k] * d);
+    }
+}
+
+__global__ void gm_cast(int64_t n, const double* __restrict__ a, float* __restrict__ b) {
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i < n) b[i] = (float)a[i];
+}
+
+__global__ void gm_set_tols(double* st, double tol, double inner, double eta2) {
+    st[S_OUTERTOL] = tol;
+    st[S_INNER] = inner;
+    st[S_TOL] = tol;
+    st[S_ETA2] = eta2;
+}
+
+template <class T>
+struct GmBufs {
+    const T* A;        // Krylov matrix (scaled or plain)
+    const T* dinv;     // for the final x update (Jacobi), or null
+    const T* Binv;     // block Jacobi, or null
+    T* V;
+    T* z;              // block Jacobi workspace
+};
+
+template <class T, int TPR, int U>
+int gm_run(const Ctx& c, const GmBufs<T>& B, const double* b, double* x, int maxit, double inner_tol, int* iters,
+           int* cycles, double* relres0) {
+    ocmp_solver_s* sv = c.sv;
+    const ocmp_space_s* s = sv->s;
+    const int64_t n = sv->n;
+    const int m = sv->m;
+    const int G = sv->grid;
+    double* csg = sv->H + (size_t)(m + 1) * m;
+    const int nbp = G;
+    double* red2 = sv->red + (m + 4);
+    const bool block = B.Binv != nullptr;
+    const int64_t ne = s->mesh->ne;
+    const int L = s->nloc;
+    auto block_apply = [&](int j, double* xo) {
+        const unsigned nbk = nblk(ne * L, kThreads);
+        switch (L) {
+        case 3: gm_block_apply<T, 3><<<nbk, kThreads, 0, c.st>>>(ne, B.Binv, xo ? B.z : B.V + (int64_t)j * n, 1.0, xo ? nullptr : sv->scale, j, B.z, xo, xo ? nullptr : sv->flags); break;
+        case 6: gm_block_apply<T, 6><<<nbk, kThreads, 0, c.st>>>(ne, B.Binv, xo ? B.z : B.V + (int64_t)j * n, 1.0, xo ? nullptr : sv->scale, j, B.z, xo, xo ? nullptr : sv->flags); break;
+        case 10: gm_block_apply<T, 10><<<nbk, kThreads, 0, c.st>>>(ne, B.Binv, xo ? B.z : B.V + (int64_t)j * n, 1.0, xo ? nullptr : sv->scale, j, B.z, xo, xo ? nullptr : sv->flags); break;
+        default: break;
+        }
+    };
+    // Classical Gram-Schmidt, repeated only when |w| lost more than 99.9% of its length to the
+    // projection (|w_new|^2 < 1e-6 |w|^2); the mass-dominated systems here lose far less per step.
+    gm_set_tols<<<1, 1, 0, c.st>>>(sv->st, sv->prm.tol, inner_tol, 1e-6);
+    OCMP_CUDA(cudaMemsetAsync(sv->flags, 0, sizeof(int) * F_NFLAG, c.st));
+    gm_resid<T, TPR, U><<<G, 256, 0, c.st>>>(n, s->d_rowptr, s->d_col, sv->mat->vals, s->d_free, b, x, B.V, sv->part,
+                                             sv->cnt, sv->st, sv->flags, sv->scale, csg, m, 3, s->d_lift_ptr,
+                                             s->d_lift_pos);
+    {
+        double r0 = 0;
+        OCMP_CUDA(cudaMemcpyAsync(&r0, sv->st + S_RES, sizeof(double), cudaMemcpyDeviceToHost, c.st));
+        if (read_flags(c)) return OCMP_ERR_CUDA;
+        *relres0 = r0;
+    }
+    int it = 0, cyc = 0;
+    bool first = true;
+    while (true) {
+        if (!first && read_flags(c)) return OCMP_ERR_CUDA;
+        first = false;
+        if (sv->hflags[F_OUTER] || sv->hflags[F_NONFIN] || it >= maxit) break;
+        // one cycle
+        int j = 0;
+        for (; j < m; j++) {
+            const T* xin = B.V + (int64_t)j * n;
+            if (block) {
+                block_apply(j, nullptr);
+                xin = B.z;
+            }
+            gm_spmv<T, TPR, U><<<nblk(n * TPR, 256), 256, 0, c.st>>>(n, j, s->d_rowptr, s->d_col, B.A, s->d_free, xin,
+                                                                     block ? 0 : 1, B.V, sv->scale, sv->flags);
+            gm_dots<T><<<G, 256, 0, c.st>>>(n, j, B.V, sv->part, nbp, sv->cnt, sv->red, sv->flags, 0, 1);
+            gm_orth<T><<<G, 256, 0, c.st>>>(n, j, m, B.V, sv->red, sv->part, sv->cnt + 1, sv->H, csg, sv->st,
+                                            sv->flags, sv->scale, 1);
+            gm_dots<T><<<G, 256, 0, c.st>>>(n, j, B.V, sv->part, nbp, sv->cnt + 2, red2, sv->flags, 1, 0);
+            gm_orth<T><<<G, 256, 0, c.st>>>(n, j, m, B.V, red2, sv->part, sv->cnt + 3, sv->H, csg, sv->st,
+                                            sv->flags, sv->scale, 2);
+            it++;
+            if (((j + 1) % std::max(1, sv->prm.check_every)) == 0 || it >= maxit) {
+                if (read_flags(c)) return OCMP_ERR_CUDA;
+                if (sv->hflags[F_CONV] || it >= maxit) break;
+            }
+        }
+        // x += P V y
+        if (block) {
+            gm_combine<T><<<G, 256, 0, c.st>>>(n, m, B.V, sv->scale, sv->H, csg, sv->flags, nullptr, x, B.z);
+            block_apply(0, x);
+        } else {
+            gm_combine<T><<<G, 256, 0, c.st>>>(n, m, B.V, sv->scale, sv->H, csg, sv->flags, B.dinv, x, nullptr);
+        }
+        cyc++;
+        if (read_flags(c)) return OCMP_ERR_CUDA;
+        if (sv->hflags[F_NONFIN]) break;
+        // next cycle: FP64 residual of the updated iterate (restart / refinement step)
+        gm_resid<T, TPR, U><<<G, 256, 0, c.st>>>(n, s->d_rowptr, s->d_col, sv->mat->vals, s->d_free, b, x, B.V,
+                                                 sv->part, sv->cnt, sv->st, sv->flags, sv->scale, csg, m, 1,
+                                                 s->d_lift_ptr, s->d_lift_pos);
+    }
+    OCMP_CUDA(cudaGetLastError());
+    *iters = sv->hflags[F_ITERS];
+    *cycles = cyc;
+    return OCMP_OK;
+}
+
+template <class T>
+int gm_dispatch(const Ctx& c, const GmBufs<T>& B, const double* b, double* x, int maxit, double inner_tol,
+                int* iters, int* cycles, double* relres0) {
+    const RowCfg rc = row_cfg(c.sv->s);
+    if (rc.tpr == 2) return gm_run<T, 2, 4>(c, B, b, x, maxit, inner_tol, iters, cycles, relres0);
+    if (rc.tpr == 4 && rc.u == 4) return gm_run<T, 4, 4>(c, B, b, x, maxit, inner_tol, iters, cycles, relres0);
+    if (rc.tpr == 4) return gm_run<T, 4, 8>(c, B, b, x, maxit, inner_tol, iters, cycles, relres0);
+    if (rc.tpr == 8) return gm_run<T, 8, 8>(c, B, b, x, maxit, inner_tol, iters, cycles, relres0);
+    return gm_run<T, 16, 8>(c, B, b, x, maxit, inner_tol, iters, cycles, relres0);
+}
+
+// |(b - A x_D)_free| and |(b - A x)_free| / that, with the fused residual kernel
+int gm_norms(const Ctx& c, const double* b, const double* x, int mode) {
+    ocmp_solver_s* sv = c.sv;
+    const ocmp_space_s* s = sv->s;
+    const RowCfg rc = row_cfg(s);
+    double* csg = sv->H + (size_t)(sv->m + 1) * sv->m;
+#define GM_R(TPR, U)                                                                                              \
+    gm_resid<double, TPR, U><<<sv->grid, 256, 0, c.st>>>(sv->n, s->d_rowptr, s->d_col, sv->mat->vals, s->d_free, b, \
+                                                         x, (double*)nullptr, sv->part, sv->cnt, sv->st, sv->flags,    \
+                                                         sv->scale, csg, sv->m, mode, s->d_lift_ptr,            \
+                                                         s->d_lift_pos)
+    if (rc.tpr == 2) GM_R(2, 4);
+    else if (rc.tpr == 4 && rc.u == 4) GM_R(4, 4);
+    else if (rc.tpr == 4) GM_R(4, 8);
+    else if (rc.tpr == 8) GM_R(8, 8);
+    else GM_R(16, 8);
+#undef GM_R
+    OCMP_CUDA(cudaGetLastError());
+    return OCMP_OK;
+}
+
 }  // namespace
 }  // namespace ocmp
 
@@ -703,7 +1143,7 @@ using namespace ocmp;
 static void free_solver(ocmp_solver_s* sv) {
     void* ps[] = {sv->dinv, sv->Binv, sv->V,   sv->w,     sv->z,   sv->r,     sv->p,    sv->dinv32, sv->Binv32,
                   sv->V32,  sv->w32,  sv->z32, sv->r32,   sv->p32, sv->d32,   sv->part, sv->pspmv,  sv->red,
-                  sv->st,   sv->H,    sv->flags};
+                  sv->st,   sv->H,    sv->flags, sv->As64, sv->As32, sv->scale, sv->cnt};
     for (void* q : ps) dfree(q);
     if (sv->hflags) cudaFreeHost(sv->hflags);
 }
@@ -715,8 +1155,8 @@ int ocmp_solver_create(ocmp_matrix_t mat, const ocmp_solve_params_t* prm, ocmp_s
     if (prm->method != OCMP_CG && prm->method != OCMP_GMRES) return fail(OCMP_ERR_ARG, "ocmp_solver_create: method");
     if (prm->precond < OCMP_PRE_NONE || prm->precond > OCMP_PRE_BLOCK_JACOBI)
         return fail(OCMP_ERR_ARG, "ocmp_solver_create: precond");
-    if (prm->precision == OCMP_MIXED && !mat->vals32)
-        return fail(OCMP_ERR_ARG, "ocmp_solver_create: mixed precision needs a matrix created with want_fp32");
+    if (prm->precision == OCMP_MIXED && prm->method == OCMP_CG && !mat->vals32)
+        return fail(OCMP_ERR_ARG, "ocmp_solver_create: mixed-precision CG needs a matrix created with OCMP_MAT_FP32");
     if (prm->method == OCMP_CG && prm->precond != OCMP_PRE_JACOBI)
         return fail(OCMP_ERR_UNSUPPORTED, "ocmp_solver_create: CG is built with the Jacobi preconditioner");
     ocmp_space_s* s = mat->space;
@@ -760,12 +1200,25 @@ int ocmp_solver_create(ocmp_matrix_t mat, const ocmp_solve_params_t* prm, ocmp_s
         }
         if (blk) A(&sv->Binv32, (size_t)s->mesh->ne * s->nloc * s->nloc);
     }
-    A(&sv->part, (size_t)(2 * m + 8) * sv->nb);
+    sv->grid = (int)std::max<int64_t>(1, std::min<int64_t>(kGridCap, nbs));
+    A(&sv->part, (size_t)(m + 4) * kGridCap);
     A(&sv->pspmv, (size_t)nbs);
     A(&sv->red, (size_t)(3 * m + 12));
     A(&sv->st, (size_t)S_NSLOT);
     A(&sv->H, (size_t)(m + 1) * m + 4 * m + 2);
+    A(&sv->scale, (size_t)(m + 2));
+    A(&sv->cnt, (size_t)8);
+    sv->borrow = gm && prm->precond == OCMP_PRE_JACOBI && mat->dinv &&
+                 (mixed ? mat->svals32 != nullptr : mat->svals64 != nullptr);
+    if (gm && !sv->borrow) {
+        if (mixed) A(&sv->As32, (size_t)s->nnz);
+        else A(&sv->As64, (size_t)s->nnz);
+    }
+    sv->K64 = sv->borrow ? mat->svals64 : sv->As64;
+    sv->K32 = sv->borrow ? mat->svals32 : sv->As32;
     A(&sv->flags, (size_t)F_NFLAG);
+    if (!st && cudaMemset(sv->cnt, 0, sizeof(unsigned) * 8) != cudaSuccess) st = fail(OCMP_ERR_CUDA, "cudaMemset");
+    if (!st && cudaMemset(sv->st, 0, sizeof(double) * S_NSLOT) != cudaSuccess) st = fail(OCMP_ERR_CUDA, "cudaMemset");
     if (!st && cudaMallocHost((void**)&sv->hflags, sizeof(int) * F_NFLAG) != cudaSuccess)
         st = fail(OCMP_ERR_NOMEM, "cudaMallocHost");
     if (st) {
@@ -808,6 +1261,20 @@ int ocmp_solver_update(ocmp_solver_t sv, void* stream) {
         default: break;
         }
     }
+    if (sv->borrow) {
+        // the assembly's D^-1 scaled the Krylov matrix: use the same one for x = D^-1 y
+        OCMP_CUDA(cudaMemcpyAsync(sv->dinv, sv->mat->dinv, sizeof(double) * n, cudaMemcpyDeviceToDevice, st));
+        if (sv->dinv32) gm_cast<<<nblk(n, kThreads), kThreads, 0, st>>>(n, sv->mat->dinv, sv->dinv32);
+    }
+    if (sv->As64 || sv->As32) {
+        const double* d = sv->prm.precond == OCMP_PRE_JACOBI ? sv->dinv : nullptr;
+        if (sv->As64)
+            gm_scale_matrix<double><<<nblk(n, kThreads), kThreads, 0, st>>>(n, s->d_rowptr, s->d_col, sv->mat->vals, d,
+                                                                            sv->As64);
+        if (sv->As32)
+            gm_scale_matrix<float><<<nblk(n, kThreads), kThreads, 0, st>>>(n, s->d_rowptr, s->d_col, sv->mat->vals, d,
+                                                                           sv->As32);
+    }
     OCMP_CUDA(cudaGetLastError());
     return OCMP_OK;
 }
@@ -822,81 +1289,96 @@ int ocmp_solve(ocmp_solver_t sv, const double* b, double* x, void* stream, ocmp_
     const int64_t n = sv->n;
     const ocmp_solve_params_t& P = sv->prm;
     const bool gm = P.method == OCMP_GMRES, mixed = P.precision == OCMP_MIXED;
-    int st = rhs_norm(c, b, x);
-    if (st) return st;
+    int st = OCMP_OK;
     double hst[S_NSLOT];
-    // initial residual
-    st = residual64(c, b, x, gm && !mixed ? sv->V : sv->r);
-    if (st) return st;
-    double red0 = 0;
-    OCMP_CUDA(cudaMemcpyAsync(&red0, sv->red, sizeof(double), cudaMemcpyDeviceToHost, c.st));
-    OCMP_CUDA(cudaMemcpyAsync(hst, sv->st, sizeof(hst), cudaMemcpyDeviceToHost, c.st));
-    OCMP_CUDA(cudaStreamSynchronize(c.st));
-    const double nbv = hst[S_NB];
-    double relres0 = std::sqrt(std::max(red0, 0.0)) / nbv;
     int iters = 0, outer = 0;
-    bool nonfin = !std::isfinite(relres0), brk = false;
-    if (!nonfin && relres0 > P.tol) {
+    bool nonfin = false, brk = false;
+    double relres0 = 0, relres = 0;
+    if (gm) {
+        const bool jac = P.precond == OCMP_PRE_JACOBI;
         if (!mixed) {
-            if (gm) {
-                st = gmres_core<double, double, double>(c, sv->mat->vals, sv->dinv, sv->Binv, sv->V, sv->w, sv->z, x, b,
-                                                        x, P.maxit, P.tol, &iters, true);
-            } else {
-                st = cg_core<double, double, double>(c, sv->mat->vals, sv->dinv, sv->r, sv->z, sv->p, sv->w, x, P.maxit,
-                                                     P.tol, &iters);
-            }
-            if (st) return st;
-            nonfin = sv->hflags[F_NONFIN] != 0;
-            brk = sv->hflags[F_BREAK] != 0;
+            GmBufs<double> B{sv->K64, jac ? sv->dinv : nullptr, sv->Binv, sv->V, sv->z};
+            st = gm_dispatch<double>(c, B, b, x, P.maxit, 0.0, &iters, &outer, &relres0);
         } else {
-            double beta = std::sqrt(std::max(red0, 0.0));
-            while (iters < P.maxit) {
-                // inner FP32 solve of A d = r / beta
-                set_state<<<1, 1, 0, c.st>>>(sv->st, S_BETA, beta);
-                set_state<<<1, 1, 0, c.st>>>(sv->st, S_NB, 1.0);
-                double itol = std::max(P.inner_tol > 0 ? P.inner_tol : 1e-4, 0.5 * P.tol * nbv / beta);
-                OCMP_CUDA(cudaMemsetAsync(sv->d32, 0, sizeof(float) * n, c.st));
-                int it_in = 0;
-                if (gm) {
-                    scale_to_float<<<c.grid, kThreads, 0, c.st>>>(n, sv->r, sv->st, sv->V32);
-                    set_state<<<1, 1, 0, c.st>>>(sv->red, 0, 1.0);
-                    st = gmres_core<float, float, float>(c, sv->mat->vals32, sv->dinv32, sv->Binv32, sv->V32, sv->w32,
-                                                         sv->z32, sv->d32, b, x, P.maxit - iters, itol, &it_in, false);
-                } else {
+            GmBufs<float> B{sv->K32, jac ? sv->dinv32 : nullptr, sv->Binv32, sv->V32, sv->z32};
+            st = gm_dispatch<float>(c, B, b, x, P.maxit, P.inner_tol > 0 ? P.inner_tol : 1e-4, &iters, &outer,
+                                    &relres0);
+        }
+        if (st) return st;
+        nonfin = sv->hflags[F_NONFIN] != 0 || !std::isfinite(relres0);
+        brk = sv->hflags[F_BREAK] != 0;
+        if (sv->hflags[F_OUTER] && !nonfin) {
+            // the last cycle-start residual is the FP64 residual of the returned x
+            OCMP_CUDA(cudaMemcpyAsync(hst, sv->st, sizeof(hst), cudaMemcpyDeviceToHost, c.st));
+            OCMP_CUDA(cudaStreamSynchronize(c.st));
+            relres = hst[S_RES];
+        } else {
+            st = gm_norms(c, b, x, 2);
+            if (st) return st;
+            OCMP_CUDA(cudaMemcpyAsync(hst, sv->st, sizeof(hst), cudaMemcpyDeviceToHost, c.st));
+            OCMP_CUDA(cudaStreamSynchronize(c.st));
+            relres = hst[S_RES];
+        }
+    } else {
+        st = rhs_norm(c, b, x);
+        if (st) return st;
+        st = residual64(c, b, x, sv->r);
+        if (st) return st;
+        double red0 = 0;
+        OCMP_CUDA(cudaMemcpyAsync(&red0, sv->red, sizeof(double), cudaMemcpyDeviceToHost, c.st));
+        OCMP_CUDA(cudaMemcpyAsync(hst, sv->st, sizeof(hst), cudaMemcpyDeviceToHost, c.st));
+        OCMP_CUDA(cudaStreamSynchronize(c.st));
+        const double nbv = hst[S_NB];
+        relres0 = std::sqrt(std::max(red0, 0.0)) / nbv;
+        nonfin = !std::isfinite(relres0);
+        if (!nonfin && relres0 > P.tol) {
+            if (!mixed) {
+                st = cg_core<double, double, double>(c, sv->mat->vals, sv->dinv, sv->r, sv->z, sv->p, sv->w, x,
+                                                     P.maxit, P.tol, &iters);
+                if (st) return st;
+                nonfin = sv->hflags[F_NONFIN] != 0;
+                brk = sv->hflags[F_BREAK] != 0;
+            } else {
+                double beta = std::sqrt(std::max(red0, 0.0));
+                while (iters < P.maxit) {
+                    set_state<<<1, 1, 0, c.st>>>(sv->st, S_BETA, beta);
+                    set_state<<<1, 1, 0, c.st>>>(sv->st, S_NB, 1.0);
+                    const double itol = std::max(P.inner_tol > 0 ? P.inner_tol : 1e-4, 0.5 * P.tol * nbv / beta);
+                    OCMP_CUDA(cudaMemsetAsync(sv->d32, 0, sizeof(float) * n, c.st));
+                    int it_in = 0;
                     scale_to_float<<<c.grid, kThreads, 0, c.st>>>(n, sv->r, sv->st, sv->r32);
                     st = cg_core<float, float, float>(c, sv->mat->vals32, sv->dinv32, sv->r32, sv->z32, sv->p32,
                                                       sv->w32, sv->d32, P.maxit - iters, itol, &it_in);
+                    if (st) return st;
+                    iters += std::max(it_in, 1);
+                    outer++;
+                    if (sv->hflags[F_NONFIN]) {
+                        nonfin = true;
+                        break;
+                    }
+                    set_state<<<1, 1, 0, c.st>>>(sv->st, S_BETA, beta);
+                    add_scaled_float<<<c.grid, kThreads, 0, c.st>>>(n, sv->d32, sv->st, x);
+                    set_state<<<1, 1, 0, c.st>>>(sv->st, S_NB, nbv);
+                    st = residual64(c, b, x, sv->r);
+                    if (st) return st;
+                    OCMP_CUDA(cudaMemcpyAsync(&red0, sv->red, sizeof(double), cudaMemcpyDeviceToHost, c.st));
+                    OCMP_CUDA(cudaStreamSynchronize(c.st));
+                    beta = std::sqrt(std::max(red0, 0.0));
+                    if (!std::isfinite(beta)) {
+                        nonfin = true;
+                        break;
+                    }
+                    if (beta / nbv <= P.tol) break;
                 }
-                if (st) return st;
-                iters += std::max(it_in, 1);
-                outer++;
-                if (sv->hflags[F_NONFIN]) {
-                    nonfin = true;
-                    break;
-                }
-                set_state<<<1, 1, 0, c.st>>>(sv->st, S_BETA, beta);
-                add_scaled_float<<<c.grid, kThreads, 0, c.st>>>(n, sv->d32, sv->st, x);
-                set_state<<<1, 1, 0, c.st>>>(sv->st, S_NB, nbv);
-                st = residual64(c, b, x, sv->r);
-                if (st) return st;
-                OCMP_CUDA(cudaMemcpyAsync(&red0, sv->red, sizeof(double), cudaMemcpyDeviceToHost, c.st));
-                OCMP_CUDA(cudaStreamSynchronize(c.st));
-                beta = std::sqrt(std::max(red0, 0.0));
-                if (!std::isfinite(beta)) {
-                    nonfin = true;
-                    break;
-                }
-                if (beta / nbv <= P.tol) break;
             }
         }
+        set_state<<<1, 1, 0, c.st>>>(sv->st, S_NB, nbv);
+        st = residual64(c, b, x, (double*)nullptr);
+        if (st) return st;
+        OCMP_CUDA(cudaMemcpyAsync(&red0, sv->red, sizeof(double), cudaMemcpyDeviceToHost, c.st));
+        OCMP_CUDA(cudaStreamSynchronize(c.st));
+        relres = std::sqrt(std::max(red0, 0.0)) / nbv;
     }
-    // final FP64 relative residual
-    set_state<<<1, 1, 0, c.st>>>(sv->st, S_NB, nbv);
-    st = residual64(c, b, x, (double*)nullptr);
-    if (st) return st;
-    OCMP_CUDA(cudaMemcpyAsync(&red0, sv->red, sizeof(double), cudaMemcpyDeviceToHost, c.st));
-    OCMP_CUDA(cudaStreamSynchronize(c.st));
-    const double relres = std::sqrt(std::max(red0, 0.0)) / nbv;
     int status = OCMP_OK;
     if (nonfin || !std::isfinite(relres)) status = OCMP_ERR_NONFINITE;
     else if (relres > P.tol) status = brk ? OCMP_BREAKDOWN : OCMP_NOT_CONVERGED;

@@ -149,15 +149,22 @@ def make_rhs(dt=1.0, src_const=None, src_qp: Optional[torch.Tensor] = None, mass
     return r
 
 
-class Matrix:
-    """Assembled sparse matrix in the space's CSR pattern (FP64 values, optional FP32 copy)."""
+MAT_FP32, MAT_JACOBI64, MAT_JACOBI32 = 1, 2, 4
 
-    def __init__(self, space: Space, fp32: bool = False):
+
+class Matrix:
+    """Assembled sparse matrix in the space's CSR pattern: FP64 values, and optionally an FP32 copy
+    (``fp32``) and the Jacobi-scaled Krylov matrices A D^-1 in FP64 / FP32 (``jacobi64`` /
+    ``jacobi32``) written by the same assembly pass."""
+
+    def __init__(self, space: Space, fp32: bool = False, jacobi64: bool = False, jacobi32: bool = False):
         self.space = space
         h = C.c_void_p()
-        LB.call('ocmp_matrix_create', space.h, int(fp32), C.byref(h))
+        flags = (MAT_FP32 if fp32 else 0) | (MAT_JACOBI64 if jacobi64 else 0) | (MAT_JACOBI32 if jacobi32 else 0)
+        LB.call('ocmp_matrix_create', space.h, flags, C.byref(h))
         self.h = h
         self.fp32 = fp32
+        self.flags = flags
 
     def __del__(self):
         if getattr(self, 'h', None) and LB._lib is not None:
@@ -174,6 +181,17 @@ class Matrix:
         v64 = _dev_view(p64.value, self.space.nnz, '<f8', self)
         v32 = _dev_view(p32.value, self.space.nnz, '<f4', self) if p32.value else None
         return v64, v32
+
+    def scaled_values(self):
+        """Host copies of (A D^-1 in FP64 or None, A D^-1 in FP32 or None, D^-1 or None)."""
+        p64, p32, pd = C.c_void_p(), C.c_void_p(), C.c_void_p()
+        LB.call('ocmp_matrix_scaled_values', self.h, C.byref(p64), C.byref(p32), C.byref(pd))
+        torch.cuda.synchronize()
+        n, nd = self.space.nnz, self.space.ndof
+        v64 = _dev_view(p64.value, n, '<f8', self).cpu().numpy() if p64.value else None
+        v32 = _dev_view(p32.value, n, '<f4', self).cpu().numpy() if p32.value else None
+        d = _dev_view(pd.value, nd, '<f8', self).cpu().numpy() if pd.value else None
+        return v64, v32, d
 
     def values(self) -> np.ndarray:
         """FP64 values copied to the host (for checks)."""

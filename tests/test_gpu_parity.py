@@ -84,7 +84,10 @@ def test_matrix_entries_match_oracle(gpu_lib, oracle, name, mk, kind, order):
     from opencmp_gb300 import fem
     m = mk()
     g, o = _spaces(oracle, m, kind, order, m.bc_names[:1])
-    A = fem.Matrix(g, fp32=True)
+    A = fem.Matrix(g, fp32=True, jacobi64=True, jacobi32=True)
+    rp, col = o.pattern()
+    rows = np.repeat(np.arange(o.ndof), np.diff(rp))
+    free = o.freedofs()
     for nm, of, gf, keep in _forms(oracle, m, kind, True):
         A.assemble(gf)
         ag = A.values()
@@ -94,6 +97,14 @@ def test_matrix_entries_match_oracle(gpu_lib, oracle, name, mk, kind, order):
         assert err <= 1e-12, (nm, err)
         a32 = A.values32()
         assert np.array_equal(a32, ag.astype(np.float32)), nm
+        # Jacobi-scaled outputs: A D^-1 with D the diagonal on free rows (0 on constrained ones)
+        s64, s32, dinv = A.scaled_values()
+        diag = ao[rp[:-1] + np.array([np.searchsorted(col[rp[r]:rp[r + 1]], r) for r in range(o.ndof)])]
+        dref = np.where(free & (diag != 0), 1.0 / np.where(diag != 0, diag, 1.0), 0.0)
+        assert np.abs(dinv - dref).max() <= 1e-12 * np.abs(dref).max(), nm
+        sref = ao * dref[col]
+        assert np.abs(s64 - sref).max() <= 1e-12 * np.abs(sref).max(), nm
+        assert np.abs(s32 - sref).max() <= 1e-6 * np.abs(sref).max(), nm
 
 
 def test_assembly_is_bit_reproducible(gpu_lib, oracle):
@@ -147,7 +158,7 @@ def _solve_pair(oracle, m, kind, order, dirichlet, fkw, method, precond, precisi
     gkw = dict(fkw)
     if 'wind_vtx' in fkw:
         gkw['wind_vtx'] = _t(fkw['wind_vtx'])
-    A = fem.Matrix(g, fp32=precision == 'mixed')
+    A = fem.Matrix(g, fp32=precision == 'mixed', jacobi64=precision == 'fp64', jacobi32=precision == 'mixed')
     A.assemble(fem.make_form(**gkw))
     fq = _t(_src_sinprod(g.quad_points(), m.dim))
     b = torch.zeros(g.ndof, dtype=torch.float64, device='cuda')
@@ -249,7 +260,7 @@ def test_reference_fixture_transient_poisson_gpu(gpu_lib, oracle, coarse_mesh, r
     f = fem.make_form(mass=1.0, diff=1.0, dt=dt)
     A = fem.Matrix(g)
     A.assemble(f)
-    sv = fem.KrylovSolver(A, method='CG', tol=1e-13, maxit=1000)
+    sv = fem.KrylovSolver(A, method='CG', tol=1e-12, maxit=1000)
     u = _t(o.project(oracle.SRC_POLY_X1MX, (1.0,)))
     b = torch.zeros_like(u)
     for _ in range(1000):
