@@ -114,7 +114,7 @@ def run_ours(args):
     ndof, nnz = space.ndof, space.nnz
     # each path assembles the Krylov matrix it iterates with (A D^-1 in FP64, or in FP32) in the same
     # pass as the FP64 values used for the residuals
-    mats = {'fp64': fem.Matrix(space, jacobi64=True), 'mixed': fem.Matrix(space, jacobi32=True)}
+    mats = {'fp64': fem.Matrix(space, jacobi64=True), 'mixed': fem.Matrix(space, jacobi32=True, dfloat=True)}
     form = fem.make_form(mass=1.0, diff=EPS, dt=DT, wind=WIND)
     u0 = torch.as_tensor(fem.interpolate_p2(space, gaussian), device='cuda')
     b = torch.zeros(ndof, dtype=torch.float64, device='cuda')
@@ -129,38 +129,55 @@ def run_ours(args):
                                   check_every=args.check_every),
     }
 
-    def step(sv, u_in, u_out, stats):
+    from opencmp_gb300.guess import LearnedGuess
+    guess = LearnedGuess(space, k=4, use_residual=True, seed=0)
+
+    def step(kind, u_in, u_out, stats):
+        sv = solvers['fp64' if kind == 'fp64' else 'mixed']
         sv.mat.assemble(form)
         sv.update()
         fem.assemble_rhs(space, form, fem.make_rhs(dt=DT, mass=1.0, uprev=u_in), b)
-        u_out.copy_(u_in)
+        used = False
+        if kind == 'learned':
+            used = guess.predict(u_out, sv.mat, b)
+        else:
+            u_out.copy_(u_in)
         info = sv.solve(b, u_out)
+        if kind == 'learned':
+            guess.push(u_out)
+            guess.judge(info, used)
         stats.append((info.iterations, info.outer_iterations, info.relres0, info.relres))
 
     def timed(kind, steps, warmup, e2e=False):
-        sv = solvers[kind]
         u = [u0.clone(), torch.empty_like(u0)]
         h_in = torch.empty(ndof, dtype=torch.float64, pin_memory=True)
         h_out = torch.empty(ndof, dtype=torch.float64, pin_memory=True)
         h_in.copy_(u0.cpu())
+        guess.reset()
+        guess.reset_judge()
+        guess.push(u0)
         stats = []
         for k in range(warmup):
-            step(sv, u[k % 2], u[(k + 1) % 2], stats)
+            step(kind, u[k % 2], u[(k + 1) % 2], stats)
         stats.clear()
+        uc = u[warmup % 2]
+        h_in.copy_(uc.cpu())
         torch.cuda.synchronize()
         if world > 1:
             dist.barrier()
         ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         ev0.record()
+        cur = warmup % 2
         for k in range(steps):
             if e2e:
-                u[0].copy_(h_in, non_blocking=True)
-                step(sv, u[0], u[1], stats)
-                h_out.copy_(u[1], non_blocking=True)
+                u[cur].copy_(h_in, non_blocking=True)
+                step(kind, u[cur], u[1 - cur], stats)
+                h_out.copy_(u[1 - cur], non_blocking=True)
                 torch.cuda.current_stream().synchronize()
                 h_in, h_out = h_out, h_in
             else:
-                step(sv, u[k % 2], u[(k + 1) % 2], stats)
+                step(kind, u[cur], u[1 - cur], stats)
+            cur = 1 - cur
         ev1.record()
         torch.cuda.synchronize()
         ms = ev0.elapsed_time(ev1)
@@ -170,12 +187,38 @@ def run_ours(args):
             ms = float(t.item())
         return ms, stats
 
+    # training of the guess network on trajectories the solver produces (not timed): eps drawn
+    # log-uniform in [1e-3, 1e-1] with numpy seed 0, first steps of each run; eps = 1e-2 is held out
+    t_train = time.perf_counter()
+    rng = np.random.default_rng(0)
+    eps_train = [float(10 ** rng.uniform(-3, -1)) for _ in range(args.train_runs)]
+    for eps in eps_train:
+        f_tr = fem.make_form(mass=1.0, diff=eps, dt=DT, wind=WIND)
+        mats['mixed'].assemble(f_tr)
+        solvers['mixed'].update()
+        uu = u0.clone()
+        guess.reset()
+        guess.push(uu)
+        for _ in range(args.train_steps):
+            fem.assemble_rhs(space, f_tr, fem.make_rhs(dt=DT, mass=1.0, uprev=uu), b)
+            xx = uu.clone()
+            solvers['mixed'].solve(b, xx)
+            guess.collect(xx, mats['mixed'], b)
+            guess.push(xx)
+            uu = xx
+    losses = guess.train(steps=args.train_iters, batch=1 << 17, lr=3e-3)
+    guess.drop_samples()
+    torch.cuda.synchronize()
+    train_s = time.perf_counter() - t_train
+
     clocks = Clocks()
     clocks.start()
     ms_plain, st_plain = timed('fp64', args.steps, args.warmup)
-    ms_opt, st_opt = timed('mixed', args.steps, args.warmup)
+    plain_relres0 = [float(np.mean([s[2] for s in st_plain]))]
+    ms_mixed, st_mixed = timed('mixed', args.steps, args.warmup)
+    ms_opt, st_opt = timed('learned', args.steps, args.warmup)
     cl = clocks.stop()
-    ms_e2e, _ = timed('mixed', args.steps, 1, e2e=True)
+    ms_e2e, _ = timed('learned', args.steps, args.warmup, e2e=True)
 
     # SpMV roofline: FP64 CSR SpMV launches timed with CUDA events on the launching stream
     x = torch.randn(ndof, dtype=torch.float64, device='cuda')
@@ -208,12 +251,22 @@ def run_ours(args):
                    'ndof': ndof, 'nnz': nnz, 'parallelism': 'replicas' if world > 1 else 'single GPU',
                    'l2': 'inputs larger than L2 (no flush)'},
         'plain_fp64': {'value': plain, 'unit': 'DOF/s', 'ms_per_step': ms_plain / args.steps,
+                       'relres0_per_step': plain_relres0[0],
                        'iters_per_step': float(np.mean([s[0] for s in st_plain]))},
-        'optimised': {'kind': 'mixed: FP32 inner GMRES + FP64 iterative refinement',
+        'optimised': {'kind': 'double-float (FP32-pair) assembly, learned initial guess (per-dof MLP, trained on '
+                              'the solver\'s own trajectories), FP32 inner GMRES + FP64 iterative refinement',
                       'relres0_per_step': float(np.mean([s[2] for s in st_opt])),
                       'iters_per_step': float(np.mean([s[0] for s in st_opt])),
                       'outer_per_step': float(np.mean([s[1] for s in st_opt])),
-                      'max_relres': float(max(s[3] for s in st_opt)), 'speedup_vs_plain_fp64': value / plain},
+                      'max_relres': float(max(s[3] for s in st_opt)), 'speedup_vs_plain_fp64': value / plain,
+                      'guess_enabled_at_end': bool(guess.enabled), 'guess_fallback': guess.fallback_reason},
+        'mixed_previous_step_guess': {'value': ndof * args.steps * world / (ms_mixed * 1e-3), 'unit': 'DOF/s',
+                                      'ms_per_step': ms_mixed / args.steps,
+                                      'relres0_per_step': float(np.mean([s[2] for s in st_mixed])),
+                                      'iters_per_step': float(np.mean([s[0] for s in st_mixed]))},
+        'guess_training': {'eps': eps_train, 'steps_per_run': args.train_steps, 'adam_steps': args.train_iters,
+                           'loss_first': float(np.mean(losses[:10])), 'loss_last': float(np.mean(losses[-10:])),
+                           'seconds': train_s},
         'e2e': {'value': e2e_val, 'unit': 'DOF/s', 'h2d_bytes_per_step': 8 * ndof, 'd2h_bytes_per_step': 8 * ndof},
         'roofline': {'bound': 'hbm', 'kernel': 'spmv_masked<double> / spmv64 (CSR FP64)', 'achieved': achieved,
                      'peak': peak, 'peak_kind': peak_kind, 'unit': 'GB/s', 'frac': achieved / peak,
@@ -294,6 +347,9 @@ def main():
     ap.add_argument('--inner-tol', type=float, default=1e-4)
     ap.add_argument('--check-every', type=int, default=8)
     ap.add_argument('--no-cpu', action='store_true')
+    ap.add_argument('--train-runs', type=int, default=4)
+    ap.add_argument('--train-steps', type=int, default=50)
+    ap.add_argument('--train-iters', type=int, default=300)
     args = ap.parse_args()
     if args.impl == 'reference':
         run_reference(args)

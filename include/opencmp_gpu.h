@@ -62,6 +62,7 @@ typedef struct ocmp_mesh_s* ocmp_mesh_t;
 typedef struct ocmp_space_s* ocmp_space_t;
 typedef struct ocmp_matrix_s* ocmp_matrix_t;
 typedef struct ocmp_solver_s* ocmp_solver_t;
+typedef struct ocmp_guess_s* ocmp_guess_t;
 
 /* Bilinear form  a(u,v) = mass (u,v) + dt [ diff (grad u, grad v) - (u, w . grad v) ]
  *                        + dt * facet terms selected by the masks (bit l = boundary label l).
@@ -142,8 +143,11 @@ int ocmp_set_boundary(ocmp_space_t space, uint32_t mask, const double* gval_host
 /* ---------------------------------------------------------------- assembly */
 /* Matrix outputs written by each assembly (flags, OR-able). The FP64 values are always written.
  * The Jacobi-scaled values A D^-1 (D = diag A on free rows) are the Krylov matrices the GMRES path
- * uses with the point-Jacobi preconditioner; assembling them in the same pass saves a sweep. */
-enum { OCMP_MAT_FP32 = 1, OCMP_MAT_JACOBI64 = 2, OCMP_MAT_JACOBI32 = 4 };
+ * uses with the point-Jacobi preconditioner; assembling them in the same pass saves a sweep.
+ * OCMP_MAT_DFLOAT assembles the element matrices and their sums in double-float arithmetic (pairs of
+ * FP32 values, about 48 significant bits) on the FP32 pipes, finishing each CSR entry with one FP64
+ * addition; the FP64 values agree with the native FP64 assembly to about 1e-14 relative. */
+enum { OCMP_MAT_FP32 = 1, OCMP_MAT_JACOBI64 = 2, OCMP_MAT_JACOBI32 = 4, OCMP_MAT_DFLOAT = 8 };
 int ocmp_matrix_create(ocmp_space_t space, int32_t flags, ocmp_matrix_t* out);
 int ocmp_matrix_destroy(ocmp_matrix_t mat);
 int ocmp_matrix_values(ocmp_matrix_t mat, double** vals64_dev, float** vals32_dev);
@@ -161,6 +165,38 @@ int ocmp_solver_destroy(ocmp_solver_t solver);
 int ocmp_solver_update(ocmp_solver_t solver, void* stream);
 /* Solve A_ff x_f = (b - A x_D)_f in place; x_dev holds the Dirichlet values and the initial guess. */
 int ocmp_solve(ocmp_solver_t solver, const double* b_dev, double* x_dev, void* stream, ocmp_solve_info_t* info);
+
+/* ---------------------------------------------------------------- learned initial guess
+ * No counterpart in the reference (OpenCMP starts each Krylov solve from the previous step's
+ * solution, base_model.py:925-937). A per-dof MLP  y = w3 . tanh(W2 tanh(W1 x + b1) + b2) + b3 + c . x,
+ * hidden width 32, FP32, predicts (u^{n+1} - u^n) / s_i from features x built by
+ * ocmp_guess_features (the last k-1 solution differences and an optional graph feature, each
+ * divided by the dof's difference norm s_i). Training: ocmp_guess_loss_grad (mean squared error over `rows` samples,
+ * deterministic gradients) + ocmp_guess_adam_step. The solve's FP64 residual test is unchanged,
+ * so the guess never decides the accuracy of the result. */
+int ocmp_guess_create(int32_t n_features, uint64_t seed, ocmp_guess_t* out);
+int ocmp_guess_destroy(ocmp_guess_t g);
+int ocmp_guess_nparams(ocmp_guess_t g);
+int ocmp_guess_params(ocmp_guess_t g, float* host, int32_t set);       /* copy out (set=0) or in (set=1) */
+int ocmp_guess_forward(ocmp_guess_t g, const float* X_dev, int64_t rows, float* Y_dev, void* stream);
+int ocmp_guess_loss_grad(ocmp_guess_t g, const float* X_dev, const float* T_dev, int64_t rows, double* loss_host,
+                         float* grad_host, void* stream);
+int ocmp_guess_adam_step(ocmp_guess_t g, float lr, void* stream);
+/* scale_dev[0] = sqrt(mean((a - b)^2)), computed on the device (no host synchronisation) */
+int ocmp_guess_scale(ocmp_guess_t g, int64_t n, const double* a_dev, const double* b_dev, double* scale_dev,
+                     void* stream);
+/* From the k history vectors h0 = u^n, h1 = u^{n-1}, ...: per dof i the differences d_j = h_j - h_{j+1},
+ * s_i = |(d_0, d_1, ...)|_2 (written to scale_dev, n doubles) and X_i = [d_0, d_1, ..., q_i] / s_i. */
+int ocmp_guess_features(int64_t n, int32_t k, const double* const* hist_dev, const double* q_dev,
+                        double* scale_dev, float* X_dev, int32_t F, void* stream);
+/* training target T_i = clamp((u^{n+1}_i - u^n_i) / s_i, -10, 10) */
+int ocmp_guess_target(int64_t n, const double* unext_dev, const double* un_dev, const double* scale_dev,
+                      float* T_dev, void* stream);
+/* x = u^n + s_i * y_i on free dofs (free_dev may be NULL: all free) */
+int ocmp_guess_apply(int64_t n, const double* un_dev, const float* y_dev, const double* scale_dev,
+                     const uint8_t* free_dev, double* x_dev, void* stream);
+/* q = D^-1 (b - A x) on free dofs (the Jacobi correction of x; the guess network's graph feature) */
+int ocmp_jacobi_residual(ocmp_matrix_t mat, const double* b_dev, const double* x_dev, double* q_dev, void* stream);
 
 /* ---------------------------------------------------------------- allocation-free solve
  * No counterpart in the reference: an addition for callers that cannot call cudaMalloc when they

@@ -88,6 +88,18 @@ SIGNATURES = {
     'ocmp_solver_update': [P, P],
     'ocmp_solve': [P, P, P, P, C.POINTER(SolveInfo)],
     'ocmp_solve_cg_noalloc': [P, P, P, D, I32, P, C.POINTER(SolveInfo)],
+    'ocmp_guess_create': [I32, C.c_uint64, C.POINTER(P)],
+    'ocmp_guess_destroy': [P],
+    'ocmp_guess_nparams': [P],
+    'ocmp_guess_params': [P, P, I32],
+    'ocmp_guess_forward': [P, P, I64, P, P],
+    'ocmp_guess_loss_grad': [P, P, P, I64, P, P, P],
+    'ocmp_guess_adam_step': [P, C.c_float, P],
+    'ocmp_guess_scale': [P, I64, P, P, P, P],
+    'ocmp_guess_features': [I64, I32, P, P, P, P, I32, P],
+    'ocmp_guess_target': [I64, P, P, P, P, P],
+    'ocmp_guess_apply': [I64, P, P, P, P, P, P],
+    'ocmp_jacobi_residual': [P, P, P, P, P],
 }
 
 _lib = None

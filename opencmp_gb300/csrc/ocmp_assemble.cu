@@ -483,6 +483,265 @@ __global__ void __launch_bounds__(128) row_scatter_kernel(
     }
 }
 
+// ---------------------------------------------------------------------------------------------
+// Double-float assembly (OCMP_MAT_DFLOAT). Values are unevaluated sums hi + lo of two floats;
+// products use an FMA-exact error term, sums an exact TwoSum of the high parts. Geometry stays FP64;
+// the element terms and the row sums run on the FP32 pipes, and each CSR entry ends with one FP64
+// add. Floats are widened to doubles with integer operations (exact for normal numbers; subnormal
+// floats, below 1.2e-38, are flushed to zero).
+__device__ __forceinline__ void ff_add(float& sh, float& sl, float ph, float pl) {
+    const float s = __fadd_rn(sh, ph);
+    const float bb = __fsub_rn(s, sh);
+    const float err = __fadd_rn(__fsub_rn(sh, __fsub_rn(s, bb)), __fsub_rn(ph, bb));
+    sl = __fadd_rn(__fadd_rn(sl, pl), err);
+    sh = s;
+}
+__device__ __forceinline__ void ff_mul(float ah, float al, float bh, float bl, float& ph, float& pl) {
+    ph = __fmul_rn(ah, bh);
+    float e = __fmaf_rn(ah, bh, -ph);
+    e = __fmaf_rn(ah, bl, e);
+    pl = __fmaf_rn(al, bh, e);
+}
+__device__ __forceinline__ double f2d_exact(float f) {
+    const uint32_t b = __float_as_uint(f);
+    const uint32_t e = (b >> 23) & 0xffu;
+    const unsigned long long sgn = (unsigned long long)(b & 0x80000000u) << 32;
+    if (e == 0) return __longlong_as_double((long long)sgn);
+    if (e == 0xffu) return (double)f;
+    const unsigned long long d = sgn | ((unsigned long long)(e + 896u) << 52) | ((unsigned long long)(b & 0x7fffffu) << 29);
+    return __longlong_as_double((long long)d);
+}
+__device__ __forceinline__ double ff_to_double(float h, float l) { return f2d_exact(h) + f2d_exact(l); }
+__device__ __forceinline__ float2 ff_split(double x) {
+    const float h = __double2float_rn(x);
+    return make_float2(h, __double2float_rn(x - f2d_exact(h)));
+}
+
+template <int D, int L>
+__global__ void __launch_bounds__(256) elem_matrix_ff_kernel(int64_t ne, const double* __restrict__ X,
+                                                             const int32_t* __restrict__ conn, FormArgs a,
+                                                             const int32_t* __restrict__ toff,
+                                                             const uint8_t* __restrict__ tgg,
+                                                             const float2* __restrict__ tcf, float2* __restrict__ K) {
+    constexpr int NP = D + 1, NS = NP * (NP + 1) / 2, LL = L * L;
+    extern __shared__ float2 Fs2[];
+    const int NTP = blockDim.x + 1, tid = threadIdx.x;
+    const int64_t e = blockIdx.x * (int64_t)blockDim.x + tid;
+    if (e >= ne) return;
+    float2* F = Fs2 + tid;
+    float2* __restrict__ Ke = K + e * LL;
+    {
+    Geo g;
+    double x0[3];
+    element_geo<D>(X, conn, e, g, x0);
+    double gl[NP][3];
+#pragma unroll
+    for (int r = 0; r < D; r++) {
+        double s0 = 0;
+#pragma unroll
+        for (int k = 0; k < D; k++) {
+            gl[k + 1][r] = g.Ji[k][r];
+            s0 += g.Ji[k][r];
+        }
+        gl[0][r] = -s0;
+    }
+    F[0] = ff_split(a.mass * g.adet);
+    const double sd = a.dt * a.diff * g.adet;
+    int pi = 1;
+#pragma unroll
+    for (int p = 0; p < NP; p++)
+#pragma unroll
+        for (int q = p; q < NP; q++, pi++) {
+            double t = 0;
+#pragma unroll
+            for (int r = 0; r < D; r++) t += gl[p][r] * gl[q][r];
+            F[pi * NTP] = ff_split(sd * t);
+        }
+    const double sw = -a.dt * g.adet;
+    if (a.wind_kind == OCMP_WIND_CONST) {
+        const double w[3] = {a.w0, a.w1, a.w2};
+#pragma unroll
+        for (int p = 0; p < NP; p++) {
+            double t = 0;
+#pragma unroll
+            for (int r = 0; r < D; r++) t += w[r] * gl[p][r];
+            F[(1 + NS + p) * NTP] = ff_split(sw * t);
+        }
+    } else if (a.wind_kind == OCMP_WIND_VERTEX) {
+#pragma unroll
+        for (int v = 0; v < NP; v++) {
+            const int32_t gv = conn[e * NP + v];
+            double w[3];
+#pragma unroll
+            for (int r = 0; r < D; r++) w[r] = a.wind_vtx[(int64_t)gv * D + r];
+#pragma unroll
+            for (int p = 0; p < NP; p++) {
+                double t = 0;
+#pragma unroll
+                for (int r = 0; r < D; r++) t += w[r] * gl[p][r];
+                F[(1 + NS + p * NP + v) * NTP] = ff_split(sw * t);
+            }
+        }
+    }
+    const bool um = a.mass != 0.0, us = sd != 0.0, uc = a.wind_kind != OCMP_WIND_NONE;
+    int slot = 0;
+    for (int i = 0; i < L; i++)
+        for (int j = i; j < L; j++, slot++) {
+            const int o0 = __ldg(toff + 4 * slot), o1 = __ldg(toff + 4 * slot + 1), o2 = __ldg(toff + 4 * slot + 2),
+                      o3 = __ldg(toff + 4 * slot + 3), o4 = __ldg(toff + 4 * slot + 4);
+            float sh = 0.f, sl = 0.f;
+            if (um)
+                for (int t = o0; t < o1; t++) {
+                    const float2 f = F[__ldg(tgg + t) * NTP], c = __ldg(tcf + t);
+                    float ph, pl;
+                    ff_mul(f.x, f.y, c.x, c.y, ph, pl);
+                    ff_add(sh, sl, ph, pl);
+                }
+            if (us)
+                for (int t = o1; t < o2; t++) {
+                    const float2 f = F[__ldg(tgg + t) * NTP], c = __ldg(tcf + t);
+                    float ph, pl;
+                    ff_mul(f.x, f.y, c.x, c.y, ph, pl);
+                    ff_add(sh, sl, ph, pl);
+                }
+            float ah = sh, al = sl, bh = sh, bl = sl;
+            if (uc) {
+                for (int t = o2; t < o3; t++) {
+                    const float2 f = F[__ldg(tgg + t) * NTP], c = __ldg(tcf + t);
+                    float ph, pl;
+                    ff_mul(f.x, f.y, c.x, c.y, ph, pl);
+                    ff_add(ah, al, ph, pl);
+                }
+                for (int t = o3; t < o4; t++) {
+                    const float2 f = F[__ldg(tgg + t) * NTP], c = __ldg(tcf + t);
+                    float ph, pl;
+                    ff_mul(f.x, f.y, c.x, c.y, ph, pl);
+                    ff_add(bh, bl, ph, pl);
+                }
+            }
+            Ke[i * L + j] = make_float2(ah, al);
+            if (j != i) Ke[j * L + i] = make_float2(bh, bl);
+        }
+    }
+}
+
+template <int L>
+__global__ void diag_ff_kernel(int64_t nd, const int32_t* __restrict__ inc_ptr, const int32_t* __restrict__ inc,
+                               const float2* __restrict__ K, const uint8_t* __restrict__ freed, int use_facets,
+                               const int32_t* __restrict__ efac_ptr, const int32_t* __restrict__ efac,
+                               const int32_t* __restrict__ ebf_ptr, const int32_t* __restrict__ ebf,
+                               const double* __restrict__ Ki, const double* __restrict__ Kb, double* __restrict__ dinv,
+                               float* __restrict__ dinv32) {
+    const int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (r >= nd) return;
+    float h = 0.f, l = 0.f;
+    for (int32_t k = inc_ptr[r]; k < inc_ptr[r + 1]; k++) {
+        const int64_t flat = inc[k];
+        const int64_t e = flat / L;
+        const int i = (int)(flat % L);
+        const float2 v = K[flat * L + i];
+        ff_add(h, l, v.x, v.y);
+        if (use_facets) {
+            if (efac_ptr)
+                for (int32_t q = efac_ptr[e]; q < efac_ptr[e + 1]; q++) {
+                    const int f = efac[q], side = f & 1;
+                    const int ri = side * L + i;
+                    const float2 w = ff_split(Ki[(int64_t)(f >> 1) * 4 * L * L + ri * 2 * L + ri]);
+                    ff_add(h, l, w.x, w.y);
+                }
+            for (int32_t q = ebf_ptr[e]; q < ebf_ptr[e + 1]; q++) {
+                const float2 w = ff_split(Kb[(int64_t)ebf[q] * L * L + i * L + i]);
+                ff_add(h, l, w.x, w.y);
+            }
+        }
+    }
+    const double d = ff_to_double(h, l);
+    const double di = (freed[r] && d != 0.0) ? 1.0 / d : 0.0;
+    dinv[r] = di;
+    if (dinv32) dinv32[r] = (float)di;
+}
+
+template <int L>
+__global__ void __launch_bounds__(128) row_scatter_ff_kernel(
+    int64_t r0, int64_t r1, const int32_t* __restrict__ rp, const int32_t* __restrict__ col,
+    const int32_t* __restrict__ inc_ptr, const int32_t* __restrict__ inc, const float2* __restrict__ K,
+    const uint8_t* __restrict__ slot, int ss, int use_facets, const int32_t* __restrict__ efac_ptr,
+    const int32_t* __restrict__ efac, const uint8_t* __restrict__ fslot, const int32_t* __restrict__ ebf_ptr,
+    const int32_t* __restrict__ ebf, const double* __restrict__ Ki, const double* __restrict__ Kb,
+    const double* __restrict__ dinv, const float* __restrict__ dinv32, double* __restrict__ vals,
+    float* __restrict__ vals32, double* __restrict__ svals64, float* __restrict__ svals32) {
+    extern __shared__ float2 acc2[];
+    const int NTP = blockDim.x + 1, tid = threadIdx.x;
+    const int64_t r = r0 + blockIdx.x * (int64_t)blockDim.x + tid;
+    if (r >= r1) return;
+    const int32_t base = rp[r], rn = rp[r + 1] - base;
+    float2* __restrict__ ac = acc2 + tid;
+    for (int q = 0; q < rn; q++) ac[q * NTP] = make_float2(0.f, 0.f);
+    const int32_t k0 = inc_ptr[r], k1 = inc_ptr[r + 1];
+    double nkv[L];
+    int nsv[L];
+    int64_t nflat = k0 < k1 ? inc[k0] : 0;
+    if (k0 < k1) load_slice<L>(reinterpret_cast<const double*>(K + nflat * L), slot + nflat * ss, nkv, nsv);
+    for (int32_t k = k0; k < k1; k++) {
+        // the slice of incidence k was loaded in the previous iteration; start loading k + 1
+        const int64_t flat = nflat;
+        double kv[L];
+        int sv[L];
+#pragma unroll
+        for (int j = 0; j < L; j++) {
+            kv[j] = nkv[j];
+            sv[j] = nsv[j];
+        }
+        if (k + 1 < k1) {
+            nflat = inc[k + 1];
+            load_slice<L>(reinterpret_cast<const double*>(K + nflat * L), slot + nflat * ss, nkv, nsv);
+        }
+#pragma unroll
+        for (int j = 0; j < L; j++) {
+            const long long bits = __double_as_longlong(kv[j]);
+            const float vh = __int_as_float((int)(bits & 0xffffffffll)), vl = __int_as_float((int)(bits >> 32));
+            float2 a2 = ac[sv[j] * NTP];
+            ff_add(a2.x, a2.y, vh, vl);
+            ac[sv[j] * NTP] = a2;
+        }
+        if (use_facets) {
+            const int64_t e = flat / L;
+            const int i = (int)(flat % L);
+            if (efac_ptr)
+                for (int32_t q = efac_ptr[e]; q < efac_ptr[e + 1]; q++) {
+                    const int f = efac[q], side = f & 1;
+                    const int64_t fi = f >> 1;
+                    const double* __restrict__ Fr = Ki + fi * 4 * L * L + (int64_t)(side * L + i) * 2 * L;
+                    const uint8_t* __restrict__ fs = fslot + ((fi * 2 + side) * L + i) * 2 * L;
+                    for (int jj = 0; jj < 2 * L; jj++) {
+                        const float2 w = ff_split(__ldg(Fr + jj));
+                        float2 a2 = ac[__ldg(fs + jj) * NTP];
+                        ff_add(a2.x, a2.y, w.x, w.y);
+                        ac[__ldg(fs + jj) * NTP] = a2;
+                    }
+                }
+            for (int32_t q = ebf_ptr[e]; q < ebf_ptr[e + 1]; q++) {
+                const double* __restrict__ Br = Kb + (int64_t)ebf[q] * L * L + i * L;
+                for (int j = 0; j < L; j++) {
+                    const float2 w = ff_split(__ldg(Br + j));
+                    float2 a2 = ac[sv[j] * NTP];
+                    ff_add(a2.x, a2.y, w.x, w.y);
+                    ac[sv[j] * NTP] = a2;
+                }
+            }
+        }
+    }
+    for (int q = 0; q < rn; q++) {
+        const float2 a2 = ac[q * NTP];
+        const double v = ff_to_double(a2.x, a2.y);
+        vals[base + q] = v;
+        const float v32 = __fadd_rn(a2.x, a2.y);
+        if (vals32) vals32[base + q] = v32;
+        if (svals64) svals64[base + q] = v * dinv[col[base + q]];
+        if (svals32) svals32[base + q] = v32 * dinv32[col[base + q]];
+    }
+}
+
 // Element right-hand sides: dt (f, phi_i) + mass (u_prev, phi_i) + boundary data.
 template <int D, int L>
 __global__ void rhs_elem_kernel(int64_t ne, const double* __restrict__ X, const int32_t* __restrict__ conn,
@@ -630,7 +889,17 @@ int assemble_impl(ocmp_matrix_s* m, const ocmp_form_t* f, cudaStream_t st) {
     const int nt = 256;
     const size_t smem = sizeof(double) * (size_t)NG * (nt + 1);
     OCMP_CUDA(cudaFuncSetAttribute(elem_matrix_kernel<D, L>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    elem_matrix_kernel<D, L><<<nblk(ne, nt), nt, smem, st>>>(ne, mesh->dX, mesh->dconn, a, tt, s->d_K);
+    const bool dfl = (m->flags & OCMP_MAT_DFLOAT) != 0;
+    float2* Kff = reinterpret_cast<float2*>(s->d_K);
+    if (dfl) {
+        const int ntf = 256;
+        const size_t smf = sizeof(float2) * (size_t)NG * (ntf + 1);
+        OCMP_CUDA(cudaFuncSetAttribute(elem_matrix_ff_kernel<D, L>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smf));
+        elem_matrix_ff_kernel<D, L><<<nblk(ne, ntf), ntf, smf, st>>>(ne, mesh->dX, mesh->dconn, a, s->d_slot_off[var],
+                                                                    s->d_term_g[var], s->d_term_coef_ff[var], Kff);
+    } else {
+        elem_matrix_kernel<D, L><<<nblk(ne, nt), nt, smem, st>>>(ne, mesh->dX, mesh->dconn, a, tt, s->d_K);
+    }
     // facet matrices
     const bool is_l2 = s->kind == OCMP_L2;
     const bool interior = is_l2 && f->dg && s->nif > 0;
@@ -653,21 +922,32 @@ int assemble_impl(ocmp_matrix_s* m, const ocmp_form_t* f, cudaStream_t st) {
                 s->d_flam, Kb);
     }
     const int32_t* efp = is_l2 ? s->d_efac_ptr : nullptr;
-    if (m->dinv)
+    if (m->dinv && dfl)
+        diag_ff_kernel<L><<<nblk(nd, 256), 256, 0, st>>>(nd, s->d_inc_ptr, s->d_inc, Kff, s->d_free, use_facets, efp,
+                                                         s->d_efac, s->d_ebf_ptr, s->d_ebf, Ki, Kb, m->dinv, m->dinv32);
+    else if (m->dinv)
         diag_kernel<L><<<nblk(nd, 256), 256, 0, st>>>(nd, s->d_inc_ptr, s->d_inc, s->d_K, s->d_free, use_facets, efp,
                                                       s->d_efac, s->d_ebf_ptr, s->d_ebf, Ki, Kb, m->dinv);
     // rows in ranges of similar length (vertex rows, then the rest) so short rows get small stripes
     const int rt = 128;
     OCMP_CUDA(cudaFuncSetAttribute(row_scatter_kernel<L>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                    (int)(sizeof(double) * (size_t)s->maxrow * (rt + 1))));
+    OCMP_CUDA(cudaFuncSetAttribute(row_scatter_ff_kernel<L>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   (int)(sizeof(double) * (size_t)s->maxrow * (rt + 1))));
     for (size_t q = 0; q + 1 < s->row_ranges.size(); q++) {
         const int64_t r0 = s->row_ranges[q], r1 = s->row_ranges[q + 1];
         if (r1 <= r0) continue;
         const size_t rsm = sizeof(double) * (size_t)s->range_maxrow[q] * (rt + 1);
-        row_scatter_kernel<L><<<nblk(r1 - r0, rt), rt, rsm, st>>>(
-            r0, r1, s->d_rowptr, s->d_col, s->d_inc_ptr, s->d_inc, s->d_K, s->d_slot, s->slot_stride, use_facets, efp,
-            s->d_efac, s->d_fslot, s->d_ebf_ptr, s->d_ebf, Ki, Kb, m->dinv, m->vals, m->vals32, m->svals64,
-            m->svals32);
+        if (dfl)
+            row_scatter_ff_kernel<L><<<nblk(r1 - r0, rt), rt, rsm, st>>>(
+                r0, r1, s->d_rowptr, s->d_col, s->d_inc_ptr, s->d_inc, Kff, s->d_slot, s->slot_stride, use_facets,
+                efp, s->d_efac, s->d_fslot, s->d_ebf_ptr, s->d_ebf, Ki, Kb, m->dinv, m->dinv32, m->vals, m->vals32,
+                m->svals64, m->svals32);
+        else
+            row_scatter_kernel<L><<<nblk(r1 - r0, rt), rt, rsm, st>>>(
+                r0, r1, s->d_rowptr, s->d_col, s->d_inc_ptr, s->d_inc, s->d_K, s->d_slot, s->slot_stride, use_facets,
+                efp, s->d_efac, s->d_fslot, s->d_ebf_ptr, s->d_ebf, Ki, Kb, m->dinv, m->vals, m->vals32, m->svals64,
+                m->svals32);
     }
     OCMP_CUDA(cudaGetLastError());
     return OCMP_OK;

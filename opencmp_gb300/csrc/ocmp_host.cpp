@@ -491,7 +491,7 @@ int ocmp_mesh_destroy(ocmp_mesh_t m) {
 static void free_space_device(ocmp_space_s* s) {
     void* ps[] = {s->d_dofs,     s->d_rowptr,   s->d_col,       s->d_free,     s->d_diag,      s->d_slot,
                   s->d_fslot,    s->d_efac_ptr, s->d_efac,      s->d_slot_off[0], s->d_term_g[0], s->d_term_coef[0],
-                  s->d_slot_off[1], s->d_term_g[1], s->d_term_coef[1],
+                  s->d_slot_off[1], s->d_term_g[1], s->d_term_coef[1], s->d_term_coef_ff[0], s->d_term_coef_ff[1],
                   s->d_inc_ptr,  s->d_inc,      s->d_ifac,      s->d_bfac,     s->d_ebf_ptr,   s->d_ebf,
                   s->d_Rc,       s->d_Rv,       s->d_qw,        s->d_qphi,     s->d_mvec,      s->d_fw,
                   s->d_fphi,     s->d_fdphi,    s->d_flam,      s->d_K,        s->d_facetK,    s->d_Fe,
@@ -803,6 +803,13 @@ int ocmp_space_create(ocmp_mesh_t mesh, int32_t kind, int32_t order, uint32_t di
         U(&s->d_slot_off[var], s->T.slot_off[var]);
         U(&s->d_term_g[var], s->T.term_g[var]);
         U(&s->d_term_coef[var], s->T.term_coef[var]);
+        std::vector<float2> ff(s->T.term_coef[var].size());
+        for (size_t t = 0; t < ff.size(); t++) {
+            const double c = s->T.term_coef[var][t];
+            const float hi = (float)c;
+            ff[t] = make_float2(hi, (float)(c - (double)hi));
+        }
+        U(&s->d_term_coef_ff[var], ff);
     }
     U(&s->d_inc_ptr, inc_ptr);
     U(&s->d_inc, inc);
@@ -909,6 +916,7 @@ int ocmp_matrix_create(ocmp_space_t s, int32_t flags, ocmp_matrix_t* out) {
     if (!st && (flags & OCMP_MAT_JACOBI64)) st = dalloc(&m->svals64, (size_t)s->nnz);
     if (!st && (flags & OCMP_MAT_JACOBI32)) st = dalloc(&m->svals32, (size_t)s->nnz);
     if (!st && (flags & (OCMP_MAT_JACOBI64 | OCMP_MAT_JACOBI32))) st = dalloc(&m->dinv, (size_t)s->ndof);
+    if (!st && (flags & OCMP_MAT_JACOBI32)) st = dalloc(&m->dinv32, (size_t)s->ndof);
     if (!st) st = cudaMemset(m->vals, 0, sizeof(double) * s->nnz) == cudaSuccess ? 0 : OCMP_ERR_CUDA;
     if (st) {
         dfree(m->vals);
@@ -916,6 +924,7 @@ int ocmp_matrix_create(ocmp_space_t s, int32_t flags, ocmp_matrix_t* out) {
         dfree(m->svals64);
         dfree(m->svals32);
         dfree(m->dinv);
+        dfree(m->dinv32);
         delete m;
         return st;
     }
@@ -930,6 +939,7 @@ int ocmp_matrix_destroy(ocmp_matrix_t m) {
     dfree(m->svals64);
     dfree(m->svals32);
     dfree(m->dinv);
+    dfree(m->dinv32);
     delete m;
     return OCMP_OK;
 }

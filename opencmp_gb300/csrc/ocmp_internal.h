@@ -104,6 +104,7 @@ struct ocmp_space_s {
     int32_t* d_slot_off[2] = {nullptr, nullptr};
     uint8_t* d_term_g[2] = {nullptr, nullptr};
     double* d_term_coef[2] = {nullptr, nullptr};
+    float2* d_term_coef_ff[2] = {nullptr, nullptr};  // the same coefficients as (hi, lo) float pairs
     int slot_stride = 0;            // bytes per (element, local row) in d_slot (nloc rounded to 16)
     int maxrow = 0;                 // longest CSR row
     std::vector<int64_t> row_ranges;  // row ranges of similar length (vertex rows, the rest)
@@ -126,7 +127,7 @@ struct ocmp_space_s {
     double* d_fdphi = nullptr;
     double* d_flam = nullptr;
     // scratch owned by the space
-    double* d_K = nullptr;          // ne*nloc^2 element matrices
+    double* d_K = nullptr;          // ne*nloc^2 element matrices (FP64, or (hi, lo) float pairs)
     double* d_facetK = nullptr;     // nif*(2 nloc)^2 + nbf*nloc^2 facet matrices
     double* d_Fe = nullptr;         // ne*nloc element right-hand sides
 };
@@ -142,6 +143,7 @@ struct ocmp_matrix_s {
     double* svals64 = nullptr;
     float* svals32 = nullptr;
     double* dinv = nullptr;
+    float* dinv32 = nullptr;        // FP32 copy of D^-1 (double-float assembly with FP32 scaled output)
 };
 
 namespace ocmp {

@@ -149,18 +149,21 @@ def make_rhs(dt=1.0, src_const=None, src_qp: Optional[torch.Tensor] = None, mass
     return r
 
 
-MAT_FP32, MAT_JACOBI64, MAT_JACOBI32 = 1, 2, 4
+MAT_FP32, MAT_JACOBI64, MAT_JACOBI32, MAT_DFLOAT = 1, 2, 4, 8
 
 
 class Matrix:
     """Assembled sparse matrix in the space's CSR pattern: FP64 values, and optionally an FP32 copy
     (``fp32``) and the Jacobi-scaled Krylov matrices A D^-1 in FP64 / FP32 (``jacobi64`` /
-    ``jacobi32``) written by the same assembly pass."""
+    ``jacobi32``) written by the same assembly pass. ``dfloat`` assembles in double-float arithmetic
+    on the FP32 pipes (about 1e-14 relative to the native FP64 assembly)."""
 
-    def __init__(self, space: Space, fp32: bool = False, jacobi64: bool = False, jacobi32: bool = False):
+    def __init__(self, space: Space, fp32: bool = False, jacobi64: bool = False, jacobi32: bool = False,
+                 dfloat: bool = False):
         self.space = space
         h = C.c_void_p()
-        flags = (MAT_FP32 if fp32 else 0) | (MAT_JACOBI64 if jacobi64 else 0) | (MAT_JACOBI32 if jacobi32 else 0)
+        flags = (MAT_FP32 if fp32 else 0) | (MAT_JACOBI64 if jacobi64 else 0) | (MAT_JACOBI32 if jacobi32 else 0) \
+            | (MAT_DFLOAT if dfloat else 0)
         LB.call('ocmp_matrix_create', space.h, flags, C.byref(h))
         self.h = h
         self.fp32 = fp32
