@@ -121,6 +121,7 @@ def run_ours(args):
     for M_ in mats.values():
         M_.assemble(form)
     A = mats['fp64']
+    tuned = A.autotune()
     solvers = {
         'fp64': fem.KrylovSolver(mats['fp64'], method='GMRES', restart=args.restart, precond='jacobi',
                                  precision='fp64', tol=1e-8, maxit=2000, check_every=args.check_every),
@@ -271,6 +272,7 @@ def run_ours(args):
         'roofline': {'bound': 'hbm', 'kernel': 'spmv_masked<double> / spmv64 (CSR FP64)', 'achieved': achieved,
                      'peak': peak, 'peak_kind': peak_kind, 'unit': 'GB/s', 'frac': achieved / peak,
                      'traffic': None, 'algorithmic_bytes': spmv_bytes, 'avg_launch_ms': spmv_ms},
+        'autotune': tuned,
         'gpu_launches': None,
         'clocks': cl,
         'setup_s': setup_s,
@@ -281,6 +283,110 @@ def run_ours(args):
         print(json.dumps(line), flush=True)
     if world > 1:
         dist.destroy_process_group()
+
+
+def run_batched(args):
+    """512 independent steady 2D convection-diffusion problems (one step = assemble + solve all)."""
+    import concurrent.futures as cf
+    import torch
+    from opencmp_gb300 import fem, mesh as M, build
+    build.build()
+    torch.cuda.set_device(0)
+    rng = np.random.default_rng(0)
+    N = args.instances
+    ns = rng.choice([16, 32, 64, 128], N)
+    ps = rng.choice([1, 2, 3], N)
+    eps = 10 ** rng.uniform(-3, 0, N)
+    ang = rng.uniform(0, 2 * np.pi, N)
+    classes = {}
+    for q in range(N):
+        classes.setdefault((int(ns[q]), int(ps[q])), []).append(q)
+    tol = 1e-8
+    C = []
+    for (n, p), idx in sorted(classes.items()):
+        m = M.unit_square(n)
+        sp = fem.Space(m, 'H1', p, m.bc_names)
+        forms = [fem.make_form(diff=float(eps[q]), dt=1.0, wind=(float(np.cos(ang[q])), float(np.sin(ang[q]))))
+                 for q in idx]
+        A = fem.Matrix(sp, batch=len(idx), jacobi32=True)
+        A1t = fem.Matrix(sp)
+        A1t.assemble(forms[0])
+        A1t.autotune()
+        b1 = torch.zeros(sp.ndof, dtype=torch.float64, device='cuda')
+        fem.assemble_rhs(sp, forms[0], fem.make_rhs(src_const=1.0), b1)
+        sv = fem.KrylovSolver(A, method='GMRES', restart=args.restart_batch, precision='mixed', tol=tol,
+                              maxit=20000, inner_tol=1e-4)
+        sv.set_graph(True)
+        C.append(dict(n=n, p=p, idx=idx, space=sp, forms=forms, A=A, b=b1.repeat(len(idx)),
+                      x=torch.zeros(len(idx) * sp.ndof, dtype=torch.float64, device='cuda'), sv=sv,
+                      stream=torch.cuda.Stream()))
+    total_dofs = sum(c['space'].ndof * len(c['idx']) for c in C)
+
+    def run_class(c):
+        with torch.cuda.stream(c['stream']):
+            c['A'].assemble_batch(c['forms'], stream=c['stream'])
+            c['sv'].update(stream=c['stream'])
+            c['x'].zero_()
+            return c['sv'].solve_batch(c['b'], c['x'], stream=c['stream'])
+
+    pool = cf.ThreadPoolExecutor(max_workers=len(C))
+
+    def batched_step():
+        res = list(pool.map(run_class, C))
+        torch.cuda.synchronize()
+        return res
+
+    # plain FP64 loop over instances: one matrix, one GMRES solve at a time
+    plain = []
+    for c in C:
+        A1 = fem.Matrix(c['space'], jacobi64=True)
+        sv1 = fem.KrylovSolver(A1, method='GMRES', restart=args.restart_batch, precision='fp64', tol=tol,
+                               maxit=20000)
+        plain.append((c, A1, sv1, torch.zeros(c['space'].ndof, dtype=torch.float64, device='cuda')))
+
+    def plain_step():
+        infos = []
+        for c, A1, sv1, x1 in plain:
+            b1 = c['b'][:c['space'].ndof]
+            for f in c['forms']:
+                A1.assemble(f)
+                sv1.update()
+                x1.zero_()
+                infos.append(sv1.solve(b1, x1))
+        torch.cuda.synchronize()
+        return infos
+
+    for _ in range(args.warmup):
+        batched_step()
+    plain_step()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        res = batched_step()
+    t_b = (time.perf_counter() - t0) / args.steps
+    t0 = time.perf_counter()
+    psteps = max(1, min(args.steps, 3))
+    for _ in range(psteps):
+        pinf = plain_step()
+    t_p = (time.perf_counter() - t0) / psteps
+    infos = [i for r in res for i in r]
+    line = {'metric': METRIC + ' (batched instances)', 'value': total_dofs / t_b, 'unit': 'DOF/s', 'n_gpus': 1,
+            'steps': args.steps, 'warmup': args.warmup, 'ms_per_step': t_b * 1e3, 'higher_is_better': True,
+            'scaling': 'weak', 'vs_baseline': None, 'dtype': 'f64+f32', 'data': 'synthetic',
+            'config': {'workload': '{} steady 2D convection-diffusion instances, n in {{16,32,64,128}}, H1 p in {{1,2,3}}, '
+                                   'eps log-uniform [1e-3,1], |w|=1, f=1, Dirichlet 0, seed 0; GMRES({}) + Jacobi to '
+                                   '1e-8'.format(N, args.restart_batch),
+                       'classes': len(C), 'total_dofs': total_dofs},
+            'optimised': {'kind': 'batched kernels per (mesh, order) class, one stream per class, FP32 inner GMRES + '
+                                  'FP64 refinement, restart cycles replayed from CUDA graphs',
+                          'max_relres': float(max(i.relres for i in infos)),
+                          'converged': int(sum(1 for i in infos if i.status == 0)),
+                          'iters_mean': float(np.mean([i.iterations for i in infos]))},
+            'plain_fp64': {'value': total_dofs / t_p, 'unit': 'DOF/s', 'ms_per_step': t_p * 1e3,
+                           'kind': 'loop over instances, FP64 GMRES',
+                           'converged': int(sum(1 for i in pinf if i.status == 0)),
+                           'iters_mean': float(np.mean([i.iterations for i in pinf]))},
+            'speedup_vs_plain_fp64': t_p / t_b}
+    print(json.dumps(line), flush=True)
 
 
 def cpu_step_sample(n_cpu, steps):
@@ -347,12 +453,17 @@ def main():
     ap.add_argument('--inner-tol', type=float, default=1e-4)
     ap.add_argument('--check-every', type=int, default=8)
     ap.add_argument('--no-cpu', action='store_true')
+    ap.add_argument('--config', default='transient3d', choices=['transient3d', 'batched'])
+    ap.add_argument('--instances', type=int, default=512)
+    ap.add_argument('--restart-batch', type=int, default=50)
     ap.add_argument('--train-runs', type=int, default=4)
     ap.add_argument('--train-steps', type=int, default=50)
     ap.add_argument('--train-iters', type=int, default=300)
     args = ap.parse_args()
     if args.impl == 'reference':
         run_reference(args)
+    elif args.config == 'batched':
+        run_batched(args)
     else:
         run_ours(args)
 

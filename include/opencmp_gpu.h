@@ -149,6 +149,9 @@ int ocmp_set_boundary(ocmp_space_t space, uint32_t mask, const double* gval_host
  * addition; the FP64 values agree with the native FP64 assembly to about 1e-14 relative. */
 enum { OCMP_MAT_FP32 = 1, OCMP_MAT_JACOBI64 = 2, OCMP_MAT_JACOBI32 = 4, OCMP_MAT_DFLOAT = 8 };
 int ocmp_matrix_create(ocmp_space_t space, int32_t flags, ocmp_matrix_t* out);
+/* nbatch independent matrices on the space's pattern (instances of a batch of problems that differ
+ * only in their coefficients); values are stored instance after instance. */
+int ocmp_matrix_create_batch(ocmp_space_t space, int32_t nbatch, int32_t flags, ocmp_matrix_t* out);
 int ocmp_matrix_destroy(ocmp_matrix_t mat);
 int ocmp_matrix_values(ocmp_matrix_t mat, double** vals64_dev, float** vals32_dev);
 /* Device pointers of the Jacobi-scaled values A D^-1 (FP64, FP32) and of D^-1 (NULL if not built). */
@@ -156,7 +159,14 @@ int ocmp_matrix_scaled_values(ocmp_matrix_t mat, double** svals64_dev, float** s
 int ocmp_assemble_matrix(ocmp_matrix_t mat, const ocmp_form_t* form, void* stream);
 int ocmp_assemble_rhs(ocmp_space_t space, const ocmp_form_t* form, const ocmp_rhs_t* rhs, double* b_dev,
                       void* stream);
+/* forms: host array of the matrix's nbatch forms (one per instance) */
+int ocmp_assemble_matrix_batch(ocmp_matrix_t mat, const ocmp_form_t* forms, void* stream);
 int ocmp_spmv(ocmp_matrix_t mat, const double* x_dev, double* y_dev, void* stream);
+/* Autotuner: times the CSR SpMV of `mat` (x, y: ndof scratch vectors) for each built pair of threads
+ * per row and loads in flight per thread, keeps the fastest for every kernel of the space that runs
+ * rows (SpMV, residuals, GMRES), and reports it. */
+int ocmp_matrix_autotune(ocmp_matrix_t mat, const double* x_dev, double* y_dev, void* stream, int32_t* tpr,
+                         int32_t* unroll, float* ms);
 
 /* ---------------------------------------------------------------- Krylov solve */
 int ocmp_solver_create(ocmp_matrix_t mat, const ocmp_solve_params_t* params, ocmp_solver_t* out);
@@ -165,6 +175,15 @@ int ocmp_solver_destroy(ocmp_solver_t solver);
 int ocmp_solver_update(ocmp_solver_t solver, void* stream);
 /* Solve A_ff x_f = (b - A x_D)_f in place; x_dev holds the Dirichlet values and the initial guess. */
 int ocmp_solve(ocmp_solver_t solver, const double* b_dev, double* x_dev, void* stream, ocmp_solve_info_t* info);
+/* GMRES on all nbatch systems of a batched matrix at once (b, x: nbatch vectors of ndof, instance
+ * after instance; infos: nbatch entries). Each system has its own Krylov space, Hessenberg matrix,
+ * tolerance test and restart count; the kernels cover every instance in one launch (instance =
+ * blockIdx.y) and instances that have converged return immediately. */
+int ocmp_solve_batch(ocmp_solver_t solver, const double* b_dev, double* x_dev, void* stream,
+                     ocmp_solve_info_t* infos);
+/* Replay each GMRES restart cycle (m iterations, the x update and the next FP64 residual) from a
+ * CUDA graph captured on first use (re-captured when b, x or the stream change). */
+int ocmp_solver_set_graph(ocmp_solver_t solver, int32_t on);
 
 /* ---------------------------------------------------------------- learned initial guess
  * No counterpart in the reference (OpenCMP starts each Krylov solve from the previous step's

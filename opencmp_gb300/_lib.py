@@ -77,12 +77,17 @@ SIGNATURES = {
     'ocmp_space_quad_points': [P, P],
     'ocmp_set_boundary': [P, U32, P, P, P],
     'ocmp_matrix_create': [P, I32, C.POINTER(P)],
+    'ocmp_matrix_create_batch': [P, I32, I32, C.POINTER(P)],
+    'ocmp_assemble_matrix_batch': [P, P, P],
+    'ocmp_solve_batch': [P, P, P, P, P],
+    'ocmp_solver_set_graph': [P, I32],
     'ocmp_matrix_destroy': [P],
     'ocmp_matrix_values': [P, C.POINTER(P), C.POINTER(P)],
     'ocmp_matrix_scaled_values': [P, C.POINTER(P), C.POINTER(P), C.POINTER(P)],
     'ocmp_assemble_matrix': [P, C.POINTER(Form), P],
     'ocmp_assemble_rhs': [P, C.POINTER(Form), C.POINTER(Rhs), P, P],
     'ocmp_spmv': [P, P, P, P],
+    'ocmp_matrix_autotune': [P, P, P, P, P, P, P],
     'ocmp_solver_create': [P, C.POINTER(SolveParams), C.POINTER(P)],
     'ocmp_solver_destroy': [P],
     'ocmp_solver_update': [P, P],

@@ -1061,6 +1061,54 @@ int launch_set_boundary(ocmp_space_s* s, uint32_t mask, const double* gval, doub
     return OCMP_OK;
 }
 
+// Autotuner: times the FP64 SpMV for every built (threads per row, unroll) pair on this matrix with
+// CUDA events (warm-up launch, then `reps` timed launches each) and records the fastest in the
+// space; every kernel built on the row kernel then uses it.
+int autotune_spmv(ocmp_space_s* s, const double* vals, const double* x, double* y, cudaStream_t st, int reps,
+                  int* best_tpr, int* best_u, float* best_ms) {
+    static const int cand[][2] = {{2, 4}, {4, 4}, {4, 8}, {8, 4}, {8, 8}, {16, 8}};
+    cudaEvent_t e0, e1;
+    OCMP_CUDA(cudaEventCreate(&e0));
+    OCMP_CUDA(cudaEventCreate(&e1));
+    float best = 1e30f;
+    int bt = 4, bu = 8;
+    const int64_t n = s->ndof;
+    for (const auto& c : cand) {
+        const int tpr = c[0], u = c[1];
+        const unsigned g = nblk(n * tpr, 256);
+        auto launch = [&]() {
+            if (tpr == 2) spmv64_kernel<2, 4><<<g, 256, 0, st>>>(n, s->d_rowptr, s->d_col, vals, x, y);
+            else if (tpr == 4 && u == 4) spmv64_kernel<4, 4><<<g, 256, 0, st>>>(n, s->d_rowptr, s->d_col, vals, x, y);
+            else if (tpr == 4) spmv64_kernel<4, 8><<<g, 256, 0, st>>>(n, s->d_rowptr, s->d_col, vals, x, y);
+            else if (tpr == 8 && u == 4) spmv64_kernel<8, 4><<<g, 256, 0, st>>>(n, s->d_rowptr, s->d_col, vals, x, y);
+            else if (tpr == 8) spmv64_kernel<8, 8><<<g, 256, 0, st>>>(n, s->d_rowptr, s->d_col, vals, x, y);
+            else spmv64_kernel<16, 8><<<g, 256, 0, st>>>(n, s->d_rowptr, s->d_col, vals, x, y);
+        };
+        launch();
+        OCMP_CUDA(cudaEventRecord(e0, st));
+        for (int r = 0; r < reps; r++) launch();
+        OCMP_CUDA(cudaEventRecord(e1, st));
+        OCMP_CUDA(cudaEventSynchronize(e1));
+        float ms = 0;
+        OCMP_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+        ms /= reps;
+        if (ms < best) {
+            best = ms;
+            bt = tpr;
+            bu = u;
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    OCMP_CUDA(cudaGetLastError());
+    s->tuned_tpr = bt;
+    s->tuned_u = bu;
+    if (best_tpr) *best_tpr = bt;
+    if (best_u) *best_u = bu;
+    if (best_ms) *best_ms = best;
+    return OCMP_OK;
+}
+
 int launch_spmv64(const ocmp_space_s* s, const double* vals, const double* x, double* y, cudaStream_t st) {
     const RowCfg rc = row_cfg(s);
     const int64_t n = s->ndof;
@@ -1068,6 +1116,7 @@ int launch_spmv64(const ocmp_space_s* s, const double* vals, const double* x, do
     if (rc.tpr == 2) spmv64_kernel<2, 4><<<g, 256, 0, st>>>(n, s->d_rowptr, s->d_col, vals, x, y);
     else if (rc.tpr == 4 && rc.u == 4) spmv64_kernel<4, 4><<<g, 256, 0, st>>>(n, s->d_rowptr, s->d_col, vals, x, y);
     else if (rc.tpr == 4) spmv64_kernel<4, 8><<<g, 256, 0, st>>>(n, s->d_rowptr, s->d_col, vals, x, y);
+    else if (rc.tpr == 8 && rc.u == 4) spmv64_kernel<8, 4><<<g, 256, 0, st>>>(n, s->d_rowptr, s->d_col, vals, x, y);
     else if (rc.tpr == 8) spmv64_kernel<8, 8><<<g, 256, 0, st>>>(n, s->d_rowptr, s->d_col, vals, x, y);
     else spmv64_kernel<16, 8><<<g, 256, 0, st>>>(n, s->d_rowptr, s->d_col, vals, x, y);
     OCMP_CUDA(cudaGetLastError());

@@ -512,6 +512,7 @@ int ocmp_jacobi_residual(ocmp_matrix_t mat, const double* b, const double* x, do
     if (rc.tpr == 2) JR(2, 4);
     else if (rc.tpr == 4 && rc.u == 4) JR(4, 4);
     else if (rc.tpr == 4) JR(4, 8);
+    else if (rc.tpr == 8 && rc.u == 4) JR(8, 4);
     else if (rc.tpr == 8) JR(8, 8);
     else JR(16, 8);
 #undef JR

@@ -906,18 +906,20 @@ int ocmp_set_boundary(ocmp_space_t s, uint32_t mask, const double* gval, double*
     return launch_set_boundary(s, mask, gval, u, (cudaStream_t)stream);
 }
 
-int ocmp_matrix_create(ocmp_space_t s, int32_t flags, ocmp_matrix_t* out) {
-    if (!s || !out) return fail(OCMP_ERR_ARG, "ocmp_matrix_create: null argument");
+int ocmp_matrix_create_batch(ocmp_space_t s, int32_t nbatch, int32_t flags, ocmp_matrix_t* out) {
+    if (!s || !out || nbatch < 1) return fail(OCMP_ERR_ARG, "ocmp_matrix_create: bad argument");
     auto* m = new ocmp_matrix_s();
     m->space = s;
     m->flags = flags;
-    int st = dalloc(&m->vals, (size_t)s->nnz);
-    if (!st && (flags & OCMP_MAT_FP32)) st = dalloc(&m->vals32, (size_t)s->nnz);
-    if (!st && (flags & OCMP_MAT_JACOBI64)) st = dalloc(&m->svals64, (size_t)s->nnz);
-    if (!st && (flags & OCMP_MAT_JACOBI32)) st = dalloc(&m->svals32, (size_t)s->nnz);
-    if (!st && (flags & (OCMP_MAT_JACOBI64 | OCMP_MAT_JACOBI32))) st = dalloc(&m->dinv, (size_t)s->ndof);
-    if (!st && (flags & OCMP_MAT_JACOBI32)) st = dalloc(&m->dinv32, (size_t)s->ndof);
-    if (!st) st = cudaMemset(m->vals, 0, sizeof(double) * s->nnz) == cudaSuccess ? 0 : OCMP_ERR_CUDA;
+    m->B = nbatch;
+    const size_t nz = (size_t)s->nnz * nbatch, nd = (size_t)s->ndof * nbatch;
+    int st = dalloc(&m->vals, nz);
+    if (!st && (flags & OCMP_MAT_FP32)) st = dalloc(&m->vals32, nz);
+    if (!st && (flags & OCMP_MAT_JACOBI64)) st = dalloc(&m->svals64, nz);
+    if (!st && (flags & OCMP_MAT_JACOBI32)) st = dalloc(&m->svals32, nz);
+    if (!st && (flags & (OCMP_MAT_JACOBI64 | OCMP_MAT_JACOBI32))) st = dalloc(&m->dinv, nd);
+    if (!st && (flags & OCMP_MAT_JACOBI32)) st = dalloc(&m->dinv32, nd);
+    if (!st) st = cudaMemset(m->vals, 0, sizeof(double) * nz) == cudaSuccess ? 0 : OCMP_ERR_CUDA;
     if (st) {
         dfree(m->vals);
         dfree(m->vals32);
@@ -930,6 +932,10 @@ int ocmp_matrix_create(ocmp_space_t s, int32_t flags, ocmp_matrix_t* out) {
     }
     *out = m;
     return OCMP_OK;
+}
+
+int ocmp_matrix_create(ocmp_space_t s, int32_t flags, ocmp_matrix_t* out) {
+    return ocmp_matrix_create_batch(s, 1, flags, out);
 }
 
 int ocmp_matrix_destroy(ocmp_matrix_t m) {
@@ -961,15 +967,44 @@ int ocmp_matrix_scaled_values(ocmp_matrix_t m, double** s64, float** s32, double
 
 int ocmp_assemble_matrix(ocmp_matrix_t m, const ocmp_form_t* f, void* stream) {
     if (!m || !f) return fail(OCMP_ERR_ARG, "ocmp_assemble_matrix: null argument");
+    if (m->B != 1) return fail(OCMP_ERR_ARG, "ocmp_assemble_matrix: batched matrix, use ocmp_assemble_matrix_batch");
     if (f->wind_kind == OCMP_WIND_VERTEX && !f->wind_vtx)
         return fail(OCMP_ERR_ARG, "ocmp_assemble_matrix: per-vertex wind needs wind_vtx");
     return launch_assemble_matrix(m, f, (cudaStream_t)stream);
+}
+
+int ocmp_assemble_matrix_batch(ocmp_matrix_t m, const ocmp_form_t* forms, void* stream) {
+    if (!m || !forms) return fail(OCMP_ERR_ARG, "ocmp_assemble_matrix_batch: null argument");
+    const ocmp_space_s* s = m->space;
+    for (int q = 0; q < m->B; q++) {
+        if (forms[q].wind_kind == OCMP_WIND_VERTEX && !forms[q].wind_vtx)
+            return fail(OCMP_ERR_ARG, "ocmp_assemble_matrix_batch: per-vertex wind needs wind_vtx");
+        // a single-instance view of instance q
+        ocmp_matrix_s v;
+        v.space = m->space;
+        v.flags = m->flags;
+        v.vals = m->vals + q * s->nnz;
+        v.vals32 = m->vals32 ? m->vals32 + q * s->nnz : nullptr;
+        v.svals64 = m->svals64 ? m->svals64 + q * s->nnz : nullptr;
+        v.svals32 = m->svals32 ? m->svals32 + q * s->nnz : nullptr;
+        v.dinv = m->dinv ? m->dinv + q * s->ndof : nullptr;
+        v.dinv32 = m->dinv32 ? m->dinv32 + q * s->ndof : nullptr;
+        const int st = launch_assemble_matrix(&v, &forms[q], (cudaStream_t)stream);
+        if (st) return st;
+    }
+    return OCMP_OK;
 }
 
 int ocmp_assemble_rhs(ocmp_space_t s, const ocmp_form_t* f, const ocmp_rhs_t* r, double* b, void* stream) {
     if (!s || !f || !r || !b) return fail(OCMP_ERR_ARG, "ocmp_assemble_rhs: null argument");
     if (r->src_kind == OCMP_SRC_QP && !r->src_qp) return fail(OCMP_ERR_ARG, "ocmp_assemble_rhs: src_qp is null");
     return launch_assemble_rhs(s, f, r, b, (cudaStream_t)stream);
+}
+
+int ocmp_matrix_autotune(ocmp_matrix_t m, const double* x, double* y, void* stream, int32_t* tpr, int32_t* unroll,
+                         float* ms) {
+    if (!m || !x || !y) return fail(OCMP_ERR_ARG, "ocmp_matrix_autotune: null argument");
+    return autotune_spmv(m->space, m->vals, x, y, (cudaStream_t)stream, 10, tpr, unroll, ms);
 }
 
 int ocmp_spmv(ocmp_matrix_t m, const double* x, double* y, void* stream) {

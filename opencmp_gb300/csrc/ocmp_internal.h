@@ -107,6 +107,7 @@ struct ocmp_space_s {
     float2* d_term_coef_ff[2] = {nullptr, nullptr};  // the same coefficients as (hi, lo) float pairs
     int slot_stride = 0;            // bytes per (element, local row) in d_slot (nloc rounded to 16)
     int maxrow = 0;                 // longest CSR row
+    int tuned_tpr = 0, tuned_u = 0; // SpMV row configuration chosen by ocmp_matrix_autotune (0: default)
     std::vector<int64_t> row_ranges;  // row ranges of similar length (vertex rows, the rest)
     std::vector<int> range_maxrow;
     int32_t* d_inc_ptr = nullptr;   // ndof+1: dof -> (element, local) incidence
@@ -138,6 +139,7 @@ struct ocmp_space_s {
 struct ocmp_matrix_s {
     ocmp_space_s* space = nullptr;
     int flags = 0;
+    int B = 1;                      // instances (independent matrices on the same pattern)
     double* vals = nullptr;
     float* vals32 = nullptr;
     double* svals64 = nullptr;
@@ -152,4 +154,6 @@ int launch_assemble_matrix(ocmp_matrix_s* m, const ocmp_form_t* f, cudaStream_t 
 int launch_assemble_rhs(ocmp_space_s* s, const ocmp_form_t* f, const ocmp_rhs_t* r, double* b, cudaStream_t st);
 int launch_set_boundary(ocmp_space_s* s, uint32_t mask, const double* gval, double* u, cudaStream_t st);
 int launch_spmv64(const ocmp_space_s* s, const double* vals, const double* x, double* y, cudaStream_t st);
+int autotune_spmv(ocmp_space_s* s, const double* vals, const double* x, double* y, cudaStream_t st, int reps,
+                  int* best_tpr, int* best_u, float* best_ms);
 }  // namespace ocmp

@@ -22,6 +22,14 @@
 #include "ocmp_internal.h"
 #include "ocmp_spmv.cuh"
 
+namespace ocmp {
+// Per-instance strides of a batch of independent systems that share one sparsity pattern: the
+// instance is blockIdx.y; a single system uses zero strides and gridDim.y = 1.
+struct Bat {
+    int64_t n, nnz, V, part, st, flags, scale, H, red, cnt;
+};
+}  // namespace ocmp
+
 struct ocmp_solver_s {
     ocmp_matrix_s* mat = nullptr;
     ocmp_space_s* s = nullptr;
@@ -63,6 +71,15 @@ struct ocmp_solver_s {
     double* scale = nullptr;    // basis scales: v_k = scale[k] * V[k]
     unsigned* cnt = nullptr;    // last-block counters (zero between launches)
     int grid = 0;               // persistent grid of the fused kernels
+    int B = 1;                  // systems in the batch (matrix instances)
+    ocmp::Bat bat{};            // per-instance strides
+    bool use_graph = false;     // replay each restart cycle from a captured CUDA graph
+    cudaGraphExec_t gexec = nullptr;
+    cudaStream_t gstream = nullptr;   // capture/launch stream when the caller passes the default stream
+    cudaEvent_t gev[2] = {nullptr, nullptr};
+    const double* g_b = nullptr;
+    const double* g_x = nullptr;
+    cudaStream_t g_stream = nullptr;
 };
 
 namespace ocmp {
@@ -573,7 +590,8 @@ int residual64(const Ctx& c, const double* b, const double* x, double* dst) {
 }
 
 int read_flags(const Ctx& c) {
-    OCMP_CUDA(cudaMemcpyAsync(c.sv->hflags, c.sv->flags, sizeof(int) * F_NFLAG, cudaMemcpyDeviceToHost, c.st));
+    OCMP_CUDA(cudaMemcpyAsync(c.sv->hflags, c.sv->flags, sizeof(int) * F_NFLAG * c.sv->B, cudaMemcpyDeviceToHost,
+                              c.st));
     OCMP_CUDA(cudaStreamSynchronize(c.st));
     return OCMP_OK;
 }
@@ -721,7 +739,20 @@ __global__ void __launch_bounds__(256) gm_resid(int64_t n, const int32_t* __rest
                                                 double* __restrict__ part, unsigned* __restrict__ cnt, double* st,
                                                 int* flags, double* scale, double* csg, int m, int mode,
                                                 const int32_t* __restrict__ lift_ptr,
-                                                const int32_t* __restrict__ lift_pos) {
+                                                const int32_t* __restrict__ lift_pos, Bat bt) {
+    const int64_t ib = blockIdx.y;
+    A += ib * bt.nnz;
+    b += ib * bt.n;
+    x += ib * bt.n;
+    if (V0) V0 += ib * bt.V;
+    part += ib * bt.part;
+    cnt += ib * bt.cnt;
+    st += ib * bt.st;
+    flags += ib * bt.flags;
+    scale += ib * bt.scale;
+    csg += ib * bt.H;
+    if (mode == 1 && flags[F_OUTER]) return;  // this instance has converged
+
     constexpr int RT = 256 / TPR;
     const int lane = threadIdx.x % TPR;
     double acc = 0, accd = 0;
@@ -835,7 +866,14 @@ __global__ void __launch_bounds__(256) gm_resid(int64_t n, const int32_t* __rest
 template <class T>
 __global__ void __launch_bounds__(256) gm_dots(int64_t n, int j, const T* __restrict__ V, double* __restrict__ part,
                                                int nbp, unsigned* __restrict__ cnt, double* __restrict__ red,
-                                               const int* __restrict__ flags, int gated, int with_norm) {
+                                               const int* __restrict__ flags, int gated, int with_norm, Bat bt) {
+    const int64_t ib = blockIdx.y;
+    V += ib * bt.V;
+    part += ib * bt.part;
+    cnt += ib * bt.cnt;
+    red += ib * bt.red;
+    flags += ib * bt.flags;
+
     if (flags[F_CONV] || (gated && !flags[F_REORTH])) return;
     const T* __restrict__ w = V + (int64_t)(j + 1) * n;
     const int warp = threadIdx.x >> 5, lane32 = threadIdx.x & 31;
@@ -867,7 +905,14 @@ __global__ void __launch_bounds__(256) gm_spmv(int64_t n, int j, const int32_t* 
                                                const int32_t* __restrict__ col, const T* __restrict__ A,
                                                const uint8_t* __restrict__ freed, const T* __restrict__ xin,
                                                int xin_is_basis, T* __restrict__ V, const double* __restrict__ scale,
-                                               const int* __restrict__ flags) {
+                                               const int* __restrict__ flags, Bat bt) {
+    const int64_t ib = blockIdx.y;
+    A += ib * bt.nnz;
+    xin += ib * (xin_is_basis ? bt.V : bt.n);
+    V += ib * bt.V;
+    scale += ib * bt.scale;
+    flags += ib * bt.flags;
+
     if (flags[F_CONV]) return;
     const int64_t r = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) / TPR;
     const int lane = threadIdx.x % TPR;
@@ -890,7 +935,18 @@ __global__ void __launch_bounds__(256) gm_orth(int64_t n, int j, int m, T* __res
                                                const double* __restrict__ red, double* __restrict__ part,
                                                unsigned* __restrict__ cnt, double* __restrict__ H,
                                                double* __restrict__ csg, double* st, int* flags, double* scale,
-                                               int pass) {
+                                               int pass, Bat bt) {
+    const int64_t ib = blockIdx.y;
+    V += ib * bt.V;
+    red += ib * bt.red;
+    part += ib * bt.part;
+    cnt += ib * bt.cnt;
+    H += ib * bt.H;
+    csg += ib * bt.H;
+    st += ib * bt.st;
+    flags += ib * bt.flags;
+    scale += ib * bt.scale;
+
     if (flags[F_CONV] || (pass == 2 && !flags[F_REORTH])) return;
     __shared__ T coef[130];
     for (int k = threadIdx.x; k <= j; k += blockDim.x) coef[k] = (T)(red[k] * scale[k] * scale[k]);
@@ -945,7 +1001,17 @@ __global__ void __launch_bounds__(256) gm_combine(int64_t n, int m, const T* __r
                                                   const double* __restrict__ scale, const double* __restrict__ H,
                                                   const double* __restrict__ csg, const int* __restrict__ flags,
                                                   const T* __restrict__ dinv, double* __restrict__ x,
-                                                  T* __restrict__ u) {
+                                                  T* __restrict__ u, Bat bt) {
+    const int64_t ib = blockIdx.y;
+    V += ib * bt.V;
+    scale += ib * bt.scale;
+    H += ib * bt.H;
+    csg += ib * bt.H;
+    flags += ib * bt.flags;
+    if (dinv) dinv += ib * bt.n;
+    x += ib * bt.n;
+    if (u) u += ib * bt.n;
+
     __shared__ double y[130];
     __shared__ T c[130];
     const int jd = flags[F_JDONE];
@@ -988,7 +1054,11 @@ __global__ void gm_block_apply(int64_t ne, const T* __restrict__ Binv, const T* 
 // A_s = A D^-1 (Jacobi) or A, cast to T
 template <class T>
 __global__ void gm_scale_matrix(int64_t n, const int32_t* __restrict__ rp, const int32_t* __restrict__ col,
-                                const double* __restrict__ A, const double* __restrict__ dinv64, T* __restrict__ As) {
+                                const double* __restrict__ A, const double* __restrict__ dinv64, T* __restrict__ As,
+                                int64_t nnz) {
+    A += blockIdx.y * nnz;
+    As += blockIdx.y * nnz;
+    if (dinv64) dinv64 += blockIdx.y * n;
     const int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (r >= n) return;
     for (int32_t k = rp[r]; k < rp[r + 1]; k++) {
@@ -1002,11 +1072,19 @@ __global__ void gm_cast(int64_t n, const double* __restrict__ a, float* __restri
     if (i < n) b[i] = (float)a[i];
 }
 
-__global__ void gm_set_tols(double* st, double tol, double inner, double eta2) {
-    st[S_OUTERTOL] = tol;
-    st[S_INNER] = inner;
-    st[S_TOL] = tol;
-    st[S_ETA2] = eta2;
+__global__ void gm_copy(int64_t n, const double* __restrict__ a, double* __restrict__ b) {
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i < n) b[i] = a[i];
+}
+
+__global__ void gm_set_tols(double* st, double tol, double inner, double eta2, int nb, int64_t stride) {
+    for (int q = 0; q < nb; q++) {
+        double* s = st + q * stride;
+        s[S_OUTERTOL] = tol;
+        s[S_INNER] = inner;
+        s[S_TOL] = tol;
+        s[S_ETA2] = eta2;
+    }
 }
 
 template <class T>
@@ -1018,6 +1096,11 @@ struct GmBufs {
     T* z;              // block Jacobi workspace
 };
 
+// Host driver of the fused GMRES over a batch of sv->B systems (B = 1 for a single solve).
+// Without graphs the host reads the convergence flags every check_every iterations; with graphs
+// one restart cycle (m iterations, the x update and the next FP64 residual) is captured once into
+// a CUDA graph and replayed, the host reading the flags only between cycles. Converged instances
+// return at the top of every kernel.
 template <class T, int TPR, int U>
 int gm_run(const Ctx& c, const GmBufs<T>& B, const double* b, double* x, int maxit, double inner_tol, int* iters,
            int* cycles, double* relres0) {
@@ -1026,79 +1109,130 @@ int gm_run(const Ctx& c, const GmBufs<T>& B, const double* b, double* x, int max
     const int64_t n = sv->n;
     const int m = sv->m;
     const int G = sv->grid;
+    const int NB = sv->B;
+    const Bat bt = sv->bat;
     double* csg = sv->H + (size_t)(m + 1) * m;
     const int nbp = G;
     double* red2 = sv->red + (m + 4);
     const bool block = B.Binv != nullptr;
     const int64_t ne = s->mesh->ne;
     const int L = s->nloc;
+    const dim3 gg(G, NB), gs(nblk(n * TPR, 256), NB);
+    cudaStream_t ls = c.st;  // launch stream of the lambdas below (switched while capturing)
     auto block_apply = [&](int j, double* xo) {
         const unsigned nbk = nblk(ne * L, kThreads);
         switch (L) {
-        case 3: gm_block_apply<T, 3><<<nbk, kThreads, 0, c.st>>>(ne, B.Binv, xo ? B.z : B.V + (int64_t)j * n, 1.0, xo ? nullptr : sv->scale, j, B.z, xo, xo ? nullptr : sv->flags); break;
-        case 6: gm_block_apply<T, 6><<<nbk, kThreads, 0, c.st>>>(ne, B.Binv, xo ? B.z : B.V + (int64_t)j * n, 1.0, xo ? nullptr : sv->scale, j, B.z, xo, xo ? nullptr : sv->flags); break;
-        case 10: gm_block_apply<T, 10><<<nbk, kThreads, 0, c.st>>>(ne, B.Binv, xo ? B.z : B.V + (int64_t)j * n, 1.0, xo ? nullptr : sv->scale, j, B.z, xo, xo ? nullptr : sv->flags); break;
+        case 3: gm_block_apply<T, 3><<<nbk, kThreads, 0, ls>>>(ne, B.Binv, xo ? B.z : B.V + (int64_t)j * n, 1.0, xo ? nullptr : sv->scale, j, B.z, xo, xo ? nullptr : sv->flags); break;
+        case 6: gm_block_apply<T, 6><<<nbk, kThreads, 0, ls>>>(ne, B.Binv, xo ? B.z : B.V + (int64_t)j * n, 1.0, xo ? nullptr : sv->scale, j, B.z, xo, xo ? nullptr : sv->flags); break;
+        case 10: gm_block_apply<T, 10><<<nbk, kThreads, 0, ls>>>(ne, B.Binv, xo ? B.z : B.V + (int64_t)j * n, 1.0, xo ? nullptr : sv->scale, j, B.z, xo, xo ? nullptr : sv->flags); break;
         default: break;
         }
     };
-    // Classical Gram-Schmidt, repeated only when |w| lost more than 99.9% of its length to the
-    // projection (|w_new|^2 < 1e-6 |w|^2); the mass-dominated systems here lose far less per step.
-    gm_set_tols<<<1, 1, 0, c.st>>>(sv->st, sv->prm.tol, inner_tol, 1e-6);
-    OCMP_CUDA(cudaMemsetAsync(sv->flags, 0, sizeof(int) * F_NFLAG, c.st));
-    gm_resid<T, TPR, U><<<G, 256, 0, c.st>>>(n, s->d_rowptr, s->d_col, sv->mat->vals, s->d_free, b, x, B.V, sv->part,
-                                             sv->cnt, sv->st, sv->flags, sv->scale, csg, m, 3, s->d_lift_ptr,
-                                             s->d_lift_pos);
-    {
-        double r0 = 0;
-        OCMP_CUDA(cudaMemcpyAsync(&r0, sv->st + S_RES, sizeof(double), cudaMemcpyDeviceToHost, c.st));
-        if (read_flags(c)) return OCMP_ERR_CUDA;
-        *relres0 = r0;
-    }
-    int it = 0, cyc = 0;
-    bool first = true;
-    while (true) {
-        if (!first && read_flags(c)) return OCMP_ERR_CUDA;
-        first = false;
-        if (sv->hflags[F_OUTER] || sv->hflags[F_NONFIN] || it >= maxit) break;
-        // one cycle
-        int j = 0;
-        for (; j < m; j++) {
-            const T* xin = B.V + (int64_t)j * n;
-            if (block) {
-                block_apply(j, nullptr);
-                xin = B.z;
-            }
-            gm_spmv<T, TPR, U><<<nblk(n * TPR, 256), 256, 0, c.st>>>(n, j, s->d_rowptr, s->d_col, B.A, s->d_free, xin,
-                                                                     block ? 0 : 1, B.V, sv->scale, sv->flags);
-            gm_dots<T><<<G, 256, 0, c.st>>>(n, j, B.V, sv->part, nbp, sv->cnt, sv->red, sv->flags, 0, 1);
-            gm_orth<T><<<G, 256, 0, c.st>>>(n, j, m, B.V, sv->red, sv->part, sv->cnt + 1, sv->H, csg, sv->st,
-                                            sv->flags, sv->scale, 1);
-            gm_dots<T><<<G, 256, 0, c.st>>>(n, j, B.V, sv->part, nbp, sv->cnt + 2, red2, sv->flags, 1, 0);
-            gm_orth<T><<<G, 256, 0, c.st>>>(n, j, m, B.V, red2, sv->part, sv->cnt + 3, sv->H, csg, sv->st,
-                                            sv->flags, sv->scale, 2);
-            it++;
-            if (((j + 1) % std::max(1, sv->prm.check_every)) == 0 || it >= maxit) {
-                if (read_flags(c)) return OCMP_ERR_CUDA;
-                if (sv->hflags[F_CONV] || it >= maxit) break;
-            }
-        }
-        // x += P V y
+    auto iteration = [&](int j) {
+        const T* xin = B.V + (int64_t)j * n;
         if (block) {
-            gm_combine<T><<<G, 256, 0, c.st>>>(n, m, B.V, sv->scale, sv->H, csg, sv->flags, nullptr, x, B.z);
+            block_apply(j, nullptr);
+            xin = B.z;
+        }
+        gm_spmv<T, TPR, U><<<gs, 256, 0, ls>>>(n, j, s->d_rowptr, s->d_col, B.A, s->d_free, xin, block ? 0 : 1, B.V,
+                                                 sv->scale, sv->flags, bt);
+        gm_dots<T><<<gg, 256, 0, ls>>>(n, j, B.V, sv->part, nbp, sv->cnt, sv->red, sv->flags, 0, 1, bt);
+        gm_orth<T><<<gg, 256, 0, ls>>>(n, j, m, B.V, sv->red, sv->part, sv->cnt + 1, sv->H, csg, sv->st, sv->flags,
+                                         sv->scale, 1, bt);
+        gm_dots<T><<<gg, 256, 0, ls>>>(n, j, B.V, sv->part, nbp, sv->cnt + 2, red2, sv->flags, 1, 0, bt);
+        gm_orth<T><<<gg, 256, 0, ls>>>(n, j, m, B.V, red2, sv->part, sv->cnt + 3, sv->H, csg, sv->st, sv->flags,
+                                         sv->scale, 2, bt);
+    };
+    auto finish_cycle = [&]() {
+        if (block) {
+            gm_combine<T><<<gg, 256, 0, ls>>>(n, m, B.V, sv->scale, sv->H, csg, sv->flags, nullptr, x, B.z, bt);
             block_apply(0, x);
         } else {
-            gm_combine<T><<<G, 256, 0, c.st>>>(n, m, B.V, sv->scale, sv->H, csg, sv->flags, B.dinv, x, nullptr);
+            gm_combine<T><<<gg, 256, 0, ls>>>(n, m, B.V, sv->scale, sv->H, csg, sv->flags, B.dinv, x, nullptr, bt);
+        }
+        gm_resid<T, TPR, U><<<gg, 256, 0, ls>>>(n, s->d_rowptr, s->d_col, sv->mat->vals, s->d_free, b, x, B.V,
+                                                  sv->part, sv->cnt, sv->st, sv->flags, sv->scale, csg, m, 1,
+                                                  s->d_lift_ptr, s->d_lift_pos, bt);
+    };
+    auto all = [&](int f) {
+        for (int q = 0; q < NB; q++)
+            if (!sv->hflags[q * F_NFLAG + f] && !sv->hflags[q * F_NFLAG + F_NONFIN]) return false;
+        return true;
+    };
+    // Classical Gram-Schmidt, repeated only when |w| lost more than 99.9% of its length to the
+    // projection (|w_new|^2 < 1e-6 |w|^2); the mass-dominated systems here lose far less per step.
+    gm_set_tols<<<1, 1, 0, c.st>>>(sv->st, sv->prm.tol, inner_tol, 1e-6, NB, bt.st);
+    OCMP_CUDA(cudaMemsetAsync(sv->flags, 0, sizeof(int) * F_NFLAG * NB, c.st));
+    gm_resid<T, TPR, U><<<gg, 256, 0, c.st>>>(n, s->d_rowptr, s->d_col, sv->mat->vals, s->d_free, b, x, B.V, sv->part,
+                                              sv->cnt, sv->st, sv->flags, sv->scale, csg, m, 3, s->d_lift_ptr,
+                                              s->d_lift_pos, bt);
+    {
+        std::vector<double> sth((size_t)S_NSLOT * NB);
+        OCMP_CUDA(cudaMemcpyAsync(sth.data(), sv->st, sizeof(double) * S_NSLOT * NB, cudaMemcpyDeviceToHost, c.st));
+        if (read_flags(c)) return OCMP_ERR_CUDA;
+        for (int q = 0; q < NB; q++) relres0[q] = sth[(size_t)q * S_NSLOT + S_RES];
+    }
+    int it = 0, cyc = 0;
+    const bool graph = sv->use_graph;
+    // Stream capture is not allowed on the legacy default stream: capture and replay on the
+    // solver's own stream instead, ordered after and before the caller's work with events.
+    Ctx cg = c;
+    if (graph && c.st == nullptr) {
+        if (!sv->gstream) {
+            OCMP_CUDA(cudaStreamCreateWithFlags(&sv->gstream, cudaStreamNonBlocking));
+            OCMP_CUDA(cudaEventCreateWithFlags(&sv->gev[0], cudaEventDisableTiming));
+            OCMP_CUDA(cudaEventCreateWithFlags(&sv->gev[1], cudaEventDisableTiming));
+        }
+        cg.st = sv->gstream;
+    }
+    if (graph && (sv->gexec == nullptr || sv->g_b != b || sv->g_x != x || sv->g_stream != cg.st)) {
+        if (sv->gexec) {
+            cudaGraphExecDestroy(sv->gexec);
+            sv->gexec = nullptr;
+        }
+        cudaGraph_t gph;
+        OCMP_CUDA(cudaStreamBeginCapture(cg.st, cudaStreamCaptureModeThreadLocal));
+        ls = cg.st;
+        for (int j = 0; j < m; j++) iteration(j);
+        finish_cycle();
+        ls = c.st;
+        OCMP_CUDA(cudaStreamEndCapture(cg.st, &gph));
+        cudaError_t e = cudaGraphInstantiate(&sv->gexec, gph, 0);
+        cudaGraphDestroy(gph);
+        if (e != cudaSuccess) return cuda_fail(e, "cudaGraphInstantiate");
+        sv->g_b = b;
+        sv->g_x = x;
+        sv->g_stream = cg.st;
+    }
+    while (true) {
+        if (all(F_OUTER) || it >= maxit) break;
+        if (graph) {
+            if (cg.st != c.st) {
+                OCMP_CUDA(cudaEventRecord(sv->gev[0], c.st));
+                OCMP_CUDA(cudaStreamWaitEvent(cg.st, sv->gev[0], 0));
+            }
+            OCMP_CUDA(cudaGraphLaunch(sv->gexec, cg.st));
+            if (cg.st != c.st) {
+                OCMP_CUDA(cudaEventRecord(sv->gev[1], cg.st));
+                OCMP_CUDA(cudaStreamWaitEvent(c.st, sv->gev[1], 0));
+            }
+            it += m;
+        } else {
+            for (int j = 0; j < m; j++) {
+                iteration(j);
+                it++;
+                if (((j + 1) % std::max(1, sv->prm.check_every)) == 0 || it >= maxit) {
+                    if (read_flags(c)) return OCMP_ERR_CUDA;
+                    if (all(F_CONV) || it >= maxit) break;
+                }
+            }
+            finish_cycle();
         }
         cyc++;
         if (read_flags(c)) return OCMP_ERR_CUDA;
-        if (sv->hflags[F_NONFIN]) break;
-        // next cycle: FP64 residual of the updated iterate (restart / refinement step)
-        gm_resid<T, TPR, U><<<G, 256, 0, c.st>>>(n, s->d_rowptr, s->d_col, sv->mat->vals, s->d_free, b, x, B.V,
-                                                 sv->part, sv->cnt, sv->st, sv->flags, sv->scale, csg, m, 1,
-                                                 s->d_lift_ptr, s->d_lift_pos);
     }
     OCMP_CUDA(cudaGetLastError());
-    *iters = sv->hflags[F_ITERS];
+    for (int q = 0; q < NB; q++) iters[q] = sv->hflags[q * F_NFLAG + F_ITERS];
     *cycles = cyc;
     return OCMP_OK;
 }
@@ -1110,6 +1244,7 @@ int gm_dispatch(const Ctx& c, const GmBufs<T>& B, const double* b, double* x, in
     if (rc.tpr == 2) return gm_run<T, 2, 4>(c, B, b, x, maxit, inner_tol, iters, cycles, relres0);
     if (rc.tpr == 4 && rc.u == 4) return gm_run<T, 4, 4>(c, B, b, x, maxit, inner_tol, iters, cycles, relres0);
     if (rc.tpr == 4) return gm_run<T, 4, 8>(c, B, b, x, maxit, inner_tol, iters, cycles, relres0);
+    if (rc.tpr == 8 && rc.u == 4) return gm_run<T, 8, 4>(c, B, b, x, maxit, inner_tol, iters, cycles, relres0);
     if (rc.tpr == 8) return gm_run<T, 8, 8>(c, B, b, x, maxit, inner_tol, iters, cycles, relres0);
     return gm_run<T, 16, 8>(c, B, b, x, maxit, inner_tol, iters, cycles, relres0);
 }
@@ -1120,14 +1255,15 @@ int gm_norms(const Ctx& c, const double* b, const double* x, int mode) {
     const ocmp_space_s* s = sv->s;
     const RowCfg rc = row_cfg(s);
     double* csg = sv->H + (size_t)(sv->m + 1) * sv->m;
-#define GM_R(TPR, U)                                                                                              \
-    gm_resid<double, TPR, U><<<sv->grid, 256, 0, c.st>>>(sv->n, s->d_rowptr, s->d_col, sv->mat->vals, s->d_free, b, \
-                                                         x, (double*)nullptr, sv->part, sv->cnt, sv->st, sv->flags,    \
-                                                         sv->scale, csg, sv->m, mode, s->d_lift_ptr,            \
-                                                         s->d_lift_pos)
+    const dim3 gg(sv->grid, sv->B);
+#define GM_R(TPR, U)                                                                                                  \
+    gm_resid<double, TPR, U><<<gg, 256, 0, c.st>>>(sv->n, s->d_rowptr, s->d_col, sv->mat->vals, s->d_free, b, x,      \
+                                                   (double*)nullptr, sv->part, sv->cnt, sv->st, sv->flags, sv->scale, \
+                                                   csg, sv->m, mode, s->d_lift_ptr, s->d_lift_pos, sv->bat)
     if (rc.tpr == 2) GM_R(2, 4);
     else if (rc.tpr == 4 && rc.u == 4) GM_R(4, 4);
     else if (rc.tpr == 4) GM_R(4, 8);
+    else if (rc.tpr == 8 && rc.u == 4) GM_R(8, 4);
     else if (rc.tpr == 8) GM_R(8, 8);
     else GM_R(16, 8);
 #undef GM_R
@@ -1146,6 +1282,10 @@ static void free_solver(ocmp_solver_s* sv) {
                   sv->st,   sv->H,    sv->flags, sv->As64, sv->As32, sv->scale, sv->cnt};
     for (void* q : ps) dfree(q);
     if (sv->hflags) cudaFreeHost(sv->hflags);
+    if (sv->gexec) cudaGraphExecDestroy(sv->gexec);
+    if (sv->gstream) cudaStreamDestroy(sv->gstream);
+    for (cudaEvent_t e : sv->gev)
+        if (e) cudaEventDestroy(e);
 }
 
 extern "C" {
@@ -1168,6 +1308,11 @@ int ocmp_solver_create(ocmp_matrix_t mat, const ocmp_solve_params_t* prm, ocmp_s
     sv->prm = *prm;
     if (sv->prm.check_every <= 0) sv->prm.check_every = 8;
     const int64_t n = sv->n = s->ndof;
+    const int NB = sv->B = mat->B;
+    if (NB > 1 && (prm->method != OCMP_GMRES || prm->precond == OCMP_PRE_BLOCK_JACOBI)) {
+        delete sv;
+        return fail(OCMP_ERR_UNSUPPORTED, "ocmp_solver_create: batches are solved with GMRES + point Jacobi");
+    }
     sv->m = std::max(1, std::min(128, prm->restart > 0 ? prm->restart : 30));
     const int m = sv->m;
     sv->nb = (int)std::max<int64_t>(1, std::min<int64_t>(1216, (n + 1023) / 1024));
@@ -1175,51 +1320,63 @@ int ocmp_solver_create(ocmp_matrix_t mat, const ocmp_solve_params_t* prm, ocmp_s
     const bool blk = prm->precond == OCMP_PRE_BLOCK_JACOBI;
     const int tpr = pick_tpr(s);
     const int64_t nbs = (n * tpr + kThreads - 1) / kThreads;
+    sv->grid = (int)std::max<int64_t>(1, std::min<int64_t>(kGridCap, nbs));
+    const int64_t hsz = (int64_t)(m + 1) * m + 4 * m + 2;
+    sv->bat = Bat{NB > 1 ? n : 0,
+                  NB > 1 ? s->nnz : 0,
+                  NB > 1 ? (int64_t)(m + 1) * n : 0,
+                  NB > 1 ? (int64_t)(m + 4) * sv->grid : 0,
+                  NB > 1 ? (int64_t)S_NSLOT : 0,
+                  NB > 1 ? (int64_t)F_NFLAG : 0,
+                  NB > 1 ? (int64_t)(m + 2) : 0,
+                  NB > 1 ? hsz : 0,
+                  NB > 1 ? (int64_t)(3 * m + 12) : 0,
+                  NB > 1 ? (int64_t)8 : 0};
     int st = OCMP_OK;
     auto A = [&](auto** p, size_t cnt) {
         if (!st) st = dalloc(p, cnt);
     };
-    A(&sv->dinv, n);
+    A(&sv->dinv, (size_t)n * NB);
     A(&sv->w, n);
     A(&sv->z, n);
     A(&sv->r, n);
     if (!mixed) {
-        if (gm) A(&sv->V, (size_t)(m + 1) * n);
+        if (gm) A(&sv->V, (size_t)(m + 1) * n * NB);
         else A(&sv->p, n);
     }
     if (blk) A(&sv->Binv, (size_t)s->mesh->ne * s->nloc * s->nloc);
     if (mixed) {
-        A(&sv->dinv32, n);
+        A(&sv->dinv32, (size_t)n * NB);
         A(&sv->w32, n);
         A(&sv->z32, n);
         A(&sv->d32, n);
-        if (gm) A(&sv->V32, (size_t)(m + 1) * n);
+        if (gm) A(&sv->V32, (size_t)(m + 1) * n * NB);
         else {
             A(&sv->r32, n);
             A(&sv->p32, n);
         }
         if (blk) A(&sv->Binv32, (size_t)s->mesh->ne * s->nloc * s->nloc);
     }
-    sv->grid = (int)std::max<int64_t>(1, std::min<int64_t>(kGridCap, nbs));
-    A(&sv->part, (size_t)(m + 4) * kGridCap);
+    A(&sv->part, (size_t)std::max<int64_t>((int64_t)(m + 4) * kGridCap, (int64_t)(m + 4) * sv->grid * NB));
     A(&sv->pspmv, (size_t)nbs);
-    A(&sv->red, (size_t)(3 * m + 12));
-    A(&sv->st, (size_t)S_NSLOT);
-    A(&sv->H, (size_t)(m + 1) * m + 4 * m + 2);
-    A(&sv->scale, (size_t)(m + 2));
-    A(&sv->cnt, (size_t)8);
+    A(&sv->red, (size_t)(3 * m + 12) * NB);
+    A(&sv->st, (size_t)S_NSLOT * NB);
+    A(&sv->H, (size_t)hsz * NB);
+    A(&sv->scale, (size_t)(m + 2) * NB);
+    A(&sv->cnt, (size_t)8 * NB);
     sv->borrow = gm && prm->precond == OCMP_PRE_JACOBI && mat->dinv &&
                  (mixed ? mat->svals32 != nullptr : mat->svals64 != nullptr);
     if (gm && !sv->borrow) {
-        if (mixed) A(&sv->As32, (size_t)s->nnz);
-        else A(&sv->As64, (size_t)s->nnz);
+        if (mixed) A(&sv->As32, (size_t)s->nnz * NB);
+        else A(&sv->As64, (size_t)s->nnz * NB);
     }
     sv->K64 = sv->borrow ? mat->svals64 : sv->As64;
     sv->K32 = sv->borrow ? mat->svals32 : sv->As32;
-    A(&sv->flags, (size_t)F_NFLAG);
-    if (!st && cudaMemset(sv->cnt, 0, sizeof(unsigned) * 8) != cudaSuccess) st = fail(OCMP_ERR_CUDA, "cudaMemset");
-    if (!st && cudaMemset(sv->st, 0, sizeof(double) * S_NSLOT) != cudaSuccess) st = fail(OCMP_ERR_CUDA, "cudaMemset");
-    if (!st && cudaMallocHost((void**)&sv->hflags, sizeof(int) * F_NFLAG) != cudaSuccess)
+    A(&sv->flags, (size_t)F_NFLAG * NB);
+    if (!st && cudaMemset(sv->cnt, 0, sizeof(unsigned) * 8 * NB) != cudaSuccess) st = fail(OCMP_ERR_CUDA, "cudaMemset");
+    if (!st && cudaMemset(sv->st, 0, sizeof(double) * S_NSLOT * NB) != cudaSuccess)
+        st = fail(OCMP_ERR_CUDA, "cudaMemset");
+    if (!st && cudaMallocHost((void**)&sv->hflags, sizeof(int) * F_NFLAG * NB) != cudaSuccess)
         st = fail(OCMP_ERR_NOMEM, "cudaMallocHost");
     if (st) {
         free_solver(sv);
@@ -1249,9 +1406,20 @@ int ocmp_solver_update(ocmp_solver_t sv, void* stream) {
     cudaStream_t st = (cudaStream_t)stream;
     ocmp_space_s* s = sv->s;
     const int64_t n = sv->n;
-    jacobi_setup<double><<<nblk(n, kThreads), kThreads, 0, st>>>(n, s->d_diag, sv->mat->vals, s->d_free, sv->dinv);
-    if (sv->dinv32)
-        jacobi_setup<float><<<nblk(n, kThreads), kThreads, 0, st>>>(n, s->d_diag, sv->mat->vals, s->d_free, sv->dinv32);
+    const int NB = sv->B;
+    if (sv->borrow) {
+        // the assembly's D^-1 scaled the Krylov matrix: use the same one for x = D^-1 y
+        OCMP_CUDA(cudaMemcpyAsync(sv->dinv, sv->mat->dinv, sizeof(double) * n * NB, cudaMemcpyDeviceToDevice, st));
+        if (sv->dinv32) gm_cast<<<nblk(n * NB, kThreads), kThreads, 0, st>>>(n * NB, sv->mat->dinv, sv->dinv32);
+    } else {
+        for (int q = 0; q < NB; q++) {
+            jacobi_setup<double><<<nblk(n, kThreads), kThreads, 0, st>>>(n, s->d_diag, sv->mat->vals + q * s->nnz,
+                                                                        s->d_free, sv->dinv + q * n);
+            if (sv->dinv32)
+                jacobi_setup<float><<<nblk(n, kThreads), kThreads, 0, st>>>(n, s->d_diag, sv->mat->vals + q * s->nnz,
+                                                                           s->d_free, sv->dinv32 + q * n);
+        }
+    }
     if (sv->Binv) {
         const int64_t ne = s->mesh->ne;
         switch (s->nloc) {
@@ -1261,22 +1429,77 @@ int ocmp_solver_update(ocmp_solver_t sv, void* stream) {
         default: break;
         }
     }
-    if (sv->borrow) {
-        // the assembly's D^-1 scaled the Krylov matrix: use the same one for x = D^-1 y
-        OCMP_CUDA(cudaMemcpyAsync(sv->dinv, sv->mat->dinv, sizeof(double) * n, cudaMemcpyDeviceToDevice, st));
-        if (sv->dinv32) gm_cast<<<nblk(n, kThreads), kThreads, 0, st>>>(n, sv->mat->dinv, sv->dinv32);
-    }
     if (sv->As64 || sv->As32) {
         const double* d = sv->prm.precond == OCMP_PRE_JACOBI ? sv->dinv : nullptr;
+        const dim3 g(nblk(n, kThreads), NB);
         if (sv->As64)
-            gm_scale_matrix<double><<<nblk(n, kThreads), kThreads, 0, st>>>(n, s->d_rowptr, s->d_col, sv->mat->vals, d,
-                                                                            sv->As64);
+            gm_scale_matrix<double><<<g, kThreads, 0, st>>>(n, s->d_rowptr, s->d_col, sv->mat->vals, d, sv->As64, s->nnz);
         if (sv->As32)
-            gm_scale_matrix<float><<<nblk(n, kThreads), kThreads, 0, st>>>(n, s->d_rowptr, s->d_col, sv->mat->vals, d,
-                                                                           sv->As32);
+            gm_scale_matrix<float><<<g, kThreads, 0, st>>>(n, s->d_rowptr, s->d_col, sv->mat->vals, d, sv->As32, s->nnz);
     }
     OCMP_CUDA(cudaGetLastError());
     return OCMP_OK;
+}
+
+int ocmp_solver_set_graph(ocmp_solver_t sv, int32_t on) {
+    if (!sv) return fail(OCMP_ERR_ARG, "ocmp_solver_set_graph: null solver");
+    if (on && sv->prm.method != OCMP_GMRES)
+        return fail(OCMP_ERR_UNSUPPORTED, "ocmp_solver_set_graph: graphs are built for GMRES");
+    sv->use_graph = on != 0;
+    if (!on && sv->gexec) {
+        cudaGraphExecDestroy(sv->gexec);
+        sv->gexec = nullptr;
+    }
+    return OCMP_OK;
+}
+
+// Batched GMRES solve of all B systems of the solver's matrix: b and x hold B vectors of ndof.
+int ocmp_solve_batch(ocmp_solver_t sv, const double* b, double* x, void* stream, ocmp_solve_info_t* infos) {
+    if (!sv || !b || !x) return fail(OCMP_ERR_ARG, "ocmp_solve_batch: null argument");
+    if (sv->prm.method != OCMP_GMRES) return fail(OCMP_ERR_UNSUPPORTED, "ocmp_solve_batch: GMRES only");
+    Ctx c;
+    c.sv = sv;
+    c.st = (cudaStream_t)stream;
+    c.tpr = pick_tpr(sv->s);
+    c.grid = sv->nb;
+    const int NB = sv->B;
+    const ocmp_solve_params_t& P = sv->prm;
+    const bool mixed = P.precision == OCMP_MIXED, jac = P.precond == OCMP_PRE_JACOBI;
+    std::vector<double> r0(NB, 0.0);
+    std::vector<int> its(NB, 0);
+    int cyc = 0, st;
+    if (!mixed) {
+        GmBufs<double> B{sv->K64, jac ? sv->dinv : nullptr, nullptr, sv->V, sv->z};
+        st = gm_dispatch<double>(c, B, b, x, P.maxit, 0.0, its.data(), &cyc, r0.data());
+    } else {
+        GmBufs<float> B{sv->K32, jac ? sv->dinv32 : nullptr, nullptr, sv->V32, sv->z32};
+        st = gm_dispatch<float>(c, B, b, x, P.maxit, P.inner_tol > 0 ? P.inner_tol : 1e-4, its.data(), &cyc,
+                                r0.data());
+    }
+    if (st) return st;
+    // the FP64 residual of each returned x: the last cycle start, or a fresh one
+    st = gm_norms(c, b, x, 2);
+    if (st) return st;
+    std::vector<double> sth((size_t)S_NSLOT * NB);
+    OCMP_CUDA(cudaMemcpyAsync(sth.data(), sv->st, sizeof(double) * S_NSLOT * NB, cudaMemcpyDeviceToHost, c.st));
+    OCMP_CUDA(cudaStreamSynchronize(c.st));
+    int worst = OCMP_OK;
+    for (int q = 0; q < NB; q++) {
+        const double rr = sth[(size_t)q * S_NSLOT + S_RES];
+        int status = OCMP_OK;
+        if (sv->hflags[q * F_NFLAG + F_NONFIN] || !std::isfinite(rr)) status = OCMP_ERR_NONFINITE;
+        else if (rr > P.tol) status = sv->hflags[q * F_NFLAG + F_BREAK] ? OCMP_BREAKDOWN : OCMP_NOT_CONVERGED;
+        if (infos) {
+            infos[q].status = status;
+            infos[q].iterations = its[q];
+            infos[q].outer_iterations = cyc;
+            infos[q].relres0 = r0[q];
+            infos[q].relres = rr;
+        }
+        if (status != OCMP_OK && worst == OCMP_OK) worst = status;
+    }
+    if (worst != OCMP_OK) set_error("ocmp_solve_batch: at least one system did not reach the tolerance");
+    return worst;
 }
 
 int ocmp_solve(ocmp_solver_t sv, const double* b, double* x, void* stream, ocmp_solve_info_t* info) {
@@ -1296,6 +1519,7 @@ int ocmp_solve(ocmp_solver_t sv, const double* b, double* x, void* stream, ocmp_
     double relres0 = 0, relres = 0;
     if (gm) {
         const bool jac = P.precond == OCMP_PRE_JACOBI;
+        if (sv->B != 1) return fail(OCMP_ERR_ARG, "ocmp_solve: batched matrix, use ocmp_solve_batch");
         if (!mixed) {
             GmBufs<double> B{sv->K64, jac ? sv->dinv : nullptr, sv->Binv, sv->V, sv->z};
             st = gm_dispatch<double>(c, B, b, x, P.maxit, 0.0, &iters, &outer, &relres0);

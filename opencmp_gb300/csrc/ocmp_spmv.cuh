@@ -17,7 +17,10 @@ namespace ocmp {
 struct RowCfg {
     int tpr, u;
 };
+// Threads per row and loads in flight per lane: the autotuned choice when there is one, else a
+// rule on the mean row length.
 inline RowCfg row_cfg(const ocmp_space_s* s) {
+    if (s->tuned_tpr > 0) return {s->tuned_tpr, s->tuned_u};
     const double avg = (double)s->nnz / (double)s->ndof;
     if (avg <= 6) return {2, 4};
     if (avg <= 16) return {4, 4};

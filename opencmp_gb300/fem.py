@@ -159,12 +159,13 @@ class Matrix:
     on the FP32 pipes (about 1e-14 relative to the native FP64 assembly)."""
 
     def __init__(self, space: Space, fp32: bool = False, jacobi64: bool = False, jacobi32: bool = False,
-                 dfloat: bool = False):
+                 dfloat: bool = False, batch: int = 1):
         self.space = space
         h = C.c_void_p()
         flags = (MAT_FP32 if fp32 else 0) | (MAT_JACOBI64 if jacobi64 else 0) | (MAT_JACOBI32 if jacobi32 else 0) \
             | (MAT_DFLOAT if dfloat else 0)
-        LB.call('ocmp_matrix_create', space.h, flags, C.byref(h))
+        self.batch = batch
+        LB.call('ocmp_matrix_create_batch', space.h, batch, flags, C.byref(h))
         self.h = h
         self.fp32 = fp32
         self.flags = flags
@@ -176,6 +177,12 @@ class Matrix:
 
     def assemble(self, form: LB.Form, stream=None):
         LB.call('ocmp_assemble_matrix', self.h, C.byref(form), _stream(stream))
+
+    def assemble_batch(self, forms, stream=None):
+        """Assemble every instance of a batched matrix, one form per instance."""
+        arr = (LB.Form * len(forms))(*forms)
+        self._forms_keep = arr
+        LB.call('ocmp_assemble_matrix_batch', self.h, arr, _stream(stream))
 
     def device_values(self):
         """Zero-copy torch views of the FP64 (and FP32, or None) value arrays on the device."""
@@ -204,6 +211,15 @@ class Matrix:
     def values32(self) -> np.ndarray:
         torch.cuda.synchronize()
         return self.device_values()[1].cpu().numpy()
+
+    def autotune(self, stream=None):
+        """Pick the SpMV row configuration by timing the candidates on this matrix."""
+        x = torch.randn(self.space.ndof, dtype=torch.float64, device='cuda')
+        y = torch.empty_like(x)
+        tpr, u, ms = C.c_int32(0), C.c_int32(0), C.c_float(0)
+        LB.call('ocmp_matrix_autotune', self.h, _ptr(x), _ptr(y), _stream(stream), C.byref(tpr), C.byref(u),
+                C.byref(ms))
+        return {'threads_per_row': tpr.value, 'unroll': u.value, 'spmv_ms': ms.value}
 
     def mult(self, x: torch.Tensor, y: torch.Tensor, stream=None):
         LB.call('ocmp_spmv', self.h, _ptr(x), _ptr(y), _stream(stream))
@@ -251,6 +267,19 @@ class KrylovSolver:
 
     def update(self, stream=None):
         LB.call('ocmp_solver_update', self.h, _stream(stream))
+
+    def set_graph(self, on: bool = True):
+        """Replay each restart cycle from a captured CUDA graph (GMRES)."""
+        LB.call('ocmp_solver_set_graph', self.h, int(on))
+
+    def solve_batch(self, b: torch.Tensor, x: torch.Tensor, stream=None, raise_on_fail=True):
+        """Solve all systems of a batched matrix; b and x hold batch x ndof values."""
+        nb = self.mat.batch
+        infos = (LB.SolveInfo * nb)()
+        st = LB.load().ocmp_solve_batch(self.h, _ptr(b), _ptr(x), _stream(stream), infos)
+        if raise_on_fail:
+            LB.check(st)
+        return list(infos)
 
     def solve(self, b: torch.Tensor, x: torch.Tensor, stream=None, raise_on_fail=True) -> LB.SolveInfo:
         info = LB.SolveInfo()

@@ -180,6 +180,13 @@ class LearnedGuess:
             losses.append(loss)
         return losses
 
+    def eval_loss(self) -> float:
+        """Mean loss of the network over every stored sample (all rows)."""
+        tot = 0.0
+        for X, T in zip(self.samples_X, self.samples_T):
+            tot += self.net.loss_grad(X, T)[0]
+        return tot / max(1, len(self.samples_X))
+
     def drop_samples(self):
         self.samples_X.clear()
         self.samples_T.clear()
