@@ -79,6 +79,10 @@ typedef struct {
     uint32_t outflow_mask;   /* labels with  dt r c max(w.n, 0)      (total-flux / unlabelled)     */
     uint32_t wn_mask;        /* labels with  dt r c (w.n)            (Neumann half)                */
     uint32_t nitsche_mask;   /* DG Dirichlet labels (penalty, consistency, inflow upwind)          */
+    int32_t skeleton_own_dt; /* nonzero: interior-facet terms take skeleton_dt instead of dt (OpenCMP
+                                keeps them in the time-coefficient form, always implicit, while the
+                                other operator terms are theta-weighted: time_integration_schemes.py) */
+    double skeleton_dt;
 } ocmp_form_t;
 
 /* Linear form  L(v) = dt (f, v) + mass (u_prev, v) + dt * sum_l bval[l] <v>_l + DG Dirichlet data */
@@ -92,12 +96,18 @@ typedef struct {
     double bval[32];         /* per label, constant Neumann-type data                              */
     uint32_t bval_mask;
     double gval[32];         /* per label, constant DG Dirichlet datum                              */
+    const double* bval_fq;   /* device, nbf*nfq or NULL: Neumann data at the boundary-facet quadrature
+                                points (ocmp_space_facet_quad_points); used instead of bval[] on the
+                                labels of bval_mask                                                  */
+    const double* gval_fq;   /* device, nbf*nfq or NULL: DG Dirichlet data there, instead of gval[] */
+    int32_t accumulate;      /* nonzero: b += L(v) instead of b = L(v)                            */
 } ocmp_rhs_t;
 
 typedef struct {
     int64_t ndof, nnz, ne, nv;
     int32_t nloc, nq, dim, order, kind;
     int64_t n_interior_facets, n_boundary_facets, n_contrib;
+    int32_t nfq;             /* quadrature points per facet                                        */
 } ocmp_space_info_t;
 
 typedef struct {
@@ -139,6 +149,23 @@ int ocmp_space_get_free(ocmp_space_t space, uint8_t* free_host);                
 int ocmp_space_quad_points(ocmp_space_t space, double* xyz_host);                /* ne*nq*dim */
 int ocmp_set_boundary(ocmp_space_t space, uint32_t mask, const double* gval_host32, double* u_dev,
                       void* stream);
+/* Boundary-facet quadrature points, nbf*nfq*dim (nbf = n_boundary_facets, nfq = info.nfq), in the
+ * space's boundary-facet order; the points at which bval_fq / gval_fq are sampled. */
+int ocmp_space_facet_quad_points(ocmp_space_t space, double* xyz_host);
+/* The space's boundary facets: (element, local facet, label) per facet, nbf*3 */
+int ocmp_space_boundary_facets(ocmp_space_t space, int32_t* elem_facet_label_host);
+/* Space-dependent Dirichlet data (GridFunction.Set(g, definedon=...), base_model.py:321-341), as a
+ * projection-based interpolation: vertex dofs take g at the vertex; the bubble dofs of each edge
+ * (and, for 3D order 3, each face) of a facet whose label is in `mask` take the L2 projection, along
+ * that edge (face), of g minus the part already fixed. ocmp_boundary_points lists the points at
+ * which the caller samples g (count first with xyz_host = NULL); ocmp_set_boundary_values takes
+ * the samples in that order and writes the constrained dofs of u_dev. */
+int ocmp_boundary_points(ocmp_space_t space, uint32_t mask, int64_t* npts, double* xyz_host);
+int ocmp_set_boundary_values(ocmp_space_t space, uint32_t mask, const double* g_host, double* u_dev, void* stream);
+/* || u_h - f ||_{L2} by the space's element rule, f at the quadrature points (fq_dev, ne*nq) or the
+ * constant fconst when fq_dev is NULL  <- opencmp/helpers/error.py:75-128 (norm('l2_norm', ...)) */
+int ocmp_l2_error(ocmp_space_t space, const double* u_dev, const double* fq_dev, double fconst, double* result_host,
+                  void* stream);
 
 /* ---------------------------------------------------------------- assembly */
 /* Matrix outputs written by each assembly (flags, OR-able). The FP64 values are always written.
@@ -162,6 +189,9 @@ int ocmp_assemble_rhs(ocmp_space_t space, const ocmp_form_t* form, const ocmp_rh
 /* forms: host array of the matrix's nbatch forms (one per instance) */
 int ocmp_assemble_matrix_batch(ocmp_matrix_t mat, const ocmp_form_t* forms, void* stream);
 int ocmp_spmv(ocmp_matrix_t mat, const double* x_dev, double* y_dev, void* stream);
+/* y = alpha * A x + beta * y (beta == 0: y is not read) - the explicit operator terms of the
+ * explicit-Euler and Crank-Nicolson right-hand sides (time_integration_schemes.py:25-76, 134-191) */
+int ocmp_spmv_axpby(ocmp_matrix_t mat, double alpha, const double* x_dev, double beta, double* y_dev, void* stream);
 /* Autotuner: times the CSR SpMV of `mat` (x, y: ndof scratch vectors) for each built pair of threads
  * per row and loads in flight per thread, keeps the fastest for every kernel of the space that runs
  * rows (SpMV, residuals, GMRES), and reports it. */

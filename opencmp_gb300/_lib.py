@@ -32,20 +32,22 @@ class OcmpError(RuntimeError):
 class Form(C.Structure):
     _fields_ = [('mass', C.c_double), ('diff', C.c_double), ('dt', C.c_double), ('wind_kind', C.c_int32),
                 ('wind', C.c_double * 3), ('wind_vtx', C.c_void_p), ('ipc', C.c_double), ('dg', C.c_int32),
-                ('outflow_mask', C.c_uint32), ('wn_mask', C.c_uint32), ('nitsche_mask', C.c_uint32)]
+                ('outflow_mask', C.c_uint32), ('wn_mask', C.c_uint32), ('nitsche_mask', C.c_uint32),
+                ('skeleton_own_dt', C.c_int32), ('skeleton_dt', C.c_double)]
 
 
 class Rhs(C.Structure):
     _fields_ = [('dt', C.c_double), ('src_kind', C.c_int32), ('src_const', C.c_double), ('src_qp', C.c_void_p),
                 ('mass', C.c_double), ('uprev', C.c_void_p), ('bval', C.c_double * 32), ('bval_mask', C.c_uint32),
-                ('gval', C.c_double * 32)]
+                ('gval', C.c_double * 32), ('bval_fq', C.c_void_p), ('gval_fq', C.c_void_p),
+                ('accumulate', C.c_int32)]
 
 
 class SpaceInfo(C.Structure):
     _fields_ = [('ndof', C.c_int64), ('nnz', C.c_int64), ('ne', C.c_int64), ('nv', C.c_int64),
                 ('nloc', C.c_int32), ('nq', C.c_int32), ('dim', C.c_int32), ('order', C.c_int32),
                 ('kind', C.c_int32), ('n_interior_facets', C.c_int64), ('n_boundary_facets', C.c_int64),
-                ('n_contrib', C.c_int64)]
+                ('n_contrib', C.c_int64), ('nfq', C.c_int32)]
 
 
 class SolveParams(C.Structure):
@@ -76,6 +78,11 @@ SIGNATURES = {
     'ocmp_space_get_free': [P, P],
     'ocmp_space_quad_points': [P, P],
     'ocmp_set_boundary': [P, U32, P, P, P],
+    'ocmp_l2_error': [P, P, P, D, P, P],
+    'ocmp_space_facet_quad_points': [P, P],
+    'ocmp_space_boundary_facets': [P, P],
+    'ocmp_boundary_points': [P, U32, P, P],
+    'ocmp_set_boundary_values': [P, U32, P, P, P],
     'ocmp_matrix_create': [P, I32, C.POINTER(P)],
     'ocmp_matrix_create_batch': [P, I32, I32, C.POINTER(P)],
     'ocmp_assemble_matrix_batch': [P, P, P],
@@ -87,6 +94,7 @@ SIGNATURES = {
     'ocmp_assemble_matrix': [P, C.POINTER(Form), P],
     'ocmp_assemble_rhs': [P, C.POINTER(Form), C.POINTER(Rhs), P, P],
     'ocmp_spmv': [P, P, P, P],
+    'ocmp_spmv_axpby': [P, D, P, D, P, P],
     'ocmp_matrix_autotune': [P, P, P, P, P, P, P],
     'ocmp_solver_create': [P, C.POINTER(SolveParams), C.POINTER(P)],
     'ocmp_solver_destroy': [P],

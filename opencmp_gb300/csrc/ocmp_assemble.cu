@@ -16,6 +16,9 @@
 // integrands (max(w.n, 0)) are not polynomial.
 #include <cuda_runtime.h>
 
+#include <cmath>
+#include <vector>
+
 #include "ocmp_internal.h"
 #include "ocmp_spmv.cuh"
 
@@ -68,7 +71,7 @@ __device__ __forceinline__ void element_geo(const double* __restrict__ X, const 
 }
 
 struct FormArgs {
-    double mass, diff, dt, ipc, w0, w1, w2;
+    double mass, diff, dt, dt_skel, ipc, w0, w1, w2;
     const double* wind_vtx;
     int wind_kind;
     uint32_t outflow, wn, nitsche;
@@ -189,7 +192,7 @@ __global__ void interior_facet_kernel(int64_t nif, const double* __restrict__ X,
         const double jv = iL ? vi : -vi;
         const double avn = 0.5 * dni;
         const double wn = wind_dot_n<D>(a, conn, eL, flam + ((size_t)fL * nfq + q) * (D + 1), nrm);
-        const double wq = fw[q] * meas * a.dt;
+        const double wq = fw[q] * meas * a.dt_skel;
 #pragma unroll
         for (int j = 0; j < 2 * L; j++) {
             const bool jL = j < L;
@@ -751,7 +754,8 @@ __global__ void rhs_elem_kernel(int64_t ne, const double* __restrict__ X, const 
                                 const double* __restrict__ mvec, const double* __restrict__ Rm,
                                 const int32_t* __restrict__ ebf_ptr, const int32_t* __restrict__ ebf,
                                 const int32_t* __restrict__ bfac, const double* __restrict__ bval, uint32_t bval_mask,
-                                const double* __restrict__ gval, int is_l2, int nfq, const double* __restrict__ fw,
+                                const double* __restrict__ gval, const double* __restrict__ bfq,
+                                const double* __restrict__ gfq, int is_l2, int nfq, const double* __restrict__ fw,
                                 const double* __restrict__ fphi, const double* __restrict__ fdphi,
                                 const double* __restrict__ flam, double* __restrict__ Fe) {
     int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
@@ -800,11 +804,13 @@ __global__ void rhs_elem_kernel(int64_t ne, const double* __restrict__ X, const 
             const size_t base = ((size_t)lf * nfq + q) * L;
             const double wq = fw[q] * meas * dt;
             const double wn = hg ? wind_dot_n<D>(a, conn, e, flam + ((size_t)lf * nfq + q) * (D + 1), nrm) : 0.0;
+            const double bv = hb ? (bfq ? bfq[(size_t)b * nfq + q] : bval[lab]) : 0.0;
+            const double gv = hg ? (gfq ? gfq[(size_t)b * nfq + q] : gval[lab]) : 0.0;
 #pragma unroll
             for (int i = 0; i < L; i++) {
                 const double vi = fphi[base + i];
                 double t = 0;
-                if (hb) t += bval[lab] * vi;
+                if (hb) t += bv * vi;
                 if (hg) {
                     double dni = 0;
 #pragma unroll
@@ -814,7 +820,6 @@ __global__ void rhs_elem_kernel(int64_t ne, const double* __restrict__ X, const 
                         for (int c = 0; c < D; c++) gr += g.Ji[c][r] * fdphi[(base + i) * D + c];
                         dni += gr * nrm[r];
                     }
-                    const double gv = gval[lab];
                     t += a.diff * gv * (alpha * vi - dni) - vi * gv * fmin(wn, 0.0);
                 }
                 out[i] += wq * t;
@@ -826,12 +831,37 @@ __global__ void rhs_elem_kernel(int64_t ne, const double* __restrict__ X, const 
 }
 
 __global__ void rhs_gather_kernel(int64_t ndof, const int32_t* __restrict__ inc_ptr, const int32_t* __restrict__ inc,
-                                  const double* __restrict__ Fe, double* __restrict__ b) {
+                                  const double* __restrict__ Fe, double* __restrict__ b, int accumulate) {
     int64_t d = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (d >= ndof) return;
     double acc = 0;
     for (int k = inc_ptr[d]; k < inc_ptr[d + 1]; k++) acc += Fe[inc[k]];
-    b[d] = acc;
+    b[d] = accumulate ? b[d] + acc : acc;
+}
+
+// per element: |det J| sum_q w_q (u_h(x_q) - f_q)^2 (f from the quadrature-point array or a constant)
+template <int D, int L>
+__global__ void l2_error_kernel(int64_t ne, const double* __restrict__ X, const int32_t* __restrict__ conn,
+                                const int32_t* __restrict__ dofs, const double* __restrict__ u, int nq,
+                                const double* __restrict__ qw, const double* __restrict__ qphi,
+                                const double* __restrict__ fq, double fconst, double* __restrict__ out) {
+    const int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (e >= ne) return;
+    Geo g;
+    double x0[3];
+    element_geo<D>(X, conn, e, g, x0);
+    double ue[L];
+#pragma unroll
+    for (int j = 0; j < L; j++) ue[j] = u[dofs[e * L + j]];
+    double acc = 0;
+    for (int q = 0; q < nq; q++) {
+        double uh = 0;
+#pragma unroll
+        for (int j = 0; j < L; j++) uh += ue[j] * qphi[q * L + j];
+        const double d = uh - (fq ? fq[e * nq + q] : fconst);
+        acc += qw[q] * d * d;
+    }
+    out[e] = acc * g.adet;
 }
 
 __global__ void set_values_kernel(int64_t n, const int32_t* __restrict__ idx, const double* __restrict__ v,
@@ -856,11 +886,30 @@ __global__ void __launch_bounds__(256) spmv64_kernel(int64_t n, const int32_t* _
     if (r < n && lane == 0) y[r] = acc;
 }
 
+// y = alpha A x + beta y (ocmp_spmv_axpby); y is not read when beta == 0.
+template <int TPR, int U>
+__global__ void __launch_bounds__(256) spmv64_axpby_kernel(int64_t n, const int32_t* __restrict__ rp,
+                                                           const int32_t* __restrict__ col,
+                                                           const double* __restrict__ val, double alpha,
+                                                           const double* __restrict__ x, double beta,
+                                                           double* __restrict__ y) {
+    const int64_t r = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) / TPR;
+    const int lane = threadIdx.x % TPR;
+    int32_t a = 0, b = 0;
+    if (r < n) {
+        a = __ldg(rp + r);
+        b = __ldg(rp + r + 1);
+    }
+    const double acc = row_dot<double, double, TPR, U>(a, b, col, val, x, lane);
+    if (r < n && lane == 0) y[r] = beta != 0.0 ? alpha * acc + beta * y[r] : alpha * acc;
+}
+
 FormArgs make_args(const ocmp_space_s* s, const ocmp_form_t* f) {
     FormArgs a;
     a.mass = f->mass;
     a.diff = f->diff;
     a.dt = f->dt;
+    a.dt_skel = f->skeleton_own_dt ? f->skeleton_dt : f->dt;
     a.ipc = f->ipc;
     a.w0 = f->wind[0];
     a.w1 = f->wind[1];
@@ -970,8 +1019,8 @@ int rhs_impl(ocmp_space_s* s, const ocmp_form_t* f, const ocmp_rhs_t* r, double*
     rhs_elem_kernel<D, L><<<nblk(ne, 128), 128, 0, st>>>(
         ne, mesh->dX, mesh->dconn, s->d_dofs, a, r->dt, r->src_kind, r->src_const, r->src_qp, r->mass, r->uprev,
         s->T.nq, s->d_qw, s->d_qphi, s->d_mvec, s->d_Rc, s->d_ebf_ptr, s->d_ebf, s->d_bfac, dvals, r->bval_mask,
-        dvals + 32, s->kind == OCMP_L2, s->T.nfq, s->d_fw, s->d_fphi, s->d_fdphi, s->d_flam, s->d_Fe);
-    rhs_gather_kernel<<<nblk(s->ndof, 256), 256, 0, st>>>(s->ndof, s->d_inc_ptr, s->d_inc, s->d_Fe, b);
+        dvals + 32, r->bval_fq, r->gval_fq, s->kind == OCMP_L2, s->T.nfq, s->d_fw, s->d_fphi, s->d_fdphi, s->d_flam, s->d_Fe);
+    rhs_gather_kernel<<<nblk(s->ndof, 256), 256, 0, st>>>(s->ndof, s->d_inc_ptr, s->d_inc, s->d_Fe, b, r->accumulate);
     OCMP_CUDA(cudaFreeAsync(dvals, st));
     OCMP_CUDA(cudaGetLastError());
     return OCMP_OK;
@@ -998,6 +1047,29 @@ int launch_assemble_matrix(ocmp_matrix_s* m, const ocmp_form_t* f, cudaStream_t 
 
 int launch_assemble_rhs(ocmp_space_s* s, const ocmp_form_t* f, const ocmp_rhs_t* r, double* b, cudaStream_t st) {
     OCMP_DISPATCH(rhs_impl, s, f, r, b, st);
+}
+
+namespace {
+template <int D, int L>
+int l2_impl(ocmp_space_s* s, const double* u, const double* fq, double fconst, double* result, cudaStream_t st) {
+    const int64_t ne = s->mesh->ne;
+    double* per = nullptr;
+    OCMP_CUDA(cudaMallocAsync((void**)&per, sizeof(double) * ne, st));
+    l2_error_kernel<D, L><<<nblk(ne, 128), 128, 0, st>>>(ne, s->mesh->dX, s->mesh->dconn, s->d_dofs, u, s->T.nq, s->d_qw,
+                                                         s->d_qphi, fq, fconst, per);
+    std::vector<double> h(ne);
+    OCMP_CUDA(cudaMemcpyAsync(h.data(), per, sizeof(double) * ne, cudaMemcpyDeviceToHost, st));
+    OCMP_CUDA(cudaFreeAsync(per, st));
+    OCMP_CUDA(cudaStreamSynchronize(st));
+    double acc = 0;
+    for (double v : h) acc += v;  // element order: deterministic
+    *result = std::sqrt(acc);
+    return OCMP_OK;
+}
+}  // namespace
+
+int launch_l2_error(ocmp_space_s* s, const double* u, const double* fq, double fconst, double* result, cudaStream_t st) {
+    OCMP_DISPATCH(l2_impl, s, u, fq, fconst, result, st);
 }
 
 // Dirichlet values (base_model.py:321-341): vertex dofs of every facet with a label in `mask` take
@@ -1045,6 +1117,12 @@ int launch_set_boundary(ocmp_space_s* s, uint32_t mask, const double* gval, doub
             idx.push_back((int32_t)i);
             v.push_back(val[i]);
         }
+    return launch_scatter_values(idx, v, u, st);
+}
+
+// u[idx[k]] = v[k]; the host lists are copied through stream-ordered scratch and the call waits for
+// the copies, so the caller may release them on return.
+int launch_scatter_values(const std::vector<int32_t>& idx, const std::vector<double>& v, double* u, cudaStream_t st) {
     if (idx.empty()) return OCMP_OK;
     int32_t* didx = nullptr;
     double* dv = nullptr;
@@ -1055,7 +1133,6 @@ int launch_set_boundary(ocmp_space_s* s, uint32_t mask, const double* gval, doub
     set_values_kernel<<<nblk((int64_t)idx.size(), 256), 256, 0, st>>>((int64_t)idx.size(), didx, dv, u);
     OCMP_CUDA(cudaFreeAsync(didx, st));
     OCMP_CUDA(cudaFreeAsync(dv, st));
-    // the host vectors must outlive the async copies
     OCMP_CUDA(cudaStreamSynchronize(st));
     OCMP_CUDA(cudaGetLastError());
     return OCMP_OK;
@@ -1119,6 +1196,22 @@ int launch_spmv64(const ocmp_space_s* s, const double* vals, const double* x, do
     else if (rc.tpr == 8 && rc.u == 4) spmv64_kernel<8, 4><<<g, 256, 0, st>>>(n, s->d_rowptr, s->d_col, vals, x, y);
     else if (rc.tpr == 8) spmv64_kernel<8, 8><<<g, 256, 0, st>>>(n, s->d_rowptr, s->d_col, vals, x, y);
     else spmv64_kernel<16, 8><<<g, 256, 0, st>>>(n, s->d_rowptr, s->d_col, vals, x, y);
+    OCMP_CUDA(cudaGetLastError());
+    return OCMP_OK;
+}
+
+int launch_spmv_axpby(const ocmp_space_s* s, const double* vals, double alpha, const double* x, double beta, double* y,
+                      cudaStream_t st) {
+    const RowCfg rc = row_cfg(s);
+    const int64_t n = s->ndof;
+    const unsigned g = nblk(n * rc.tpr, 256);
+    const int32_t *rp = s->d_rowptr, *col = s->d_col;
+    if (rc.tpr == 2) spmv64_axpby_kernel<2, 4><<<g, 256, 0, st>>>(n, rp, col, vals, alpha, x, beta, y);
+    else if (rc.tpr == 4 && rc.u == 4) spmv64_axpby_kernel<4, 4><<<g, 256, 0, st>>>(n, rp, col, vals, alpha, x, beta, y);
+    else if (rc.tpr == 4) spmv64_axpby_kernel<4, 8><<<g, 256, 0, st>>>(n, rp, col, vals, alpha, x, beta, y);
+    else if (rc.tpr == 8 && rc.u == 4) spmv64_axpby_kernel<8, 4><<<g, 256, 0, st>>>(n, rp, col, vals, alpha, x, beta, y);
+    else if (rc.tpr == 8) spmv64_axpby_kernel<8, 8><<<g, 256, 0, st>>>(n, rp, col, vals, alpha, x, beta, y);
+    else spmv64_axpby_kernel<16, 8><<<g, 256, 0, st>>>(n, rp, col, vals, alpha, x, beta, y);
     OCMP_CUDA(cudaGetLastError());
     return OCMP_OK;
 }

@@ -861,6 +861,7 @@ int ocmp_space_info(ocmp_space_t s, ocmp_space_info_t* info) {
     info->n_interior_facets = s->nif;
     info->n_boundary_facets = s->nbf;
     info->n_contrib = s->ncontrib;
+    info->nfq = s->T.nfq;
     return OCMP_OK;
 }
 
@@ -904,6 +905,189 @@ int ocmp_space_quad_points(ocmp_space_t s, double* xyz) {
 int ocmp_set_boundary(ocmp_space_t s, uint32_t mask, const double* gval, double* u, void* stream) {
     if (!s || !gval || !u) return fail(OCMP_ERR_ARG, "ocmp_set_boundary: null argument");
     return launch_set_boundary(s, mask, gval, u, (cudaStream_t)stream);
+}
+
+int ocmp_space_facet_quad_points(ocmp_space_t s, double* xyz) {
+    if (!s || !xyz) return fail(OCMP_ERR_ARG, "ocmp_space_facet_quad_points: null argument");
+    const int D = s->dim, nvp = D + 1, nfq = s->T.nfq;
+    const ocmp_mesh_s* m = s->mesh;
+    for (int64_t b = 0; b < s->nbf; b++) {
+        const int64_t e = s->bfac[3 * b];
+        const int lf = s->bfac[3 * b + 1];
+        const int32_t* v = &m->conn[e * nvp];
+        for (int q = 0; q < nfq; q++) {
+            const double* lam = &s->T.flam[((size_t)lf * nfq + q) * nvp];
+            for (int r = 0; r < D; r++) {
+                double acc = 0;
+                for (int a = 0; a < nvp; a++) acc += lam[a] * m->X[(int64_t)v[a] * D + r];
+                xyz[(b * nfq + q) * D + r] = acc;
+            }
+        }
+    }
+    return OCMP_OK;
+}
+
+int ocmp_space_boundary_facets(ocmp_space_t s, int32_t* out) {
+    if (!s || !out) return fail(OCMP_ERR_ARG, "ocmp_space_boundary_facets: null argument");
+    std::memcpy(out, s->bfac.data(), s->bfac.size() * sizeof(int32_t));
+    return OCMP_OK;
+}
+
+namespace {
+// Walks the facets whose label is in `mask` in the space's boundary-facet order. Per facet the
+// sample points are: its D vertices; for order >= 2 the (p+2)-point Gauss rule on each of its edges
+// (local vertex pairs in ascending order); for a tetrahedral face at order 3 the collapsed
+// (p+2)^2-point rule on the face. With `xyz` the points are written; with `g` (samples at those
+// points) the constrained dofs and their values are appended to idx/val: vertex dofs take g, edge
+// bubbles the 1D L2 projection of what the vertex part leaves, face bubbles the 2D projection of what
+// vertices and edges leave. A dof met again on a later facet takes the later facet's value.
+int64_t walk_boundary(const ocmp_space_s* s, uint32_t mask, const double* g, double* xyz, std::vector<int32_t>* idx,
+                      std::vector<double>* val) {
+    const int D = s->dim, nvp = D + 1, p = s->order, L = s->nloc;
+    const int nedge = nvp * (nvp - 1) / 2;
+    std::vector<double> x1, w1, x2, w2;
+    const int n1 = simplex_rule(1, p + 2, x1, w1), n2 = simplex_rule(2, p + 2, x2, w2);
+    const ocmp_mesh_s* m = s->mesh;
+    std::vector<double> dval;
+    std::vector<uint8_t> own;
+    if (g) {
+        dval.assign(s->ndof, 0.0);
+        own.assign(s->ndof, 0);
+    }
+    auto edge_id = [nvp](int a, int b) {
+        int k = 0;
+        for (int i = 0; i < nvp; i++)
+            for (int j = i + 1; j < nvp; j++, k++)
+                if (i == a && j == b) return k;
+        return -1;
+    };
+    int64_t np = 0;
+    Dn bb[kMaxLoc];
+    for (int64_t b = 0; b < s->nbf; b++) {
+        const int lab = s->bfac[3 * b + 2];
+        if (lab < 0 || lab >= 32 || !((mask >> lab) & 1u)) continue;
+        const int64_t e = s->bfac[3 * b];
+        const int lf = s->bfac[3 * b + 1];
+        const int32_t* cv = &m->conn[e * nvp];
+        int av[3], c = 0;
+        for (int v = 0; v < nvp; v++)
+            if (v != lf) av[c++] = v;
+        double coef[kMaxLoc] = {0};
+        std::vector<int> touched;
+        auto point = [&](const double* lam) {
+            if (xyz)
+                for (int r = 0; r < D; r++) {
+                    double acc = 0;
+                    for (int a = 0; a < nvp; a++) acc += lam[a] * m->X[(int64_t)cv[a] * D + r];
+                    xyz[np * D + r] = acc;
+                }
+            return np++;
+        };
+        auto eval = [&](const double* lam) {
+            double xi[3];
+            for (int k = 0; k < D; k++) xi[k] = lam[k + 1];
+            basis(s->kind, D, p, xi, bb);
+        };
+        for (int k = 0; k < D; k++) {
+            double lam[4] = {0, 0, 0, 0};
+            lam[av[k]] = 1;
+            const int64_t q = point(lam);
+            if (g) coef[av[k]] = g[q];
+            touched.push_back(av[k]);
+        }
+        if (p >= 2)
+            for (int i = 0; i < D; i++)
+                for (int j = i + 1; j < D; j++) {
+                    const int a = av[i], bv = av[j], e0 = nvp + edge_id(a, bv) * (p - 1);
+                    double M[2][2] = {{0, 0}, {0, 0}}, r[2] = {0, 0};
+                    for (int q = 0; q < n1; q++) {
+                        double lam[4] = {0, 0, 0, 0};
+                        lam[a] = 1 - x1[q];
+                        lam[bv] = x1[q];
+                        const int64_t pi = point(lam);
+                        if (!g) continue;
+                        eval(lam);
+                        const double res = g[pi] - coef[a] * bb[a].v - coef[bv] * bb[bv].v;
+                        for (int k = 0; k < p - 1; k++) {
+                            r[k] += w1[q] * bb[e0 + k].v * res;
+                            for (int l = 0; l < p - 1; l++) M[k][l] += w1[q] * bb[e0 + k].v * bb[e0 + l].v;
+                        }
+                    }
+                    if (g) {
+                        if (p == 2) {
+                            coef[e0] = r[0] / M[0][0];
+                        } else {
+                            const double det = M[0][0] * M[1][1] - M[0][1] * M[1][0];
+                            coef[e0] = (M[1][1] * r[0] - M[0][1] * r[1]) / det;
+                            coef[e0 + 1] = (M[0][0] * r[1] - M[1][0] * r[0]) / det;
+                        }
+                    }
+                    for (int k = 0; k < p - 1; k++) touched.push_back(e0 + k);
+                }
+        if (D == 3 && p == 3) {
+            int fid = 0;
+            for (int a = 0; a < nvp; a++)
+                for (int b2 = a + 1; b2 < nvp; b2++)
+                    for (int c2 = b2 + 1; c2 < nvp; c2++, fid++)
+                        if (a == av[0] && b2 == av[1] && c2 == av[2]) goto found;
+        found:
+            const int f0 = nvp + nedge * (p - 1) + fid;
+            double num = 0, den = 0;
+            for (int q = 0; q < n2; q++) {
+                double lam[4] = {0, 0, 0, 0};
+                lam[av[0]] = 1 - x2[2 * q] - x2[2 * q + 1];
+                lam[av[1]] = x2[2 * q];
+                lam[av[2]] = x2[2 * q + 1];
+                const int64_t pi = point(lam);
+                if (!g) continue;
+                eval(lam);
+                double res = g[pi];
+                for (int t : touched) res -= coef[t] * bb[t].v;
+                num += w2[q] * bb[f0].v * res;
+                den += w2[q] * bb[f0].v * bb[f0].v;
+            }
+            if (g) coef[f0] = num / den;
+            touched.push_back(f0);
+        }
+        if (g)
+            for (int t : touched) {
+                const int32_t d = s->dofs[e * L + t];
+                dval[d] = coef[t];
+                own[d] = 1;
+            }
+    }
+    if (g)
+        for (int64_t i = 0; i < s->ndof; i++)
+            if (own[i]) {
+                idx->push_back((int32_t)i);
+                val->push_back(dval[i]);
+            }
+    return np;
+}
+}  // namespace
+
+int ocmp_boundary_points(ocmp_space_t s, uint32_t mask, int64_t* npts, double* xyz) {
+    if (!s || !npts) return fail(OCMP_ERR_ARG, "ocmp_boundary_points: null argument");
+    if (s->kind != OCMP_H1) {
+        *npts = 0;
+        return OCMP_OK;
+    }
+    *npts = walk_boundary(s, mask, nullptr, xyz, nullptr, nullptr);
+    return OCMP_OK;
+}
+
+int ocmp_set_boundary_values(ocmp_space_t s, uint32_t mask, const double* g, double* u, void* stream) {
+    if (!s || !g || !u) return fail(OCMP_ERR_ARG, "ocmp_set_boundary_values: null argument");
+    if (s->kind != OCMP_H1) return OCMP_OK;
+    std::vector<int32_t> idx;
+    std::vector<double> val;
+    walk_boundary(s, mask, g, nullptr, &idx, &val);
+    return launch_scatter_values(idx, val, u, (cudaStream_t)stream);
+}
+
+int ocmp_l2_error(ocmp_space_t s, const double* u, const double* fq, double fconst, double* result, void* stream) {
+    if (!s || !u || !result) return fail(OCMP_ERR_ARG, "ocmp_l2_error: null argument");
+    return launch_l2_error(s, u, fq, fconst, result, (cudaStream_t)stream);
 }
 
 int ocmp_matrix_create_batch(ocmp_space_t s, int32_t nbatch, int32_t flags, ocmp_matrix_t* out) {
@@ -1010,6 +1194,11 @@ int ocmp_matrix_autotune(ocmp_matrix_t m, const double* x, double* y, void* stre
 int ocmp_spmv(ocmp_matrix_t m, const double* x, double* y, void* stream) {
     if (!m || !x || !y) return fail(OCMP_ERR_ARG, "ocmp_spmv: null argument");
     return launch_spmv64(m->space, m->vals, x, y, (cudaStream_t)stream);
+}
+
+int ocmp_spmv_axpby(ocmp_matrix_t m, double alpha, const double* x, double beta, double* y, void* stream) {
+    if (!m || !x || !y) return fail(OCMP_ERR_ARG, "ocmp_spmv_axpby: null argument");
+    return launch_spmv_axpby(m->space, m->vals, alpha, x, beta, y, (cudaStream_t)stream);
 }
 
 }  // extern "C"

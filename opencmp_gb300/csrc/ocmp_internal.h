@@ -153,7 +153,11 @@ namespace ocmp {
 int launch_assemble_matrix(ocmp_matrix_s* m, const ocmp_form_t* f, cudaStream_t st);
 int launch_assemble_rhs(ocmp_space_s* s, const ocmp_form_t* f, const ocmp_rhs_t* r, double* b, cudaStream_t st);
 int launch_set_boundary(ocmp_space_s* s, uint32_t mask, const double* gval, double* u, cudaStream_t st);
+int launch_scatter_values(const std::vector<int32_t>& idx, const std::vector<double>& v, double* u, cudaStream_t st);
+int launch_l2_error(ocmp_space_s* s, const double* u, const double* fq, double fconst, double* result, cudaStream_t st);
 int launch_spmv64(const ocmp_space_s* s, const double* vals, const double* x, double* y, cudaStream_t st);
+int launch_spmv_axpby(const ocmp_space_s* s, const double* vals, double alpha, const double* x, double beta, double* y,
+                      cudaStream_t st);
 int autotune_spmv(ocmp_space_s* s, const double* vals, const double* x, double* y, cudaStream_t st, int reps,
                   int* best_tpr, int* best_u, float* best_ms);
 }  // namespace ocmp

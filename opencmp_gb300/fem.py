@@ -102,6 +102,42 @@ class Space:
         LB.call('ocmp_space_quad_points', self.h, _ptr(x))
         return x
 
+    def l2_error(self, u: torch.Tensor, f=None, stream=None) -> float:
+        """||u_h - f||_L2; f a constant, a (ne, nq) tensor of quadrature-point values, or None (= 0)."""
+        out = C.c_double(0)
+        if isinstance(f, torch.Tensor):
+            LB.call('ocmp_l2_error', self.h, _ptr(u), _ptr(f), 0.0, C.byref(out), _stream(stream))
+        else:
+            LB.call('ocmp_l2_error', self.h, _ptr(u), None, float(f or 0.0), C.byref(out), _stream(stream))
+        return out.value
+
+    def boundary_facets(self) -> np.ndarray:
+        """(element, local facet, label) of each boundary facet, in the space's facet order."""
+        out = np.empty((self.info.n_boundary_facets, 3), np.int32)
+        LB.call('ocmp_space_boundary_facets', self.h, _ptr(out))
+        return out
+
+    def facet_quad_points(self) -> np.ndarray:
+        """(nbf, nfq, dim) quadrature points of the boundary facets (where bval_fq/gval_fq are sampled)."""
+        x = np.empty((self.info.n_boundary_facets, self.info.nfq, self.mesh.dim), np.float64)
+        LB.call('ocmp_space_facet_quad_points', self.h, _ptr(x))
+        return x
+
+    def boundary_points(self, mask: int) -> np.ndarray:
+        """Points at which space-dependent Dirichlet data on the labels of `mask` is sampled."""
+        n = C.c_int64(0)
+        LB.call('ocmp_boundary_points', self.h, mask, C.byref(n), None)
+        x = np.empty((n.value, self.mesh.dim), np.float64)
+        if n.value:
+            LB.call('ocmp_boundary_points', self.h, mask, C.byref(n), _ptr(x))
+        return x
+
+    def set_boundary_values(self, mask: int, g: np.ndarray, u: torch.Tensor, stream=None):
+        """Dirichlet dofs of u on the labels of `mask` from samples g at ``boundary_points(mask)``."""
+        g = np.ascontiguousarray(g, np.float64)
+        if g.size:
+            LB.call('ocmp_set_boundary_values', self.h, mask, _ptr(g), _ptr(u), _stream(stream))
+
     def set_boundary(self, labels: Dict[int, float], u: torch.Tensor, mask: Optional[int] = None, stream=None):
         g = np.zeros(32, np.float64)
         m = 0
@@ -131,7 +167,8 @@ def make_form(mass=0.0, diff=0.0, dt=1.0, wind=None, wind_vtx: Optional[torch.Te
 
 def make_rhs(dt=1.0, src_const=None, src_qp: Optional[torch.Tensor] = None, mass=0.0,
              uprev: Optional[torch.Tensor] = None, bval: Optional[Dict[int, float]] = None,
-             gval: Optional[Dict[int, float]] = None) -> LB.Rhs:
+             gval: Optional[Dict[int, float]] = None, bval_fq: Optional[torch.Tensor] = None,
+             gval_fq: Optional[torch.Tensor] = None, bval_mask: Optional[int] = None) -> LB.Rhs:
     r = LB.Rhs()
     r.dt, r.mass = dt, mass
     r.src_kind = LB.SRC_NONE
@@ -146,6 +183,12 @@ def make_rhs(dt=1.0, src_const=None, src_qp: Optional[torch.Tensor] = None, mass
         r.bval_mask |= 1 << lab
     for lab, v in (gval or {}).items():
         r.gval[lab] = v
+    if bval_mask is not None:
+        r.bval_mask = bval_mask
+    if bval_fq is not None:
+        r.bval_fq = bval_fq.data_ptr()
+    if gval_fq is not None:
+        r.gval_fq = gval_fq.data_ptr()
     return r
 
 

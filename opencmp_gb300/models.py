@@ -1,0 +1,363 @@
+"""OpenCMP models on the GPU path.
+
+Mirrors ``opencmp/models`` for the models of the hot path: :class:`Poisson`
+(``opencmp/models/poisson.py:71-158``) and :class:`MultiComponentINS` with ``velocity_fixed = True``
+(``opencmp/models/multi_component_ins.py:158-388``: diffusion, conservative advection, upwind
+facets, outflow on total-flux and unlabelled boundaries, the Neumann (w.n) half, DG Dirichlet
+terms). The registry and lookup follow ``opencmp/models/__init__.py:30-36`` and
+``opencmp/models/misc.py:27-50``.
+
+Each model variable (Poisson's u; each MCINS component) is a scalar GPU space with its matrices and
+Krylov solver. OpenCMP assembles the MCINS components in one compound space; with the velocity fixed
+and no reactions the compound system is block diagonal, so solving the components one after another
+gives the same solution.
+
+OpenCMP splits each model's operator into a *time-coefficient* part (the interior-facet DG terms,
+always implicit) and an *ODE* part (everything else), which the time schemes weight
+(``time_integration_schemes.py``). The forms built here keep that split: ``dt`` scales the ODE terms
+and ``skeleton_dt`` the interior-facet terms.
+"""
+from __future__ import annotations
+
+from typing import Dict, List, Optional
+
+import numpy as np
+import torch
+
+from . import _lib as LB
+from . import fem
+from .config import ConfigParser, Expr, load_sub_config, parse, value_map
+from .mesh import load_mesh
+
+
+def _scalar_at(v, t) -> Optional[float]:
+    """The value as a float when it does not depend on x, y, z (None otherwise)."""
+    if isinstance(v, Expr):
+        if v.depends_on_space:
+            return None
+        return float(v(None, t))
+    if v is None:
+        return None
+    return float(v)
+
+
+def _at(v, X, t):
+    """A parsed config value at the points X (..., dim) and time t."""
+    if isinstance(v, Expr):
+        return v(X, t)
+    return np.full(X.shape[:-1], float(v))
+
+
+class Variable:
+    """One scalar unknown: its GPU space, system and operator matrices, solver and solution."""
+
+    def __init__(self, model: 'Model', name: str, element: str):
+        self.model = model
+        self.name = name
+        self.kind = 'L2' if (model.DG or element == 'L2') else 'H1'
+        bc = model.bc
+        self.dirichlet = bc.get('dirichlet', {}).get(name, {})
+        self.neumann = bc.get('neumann', {}).get(name, {})
+        self.total_flux = bc.get('total_flux', {}).get(name, {})
+        if bc.get('robin', {}).get(name) or bc.get('surface_rxn', {}).get(name):
+            raise NotImplementedError('Robin and surface-reaction boundary conditions are not on the GPU path')
+        names = set(model.mesh.bc_names)
+        for d in (self.dirichlet, self.neumann, self.total_flux):
+            for marker in d:
+                if marker not in names:
+                    raise ValueError('boundary {!r} is not a label of the mesh ({})'.format(marker, sorted(names)))
+        dnames = list(self.dirichlet) if self.kind == 'H1' else []
+        self.space = fem.Space(model.mesh, self.kind, model.interp_ord, dnames, gmesh=model.gmesh)
+        P = model.solver_params
+        self.mat = fem.Matrix(self.space, jacobi64=P['precision'] == 'fp64', jacobi32=P['precision'] == 'mixed',
+                              fp32=P['method'] == 'CG' and P['precision'] == 'mixed')
+        self.solver = fem.KrylovSolver(self.mat, method=P['method'], restart=P['restart'], precond=P['precond'],
+                                       precision=P['precision'], tol=P['tol'], maxit=P['maxit'],
+                                       inner_tol=P['inner_tol'])
+        self.op = None                      # ODE-part operator, for explicit terms
+        n = self.space.ndof
+        self.u = torch.zeros(n, dtype=torch.float64, device='cuda')
+        self.b = torch.zeros(n, dtype=torch.float64, device='cuda')
+        self._qp = None
+        self._fq = None
+        self._flab = None
+        self._bpts: Dict[int, np.ndarray] = {}
+
+    # ---------------------------------------------------------------- geometry caches
+    def quad_points(self):
+        if self._qp is None:
+            self._qp = self.space.quad_points()
+        return self._qp
+
+    def _facets(self):
+        if self._fq is None:
+            self._fq = self.space.facet_quad_points()
+            self._flab = self.space.boundary_facets()[:, 2]
+        return self._fq, self._flab
+
+    def lab(self, marker: str) -> int:
+        return self.model.mesh.bc_names.index(marker)
+
+    def mask(self, markers) -> int:
+        return self.model.mesh.label_mask(list(markers))
+
+    # ---------------------------------------------------------------- boundary data
+    def facet_data(self, d: Dict[str, object], t: float, scale: float = 1.0):
+        """Per-label constants {label: scale*value}, or, when some value depends on x, y, z, the
+        values at every boundary-facet quadrature point as a device tensor (labels outside `d` 0)."""
+        consts, spatial = {}, False
+        for marker, v in d.items():
+            c = _scalar_at(v, t)
+            if c is None:
+                spatial = True
+            else:
+                consts[self.lab(marker)] = scale * c
+        if not spatial:
+            return consts, None
+        X, labs = self._facets()
+        vals = np.zeros(X.shape[:2])
+        for marker, v in d.items():
+            sel = labs == self.lab(marker)
+            if sel.any():
+                vals[sel] = scale * _at(v, X[sel], t)
+        return consts, torch.as_tensor(vals, device='cuda')
+
+    def set_dirichlet(self, t: float):
+        """gfu.Set(g_D, definedon=Dirichlet boundaries) (base_model.py:321-341)."""
+        if self.kind != 'H1' or not self.dirichlet:
+            return
+        consts = {}
+        for marker, v in self.dirichlet.items():
+            c = _scalar_at(v, t)
+            if c is not None:
+                consts[self.lab(marker)] = c
+        if consts:
+            self.space.set_boundary(consts, self.u)
+        for marker, v in self.dirichlet.items():
+            if _scalar_at(v, t) is None:
+                lab = self.lab(marker)
+                if lab not in self._bpts:
+                    self._bpts[lab] = self.space.boundary_points(1 << lab)
+                self.space.set_boundary_values(1 << lab, _at(v, self._bpts[lab], t), self.u)
+
+    def project(self, value, t: float = 0.0):
+        """Initial condition: the L2 projection of `value` onto the space (exact for constants)."""
+        if value is None:
+            self.u.zero_()
+            return
+        c = _scalar_at(value, t)
+        if c is not None and self.kind == 'H1':
+            h = np.zeros(self.space.ndof)
+            h[:self.model.mesh.nv] = c
+            self.u.copy_(torch.as_tensor(h))
+            return
+        sp = fem.Space(self.model.mesh, self.kind, self.model.interp_ord, (), gmesh=self.model.gmesh)
+        M = fem.Matrix(sp)
+        f = fem.make_form(mass=1.0)
+        M.assemble(f)
+        if c is not None:
+            rhs = fem.make_rhs(src_const=c)
+            fq = None
+        else:
+            fq = torch.as_tensor(_at(value, sp.quad_points(), t).reshape(self.model.mesh.ne, -1), device='cuda')
+            rhs = fem.make_rhs(src_qp=fq)
+        b = torch.zeros(sp.ndof, dtype=torch.float64, device='cuda')
+        fem.assemble_rhs(sp, f, rhs, b)
+        x = torch.zeros_like(b)
+        fem.KrylovSolver(M, method='CG', tol=1e-13, maxit=20000).solve(b, x)
+        self.u.copy_(x)
+
+    def source(self, t: float):
+        """(constant, quadrature-point tensor) of the source; one of them is None."""
+        fs = self.model.functions.get('source', {})
+        f = fs.get(self.name, fs.get('all'))
+        if f is None:
+            return None, None
+        c = _scalar_at(f, t)
+        if c is not None:
+            return (c if c != 0.0 else None), None
+        X = self.quad_points()
+        return None, torch.as_tensor(_at(f, X, t).reshape(self.model.mesh.ne, -1), device='cuda')
+
+
+class Model:
+    """Configuration, mesh, boundary/initial/model data (base_model.py:44-257)."""
+
+    components: List[str] = []
+
+    def __init__(self, config: ConfigParser):
+        self.config = config
+        self.run_dir = config.get_item(['OTHER', 'run_dir'], str)
+        self.mesh = load_mesh(config.get_item(['MESH', 'filename'], str))
+        self.gmesh = fem.GPUMesh(self.mesh)
+        self.DG = config.get_item(['DG', 'DG'], bool)
+        self.ipc = config.get_item(['DG', 'interior_penalty_coefficient'], float)
+        self.interp_ord = config.get_item(['FINITE ELEMENT SPACE', 'interpolant_order'], int)
+        self.elements = config.get_dict(['FINITE ELEMENT SPACE', 'elements'], all_str=True)
+        bc = load_sub_config(self.run_dir, 'bc')
+        self.bc = {k.lower(): value_map(bc, k) for k in (bc.sections() if bc else [])}
+        ic = load_sub_config(self.run_dir, 'ic')
+        self.ic = value_map(ic, ic.sections()[0]) if ic and ic.sections() else {}
+        mc = load_sub_config(self.run_dir, 'model')
+        self.params = value_map(mc, 'PARAMETERS')
+        self.functions = value_map(mc, 'FUNCTIONS')
+        rs = load_sub_config(self.run_dir, 'ref_sol')
+        self.ref_sol: Dict[str, object] = {}
+        self.metrics: Dict[str, List[str]] = {}
+        if rs is not None:
+            if rs.has_section('REFERENCE SOLUTIONS'):
+                self.ref_sol = {k: parse(v) for k, v in rs.items('REFERENCE SOLUTIONS')}
+            if rs.has_section('METRICS'):
+                self.metrics = {k: [s.strip() for s in v.split(',') if s.strip()] for k, v in rs.items('METRICS')}
+        self.solver_params = self._solver_params()
+        self.vars: Dict[str, Variable] = {}
+
+    def _solver_params(self) -> dict:
+        c = self.config
+        ls = c.get_item(['SOLVER', 'linear_solver'], str)
+        pre = c.get_item(['SOLVER', 'preconditioner'], str)
+        tol = c.get_item(['SOLVER', 'linear_tolerance'], float)
+        maxit = c.get_item(['SOLVER', 'linear_max_iterations'], int)
+        # 'default' / 'direct' (a sparse LU in OpenCMP, base_model.py:918) run as FP64 Krylov to 1e-12.
+        if ls in ('default', 'direct'):
+            method, tol, maxit = 'GMRES', 1e-12, max(maxit, 5000)
+        elif ls == 'CG':
+            method = 'CG'
+        elif ls in ('GMRes', 'GMRES', 'MinRes', 'Richardson'):
+            method = 'GMRES'
+        else:
+            raise ValueError('No linear solver specified.')
+        precond = {'default': 'jacobi', 'local': 'jacobi', 'None': 'none', 'block_jacobi': 'block_jacobi'}.get(pre)
+        if precond is None:
+            raise NotImplementedError('preconditioner {!r} is not on the GPU path'.format(pre))
+        if self.DG and pre == 'default':
+            precond = 'block_jacobi'
+        prec = c.get_item(['SOLVER', 'gpu_precision'], str)
+        return dict(method=method, precond=precond, tol=max(tol, 1e-12), maxit=max(maxit, 1000),
+                    precision='mixed' if prec == 'mixed' and method == 'GMRES' else 'fp64',
+                    restart=c.get_item(['SOLVER', 'gpu_restart'], int), inner_tol=1e-4)
+
+    # ---------------------------------------------------------------- per-model terms
+    def operator(self, var: Variable) -> dict:
+        """make_form keywords of the variable's operator (no mass, no dt)."""
+        raise NotImplementedError
+
+    def boundary_rhs(self, var: Variable, t: float):
+        """((Neumann-type {label: value}, facet tensor or None), (DG Dirichlet {label: g}, tensor or None))."""
+        raise NotImplementedError
+
+    def boundary_mask(self, var: Variable) -> int:
+        """Labels that carry Neumann-type data in the linear form."""
+        raise NotImplementedError
+
+    # ---------------------------------------------------------------- forms
+    def form(self, var: Variable, mass: float, dt: float, skeleton_dt: float) -> LB.Form:
+        f = fem.make_form(mass=mass, dt=dt, **self.operator(var))
+        f.skeleton_own_dt, f.skeleton_dt = 1, skeleton_dt
+        return f
+
+    def rhs(self, var: Variable, t: float, dt: float, mass: float = 0.0, uprev=None, accumulate: bool = False):
+        """The linear form and the device tensors it points to (keep them alive until assembled)."""
+        c, fq = var.source(t)
+        (bc, bq), (gc, gq) = self.boundary_rhs(var, t)
+        r = fem.make_rhs(dt=dt, src_const=c, src_qp=fq, mass=mass, uprev=uprev, bval=bc, gval=gc, bval_fq=bq,
+                         gval_fq=gq, bval_mask=self.boundary_mask(var))
+        r.accumulate = int(accumulate)
+        return r, (fq, bq, gq)
+
+    def setup(self):
+        for name in self.components:
+            self.vars[name] = Variable(self, name, self.elements.get(name, 'H1'))
+        for name, v in self.vars.items():
+            v.project(self.ic.get(name, {}).get('all', 0.0), 0.0)
+
+    def errors(self, t: float) -> List[str]:
+        """``L2 norm in <var>: <value>`` lines, as opencmp/helpers/error.py:238-301 prints them."""
+        lines = []
+        for metric, names in self.metrics.items():
+            if metric.lower() != 'l2_norm':
+                raise NotImplementedError('{} is not on the GPU path'.format(metric))
+            for name in names:
+                v = self.vars[name]
+                ref = self.ref_sol.get(name, 0.0)
+                c = _scalar_at(ref, t)
+                if c is not None:
+                    err = v.space.l2_error(v.u, c)
+                else:
+                    fq = torch.as_tensor(_at(ref, v.quad_points(), t).reshape(self.mesh.ne, -1), device='cuda')
+                    err = v.space.l2_error(v.u, fq)
+                lines.append('{0} in {1}: {2}'.format(metric.replace('_', ' '), name, err))
+        return lines
+
+
+class Poisson(Model):
+    components = ['u']
+
+    def __init__(self, config):
+        super().__init__(config)
+        dc = self.params.get('diffusion_coefficient', {}).get('all', 1.0)
+        self.dc = _scalar_at(dc, 0.0)
+        if self.dc is None:
+            raise NotImplementedError('a space-dependent diffusion coefficient is not on the GPU path')
+
+    def operator(self, var):
+        return dict(diff=self.dc, ipc=self.ipc, dg=self.DG, nitsche_mask=var.mask(var.dirichlet) if self.DG else 0)
+
+    def boundary_rhs(self, var, t):
+        neu = var.facet_data(var.neumann, t, self.dc)
+        dir_ = var.facet_data(var.dirichlet, t) if self.DG else ({}, None)
+        return neu, dir_
+
+    def boundary_mask(self, var):
+        return var.mask(var.neumann)
+
+
+class MultiComponentINS(Model):
+    """Fixed-velocity transport of the configured components (``velocity_fixed = True``)."""
+
+    def __init__(self, config):
+        super().__init__(config)
+        if not config.get_item(['OTHER', 'velocity_fixed'], bool):
+            raise NotImplementedError('MultiComponentINS runs on the GPU path with velocity_fixed = True')
+        self.components = config.get_list(['OTHER', 'component_names'], str)
+        self.D = {k: _scalar_at(v, 0.0) for k, v in self.params.get('diffusion_coefficients', {}).items()}
+        W = self.ic.get('u', {}).get('all')
+        self._wind_vtx = None
+        self._wind_const = None
+        if isinstance(W, Expr) and W.depends_on_space:
+            self._wind_vtx = torch.as_tensor(np.ascontiguousarray(W(self.mesh.coords, 0.0)), device='cuda')
+        elif W is not None:
+            self._wind_const = tuple(np.ravel(W(None, 0.0) if isinstance(W, Expr) else [float(W)]))
+
+    def operator(self, var):
+        flux = set(self.mesh.bc_names) - set(var.dirichlet) - set(var.neumann)
+        if var.neumann and self.D[var.name] == 0:
+            raise ValueError('Trying to apply a neuman boundary condition for purely advective flow '
+                             '(diffusion coefficient is 0).')
+        return dict(diff=self.D[var.name], wind=self._wind_const, wind_vtx=self._wind_vtx, ipc=self.ipc, dg=self.DG,
+                    outflow_mask=var.mask(flux), wn_mask=var.mask(var.neumann),
+                    nitsche_mask=var.mask(var.dirichlet) if self.DG else 0)
+
+    def boundary_rhs(self, var, t):
+        d = dict(var.neumann)
+        d.update(var.total_flux)
+        neu = var.facet_data(d, t, -1.0)
+        dir_ = var.facet_data(var.dirichlet, t) if self.DG else ({}, None)
+        return neu, dir_
+
+    def boundary_mask(self, var):
+        return var.mask(list(var.neumann) + list(var.total_flux))
+
+
+models_dict = {'Poisson': Poisson, 'MultiComponentINS': MultiComponentINS}
+
+
+def get_model_class(model_name: str, dim_used: bool = False):
+    """Model class by name (opencmp/models/misc.py:27-50)."""
+    if dim_used:
+        raise NotImplementedError('the diffuse interface method is not on the GPU path')
+    try:
+        return models_dict[model_name]
+    except KeyError:
+        raise KeyError('Tried to run with class {' + model_name + '}. \nThe available models are ' +
+                       str(list(models_dict.keys())))

@@ -1,0 +1,121 @@
+"""OpenCMP solvers on the GPU path (``opencmp/solvers``).
+
+:class:`StationarySolver` follows ``opencmp/solvers/stationary.py:37-77``: the forms with dt = 1 and
+no time-derivative term, one assembly, one linear solve.
+
+:class:`TransientMultiStepSolver` runs the one-step schemes of
+``opencmp/solvers/time_integration_schemes.py`` as a theta method (explicit Euler theta = 0,
+lines 25-76; Crank-Nicolson theta = 1/2, lines 134-191; implicit Euler theta = 1, lines 79-132):
+
+    (M + theta dt K_ode + dt K_skel) u^{n+1} = M u^n - (1 - theta) dt K_ode u^n
+                                              + theta L(t^{n+1}) + (1 - theta) L(t^n)
+
+where K_skel are the interior-facet DG terms (the time-coefficient form, always implicit) and K_ode
+the rest of the operator. Every step advances t, applies the Dirichlet data at the new time,
+reassembles both forms (``base_solver.py:521-607``), refreshes the preconditioner and solves from
+the previous step's solution. ``get_solver_class`` follows ``opencmp/solvers/misc.py:27-63``.
+
+For MultiComponentINS with a fixed velocity OpenCMP's stationary driver takes the nonlinear
+(Anderson) branch; here the stationary solve is the single linear solve that model reduces to.
+"""
+from __future__ import annotations
+
+import numpy as np
+
+from . import _lib as LB
+from . import fem
+from .config import ConfigParser
+from .fem import _ptr, _stream
+
+THETA = {'explicit euler': 0.0, 'crank nicolson': 0.5, 'implicit euler': 1.0}
+
+
+class Solver:
+    def __init__(self, model_class, config: ConfigParser):
+        self.config = config
+        self.model = model_class(config)
+        self.model.setup()
+        self.transient = config.get_item(['TRANSIENT', 'transient'], bool)
+        self.check_error = config.get_item(['ERROR ANALYSIS', 'check_error'], bool)
+        self.t = 0.0
+        self.infos = []
+
+    def _solve_var(self, v, theta: float, dt: float, t_new: float, t_old: float, transient: bool):
+        m = self.model
+        uprev = v.u.clone() if transient else None
+        v.set_dirichlet(t_new)
+        mass = 1.0 if transient else 0.0
+        v.mat.assemble(m.form(v, mass, theta * dt, dt))
+        v.solver.update()
+        r, keep = m.rhs(v, t_new, theta * dt, mass=mass, uprev=uprev)
+        fem.assemble_rhs(v.space, m.form(v, mass, theta * dt, dt), r, v.b)
+        if transient and theta < 1.0:
+            # (1 - theta) [L(t^n) - dt K_ode u^n]
+            r0, keep0 = m.rhs(v, t_old, (1.0 - theta) * dt, accumulate=True)
+            op_form = m.form(v, 0.0, 1.0, 0.0)
+            fem.assemble_rhs(v.space, op_form, r0, v.b)
+            if v.op is None:
+                v.op = fem.Matrix(v.space)
+            v.op.assemble(op_form)
+            LB.call('ocmp_spmv_axpby', v.op.h, -(1.0 - theta) * dt, _ptr(uprev), 1.0, _ptr(v.b), _stream(None))
+            del keep0
+        info = v.solver.solve(v.b, v.u)
+        del keep
+        self.infos.append(info)
+        return info
+
+    def _step(self, theta: float, dt: float, t_new: float, t_old: float, transient: bool):
+        for v in self.model.vars.values():
+            self._solve_var(v, theta, dt, t_new, t_old, transient)
+
+    def solve(self):
+        raise NotImplementedError
+
+    def report(self):
+        if self.check_error:
+            for ln in self.model.errors(self.t):
+                print(ln)
+
+
+class StationarySolver(Solver):
+    def solve(self):
+        self._step(1.0, 1.0, 0.0, 0.0, False)
+        return self.model.vars
+
+
+class TransientMultiStepSolver(Solver):
+    def __init__(self, model_class, config):
+        super().__init__(model_class, config)
+        self.scheme = config.get_item(['TRANSIENT', 'scheme'], str)
+        if self.scheme not in THETA:
+            raise NotImplementedError('time scheme {!r} is not on the GPU path (one of {})'.format(
+                self.scheme, sorted(THETA)))
+        self.theta = THETA[self.scheme]
+        self.t_range = config.get_list(['TRANSIENT', 'time_range'], float)
+        self.dt = config.get_item(['TRANSIENT', 'dt'], float)
+        self.t = self.t_range[0]
+
+    def solve(self):
+        """The time loop of base_solver.py:801-865: step until t reaches the end of the range
+        (np.isclose), printing the error metrics after every step when check_error is set."""
+        t1 = self.t_range[1]
+        while self.t < t1 and not np.isclose(self.t, t1):
+            t_old = self.t
+            self.t = t_old + self.dt
+            self._step(self.theta, self.dt, self.t, t_old, True)
+            if self.check_error:
+                self.report()
+        return self.model.vars
+
+
+def get_solver_class(config: ConfigParser):
+    """Solver class for the configured time scheme (opencmp/solvers/misc.py:27-63)."""
+    transient = config.get_item(['TRANSIENT', 'transient'], bool)
+    scheme = config.get_item(['TRANSIENT', 'scheme'], str)
+    if not transient:
+        return StationarySolver
+    if scheme in THETA:
+        return TransientMultiStepSolver
+    if scheme in ('euler IMEX', 'CNLF', 'SBDF') or 'adaptive' in scheme:
+        raise NotImplementedError('time scheme {!r} is not on the GPU path'.format(scheme))
+    raise TypeError('Have not implemented {} time integration yet.'.format(scheme))

@@ -30,7 +30,9 @@ def coarse_mesh():
 def ref_bounds():
     import json
     with open(os.path.join(ROOT, 'tests', 'golden', 'reference_bounds.json')) as fh:
-        return json.load(fh)
+        d = json.load(fh)
+    d['by_id'] = {t['id']: t for t in d['tests']}
+    return d
 
 
 @pytest.fixture(scope='session')

@@ -272,7 +272,7 @@ def test_reference_fixture_transient_poisson_gpu(gpu_lib, oracle, coarse_mesh, r
         sv.solve(b, x)
         u = x
     err = o.l2_error(u.cpu().numpy(), oracle.SRC_NONE, ())
-    exp = ref_bounds['poisson_transient_implicit_euler_cg']['bounds'][0]
+    exp = ref_bounds['by_id']['test_poisson.py::TestTransient::test_implicit_euler_cg']['bounds'][0]
     assert math.isclose(err, exp, rel_tol=ref_bounds['rtol']['value'], abs_tol=1e-12)
     analytic = 8 / math.pi ** 3 / math.sqrt(2) * (1 / (1 + math.pi ** 2 * 1e-3)) ** 1000
     assert abs(err - analytic) < 0.01 * analytic

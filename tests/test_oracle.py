@@ -110,7 +110,7 @@ def _transient_poisson(oracle, m, dg):
 def test_reference_fixture_transient_poisson(oracle, coarse_mesh, ref_bounds, dg):
     """pytests/full_system/poisson (implicit Euler, unit_square_coarse.vol, H1/L2 order 3)."""
     err = _transient_poisson(oracle, coarse_mesh, dg)
-    exp = ref_bounds['poisson_transient_implicit_euler_cg']['bounds'][0]
+    exp = ref_bounds['by_id']['test_poisson.py::TestTransient::test_implicit_euler_cg']['bounds'][0]
     rtol = ref_bounds['rtol']['value']
     assert math.isclose(err, exp, rel_tol=rtol, abs_tol=1e-12)           # the reference's own check
     analytic = 8 / math.pi ** 3 / math.sqrt(2) * (1 / (1 + math.pi ** 2 * 1e-3)) ** 1000
@@ -128,7 +128,7 @@ def test_reference_fixture_mcins_diffusion_convection(oracle, coarse_mesh, ref_b
 
     def ramp(t):
         return 0.5 * (0 - 1) * math.cos(t * math.pi) + 0.5 if t < 1.0 else 1.0
-    bounds = ref_bounds['mcins_diffusion_convection_implicit_euler_cg']['bounds']
+    bounds = ref_bounds['by_id']['test_mcins.py::TestDiffusionConvection::test_implicit_euler_cg']['bounds']
     for (g, ic, ref), exp in zip([(lambda t: 1.1 - ramp(t), 1.1, 0.1), (ramp, 0.0, 1.0)], bounds):
         u = s.project(oracle.SRC_CONST, (ic,))
         for k in range(1000):
