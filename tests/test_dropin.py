@@ -210,3 +210,67 @@ def test_reference_test_through_run(gpu_lib, oracle, case, capsys):
         for name, (s, u_o, _) in _oracle_case(oracle, case).items():
             u_g = sol[name].u.cpu().numpy()
             assert np.linalg.norm(u_g - u_o) <= 1e-8 * np.linalg.norm(u_o) + 1e-14, name
+
+
+def _write_mesh(tmp_path, m, name):
+    p = os.path.join(str(tmp_path), name + '.npz')
+    np.savez(p, coords=m.coords, elements=m.elements, bfacets=m.bfacets, blabels=m.blabels,
+             bc_names=np.array(m.bc_names))
+    return p
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize('dg', [False, True])
+def test_h_convergence_through_run(gpu_lib, tmp_path, capsys, dg):
+    """The reference's h-convergence Poisson fixture (space-dependent Dirichlet and Neumann data,
+    source sin-cos, order 3) through run() on refined structured meshes: the L2 error falls at
+    the order-(p+1) rate."""
+    from opencmp_gb300 import mesh as M
+    from opencmp_gb300.run import run
+    errs = []
+    for n in (4, 8, 16):
+        cfg = ConfigParser(os.path.join(FIX, 'poisson_h_convergence', 'config'))
+        cfg['MESH']['filename'] = _write_mesh(tmp_path, M.unit_square(n), 'sq{}'.format(n))
+        cfg['OTHER']['run_dir'] = os.path.join(FIX, 'poisson_h_convergence')
+        cfg['ERROR ANALYSIS']['check_error'] = 'True'
+        cfg['DG']['DG'] = str(dg)
+        run('', cfg)
+        line = capsys.readouterr().out.strip().split('\n')[-1]
+        assert line.startswith('L2 norm in u: ')
+        errs.append(float(line.split(': ')[1]))
+    rates = [math.log2(errs[i] / errs[i + 1]) for i in range(2)]
+    assert errs[-1] < 1e-5
+    assert min(rates) > (3.5 if not dg else 3.3), (errs, rates)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize('order', [1, 2, 3])
+def test_space_dependent_dirichlet_is_exact_for_polynomials(gpu_lib, order):
+    """ocmp_set_boundary_values reproduces boundary data that lies in the trace space: its dofs
+    agree with the L2 projection of the same polynomial over the whole domain."""
+    import torch
+    from opencmp_gb300 import fem, mesh as M
+    m = M.unit_square(5)
+    g = fem.Space(m, 'H1', order, m.bc_names)
+    pts = g.boundary_points(m.label_mask(m.bc_names))
+    assert pts.shape[0] > 0
+    on_bdry = np.minimum.reduce([pts[:, 0], 1 - pts[:, 0], pts[:, 1], 1 - pts[:, 1]])
+    assert np.abs(on_bdry).max() < 1e-14
+
+    def poly(X):
+        x, y = X[..., 0], X[..., 1]
+        return {1: 0.3 + x - 2 * y, 2: x * x - 0.5 * x * y + y, 3: x ** 3 - 2 * x * y * y + y * y - 0.1}[order]
+    u = torch.zeros(g.ndof, dtype=torch.float64, device='cuda')
+    g.set_boundary_values(m.label_mask(m.bc_names), poly(pts), u)
+    free = g.FreeDofs()
+    sp = fem.Space(m, 'H1', order)
+    Mm = fem.Matrix(sp)
+    f = fem.make_form(mass=1.0)
+    Mm.assemble(f)
+    fq = torch.as_tensor(poly(sp.quad_points()), device='cuda')
+    b = torch.zeros(sp.ndof, dtype=torch.float64, device='cuda')
+    fem.assemble_rhs(sp, f, fem.make_rhs(src_qp=fq), b)
+    x = torch.zeros_like(b)
+    fem.KrylovSolver(Mm, method="CG", tol=1e-13, maxit=5000).solve(b, x)
+    ub, xb = u.cpu().numpy()[~free], x.cpu().numpy()[~free]
+    assert np.abs(ub - xb).max() < 1e-9 * max(1.0, np.abs(xb).max())
