@@ -15,6 +15,7 @@ threads) on a bounded sample, the 32^3 x 6 mesh (274,625 dofs), since NGSolve ca
 from __future__ import annotations
 
 import argparse
+import contextlib
 import json
 import math
 import os
@@ -89,6 +90,37 @@ class Clocks:
                 'reasons': reasons, 'samples': len(sm)}
 
 
+class LaunchCounter:
+    """Context manager: kernels launched inside it, from the CUDA activity records torch.profiler
+    collects (this library's kernels, all kernels)."""
+
+    def __init__(self):
+        self.ours = self.total = None
+        self.prof = None
+
+    def __enter__(self):
+        from torch.profiler import ProfilerActivity, profile
+        try:
+            self.prof = profile(activities=[ProfilerActivity.CUDA])
+            self.prof.__enter__()
+        except Exception as exc:  # profiler unavailable: report no count rather than a guess
+            print('launch count unavailable: {}'.format(exc), file=sys.stderr)
+            self.prof = None
+        return self
+
+    def __exit__(self, *exc):
+        import torch
+        from torch.autograd import DeviceType
+        if self.prof is None:
+            return False
+        torch.cuda.synchronize()
+        self.prof.__exit__(None, None, None)
+        ev = [e for e in self.prof.events() if e.device_type == DeviceType.CUDA]
+        self.ours = sum(1 for e in ev if 'ocmp' in e.name)
+        self.total = len(ev)
+        return False
+
+
 def run_ours(args):
     import torch
     import torch.distributed as dist
@@ -149,7 +181,7 @@ def run_ours(args):
             guess.judge(info, used)
         stats.append((info.iterations, info.outer_iterations, info.relres0, info.relres))
 
-    def timed(kind, steps, warmup, e2e=False):
+    def timed(kind, steps, warmup, e2e=False, around=None):
         u = [u0.clone(), torch.empty_like(u0)]
         h_in = torch.empty(ndof, dtype=torch.float64, pin_memory=True)
         h_out = torch.empty(ndof, dtype=torch.float64, pin_memory=True)
@@ -169,16 +201,19 @@ def run_ours(args):
         ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         ev0.record()
         cur = warmup % 2
-        for k in range(steps):
-            if e2e:
-                u[cur].copy_(h_in, non_blocking=True)
-                step(kind, u[cur], u[1 - cur], stats)
-                h_out.copy_(u[1 - cur], non_blocking=True)
-                torch.cuda.current_stream().synchronize()
-                h_in, h_out = h_out, h_in
-            else:
-                step(kind, u[cur], u[1 - cur], stats)
-            cur = 1 - cur
+        torch.cuda.nvtx.range_push('timed_' + kind + ('_e2e' if e2e else ''))
+        with (around if around is not None else contextlib.nullcontext()):
+            for k in range(steps):
+                if e2e:
+                    u[cur].copy_(h_in, non_blocking=True)
+                    step(kind, u[cur], u[1 - cur], stats)
+                    h_out.copy_(u[1 - cur], non_blocking=True)
+                    torch.cuda.current_stream().synchronize()
+                    h_in, h_out = h_out, h_in
+                else:
+                    step(kind, u[cur], u[1 - cur], stats)
+                cur = 1 - cur
+        torch.cuda.nvtx.range_pop()
         ev1.record()
         torch.cuda.synchronize()
         ms = ev0.elapsed_time(ev1)
@@ -220,6 +255,12 @@ def run_ours(args):
     ms_opt, st_opt = timed('learned', args.steps, args.warmup)
     cl = clocks.stop()
     ms_e2e, _ = timed('learned', args.steps, args.warmup, e2e=True)
+    # the timed region replayed once more (same inputs, same iteration counts) under the profiler
+    launches = all_kernels = None
+    if not args.no_launch_count:
+        counter = LaunchCounter()
+        timed('learned', args.steps, args.warmup, around=counter)
+        launches, all_kernels = counter.ours, counter.total
 
     # SpMV roofline: FP64 CSR SpMV launches timed with CUDA events on the launching stream
     x = torch.randn(ndof, dtype=torch.float64, device='cuda')
@@ -273,7 +314,10 @@ def run_ours(args):
                      'peak': peak, 'peak_kind': peak_kind, 'unit': 'GB/s', 'frac': achieved / peak,
                      'traffic': None, 'algorithmic_bytes': spmv_bytes, 'avg_launch_ms': spmv_ms},
         'autotune': tuned,
-        'gpu_launches': None,
+        'gpu_launches': launches,
+        'gpu_launches_note': 'kernels of libopencmp_gpu.so in one replay of the {} timed steps of the optimised '
+                             'path (CUDA activity records); all kernels incl. torch copies: {}'.format(args.steps,
+                                                                                                     all_kernels),
         'clocks': cl,
         'setup_s': setup_s,
     }
@@ -453,6 +497,8 @@ def main():
     ap.add_argument('--inner-tol', type=float, default=1e-4)
     ap.add_argument('--check-every', type=int, default=8)
     ap.add_argument('--no-cpu', action='store_true')
+    ap.add_argument('--no-launch-count', action='store_true',
+                    help='skip the profiler replay that counts kernel launches (for runs under ncu)')
     ap.add_argument('--config', default='transient3d', choices=['transient3d', 'batched'])
     ap.add_argument('--instances', type=int, default=512)
     ap.add_argument('--restart-batch', type=int, default=50)

@@ -68,9 +68,14 @@ class Variable:
                     raise ValueError('boundary {!r} is not a label of the mesh ({})'.format(marker, sorted(names)))
         dnames = list(self.dirichlet) if self.kind == 'H1' else []
         self.space = fem.Space(model.mesh, self.kind, model.interp_ord, dnames, gmesh=model.gmesh)
-        P = model.solver_params
-        self.mat = fem.Matrix(self.space, jacobi64=P['precision'] == 'fp64', jacobi32=P['precision'] == 'mixed',
-                              fp32=P['method'] == 'CG' and P['precision'] == 'mixed')
+        P = dict(model.solver_params)
+        if P['method'] == 'auto':
+            # a direct solve in OpenCMP: CG where the operator is symmetric positive definite
+            P['method'] = 'CG' if model.symmetric(self) else 'GMRES'
+        if P['method'] == 'CG' and P['precision'] == 'mixed':
+            P['precision'] = 'fp64'
+        self.params = P
+        self.mat = fem.Matrix(self.space, jacobi64=P['precision'] == 'fp64', jacobi32=P['precision'] == 'mixed')
         self.solver = fem.KrylovSolver(self.mat, method=P['method'], restart=P['restart'], precond=P['precond'],
                                        precision=P['precision'], tol=P['tol'], maxit=P['maxit'],
                                        inner_tol=P['inner_tol'])
@@ -218,9 +223,10 @@ class Model:
         pre = c.get_item(['SOLVER', 'preconditioner'], str)
         tol = c.get_item(['SOLVER', 'linear_tolerance'], float)
         maxit = c.get_item(['SOLVER', 'linear_max_iterations'], int)
-        # 'default' / 'direct' (a sparse LU in OpenCMP, base_model.py:918) run as FP64 Krylov to 1e-12.
+        # 'default' / 'direct' (a sparse LU in OpenCMP, base_model.py:918) run as FP64 Krylov to a 1e-12
+        # relative residual: CG for symmetric operators, GMRES otherwise (chosen per variable)
         if ls in ('default', 'direct'):
-            method, tol, maxit = 'GMRES', 1e-12, max(maxit, 5000)
+            method, tol, maxit = 'auto', 1e-12, max(maxit, 20000)
         elif ls == 'CG':
             method = 'CG'
         elif ls in ('GMRes', 'GMRES', 'MinRes', 'Richardson'):
@@ -234,8 +240,12 @@ class Model:
             precond = 'block_jacobi'
         prec = c.get_item(['SOLVER', 'gpu_precision'], str)
         return dict(method=method, precond=precond, tol=max(tol, 1e-12), maxit=max(maxit, 1000),
-                    precision='mixed' if prec == 'mixed' and method == 'GMRES' else 'fp64',
+                    precision='mixed' if prec == 'mixed' else 'fp64',
                     restart=c.get_item(['SOLVER', 'gpu_restart'], int), inner_tol=1e-4)
+
+    def symmetric(self, var: Variable) -> bool:
+        """Whether the variable's operator is symmetric (no convection)."""
+        return True
 
     # ---------------------------------------------------------------- per-model terms
     def operator(self, var: Variable) -> dict:
@@ -328,6 +338,11 @@ class MultiComponentINS(Model):
             self._wind_vtx = torch.as_tensor(np.ascontiguousarray(W(self.mesh.coords, 0.0)), device='cuda')
         elif W is not None:
             self._wind_const = tuple(np.ravel(W(None, 0.0) if isinstance(W, Expr) else [float(W)]))
+
+    def symmetric(self, var):
+        if self._wind_vtx is not None:
+            return False
+        return self._wind_const is None or not any(self._wind_const)
 
     def operator(self, var):
         flux = set(self.mesh.bc_names) - set(var.dirichlet) - set(var.neumann)

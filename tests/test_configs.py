@@ -1,0 +1,120 @@
+"""The steady benchmark configurations as parity cases.
+
+* Poisson -lap u = 2 pi^2 sin(pi x) sin(pi y) on the unit square, 64 x 64 x 2 triangles, H1 order 2,
+  u = 0 on every side, one steady solve (CG to 1e-10): the L2 error against sin(pi x) sin(pi y),
+  the solution against the oracle's, and the order-3 error rate on a refinement series.
+* Steady convection-diffusion -eps lap u + w.grad u = f, eps = 1e-3, w = (-(y - 0.5), x - 0.5),
+  f a Gaussian blob (sigma 0.05 at (0.3, 0.5)), u = 0 weakly on every side, DG order 2 with upwind
+  facets and interior penalty, GMRES(50) + block Jacobi: plain FP64 and FP32-inner / FP64-refinement
+  solutions against the oracle at 64 x 64 x 2, and against each other at the full 256 x 256 x 2.
+"""
+import math
+
+import numpy as np
+import pytest
+
+from opencmp_gb300 import mesh as M
+
+pytestmark = pytest.mark.gpu
+
+
+def _poisson(fem, n, order=2, method='CG', tol=1e-10):
+    import torch
+    m = M.unit_square(n)
+    sp = fem.Space(m, 'H1', order, m.bc_names)
+    A = fem.Matrix(sp, jacobi64=True)
+    f = fem.make_form(diff=1.0, dt=1.0)
+    A.assemble(f)
+    X = sp.quad_points()
+    fq = torch.as_tensor(2 * math.pi ** 2 * np.sin(math.pi * X[..., 0]) * np.sin(math.pi * X[..., 1]), device='cuda')
+    b = torch.zeros(sp.ndof, dtype=torch.float64, device='cuda')
+    fem.assemble_rhs(sp, f, fem.make_rhs(src_qp=fq), b)
+    x = torch.zeros_like(b)
+    info = fem.KrylovSolver(A, method=method, tol=tol, maxit=20000).solve(b, x)
+    uq = torch.as_tensor(np.sin(math.pi * X[..., 0]) * np.sin(math.pi * X[..., 1]), device='cuda')
+    return m, sp, x, info, sp.l2_error(x, uq)
+
+
+def test_poisson_manufactured_solution(gpu_lib, oracle):
+    from opencmp_gb300 import fem
+    m, sp, x, info, err = _poisson(fem, 64)
+    assert sp.ndof == 16641 and sp.nnz == 189441
+    assert info.status == 0 and info.relres <= 1e-10
+    o = oracle.Space(m, oracle.H1, 2, m.label_mask(m.bc_names))
+    of = oracle.make_form(diff=1.0, dt=1.0)
+    A = o.assemble(of)
+    bo = o.rhs(of, oracle.make_rhs(src_kind=oracle.SRC_SINPROD, src=(2 * math.pi ** 2,)))
+    xo = np.zeros(o.ndof)
+    o.cg(A, bo, xo, tol=1e-13, maxit=20000)
+    xg = x.cpu().numpy()
+    assert np.linalg.norm(xg - xo) <= 1e-8 * np.linalg.norm(xo)
+    err_o = o.l2_error(xo, oracle.SRC_SINPROD, (1.0,))
+    assert abs(err - err_o) <= 1e-6 * err_o
+    assert 1e-7 < err < 5e-6
+
+
+def test_poisson_error_rate(gpu_lib):
+    from opencmp_gb300 import fem
+    errs = [_poisson(fem, n)[-1] for n in (8, 16, 32, 64)]
+    rates = [math.log2(errs[i] / errs[i + 1]) for i in range(3)]
+    assert min(rates) > 2.85, (errs, rates)
+
+
+EPS_CD = 1e-3
+
+
+def _wind_vtx(m):
+    X = m.coords
+    return np.stack([-(X[:, 1] - 0.5), X[:, 0] - 0.5], axis=1)
+
+
+def _cd_dg(fem, n, precision, restart=50, tol=1e-10):
+    import torch
+    m = M.unit_square(n)
+    sp = fem.Space(m, 'L2', 2)
+    W = torch.as_tensor(np.ascontiguousarray(_wind_vtx(m)), device='cuda')
+    allb = m.label_mask(m.bc_names)
+    f = fem.make_form(diff=EPS_CD, dt=1.0, wind_vtx=W, dg=True, ipc=10.0, nitsche_mask=allb)
+    A = fem.Matrix(sp)                  # block Jacobi keeps its own scaled Krylov copy
+    A.assemble(f)
+    X = sp.quad_points()
+    r2 = (X[..., 0] - 0.3) ** 2 + (X[..., 1] - 0.5) ** 2
+    fq = torch.as_tensor(np.exp(-r2 / (2 * 0.05 ** 2)), device='cuda')
+    b = torch.zeros(sp.ndof, dtype=torch.float64, device='cuda')
+    fem.assemble_rhs(sp, f, fem.make_rhs(src_qp=fq, gval={k: 0.0 for k in range(len(m.bc_names))}), b)
+    x = torch.zeros_like(b)
+    sv = fem.KrylovSolver(A, method='GMRES', restart=restart, precond='block_jacobi', precision=precision, tol=tol,
+                          maxit=20000, inner_tol=1e-4)
+    info = sv.solve(b, x)
+    return m, sp, x, info, W
+
+
+@pytest.mark.parametrize('precision', ['fp64', 'mixed'])
+def test_dg_convection_diffusion_matches_oracle(gpu_lib, oracle, precision):
+    from opencmp_gb300 import fem
+    m, sp, x, info, W = _cd_dg(fem, 64, precision)
+    assert info.status == 0 and info.relres <= 1e-10
+    o = oracle.Space(m, oracle.L2, 2, 0)
+    allb = m.label_mask(m.bc_names)
+    of = oracle.make_form(diff=EPS_CD, dt=1.0, wind_vtx=_wind_vtx(m), dg=True, ipc=10.0, nitsche_mask=allb)
+    A = o.assemble(of)
+    bo = o.rhs(of, oracle.make_rhs(src_kind=oracle.SRC_GAUSS, src=(1.0, 0.3, 0.5, 0.0, 0.05)))
+    xo = np.zeros(o.ndof)
+    o.gmres(A, bo, xo, restart=50, precond=2, tol=1e-12, maxit=20000)
+    xg = x.cpu().numpy()
+    # the FP64 relative residual of 1e-10 bounds the error by cond(A) * 1e-10
+    assert np.linalg.norm(xg - xo) <= 1e-6 * np.linalg.norm(xo)
+    assert o.relres(A, bo, xg) <= 1.05e-10
+
+
+def test_dg_convection_diffusion_full_size(gpu_lib):
+    """256 x 256 x 2, 786,432 dofs: both precisions reach the FP64 residual and agree."""
+    from opencmp_gb300 import fem
+    m, sp, x64, i64, _ = _cd_dg(fem, 256, 'fp64', tol=1e-8)
+    _, _, x32, i32, _ = _cd_dg(fem, 256, 'mixed', tol=1e-8)
+    assert sp.ndof == 786432 and sp.nnz == 18837504
+    assert sp.info.n_interior_facets == 196096 and sp.info.n_boundary_facets == 1024
+    assert i64.status == 0 and i64.relres <= 1e-8
+    assert i32.status == 0 and i32.relres <= 1e-8
+    d = (x64 - x32).norm().item() / x64.norm().item()
+    assert d <= 1e-5, d

@@ -205,7 +205,9 @@ def test_reference_test_through_run(gpu_lib, oracle, case, capsys):
     for e, bound in zip(errs, case['bounds']):
         assert math.isfinite(e)
         assert math.isclose(e, bound, rel_tol=3, abs_tol=1e-12)
-        assert e <= 4 * bound + 1e-12, (case['id'], errs)
+        # bounds below 1e-12 mark solutions that lie in the discrete space (NGSolve's direct solve
+        # reaches round-off); the Krylov stop at a 1e-12 relative residual leaves ~1e-11 there
+        assert e <= 4 * bound + 1e-10, (case['id'], errs)
     if case['fixture'] in ORACLE_FIXTURES:
         for name, (s, u_o, _) in _oracle_case(oracle, case).items():
             u_g = sol[name].u.cpu().numpy()
