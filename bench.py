@@ -15,7 +15,6 @@ threads) on a bounded sample, the 32^3 x 6 mesh (274,625 dofs), since NGSolve ca
 from __future__ import annotations
 
 import argparse
-import contextlib
 import json
 import math
 import os
@@ -32,6 +31,10 @@ sys.path.insert(0, ROOT)
 EPS, WIND, DT = 1e-2, (1.0, 0.5, 0.25), 1e-3
 GAUSS = dict(c=(0.25, 0.25, 0.25), s=0.1)
 METRIC = 'DOF/s to 1e-8 FP64 rel. residual: mixed+batched+learned vs plain FP64, 1 GB300'
+# DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum) of the dominant kernel from an
+# ncu capture of the same kernel on the 48^3 x 6 case, scaled to the 64^3 x 6 launch by nnz; filled
+# in from the committed profile summary (profiles/), None until measured
+TRAFFIC = {}
 
 
 def gaussian(X):
@@ -90,37 +93,6 @@ class Clocks:
                 'reasons': reasons, 'samples': len(sm)}
 
 
-class LaunchCounter:
-    """Context manager: kernels launched inside it, from the CUDA activity records torch.profiler
-    collects (this library's kernels, all kernels)."""
-
-    def __init__(self):
-        self.ours = self.total = None
-        self.prof = None
-
-    def __enter__(self):
-        from torch.profiler import ProfilerActivity, profile
-        try:
-            self.prof = profile(activities=[ProfilerActivity.CUDA])
-            self.prof.__enter__()
-        except Exception as exc:  # profiler unavailable: report no count rather than a guess
-            print('launch count unavailable: {}'.format(exc), file=sys.stderr)
-            self.prof = None
-        return self
-
-    def __exit__(self, *exc):
-        import torch
-        from torch.autograd import DeviceType
-        if self.prof is None:
-            return False
-        torch.cuda.synchronize()
-        self.prof.__exit__(None, None, None)
-        ev = [e for e in self.prof.events() if e.device_type == DeviceType.CUDA]
-        self.ours = sum(1 for e in ev if 'ocmp' in e.name)
-        self.total = len(ev)
-        return False
-
-
 def run_ours(args):
     import torch
     import torch.distributed as dist
@@ -165,6 +137,8 @@ def run_ours(args):
     from opencmp_gb300.guess import LearnedGuess
     guess = LearnedGuess(space, k=4, use_residual=True, seed=0)
 
+    launches = {}
+
     def step(kind, u_in, u_out, stats):
         sv = solvers['fp64' if kind == 'fp64' else 'mixed']
         sv.mat.assemble(form)
@@ -181,7 +155,7 @@ def run_ours(args):
             guess.judge(info, used)
         stats.append((info.iterations, info.outer_iterations, info.relres0, info.relres))
 
-    def timed(kind, steps, warmup, e2e=False, around=None):
+    def timed(kind, steps, warmup, e2e=False):
         u = [u0.clone(), torch.empty_like(u0)]
         h_in = torch.empty(ndof, dtype=torch.float64, pin_memory=True)
         h_out = torch.empty(ndof, dtype=torch.float64, pin_memory=True)
@@ -202,17 +176,18 @@ def run_ours(args):
         ev0.record()
         cur = warmup % 2
         torch.cuda.nvtx.range_push('timed_' + kind + ('_e2e' if e2e else ''))
-        with (around if around is not None else contextlib.nullcontext()):
-            for k in range(steps):
-                if e2e:
-                    u[cur].copy_(h_in, non_blocking=True)
-                    step(kind, u[cur], u[1 - cur], stats)
-                    h_out.copy_(u[1 - cur], non_blocking=True)
-                    torch.cuda.current_stream().synchronize()
-                    h_in, h_out = h_out, h_in
-                else:
-                    step(kind, u[cur], u[1 - cur], stats)
-                cur = 1 - cur
+        l0 = _lib.load().ocmp_launch_count()
+        for k in range(steps):
+            if e2e:
+                u[cur].copy_(h_in, non_blocking=True)
+                step(kind, u[cur], u[1 - cur], stats)
+                h_out.copy_(u[1 - cur], non_blocking=True)
+                torch.cuda.current_stream().synchronize()
+                h_in, h_out = h_out, h_in
+            else:
+                step(kind, u[cur], u[1 - cur], stats)
+            cur = 1 - cur
+        launches[kind + ('_e2e' if e2e else '')] = int(_lib.load().ocmp_launch_count() - l0)
         torch.cuda.nvtx.range_pop()
         ev1.record()
         torch.cuda.synchronize()
@@ -252,15 +227,15 @@ def run_ours(args):
     ms_plain, st_plain = timed('fp64', args.steps, args.warmup)
     plain_relres0 = [float(np.mean([s[2] for s in st_plain]))]
     ms_mixed, st_mixed = timed('mixed', args.steps, args.warmup)
+    # the dominant kernel of the optimised path, timed live: every FP32 GMRES SpMV launch of the timed
+    # steps between CUDA events on its stream
+    solvers['mixed'].spmv_timing(True)
     ms_opt, st_opt = timed('learned', args.steps, args.warmup)
+    spmv_live = solvers['mixed'].spmv_stats()
+    solvers['mixed'].spmv_timing(False)
     cl = clocks.stop()
     ms_e2e, _ = timed('learned', args.steps, args.warmup, e2e=True)
     # the timed region replayed once more (same inputs, same iteration counts) under the profiler
-    launches = all_kernels = None
-    if not args.no_launch_count:
-        counter = LaunchCounter()
-        timed('learned', args.steps, args.warmup, around=counter)
-        launches, all_kernels = counter.ours, counter.total
 
     # SpMV roofline: FP64 CSR SpMV launches timed with CUDA events on the launching stream
     x = torch.randn(ndof, dtype=torch.float64, device='cuda')
@@ -279,6 +254,12 @@ def run_ours(args):
     spmv_bytes = 12 * nnz + 4 * (ndof + 1) + 16 * ndof
     peak, peak_kind = peaks()
     achieved = spmv_bytes / (spmv_ms * 1e-3) / 1e9
+    # gm_spmv<float>: FP32 values + int32 columns (8 B per entry), row pointers, the input vector and
+    # the new basis vector (4 B per row each), the free mask (1 B per row)
+    g_bytes = 8 * nnz + 4 * (ndof + 1) + 9 * ndof
+    g_launches, g_ms = spmv_live
+    g_avg = g_ms / max(g_launches, 1)
+    g_achieved = g_bytes / (g_avg * 1e-3) / 1e9 if g_launches else None
 
     value = ndof * args.steps * world / (ms_opt * 1e-3)
     plain = ndof * args.steps * world / (ms_plain * 1e-3)
@@ -310,14 +291,17 @@ def run_ours(args):
                            'loss_first': float(np.mean(losses[:10])), 'loss_last': float(np.mean(losses[-10:])),
                            'seconds': train_s},
         'e2e': {'value': e2e_val, 'unit': 'DOF/s', 'h2d_bytes_per_step': 8 * ndof, 'd2h_bytes_per_step': 8 * ndof},
-        'roofline': {'bound': 'hbm', 'kernel': 'spmv_masked<double> / spmv64 (CSR FP64)', 'achieved': achieved,
-                     'peak': peak, 'peak_kind': peak_kind, 'unit': 'GB/s', 'frac': achieved / peak,
-                     'traffic': None, 'algorithmic_bytes': spmv_bytes, 'avg_launch_ms': spmv_ms},
+        'roofline': {'bound': 'hbm', 'kernel': 'gm_spmv<float> (FP32 Krylov SpMV of the optimised path, CSR)',
+                     'achieved': g_achieved, 'peak': peak, 'peak_kind': peak_kind, 'unit': 'GB/s',
+                     'frac': g_achieved / peak if g_achieved else None, 'traffic': TRAFFIC.get('gm_spmv_float'),
+                     'algorithmic_bytes': g_bytes, 'avg_launch_ms': g_avg, 'launches_timed': g_launches,
+                     'timing': 'CUDA events around every launch in the timed steps, on the launching stream'},
+        'roofline_fp64_spmv': {'bound': 'hbm', 'kernel': 'spmv64 (CSR FP64, ocmp_spmv) timed alone, 50 launches',
+                               'achieved': achieved, 'peak': peak, 'unit': 'GB/s', 'frac': achieved / peak,
+                               'algorithmic_bytes': spmv_bytes, 'avg_launch_ms': spmv_ms},
         'autotune': tuned,
-        'gpu_launches': launches,
-        'gpu_launches_note': 'kernels of libopencmp_gpu.so in one replay of the {} timed steps of the optimised '
-                             'path (CUDA activity records); all kernels incl. torch copies: {}'.format(args.steps,
-                                                                                                     all_kernels),
+        'gpu_launches': launches['learned'],
+        'gpu_launches_by_path': launches,
         'clocks': cl,
         'setup_s': setup_s,
     }
@@ -497,8 +481,6 @@ def main():
     ap.add_argument('--inner-tol', type=float, default=1e-4)
     ap.add_argument('--check-every', type=int, default=8)
     ap.add_argument('--no-cpu', action='store_true')
-    ap.add_argument('--no-launch-count', action='store_true',
-                    help='skip the profiler replay that counts kernel launches (for runs under ncu)')
     ap.add_argument('--config', default='transient3d', choices=['transient3d', 'batched'])
     ap.add_argument('--instances', type=int, default=512)
     ap.add_argument('--restart-batch', type=int, default=50)

@@ -51,11 +51,11 @@ typedef enum {
     OCMP_ERR_NOMEM = 8         /* device allocation failed                                        */
 } ocmp_status;
 
-enum { OCMP_H1 = 0, OCMP_L2 = 1 };
+enum { OCMP_H1 = 0, OCMP_L2 = 1, OCMP_COMPOUND = 2 };  /* compound: the Taylor-Hood system (ocmp_th_*) */
 enum { OCMP_WIND_NONE = 0, OCMP_WIND_CONST = 1, OCMP_WIND_VERTEX = 2 };
 enum { OCMP_SRC_NONE = 0, OCMP_SRC_CONST = 1, OCMP_SRC_QP = 2 };
 enum { OCMP_CG = 0, OCMP_GMRES = 1 };
-enum { OCMP_PRE_NONE = 0, OCMP_PRE_JACOBI = 1, OCMP_PRE_BLOCK_JACOBI = 2 };
+enum { OCMP_PRE_NONE = 0, OCMP_PRE_JACOBI = 1, OCMP_PRE_BLOCK_JACOBI = 2, OCMP_PRE_USER = 3 };
 enum { OCMP_FP64 = 0, OCMP_MIXED = 1 };
 
 typedef struct ocmp_mesh_s* ocmp_mesh_t;
@@ -131,6 +131,8 @@ typedef struct {
 
 /* ---------------------------------------------------------------- general */
 int ocmp_abi_version(void);
+/* Kernels launched by this library so far (graph replays included); no counterpart in the reference */
+uint64_t ocmp_launch_count(void);
 int ocmp_last_error(char* buf, int len);
 int ocmp_device_sync(void* stream);
 
@@ -214,6 +216,58 @@ int ocmp_solve_batch(ocmp_solver_t solver, const double* b_dev, double* x_dev, v
 /* Replay each GMRES restart cycle (m iterations, the x update and the next FP64 residual) from a
  * CUDA graph captured on first use (re-captured when b, x or the stream change). */
 int ocmp_solver_set_graph(ocmp_solver_t solver, int32_t on);
+/* OCMP_PRE_USER: the inverse diagonal (ndof, device) applied as the preconditioner; copied, and
+ * taken over by the next ocmp_solver_update. */
+int ocmp_solver_set_diag(ocmp_solver_t solver, const double* dinv_dev, void* stream);
+/* Time every GMRES SpMV launch with CUDA events on its stream (single solves, outside graphs);
+ * ocmp_solver_spmv_stats returns the launches timed and their total milliseconds since the timing
+ * was switched on. No counterpart in the reference (measurement). */
+int ocmp_solver_spmv_timing(ocmp_solver_t solver, int32_t on);
+int ocmp_solver_spmv_stats(ocmp_solver_t solver, int64_t* launches, double* total_ms);
+
+/* ---------------------------------------------------------------- incompressible Navier-Stokes
+ * Taylor-Hood system of OpenCMP's INS model (opencmp/models/ins.py) on triangles: velocity H1
+ * order k (2 or 3) per component, pressure H1 order k-1, compound vector [u_x | u_y | p].
+ *   ocmp_th_create       <- ins.py:90-128 (_construct_fes: VectorH1 x H1, velocity Dirichlet labels)
+ *   ocmp_th_assemble     <- BilinearForm.Assemble of ins.py:178-251 plus the time-derivative mass
+ *                           term (base_model.py:418-497); the interior-facet DG terms are not built
+ *   ocmp_th_assemble_rhs <- LinearForm.Assemble of ins.py:253-314 (source, u_prev mass term, IMEX
+ *                           explicit convection of construct_imex_explicit)
+ *   ocmp_th_errors       <- opencmp/helpers/error.py:75-128 (l2_norm of u) and 151-167 (divergence)
+ * Matrices on the compound space come from ocmp_matrix_create(compound, 0, ...); they are solved by
+ * GMRES with OCMP_PRE_USER and the inverse diagonal of ocmp_th_block_diag. */
+typedef struct ocmp_th_s* ocmp_th_t;
+typedef struct {
+    double mass;           /* coefficient of (u, v)                                              */
+    double nu;             /* kinematic viscosity                                                */
+    double dt;             /* factor of the viscous, convection and pressure terms               */
+    double eps_p;          /* pressure regularisation  -dt eps_p (p, q)  (OpenCMP: 1e-10)        */
+    const double* wind;    /* device: Oseen wind as a compound vector (velocity part read), or NULL */
+} ocmp_th_form_t;
+typedef struct {
+    double dt;
+    double src[2];         /* constant body force                                                */
+    const double* src_qp;  /* device, ne*nq*2: body force at ocmp_th_quad_points, or NULL        */
+    double mass;           /* coefficient of (u_prev, v)                                         */
+    const double* uprev;   /* device compound vector, or NULL                                    */
+    const double* imex;    /* device compound vector u^n: adds -dt ((grad u^n) u^n, v), or NULL  */
+} ocmp_th_rhs_t;
+int ocmp_th_create(ocmp_mesh_t mesh, int32_t order_u, uint32_t dirichlet_mask_u, ocmp_th_t* out);
+int ocmp_th_destroy(ocmp_th_t th);
+/* the velocity component space (order k), the pressure space (k-1) and the compound space; owned
+ * by the system (do not destroy them) */
+int ocmp_th_spaces(ocmp_th_t th, ocmp_space_t* velocity, ocmp_space_t* pressure, ocmp_space_t* compound);
+int ocmp_th_nq(ocmp_th_t th);
+int ocmp_th_quad_points(ocmp_th_t th, double* xyz_host);                       /* ne*nq*2 */
+int ocmp_th_assemble(ocmp_th_t th, ocmp_matrix_t mat, const ocmp_th_form_t* form, void* stream);
+int ocmp_th_assemble_rhs(ocmp_th_t th, const ocmp_th_rhs_t* rhs, double* b_dev, void* stream);
+/* Inverse of the block-diagonal preconditioner: 1/a_ii on free velocity rows; on pressure rows
+ * -1/(|a_ii| + sum_j a_ij^2 / |a_jj|) over free velocity columns j (the diagonal of the Schur
+ * complement B diag(A)^-1 B^T); 0 on constrained rows. */
+int ocmp_th_block_diag(ocmp_th_t th, ocmp_matrix_t mat, double* dinv_dev, void* stream);
+/* || u_h - ref ||_L2 over both velocity components (ref_qp: ne*nq*2, or NULL for 0) and || div u_h ||_L2 */
+int ocmp_th_errors(ocmp_th_t th, const double* u_dev, const double* ref_qp_dev, double* l2, double* div,
+                   void* stream);
 
 /* ---------------------------------------------------------------- learned initial guess
  * No counterpart in the reference (OpenCMP starts each Krylov solve from the previous step's

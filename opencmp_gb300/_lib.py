@@ -14,11 +14,11 @@ LIB_PATH = os.path.join(HERE, 'libopencmp_gpu.so')
 OK, ERR_ARG, ERR_CUDA, ERR_NONFINITE, NOT_CONVERGED, BREAKDOWN, TIMEOUT, ERR_UNSUPPORTED, ERR_NOMEM = range(9)
 STATUS_NAMES = ['OK', 'ERR_ARG', 'ERR_CUDA', 'ERR_NONFINITE', 'NOT_CONVERGED', 'BREAKDOWN', 'TIMEOUT',
                 'ERR_UNSUPPORTED', 'ERR_NOMEM']
-H1, L2 = 0, 1
+H1, L2, COMPOUND = 0, 1, 2
 WIND_NONE, WIND_CONST, WIND_VERTEX = 0, 1, 2
 SRC_NONE, SRC_CONST, SRC_QP = 0, 1, 2
 CG, GMRES = 0, 1
-PRE_NONE, PRE_JACOBI, PRE_BLOCK_JACOBI = 0, 1, 2
+PRE_NONE, PRE_JACOBI, PRE_BLOCK_JACOBI, PRE_USER = 0, 1, 2, 3
 FP64, MIXED = 0, 1
 
 
@@ -41,6 +41,16 @@ class Rhs(C.Structure):
                 ('mass', C.c_double), ('uprev', C.c_void_p), ('bval', C.c_double * 32), ('bval_mask', C.c_uint32),
                 ('gval', C.c_double * 32), ('bval_fq', C.c_void_p), ('gval_fq', C.c_void_p),
                 ('accumulate', C.c_int32)]
+
+
+class THForm(C.Structure):
+    _fields_ = [('mass', C.c_double), ('nu', C.c_double), ('dt', C.c_double), ('eps_p', C.c_double),
+                ('wind', C.c_void_p)]
+
+
+class THRhs(C.Structure):
+    _fields_ = [('dt', C.c_double), ('src', C.c_double * 2), ('src_qp', C.c_void_p), ('mass', C.c_double),
+                ('uprev', C.c_void_p), ('imex', C.c_void_p)]
 
 
 class SpaceInfo(C.Structure):
@@ -95,6 +105,19 @@ SIGNATURES = {
     'ocmp_assemble_rhs': [P, C.POINTER(Form), C.POINTER(Rhs), P, P],
     'ocmp_spmv': [P, P, P, P],
     'ocmp_spmv_axpby': [P, D, P, D, P, P],
+    'ocmp_solver_set_diag': [P, P, P],
+    'ocmp_launch_count': [],
+    'ocmp_solver_spmv_timing': [P, I32],
+    'ocmp_solver_spmv_stats': [P, P, P],
+    'ocmp_th_create': [P, I32, U32, P],
+    'ocmp_th_destroy': [P],
+    'ocmp_th_spaces': [P, P, P, P],
+    'ocmp_th_nq': [P],
+    'ocmp_th_quad_points': [P, P],
+    'ocmp_th_assemble': [P, P, P, P],
+    'ocmp_th_assemble_rhs': [P, P, P, P],
+    'ocmp_th_block_diag': [P, P, P, P],
+    'ocmp_th_errors': [P, P, P, P, P, P],
     'ocmp_matrix_autotune': [P, P, P, P, P, P, P],
     'ocmp_solver_create': [P, C.POINTER(SolveParams), C.POINTER(P)],
     'ocmp_solver_destroy': [P],
@@ -131,6 +154,7 @@ def load():
         fn = getattr(L, name)
         fn.argtypes = argt
         fn.restype = C.c_int
+    L.ocmp_launch_count.restype = C.c_uint64
     _lib = L
     return L
 

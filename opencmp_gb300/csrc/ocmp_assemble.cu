@@ -944,10 +944,10 @@ int assemble_impl(ocmp_matrix_s* m, const ocmp_form_t* f, cudaStream_t st) {
         const int ntf = 256;
         const size_t smf = sizeof(float2) * (size_t)NG * (ntf + 1);
         OCMP_CUDA(cudaFuncSetAttribute(elem_matrix_ff_kernel<D, L>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smf));
-        elem_matrix_ff_kernel<D, L><<<nblk(ne, ntf), ntf, smf, st>>>(ne, mesh->dX, mesh->dconn, a, s->d_slot_off[var],
-                                                                    s->d_term_g[var], s->d_term_coef_ff[var], Kff);
+        OCMP_LAUNCH(elem_matrix_ff_kernel<D, L><<<nblk(ne, ntf), ntf, smf, st>>>(ne, mesh->dX, mesh->dconn, a, s->d_slot_off[var],
+                                                                    s->d_term_g[var], s->d_term_coef_ff[var], Kff));
     } else {
-        elem_matrix_kernel<D, L><<<nblk(ne, nt), nt, smem, st>>>(ne, mesh->dX, mesh->dconn, a, tt, s->d_K);
+        OCMP_LAUNCH(elem_matrix_kernel<D, L><<<nblk(ne, nt), nt, smem, st>>>(ne, mesh->dX, mesh->dconn, a, tt, s->d_K));
     }
     // facet matrices
     const bool is_l2 = s->kind == OCMP_L2;
@@ -960,23 +960,23 @@ int assemble_impl(ocmp_matrix_s* m, const ocmp_form_t* f, cudaStream_t st) {
     if (use_facets) {
         if (is_l2 && s->nif > 0) {
             if (interior)
-                interior_facet_kernel<D, L><<<nblk(s->nif * 2 * L, 128), 128, 0, st>>>(
-                    s->nif, mesh->dX, mesh->dconn, s->d_ifac, a, s->T.nfq, s->d_fw, s->d_fphi, s->d_fdphi, s->d_flam, Ki);
+                OCMP_LAUNCH(interior_facet_kernel<D, L><<<nblk(s->nif * 2 * L, 128), 128, 0, st>>>(
+                    s->nif, mesh->dX, mesh->dconn, s->d_ifac, a, s->T.nfq, s->d_fw, s->d_fphi, s->d_fdphi, s->d_flam, Ki));
             else
                 OCMP_CUDA(cudaMemsetAsync(Ki, 0, sizeof(double) * s->nif * 4 * LL, st));
         }
         if (s->nbf > 0)
-            boundary_facet_kernel<D, L><<<nblk(s->nbf * L, 128), 128, 0, st>>>(
+            OCMP_LAUNCH(boundary_facet_kernel<D, L><<<nblk(s->nbf * L, 128), 128, 0, st>>>(
                 s->nbf, mesh->dX, mesh->dconn, s->d_bfac, a, is_l2, s->T.nfq, s->d_fw, s->d_fphi, s->d_fdphi,
-                s->d_flam, Kb);
+                s->d_flam, Kb));
     }
     const int32_t* efp = is_l2 ? s->d_efac_ptr : nullptr;
     if (m->dinv && dfl)
-        diag_ff_kernel<L><<<nblk(nd, 256), 256, 0, st>>>(nd, s->d_inc_ptr, s->d_inc, Kff, s->d_free, use_facets, efp,
-                                                         s->d_efac, s->d_ebf_ptr, s->d_ebf, Ki, Kb, m->dinv, m->dinv32);
+        OCMP_LAUNCH(diag_ff_kernel<L><<<nblk(nd, 256), 256, 0, st>>>(nd, s->d_inc_ptr, s->d_inc, Kff, s->d_free, use_facets, efp,
+                                                         s->d_efac, s->d_ebf_ptr, s->d_ebf, Ki, Kb, m->dinv, m->dinv32));
     else if (m->dinv)
-        diag_kernel<L><<<nblk(nd, 256), 256, 0, st>>>(nd, s->d_inc_ptr, s->d_inc, s->d_K, s->d_free, use_facets, efp,
-                                                      s->d_efac, s->d_ebf_ptr, s->d_ebf, Ki, Kb, m->dinv);
+        OCMP_LAUNCH(diag_kernel<L><<<nblk(nd, 256), 256, 0, st>>>(nd, s->d_inc_ptr, s->d_inc, s->d_K, s->d_free, use_facets, efp,
+                                                      s->d_efac, s->d_ebf_ptr, s->d_ebf, Ki, Kb, m->dinv));
     // rows in ranges of similar length (vertex rows, then the rest) so short rows get small stripes
     const int rt = 128;
     OCMP_CUDA(cudaFuncSetAttribute(row_scatter_kernel<L>, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -988,15 +988,15 @@ int assemble_impl(ocmp_matrix_s* m, const ocmp_form_t* f, cudaStream_t st) {
         if (r1 <= r0) continue;
         const size_t rsm = sizeof(double) * (size_t)s->range_maxrow[q] * (rt + 1);
         if (dfl)
-            row_scatter_ff_kernel<L><<<nblk(r1 - r0, rt), rt, rsm, st>>>(
+            OCMP_LAUNCH(row_scatter_ff_kernel<L><<<nblk(r1 - r0, rt), rt, rsm, st>>>(
                 r0, r1, s->d_rowptr, s->d_col, s->d_inc_ptr, s->d_inc, Kff, s->d_slot, s->slot_stride, use_facets,
                 efp, s->d_efac, s->d_fslot, s->d_ebf_ptr, s->d_ebf, Ki, Kb, m->dinv, m->dinv32, m->vals, m->vals32,
-                m->svals64, m->svals32);
+                m->svals64, m->svals32));
         else
-            row_scatter_kernel<L><<<nblk(r1 - r0, rt), rt, rsm, st>>>(
+            OCMP_LAUNCH(row_scatter_kernel<L><<<nblk(r1 - r0, rt), rt, rsm, st>>>(
                 r0, r1, s->d_rowptr, s->d_col, s->d_inc_ptr, s->d_inc, s->d_K, s->d_slot, s->slot_stride, use_facets,
                 efp, s->d_efac, s->d_fslot, s->d_ebf_ptr, s->d_ebf, Ki, Kb, m->dinv, m->vals, m->vals32, m->svals64,
-                m->svals32);
+                m->svals32));
     }
     OCMP_CUDA(cudaGetLastError());
     return OCMP_OK;
@@ -1016,11 +1016,11 @@ int rhs_impl(ocmp_space_s* s, const ocmp_form_t* f, const ocmp_rhs_t* r, double*
         hv[32 + k] = r->gval[k];
     }
     OCMP_CUDA(cudaMemcpyAsync(dvals, hv, sizeof(hv), cudaMemcpyHostToDevice, st));
-    rhs_elem_kernel<D, L><<<nblk(ne, 128), 128, 0, st>>>(
+    OCMP_LAUNCH(rhs_elem_kernel<D, L><<<nblk(ne, 128), 128, 0, st>>>(
         ne, mesh->dX, mesh->dconn, s->d_dofs, a, r->dt, r->src_kind, r->src_const, r->src_qp, r->mass, r->uprev,
         s->T.nq, s->d_qw, s->d_qphi, s->d_mvec, s->d_Rc, s->d_ebf_ptr, s->d_ebf, s->d_bfac, dvals, r->bval_mask,
-        dvals + 32, r->bval_fq, r->gval_fq, s->kind == OCMP_L2, s->T.nfq, s->d_fw, s->d_fphi, s->d_fdphi, s->d_flam, s->d_Fe);
-    rhs_gather_kernel<<<nblk(s->ndof, 256), 256, 0, st>>>(s->ndof, s->d_inc_ptr, s->d_inc, s->d_Fe, b, r->accumulate);
+        dvals + 32, r->bval_fq, r->gval_fq, s->kind == OCMP_L2, s->T.nfq, s->d_fw, s->d_fphi, s->d_fdphi, s->d_flam, s->d_Fe));
+    OCMP_LAUNCH(rhs_gather_kernel<<<nblk(s->ndof, 256), 256, 0, st>>>(s->ndof, s->d_inc_ptr, s->d_inc, s->d_Fe, b, r->accumulate));
     OCMP_CUDA(cudaFreeAsync(dvals, st));
     OCMP_CUDA(cudaGetLastError());
     return OCMP_OK;
@@ -1055,8 +1055,8 @@ int l2_impl(ocmp_space_s* s, const double* u, const double* fq, double fconst, d
     const int64_t ne = s->mesh->ne;
     double* per = nullptr;
     OCMP_CUDA(cudaMallocAsync((void**)&per, sizeof(double) * ne, st));
-    l2_error_kernel<D, L><<<nblk(ne, 128), 128, 0, st>>>(ne, s->mesh->dX, s->mesh->dconn, s->d_dofs, u, s->T.nq, s->d_qw,
-                                                         s->d_qphi, fq, fconst, per);
+    OCMP_LAUNCH(l2_error_kernel<D, L><<<nblk(ne, 128), 128, 0, st>>>(ne, s->mesh->dX, s->mesh->dconn, s->d_dofs, u, s->T.nq, s->d_qw,
+                                                         s->d_qphi, fq, fconst, per));
     std::vector<double> h(ne);
     OCMP_CUDA(cudaMemcpyAsync(h.data(), per, sizeof(double) * ne, cudaMemcpyDeviceToHost, st));
     OCMP_CUDA(cudaFreeAsync(per, st));
@@ -1130,7 +1130,7 @@ int launch_scatter_values(const std::vector<int32_t>& idx, const std::vector<dou
     OCMP_CUDA(cudaMallocAsync((void**)&dv, v.size() * sizeof(double), st));
     OCMP_CUDA(cudaMemcpyAsync(didx, idx.data(), idx.size() * sizeof(int32_t), cudaMemcpyHostToDevice, st));
     OCMP_CUDA(cudaMemcpyAsync(dv, v.data(), v.size() * sizeof(double), cudaMemcpyHostToDevice, st));
-    set_values_kernel<<<nblk((int64_t)idx.size(), 256), 256, 0, st>>>((int64_t)idx.size(), didx, dv, u);
+    OCMP_LAUNCH(set_values_kernel<<<nblk((int64_t)idx.size(), 256), 256, 0, st>>>((int64_t)idx.size(), didx, dv, u));
     OCMP_CUDA(cudaFreeAsync(didx, st));
     OCMP_CUDA(cudaFreeAsync(dv, st));
     OCMP_CUDA(cudaStreamSynchronize(st));
@@ -1154,12 +1154,12 @@ int autotune_spmv(ocmp_space_s* s, const double* vals, const double* x, double* 
         const int tpr = c[0], u = c[1];
         const unsigned g = nblk(n * tpr, 256);
         auto launch = [&]() {
-            if (tpr == 2) spmv64_kernel<2, 4><<<g, 256, 0, st>>>(n, s->d_rowptr, s->d_col, vals, x, y);
-            else if (tpr == 4 && u == 4) spmv64_kernel<4, 4><<<g, 256, 0, st>>>(n, s->d_rowptr, s->d_col, vals, x, y);
-            else if (tpr == 4) spmv64_kernel<4, 8><<<g, 256, 0, st>>>(n, s->d_rowptr, s->d_col, vals, x, y);
-            else if (tpr == 8 && u == 4) spmv64_kernel<8, 4><<<g, 256, 0, st>>>(n, s->d_rowptr, s->d_col, vals, x, y);
-            else if (tpr == 8) spmv64_kernel<8, 8><<<g, 256, 0, st>>>(n, s->d_rowptr, s->d_col, vals, x, y);
-            else spmv64_kernel<16, 8><<<g, 256, 0, st>>>(n, s->d_rowptr, s->d_col, vals, x, y);
+            if (tpr == 2) OCMP_LAUNCH(spmv64_kernel<2, 4><<<g, 256, 0, st>>>(n, s->d_rowptr, s->d_col, vals, x, y));
+            else if (tpr == 4 && u == 4) OCMP_LAUNCH(spmv64_kernel<4, 4><<<g, 256, 0, st>>>(n, s->d_rowptr, s->d_col, vals, x, y));
+            else if (tpr == 4) OCMP_LAUNCH(spmv64_kernel<4, 8><<<g, 256, 0, st>>>(n, s->d_rowptr, s->d_col, vals, x, y));
+            else if (tpr == 8 && u == 4) OCMP_LAUNCH(spmv64_kernel<8, 4><<<g, 256, 0, st>>>(n, s->d_rowptr, s->d_col, vals, x, y));
+            else if (tpr == 8) OCMP_LAUNCH(spmv64_kernel<8, 8><<<g, 256, 0, st>>>(n, s->d_rowptr, s->d_col, vals, x, y));
+            else OCMP_LAUNCH(spmv64_kernel<16, 8><<<g, 256, 0, st>>>(n, s->d_rowptr, s->d_col, vals, x, y));
         };
         launch();
         OCMP_CUDA(cudaEventRecord(e0, st));
@@ -1190,12 +1190,12 @@ int launch_spmv64(const ocmp_space_s* s, const double* vals, const double* x, do
     const RowCfg rc = row_cfg(s);
     const int64_t n = s->ndof;
     const unsigned g = nblk(n * rc.tpr, 256);
-    if (rc.tpr == 2) spmv64_kernel<2, 4><<<g, 256, 0, st>>>(n, s->d_rowptr, s->d_col, vals, x, y);
-    else if (rc.tpr == 4 && rc.u == 4) spmv64_kernel<4, 4><<<g, 256, 0, st>>>(n, s->d_rowptr, s->d_col, vals, x, y);
-    else if (rc.tpr == 4) spmv64_kernel<4, 8><<<g, 256, 0, st>>>(n, s->d_rowptr, s->d_col, vals, x, y);
-    else if (rc.tpr == 8 && rc.u == 4) spmv64_kernel<8, 4><<<g, 256, 0, st>>>(n, s->d_rowptr, s->d_col, vals, x, y);
-    else if (rc.tpr == 8) spmv64_kernel<8, 8><<<g, 256, 0, st>>>(n, s->d_rowptr, s->d_col, vals, x, y);
-    else spmv64_kernel<16, 8><<<g, 256, 0, st>>>(n, s->d_rowptr, s->d_col, vals, x, y);
+    if (rc.tpr == 2) OCMP_LAUNCH(spmv64_kernel<2, 4><<<g, 256, 0, st>>>(n, s->d_rowptr, s->d_col, vals, x, y));
+    else if (rc.tpr == 4 && rc.u == 4) OCMP_LAUNCH(spmv64_kernel<4, 4><<<g, 256, 0, st>>>(n, s->d_rowptr, s->d_col, vals, x, y));
+    else if (rc.tpr == 4) OCMP_LAUNCH(spmv64_kernel<4, 8><<<g, 256, 0, st>>>(n, s->d_rowptr, s->d_col, vals, x, y));
+    else if (rc.tpr == 8 && rc.u == 4) OCMP_LAUNCH(spmv64_kernel<8, 4><<<g, 256, 0, st>>>(n, s->d_rowptr, s->d_col, vals, x, y));
+    else if (rc.tpr == 8) OCMP_LAUNCH(spmv64_kernel<8, 8><<<g, 256, 0, st>>>(n, s->d_rowptr, s->d_col, vals, x, y));
+    else OCMP_LAUNCH(spmv64_kernel<16, 8><<<g, 256, 0, st>>>(n, s->d_rowptr, s->d_col, vals, x, y));
     OCMP_CUDA(cudaGetLastError());
     return OCMP_OK;
 }
@@ -1206,12 +1206,12 @@ int launch_spmv_axpby(const ocmp_space_s* s, const double* vals, double alpha, c
     const int64_t n = s->ndof;
     const unsigned g = nblk(n * rc.tpr, 256);
     const int32_t *rp = s->d_rowptr, *col = s->d_col;
-    if (rc.tpr == 2) spmv64_axpby_kernel<2, 4><<<g, 256, 0, st>>>(n, rp, col, vals, alpha, x, beta, y);
-    else if (rc.tpr == 4 && rc.u == 4) spmv64_axpby_kernel<4, 4><<<g, 256, 0, st>>>(n, rp, col, vals, alpha, x, beta, y);
-    else if (rc.tpr == 4) spmv64_axpby_kernel<4, 8><<<g, 256, 0, st>>>(n, rp, col, vals, alpha, x, beta, y);
-    else if (rc.tpr == 8 && rc.u == 4) spmv64_axpby_kernel<8, 4><<<g, 256, 0, st>>>(n, rp, col, vals, alpha, x, beta, y);
-    else if (rc.tpr == 8) spmv64_axpby_kernel<8, 8><<<g, 256, 0, st>>>(n, rp, col, vals, alpha, x, beta, y);
-    else spmv64_axpby_kernel<16, 8><<<g, 256, 0, st>>>(n, rp, col, vals, alpha, x, beta, y);
+    if (rc.tpr == 2) OCMP_LAUNCH(spmv64_axpby_kernel<2, 4><<<g, 256, 0, st>>>(n, rp, col, vals, alpha, x, beta, y));
+    else if (rc.tpr == 4 && rc.u == 4) OCMP_LAUNCH(spmv64_axpby_kernel<4, 4><<<g, 256, 0, st>>>(n, rp, col, vals, alpha, x, beta, y));
+    else if (rc.tpr == 4) OCMP_LAUNCH(spmv64_axpby_kernel<4, 8><<<g, 256, 0, st>>>(n, rp, col, vals, alpha, x, beta, y));
+    else if (rc.tpr == 8 && rc.u == 4) OCMP_LAUNCH(spmv64_axpby_kernel<8, 4><<<g, 256, 0, st>>>(n, rp, col, vals, alpha, x, beta, y));
+    else if (rc.tpr == 8) OCMP_LAUNCH(spmv64_axpby_kernel<8, 8><<<g, 256, 0, st>>>(n, rp, col, vals, alpha, x, beta, y));
+    else OCMP_LAUNCH(spmv64_axpby_kernel<16, 8><<<g, 256, 0, st>>>(n, rp, col, vals, alpha, x, beta, y));
     OCMP_CUDA(cudaGetLastError());
     return OCMP_OK;
 }

@@ -412,8 +412,8 @@ int ocmp_guess_params(ocmp_guess_t g, float* host, int32_t set) {
 int ocmp_guess_forward(ocmp_guess_t g, const float* X, int64_t rows, float* Y, void* stream) {
     if (!g || !X || !Y || rows < 0) return fail(OCMP_ERR_ARG, "ocmp_guess_forward: bad argument");
     if (rows == 0) return OCMP_OK;
-    mlp_forward_kernel<<<(unsigned)((rows + kRowsPerBlock - 1) / kRowsPerBlock), kRowsPerBlock,
-                         sizeof(float) * g->L.n, (cudaStream_t)stream>>>(rows, g->F, g->P, X, Y);
+    OCMP_LAUNCH(mlp_forward_kernel<<<(unsigned)((rows + kRowsPerBlock - 1) / kRowsPerBlock), kRowsPerBlock,
+                         sizeof(float) * g->L.n, (cudaStream_t)stream>>>(rows, g->F, g->P, X, Y));
     OCMP_CUDA(cudaGetLastError());
     return OCMP_OK;
 }
@@ -427,9 +427,9 @@ int ocmp_guess_loss_grad(ocmp_guess_t g, const float* X, const float* T, int64_t
     const int nb = (int)((rows + kRowsPerBlock - 1) / kRowsPerBlock);
     const size_t smem = sizeof(double) * kRowsPerBlock + sizeof(float) * (g->L.n + kRowsPerBlock * (4 * kH + kMaxF + 1));
     OCMP_CUDA(cudaFuncSetAttribute(mlp_grad_partial_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    mlp_grad_partial_kernel<<<nb, kRowsPerBlock, smem, s>>>(rows, g->F, g->P, X, T, g->Gpart, g->Lpart);
-    mlp_grad_reduce_kernel<<<(g->L.n + 255) / 256, 256, 0, s>>>(nb, g->L.n, g->Gpart, g->G, g->Lpart, (int64_t)nb,
-                                                                g->loss);
+    OCMP_LAUNCH(mlp_grad_partial_kernel<<<nb, kRowsPerBlock, smem, s>>>(rows, g->F, g->P, X, T, g->Gpart, g->Lpart));
+    OCMP_LAUNCH(mlp_grad_reduce_kernel<<<(g->L.n + 255) / 256, 256, 0, s>>>(nb, g->L.n, g->Gpart, g->G, g->Lpart, (int64_t)nb,
+                                                                g->loss));
     OCMP_CUDA(cudaGetLastError());
     if (loss_host) {
         OCMP_CUDA(cudaMemcpyAsync(loss_host, g->loss, sizeof(double), cudaMemcpyDeviceToHost, s));
@@ -447,8 +447,8 @@ int ocmp_guess_adam_step(ocmp_guess_t g, float lr, void* stream) {
     g->step++;
     const float b1 = 0.9f, b2 = 0.999f;
     const float c1 = 1.f - std::pow(b1, (float)g->step), c2 = 1.f - std::pow(b2, (float)g->step);
-    adam_kernel<<<(g->L.n + 255) / 256, 256, 0, (cudaStream_t)stream>>>(g->L.n, g->P, g->G, g->M, g->V, lr, b1, b2,
-                                                                        1e-8f, c1, c2);
+    OCMP_LAUNCH(adam_kernel<<<(g->L.n + 255) / 256, 256, 0, (cudaStream_t)stream>>>(g->L.n, g->P, g->G, g->M, g->V, lr, b1, b2,
+                                                                        1e-8f, c1, c2));
     OCMP_CUDA(cudaGetLastError());
     return OCMP_OK;
 }
@@ -460,9 +460,9 @@ int ocmp_guess_features(int64_t n, int32_t k, const double* const* hist, const d
     for (int d = 0; d < k; d++)
         if (!hist[d]) return fail(OCMP_ERR_ARG, "ocmp_guess_features: null history vector");
     if (n == 0) return OCMP_OK;
-    features_kernel<<<(unsigned)((n + 255) / 256), 256, 0, (cudaStream_t)stream>>>(
+    OCMP_LAUNCH(features_kernel<<<(unsigned)((n + 255) / 256), 256, 0, (cudaStream_t)stream>>>(
         n, k, hist[0], k > 1 ? hist[1] : hist[0], k > 2 ? hist[2] : hist[0], k > 3 ? hist[3] : hist[0], q, scale, X,
-        F);
+        F));
     OCMP_CUDA(cudaGetLastError());
     return OCMP_OK;
 }
@@ -471,7 +471,7 @@ int ocmp_guess_apply(int64_t n, const double* un, const float* y, const double* 
                      double* x, void* stream) {
     if (!un || !y || !x || !scale || n < 0) return fail(OCMP_ERR_ARG, "ocmp_guess_apply: bad argument");
     if (n == 0) return OCMP_OK;
-    apply_kernel<<<(unsigned)((n + 255) / 256), 256, 0, (cudaStream_t)stream>>>(n, un, y, scale, freed, x);
+    OCMP_LAUNCH(apply_kernel<<<(unsigned)((n + 255) / 256), 256, 0, (cudaStream_t)stream>>>(n, un, y, scale, freed, x));
     OCMP_CUDA(cudaGetLastError());
     return OCMP_OK;
 }
@@ -480,7 +480,7 @@ int ocmp_guess_target(int64_t n, const double* unext, const double* un, const do
                       void* stream) {
     if (!unext || !un || !scale || !T || n < 0) return fail(OCMP_ERR_ARG, "ocmp_guess_target: bad argument");
     if (n == 0) return OCMP_OK;
-    target_kernel<<<(unsigned)((n + 255) / 256), 256, 0, (cudaStream_t)stream>>>(n, unext, un, scale, T);
+    OCMP_LAUNCH(target_kernel<<<(unsigned)((n + 255) / 256), 256, 0, (cudaStream_t)stream>>>(n, unext, un, scale, T));
     OCMP_CUDA(cudaGetLastError());
     return OCMP_OK;
 }
@@ -494,7 +494,7 @@ int ocmp_guess_scale(ocmp_guess_t g, int64_t n, const double* a, const double* b
         if (st) return st;
         OCMP_CUDA(cudaMemset(g->scnt, 0, sizeof(unsigned)));
     }
-    rms_diff_kernel<<<nb, 256, 0, (cudaStream_t)stream>>>(n, a, b, g->spart, g->scnt, scale);
+    OCMP_LAUNCH(rms_diff_kernel<<<nb, 256, 0, (cudaStream_t)stream>>>(n, a, b, g->spart, g->scnt, scale));
     OCMP_CUDA(cudaGetLastError());
     return OCMP_OK;
 }
@@ -507,8 +507,8 @@ int ocmp_jacobi_residual(ocmp_matrix_t mat, const double* b, const double* x, do
     const unsigned g = (unsigned)((n * rc.tpr + 255) / 256);
     cudaStream_t st = (cudaStream_t)stream;
 #define JR(TPR, U)                                                                                                    \
-    jacobi_resid_kernel<TPR, U><<<g, 256, 0, st>>>(n, s->d_rowptr, s->d_col, mat->vals, mat->dinv, s->d_diag, s->d_free, \
-                                                   b, x, q)
+    OCMP_LAUNCH(jacobi_resid_kernel<TPR, U><<<g, 256, 0, st>>>(n, s->d_rowptr, s->d_col, mat->vals, mat->dinv, s->d_diag, s->d_free, \
+                                                   b, x, q))
     if (rc.tpr == 2) JR(2, 4);
     else if (rc.tpr == 4 && rc.u == 4) JR(4, 4);
     else if (rc.tpr == 4) JR(4, 8);

@@ -24,6 +24,7 @@
 
 namespace ocmp {
 
+std::atomic<unsigned long long> g_launches{0};
 static thread_local std::string g_err;
 void set_error(const std::string& msg) { g_err = msg; }
 int fail(int code, const std::string& msg) {
@@ -177,6 +178,20 @@ static int simplex_rule(int D, int n, std::vector<double>& pts, std::vector<doub
     }
     return (int)wts.size();
 }
+
+int tabulate(int kind, int D, int p, int npts, const double* xi, double* val, double* grad) {
+    Dn b[kMaxLoc];
+    int L = 0;
+    for (int q = 0; q < npts; q++) {
+        L = basis(kind, D, p, xi + (size_t)q * D, b);
+        for (int i = 0; i < L; i++) {
+            val[(size_t)q * L + i] = b[i].v;
+            for (int k = 0; k < D; k++) grad[((size_t)q * L + i) * D + k] = b[i].d[k];
+        }
+    }
+    return L;
+}
+int quad_rule(int D, int n, std::vector<double>& pts, std::vector<double>& wts) { return simplex_rule(D, n, pts, wts); }
 
 // Basis as polynomials in independent barycentric variables: values and d/d lam_a (a = 0..D).
 // Every function of both spaces is such a polynomial, so grad phi = sum_a dphi/dlam_a grad lam_a.
@@ -431,6 +446,8 @@ using namespace ocmp;
 extern "C" {
 
 int ocmp_abi_version(void) { return OCMP_ABI_VERSION; }
+
+uint64_t ocmp_launch_count(void) { return (uint64_t)g_launches.load(); }
 
 int ocmp_last_error(char* buf, int len) {
     if (!buf || len <= 0) return OCMP_ERR_ARG;
@@ -867,6 +884,7 @@ int ocmp_space_info(ocmp_space_t s, ocmp_space_info_t* info) {
 
 int ocmp_space_get_dofs(ocmp_space_t s, int32_t* d) {
     if (!s || !d) return fail(OCMP_ERR_ARG, "ocmp_space_get_dofs: null argument");
+    if (s->kind == OCMP_COMPOUND) return fail(OCMP_ERR_UNSUPPORTED, "ocmp_space_get_dofs: compound space");
     std::memcpy(d, s->dofs.data(), s->dofs.size() * sizeof(int32_t));
     return OCMP_OK;
 }
@@ -885,6 +903,7 @@ int ocmp_space_get_free(ocmp_space_t s, uint8_t* f) {
 }
 
 int ocmp_space_quad_points(ocmp_space_t s, double* xyz) {
+    if (s && s->kind == OCMP_COMPOUND) return fail(OCMP_ERR_UNSUPPORTED, "ocmp_space_quad_points: compound space");
     if (!s || !xyz) return fail(OCMP_ERR_ARG, "ocmp_space_quad_points: null argument");
     const int D = s->dim, nvp = D + 1, nq = s->T.nq;
     const ocmp_mesh_s* m = s->mesh;
@@ -903,11 +922,13 @@ int ocmp_space_quad_points(ocmp_space_t s, double* xyz) {
 }
 
 int ocmp_set_boundary(ocmp_space_t s, uint32_t mask, const double* gval, double* u, void* stream) {
+    if (s && s->kind == OCMP_COMPOUND) return fail(OCMP_ERR_UNSUPPORTED, "ocmp_set_boundary: compound space");
     if (!s || !gval || !u) return fail(OCMP_ERR_ARG, "ocmp_set_boundary: null argument");
     return launch_set_boundary(s, mask, gval, u, (cudaStream_t)stream);
 }
 
 int ocmp_space_facet_quad_points(ocmp_space_t s, double* xyz) {
+    if (s && s->kind == OCMP_COMPOUND) return fail(OCMP_ERR_UNSUPPORTED, "ocmp_space_facet_quad_points: compound space");
     if (!s || !xyz) return fail(OCMP_ERR_ARG, "ocmp_space_facet_quad_points: null argument");
     const int D = s->dim, nvp = D + 1, nfq = s->T.nfq;
     const ocmp_mesh_s* m = s->mesh;
@@ -928,6 +949,7 @@ int ocmp_space_facet_quad_points(ocmp_space_t s, double* xyz) {
 }
 
 int ocmp_space_boundary_facets(ocmp_space_t s, int32_t* out) {
+    if (s && s->kind == OCMP_COMPOUND) return fail(OCMP_ERR_UNSUPPORTED, "ocmp_space_boundary_facets: compound space");
     if (!s || !out) return fail(OCMP_ERR_ARG, "ocmp_space_boundary_facets: null argument");
     std::memcpy(out, s->bfac.data(), s->bfac.size() * sizeof(int32_t));
     return OCMP_OK;
@@ -1067,6 +1089,7 @@ int64_t walk_boundary(const ocmp_space_s* s, uint32_t mask, const double* g, dou
 }  // namespace
 
 int ocmp_boundary_points(ocmp_space_t s, uint32_t mask, int64_t* npts, double* xyz) {
+    if (s && s->kind == OCMP_COMPOUND) return fail(OCMP_ERR_UNSUPPORTED, "ocmp_boundary_points: compound space");
     if (!s || !npts) return fail(OCMP_ERR_ARG, "ocmp_boundary_points: null argument");
     if (s->kind != OCMP_H1) {
         *npts = 0;
@@ -1077,6 +1100,7 @@ int ocmp_boundary_points(ocmp_space_t s, uint32_t mask, int64_t* npts, double* x
 }
 
 int ocmp_set_boundary_values(ocmp_space_t s, uint32_t mask, const double* g, double* u, void* stream) {
+    if (s && s->kind == OCMP_COMPOUND) return fail(OCMP_ERR_UNSUPPORTED, "ocmp_set_boundary_values: compound space");
     if (!s || !g || !u) return fail(OCMP_ERR_ARG, "ocmp_set_boundary_values: null argument");
     if (s->kind != OCMP_H1) return OCMP_OK;
     std::vector<int32_t> idx;
@@ -1086,6 +1110,7 @@ int ocmp_set_boundary_values(ocmp_space_t s, uint32_t mask, const double* g, dou
 }
 
 int ocmp_l2_error(ocmp_space_t s, const double* u, const double* fq, double fconst, double* result, void* stream) {
+    if (s && s->kind == OCMP_COMPOUND) return fail(OCMP_ERR_UNSUPPORTED, "ocmp_l2_error: compound space");
     if (!s || !u || !result) return fail(OCMP_ERR_ARG, "ocmp_l2_error: null argument");
     return launch_l2_error(s, u, fq, fconst, result, (cudaStream_t)stream);
 }
@@ -1150,6 +1175,7 @@ int ocmp_matrix_scaled_values(ocmp_matrix_t m, double** s64, float** s32, double
 }
 
 int ocmp_assemble_matrix(ocmp_matrix_t m, const ocmp_form_t* f, void* stream) {
+    if (m && m->space->kind == OCMP_COMPOUND) return fail(OCMP_ERR_UNSUPPORTED, "ocmp_assemble_matrix: compound space (ocmp_th_assemble)");
     if (!m || !f) return fail(OCMP_ERR_ARG, "ocmp_assemble_matrix: null argument");
     if (m->B != 1) return fail(OCMP_ERR_ARG, "ocmp_assemble_matrix: batched matrix, use ocmp_assemble_matrix_batch");
     if (f->wind_kind == OCMP_WIND_VERTEX && !f->wind_vtx)
@@ -1158,6 +1184,7 @@ int ocmp_assemble_matrix(ocmp_matrix_t m, const ocmp_form_t* f, void* stream) {
 }
 
 int ocmp_assemble_matrix_batch(ocmp_matrix_t m, const ocmp_form_t* forms, void* stream) {
+    if (m && m->space->kind == OCMP_COMPOUND) return fail(OCMP_ERR_UNSUPPORTED, "ocmp_assemble_matrix_batch: compound space (ocmp_th_assemble)");
     if (!m || !forms) return fail(OCMP_ERR_ARG, "ocmp_assemble_matrix_batch: null argument");
     const ocmp_space_s* s = m->space;
     for (int q = 0; q < m->B; q++) {
@@ -1180,6 +1207,7 @@ int ocmp_assemble_matrix_batch(ocmp_matrix_t m, const ocmp_form_t* forms, void* 
 }
 
 int ocmp_assemble_rhs(ocmp_space_t s, const ocmp_form_t* f, const ocmp_rhs_t* r, double* b, void* stream) {
+    if (s && s->kind == OCMP_COMPOUND) return fail(OCMP_ERR_UNSUPPORTED, "ocmp_assemble_rhs: compound space");
     if (!s || !f || !r || !b) return fail(OCMP_ERR_ARG, "ocmp_assemble_rhs: null argument");
     if (r->src_kind == OCMP_SRC_QP && !r->src_qp) return fail(OCMP_ERR_ARG, "ocmp_assemble_rhs: src_qp is null");
     return launch_assemble_rhs(s, f, r, b, (cudaStream_t)stream);

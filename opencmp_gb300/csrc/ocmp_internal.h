@@ -3,6 +3,7 @@
 
 #include <cuda_runtime.h>
 
+#include <atomic>
 #include <cstdint>
 #include <string>
 #include <vector>
@@ -14,6 +15,15 @@ namespace ocmp {
 constexpr int kMaxLoc = 20;     // largest nloc built: H1 order 3 on tetrahedra
 constexpr int kMaxNg = 27;      // element factors: 1 mass + 10 stiffness + 16 per-vertex wind (3D)
 constexpr int kMaxFq = 25;      // facet quadrature points
+
+// Kernels this library has launched (ocmp_launch_count); every launch site goes through OCMP_LAUNCH,
+// and graph replays add the launches captured in the graph.
+extern std::atomic<unsigned long long> g_launches;
+#define OCMP_LAUNCH(...)                                                   \
+    do {                                                                   \
+        ::ocmp::g_launches.fetch_add(1, std::memory_order_relaxed);        \
+        __VA_ARGS__;                                                       \
+    } while (0)
 
 void set_error(const std::string& msg);
 int fail(int code, const std::string& msg);
@@ -149,6 +159,9 @@ struct ocmp_matrix_s {
 };
 
 namespace ocmp {
+// reference basis values/gradients (ocmp_host.cpp) and the collapsed simplex rule
+int tabulate(int kind, int D, int p, int npts, const double* xi, double* val, double* grad);
+int quad_rule(int D, int n, std::vector<double>& pts, std::vector<double>& wts);
 // kernels (ocmp_assemble.cu)
 int launch_assemble_matrix(ocmp_matrix_s* m, const ocmp_form_t* f, cudaStream_t st);
 int launch_assemble_rhs(ocmp_space_s* s, const ocmp_form_t* f, const ocmp_rhs_t* r, double* b, cudaStream_t st);

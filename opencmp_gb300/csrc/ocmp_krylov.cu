@@ -39,6 +39,8 @@ struct ocmp_solver_s {
     int m = 0;                  // GMRES restart
     // FP64 path
     double* dinv = nullptr;     // Jacobi (0 on constrained rows)
+    double* udiag = nullptr;    // caller's inverse diagonal (OCMP_PRE_USER)
+    bool udiag_set = false;
     double* Binv = nullptr;     // block Jacobi (L2 element blocks)
     double* V = nullptr;        // (m+1) x n
     double* w = nullptr;
@@ -75,6 +77,13 @@ struct ocmp_solver_s {
     ocmp::Bat bat{};            // per-instance strides
     bool use_graph = false;     // replay each restart cycle from a captured CUDA graph
     cudaGraphExec_t gexec = nullptr;
+    unsigned long long graph_kernels = 0;  // kernel launches captured in gexec
+    // optional live timing of the Krylov SpMV launches (ocmp_solver_spmv_timing)
+    bool time_spmv = false;
+    std::vector<cudaEvent_t> tev;
+    size_t tev_used = 0;
+    int64_t spmv_launches = 0;
+    double spmv_ms = 0;
     cudaStream_t gstream = nullptr;   // capture/launch stream when the caller passes the default stream
     cudaEvent_t gev[2] = {nullptr, nullptr};
     const double* g_b = nullptr;
@@ -546,10 +555,10 @@ void launch_spmv_masked(const Ctx& c, const TM* vals, const TV* x, TV* y, double
     const ocmp_space_s* s = c.sv->s;
     const int64_t n = s->ndof;
     switch (c.tpr) {
-    case 2: spmv_masked<TM, TV, 2><<<nblk(n * 2, kThreads), kThreads, 0, c.st>>>(n, s->d_rowptr, s->d_col, vals, s->d_free, x, y, part, flags); break;
-    case 4: spmv_masked<TM, TV, 4><<<nblk(n * 4, kThreads), kThreads, 0, c.st>>>(n, s->d_rowptr, s->d_col, vals, s->d_free, x, y, part, flags); break;
-    case 8: spmv_masked<TM, TV, 8><<<nblk(n * 8, kThreads), kThreads, 0, c.st>>>(n, s->d_rowptr, s->d_col, vals, s->d_free, x, y, part, flags); break;
-    default: spmv_masked<TM, TV, 16><<<nblk(n * 16, kThreads), kThreads, 0, c.st>>>(n, s->d_rowptr, s->d_col, vals, s->d_free, x, y, part, flags); break;
+    case 2: OCMP_LAUNCH(spmv_masked<TM, TV, 2><<<nblk(n * 2, kThreads), kThreads, 0, c.st>>>(n, s->d_rowptr, s->d_col, vals, s->d_free, x, y, part, flags)); break;
+    case 4: OCMP_LAUNCH(spmv_masked<TM, TV, 4><<<nblk(n * 4, kThreads), kThreads, 0, c.st>>>(n, s->d_rowptr, s->d_col, vals, s->d_free, x, y, part, flags)); break;
+    case 8: OCMP_LAUNCH(spmv_masked<TM, TV, 8><<<nblk(n * 8, kThreads), kThreads, 0, c.st>>>(n, s->d_rowptr, s->d_col, vals, s->d_free, x, y, part, flags)); break;
+    default: OCMP_LAUNCH(spmv_masked<TM, TV, 16><<<nblk(n * 16, kThreads), kThreads, 0, c.st>>>(n, s->d_rowptr, s->d_col, vals, s->d_free, x, y, part, flags)); break;
     }
 }
 inline int spmv_blocks(const Ctx& c) { return (int)nblk(c.sv->s->ndof * c.tpr, kThreads); }
@@ -559,9 +568,9 @@ void launch_block_prec(const Ctx& c, const T* Binv, const T* v, T* z, const int*
     const ocmp_space_s* s = c.sv->s;
     const int64_t ne = s->mesh->ne;
     switch (s->nloc) {
-    case 3: block_prec<T, 3><<<nblk(ne * 3, kThreads), kThreads, 0, c.st>>>(ne, Binv, v, z, flags); break;
-    case 6: block_prec<T, 6><<<nblk(ne * 6, kThreads), kThreads, 0, c.st>>>(ne, Binv, v, z, flags); break;
-    case 10: block_prec<T, 10><<<nblk(ne * 10, kThreads), kThreads, 0, c.st>>>(ne, Binv, v, z, flags); break;
+    case 3: OCMP_LAUNCH(block_prec<T, 3><<<nblk(ne * 3, kThreads), kThreads, 0, c.st>>>(ne, Binv, v, z, flags)); break;
+    case 6: OCMP_LAUNCH(block_prec<T, 6><<<nblk(ne * 6, kThreads), kThreads, 0, c.st>>>(ne, Binv, v, z, flags)); break;
+    case 10: OCMP_LAUNCH(block_prec<T, 10><<<nblk(ne * 10, kThreads), kThreads, 0, c.st>>>(ne, Binv, v, z, flags)); break;
     default: break;
     }
 }
@@ -570,11 +579,11 @@ void launch_block_prec(const Ctx& c, const T* Binv, const T* v, T* z, const int*
 int rhs_norm(const Ctx& c, const double* b, const double* x) {
     ocmp_solver_s* sv = c.sv;
     const int64_t n = sv->n;
-    zero_free<<<c.grid, kThreads, 0, c.st>>>(n, sv->s->d_free, x, sv->z);
+    OCMP_LAUNCH(zero_free<<<c.grid, kThreads, 0, c.st>>>(n, sv->s->d_free, x, sv->z));
     launch_spmv64(sv->s, sv->mat->vals, sv->z, sv->w, c.st);
-    resid_kernel<double><<<sv->nb, kThreads, 0, c.st>>>(n, b, sv->w, sv->s->d_free, (double*)nullptr, sv->part, sv->nb);
-    reduce_kernel<<<1, kThreads, 0, c.st>>>(sv->nb, 1, sv->part, sv->red, nullptr, -1);
-    set_nb_from<<<1, 1, 0, c.st>>>(sv->red, sv->st);
+    OCMP_LAUNCH(resid_kernel<double><<<sv->nb, kThreads, 0, c.st>>>(n, b, sv->w, sv->s->d_free, (double*)nullptr, sv->part, sv->nb));
+    OCMP_LAUNCH(reduce_kernel<<<1, kThreads, 0, c.st>>>(sv->nb, 1, sv->part, sv->red, nullptr, -1));
+    OCMP_LAUNCH(set_nb_from<<<1, 1, 0, c.st>>>(sv->red, sv->st));
     OCMP_CUDA(cudaGetLastError());
     return OCMP_OK;
 }
@@ -583,8 +592,8 @@ int rhs_norm(const Ctx& c, const double* b, const double* x) {
 int residual64(const Ctx& c, const double* b, const double* x, double* dst) {
     ocmp_solver_s* sv = c.sv;
     launch_spmv64(sv->s, sv->mat->vals, x, sv->w, c.st);
-    resid_kernel<double><<<sv->nb, kThreads, 0, c.st>>>(sv->n, b, sv->w, sv->s->d_free, dst, sv->part, sv->nb);
-    reduce_kernel<<<1, kThreads, 0, c.st>>>(sv->nb, 1, sv->part, sv->red, nullptr, -1);
+    OCMP_LAUNCH(resid_kernel<double><<<sv->nb, kThreads, 0, c.st>>>(sv->n, b, sv->w, sv->s->d_free, dst, sv->part, sv->nb));
+    OCMP_LAUNCH(reduce_kernel<<<1, kThreads, 0, c.st>>>(sv->nb, 1, sv->part, sv->red, nullptr, -1));
     OCMP_CUDA(cudaGetLastError());
     return OCMP_OK;
 }
@@ -603,23 +612,23 @@ int cg_core(const Ctx& c, const TM* vals, const T* dinv, T* r, T* z, T* p, T* q,
             int* iters_out) {
     ocmp_solver_s* sv = c.sv;
     const int64_t n = sv->n;
-    set_state<<<1, 1, 0, c.st>>>(sv->st, S_TOL, tol);
+    OCMP_LAUNCH(set_state<<<1, 1, 0, c.st>>>(sv->st, S_TOL, tol));
     OCMP_CUDA(cudaMemsetAsync(sv->flags, 0, sizeof(int) * F_NFLAG, c.st));
-    cg_init<T><<<sv->nb, kThreads, 0, c.st>>>(n, r, dinv, z, p, sv->part, sv->nb);
-    reduce_kernel<<<2, kThreads, 0, c.st>>>(sv->nb, 2, sv->part, sv->red, nullptr, -1);
-    cg_scalars_init<<<1, 1, 0, c.st>>>(sv->red, sv->st, sv->flags);
+    OCMP_LAUNCH(cg_init<T><<<sv->nb, kThreads, 0, c.st>>>(n, r, dinv, z, p, sv->part, sv->nb));
+    OCMP_LAUNCH(reduce_kernel<<<2, kThreads, 0, c.st>>>(sv->nb, 2, sv->part, sv->red, nullptr, -1));
+    OCMP_LAUNCH(cg_scalars_init<<<1, 1, 0, c.st>>>(sv->red, sv->st, sv->flags));
     int it = 0;
     if (read_flags(c)) return OCMP_ERR_CUDA;
     if (!sv->hflags[F_CONV]) {
         const int nbs = spmv_blocks(c);
         while (it < maxit) {
             launch_spmv_masked<TM, T>(c, vals, p, q, sv->pspmv, sv->flags);
-            reduce_kernel<<<1, kThreads, 0, c.st>>>(nbs, 1, sv->pspmv, sv->red, nullptr, -1);
-            cg_alpha<<<1, 1, 0, c.st>>>(sv->red, sv->st, sv->flags);
-            cg_update<T><<<sv->nb, kThreads, 0, c.st>>>(n, sv->st, x, r, p, q, dinv, z, sv->part, sv->nb, sv->flags);
-            reduce_kernel<<<2, kThreads, 0, c.st>>>(sv->nb, 2, sv->part, sv->red, sv->flags, -1);
-            cg_beta<<<1, 1, 0, c.st>>>(sv->red, sv->st, sv->flags);
-            cg_pupdate<T><<<c.grid, kThreads, 0, c.st>>>(n, sv->st, z, p, sv->flags);
+            OCMP_LAUNCH(reduce_kernel<<<1, kThreads, 0, c.st>>>(nbs, 1, sv->pspmv, sv->red, nullptr, -1));
+            OCMP_LAUNCH(cg_alpha<<<1, 1, 0, c.st>>>(sv->red, sv->st, sv->flags));
+            OCMP_LAUNCH(cg_update<T><<<sv->nb, kThreads, 0, c.st>>>(n, sv->st, x, r, p, q, dinv, z, sv->part, sv->nb, sv->flags));
+            OCMP_LAUNCH(reduce_kernel<<<2, kThreads, 0, c.st>>>(sv->nb, 2, sv->part, sv->red, sv->flags, -1));
+            OCMP_LAUNCH(cg_beta<<<1, 1, 0, c.st>>>(sv->red, sv->st, sv->flags));
+            OCMP_LAUNCH(cg_pupdate<T><<<c.grid, kThreads, 0, c.st>>>(n, sv->st, z, p, sv->flags));
             it++;
             if ((it % std::max(1, sv->prm.check_every)) == 0 || it >= maxit) {
                 if (read_flags(c)) return OCMP_ERR_CUDA;
@@ -1122,9 +1131,9 @@ int gm_run(const Ctx& c, const GmBufs<T>& B, const double* b, double* x, int max
     auto block_apply = [&](int j, double* xo) {
         const unsigned nbk = nblk(ne * L, kThreads);
         switch (L) {
-        case 3: gm_block_apply<T, 3><<<nbk, kThreads, 0, ls>>>(ne, B.Binv, xo ? B.z : B.V + (int64_t)j * n, 1.0, xo ? nullptr : sv->scale, j, B.z, xo, xo ? nullptr : sv->flags); break;
-        case 6: gm_block_apply<T, 6><<<nbk, kThreads, 0, ls>>>(ne, B.Binv, xo ? B.z : B.V + (int64_t)j * n, 1.0, xo ? nullptr : sv->scale, j, B.z, xo, xo ? nullptr : sv->flags); break;
-        case 10: gm_block_apply<T, 10><<<nbk, kThreads, 0, ls>>>(ne, B.Binv, xo ? B.z : B.V + (int64_t)j * n, 1.0, xo ? nullptr : sv->scale, j, B.z, xo, xo ? nullptr : sv->flags); break;
+        case 3: OCMP_LAUNCH(gm_block_apply<T, 3><<<nbk, kThreads, 0, ls>>>(ne, B.Binv, xo ? B.z : B.V + (int64_t)j * n, 1.0, xo ? nullptr : sv->scale, j, B.z, xo, xo ? nullptr : sv->flags)); break;
+        case 6: OCMP_LAUNCH(gm_block_apply<T, 6><<<nbk, kThreads, 0, ls>>>(ne, B.Binv, xo ? B.z : B.V + (int64_t)j * n, 1.0, xo ? nullptr : sv->scale, j, B.z, xo, xo ? nullptr : sv->flags)); break;
+        case 10: OCMP_LAUNCH(gm_block_apply<T, 10><<<nbk, kThreads, 0, ls>>>(ne, B.Binv, xo ? B.z : B.V + (int64_t)j * n, 1.0, xo ? nullptr : sv->scale, j, B.z, xo, xo ? nullptr : sv->flags)); break;
         default: break;
         }
     };
@@ -1134,25 +1143,38 @@ int gm_run(const Ctx& c, const GmBufs<T>& B, const double* b, double* x, int max
             block_apply(j, nullptr);
             xin = B.z;
         }
-        gm_spmv<T, TPR, U><<<gs, 256, 0, ls>>>(n, j, s->d_rowptr, s->d_col, B.A, s->d_free, xin, block ? 0 : 1, B.V,
-                                                 sv->scale, sv->flags, bt);
-        gm_dots<T><<<gg, 256, 0, ls>>>(n, j, B.V, sv->part, nbp, sv->cnt, sv->red, sv->flags, 0, 1, bt);
-        gm_orth<T><<<gg, 256, 0, ls>>>(n, j, m, B.V, sv->red, sv->part, sv->cnt + 1, sv->H, csg, sv->st, sv->flags,
-                                         sv->scale, 1, bt);
-        gm_dots<T><<<gg, 256, 0, ls>>>(n, j, B.V, sv->part, nbp, sv->cnt + 2, red2, sv->flags, 1, 0, bt);
-        gm_orth<T><<<gg, 256, 0, ls>>>(n, j, m, B.V, red2, sv->part, sv->cnt + 3, sv->H, csg, sv->st, sv->flags,
-                                         sv->scale, 2, bt);
+        const bool timing = sv->time_spmv && ls == c.st;
+        if (timing) {
+            while (sv->tev.size() < sv->tev_used + 2) {
+                cudaEvent_t e;
+                cudaEventCreate(&e);
+                sv->tev.push_back(e);
+            }
+            cudaEventRecord(sv->tev[sv->tev_used], ls);
+        }
+        OCMP_LAUNCH(gm_spmv<T, TPR, U><<<gs, 256, 0, ls>>>(n, j, s->d_rowptr, s->d_col, B.A, s->d_free, xin, block ? 0 : 1, B.V,
+                                                 sv->scale, sv->flags, bt));
+        if (timing) {
+            cudaEventRecord(sv->tev[sv->tev_used + 1], ls);
+            sv->tev_used += 2;
+        }
+        OCMP_LAUNCH(gm_dots<T><<<gg, 256, 0, ls>>>(n, j, B.V, sv->part, nbp, sv->cnt, sv->red, sv->flags, 0, 1, bt));
+        OCMP_LAUNCH(gm_orth<T><<<gg, 256, 0, ls>>>(n, j, m, B.V, sv->red, sv->part, sv->cnt + 1, sv->H, csg, sv->st, sv->flags,
+                                         sv->scale, 1, bt));
+        OCMP_LAUNCH(gm_dots<T><<<gg, 256, 0, ls>>>(n, j, B.V, sv->part, nbp, sv->cnt + 2, red2, sv->flags, 1, 0, bt));
+        OCMP_LAUNCH(gm_orth<T><<<gg, 256, 0, ls>>>(n, j, m, B.V, red2, sv->part, sv->cnt + 3, sv->H, csg, sv->st, sv->flags,
+                                         sv->scale, 2, bt));
     };
     auto finish_cycle = [&]() {
         if (block) {
-            gm_combine<T><<<gg, 256, 0, ls>>>(n, m, B.V, sv->scale, sv->H, csg, sv->flags, nullptr, x, B.z, bt);
+            OCMP_LAUNCH(gm_combine<T><<<gg, 256, 0, ls>>>(n, m, B.V, sv->scale, sv->H, csg, sv->flags, nullptr, x, B.z, bt));
             block_apply(0, x);
         } else {
-            gm_combine<T><<<gg, 256, 0, ls>>>(n, m, B.V, sv->scale, sv->H, csg, sv->flags, B.dinv, x, nullptr, bt);
+            OCMP_LAUNCH(gm_combine<T><<<gg, 256, 0, ls>>>(n, m, B.V, sv->scale, sv->H, csg, sv->flags, B.dinv, x, nullptr, bt));
         }
-        gm_resid<T, TPR, U><<<gg, 256, 0, ls>>>(n, s->d_rowptr, s->d_col, sv->mat->vals, s->d_free, b, x, B.V,
+        OCMP_LAUNCH(gm_resid<T, TPR, U><<<gg, 256, 0, ls>>>(n, s->d_rowptr, s->d_col, sv->mat->vals, s->d_free, b, x, B.V,
                                                   sv->part, sv->cnt, sv->st, sv->flags, sv->scale, csg, m, 1,
-                                                  s->d_lift_ptr, s->d_lift_pos, bt);
+                                                  s->d_lift_ptr, s->d_lift_pos, bt));
     };
     auto all = [&](int f) {
         for (int q = 0; q < NB; q++)
@@ -1161,11 +1183,11 @@ int gm_run(const Ctx& c, const GmBufs<T>& B, const double* b, double* x, int max
     };
     // Classical Gram-Schmidt, repeated only when |w| lost more than 99.9% of its length to the
     // projection (|w_new|^2 < 1e-6 |w|^2); the mass-dominated systems here lose far less per step.
-    gm_set_tols<<<1, 1, 0, c.st>>>(sv->st, sv->prm.tol, inner_tol, 1e-6, NB, bt.st);
+    OCMP_LAUNCH(gm_set_tols<<<1, 1, 0, c.st>>>(sv->st, sv->prm.tol, inner_tol, 1e-6, NB, bt.st));
     OCMP_CUDA(cudaMemsetAsync(sv->flags, 0, sizeof(int) * F_NFLAG * NB, c.st));
-    gm_resid<T, TPR, U><<<gg, 256, 0, c.st>>>(n, s->d_rowptr, s->d_col, sv->mat->vals, s->d_free, b, x, B.V, sv->part,
+    OCMP_LAUNCH(gm_resid<T, TPR, U><<<gg, 256, 0, c.st>>>(n, s->d_rowptr, s->d_col, sv->mat->vals, s->d_free, b, x, B.V, sv->part,
                                               sv->cnt, sv->st, sv->flags, sv->scale, csg, m, 3, s->d_lift_ptr,
-                                              s->d_lift_pos, bt);
+                                              s->d_lift_pos, bt));
     {
         std::vector<double> sth((size_t)S_NSLOT * NB);
         OCMP_CUDA(cudaMemcpyAsync(sth.data(), sv->st, sizeof(double) * S_NSLOT * NB, cudaMemcpyDeviceToHost, c.st));
@@ -1191,12 +1213,16 @@ int gm_run(const Ctx& c, const GmBufs<T>& B, const double* b, double* x, int max
             sv->gexec = nullptr;
         }
         cudaGraph_t gph;
+        const unsigned long long l0 = g_launches.load();
         OCMP_CUDA(cudaStreamBeginCapture(cg.st, cudaStreamCaptureModeThreadLocal));
         ls = cg.st;
         for (int j = 0; j < m; j++) iteration(j);
         finish_cycle();
         ls = c.st;
         OCMP_CUDA(cudaStreamEndCapture(cg.st, &gph));
+        // captured launches run at each replay, not now
+        sv->graph_kernels = g_launches.load() - l0;
+        g_launches.fetch_sub(sv->graph_kernels);
         cudaError_t e = cudaGraphInstantiate(&sv->gexec, gph, 0);
         cudaGraphDestroy(gph);
         if (e != cudaSuccess) return cuda_fail(e, "cudaGraphInstantiate");
@@ -1212,6 +1238,7 @@ int gm_run(const Ctx& c, const GmBufs<T>& B, const double* b, double* x, int max
                 OCMP_CUDA(cudaStreamWaitEvent(cg.st, sv->gev[0], 0));
             }
             OCMP_CUDA(cudaGraphLaunch(sv->gexec, cg.st));
+            g_launches.fetch_add(sv->graph_kernels);
             if (cg.st != c.st) {
                 OCMP_CUDA(cudaEventRecord(sv->gev[1], cg.st));
                 OCMP_CUDA(cudaStreamWaitEvent(c.st, sv->gev[1], 0));
@@ -1257,9 +1284,9 @@ int gm_norms(const Ctx& c, const double* b, const double* x, int mode) {
     double* csg = sv->H + (size_t)(sv->m + 1) * sv->m;
     const dim3 gg(sv->grid, sv->B);
 #define GM_R(TPR, U)                                                                                                  \
-    gm_resid<double, TPR, U><<<gg, 256, 0, c.st>>>(sv->n, s->d_rowptr, s->d_col, sv->mat->vals, s->d_free, b, x,      \
+    OCMP_LAUNCH(gm_resid<double, TPR, U><<<gg, 256, 0, c.st>>>(sv->n, s->d_rowptr, s->d_col, sv->mat->vals, s->d_free, b, x,      \
                                                    (double*)nullptr, sv->part, sv->cnt, sv->st, sv->flags, sv->scale, \
-                                                   csg, sv->m, mode, s->d_lift_ptr, s->d_lift_pos, sv->bat)
+                                                   csg, sv->m, mode, s->d_lift_ptr, s->d_lift_pos, sv->bat))
     if (rc.tpr == 2) GM_R(2, 4);
     else if (rc.tpr == 4 && rc.u == 4) GM_R(4, 4);
     else if (rc.tpr == 4) GM_R(4, 8);
@@ -1277,13 +1304,14 @@ int gm_norms(const Ctx& c, const double* b, const double* x, int mode) {
 using namespace ocmp;
 
 static void free_solver(ocmp_solver_s* sv) {
-    void* ps[] = {sv->dinv, sv->Binv, sv->V,   sv->w,     sv->z,   sv->r,     sv->p,    sv->dinv32, sv->Binv32,
+    void* ps[] = {sv->udiag, sv->dinv, sv->Binv, sv->V,   sv->w,     sv->z,   sv->r,     sv->p,    sv->dinv32, sv->Binv32,
                   sv->V32,  sv->w32,  sv->z32, sv->r32,   sv->p32, sv->d32,   sv->part, sv->pspmv,  sv->red,
                   sv->st,   sv->H,    sv->flags, sv->As64, sv->As32, sv->scale, sv->cnt};
     for (void* q : ps) dfree(q);
     if (sv->hflags) cudaFreeHost(sv->hflags);
     if (sv->gexec) cudaGraphExecDestroy(sv->gexec);
     if (sv->gstream) cudaStreamDestroy(sv->gstream);
+    for (cudaEvent_t e : sv->tev) cudaEventDestroy(e);
     for (cudaEvent_t e : sv->gev)
         if (e) cudaEventDestroy(e);
 }
@@ -1293,12 +1321,12 @@ extern "C" {
 int ocmp_solver_create(ocmp_matrix_t mat, const ocmp_solve_params_t* prm, ocmp_solver_t* out) {
     if (!mat || !prm || !out) return fail(OCMP_ERR_ARG, "ocmp_solver_create: null argument");
     if (prm->method != OCMP_CG && prm->method != OCMP_GMRES) return fail(OCMP_ERR_ARG, "ocmp_solver_create: method");
-    if (prm->precond < OCMP_PRE_NONE || prm->precond > OCMP_PRE_BLOCK_JACOBI)
+    if (prm->precond < OCMP_PRE_NONE || prm->precond > OCMP_PRE_USER)
         return fail(OCMP_ERR_ARG, "ocmp_solver_create: precond");
     if (prm->precision == OCMP_MIXED && prm->method == OCMP_CG && !mat->vals32)
         return fail(OCMP_ERR_ARG, "ocmp_solver_create: mixed-precision CG needs a matrix created with OCMP_MAT_FP32");
-    if (prm->method == OCMP_CG && prm->precond != OCMP_PRE_JACOBI)
-        return fail(OCMP_ERR_UNSUPPORTED, "ocmp_solver_create: CG is built with the Jacobi preconditioner");
+    if (prm->method == OCMP_CG && prm->precond != OCMP_PRE_JACOBI && prm->precond != OCMP_PRE_USER)
+        return fail(OCMP_ERR_UNSUPPORTED, "ocmp_solver_create: CG is built with a diagonal preconditioner");
     ocmp_space_s* s = mat->space;
     if (prm->precond == OCMP_PRE_BLOCK_JACOBI && (s->kind != OCMP_L2 || (s->nloc != 3 && s->nloc != 6 && s->nloc != 10)))
         return fail(OCMP_ERR_UNSUPPORTED, "ocmp_solver_create: block Jacobi is built for L2 element blocks");
@@ -1337,6 +1365,7 @@ int ocmp_solver_create(ocmp_matrix_t mat, const ocmp_solve_params_t* prm, ocmp_s
         if (!st) st = dalloc(p, cnt);
     };
     A(&sv->dinv, (size_t)n * NB);
+    if (prm->precond == OCMP_PRE_USER) A(&sv->udiag, (size_t)n * NB);
     A(&sv->w, n);
     A(&sv->z, n);
     A(&sv->r, n);
@@ -1407,37 +1436,65 @@ int ocmp_solver_update(ocmp_solver_t sv, void* stream) {
     ocmp_space_s* s = sv->s;
     const int64_t n = sv->n;
     const int NB = sv->B;
-    if (sv->borrow) {
+    if (sv->prm.precond == OCMP_PRE_USER) {
+        if (!sv->udiag_set) return fail(OCMP_ERR_ARG, "ocmp_solver_update: set the diagonal with ocmp_solver_set_diag");
+        OCMP_CUDA(cudaMemcpyAsync(sv->dinv, sv->udiag, sizeof(double) * n * NB, cudaMemcpyDeviceToDevice, st));
+        if (sv->dinv32) OCMP_LAUNCH(gm_cast<<<nblk(n * NB, kThreads), kThreads, 0, st>>>(n * NB, sv->dinv, sv->dinv32));
+    } else if (sv->borrow) {
         // the assembly's D^-1 scaled the Krylov matrix: use the same one for x = D^-1 y
         OCMP_CUDA(cudaMemcpyAsync(sv->dinv, sv->mat->dinv, sizeof(double) * n * NB, cudaMemcpyDeviceToDevice, st));
-        if (sv->dinv32) gm_cast<<<nblk(n * NB, kThreads), kThreads, 0, st>>>(n * NB, sv->mat->dinv, sv->dinv32);
+        if (sv->dinv32) OCMP_LAUNCH(gm_cast<<<nblk(n * NB, kThreads), kThreads, 0, st>>>(n * NB, sv->mat->dinv, sv->dinv32));
     } else {
         for (int q = 0; q < NB; q++) {
-            jacobi_setup<double><<<nblk(n, kThreads), kThreads, 0, st>>>(n, s->d_diag, sv->mat->vals + q * s->nnz,
-                                                                        s->d_free, sv->dinv + q * n);
+            OCMP_LAUNCH(jacobi_setup<double><<<nblk(n, kThreads), kThreads, 0, st>>>(n, s->d_diag, sv->mat->vals + q * s->nnz,
+                                                                        s->d_free, sv->dinv + q * n));
             if (sv->dinv32)
-                jacobi_setup<float><<<nblk(n, kThreads), kThreads, 0, st>>>(n, s->d_diag, sv->mat->vals + q * s->nnz,
-                                                                           s->d_free, sv->dinv32 + q * n);
+                OCMP_LAUNCH(jacobi_setup<float><<<nblk(n, kThreads), kThreads, 0, st>>>(n, s->d_diag, sv->mat->vals + q * s->nnz,
+                                                                           s->d_free, sv->dinv32 + q * n));
         }
     }
     if (sv->Binv) {
         const int64_t ne = s->mesh->ne;
         switch (s->nloc) {
-        case 3: block_jacobi_setup<3><<<nblk(ne, 128), 128, 0, st>>>(ne, s->d_rowptr, s->d_col, sv->mat->vals, sv->Binv, sv->Binv32); break;
-        case 6: block_jacobi_setup<6><<<nblk(ne, 128), 128, 0, st>>>(ne, s->d_rowptr, s->d_col, sv->mat->vals, sv->Binv, sv->Binv32); break;
-        case 10: block_jacobi_setup<10><<<nblk(ne, 128), 128, 0, st>>>(ne, s->d_rowptr, s->d_col, sv->mat->vals, sv->Binv, sv->Binv32); break;
+        case 3: OCMP_LAUNCH(block_jacobi_setup<3><<<nblk(ne, 128), 128, 0, st>>>(ne, s->d_rowptr, s->d_col, sv->mat->vals, sv->Binv, sv->Binv32)); break;
+        case 6: OCMP_LAUNCH(block_jacobi_setup<6><<<nblk(ne, 128), 128, 0, st>>>(ne, s->d_rowptr, s->d_col, sv->mat->vals, sv->Binv, sv->Binv32)); break;
+        case 10: OCMP_LAUNCH(block_jacobi_setup<10><<<nblk(ne, 128), 128, 0, st>>>(ne, s->d_rowptr, s->d_col, sv->mat->vals, sv->Binv, sv->Binv32)); break;
         default: break;
         }
     }
     if (sv->As64 || sv->As32) {
-        const double* d = sv->prm.precond == OCMP_PRE_JACOBI ? sv->dinv : nullptr;
+        const double* d = sv->prm.precond == OCMP_PRE_JACOBI || sv->prm.precond == OCMP_PRE_USER ? sv->dinv : nullptr;
         const dim3 g(nblk(n, kThreads), NB);
         if (sv->As64)
-            gm_scale_matrix<double><<<g, kThreads, 0, st>>>(n, s->d_rowptr, s->d_col, sv->mat->vals, d, sv->As64, s->nnz);
+            OCMP_LAUNCH(gm_scale_matrix<double><<<g, kThreads, 0, st>>>(n, s->d_rowptr, s->d_col, sv->mat->vals, d, sv->As64, s->nnz));
         if (sv->As32)
-            gm_scale_matrix<float><<<g, kThreads, 0, st>>>(n, s->d_rowptr, s->d_col, sv->mat->vals, d, sv->As32, s->nnz);
+            OCMP_LAUNCH(gm_scale_matrix<float><<<g, kThreads, 0, st>>>(n, s->d_rowptr, s->d_col, sv->mat->vals, d, sv->As32, s->nnz));
     }
     OCMP_CUDA(cudaGetLastError());
+    return OCMP_OK;
+}
+
+int ocmp_solver_set_diag(ocmp_solver_t sv, const double* dinv, void* stream) {
+    if (!sv || !dinv) return fail(OCMP_ERR_ARG, "ocmp_solver_set_diag: null argument");
+    if (sv->prm.precond != OCMP_PRE_USER) return fail(OCMP_ERR_ARG, "ocmp_solver_set_diag: solver not created with OCMP_PRE_USER");
+    OCMP_CUDA(cudaMemcpyAsync(sv->udiag, dinv, sizeof(double) * sv->n * sv->B, cudaMemcpyDeviceToDevice,
+                              (cudaStream_t)stream));
+    sv->udiag_set = true;
+    return OCMP_OK;
+}
+
+int ocmp_solver_spmv_timing(ocmp_solver_t sv, int32_t on) {
+    if (!sv) return fail(OCMP_ERR_ARG, "ocmp_solver_spmv_timing: null solver");
+    sv->time_spmv = on != 0;
+    sv->spmv_launches = 0;
+    sv->spmv_ms = 0;
+    return OCMP_OK;
+}
+
+int ocmp_solver_spmv_stats(ocmp_solver_t sv, int64_t* launches, double* total_ms) {
+    if (!sv || !launches || !total_ms) return fail(OCMP_ERR_ARG, "ocmp_solver_spmv_stats: null argument");
+    *launches = sv->spmv_launches;
+    *total_ms = sv->spmv_ms;
     return OCMP_OK;
 }
 
@@ -1464,7 +1521,7 @@ int ocmp_solve_batch(ocmp_solver_t sv, const double* b, double* x, void* stream,
     c.grid = sv->nb;
     const int NB = sv->B;
     const ocmp_solve_params_t& P = sv->prm;
-    const bool mixed = P.precision == OCMP_MIXED, jac = P.precond == OCMP_PRE_JACOBI;
+    const bool mixed = P.precision == OCMP_MIXED, jac = P.precond == OCMP_PRE_JACOBI || P.precond == OCMP_PRE_USER;
     std::vector<double> r0(NB, 0.0);
     std::vector<int> its(NB, 0);
     int cyc = 0, st;
@@ -1518,7 +1575,7 @@ int ocmp_solve(ocmp_solver_t sv, const double* b, double* x, void* stream, ocmp_
     bool nonfin = false, brk = false;
     double relres0 = 0, relres = 0;
     if (gm) {
-        const bool jac = P.precond == OCMP_PRE_JACOBI;
+        const bool jac = P.precond == OCMP_PRE_JACOBI || P.precond == OCMP_PRE_USER;
         if (sv->B != 1) return fail(OCMP_ERR_ARG, "ocmp_solve: batched matrix, use ocmp_solve_batch");
         if (!mixed) {
             GmBufs<double> B{sv->K64, jac ? sv->dinv : nullptr, sv->Binv, sv->V, sv->z};
@@ -1543,6 +1600,13 @@ int ocmp_solve(ocmp_solver_t sv, const double* b, double* x, void* stream, ocmp_
             OCMP_CUDA(cudaStreamSynchronize(c.st));
             relres = hst[S_RES];
         }
+        for (size_t k = 0; k + 1 < sv->tev_used; k += 2) {
+            float ms = 0;
+            OCMP_CUDA(cudaEventElapsedTime(&ms, sv->tev[k], sv->tev[k + 1]));
+            sv->spmv_ms += ms;
+            sv->spmv_launches++;
+        }
+        sv->tev_used = 0;
     } else {
         st = rhs_norm(c, b, x);
         if (st) return st;
@@ -1565,12 +1629,12 @@ int ocmp_solve(ocmp_solver_t sv, const double* b, double* x, void* stream, ocmp_
             } else {
                 double beta = std::sqrt(std::max(red0, 0.0));
                 while (iters < P.maxit) {
-                    set_state<<<1, 1, 0, c.st>>>(sv->st, S_BETA, beta);
-                    set_state<<<1, 1, 0, c.st>>>(sv->st, S_NB, 1.0);
+                    OCMP_LAUNCH(set_state<<<1, 1, 0, c.st>>>(sv->st, S_BETA, beta));
+                    OCMP_LAUNCH(set_state<<<1, 1, 0, c.st>>>(sv->st, S_NB, 1.0));
                     const double itol = std::max(P.inner_tol > 0 ? P.inner_tol : 1e-4, 0.5 * P.tol * nbv / beta);
                     OCMP_CUDA(cudaMemsetAsync(sv->d32, 0, sizeof(float) * n, c.st));
                     int it_in = 0;
-                    scale_to_float<<<c.grid, kThreads, 0, c.st>>>(n, sv->r, sv->st, sv->r32);
+                    OCMP_LAUNCH(scale_to_float<<<c.grid, kThreads, 0, c.st>>>(n, sv->r, sv->st, sv->r32));
                     st = cg_core<float, float, float>(c, sv->mat->vals32, sv->dinv32, sv->r32, sv->z32, sv->p32,
                                                       sv->w32, sv->d32, P.maxit - iters, itol, &it_in);
                     if (st) return st;
@@ -1580,9 +1644,9 @@ int ocmp_solve(ocmp_solver_t sv, const double* b, double* x, void* stream, ocmp_
                         nonfin = true;
                         break;
                     }
-                    set_state<<<1, 1, 0, c.st>>>(sv->st, S_BETA, beta);
-                    add_scaled_float<<<c.grid, kThreads, 0, c.st>>>(n, sv->d32, sv->st, x);
-                    set_state<<<1, 1, 0, c.st>>>(sv->st, S_NB, nbv);
+                    OCMP_LAUNCH(set_state<<<1, 1, 0, c.st>>>(sv->st, S_BETA, beta));
+                    OCMP_LAUNCH(add_scaled_float<<<c.grid, kThreads, 0, c.st>>>(n, sv->d32, sv->st, x));
+                    OCMP_LAUNCH(set_state<<<1, 1, 0, c.st>>>(sv->st, S_NB, nbv));
                     st = residual64(c, b, x, sv->r);
                     if (st) return st;
                     OCMP_CUDA(cudaMemcpyAsync(&red0, sv->red, sizeof(double), cudaMemcpyDeviceToHost, c.st));
@@ -1596,7 +1660,7 @@ int ocmp_solve(ocmp_solver_t sv, const double* b, double* x, void* stream, ocmp_
                 }
             }
         }
-        set_state<<<1, 1, 0, c.st>>>(sv->st, S_NB, nbv);
+        OCMP_LAUNCH(set_state<<<1, 1, 0, c.st>>>(sv->st, S_NB, nbv));
         st = residual64(c, b, x, (double*)nullptr);
         if (st) return st;
         OCMP_CUDA(cudaMemcpyAsync(&red0, sv->red, sizeof(double), cudaMemcpyDeviceToHost, c.st));
@@ -1718,7 +1782,7 @@ extern "C" int ocmp_solve_cg_noalloc(ocmp_matrix_t mat, const double* b, double*
     // the workspace keeps the previous call's contents: reset the flags and scalars
     OCMP_CUDA(cudaMemsetAsync(flg, 0, sizeof(int) * 64, c.st));
     OCMP_CUDA(cudaMemsetAsync(sv.red, 0, sizeof(double) * kNoAllocState, c.st));
-    jacobi_setup<double><<<nblk(n, kThreads), kThreads, 0, c.st>>>(n, s->d_diag, mat->vals, s->d_free, sv.dinv);
+    OCMP_LAUNCH(jacobi_setup<double><<<nblk(n, kThreads), kThreads, 0, c.st>>>(n, s->d_diag, mat->vals, s->d_free, sv.dinv));
     st = rhs_norm(c, b, x);
     if (st) return st;
     st = residual64(c, b, x, sv.r);

@@ -295,7 +295,8 @@ class KrylovSolver:
         p.method = LB.CG if str(method).upper() == 'CG' else LB.GMRES
         p.restart = restart
         p.precond = {'none': LB.PRE_NONE, 'jacobi': LB.PRE_JACOBI, 'local': LB.PRE_JACOBI,
-                     'block_jacobi': LB.PRE_BLOCK_JACOBI, 'block': LB.PRE_BLOCK_JACOBI}[str(precond).lower()]
+                     'block_jacobi': LB.PRE_BLOCK_JACOBI, 'block': LB.PRE_BLOCK_JACOBI,
+                     'user': LB.PRE_USER}[str(precond).lower()]
         p.precision = LB.MIXED if str(precision).lower() == 'mixed' else LB.FP64
         p.tol, p.maxit, p.inner_tol, p.check_every = tol, maxit, inner_tol, check_every
         self.params = p
@@ -310,6 +311,20 @@ class KrylovSolver:
 
     def update(self, stream=None):
         LB.call('ocmp_solver_update', self.h, _stream(stream))
+
+    def set_diag(self, dinv: torch.Tensor, stream=None):
+        """The inverse diagonal used by precond='user' (taken over by the next update())."""
+        LB.call('ocmp_solver_set_diag', self.h, _ptr(dinv), _stream(stream))
+
+    def spmv_timing(self, on: bool = True):
+        """Time each GMRES SpMV launch with CUDA events (resets the totals)."""
+        LB.call('ocmp_solver_spmv_timing', self.h, int(on))
+
+    def spmv_stats(self):
+        """(launches timed, total milliseconds) since spmv_timing(True)."""
+        n, ms = C.c_int64(0), C.c_double(0)
+        LB.call('ocmp_solver_spmv_stats', self.h, C.byref(n), C.byref(ms))
+        return n.value, ms.value
 
     def set_graph(self, on: bool = True):
         """Replay each restart cycle from a captured CUDA graph (GMRES)."""
@@ -355,3 +370,86 @@ def interpolate_p2(space: 'Space', fn):
         raise ValueError('interpolate_p2 needs an H1 order-2 space')
     m = space.mesh
     return interpolate_p2_arrays(m.coords, np.sort(m.elements, axis=1), space.dofs(), space.ndof, fn)
+
+
+class TaylorHood:
+    """Taylor-Hood velocity/pressure system on triangles (``ocmp_th_*``): velocity H1 order k per
+    component, pressure H1 order k-1, compound vector [u_x | u_y | p]; ``dirichlet`` names the
+    velocity Dirichlet labels."""
+
+    def __init__(self, mesh: Mesh, k: int = 2, dirichlet: Sequence[str] | str = (), gmesh: Optional[GPUMesh] = None):
+        self.mesh = mesh
+        self.gmesh = gmesh or GPUMesh(mesh)
+        self.k = k
+        self.dirichlet_mask = mesh.label_mask(dirichlet)
+        h = C.c_void_p()
+        LB.call('ocmp_th_create', self.gmesh.h, k, self.dirichlet_mask, C.byref(h))
+        self.h = h
+        v, p, c = C.c_void_p(), C.c_void_p(), C.c_void_p()
+        LB.call('ocmp_th_spaces', self.h, C.byref(v), C.byref(p), C.byref(c))
+        self.V = _SpaceView(mesh, self.gmesh, v, 'H1', k)
+        self.Q = _SpaceView(mesh, self.gmesh, p, 'H1', k - 1)
+        self.C = _SpaceView(mesh, self.gmesh, c, 'compound', k)
+        self.nu, self.np = self.V.ndof, self.Q.ndof
+        self.ndof, self.nnz = self.C.ndof, self.C.nnz
+        self.nq = LB.load().ocmp_th_nq(self.h)
+
+    def __del__(self):
+        if getattr(self, 'h', None) and LB._lib is not None:
+            LB._lib.ocmp_th_destroy(self.h)
+            self.h = None
+
+    def quad_points(self) -> np.ndarray:
+        x = np.empty((self.mesh.ne, self.nq, 2), np.float64)
+        LB.call('ocmp_th_quad_points', self.h, _ptr(x))
+        return x
+
+    def matrix(self) -> 'Matrix':
+        return Matrix(self.C)
+
+    def assemble(self, mat: 'Matrix', mass=0.0, nu=1.0, dt=1.0, eps_p=1e-10, wind: Optional[torch.Tensor] = None,
+                 stream=None):
+        f = LB.THForm(mass, nu, dt, eps_p, wind.data_ptr() if wind is not None else None)
+        LB.call('ocmp_th_assemble', self.h, mat.h, C.byref(f), _stream(stream))
+
+    def assemble_rhs(self, b: torch.Tensor, dt=1.0, src=(0.0, 0.0), src_qp: Optional[torch.Tensor] = None, mass=0.0,
+                     uprev: Optional[torch.Tensor] = None, imex: Optional[torch.Tensor] = None, stream=None):
+        r = LB.THRhs()
+        r.dt, r.mass = dt, mass
+        r.src[0], r.src[1] = src
+        r.src_qp = src_qp.data_ptr() if src_qp is not None else None
+        r.uprev = uprev.data_ptr() if uprev is not None else None
+        r.imex = imex.data_ptr() if imex is not None else None
+        LB.call('ocmp_th_assemble_rhs', self.h, C.byref(r), _ptr(b), _stream(stream))
+
+    def block_diag(self, mat: 'Matrix', out: torch.Tensor, stream=None):
+        LB.call('ocmp_th_block_diag', self.h, mat.h, _ptr(out), _stream(stream))
+
+    def errors(self, u: torch.Tensor, ref_qp: Optional[torch.Tensor] = None, stream=None):
+        l2, dv = C.c_double(0), C.c_double(0)
+        LB.call('ocmp_th_errors', self.h, _ptr(u), _ptr(ref_qp) if ref_qp is not None else None, C.byref(l2),
+                C.byref(dv), _stream(stream))
+        return l2.value, dv.value
+
+    def component(self, u: torch.Tensor, c: int) -> torch.Tensor:
+        """View of velocity component c (0, 1) or the pressure (2) of a compound vector."""
+        if c < 2:
+            return u[c * self.nu:(c + 1) * self.nu]
+        return u[2 * self.nu:]
+
+
+class _SpaceView(Space):
+    """A space owned by another object (the Taylor-Hood system): same queries, no destroy."""
+
+    def __init__(self, mesh, gmesh, h, kind, order):
+        self.mesh, self.gmesh, self.h, self.order = mesh, gmesh, h, order
+        self.kind = {'H1': LB.H1, 'L2': LB.L2}.get(kind, LB.COMPOUND)
+        self.dirichlet_mask = 0
+        info = LB.SpaceInfo()
+        LB.call('ocmp_space_info', self.h, C.byref(info))
+        self.info = info
+        self.ndof, self.nnz, self.nloc, self.nq = info.ndof, info.nnz, info.nloc, info.nq
+        self._free = None
+
+    def __del__(self):
+        pass

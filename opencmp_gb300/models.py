@@ -19,6 +19,7 @@ and ``skeleton_dt`` the interior-facet terms.
 """
 from __future__ import annotations
 
+import math
 from typing import Dict, List, Optional
 
 import numpy as np
@@ -74,6 +75,8 @@ class Variable:
             P['method'] = 'CG' if model.symmetric(self) else 'GMRES'
         if P['method'] == 'CG' and P['precision'] == 'mixed':
             P['precision'] = 'fp64'
+        if P['method'] == 'CG' and P['precond'] == 'block_jacobi':
+            P['precond'] = 'jacobi'            # CG is built with a diagonal preconditioner
         self.params = P
         self.mat = fem.Matrix(self.space, jacobi64=P['precision'] == 'fp64', jacobi32=P['precision'] == 'mixed')
         self.solver = fem.KrylovSolver(self.mat, method=P['method'], restart=P['restart'], precond=P['precond'],
@@ -364,7 +367,173 @@ class MultiComponentINS(Model):
         return var.mask(list(var.neumann) + list(var.total_flux))
 
 
-models_dict = {'Poisson': Poisson, 'MultiComponentINS': MultiComponentINS}
+def _vec_at(v, X, t):
+    """A vector-valued config value ([a, b] or vec(a, b)) at the points X (..., 2) -> (..., 2)."""
+    if isinstance(v, Expr):
+        r = v(X.reshape(-1, X.shape[-1]), t)
+        return np.asarray(r).reshape(X.shape[:-1] + (2,))
+    return np.broadcast_to(np.asarray(v, float), X.shape[:-1] + (2,)).copy()
+
+
+class INS(Model):
+    """Incompressible Navier-Stokes (opencmp/models/ins.py) on Taylor-Hood spaces: velocity order
+    ``interpolant_order``, pressure one lower, velocity Dirichlet data per label, the Oseen
+    linearisation (Picard iteration on the wind, ins.py:323-355) or IMEX (explicit convection,
+    ins.py:302-314). The system is solved by GMRES with the block-diagonal preconditioner of
+    ocmp_th_block_diag (velocity Jacobi, pressure Schur-complement diagonal)."""
+
+    components = ['u', 'p']
+
+    def __init__(self, config):
+        super().__init__(config)
+        if self.DG:
+            raise NotImplementedError('INS runs on the GPU path with continuous Taylor-Hood elements (DG = False)')
+        self.kv = _scalar_at(self.params.get('kinematic_viscosity', {}).get('all', 1.0), 0.0)
+        lin = config.get_item(['SOLVER', 'linearization_method'], str)
+        self.linearize = lin if lin in ('Oseen', 'IMEX') else 'Oseen'
+        if self.linearize == 'Oseen':
+            tol = config.get_dict(['SOLVER', 'nonlinear_tolerance'])
+            self.abs_tol, self.rel_tol = float(tol.get('absolute', 0.0)), float(tol['relative'])
+            self.max_picard = config.get_item(['SOLVER', 'nonlinear_max_iterations'], int)
+        for kind in ('stress', 'parallel', 'neumann', 'robin'):
+            if self.bc.get(kind, {}).get('u'):
+                raise NotImplementedError('{} boundary conditions for INS are not on the GPU path'.format(kind))
+        self.dirichlet = self.bc.get('dirichlet', {}).get('u', {})
+
+    def setup(self):
+        k = self.interp_ord
+        self.th = fem.TaylorHood(self.mesh, k, list(self.dirichlet), gmesh=self.gmesh)
+        th = self.th
+        self.A = th.matrix()
+        P = self.solver_params
+        self.solver = fem.KrylovSolver(self.A, method='GMRES', restart=max(P['restart'], 50), precond='user',
+                                       precision=P['precision'], tol=P['tol'], maxit=P['maxit'],
+                                       inner_tol=P['inner_tol'])
+        dev = 'cuda'
+        self.u = torch.zeros(th.ndof, dtype=torch.float64, device=dev)
+        self.b = torch.zeros_like(self.u)
+        self.dinv = torch.zeros_like(self.u)
+        self.W = torch.zeros_like(self.u)
+        self._qp = None
+        self._bpts = {}
+        ic_u = self.ic.get('u', {}).get('all')
+        ic_p = self.ic.get('p', {}).get('all')
+        self._project(ic_u, ic_p)
+        self.W.copy_(self.u)
+        self.vars = {}
+
+    def quad_points(self):
+        if self._qp is None:
+            self._qp = self.th.quad_points()
+        return self._qp
+
+    def _project(self, vu, vp):
+        """Initial condition: L2 projection of each velocity component and of the pressure."""
+        th = self.th
+        for c, (sp_, val) in enumerate(((th.V, vu), (th.V, vu), (th.Q, vp))):
+            if val is None:
+                continue
+            M = fem.Matrix(sp_)
+            f = fem.make_form(mass=1.0)
+            M.assemble(f)
+            X = sp_.quad_points()
+            vals = _vec_at(val, X, 0.0)[..., c] if c < 2 else _at(val, X, 0.0)
+            fq = torch.as_tensor(np.ascontiguousarray(vals.reshape(self.mesh.ne, -1)), device='cuda')
+            bb = torch.zeros(sp_.ndof, dtype=torch.float64, device='cuda')
+            fem.assemble_rhs(sp_, f, fem.make_rhs(src_qp=fq), bb)
+            x = torch.zeros_like(bb)
+            fem.KrylovSolver(M, method='CG', tol=1e-13, maxit=20000).solve(bb, x)
+            th.component(self.u, c).copy_(x)
+
+    def set_dirichlet(self, t: float):
+        th = self.th
+        for marker, v in self.dirichlet.items():
+            lab = self.mesh.bc_names.index(marker)
+            if lab not in self._bpts:
+                self._bpts[lab] = th.V.boundary_points(1 << lab)
+            g = _vec_at(v, self._bpts[lab], t)
+            for c in range(2):
+                th.V.set_boundary_values(1 << lab, g[:, c], th.component(self.u, c))
+
+    def source(self, t):
+        f = self.functions.get('source', {}).get('u')
+        if f is None:
+            return (0.0, 0.0), None
+        if isinstance(f, Expr) and f.depends_on_space:
+            return (0.0, 0.0), torch.as_tensor(_vec_at(f, self.quad_points(), t), device='cuda')
+        v = _vec_at(f, np.zeros((1, 2)), t)[0]
+        return (float(v[0]), float(v[1])), None
+
+    def _solve(self):
+        self.th.block_diag(self.A, self.dinv)
+        self.solver.set_diag(self.dinv)
+        self.solver.update()
+        return self.solver.solve(self.b, self.u)
+
+    def step(self, theta, dt, t_new, t_old, transient, infos):
+        """One time step (implicit Euler with Oseen Picard iterations, or Euler IMEX); the
+        stationary solve when not transient."""
+        if theta != 1.0:
+            raise NotImplementedError('INS runs on the GPU path with implicit Euler or Euler IMEX')
+        th = self.th
+        uprev = self.u.clone() if transient else None
+        mass = 1.0 if transient else 0.0
+        f, fq = self.source(t_new)
+        if self.linearize == 'IMEX':
+            self.set_dirichlet(t_new)
+            th.assemble(self.A, mass=mass, nu=self.kv, dt=dt)
+            th.assemble_rhs(self.b, dt=dt, src=f, src_qp=fq, mass=mass, uprev=uprev, imex=uprev)
+            infos.append(self._solve())
+            return
+        area = float(self.mesh_area())
+        for it in range(self.max_picard):
+            self.set_dirichlet(t_new)
+            th.assemble(self.A, mass=mass, nu=self.kv, dt=dt, wind=self.W)
+            th.assemble_rhs(self.b, dt=dt, src=f, src_qp=fq, mass=mass, uprev=uprev)
+            infos.append(self._solve())
+            d = self.u - self.W
+            err, _ = th.errors(d)
+            unorm, _ = th.errors(self.u)
+            self.W.copy_(self.u)
+            if err < self.abs_tol + self.rel_tol * unorm / math.sqrt(area):
+                break
+
+    def mesh_area(self):
+        X = self.mesh.coords[self.mesh.elements]
+        a = X[:, 1] - X[:, 0]
+        b = X[:, 2] - X[:, 0]
+        return 0.5 * np.abs(a[:, 0] * b[:, 1] - a[:, 1] * b[:, 0]).sum()
+
+    def errors(self, t: float) -> List[str]:
+        lines = []
+        th = self.th
+        for metric, names in self.metrics.items():
+            for name in names:
+                if metric.lower() == 'l2_norm' and name == 'u':
+                    ref = self.ref_sol.get('u')
+                    rq = None if ref is None else torch.as_tensor(_vec_at(ref, self.quad_points(), t), device='cuda')
+                    err, _ = th.errors(self.u, rq)
+                    lines.append('L2 norm in u: {}'.format(err))
+                elif metric.lower() == 'l2_norm' and name == 'p':
+                    ref = self.ref_sol.get('p', 0.0)
+                    c = _scalar_at(ref, t)
+                    pv = th.component(self.u, 2)
+                    if c is not None:
+                        err = th.Q.l2_error(pv, c)
+                    else:
+                        Xq = th.Q.quad_points()
+                        err = th.Q.l2_error(pv, torch.as_tensor(_at(ref, Xq, t).reshape(self.mesh.ne, -1),
+                                                                device='cuda'))
+                    lines.append('L2 norm in p: {}'.format(err))
+                elif metric == 'divergence' and name == 'u':
+                    _, dv = th.errors(self.u)
+                    lines.append('divergence of u: {}'.format(dv))
+                else:
+                    raise NotImplementedError('{} of {} is not on the GPU path'.format(metric, name))
+        return lines
+
+
+models_dict = {'Poisson': Poisson, 'MultiComponentINS': MultiComponentINS, 'INS': INS}
 
 
 def get_model_class(model_name: str, dim_used: bool = False):

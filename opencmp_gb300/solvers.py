@@ -28,6 +28,8 @@ from .config import ConfigParser
 from .fem import _ptr, _stream
 
 THETA = {'explicit euler': 0.0, 'crank nicolson': 0.5, 'implicit euler': 1.0}
+# schemes whose implicit part is implicit Euler and whose explicit part the model supplies
+IMEX = {'euler IMEX': 1.0}
 
 
 class Solver:
@@ -65,6 +67,9 @@ class Solver:
         return info
 
     def _step(self, theta: float, dt: float, t_new: float, t_old: float, transient: bool):
+        if hasattr(self.model, 'step'):
+            self.model.step(theta, dt, t_new, t_old, transient, self.infos)
+            return
         for v in self.model.vars.values():
             self._solve_var(v, theta, dt, t_new, t_old, transient)
 
@@ -87,10 +92,13 @@ class TransientMultiStepSolver(Solver):
     def __init__(self, model_class, config):
         super().__init__(model_class, config)
         self.scheme = config.get_item(['TRANSIENT', 'scheme'], str)
-        if self.scheme not in THETA:
+        if self.scheme in IMEX and getattr(self.model, 'linearize', None) != 'IMEX':
+            raise NotImplementedError('{!r} needs a model with the IMEX linearisation on the GPU path'.format(
+                self.scheme))
+        if self.scheme not in THETA and self.scheme not in IMEX:
             raise NotImplementedError('time scheme {!r} is not on the GPU path (one of {})'.format(
-                self.scheme, sorted(THETA)))
-        self.theta = THETA[self.scheme]
+                self.scheme, sorted(THETA) + sorted(IMEX)))
+        self.theta = THETA.get(self.scheme, IMEX.get(self.scheme))
         self.t_range = config.get_list(['TRANSIENT', 'time_range'], float)
         self.dt = config.get_item(['TRANSIENT', 'dt'], float)
         self.t = self.t_range[0]
@@ -114,8 +122,8 @@ def get_solver_class(config: ConfigParser):
     scheme = config.get_item(['TRANSIENT', 'scheme'], str)
     if not transient:
         return StationarySolver
-    if scheme in THETA:
+    if scheme in THETA or scheme in IMEX:
         return TransientMultiStepSolver
-    if scheme in ('euler IMEX', 'CNLF', 'SBDF') or 'adaptive' in scheme:
+    if scheme in ('CNLF', 'SBDF') or 'adaptive' in scheme:
         raise NotImplementedError('time scheme {!r} is not on the GPU path'.format(scheme))
     raise TypeError('Have not implemented {} time integration yet.'.format(scheme))

@@ -1122,3 +1122,20 @@ double or_l2_error(void* sp, const double* u, int src_kind, const double* src) {
     }
     return sqrt(acc);
 }
+
+/* ---------------------------------------------------------------- reference tables (for the
+ * numpy parts of the oracle: Taylor-Hood assembly in oracle/ins.py) */
+int or_tabulate(int D, int kind, int p, int npts, const double* xi, double* vals, double* grads) {
+    dn b[64];
+    int L = 0;
+    for (int q = 0; q < npts; q++) {
+        L = kind == OR_H1 ? h1_eval(D, p, xi + (size_t)q * D, b) : l2_eval(D, p, xi + (size_t)q * D, b);
+        for (int i = 0; i < L; i++) {
+            vals[(size_t)q * L + i] = b[i].v;
+            for (int k = 0; k < D; k++) grads[((size_t)q * L + i) * D + k] = b[i].d[k];
+        }
+    }
+    return L;
+}
+
+int or_rule(int D, int n, double* pts, double* wts) { return simplex_rule(D, n, pts, wts); }

@@ -87,6 +87,11 @@ int or_gmres(void* sp, const double* vals, const double* b, double* x, int resta
 double or_relres(void* sp, const double* vals, const double* b, const double* x);
 void or_set_threads(int n);
 
+/* reference basis values (npts*L) and reference gradients (npts*L*D) at npts points; returns L */
+int or_tabulate(int D, int kind, int p, int npts, const double* xi, double* vals, double* grads);
+/* the collapsed simplex rule with n points per direction (n^D points, weights summing to 1/D!) */
+int or_rule(int D, int n, double* pts, double* wts);
+
 #ifdef __cplusplus
 }
 #endif

@@ -77,6 +77,8 @@ def lib():
         L.or_relres.argtypes = [P, P, P, P]
         L.or_spmv.argtypes = [C.c_int64, P, P, P, P, P]
         L.or_set_threads.argtypes = [C.c_int]
+        L.or_tabulate.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int, P, P, P]
+        L.or_rule.argtypes = [C.c_int, C.c_int, P, P]
         _lib = L
     return _lib
 
@@ -118,6 +120,24 @@ def make_rhs(dt=1.0, src_kind=SRC_NONE, src=(), mass=0.0, uprev=None, bval=None,
         for lab, v in gval.items():
             r.gval[lab] = v
     return r
+
+
+def tabulate(D: int, kind: int, p: int, xi):
+    """Reference basis values (npts, L) and reference gradients (npts, L, D) at the points xi."""
+    xi = np.ascontiguousarray(xi, np.float64).reshape(-1, D)
+    L = (p + 1) * (p + 2) // 2 if D == 2 else (p + 1) * (p + 2) * (p + 3) // 6
+    v = np.empty((xi.shape[0], L))
+    g = np.empty((xi.shape[0], L, D))
+    lib().or_tabulate(D, kind, p, xi.shape[0], _p(xi), _p(v), _p(g))
+    return v, g
+
+
+def rule(D: int, n: int):
+    """The collapsed simplex rule with n points per direction: (points (n^D, D), weights)."""
+    x = np.empty((n ** D, D))
+    w = np.empty(n ** D)
+    lib().or_rule(D, n, _p(x), _p(w))
+    return x, w
 
 
 class Space:

@@ -9,7 +9,8 @@ pyparsing are absent), so the fixtures are its test inputs and pinned numbers, r
   opencmp_gb300.mesh.load_mesh;
 * reference_bounds.json  - the error bounds those tests assert (automated_output_check compares
   with isclose(rtol=3, atol=1e-12), opencmp/helpers/testing.py:58-86), with their file:line;
-* square.npz - pytests/mesh_files/square.msh (the purely convective MCINS test's mesh);
+* square.npz, coarse_large_square_4bcs.npz - pytests/mesh_files/square.msh (the purely convective
+  MCINS test's mesh) and coarse_large_square_4bcs.vol (the transient INS test's);
 * fixtures/<group>_<case>/ - the run directories of the full-system tests the GPU path runs
   (config plus bc/ic/model/ref_sol sub-configs), copied as data. The tests point their mesh file
   and run_dir at this tree before running them.
@@ -29,16 +30,18 @@ from opencmp_gb300.mesh import load_mesh  # noqa: E402
 
 
 FIXTURES = ['poisson/transient_coarse', 'poisson/h_convergence', 'mcins/diffusion', 'mcins/diffusion_convection',
-            'mcins/purely_convective']
+            'mcins/purely_convective', 'ins/sinusoidal_transient']
+MESHES = ['unit_square_coarse.vol', 'square.msh', 'coarse_large_square_4bcs.vol']
 
 
 def main(ref='/root/reference'):
     m = load_mesh(os.path.join(ref, 'pytests/mesh_files/unit_square_coarse.vol'))
     np.savez(os.path.join(HERE, 'unit_square_coarse.npz'), coords=m.coords, elements=m.elements,
              bfacets=m.bfacets, blabels=m.blabels, bc_names=np.array(m.bc_names))
-    m = load_mesh(os.path.join(ref, 'pytests/mesh_files/square.msh'))
-    np.savez(os.path.join(HERE, 'square.npz'), coords=m.coords, elements=m.elements,
-             bfacets=m.bfacets, blabels=m.blabels, bc_names=np.array(m.bc_names))
+    for name in MESHES[1:]:
+        m = load_mesh(os.path.join(ref, 'pytests/mesh_files', name))
+        np.savez(os.path.join(HERE, os.path.splitext(name)[0] + '.npz'), coords=m.coords, elements=m.elements,
+                 bfacets=m.bfacets, blabels=m.blabels, bc_names=np.array(m.bc_names))
     for case in FIXTURES:
         src = os.path.join(ref, 'pytests/full_system', case)
         dst = os.path.join(HERE, 'fixtures', case.replace('/', '_'))
@@ -51,7 +54,8 @@ def main(ref='/root/reference'):
                 shutil.copyfile(f, os.path.join(dst, sub + '_dir', sub + '_config'))
     bounds = {'rtol': {'value': 3.0, 'atol': 1e-12, 'source': 'opencmp/helpers/testing.py:82'},
               'tests': []}
-    for tf in ('pytests/full_system/poisson/test_poisson.py', 'pytests/full_system/mcins/test_mcins.py'):
+    for tf in ('pytests/full_system/poisson/test_poisson.py', 'pytests/full_system/mcins/test_mcins.py',
+               'pytests/full_system/ins/test_ins.py'):
         bounds['tests'] += reference_tests(ref, tf)
     with open(os.path.join(HERE, 'reference_bounds.json'), 'w') as fh:
         json.dump(bounds, fh, indent=1)

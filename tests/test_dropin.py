@@ -18,7 +18,7 @@ from opencmp_gb300.config import ConfigParser, Expr, parse, value_map, load_sub_
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 GOLDEN = os.path.join(ROOT, 'tests', 'golden')
 FIX = os.path.join(GOLDEN, 'fixtures')
-SUPPORTED = ('explicit euler', 'implicit euler', 'crank nicolson')
+SUPPORTED = ('explicit euler', 'implicit euler', 'crank nicolson', 'euler IMEX')
 # Explicit Euler on the order-3 DG Poisson forms of the coarse fixture amplifies by 5.0 per step
 # (test_explicit_dg_poisson_is_unstable): every run of it, the oracle's included, overflows.
 UNSTABLE = {'test_poisson.py::TestTransient::test_explicit_euler_dg'}
@@ -44,8 +44,15 @@ def _cases():
     for t in tests:
         cfg = _load(t)
         scheme = cfg.get_item(['TRANSIENT', 'scheme'], str)
+        model = cfg.get_item(['OTHER', 'model'], str)
+        dg = cfg.get_item(['DG', 'DG'], bool)
         if scheme not in SUPPORTED:
             marks = [pytest.mark.skip(reason='time scheme {!r} is not on the GPU path'.format(scheme))]
+        elif scheme == 'euler IMEX' and model != 'INS':
+            marks = [pytest.mark.skip(reason='IMEX linearisation is on the GPU path for INS only')]
+        elif model == 'INS' and (dg or scheme not in ('implicit euler', 'euler IMEX')):
+            marks = [pytest.mark.skip(reason='INS runs on the GPU path as continuous Taylor-Hood with implicit '
+                                             'Euler (Oseen) or Euler IMEX')]
         elif t['id'] in UNSTABLE:
             marks = [pytest.mark.skip(reason='the scheme is unstable on these forms (amplification 5.0 per step)')]
         else:
@@ -97,7 +104,7 @@ def test_reference_fixture_configs_parse():
                 for sec in s.sections():
                     if sec != 'METRICS':                       # a list of variable names
                         value_map(s, sec)
-        assert c.get_item(['OTHER', 'model'], str) in ('Poisson', 'MultiComponentINS')
+        assert c.get_item(['OTHER', 'model'], str) in ('Poisson', 'MultiComponentINS', 'INS')
     with pytest.raises(ValueError):
         ConfigParser(os.path.join(FIX, 'poisson_h_convergence', 'config')).get_item(['MESH', 'nonexistent_key'])
 
@@ -201,7 +208,7 @@ def test_reference_test_through_run(gpu_lib, oracle, case, capsys):
     lines = capsys.readouterr().out.strip().split('\n')
     nb = len(case['bounds'])
     errs = [float(ln.split(': ')[1]) for ln in lines[-nb:]]
-    assert all(ln.startswith('L2 norm in ') for ln in lines[-nb:])
+    assert all(ln.startswith('L2 norm in ') or ln.startswith('divergence of ') for ln in lines[-nb:])
     for e, bound in zip(errs, case['bounds']):
         assert math.isfinite(e)
         assert math.isclose(e, bound, rel_tol=3, abs_tol=1e-12)
