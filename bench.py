@@ -31,10 +31,10 @@ sys.path.insert(0, ROOT)
 EPS, WIND, DT = 1e-2, (1.0, 0.5, 0.25), 1e-3
 GAUSS = dict(c=(0.25, 0.25, 0.25), s=0.1)
 METRIC = 'DOF/s to 1e-8 FP64 rel. residual: mixed+batched+learned vs plain FP64, 1 GB300'
-# DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum) of the dominant kernel from an
-# ncu capture of the same kernel on the 48^3 x 6 case, scaled to the 64^3 x 6 launch by nnz; filled
-# in from the committed profile summary (profiles/), None until measured
-TRAFFIC = {}
+# DRAM bytes per matrix entry (dram__bytes_read.sum + dram__bytes_write.sum per launch / nnz) of the
+# dominant kernel, gm_spmv<float>, from an ncu capture on the 48^3 x 6 case (nnz 25,755,265; two
+# launches: 221.7 and 222.0 MB); the traffic of a launch is this figure times the launch's nnz
+TRAFFIC_PER_NNZ = {'gm_spmv_float': 8.615}
 
 
 def gaussian(X):
@@ -293,7 +293,8 @@ def run_ours(args):
         'e2e': {'value': e2e_val, 'unit': 'DOF/s', 'h2d_bytes_per_step': 8 * ndof, 'd2h_bytes_per_step': 8 * ndof},
         'roofline': {'bound': 'hbm', 'kernel': 'gm_spmv<float> (FP32 Krylov SpMV of the optimised path, CSR)',
                      'achieved': g_achieved, 'peak': peak, 'peak_kind': peak_kind, 'unit': 'GB/s',
-                     'frac': g_achieved / peak if g_achieved else None, 'traffic': TRAFFIC.get('gm_spmv_float'),
+                     'frac': g_achieved / peak if g_achieved else None, 'traffic': TRAFFIC_PER_NNZ['gm_spmv_float'] * nnz,
+                     'traffic_source': 'ncu dram bytes on the 48^3 x 6 case, scaled by nnz',
                      'algorithmic_bytes': g_bytes, 'avg_launch_ms': g_avg, 'launches_timed': g_launches,
                      'timing': 'CUDA events around every launch in the timed steps, on the launching stream'},
         'roofline_fp64_spmv': {'bound': 'hbm', 'kernel': 'spmv64 (CSR FP64, ocmp_spmv) timed alone, 50 launches',
@@ -311,6 +312,76 @@ def run_ours(args):
         print(json.dumps(line), flush=True)
     if world > 1:
         dist.destroy_process_group()
+
+
+def run_ins(args):
+    """Lid-driven cavity (OpenCMP INS model): unit square 256 x 256 x 2, Taylor-Hood P2/P1, nu = 1e-3
+    (Re = 1000 with lid speed 1), Euler IMEX steps dt = 1e-3 from rest (explicit convection,
+    reassembly every step), GMRES(50) with the block-diagonal preconditioner (velocity Jacobi,
+    pressure Schur-complement diagonal) to 1e-8; plain FP64 against FP32 inner / FP64 refinement."""
+    import torch
+    from opencmp_gb300 import fem, mesh as M, build, _lib
+    build.build()
+    torch.cuda.set_device(0)
+    n = args.n_ins
+    m = M.unit_square(n)
+    th = fem.TaylorHood(m, 2, m.bc_names)
+    lab = {k: m.bc_names.index(k) for k in m.bc_names}
+    nd = th.ndof
+    dt, nu = 1e-3, 1e-3
+    A = th.matrix()
+    dinv = torch.zeros(nd, dtype=torch.float64, device='cuda')
+    b = torch.zeros_like(dinv)
+    solvers = {p: fem.KrylovSolver(A, method='GMRES', restart=50, precond='user', precision=p, tol=1e-8, maxit=20000,
+                                   inner_tol=1e-4) for p in ('fp64', 'mixed')}
+
+    def step(sv, u, stats):
+        uprev = u.clone()
+        for c, val in ((0, 1.0), (1, 0.0)):
+            th.V.set_boundary({lab['bottom']: 0.0, lab['left']: 0.0, lab['right']: 0.0, lab['top']: val},
+                              th.component(u, c))
+        th.assemble(A, mass=1.0, nu=nu, dt=dt)
+        th.assemble_rhs(b, dt=dt, mass=1.0, uprev=uprev, imex=uprev)
+        th.block_diag(A, dinv)
+        sv.set_diag(dinv)
+        sv.update()
+        info = sv.solve(b, u, raise_on_fail=False)
+        stats.append((info.iterations, info.relres, info.status))
+
+    res = {}
+    for p in ('fp64', 'mixed'):
+        u = torch.zeros(nd, dtype=torch.float64, device='cuda')
+        st = []
+        for _ in range(args.warmup):
+            step(solvers[p], u, st)
+        st.clear()
+        torch.cuda.synchronize()
+        l0 = _lib.load().ocmp_launch_count()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(args.steps):
+            step(solvers[p], u, st)
+        e1.record()
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1)
+        l2, dv = th.errors(u)
+        res[p] = dict(ms=ms, launches=int(_lib.load().ocmp_launch_count() - l0),
+                      iters=float(np.mean([s[0] for s in st])), max_relres=float(max(s[1] for s in st)),
+                      converged=int(sum(1 for s in st if s[2] == 0)), u_l2=l2, div_l2=dv)
+    val = nd * args.steps / (res['mixed']['ms'] * 1e-3)
+    line = {'metric': METRIC + ' (INS lid-driven cavity)', 'value': val, 'unit': 'DOF/s', 'n_gpus': 1,
+            'steps': args.steps, 'warmup': args.warmup, 'ms_per_step': res['mixed']['ms'] / args.steps,
+            'higher_is_better': True, 'scaling': 'weak', 'vs_baseline': None, 'dtype': 'f64+f32',
+            'data': 'synthetic (generated structured mesh, cavity at rest)',
+            'config': {'workload': 'INS lid-driven cavity {0}x{0}x2 tri, Taylor-Hood P2/P1, Re=1000, Euler IMEX '
+                                   'dt=1e-3, GMRES(50) + block-diagonal (velocity Jacobi, pressure Schur '
+                                   'diagonal) to 1e-8'.format(n), 'ndof': nd, 'nnz': th.nnz,
+                       'l2': 'inputs larger than L2 (no flush)'},
+            'plain_fp64': dict(res['fp64'], value=nd * args.steps / (res['fp64']['ms'] * 1e-3), unit='DOF/s'),
+            'optimised': dict(res['mixed'], kind='FP32 inner GMRES + FP64 iterative refinement'),
+            'gpu_launches': res['mixed']['launches'],
+            'learned_guess': 'not applied to INS in this build'}
+    print(json.dumps(line), flush=True)
 
 
 def run_batched(args):
@@ -481,7 +552,8 @@ def main():
     ap.add_argument('--inner-tol', type=float, default=1e-4)
     ap.add_argument('--check-every', type=int, default=8)
     ap.add_argument('--no-cpu', action='store_true')
-    ap.add_argument('--config', default='transient3d', choices=['transient3d', 'batched'])
+    ap.add_argument('--config', default='transient3d', choices=['transient3d', 'batched', 'ins'])
+    ap.add_argument('--n-ins', type=int, default=256)
     ap.add_argument('--instances', type=int, default=512)
     ap.add_argument('--restart-batch', type=int, default=50)
     ap.add_argument('--train-runs', type=int, default=4)
@@ -490,6 +562,8 @@ def main():
     args = ap.parse_args()
     if args.impl == 'reference':
         run_reference(args)
+    elif args.config == 'ins':
+        run_ins(args)
     elif args.config == 'batched':
         run_batched(args)
     else:

@@ -357,23 +357,26 @@ __global__ void __launch_bounds__(256) elem_matrix_kernel(int64_t ne, const doub
     }
     const bool um = a.mass != 0.0, us = sd != 0.0, uc = a.wind_kind != OCMP_WIND_NONE;
     double* __restrict__ Ke = K + e * LL;
-    int slot = 0;
+    // Row-major order, each entry written once: a thread's successive stores fill the same sectors,
+    // so L2 merges them into full-sector writes (mirror stores to K_ji would leave partial sectors
+    // in flight). The symmetric part of an off-diagonal entry is evaluated for both (i,j), (j,i).
     for (int i = 0; i < L; i++)
-        for (int j = i; j < L; j++, slot++) {
+        for (int j = 0; j < L; j++) {
+            const int lo = i < j ? i : j, hi = i < j ? j : i;
+            const int slot = lo * L - lo * (lo - 1) / 2 + (hi - lo);
             const int o0 = __ldg(tt.off + 4 * slot), o1 = __ldg(tt.off + 4 * slot + 1),
                       o2 = __ldg(tt.off + 4 * slot + 2), o3 = __ldg(tt.off + 4 * slot + 3),
                       o4 = __ldg(tt.off + 4 * slot + 4);
-            double sv = 0, cij = 0, cji = 0;
+            double v = 0;
             if (um)
-                for (int t = o0; t < o1; t++) sv += F[__ldg(tt.g + t) * NTP] * __ldg(tt.coef + t);
+                for (int t = o0; t < o1; t++) v += F[__ldg(tt.g + t) * NTP] * __ldg(tt.coef + t);
             if (us)
-                for (int t = o1; t < o2; t++) sv += F[__ldg(tt.g + t) * NTP] * __ldg(tt.coef + t);
+                for (int t = o1; t < o2; t++) v += F[__ldg(tt.g + t) * NTP] * __ldg(tt.coef + t);
             if (uc) {
-                for (int t = o2; t < o3; t++) cij += F[__ldg(tt.g + t) * NTP] * __ldg(tt.coef + t);
-                for (int t = o3; t < o4; t++) cji += F[__ldg(tt.g + t) * NTP] * __ldg(tt.coef + t);
+                const int c0 = i <= j ? o2 : o3, c1 = i <= j ? o3 : o4;
+                for (int t = c0; t < c1; t++) v += F[__ldg(tt.g + t) * NTP] * __ldg(tt.coef + t);
             }
-            Ke[i * L + j] = sv + cij;
-            if (j != i) Ke[j * L + i] = sv + cji;
+            Ke[i * L + j] = v;
         }
 }
 
@@ -587,9 +590,11 @@ __global__ void __launch_bounds__(256) elem_matrix_ff_kernel(int64_t ne, const d
         }
     }
     const bool um = a.mass != 0.0, us = sd != 0.0, uc = a.wind_kind != OCMP_WIND_NONE;
-    int slot = 0;
+    // row-major order, each entry written once (see elem_matrix_kernel)
     for (int i = 0; i < L; i++)
-        for (int j = i; j < L; j++, slot++) {
+        for (int j = 0; j < L; j++) {
+            const int lo = i < j ? i : j, hi = i < j ? j : i;
+            const int slot = lo * L - lo * (lo - 1) / 2 + (hi - lo);
             const int o0 = __ldg(toff + 4 * slot), o1 = __ldg(toff + 4 * slot + 1), o2 = __ldg(toff + 4 * slot + 2),
                       o3 = __ldg(toff + 4 * slot + 3), o4 = __ldg(toff + 4 * slot + 4);
             float sh = 0.f, sl = 0.f;
@@ -607,23 +612,16 @@ __global__ void __launch_bounds__(256) elem_matrix_ff_kernel(int64_t ne, const d
                     ff_mul(f.x, f.y, c.x, c.y, ph, pl);
                     ff_add(sh, sl, ph, pl);
                 }
-            float ah = sh, al = sl, bh = sh, bl = sl;
             if (uc) {
-                for (int t = o2; t < o3; t++) {
+                const int c0 = i <= j ? o2 : o3, c1 = i <= j ? o3 : o4;
+                for (int t = c0; t < c1; t++) {
                     const float2 f = F[__ldg(tgg + t) * NTP], c = __ldg(tcf + t);
                     float ph, pl;
                     ff_mul(f.x, f.y, c.x, c.y, ph, pl);
-                    ff_add(ah, al, ph, pl);
-                }
-                for (int t = o3; t < o4; t++) {
-                    const float2 f = F[__ldg(tgg + t) * NTP], c = __ldg(tcf + t);
-                    float ph, pl;
-                    ff_mul(f.x, f.y, c.x, c.y, ph, pl);
-                    ff_add(bh, bl, ph, pl);
+                    ff_add(sh, sl, ph, pl);
                 }
             }
-            Ke[i * L + j] = make_float2(ah, al);
-            if (j != i) Ke[j * L + i] = make_float2(bh, bl);
+            Ke[i * L + j] = make_float2(sh, sl);
         }
     }
 }

@@ -1348,7 +1348,25 @@ int ocmp_solver_create(ocmp_matrix_t mat, const ocmp_solve_params_t* prm, ocmp_s
     const bool blk = prm->precond == OCMP_PRE_BLOCK_JACOBI;
     const int tpr = pick_tpr(s);
     const int64_t nbs = (n * tpr + kThreads - 1) / kThreads;
-    sv->grid = (int)std::max<int64_t>(1, std::min<int64_t>(kGridCap, nbs));
+    // one wave of the grid-stride reduction kernels: resident blocks per SM of the heaviest of them
+    // (they share the partial-sum layout, so they share the grid) times the SM count
+    {
+        int dev = 0, sms = 152, bmin = 8;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        auto occ = [&](const void* k) {
+            int nbk = 0;
+            if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nbk, k, kThreads, 0) == cudaSuccess && nbk > 0)
+                bmin = std::min(bmin, nbk);
+        };
+        occ((const void*)gm_resid<double, 4, 8>);
+        occ((const void*)gm_resid<float, 4, 8>);
+        occ((const void*)gm_dots<double>);
+        occ((const void*)gm_orth<double>);
+        occ((const void*)gm_dots<float>);
+        occ((const void*)gm_orth<float>);
+        sv->grid = (int)std::max<int64_t>(1, std::min<int64_t>(std::min<int64_t>(kGridCap, (int64_t)bmin * sms), nbs));
+    }
     const int64_t hsz = (int64_t)(m + 1) * m + 4 * m + 2;
     sv->bat = Bat{NB > 1 ? n : 0,
                   NB > 1 ? s->nnz : 0,
@@ -1412,7 +1430,7 @@ int ocmp_solver_create(ocmp_matrix_t mat, const ocmp_solve_params_t* prm, ocmp_s
         delete sv;
         return st;
     }
-    st = ocmp_solver_update(sv, nullptr);
+    if (prm->precond != OCMP_PRE_USER) st = ocmp_solver_update(sv, nullptr);  // USER: after ocmp_solver_set_diag
     if (st) {
         free_solver(sv);
         delete sv;

@@ -61,7 +61,7 @@ class Solver:
             v.op.assemble(op_form)
             LB.call('ocmp_spmv_axpby', v.op.h, -(1.0 - theta) * dt, _ptr(uprev), 1.0, _ptr(v.b), _stream(None))
             del keep0
-        info = v.solver.solve(v.b, v.u)
+        info = v.solve()
         del keep
         self.infos.append(info)
         return info
