@@ -143,7 +143,7 @@ def run_ours(args):
         sv = solvers['fp64' if kind == 'fp64' else 'mixed']
         sv.mat.assemble(form)
         sv.update()
-        fem.assemble_rhs(space, form, fem.make_rhs(dt=DT, mass=1.0, uprev=u_in), b)
+        fem.assemble_rhs(space, form, fem.make_rhs(dt=DT, mass=1.0, uprev=u_in, dfloat=kind != 'fp64'), b)
         used = False
         if kind == 'learned':
             used = guess.predict(u_out, sv.mat, b)

@@ -101,6 +101,8 @@ typedef struct {
                                 labels of bval_mask                                                  */
     const double* gval_fq;   /* device, nbf*nfq or NULL: DG Dirichlet data there, instead of gval[] */
     int32_t accumulate;      /* nonzero: b += L(v) instead of b = L(v)                            */
+    int32_t dfloat;          /* nonzero: the mass term in double-float arithmetic on the FP32 pipes
+                                (about 1e-14 relative to the FP64 product)                          */
 } ocmp_rhs_t;
 
 typedef struct {

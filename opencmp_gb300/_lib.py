@@ -40,7 +40,7 @@ class Rhs(C.Structure):
     _fields_ = [('dt', C.c_double), ('src_kind', C.c_int32), ('src_const', C.c_double), ('src_qp', C.c_void_p),
                 ('mass', C.c_double), ('uprev', C.c_void_p), ('bval', C.c_double * 32), ('bval_mask', C.c_uint32),
                 ('gval', C.c_double * 32), ('bval_fq', C.c_void_p), ('gval_fq', C.c_void_p),
-                ('accumulate', C.c_int32)]
+                ('accumulate', C.c_int32), ('dfloat', C.c_int32)]
 
 
 class THForm(C.Structure):

@@ -227,6 +227,15 @@ class ConfigParser(configparser.ConfigParser):
                 raise FileNotFoundError('The given config file "{}" does not exist.'.format(config_file_path))
             self.read(config_file_path)
 
+    @classmethod
+    def from_parser(cls, other: configparser.ConfigParser) -> 'ConfigParser':
+        """A copy of another configparser's sections (e.g. OpenCMP's own ConfigParser)."""
+        c = cls()
+        for sec in other.sections():
+            c[sec] = {k: v for k, v in other.items(sec, raw=True)}
+        c.path = getattr(other, 'path', None)
+        return c
+
     def _raw(self, keys: List[str]):
         sec, key = keys[0], keys[1]
         if self.has_option(sec, key):

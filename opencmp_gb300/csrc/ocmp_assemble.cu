@@ -755,7 +755,8 @@ __global__ void rhs_elem_kernel(int64_t ne, const double* __restrict__ X, const 
                                 const double* __restrict__ gval, const double* __restrict__ bfq,
                                 const double* __restrict__ gfq, int is_l2, int nfq, const double* __restrict__ fw,
                                 const double* __restrict__ fphi, const double* __restrict__ fdphi,
-                                const double* __restrict__ flam, double* __restrict__ Fe) {
+                                const double* __restrict__ flam, const float2* __restrict__ Rmf,
+                                double* __restrict__ Fe) {
     int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (e >= ne) return;
     Geo g;
@@ -774,7 +775,29 @@ __global__ void rhs_elem_kernel(int64_t ne, const double* __restrict__ X, const 
             for (int i = 0; i < L; i++) out[i] += fq * qphi[q * L + i];
         }
     }
-    if (uprev) {
+    if (uprev && Rmf) {
+        // double-float: (sum_j Rm_ij u_j) with Rm and u as (hi, lo) float pairs, then one FP64 scale
+        float uh[L], ul[L];
+#pragma unroll
+        for (int j = 0; j < L; j++) {
+            const float2 p = ff_split(uprev[dofs[e * L + j]]);
+            uh[j] = p.x;
+            ul[j] = p.y;
+        }
+        const double s = mass * g.adet;
+#pragma unroll
+        for (int i = 0; i < L; i++) {
+            float sh = 0.f, sl = 0.f;
+#pragma unroll
+            for (int j = 0; j < L; j++) {
+                const float2 c = __ldg(Rmf + i * L + j);
+                float ph, pl;
+                ff_mul(c.x, c.y, uh[j], ul[j], ph, pl);
+                ff_add(sh, sl, ph, pl);
+            }
+            out[i] += s * ff_to_double(sh, sl);
+        }
+    } else if (uprev) {
         double u[L];
 #pragma unroll
         for (int j = 0; j < L; j++) u[j] = uprev[dofs[e * L + j]];
@@ -1017,7 +1040,8 @@ int rhs_impl(ocmp_space_s* s, const ocmp_form_t* f, const ocmp_rhs_t* r, double*
     OCMP_LAUNCH(rhs_elem_kernel<D, L><<<nblk(ne, 128), 128, 0, st>>>(
         ne, mesh->dX, mesh->dconn, s->d_dofs, a, r->dt, r->src_kind, r->src_const, r->src_qp, r->mass, r->uprev,
         s->T.nq, s->d_qw, s->d_qphi, s->d_mvec, s->d_Rc, s->d_ebf_ptr, s->d_ebf, s->d_bfac, dvals, r->bval_mask,
-        dvals + 32, r->bval_fq, r->gval_fq, s->kind == OCMP_L2, s->T.nfq, s->d_fw, s->d_fphi, s->d_fdphi, s->d_flam, s->d_Fe));
+        dvals + 32, r->bval_fq, r->gval_fq, s->kind == OCMP_L2, s->T.nfq, s->d_fw, s->d_fphi, s->d_fdphi, s->d_flam,
+        r->dfloat ? s->d_Rm_ff : nullptr, s->d_Fe));
     OCMP_LAUNCH(rhs_gather_kernel<<<nblk(s->ndof, 256), 256, 0, st>>>(s->ndof, s->d_inc_ptr, s->d_inc, s->d_Fe, b, r->accumulate));
     OCMP_CUDA(cudaFreeAsync(dvals, st));
     OCMP_CUDA(cudaGetLastError());

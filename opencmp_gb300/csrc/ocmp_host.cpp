@@ -512,7 +512,7 @@ static void free_space_device(ocmp_space_s* s) {
                   s->d_inc_ptr,  s->d_inc,      s->d_ifac,      s->d_bfac,     s->d_ebf_ptr,   s->d_ebf,
                   s->d_Rc,       s->d_Rv,       s->d_qw,        s->d_qphi,     s->d_mvec,      s->d_fw,
                   s->d_fphi,     s->d_fdphi,    s->d_flam,      s->d_K,        s->d_facetK,    s->d_Fe,
-                  s->d_lift_ptr, s->d_lift_pos};
+                  s->d_lift_ptr, s->d_lift_pos, s->d_Rm_ff};
     for (void* p : ps) dfree(p);
 }
 
@@ -837,6 +837,17 @@ int ocmp_space_create(ocmp_mesh_t mesh, int32_t kind, int32_t order, uint32_t di
     U(&s->d_lift_ptr, lift_ptr);
     U(&s->d_lift_pos, lift_pos);
     U(&s->d_Rc, s->T.R_const);
+    {
+        // reference mass matrix as (hi, lo) float pairs for the double-float RHS
+        const size_t LLm = (size_t)s->nloc * s->nloc;
+        std::vector<float2> rm(LLm);
+        for (size_t t = 0; t < LLm; t++) {
+            const double c = s->T.R_const[t];
+            const float hi = (float)c;
+            rm[t] = make_float2(hi, (float)(c - (double)hi));
+        }
+        U(&s->d_Rm_ff, rm);
+    }
     U(&s->d_Rv, s->T.R_vtx);
     U(&s->d_qw, s->T.qw);
     U(&s->d_qphi, s->T.qphi);

@@ -129,6 +129,7 @@ struct ocmp_space_s {
     int32_t* d_lift_ptr = nullptr;  // ndof+1: per free row, CSR positions whose column is constrained
     int32_t* d_lift_pos = nullptr;
     double* d_Rc = nullptr;         // R_const
+    float2* d_Rm_ff = nullptr;      // reference mass matrix as (hi, lo) float pairs
     double* d_Rv = nullptr;         // R_vtx
     double* d_qw = nullptr;
     double* d_qphi = nullptr;

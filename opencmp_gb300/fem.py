@@ -168,7 +168,7 @@ def make_form(mass=0.0, diff=0.0, dt=1.0, wind=None, wind_vtx: Optional[torch.Te
 def make_rhs(dt=1.0, src_const=None, src_qp: Optional[torch.Tensor] = None, mass=0.0,
              uprev: Optional[torch.Tensor] = None, bval: Optional[Dict[int, float]] = None,
              gval: Optional[Dict[int, float]] = None, bval_fq: Optional[torch.Tensor] = None,
-             gval_fq: Optional[torch.Tensor] = None, bval_mask: Optional[int] = None) -> LB.Rhs:
+             gval_fq: Optional[torch.Tensor] = None, bval_mask: Optional[int] = None, dfloat: bool = False) -> LB.Rhs:
     r = LB.Rhs()
     r.dt, r.mass = dt, mass
     r.src_kind = LB.SRC_NONE
@@ -185,6 +185,7 @@ def make_rhs(dt=1.0, src_const=None, src_qp: Optional[torch.Tensor] = None, mass
         r.gval[lab] = v
     if bval_mask is not None:
         r.bval_mask = bval_mask
+    r.dfloat = int(dfloat)
     if bval_fq is not None:
         r.bval_fq = bval_fq.data_ptr()
     if gval_fq is not None:

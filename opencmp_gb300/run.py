@@ -14,6 +14,8 @@ from .solvers import get_solver_class
 def run(config_file_path: str, config_parser: Optional[ConfigParser] = None):
     if config_parser is None:
         config_parser = ConfigParser(config_file_path)
+    elif not isinstance(config_parser, ConfigParser):
+        config_parser = ConfigParser.from_parser(config_parser)   # e.g. OpenCMP's own parser
     model_name = config_parser.get_item(['OTHER', 'model'], str)
     dim_used = config_parser.get_item(['DIM', 'diffuse_interface_method'], bool, quiet=True)
     model_class = get_model_class(model_name, dim_used)

@@ -283,3 +283,15 @@ def test_space_dependent_dirichlet_is_exact_for_polynomials(gpu_lib, order):
     fem.KrylovSolver(Mm, method="CG", tol=1e-13, maxit=5000).solve(b, x)
     ub, xb = u.cpu().numpy()[~free], x.cpu().numpy()[~free]
     assert np.abs(ub - xb).max() < 1e-9 * max(1.0, np.abs(xb).max())
+
+
+def test_config_copied_from_another_parser():
+    """run() accepts OpenCMP's own parser: its sections are copied into this package's parser."""
+    import configparser
+    other = configparser.ConfigParser()
+    other.optionxform = str
+    other.read(os.path.join(FIX, 'mcins_diffusion_convection', 'config'))
+    c = ConfigParser.from_parser(other)
+    assert c.get_item(['TRANSIENT', 'dt'], float) == 0.01
+    assert c.get_dict(['FINITE ELEMENT SPACE', 'elements'], all_str=True)['b'] == 'H1'
+    assert c.get_dict(['SOLVER', 'nonlinear_tolerance'])['absolute'] == 1e-8

@@ -128,8 +128,9 @@ def _src_sinprod(X, D):
     return v
 
 
+@pytest.mark.parametrize('dfloat', [False, True])
 @pytest.mark.parametrize('name,mk,kind,order', CASES, ids=[c[0] for c in CASES])
-def test_rhs_matches_oracle(gpu_lib, oracle, name, mk, kind, order):
+def test_rhs_matches_oracle(gpu_lib, oracle, name, mk, kind, order, dfloat):
     import torch
     from opencmp_gb300 import fem
     m = mk()
@@ -144,7 +145,8 @@ def test_rhs_matches_oracle(gpu_lib, oracle, name, mk, kind, order):
     fq = _t(_src_sinprod(g.quad_points(), D))
     b = torch.zeros(g.ndof, dtype=torch.float64, device='cuda')
     gv = {0: 0.7, 1: -0.4}
-    fem.assemble_rhs(g, gf, fem.make_rhs(dt=0.2, src_qp=fq, mass=0.9, uprev=_t(up), bval={lab0: 2.5}, gval=gv), b)
+    fem.assemble_rhs(g, gf, fem.make_rhs(dt=0.2, src_qp=fq, mass=0.9, uprev=_t(up), bval={lab0: 2.5}, gval=gv,
+                                         dfloat=dfloat), b)
     bo = o.rhs(of, oracle.make_rhs(dt=0.2, src_kind=oracle.SRC_SINPROD, src=(2 * math.pi ** 2,), mass=0.9, uprev=up,
                                    bval={lab0: 2.5}, gval=gv))
     bg = b.cpu().numpy()
