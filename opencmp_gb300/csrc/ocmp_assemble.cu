@@ -357,26 +357,23 @@ __global__ void __launch_bounds__(256) elem_matrix_kernel(int64_t ne, const doub
     }
     const bool um = a.mass != 0.0, us = sd != 0.0, uc = a.wind_kind != OCMP_WIND_NONE;
     double* __restrict__ Ke = K + e * LL;
-    // Row-major order, each entry written once: a thread's successive stores fill the same sectors,
-    // so L2 merges them into full-sector writes (mirror stores to K_ji would leave partial sectors
-    // in flight). The symmetric part of an off-diagonal entry is evaluated for both (i,j), (j,i).
+    int slot = 0;
     for (int i = 0; i < L; i++)
-        for (int j = 0; j < L; j++) {
-            const int lo = i < j ? i : j, hi = i < j ? j : i;
-            const int slot = lo * L - lo * (lo - 1) / 2 + (hi - lo);
+        for (int j = i; j < L; j++, slot++) {
             const int o0 = __ldg(tt.off + 4 * slot), o1 = __ldg(tt.off + 4 * slot + 1),
                       o2 = __ldg(tt.off + 4 * slot + 2), o3 = __ldg(tt.off + 4 * slot + 3),
                       o4 = __ldg(tt.off + 4 * slot + 4);
-            double v = 0;
+            double sv = 0, cij = 0, cji = 0;
             if (um)
-                for (int t = o0; t < o1; t++) v += F[__ldg(tt.g + t) * NTP] * __ldg(tt.coef + t);
+                for (int t = o0; t < o1; t++) sv += F[__ldg(tt.g + t) * NTP] * __ldg(tt.coef + t);
             if (us)
-                for (int t = o1; t < o2; t++) v += F[__ldg(tt.g + t) * NTP] * __ldg(tt.coef + t);
+                for (int t = o1; t < o2; t++) sv += F[__ldg(tt.g + t) * NTP] * __ldg(tt.coef + t);
             if (uc) {
-                const int c0 = i <= j ? o2 : o3, c1 = i <= j ? o3 : o4;
-                for (int t = c0; t < c1; t++) v += F[__ldg(tt.g + t) * NTP] * __ldg(tt.coef + t);
+                for (int t = o2; t < o3; t++) cij += F[__ldg(tt.g + t) * NTP] * __ldg(tt.coef + t);
+                for (int t = o3; t < o4; t++) cji += F[__ldg(tt.g + t) * NTP] * __ldg(tt.coef + t);
             }
-            Ke[i * L + j] = v;
+            Ke[i * L + j] = sv + cij;
+            if (j != i) Ke[j * L + i] = sv + cji;
         }
 }
 
@@ -523,20 +520,15 @@ __device__ __forceinline__ float2 ff_split(double x) {
     return make_float2(h, __double2float_rn(x - f2d_exact(h)));
 }
 
-template <int D, int L>
-__global__ void __launch_bounds__(256) elem_matrix_ff_kernel(int64_t ne, const double* __restrict__ X,
-                                                             const int32_t* __restrict__ conn, FormArgs a,
-                                                             const int32_t* __restrict__ toff,
-                                                             const uint8_t* __restrict__ tgg,
-                                                             const float2* __restrict__ tcf, float2* __restrict__ K) {
-    constexpr int NP = D + 1, NS = NP * (NP + 1) / 2, LL = L * L;
-    extern __shared__ float2 Fs2[];
-    const int NTP = blockDim.x + 1, tid = threadIdx.x;
-    const int64_t e = blockIdx.x * (int64_t)blockDim.x + tid;
+// Static element geometry of a mesh, once per space (the mesh does not move): |det J|,
+// |det J| grad(lam_p).grad(lam_q) (p <= q) and |det J| grad(lam_p), as (hi, lo) float pairs in
+// structure-of-arrays order (quantity k of element e at G[k * ne + e]).
+template <int D>
+__global__ void geo_ff_kernel(int64_t ne, const double* __restrict__ X, const int32_t* __restrict__ conn,
+                              float2* __restrict__ G) {
+    constexpr int NP = D + 1;
+    const int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (e >= ne) return;
-    float2* F = Fs2 + tid;
-    float2* __restrict__ Ke = K + e * LL;
-    {
     Geo g;
     double x0[3];
     element_geo<D>(X, conn, e, g, x0);
@@ -551,44 +543,83 @@ __global__ void __launch_bounds__(256) elem_matrix_ff_kernel(int64_t ne, const d
         }
         gl[0][r] = -s0;
     }
-    F[0] = ff_split(a.mass * g.adet);
-    const double sd = a.dt * a.diff * g.adet;
-    int pi = 1;
+    int k = 0;
+    G[(k++) * ne + e] = ff_split(g.adet);
 #pragma unroll
     for (int p = 0; p < NP; p++)
 #pragma unroll
-        for (int q = p; q < NP; q++, pi++) {
+        for (int q = p; q < NP; q++) {
             double t = 0;
 #pragma unroll
             for (int r = 0; r < D; r++) t += gl[p][r] * gl[q][r];
-            F[pi * NTP] = ff_split(sd * t);
+            G[(k++) * ne + e] = ff_split(g.adet * t);
         }
-    const double sw = -a.dt * g.adet;
+#pragma unroll
+    for (int p = 0; p < NP; p++)
+#pragma unroll
+        for (int r = 0; r < D; r++) G[(k++) * ne + e] = ff_split(g.adet * gl[p][r]);
+}
+
+// (ah + al)(bh + bl), renormalised so the pair can feed further products
+__device__ __forceinline__ float2 ff_prod(float2 a, float2 b) {
+    float ph, pl;
+    ff_mul(a.x, a.y, b.x, b.y, ph, pl);
+    const float s = __fadd_rn(ph, pl);
+    return make_float2(s, __fsub_rn(pl, __fsub_rn(s, ph)));
+}
+
+template <int D, int L>
+__global__ void __launch_bounds__(256) elem_matrix_ff_kernel(int64_t ne, const float2* __restrict__ geo,
+                                                             const int32_t* __restrict__ conn, FormArgs a,
+                                                             const int32_t* __restrict__ toff,
+                                                             const uint8_t* __restrict__ tgg,
+                                                             const float2* __restrict__ tcf, float2* __restrict__ K) {
+    constexpr int NP = D + 1, NS = NP * (NP + 1) / 2, LL = L * L;
+    extern __shared__ float2 Fs2[];
+    const int NTP = blockDim.x + 1, tid = threadIdx.x;
+    const int64_t e = blockIdx.x * (int64_t)blockDim.x + tid;
+    if (e >= ne) return;
+    float2* F = Fs2 + tid;
+    float2* __restrict__ Ke = K + e * LL;
+    {
+    // factors = coefficients (split once per thread) x the element's static geometry
+    const float2 cm = ff_split(a.mass), cs = ff_split(a.dt * a.diff), cw = ff_split(-a.dt);
+    F[0] = ff_prod(cm, __ldg(geo + e));
+#pragma unroll
+    for (int pi = 0; pi < NS; pi++) F[(1 + pi) * NTP] = ff_prod(cs, __ldg(geo + (1 + pi) * ne + e));
+    const float2* __restrict__ ggl = geo + (1 + NS) * ne + e;   // |det J| grad(lam_p)_r at [(p * D + r) * ne]
     if (a.wind_kind == OCMP_WIND_CONST) {
-        const double w[3] = {a.w0, a.w1, a.w2};
+        const float2 w[3] = {ff_split(a.w0), ff_split(a.w1), ff_split(a.w2)};
 #pragma unroll
         for (int p = 0; p < NP; p++) {
-            double t = 0;
+            float th = 0.f, tl = 0.f;
 #pragma unroll
-            for (int r = 0; r < D; r++) t += w[r] * gl[p][r];
-            F[(1 + NS + p) * NTP] = ff_split(sw * t);
+            for (int r = 0; r < D; r++) {
+                const float2 m = ff_prod(w[r], __ldg(ggl + (p * D + r) * ne));
+                ff_add(th, tl, m.x, m.y);
+            }
+            F[(1 + NS + p) * NTP] = ff_prod(cw, make_float2(th, tl));
         }
     } else if (a.wind_kind == OCMP_WIND_VERTEX) {
 #pragma unroll
         for (int v = 0; v < NP; v++) {
             const int32_t gv = conn[e * NP + v];
-            double w[3];
+            float2 w[3];
 #pragma unroll
-            for (int r = 0; r < D; r++) w[r] = a.wind_vtx[(int64_t)gv * D + r];
+            for (int r = 0; r < D; r++) w[r] = ff_split(a.wind_vtx[(int64_t)gv * D + r]);
 #pragma unroll
             for (int p = 0; p < NP; p++) {
-                double t = 0;
+                float th = 0.f, tl = 0.f;
 #pragma unroll
-                for (int r = 0; r < D; r++) t += w[r] * gl[p][r];
-                F[(1 + NS + p * NP + v) * NTP] = ff_split(sw * t);
+                for (int r = 0; r < D; r++) {
+                    const float2 m = ff_prod(w[r], __ldg(ggl + (p * D + r) * ne));
+                    ff_add(th, tl, m.x, m.y);
+                }
+                F[(1 + NS + p * NP + v) * NTP] = ff_prod(cw, make_float2(th, tl));
             }
         }
     }
+    const double sd = a.dt * a.diff;
     const bool um = a.mass != 0.0, us = sd != 0.0, uc = a.wind_kind != OCMP_WIND_NONE;
     // row-major order, each entry written once (see elem_matrix_kernel)
     for (int i = 0; i < L; i++)
@@ -743,6 +774,95 @@ __global__ void __launch_bounds__(128) row_scatter_ff_kernel(
     }
 }
 
+// Warp-per-row gather for element-only assembly (no facet terms). The row's accumulator sits in a
+// per-warp shared-memory stripe; lanes are split into G = 32 / L groups, each loading one incidence's
+// row slice (L values, coalesced) and slot bytes, so G slices are in flight per round. The adds run
+// group after group, i.e. in incidence order, so every entry is summed in the same order as the
+// thread-per-row kernel and the values are bit-identical to it. The row is then written with
+// consecutive lanes on consecutive entries. AccT: double (FP64 path) or float2 (double-float path).
+template <int L, bool FF>
+__global__ void __launch_bounds__(256) row_gather_warp_kernel(
+    int64_t r0, int64_t r1, const int32_t* __restrict__ rp, const int32_t* __restrict__ col,
+    const int32_t* __restrict__ inc_ptr, const int32_t* __restrict__ inc, const void* __restrict__ Kv,
+    const uint8_t* __restrict__ slot, int ss, int stripe, const double* __restrict__ dinv,
+    const float* __restrict__ dinv32, double* __restrict__ vals, float* __restrict__ vals32,
+    double* __restrict__ svals64, float* __restrict__ svals32) {
+    constexpr int G = 32 / L > 0 ? 32 / L : 1;
+    extern __shared__ double wacc[];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int g = lane / L, j = lane % L;
+    const bool act = g < G;
+    double* __restrict__ acc = wacc + (size_t)w * stripe;
+    float2* __restrict__ acc2 = reinterpret_cast<float2*>(acc);
+    const int64_t wpb = blockDim.x >> 5;
+    for (int64_t r = r0 + blockIdx.x * wpb + w; r < r1; r += (int64_t)gridDim.x * wpb) {
+        const int32_t base = rp[r], rn = rp[r + 1] - base;
+        for (int q = lane; q < rn; q += 32) acc[q] = 0.0;
+        __syncwarp();
+        const int32_t k0 = inc_ptr[r], k1 = inc_ptr[r + 1];
+        // round k: incidences kb .. kb + G - 1; the next round's loads are issued before the adds
+        double v = 0.0;
+        int sl = 0;
+        bool have = act && k0 + g < k1;
+        if (have) {
+            const int64_t flat = inc[k0 + g];
+            v = FF ? __longlong_as_double(__ldg(reinterpret_cast<const long long*>(Kv) + flat * L + j))
+                   : __ldg(reinterpret_cast<const double*>(Kv) + flat * L + j);
+            sl = __ldg(slot + flat * ss + j);
+        }
+        for (int32_t kb = k0; kb < k1; kb += G) {
+            double vn = 0.0;
+            int sln = 0;
+            const bool hn = act && kb + G + g < k1;
+            if (hn) {
+                const int64_t flat = inc[kb + G + g];
+                vn = FF ? __longlong_as_double(__ldg(reinterpret_cast<const long long*>(Kv) + flat * L + j))
+                        : __ldg(reinterpret_cast<const double*>(Kv) + flat * L + j);
+                sln = __ldg(slot + flat * ss + j);
+            }
+#pragma unroll
+            for (int gg = 0; gg < G; gg++) {
+                if (have && g == gg) {
+                    if (FF) {
+                        const long long bits = __double_as_longlong(v);
+                        const float vh = __int_as_float((int)(bits & 0xffffffffll)), vl = __int_as_float((int)(bits >> 32));
+                        float2 a2 = acc2[sl];
+                        ff_add(a2.x, a2.y, vh, vl);
+                        acc2[sl] = a2;
+                    } else {
+                        acc[sl] += v;
+                    }
+                }
+                __syncwarp();
+            }
+            v = vn;
+            sl = sln;
+            have = hn;
+        }
+        for (int q = lane; q < rn; q += 32) {
+            if (FF) {
+                const float2 a2 = acc2[q];
+                const double vv = ff_to_double(a2.x, a2.y);
+                vals[base + q] = vv;
+                const float v32 = __fadd_rn(a2.x, a2.y);
+                if (vals32) vals32[base + q] = v32;
+                if (svals64) svals64[base + q] = vv * dinv[col[base + q]];
+                if (svals32) svals32[base + q] = v32 * dinv32[col[base + q]];
+            } else {
+                const double vv = acc[q];
+                vals[base + q] = vv;
+                if (vals32) vals32[base + q] = (float)vv;
+                if (svals64 || svals32) {
+                    const double sv = vv * dinv[col[base + q]];
+                    if (svals64) svals64[base + q] = sv;
+                    if (svals32) svals32[base + q] = (float)sv;
+                }
+            }
+        }
+        __syncwarp();
+    }
+}
+
 // Element right-hand sides: dt (f, phi_i) + mass (u_prev, phi_i) + boundary data.
 template <int D, int L>
 __global__ void rhs_elem_kernel(int64_t ne, const double* __restrict__ X, const int32_t* __restrict__ conn,
@@ -756,12 +876,21 @@ __global__ void rhs_elem_kernel(int64_t ne, const double* __restrict__ X, const 
                                 const double* __restrict__ gfq, int is_l2, int nfq, const double* __restrict__ fw,
                                 const double* __restrict__ fphi, const double* __restrict__ fdphi,
                                 const double* __restrict__ flam, const float2* __restrict__ Rmf,
-                                double* __restrict__ Fe) {
+                                const float2* __restrict__ geo, double* __restrict__ Fe) {
     int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (e >= ne) return;
+    // |det J| from the static geometry when the space has it; the full geometry (J^-1) only for
+    // elements with boundary-facet terms
     Geo g;
     double x0[3];
-    element_geo<D>(X, conn, e, g, x0);
+    bool have_geo = false;
+    if (geo) {
+        const float2 a0 = __ldg(geo + e);
+        g.adet = ff_to_double(a0.x, a0.y);
+    } else {
+        element_geo<D>(X, conn, e, g, x0);
+        have_geo = true;
+    }
     double out[L];
 #pragma unroll
     for (int i = 0; i < L; i++) out[i] = 0;
@@ -817,6 +946,10 @@ __global__ void rhs_elem_kernel(int64_t ne, const double* __restrict__ X, const 
         const uint32_t bit = 1u << lab;
         const bool hb = bval_mask & bit, hg = is_l2 && (a.nitsche & bit);
         if (!hb && !hg) continue;
+        if (!have_geo) {
+            element_geo<D>(X, conn, e, g, x0);
+            have_geo = true;
+        }
         double nrm[3], meas;
         facet_geo<D>(X, conn, e, lf, nrm, meas);
         const double h = D == 2 ? sqrt(g.adet) : cbrt(g.adet);
@@ -965,8 +1098,14 @@ int assemble_impl(ocmp_matrix_s* m, const ocmp_form_t* f, cudaStream_t st) {
         const int ntf = 256;
         const size_t smf = sizeof(float2) * (size_t)NG * (ntf + 1);
         OCMP_CUDA(cudaFuncSetAttribute(elem_matrix_ff_kernel<D, L>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smf));
-        OCMP_LAUNCH(elem_matrix_ff_kernel<D, L><<<nblk(ne, ntf), ntf, smf, st>>>(ne, mesh->dX, mesh->dconn, a, s->d_slot_off[var],
-                                                                    s->d_term_g[var], s->d_term_coef_ff[var], Kff));
+        if (!s->d_geo_ff) {
+            constexpr int NGEO = 1 + (D + 1) * (D + 2) / 2 + (D + 1) * D;
+            OCMP_CUDA(cudaMalloc((void**)&s->d_geo_ff, sizeof(float2) * (size_t)NGEO * ne));
+            OCMP_LAUNCH(geo_ff_kernel<D><<<nblk(ne, 128), 128, 0, st>>>(ne, mesh->dX, mesh->dconn, s->d_geo_ff));
+        }
+        OCMP_LAUNCH(elem_matrix_ff_kernel<D, L><<<nblk(ne, ntf), ntf, smf, st>>>(ne, s->d_geo_ff, mesh->dconn, a,
+                                                                    s->d_slot_off[var], s->d_term_g[var],
+                                                                    s->d_term_coef_ff[var], Kff));
     } else {
         OCMP_LAUNCH(elem_matrix_kernel<D, L><<<nblk(ne, nt), nt, smem, st>>>(ne, mesh->dX, mesh->dconn, a, tt, s->d_K));
     }
@@ -998,6 +1137,26 @@ int assemble_impl(ocmp_matrix_s* m, const ocmp_form_t* f, cudaStream_t st) {
     else if (m->dinv)
         OCMP_LAUNCH(diag_kernel<L><<<nblk(nd, 256), 256, 0, st>>>(nd, s->d_inc_ptr, s->d_inc, s->d_K, s->d_free, use_facets, efp,
                                                       s->d_efac, s->d_ebf_ptr, s->d_ebf, Ki, Kb, m->dinv));
+    if (!use_facets) {
+        // element-only assembly: one warp per row (row_gather_warp_kernel)
+        const int wt = 256, wpb = wt / 32;
+        const int stripe = s->maxrow;
+        const size_t wsm = sizeof(double) * (size_t)stripe * wpb;
+        auto kern = dfl ? row_gather_warp_kernel<L, true> : row_gather_warp_kernel<L, false>;
+        OCMP_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)wsm));
+        int dev = 0, sms = 152, per = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        OCMP_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kern, wt, wsm));
+        const int64_t want = (nd + wpb - 1) / wpb;
+        const unsigned grid = (unsigned)std::max<int64_t>(1, std::min<int64_t>(want, (int64_t)std::max(per, 1) * sms));
+        const void* Kv = dfl ? (const void*)Kff : (const void*)s->d_K;
+        OCMP_LAUNCH(kern<<<grid, wt, wsm, st>>>(0, nd, s->d_rowptr, s->d_col, s->d_inc_ptr, s->d_inc, Kv, s->d_slot,
+                                              s->slot_stride, stripe, m->dinv, m->dinv32, m->vals, m->vals32,
+                                              m->svals64, m->svals32));
+        OCMP_CUDA(cudaGetLastError());
+        return OCMP_OK;
+    }
     // rows in ranges of similar length (vertex rows, then the rest) so short rows get small stripes
     const int rt = 128;
     OCMP_CUDA(cudaFuncSetAttribute(row_scatter_kernel<L>, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -1041,7 +1200,7 @@ int rhs_impl(ocmp_space_s* s, const ocmp_form_t* f, const ocmp_rhs_t* r, double*
         ne, mesh->dX, mesh->dconn, s->d_dofs, a, r->dt, r->src_kind, r->src_const, r->src_qp, r->mass, r->uprev,
         s->T.nq, s->d_qw, s->d_qphi, s->d_mvec, s->d_Rc, s->d_ebf_ptr, s->d_ebf, s->d_bfac, dvals, r->bval_mask,
         dvals + 32, r->bval_fq, r->gval_fq, s->kind == OCMP_L2, s->T.nfq, s->d_fw, s->d_fphi, s->d_fdphi, s->d_flam,
-        r->dfloat ? s->d_Rm_ff : nullptr, s->d_Fe));
+        r->dfloat ? s->d_Rm_ff : nullptr, r->dfloat ? s->d_geo_ff : nullptr, s->d_Fe));
     OCMP_LAUNCH(rhs_gather_kernel<<<nblk(s->ndof, 256), 256, 0, st>>>(s->ndof, s->d_inc_ptr, s->d_inc, s->d_Fe, b, r->accumulate));
     OCMP_CUDA(cudaFreeAsync(dvals, st));
     OCMP_CUDA(cudaGetLastError());

@@ -130,6 +130,7 @@ struct ocmp_space_s {
     int32_t* d_lift_pos = nullptr;
     double* d_Rc = nullptr;         // R_const
     float2* d_Rm_ff = nullptr;      // reference mass matrix as (hi, lo) float pairs
+    float2* d_geo_ff = nullptr;     // static element geometry for the double-float element kernel
     double* d_Rv = nullptr;         // R_vtx
     double* d_qw = nullptr;
     double* d_qphi = nullptr;

@@ -143,6 +143,9 @@ def test_rhs_matches_oracle(gpu_lib, oracle, name, mk, kind, order, dfloat):
     of = oracle.make_form(diff=0.3, dt=0.2, wind=(1.0, -0.5, 0.2)[:D], nitsche_mask=nit, dg=kind == 1)
     gf = fem.make_form(diff=0.3, dt=0.2, wind=(1.0, -0.5, 0.2)[:D], nitsche_mask=nit, dg=kind == 1)
     fq = _t(_src_sinprod(g.quad_points(), D))
+    if dfloat:
+        # a double-float assembly first, so the RHS also runs on the space's static geometry
+        fem.Matrix(g, dfloat=True).assemble(gf)
     b = torch.zeros(g.ndof, dtype=torch.float64, device='cuda')
     gv = {0: 0.7, 1: -0.4}
     fem.assemble_rhs(g, gf, fem.make_rhs(dt=0.2, src_qp=fq, mass=0.9, uprev=_t(up), bval={lab0: 2.5}, gval=gv,
