@@ -143,23 +143,25 @@ class Variable:
                 vals[sel] = scale * _at(v, X[sel], t)
         return consts, torch.as_tensor(vals, device='cuda')
 
-    def set_dirichlet(self, t: float):
-        """gfu.Set(g_D, definedon=Dirichlet boundaries) (base_model.py:321-341)."""
+    def set_dirichlet(self, t: float, u: Optional[torch.Tensor] = None):
+        """gfu.Set(g_D, definedon=Dirichlet boundaries) (base_model.py:321-341) on u (default: the
+        variable's solution)."""
         if self.kind != 'H1' or not self.dirichlet:
             return
+        u = self.u if u is None else u
         consts = {}
         for marker, v in self.dirichlet.items():
             c = _scalar_at(v, t)
             if c is not None:
                 consts[self.lab(marker)] = c
         if consts:
-            self.space.set_boundary(consts, self.u)
+            self.space.set_boundary(consts, u)
         for marker, v in self.dirichlet.items():
             if _scalar_at(v, t) is None:
                 lab = self.lab(marker)
                 if lab not in self._bpts:
                     self._bpts[lab] = self.space.boundary_points(1 << lab)
-                self.space.set_boundary_values(1 << lab, _at(v, self._bpts[lab], t), self.u)
+                self.space.set_boundary_values(1 << lab, _at(v, self._bpts[lab], t), u)
 
     def project(self, value, t: float = 0.0):
         """Initial condition: the L2 projection of `value` onto the space (exact for constants)."""
@@ -188,8 +190,8 @@ class Variable:
         fem.KrylovSolver(M, method='CG', tol=1e-13, maxit=20000).solve(b, x)
         self.u.copy_(x)
 
-    def solve(self):
-        return checked_solve(self.solver, self.b, self.u, self.accept)
+    def solve(self, x: Optional[torch.Tensor] = None):
+        return checked_solve(self.solver, self.b, self.u if x is None else x, self.accept)
 
     def source(self, t: float):
         """(constant, quadrature-point tensor) of the source; one of them is None."""

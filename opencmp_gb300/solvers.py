@@ -20,7 +20,10 @@ For MultiComponentINS with a fixed velocity OpenCMP's stationary driver takes th
 """
 from __future__ import annotations
 
+import math
+
 import numpy as np
+import torch
 
 from . import _lib as LB
 from . import fem
@@ -42,10 +45,15 @@ class Solver:
         self.t = 0.0
         self.infos = []
 
-    def _solve_var(self, v, theta: float, dt: float, t_new: float, t_old: float, transient: bool):
+    def _solve_var(self, v, theta: float, dt: float, t_new: float, t_old: float, transient: bool,
+                   u_from=None, u_to=None):
+        """One theta step of variable v from u_from (default v.u) into u_to (default v.u)."""
         m = self.model
-        uprev = v.u.clone() if transient else None
-        v.set_dirichlet(t_new)
+        u_to = v.u if u_to is None else u_to
+        uprev = (v.u if u_from is None else u_from).clone() if transient else None
+        if uprev is not None and u_to.data_ptr() != uprev.data_ptr():
+            u_to.copy_(uprev)
+        v.set_dirichlet(t_new, u_to)
         mass = 1.0 if transient else 0.0
         v.mat.assemble(m.form(v, mass, theta * dt, dt))
         v.solver.update()
@@ -61,7 +69,7 @@ class Solver:
             v.op.assemble(op_form)
             LB.call('ocmp_spmv_axpby', v.op.h, -(1.0 - theta) * dt, _ptr(uprev), 1.0, _ptr(v.b), _stream(None))
             del keep0
-        info = v.solve()
+        info = v.solve(u_to)
         del keep
         self.infos.append(info)
         return info
@@ -105,14 +113,101 @@ class TransientMultiStepSolver(Solver):
 
     def solve(self):
         """The time loop of base_solver.py:801-865: step until t reaches the end of the range
-        (np.isclose), printing the error metrics after every step when check_error is set."""
+        (np.isclose), the step shortened to land on the end time (base_solver.py:379-420), printing
+        the error metrics after every step when check_error is set."""
         t1 = self.t_range[1]
         while self.t < t1 and not np.isclose(self.t, t1):
             t_old = self.t
-            self.t = t_old + self.dt
-            self._step(self.theta, self.dt, self.t, t_old, True)
+            dt = min(self.dt, t1 - t_old)
+            self.t = t_old + dt
+            self._step(self.theta, dt, self.t, t_old, True)
             if self.check_error:
                 self.report()
+        return self.model.vars
+
+
+class AdaptiveSolver(TransientMultiStepSolver):
+    """Adaptive time stepping of opencmp/solvers/adaptive_transient_solvers: each attempt solves the
+    step twice, estimates the local error from the L2 difference of the two solutions and accepts
+    or repeats the step (base_adaptive_transient_multistep.py:41-143):
+
+      factor = clamp(sqrt((abs + rel |u|) / err), 0.3, 2), dt_new = min(0.9 dt factor, dt_max, t_end - t)
+
+    over the components; the step is accepted when every err <= abs + rel |u|.
+      two step   (adaptive_two_step.py): Crank-Nicolson predictor, implicit-Euler corrector (kept);
+      three step (adaptive_three_step.py): one implicit-Euler step of dt against two of dt/2 (kept);
+                 a rejected attempt repeats with dt/2 (base_adaptive_transient_RK.py)."""
+
+    def __init__(self, model_class, config):
+        Solver.__init__(self, model_class, config)
+        if hasattr(self.model, 'step'):
+            raise NotImplementedError('adaptive time stepping is not on the GPU path for this model')
+        self.scheme = config.get_item(['TRANSIENT', 'scheme'], str)
+        self.t_range = config.get_list(['TRANSIENT', 'time_range'], float)
+        self.dt = config.get_item(['TRANSIENT', 'dt'], float)
+        self.t = self.t_range[0]
+        tol = config.get_dict(['TRANSIENT', 'dt_tolerance'])
+        self.abs_tol, self.rel_tol = float(tol.get('absolute', 0.0)), float(tol['relative'])
+        self.dt_range = sorted(config.get_list(['TRANSIENT', 'dt_range'], float))
+        self.max_rejects = config.get_item(['TRANSIENT', 'maximum_rejected_solves'], int)
+        self._scratch = {}
+
+    def _buf(self, v, k):
+        key = (v.name, k)
+        if key not in self._scratch:
+            self._scratch[key] = torch.zeros_like(v.u)
+        return self._scratch[key]
+
+    def _attempt(self, dt, t_old):
+        """Both solutions of every variable for one attempt; returns {name: (kept, other)}."""
+        out = {}
+        t_new = t_old + dt
+        for v in self.model.vars.values():
+            if self.scheme == 'adaptive two step':
+                pred, corr = self._buf(v, 'a'), self._buf(v, 'b')
+                self._solve_var(v, 0.5, dt, t_new, t_old, True, u_from=v.u, u_to=pred)
+                self._solve_var(v, 1.0, dt, t_new, t_old, True, u_from=v.u, u_to=corr)
+                out[v.name] = (corr, pred)
+            else:
+                long_, half, short = self._buf(v, 'a'), self._buf(v, 'b'), self._buf(v, 'c')
+                self._solve_var(v, 1.0, dt, t_new, t_old, True, u_from=v.u, u_to=long_)
+                self._solve_var(v, 1.0, dt / 2, t_old + dt / 2, t_old, True, u_from=v.u, u_to=half)
+                self._solve_var(v, 1.0, dt / 2, t_new, t_old + dt / 2, True, u_from=half, u_to=short)
+                out[v.name] = (short, long_)
+        return out
+
+    def solve(self):
+        t1 = self.t_range[1]
+        rejects = 0
+        while self.t < t1 and not np.isclose(self.t, t1):
+            dt = min(self.dt, t1 - self.t)
+            sols = self._attempt(dt, self.t)
+            errs, norms = [], []
+            for name, (kept, other) in sols.items():
+                v = self.model.vars[name]
+                errs.append(v.space.l2_error(kept - other) or 1e-10)
+                norms.append(v.space.l2_error(kept) or 1e-10)
+            dt_err = min(dt * 0.9 * min(2.0, max(0.3, math.sqrt((self.abs_tol + self.rel_tol * nrm) / e)))
+                         for e, nrm in zip(errs, norms))
+            if dt_err < self.dt_range[0]:
+                raise RuntimeError('At t = {} further time steps must be smaller than the minimum time step ({}).'
+                                   .format(self.t, dt_err))
+            accept = all(e <= self.abs_tol + self.rel_tol * nrm for e, nrm in zip(errs, norms))
+            if accept:
+                for name, (kept, _) in sols.items():
+                    self.model.vars[name].u.copy_(kept)
+                self.t += dt
+                rest = t1 - self.t
+                self.dt = min(dt_err, self.dt_range[1], rest if rest > 0 else dt_err)
+                rejects = 0
+                if self.check_error:
+                    self.report()
+            else:
+                rejects += 1
+                if rejects > self.max_rejects:
+                    raise RuntimeError('At t = {} the maximum number of rejected time steps has been exceeded.'
+                                       .format(self.t))
+                self.dt = dt / 2 if self.scheme == 'adaptive three step' else min(dt_err, self.dt_range[1])
         return self.model.vars
 
 
@@ -124,6 +219,8 @@ def get_solver_class(config: ConfigParser):
         return StationarySolver
     if scheme in THETA or scheme in IMEX:
         return TransientMultiStepSolver
+    if scheme in ('adaptive two step', 'adaptive three step'):
+        return AdaptiveSolver
     if scheme in ('CNLF', 'SBDF') or 'adaptive' in scheme:
         raise NotImplementedError('time scheme {!r} is not on the GPU path'.format(scheme))
     raise TypeError('Have not implemented {} time integration yet.'.format(scheme))
