@@ -18,7 +18,8 @@ NVCC = os.environ.get('NVCC', '/usr/local/cuda/bin/nvcc' if os.path.exists('/usr
 CUDA_INC = os.path.join(os.path.dirname(os.path.dirname(os.path.realpath(NVCC))), 'include') \
     if os.path.isabs(NVCC) else '/usr/local/cuda/include'
 ARCH = ['-gencode', 'arch=compute_103a,code=sm_103a']
-CU_FLAGS = ARCH + ['-O3', '-lineinfo', '-std=c++17', '-Xcompiler', '-fPIC', '--expt-relaxed-constexpr']
+CU_FLAGS = ARCH + ['-O3', '-lineinfo', '-std=c++17', '-Xcompiler', '-fPIC', '--expt-relaxed-constexpr',
+                   '-I' + os.path.join(os.path.dirname(os.path.abspath(__file__)), '_build')]
 CXX_FLAGS = ['-O2', '-std=c++17', '-fPIC', '-I' + CUDA_INC]
 
 
@@ -32,11 +33,40 @@ def _newer(out, deps):
     return os.path.exists(out) and all(os.path.getmtime(out) >= os.path.getmtime(d) for d in deps)
 
 
+GEN_HEADER = os.path.join(BUILD, 'ocmp_terms_gen.h')
+
+
+def _generate_terms(verbose: bool):
+    """Compile and run the term-table generator (ocmp_host.cpp, OCMP_TERM_GENERATOR), which writes
+    the straight-line element-matrix code the double-float kernel includes."""
+    src = os.path.join(CSRC, 'ocmp_host.cpp')
+    deps = [src, os.path.join(CSRC, 'ocmp_internal.h')]
+    if _newer(GEN_HEADER, deps):
+        return
+    exe = os.path.join(BUILD, 'ocmp_termgen')
+    # only the table builders run; the kernel launchers the TU references are never called
+    cmd = [NVCC, '-std=c++17', '-O1', '-DOCMP_TERM_GENERATOR', '-x', 'c++', src, '-o', exe,
+           '-Xlinker', '--unresolved-symbols=ignore-all']
+    if verbose:
+        print(' '.join(cmd), flush=True)
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError('term generator build failed:\n{}{}'.format(r.stdout, r.stderr))
+    r = subprocess.run([exe, GEN_HEADER + '.tmp'], capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError('term generator failed ({}): {}'.format(r.returncode, r.stderr))
+    os.replace(GEN_HEADER + '.tmp', GEN_HEADER)
+
+
 def build(force: bool = False, verbose: bool = False) -> str:
     os.makedirs(BUILD, exist_ok=True)
+    if force and os.path.exists(GEN_HEADER):
+        os.remove(GEN_HEADER)
+    _generate_terms(verbose)
     cu, cpp = sources()
     headers = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith(('.h', '.cuh'))]
     headers.append(os.path.join(HERE, '..', 'include', 'opencmp_gpu.h'))
+    headers.append(GEN_HEADER)
     jobs, objs = [], []
     for f in cu + cpp:
         src = os.path.join(CSRC, f)

@@ -568,6 +568,74 @@ __device__ __forceinline__ float2 ff_prod(float2 a, float2 b) {
     return make_float2(s, __fsub_rn(pl, __fsub_rn(s, ph)));
 }
 
+// Straight-line element matrices: the term tables of the H1 element types, written out at build
+// time as device code (ocmp_terms_gen.h, from ocmp_host.cpp's generator). Each product is
+// gterm(acc, F[g], coefficient) with g and the coefficient compile-time constants, so the factors
+// stay in registers; the sums are the same double-float operations in the same order as
+// elem_matrix_ff_kernel, entry (j, i) written with (i, j) as the term tables pair them.
+template <int D, int L, int VAR>
+struct GenTerms {
+    static constexpr bool value = false;
+    static constexpr int NG = 1;
+    static __device__ __forceinline__ void run(const float2 (&)[1], float2*) {}
+};
+__device__ __forceinline__ void gterm(float& sh, float& sl, float2 f, float ch, float cl) {
+    float ph, pl;
+    ff_mul(f.x, f.y, ch, cl, ph, pl);
+    ff_add(sh, sl, ph, pl);
+}
+#include "ocmp_terms_gen.h"
+
+template <int D, int L, int VAR>
+__global__ void __launch_bounds__(128) elem_gen_ff_kernel(int64_t ne, const float2* __restrict__ geo,
+                                                          const int32_t* __restrict__ conn, FormArgs a,
+                                                          float2* __restrict__ K) {
+    using GT = GenTerms<D, L, VAR>;
+    constexpr int NP = D + 1, NS = NP * (NP + 1) / 2, LL = L * L;
+    const int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (e >= ne) return;
+    float2 F[GT::NG];
+#pragma unroll
+    for (int g = 0; g < GT::NG; g++) F[g] = make_float2(0.f, 0.f);
+    const float2 cm = ff_split(a.mass), cs = ff_split(a.dt * a.diff), cw = ff_split(-a.dt);
+    F[0] = ff_prod(cm, __ldg(geo + e));
+#pragma unroll
+    for (int pi = 0; pi < NS; pi++) F[1 + pi] = ff_prod(cs, __ldg(geo + (1 + pi) * ne + e));
+    const float2* __restrict__ ggl = geo + (1 + NS) * ne + e;
+    if (VAR == 0 && a.wind_kind == OCMP_WIND_CONST) {
+        const float2 w[3] = {ff_split(a.w0), ff_split(a.w1), ff_split(a.w2)};
+#pragma unroll
+        for (int p = 0; p < NP; p++) {
+            float th = 0.f, tl = 0.f;
+#pragma unroll
+            for (int r = 0; r < D; r++) {
+                const float2 m = ff_prod(w[r], __ldg(ggl + (p * D + r) * ne));
+                ff_add(th, tl, m.x, m.y);
+            }
+            F[1 + NS + p] = ff_prod(cw, make_float2(th, tl));
+        }
+    } else if (VAR == 1 && a.wind_kind == OCMP_WIND_VERTEX) {
+#pragma unroll
+        for (int v = 0; v < NP; v++) {
+            const int32_t gv = conn[e * NP + v];
+            float2 w[3];
+#pragma unroll
+            for (int r = 0; r < D; r++) w[r] = ff_split(a.wind_vtx[(int64_t)gv * D + r]);
+#pragma unroll
+            for (int p = 0; p < NP; p++) {
+                float th = 0.f, tl = 0.f;
+#pragma unroll
+                for (int r = 0; r < D; r++) {
+                    const float2 m = ff_prod(w[r], __ldg(ggl + (p * D + r) * ne));
+                    ff_add(th, tl, m.x, m.y);
+                }
+                F[1 + NS + p * NP + v] = ff_prod(cw, make_float2(th, tl));
+            }
+        }
+    }
+    GT::run(F, K + e * LL);
+}
+
 template <int D, int L>
 __global__ void __launch_bounds__(256) elem_matrix_ff_kernel(int64_t ne, const float2* __restrict__ geo,
                                                              const int32_t* __restrict__ conn, FormArgs a,
@@ -774,12 +842,12 @@ __global__ void __launch_bounds__(128) row_scatter_ff_kernel(
     }
 }
 
-// Warp-per-row gather for element-only assembly (no facet terms). The row's accumulator sits in a
-// per-warp shared-memory stripe; lanes are split into G = 32 / L groups, each loading one incidence's
-// row slice (L values, coalesced) and slot bytes, so G slices are in flight per round. The adds run
-// group after group, i.e. in incidence order, so every entry is summed in the same order as the
-// thread-per-row kernel and the values are bit-identical to it. The row is then written with
-// consecutive lanes on consecutive entries. AccT: double (FP64 path) or float2 (double-float path).
+// Warp-per-row gather for element-only assembly (no facet terms). Lanes are split into G = 32 / L
+// groups; group g takes incidences k0 + g, k0 + g + G, ... of the row, loading each one's row slice
+// (L values, coalesced) and slot bytes, and adds them into its own accumulator stripe in shared
+// memory (a slice's slots are distinct, so the lanes of a group never collide). The G stripes are
+// then summed in group order and the row written with consecutive lanes on consecutive entries.
+// The summation order is fixed by the incidence list, so the values are deterministic.
 template <int L, bool FF>
 __global__ void __launch_bounds__(256) row_gather_warp_kernel(
     int64_t r0, int64_t r1, const int32_t* __restrict__ rp, const int32_t* __restrict__ col,
@@ -792,15 +860,15 @@ __global__ void __launch_bounds__(256) row_gather_warp_kernel(
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     const int g = lane / L, j = lane % L;
     const bool act = g < G;
-    double* __restrict__ acc = wacc + (size_t)w * stripe;
+    double* __restrict__ base_acc = wacc + (size_t)w * stripe * G;
+    double* __restrict__ acc = base_acc + (size_t)(act ? g : 0) * stripe;
     float2* __restrict__ acc2 = reinterpret_cast<float2*>(acc);
     const int64_t wpb = blockDim.x >> 5;
     for (int64_t r = r0 + blockIdx.x * wpb + w; r < r1; r += (int64_t)gridDim.x * wpb) {
         const int32_t base = rp[r], rn = rp[r + 1] - base;
-        for (int q = lane; q < rn; q += 32) acc[q] = 0.0;
+        for (int q = lane; q < rn * G; q += 32) base_acc[(q / rn) * stripe + q % rn] = 0.0;
         __syncwarp();
         const int32_t k0 = inc_ptr[r], k1 = inc_ptr[r + 1];
-        // round k: incidences kb .. kb + G - 1; the next round's loads are issued before the adds
         double v = 0.0;
         int sl = 0;
         bool have = act && k0 + g < k1;
@@ -811,6 +879,7 @@ __global__ void __launch_bounds__(256) row_gather_warp_kernel(
             sl = __ldg(slot + flat * ss + j);
         }
         for (int32_t kb = k0; kb < k1; kb += G) {
+            // issue the next round's loads before this round's adds
             double vn = 0.0;
             int sln = 0;
             const bool hn = act && kb + G + g < k1;
@@ -820,28 +889,30 @@ __global__ void __launch_bounds__(256) row_gather_warp_kernel(
                         : __ldg(reinterpret_cast<const double*>(Kv) + flat * L + j);
                 sln = __ldg(slot + flat * ss + j);
             }
-#pragma unroll
-            for (int gg = 0; gg < G; gg++) {
-                if (have && g == gg) {
-                    if (FF) {
-                        const long long bits = __double_as_longlong(v);
-                        const float vh = __int_as_float((int)(bits & 0xffffffffll)), vl = __int_as_float((int)(bits >> 32));
-                        float2 a2 = acc2[sl];
-                        ff_add(a2.x, a2.y, vh, vl);
-                        acc2[sl] = a2;
-                    } else {
-                        acc[sl] += v;
-                    }
+            if (have) {
+                if (FF) {
+                    const long long bits = __double_as_longlong(v);
+                    const float vh = __int_as_float((int)(bits & 0xffffffffll)), vl = __int_as_float((int)(bits >> 32));
+                    float2 a2 = acc2[sl];
+                    ff_add(a2.x, a2.y, vh, vl);
+                    acc2[sl] = a2;
+                } else {
+                    acc[sl] += v;
                 }
-                __syncwarp();
             }
             v = vn;
             sl = sln;
             have = hn;
         }
+        __syncwarp();
         for (int q = lane; q < rn; q += 32) {
             if (FF) {
-                const float2 a2 = acc2[q];
+                float2 a2 = reinterpret_cast<const float2*>(base_acc)[q];
+#pragma unroll
+                for (int gg = 1; gg < G; gg++) {
+                    const float2 b2 = reinterpret_cast<const float2*>(base_acc + (size_t)gg * stripe)[q];
+                    ff_add(a2.x, a2.y, b2.x, b2.y);
+                }
                 const double vv = ff_to_double(a2.x, a2.y);
                 vals[base + q] = vv;
                 const float v32 = __fadd_rn(a2.x, a2.y);
@@ -849,7 +920,9 @@ __global__ void __launch_bounds__(256) row_gather_warp_kernel(
                 if (svals64) svals64[base + q] = vv * dinv[col[base + q]];
                 if (svals32) svals32[base + q] = v32 * dinv32[col[base + q]];
             } else {
-                const double vv = acc[q];
+                double vv = base_acc[q];
+#pragma unroll
+                for (int gg = 1; gg < G; gg++) vv += base_acc[(size_t)gg * stripe + q];
                 vals[base + q] = vv;
                 if (vals32) vals32[base + q] = (float)vv;
                 if (svals64 || svals32) {
@@ -1103,9 +1176,22 @@ int assemble_impl(ocmp_matrix_s* m, const ocmp_form_t* f, cudaStream_t st) {
             OCMP_CUDA(cudaMalloc((void**)&s->d_geo_ff, sizeof(float2) * (size_t)NGEO * ne));
             OCMP_LAUNCH(geo_ff_kernel<D><<<nblk(ne, 128), 128, 0, st>>>(ne, mesh->dX, mesh->dconn, s->d_geo_ff));
         }
-        OCMP_LAUNCH(elem_matrix_ff_kernel<D, L><<<nblk(ne, ntf), ntf, smf, st>>>(ne, s->d_geo_ff, mesh->dconn, a,
-                                                                    s->d_slot_off[var], s->d_term_g[var],
-                                                                    s->d_term_coef_ff[var], Kff));
+        bool done = false;
+        if constexpr (GenTerms<D, L, 0>::value && GenTerms<D, L, 1>::value) {
+            if (s->kind == OCMP_H1) {
+                if (var == 0)
+                    OCMP_LAUNCH(elem_gen_ff_kernel<D, L, 0><<<nblk(ne, 128), 128, 0, st>>>(ne, s->d_geo_ff, mesh->dconn, a,
+                                                                                           Kff));
+                else
+                    OCMP_LAUNCH(elem_gen_ff_kernel<D, L, 1><<<nblk(ne, 128), 128, 0, st>>>(ne, s->d_geo_ff, mesh->dconn, a,
+                                                                                           Kff));
+                done = true;
+            }
+        }
+        if (!done)
+            OCMP_LAUNCH(elem_matrix_ff_kernel<D, L><<<nblk(ne, ntf), ntf, smf, st>>>(ne, s->d_geo_ff, mesh->dconn, a,
+                                                                        s->d_slot_off[var], s->d_term_g[var],
+                                                                        s->d_term_coef_ff[var], Kff));
     } else {
         OCMP_LAUNCH(elem_matrix_kernel<D, L><<<nblk(ne, nt), nt, smem, st>>>(ne, mesh->dX, mesh->dconn, a, tt, s->d_K));
     }
@@ -1141,7 +1227,8 @@ int assemble_impl(ocmp_matrix_s* m, const ocmp_form_t* f, cudaStream_t st) {
         // element-only assembly: one warp per row (row_gather_warp_kernel)
         const int wt = 256, wpb = wt / 32;
         const int stripe = s->maxrow;
-        const size_t wsm = sizeof(double) * (size_t)stripe * wpb;
+        const int G = 32 / L > 0 ? 32 / L : 1;
+        const size_t wsm = sizeof(double) * (size_t)stripe * G * wpb;
         auto kern = dfl ? row_gather_warp_kernel<L, true> : row_gather_warp_kernel<L, false>;
         OCMP_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)wsm));
         int dev = 0, sms = 152, per = 0;

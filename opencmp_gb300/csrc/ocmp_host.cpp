@@ -1241,3 +1241,66 @@ int ocmp_spmv_axpby(ocmp_matrix_t m, double alpha, const double* x, double beta,
 }
 
 }  // extern "C"
+
+#ifdef OCMP_TERM_GENERATOR
+// Build-time generator (opencmp_gb300/build.py): writes, for the H1 element types of the
+// double-float path, the element-matrix term tables of build_terms as straight-line device code,
+// one function per (dimension, local size, wind variant). With every factor index and coefficient
+// a compile-time constant, the factors live in registers and the products need no table loads.
+#include <cstdio>
+
+int main(int argc, char** argv) {
+    if (argc < 2) return 1;
+    FILE* o = std::fopen(argv[1], "w");
+    if (!o) return 2;
+    std::fprintf(o, "// Generated by ocmp_host.cpp (OCMP_TERM_GENERATOR) at build time; do not edit.\n#pragma once\n\n");
+    const int cases[][2] = {{2, 1}, {2, 2}, {2, 3}, {3, 1}, {3, 2}};
+    for (const auto& cs : cases) {
+        const int D = cs[0], p = cs[1];
+        ocmp_tables T;
+        ocmp::build_tables(OCMP_H1, D, p, T);
+        ocmp::build_terms(OCMP_H1, D, p, T);
+        const int L = T.nloc, NP = D + 1, NS = NP * (NP + 1) / 2;
+        for (int var = 0; var < 2; var++) {
+            const int NG = 1 + NS + (var ? NP * NP : NP);
+            std::fprintf(o, "template <> struct GenTerms<%d, %d, %d> {\n    static constexpr bool value = true;\n"
+                            "    static constexpr int NG = %d;\n"
+                            "    static __device__ __forceinline__ void run(const float2 (&F)[%d], float2* __restrict__ Ke) {\n",
+                         D, L, var, NG, NG);
+            const auto& off = T.slot_off[var];
+            const auto& tg = T.term_g[var];
+            const auto& tc = T.term_coef[var];
+            auto emit = [&](const char* acc, int a, int b) {
+                for (int t = a; t < b; t++) {
+                    const double c = tc[t];
+                    const float hi = (float)c, lo = (float)(c - (double)hi);
+                    uint32_t hb, lb;
+                    std::memcpy(&hb, &hi, 4);
+                    std::memcpy(&lb, &lo, 4);
+                    std::fprintf(o, "        gterm(%sh, %sl, F[%d], __uint_as_float(0x%08xu), __uint_as_float(0x%08xu));\n", acc,
+                                 acc, (int)tg[t], hb, lb);
+                }
+            };
+            int slot = 0;
+            for (int i = 0; i < L; i++)
+                for (int j = i; j < L; j++, slot++) {
+                    const int o0 = off[4 * slot], o2 = off[4 * slot + 2], o3 = off[4 * slot + 3], o4 = off[4 * slot + 4];
+                    std::fprintf(o, "        {\n        float sh = 0.f, sl = 0.f;\n");
+                    emit("s", o0, o2);
+                    std::fprintf(o, "        float ah = sh, al = sl;\n");
+                    emit("a", o2, o3);
+                    std::fprintf(o, "        Ke[%d] = make_float2(ah, al);\n", i * L + j);
+                    if (j != i) {
+                        std::fprintf(o, "        float bh = sh, bl = sl;\n");
+                        emit("b", o3, o4);
+                        std::fprintf(o, "        Ke[%d] = make_float2(bh, bl);\n", j * L + i);
+                    }
+                    std::fprintf(o, "        }\n");
+                }
+            std::fprintf(o, "    }\n};\n\n");
+        }
+    }
+    std::fclose(o);
+    return 0;
+}
+#endif
