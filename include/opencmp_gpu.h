@@ -245,6 +245,8 @@ typedef struct {
     double dt;             /* factor of the viscous, convection and pressure terms               */
     double eps_p;          /* pressure regularisation  -dt eps_p (p, q)  (OpenCMP: 1e-10)        */
     const double* wind;    /* device: Oseen wind as a compound vector (velocity part read), or NULL */
+    double tcoef;          /* factor of the time-coefficient terms (div u q, div v p, eps_p p q) in
+                              place of dt: OpenCMP's CNLF doubles them (time_integration_schemes.py) */
 } ocmp_th_form_t;
 typedef struct {
     double dt;
@@ -252,7 +254,9 @@ typedef struct {
     const double* src_qp;  /* device, ne*nq*2: body force at ocmp_th_quad_points, or NULL        */
     double mass;           /* coefficient of (u_prev, v)                                         */
     const double* uprev;   /* device compound vector, or NULL                                    */
-    const double* imex;    /* device compound vector u^n: adds -dt ((grad u^n) u^n, v), or NULL  */
+    const double* imex;    /* device compound vector w: adds -imex_coef dt ((grad w) w, v), or NULL */
+    double imex_coef;      /* factor of the explicit convection term                              */
+    int32_t accumulate;    /* nonzero: b += L(v) instead of b = L(v)                            */
 } ocmp_th_rhs_t;
 int ocmp_th_create(ocmp_mesh_t mesh, int32_t order_u, uint32_t dirichlet_mask_u, ocmp_th_t* out);
 int ocmp_th_destroy(ocmp_th_t th);

@@ -45,12 +45,12 @@ class Rhs(C.Structure):
 
 class THForm(C.Structure):
     _fields_ = [('mass', C.c_double), ('nu', C.c_double), ('dt', C.c_double), ('eps_p', C.c_double),
-                ('wind', C.c_void_p)]
+                ('wind', C.c_void_p), ('tcoef', C.c_double)]
 
 
 class THRhs(C.Structure):
     _fields_ = [('dt', C.c_double), ('src', C.c_double * 2), ('src_qp', C.c_void_p), ('mass', C.c_double),
-                ('uprev', C.c_void_p), ('imex', C.c_void_p)]
+                ('uprev', C.c_void_p), ('imex', C.c_void_p), ('imex_coef', C.c_double), ('accumulate', C.c_int32)]
 
 
 class SpaceInfo(C.Structure):

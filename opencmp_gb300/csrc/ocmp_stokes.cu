@@ -62,7 +62,7 @@ template <int LU, int LP, int NQ>
 __global__ void __launch_bounds__(128) th_elem_kernel(int64_t ne, const double* __restrict__ X,
                                                       const int32_t* __restrict__ conn,
                                                       const int32_t* __restrict__ vdofs, ThTabs t, double mass,
-                                                      double nu, double dt, double eps_p,
+                                                      double nu, double dt, double tcoef, double eps_p,
                                                       const double* __restrict__ wind, int64_t nu_dofs,
                                                       double* __restrict__ Ke) {
     const int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
@@ -113,15 +113,16 @@ __global__ void __launch_bounds__(128) th_elem_kernel(int64_t ne, const double* 
         }
         Ke[ij * ne + e] = v;
     }
-    // B_c(i, j) = -dt |det| sum_d Ji[d][c] T_d(i, j)
+    // B_c(i, j) = -tcoef |det| sum_d Ji[d][c] T_d(i, j)
+    const double sb = -tcoef * g.adet;
 #pragma unroll 1
     for (int c = 0; c < 2; c++)
 #pragma unroll 1
         for (int ij = 0; ij < LP * LU; ij++) {
-            const double v = sc * (g.Ji[0][c] * __ldg(t.T + ij) + g.Ji[1][c] * __ldg(t.T + LP * LU + ij));
+            const double v = sb * (g.Ji[0][c] * __ldg(t.T + ij) + g.Ji[1][c] * __ldg(t.T + LP * LU + ij));
             Ke[(LU * LU + c * LP * LU + ij) * ne + e] = v;
         }
-    const double sp = -dt * eps_p * g.adet;
+    const double sp = -tcoef * eps_p * g.adet;
 #pragma unroll 1
     for (int ij = 0; ij < LP * LP; ij++) Ke[(LU * LU + 2 * LP * LU + ij) * ne + e] = sp * __ldg(t.Mp + ij);
 }
@@ -143,8 +144,8 @@ __global__ void __launch_bounds__(128) th_rhs_kernel(int64_t ne, const double* _
                                                      const int32_t* __restrict__ vdofs, ThTabs t, double dt,
                                                      double f0, double f1, const double* __restrict__ fq,
                                                      double mass, const double* __restrict__ uprev,
-                                                     const double* __restrict__ imex, int64_t nu_dofs,
-                                                     double* __restrict__ Fe) {
+                                                     const double* __restrict__ imex, double imex_coef,
+                                                     int64_t nu_dofs, double* __restrict__ Fe) {
     const int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (e >= ne) return;
     ThGeo g;
@@ -195,7 +196,7 @@ __global__ void __launch_bounds__(128) th_rhs_kernel(int64_t ne, const double* _
                 double s = 0;
 #pragma unroll
                 for (int r = 0; r < 2; r++) s += (gr[c][0] * g.Ji[0][r] + gr[c][1] * g.Ji[1][r]) * u[r];
-                val[c] -= dt * s;
+                val[c] -= imex_coef * dt * s;
             }
         }
         const double w = __ldg(t.qw + q) * g.adet;
@@ -215,11 +216,11 @@ __global__ void __launch_bounds__(128) th_rhs_kernel(int64_t ne, const double* _
 
 __global__ void th_rhs_gather_kernel(int64_t nu_dofs, int64_t ndof, int64_t ne_lu, const int32_t* __restrict__ inc_ptr,
                                      const int32_t* __restrict__ inc, const double* __restrict__ Fe,
-                                     double* __restrict__ b) {
+                                     double* __restrict__ b, int accumulate) {
     const int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (r >= ndof) return;
     if (r >= 2 * nu_dofs) {
-        b[r] = 0.0;
+        if (!accumulate) b[r] = 0.0;
         return;
     }
     const int c = r >= nu_dofs ? 1 : 0;
@@ -227,7 +228,7 @@ __global__ void th_rhs_gather_kernel(int64_t nu_dofs, int64_t ndof, int64_t ne_l
     const double* F = Fe + c * ne_lu;
     double acc = 0;
     for (int k = inc_ptr[d]; k < inc_ptr[d + 1]; k++) acc += F[inc[k]];
-    b[r] = acc;
+    b[r] = accumulate ? b[r] + acc : acc;
 }
 
 // Inverse block-diagonal preconditioner: velocity rows 1/a_ii; pressure rows
@@ -510,7 +511,7 @@ template <int LU, int LP, int NQ>
 int th_assemble_impl(ocmp_th_s* th, ocmp_matrix_s* mat, const ocmp_th_form_t* f, cudaStream_t st) {
     const int64_t ne = th->mesh->ne;
     OCMP_LAUNCH(th_elem_kernel<LU, LP, NQ><<<nblk_s(ne, 128), 128, 0, st>>>(ne, th->mesh->dX, th->mesh->dconn, th->V->d_dofs,
-                                                               th->tabs, f->mass, f->nu, f->dt, f->eps_p, f->wind,
+                                                               th->tabs, f->mass, f->nu, f->dt, f->tcoef, f->eps_p, f->wind,
                                                                th->nu, th->d_Ke));
     OCMP_LAUNCH(th_gather_kernel<<<nblk_s(th->C->nnz, 256), 256, 0, st>>>(th->C->nnz, th->d_seg, th->d_src, th->d_Ke, mat->vals));
     OCMP_CUDA(cudaGetLastError());
@@ -522,9 +523,9 @@ int th_rhs_impl(ocmp_th_s* th, const ocmp_th_rhs_t* r, double* b, cudaStream_t s
     const int64_t ne = th->mesh->ne;
     OCMP_LAUNCH(th_rhs_kernel<LU, NQ><<<nblk_s(ne, 128), 128, 0, st>>>(ne, th->mesh->dX, th->mesh->dconn, th->V->d_dofs, th->tabs,
                                                           r->dt, r->src[0], r->src[1], r->src_qp, r->mass, r->uprev,
-                                                          r->imex, th->nu, th->d_Fe));
+                                                          r->imex, r->imex_coef, th->nu, th->d_Fe));
     OCMP_LAUNCH(th_rhs_gather_kernel<<<nblk_s(th->C->ndof, 256), 256, 0, st>>>(th->nu, th->C->ndof, ne * LU, th->V->d_inc_ptr,
-                                                                  th->V->d_inc, th->d_Fe, b));
+                                                                  th->V->d_inc, th->d_Fe, b, r->accumulate));
     OCMP_CUDA(cudaGetLastError());
     return OCMP_OK;
 }

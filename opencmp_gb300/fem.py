@@ -409,14 +409,18 @@ class TaylorHood:
         return Matrix(self.C)
 
     def assemble(self, mat: 'Matrix', mass=0.0, nu=1.0, dt=1.0, eps_p=1e-10, wind: Optional[torch.Tensor] = None,
-                 stream=None):
-        f = LB.THForm(mass, nu, dt, eps_p, wind.data_ptr() if wind is not None else None)
+                 tcoef: Optional[float] = None, stream=None):
+        """tcoef: factor of the divergence / pressure terms (default dt)."""
+        f = LB.THForm(mass, nu, dt, eps_p, wind.data_ptr() if wind is not None else None,
+                      dt if tcoef is None else tcoef)
         LB.call('ocmp_th_assemble', self.h, mat.h, C.byref(f), _stream(stream))
 
     def assemble_rhs(self, b: torch.Tensor, dt=1.0, src=(0.0, 0.0), src_qp: Optional[torch.Tensor] = None, mass=0.0,
-                     uprev: Optional[torch.Tensor] = None, imex: Optional[torch.Tensor] = None, stream=None):
+                     uprev: Optional[torch.Tensor] = None, imex: Optional[torch.Tensor] = None, imex_coef=1.0,
+                     accumulate=False, stream=None):
         r = LB.THRhs()
         r.dt, r.mass = dt, mass
+        r.imex_coef, r.accumulate = imex_coef, int(accumulate)
         r.src[0], r.src[1] = src
         r.src_qp = src_qp.data_ptr() if src_qp is not None else None
         r.uprev = uprev.data_ptr() if uprev is not None else None

@@ -417,6 +417,10 @@ class INS(Model):
             if self.bc.get(kind, {}).get('u'):
                 raise NotImplementedError('{} boundary conditions for INS are not on the GPU path'.format(kind))
         self.dirichlet = self.bc.get('dirichlet', {}).get('u', {})
+        self.scheme = config.get_item(['TRANSIENT', 'scheme'], str) if config.get_item(['TRANSIENT', 'transient'], bool) \
+            else 'stationary'
+        if self.scheme in ('CNLF', 'SBDF') and self.linearize != 'IMEX':
+            raise NotImplementedError('{} needs the IMEX linearisation'.format(self.scheme))
 
     def setup(self):
         k = self.interp_ord
@@ -438,6 +442,10 @@ class INS(Model):
         ic_p = self.ic.get('p', {}).get('all')
         self._project(ic_u, ic_p)
         self.W.copy_(self.u)
+        # previous solutions, most recent first (all the initial condition at the start, as OpenCMP's
+        # gfu_0_list); the multistep IMEX schemes read them
+        self.hist = [self.u.clone() for _ in range(3)]
+        self.Kv = None
         self.vars = {}
 
     def quad_points(self):
@@ -489,20 +497,64 @@ class INS(Model):
         return checked_solve(self.solver, self.b, self.u, 1e-9 if self.solver_params['tol'] <= 1e-12 else
                              self.solver_params['tol'])
 
+    def _push(self):
+        self.hist = [self.u.clone()] + self.hist[:-1]
+
+    def startup_step(self, dt, t_new, infos):
+        """A start-up step of the multistep schemes (transient_multistep.py:51-100): implicit Euler
+        with the IMEX linearisation (no convection term) and a tiny dt."""
+        th = self.th
+        uprev = self.u.clone()
+        f, fq = self.source(t_new)
+        self.set_dirichlet(t_new)
+        th.assemble(self.A, mass=1.0, nu=self.kv, dt=dt)
+        th.assemble_rhs(self.b, dt=dt, src=f, src_qp=fq, mass=1.0, uprev=uprev)
+        infos.append(self._solve())
+        self._push()
+
     def step(self, theta, dt, t_new, t_old, transient, infos):
-        """One time step (implicit Euler with Oseen Picard iterations, or Euler IMEX); the
-        stationary solve when not transient."""
+        """One time step: implicit Euler with Oseen Picard iterations, or one of the IMEX schemes
+        (Euler IMEX, CNLF, SBDF of time_integration_schemes.py); the stationary solve when not
+        transient."""
         if theta != 1.0:
-            raise NotImplementedError('INS runs on the GPU path with implicit Euler or Euler IMEX')
+            raise NotImplementedError('INS runs on the GPU path with implicit Euler, Euler IMEX, CNLF or SBDF')
         th = self.th
         uprev = self.u.clone() if transient else None
         mass = 1.0 if transient else 0.0
         f, fq = self.source(t_new)
+        if self.linearize == 'IMEX' and self.scheme == 'CNLF':
+            # (2 coef + ODE + M) u = M u^{n-1} + L(t^{n-1}) - ODE(u^{n-1}) + 2 N(u^n)
+            u1 = self.hist[1]
+            f0, fq0 = self.source(t_old)
+            self.set_dirichlet(t_new)
+            th.assemble(self.A, mass=1.0, nu=self.kv, dt=dt, tcoef=2.0 * dt)
+            th.assemble_rhs(self.b, dt=dt, src=f0, src_qp=fq0, mass=1.0, uprev=u1, imex=uprev, imex_coef=2.0)
+            if self.Kv is None:
+                self.Kv = th.matrix()
+            th.assemble(self.Kv, mass=0.0, nu=self.kv, dt=dt, tcoef=0.0)
+            LB.call('ocmp_spmv_axpby', self.Kv.h, -1.0, fem._ptr(u1), 1.0, fem._ptr(self.b), None)
+            infos.append(self._solve())
+            self._push()
+            return
+        if self.linearize == 'IMEX' and self.scheme == 'SBDF':
+            # (coef + ODE + 11/6 M) u = L(t^{n+1}) + M (3 u^n - 3/2 u^{n-1} + 1/3 u^{n-2})
+            #                            + 3 N(u^n) - 3 N(u^{n-1}) + N(u^{n-2})
+            u1, u2 = self.hist[1], self.hist[2]
+            comb = 3.0 * uprev - 1.5 * u1 + u2 / 3.0
+            self.set_dirichlet(t_new)
+            th.assemble(self.A, mass=11.0 / 6.0, nu=self.kv, dt=dt)
+            th.assemble_rhs(self.b, dt=dt, src=f, src_qp=fq, mass=1.0, uprev=comb, imex=uprev, imex_coef=3.0)
+            th.assemble_rhs(self.b, dt=dt, imex=u1, imex_coef=-3.0, accumulate=True)
+            th.assemble_rhs(self.b, dt=dt, imex=u2, imex_coef=1.0, accumulate=True)
+            infos.append(self._solve())
+            self._push()
+            return
         if self.linearize == 'IMEX':
             self.set_dirichlet(t_new)
             th.assemble(self.A, mass=mass, nu=self.kv, dt=dt)
             th.assemble_rhs(self.b, dt=dt, src=f, src_qp=fq, mass=mass, uprev=uprev, imex=uprev)
             infos.append(self._solve())
+            self._push()
             return
         area = float(self.mesh_area())
         for it in range(self.max_picard):
@@ -516,6 +568,7 @@ class INS(Model):
             self.W.copy_(self.u)
             if err < self.abs_tol + self.rel_tol * unorm / math.sqrt(area):
                 break
+        self._push()
 
     def mesh_area(self):
         X = self.mesh.coords[self.mesh.elements]

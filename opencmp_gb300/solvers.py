@@ -31,8 +31,9 @@ from .config import ConfigParser
 from .fem import _ptr, _stream
 
 THETA = {'explicit euler': 0.0, 'crank nicolson': 0.5, 'implicit euler': 1.0}
-# schemes whose implicit part is implicit Euler and whose explicit part the model supplies
-IMEX = {'euler IMEX': 1.0}
+# schemes whose implicit part the model builds itself, with the explicit (IMEX) part; the value is
+# the number of previous solutions the scheme reads (base_solver.py:44-55)
+IMEX = {'euler IMEX': 1, 'CNLF': 2, 'SBDF': 3}
 
 
 class Solver:
@@ -106,10 +107,20 @@ class TransientMultiStepSolver(Solver):
         if self.scheme not in THETA and self.scheme not in IMEX:
             raise NotImplementedError('time scheme {!r} is not on the GPU path (one of {})'.format(
                 self.scheme, sorted(THETA) + sorted(IMEX)))
-        self.theta = THETA.get(self.scheme, IMEX.get(self.scheme))
+        self.theta = THETA.get(self.scheme, 1.0)
         self.t_range = config.get_list(['TRANSIENT', 'time_range'], float)
         self.dt = config.get_item(['TRANSIENT', 'dt'], float)
         self.t = self.t_range[0]
+        self._next_dt = None
+        order = IMEX.get(self.scheme, 1)
+        if order > 1:
+            # start-up (transient_multistep.py:51-100): order - 1 implicit-Euler steps of dt = 1e-10;
+            # the first step of the scheme itself also takes 1e-10 (its dt is reset after the step)
+            for _ in range(order - 1):
+                t_old = self.t
+                self.t = t_old + 1e-10
+                self.model.startup_step(1e-10, self.t, self.infos)
+            self._next_dt = 1e-10
 
     def solve(self):
         """The time loop of base_solver.py:801-865: step until t reaches the end of the range
@@ -118,7 +129,8 @@ class TransientMultiStepSolver(Solver):
         t1 = self.t_range[1]
         while self.t < t1 and not np.isclose(self.t, t1):
             t_old = self.t
-            dt = min(self.dt, t1 - t_old)
+            dt = min(self.dt if self._next_dt is None else self._next_dt, t1 - t_old)
+            self._next_dt = None
             self.t = t_old + dt
             self._step(self.theta, dt, self.t, t_old, True)
             if self.check_error:
@@ -221,6 +233,6 @@ def get_solver_class(config: ConfigParser):
         return TransientMultiStepSolver
     if scheme in ('adaptive two step', 'adaptive three step'):
         return AdaptiveSolver
-    if scheme in ('CNLF', 'SBDF') or 'adaptive' in scheme:
+    if 'adaptive' in scheme or scheme in ('RK 222', 'RK 232'):
         raise NotImplementedError('time scheme {!r} is not on the GPU path'.format(scheme))
     raise TypeError('Have not implemented {} time integration yet.'.format(scheme))

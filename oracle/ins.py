@@ -58,9 +58,11 @@ class TaylorHood:
         grad = np.einsum('eqir,eci->eqcr', self.gphi, ue)
         return val, grad
 
-    def matrix(self, mass: float, nu: float, dt: float, wind=None, eps_p: float = 1e-10):
+    def matrix(self, mass: float, nu: float, dt: float, wind=None, eps_p: float = 1e-10, tcoef=None):
         """The compound system matrix (scipy CSR); `wind` a compound vector whose velocity is the
-        Oseen wind, or None (Stokes / IMEX)."""
+        Oseen wind, or None (Stokes / IMEX); tcoef the factor of the divergence and pressure terms
+        (default dt; OpenCMP's CNLF doubles them)."""
+        tc = dt if tcoef is None else tcoef
         W = self.W
         M = np.einsum('eq,qi,qj->eij', W, self.phi, self.phi)
         K = np.einsum('eq,eqir,eqjr->eij', W, self.gphi, self.gphi)
@@ -69,8 +71,8 @@ class TaylorHood:
             wv, _ = self._field(wind)
             wg = np.einsum('eqc,eqic->eqi', wv, self.gphi)            # w . grad phi_i
             Kuu = Kuu - dt * np.einsum('eq,eqi,qj->eij', W, wg, self.phi)
-        B = [-dt * np.einsum('eq,qi,eqj->eij', W, self.psi, self.gphi[..., c]) for c in range(2)]   # (ne, Lp, Lu)
-        Kpp = -dt * eps_p * np.einsum('eq,qi,qj->eij', W, self.psi, self.psi)
+        B = [-tc * np.einsum('eq,qi,eqj->eij', W, self.psi, self.gphi[..., c]) for c in range(2)]   # (ne, Lp, Lu)
+        Kpp = -tc * eps_p * np.einsum('eq,qi,qj->eij', W, self.psi, self.psi)
         rows, cols, vals = [], [], []
 
         def add(rd, cd, blocks):
@@ -91,8 +93,8 @@ class TaylorHood:
         A.sum_duplicates()
         return A
 
-    def rhs(self, dt: float, f=(0.0, 0.0), mass: float = 0.0, uprev=None, imex=None):
-        """dt f . v + mass u_prev . v - dt (grad(u^n) u^n) . v (the last with imex = u^n)."""
+    def rhs(self, dt: float, f=(0.0, 0.0), mass: float = 0.0, uprev=None, imex=None, imex_coef: float = 1.0):
+        """dt f . v + mass u_prev . v - imex_coef dt (grad(w) w) . v (the last with imex = w)."""
         W = self.W
         Fe = np.zeros((self.mesh.ne, 2, self.phi.shape[1]))
         fq = np.zeros((self.mesh.ne, len(self.wq), 2))
@@ -103,7 +105,7 @@ class TaylorHood:
             q = q + mass * val
         if imex is not None:
             val, grad = self._field(imex)
-            q = q - dt * np.einsum('eqcr,eqr->eqc', grad, val)
+            q = q - imex_coef * dt * np.einsum('eqcr,eqr->eqc', grad, val)
         Fe = np.einsum('eq,qi,eqc->eci', W, self.phi, q)
         b = np.zeros(self.ndof)
         np.add.at(b, self.dv, Fe[:, 0])

@@ -19,7 +19,7 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 GOLDEN = os.path.join(ROOT, 'tests', 'golden')
 FIX = os.path.join(GOLDEN, 'fixtures')
 SUPPORTED = ('explicit euler', 'implicit euler', 'crank nicolson', 'euler IMEX', 'adaptive two step',
-             'adaptive three step')
+             'adaptive three step', 'CNLF', 'SBDF')
 # Explicit Euler on the order-3 DG Poisson forms of the coarse fixture amplifies by 5.0 per step
 # (test_explicit_dg_poisson_is_unstable): every run of it, the oracle's included, overflows.
 UNSTABLE = {'test_poisson.py::TestTransient::test_explicit_euler_dg'}
@@ -49,11 +49,11 @@ def _cases():
         dg = cfg.get_item(['DG', 'DG'], bool)
         if scheme not in SUPPORTED:
             marks = [pytest.mark.skip(reason='time scheme {!r} is not on the GPU path'.format(scheme))]
-        elif scheme == 'euler IMEX' and model != 'INS':
+        elif scheme in ('euler IMEX', 'CNLF', 'SBDF') and model != 'INS':
             marks = [pytest.mark.skip(reason='IMEX linearisation is on the GPU path for INS only')]
-        elif model == 'INS' and (dg or scheme not in ('implicit euler', 'euler IMEX')):
+        elif model == 'INS' and (dg or scheme not in ('implicit euler', 'euler IMEX', 'CNLF', 'SBDF')):
             marks = [pytest.mark.skip(reason='INS runs on the GPU path as continuous Taylor-Hood with implicit '
-                                             'Euler (Oseen) or Euler IMEX')]
+                                             'Euler (Oseen) or the IMEX schemes')]
         elif t['id'] in UNSTABLE:
             marks = [pytest.mark.skip(reason='the scheme is unstable on these forms (amplification 5.0 per step)')]
         else:
@@ -124,6 +124,8 @@ def test_registries():
     cfg['TRANSIENT']['scheme'] = 'adaptive two step'
     assert get_solver_class(cfg) is AdaptiveSolver
     cfg['TRANSIENT']['scheme'] = 'SBDF'
+    assert get_solver_class(cfg) is TransientMultiStepSolver
+    cfg['TRANSIENT']['scheme'] = 'RK 222'
     with pytest.raises(NotImplementedError):
         get_solver_class(cfg)
     cfg['TRANSIENT']['scheme'] = 'leapfrog'

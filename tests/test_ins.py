@@ -57,16 +57,17 @@ def _pair(oracle, n, k):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize('k,oseen', [(2, False), (2, True), (3, False), (3, True)])
-def test_th_matrix_matches_oracle(gpu_lib, oracle, k, oseen):
+@pytest.mark.parametrize('k,oseen,tcoef', [(2, False, None), (2, True, None), (3, False, None), (3, True, None),
+                                           (2, False, 2e-3)])
+def test_th_matrix_matches_oracle(gpu_lib, oracle, k, oseen, tcoef):
     import torch
     m, g, o = _pair(oracle, 6, k)
     rng = np.random.default_rng(k)
     w = rng.standard_normal(o.ndof) if oseen else None
     A = g.matrix()
     g.assemble(A, mass=1.0, nu=1e-3, dt=1e-3, eps_p=1e-10,
-               wind=torch.as_tensor(w, device='cuda') if oseen else None)
-    Ao = o.matrix(1.0, 1e-3, 1e-3, wind=w)
+               wind=torch.as_tensor(w, device='cuda') if oseen else None, tcoef=tcoef)
+    Ao = o.matrix(1.0, 1e-3, 1e-3, wind=w, tcoef=tcoef)
     rp, col = g.C.pattern()
     np.testing.assert_array_equal(rp, Ao.indptr)
     np.testing.assert_array_equal(col, Ao.indices)
@@ -85,8 +86,10 @@ def test_th_rhs_matches_oracle(gpu_lib, oracle, k):
     u0 = rng.standard_normal(o.ndof)
     b = torch.zeros(g.ndof, dtype=torch.float64, device='cuda')
     ut = torch.as_tensor(u0, device='cuda')
+    u1 = rng.standard_normal(o.ndof)
     g.assemble_rhs(b, dt=0.01, src=(0.5, -1.0), mass=1.0, uprev=ut, imex=ut)
-    bo = o.rhs(0.01, f=(0.5, -1.0), mass=1.0, uprev=u0, imex=u0)
+    g.assemble_rhs(b, dt=0.01, imex=torch.as_tensor(u1, device='cuda'), imex_coef=-3.0, accumulate=True)
+    bo = o.rhs(0.01, f=(0.5, -1.0), mass=1.0, uprev=u0, imex=u0) + o.rhs(0.01, imex=u1, imex_coef=-3.0)
     bg = b.cpu().numpy()
     assert np.abs(bg - bo).max() <= 1e-12 * np.abs(bo).max()
 
