@@ -277,35 +277,56 @@ int ocmp_th_errors(ocmp_th_t th, const double* u_dev, const double* ref_qp_dev, 
 
 /* ---------------------------------------------------------------- learned initial guess
  * No counterpart in the reference (OpenCMP starts each Krylov solve from the previous step's
- * solution, base_model.py:925-937). A per-dof MLP  y = w3 . tanh(W2 tanh(W1 x + b1) + b2) + b3 + c . x,
- * hidden width 32, FP32, predicts (u^{n+1} - u^n) / s_i from features x built by
- * ocmp_guess_features (the last k-1 solution differences and an optional graph feature, each
- * divided by the dof's difference norm s_i). Training: ocmp_guess_loss_grad (mean squared error over `rows` samples,
- * deterministic gradients) + ocmp_guess_adam_step. The solve's FP64 residual test is unchanged,
+ * solution, base_model.py:925-937). From the last k solutions u^n, u^{n-1}, ... (k <= 6) each dof
+ * has the backward differences D_j = nabla^j u^n, j = 1..k-1. The guess
+ *     x = u^n + D_1 + ... + D_p + S_{k-1} y(X),   X = [D_1 / S_1, ..., D_{k-1} / S_{k-1}]
+ * is the degree-p extrapolation in time plus the correction of a per-dof MLP
+ *     y = w3 . tanh(W2 tanh(W1 x + b1) + b2) + b3 + c . x   (hidden width 16, FP32, F = k-1 inputs),
+ * S_j being the root mean square of D_j over the free dofs. A new network has zero output. Training
+ * (ocmp_guess_residual_loss, ocmp_guess_backward, ocmp_guess_adam_step) minimises the FP64
+ * relative residual |A e| / |b| the guess leaves; the solve's own FP64 residual test is unchanged,
  * so the guess never decides the accuracy of the result. */
 int ocmp_guess_create(int32_t n_features, uint64_t seed, ocmp_guess_t* out);
 int ocmp_guess_destroy(ocmp_guess_t g);
 int ocmp_guess_nparams(ocmp_guess_t g);
 int ocmp_guess_params(ocmp_guess_t g, float* host, int32_t set);       /* copy out (set=0) or in (set=1) */
 int ocmp_guess_forward(ocmp_guess_t g, const float* X_dev, int64_t rows, float* Y_dev, void* stream);
+/* mean squared error over `rows` samples and its parameter gradient (deterministic) */
 int ocmp_guess_loss_grad(ocmp_guess_t g, const float* X_dev, const float* T_dev, int64_t rows, double* loss_host,
                          float* grad_host, void* stream);
+/* parameter gradient of sum_r dY_r y_r (back-propagation of an upstream gradient), deterministic;
+ * kept on the device for ocmp_guess_adam_step, copied to grad_host when it is not NULL */
+int ocmp_guess_backward(ocmp_guess_t g, const float* X_dev, const float* dY_dev, int64_t rows, float* grad_host,
+                        void* stream);
 int ocmp_guess_adam_step(ocmp_guess_t g, float lr, void* stream);
-/* scale_dev[0] = sqrt(mean((a - b)^2)), computed on the device (no host synchronisation) */
-int ocmp_guess_scale(ocmp_guess_t g, int64_t n, const double* a_dev, const double* b_dev, double* scale_dev,
-                     void* stream);
-/* From the k history vectors h0 = u^n, h1 = u^{n-1}, ...: per dof i the differences d_j = h_j - h_{j+1},
- * s_i = |(d_0, d_1, ...)|_2 (written to scale_dev, n doubles) and X_i = [d_0, d_1, ..., q_i] / s_i. */
-int ocmp_guess_features(int64_t n, int32_t k, const double* const* hist_dev, const double* q_dev,
-                        double* scale_dev, float* X_dev, int32_t F, void* stream);
-/* training target T_i = clamp((u^{n+1}_i - u^n_i) / s_i, -10, 10) */
-int ocmp_guess_target(int64_t n, const double* unext_dev, const double* un_dev, const double* scale_dev,
-                      float* T_dev, void* stream);
-/* x = u^n + s_i * y_i on free dofs (free_dev may be NULL: all free) */
-int ocmp_guess_apply(int64_t n, const double* un_dev, const float* y_dev, const double* scale_dev,
-                     const uint8_t* free_dev, double* x_dev, void* stream);
-/* q = D^-1 (b - A x) on free dofs (the Jacobi correction of x; the guess network's graph feature) */
-int ocmp_jacobi_residual(ocmp_matrix_t mat, const double* b_dev, const double* x_dev, double* q_dev, void* stream);
+/* The history is a backward-difference table in double-float held by the caller: tab_dev = k rows
+ * of n (hi, lo) float pairs (2 k n floats), row j = nabla^j u^n, row 0 = u^n. ocmp_guess_push adds
+ * the newest solution u_dev, m being the number of rows already valid (0 after a reset; after the
+ * push min(m + 1, k) rows are valid). All table arithmetic runs on the FP32 pipes. */
+int ocmp_guess_push(int64_t n, int32_t k, int32_t m, float* tab_dev, const double* u_dev, void* stream);
+/* S_1..S_{k-1} into scales_dev (a 32-double buffer; on the device, no host synchronisation) and,
+ * when X_dev is not NULL, the features X (ndof rows of k-1 floats, zero rows at constrained dofs;
+ * the network must take F = k-1). free_dev may be NULL (all dofs free). k = 2..6 valid rows. */
+int ocmp_guess_features(ocmp_guess_t g, int64_t n, int32_t k, const float* tab_dev, const uint8_t* free_dev,
+                        double* scales_dev, float* X_dev, void* stream);
+/* x = u^n + D_1 + ... + D_p (+ S_{k-1} y(X) when g is not NULL) on free dofs, u^n on constrained
+ * dofs; p = base_order < k valid rows. With g = NULL it is the plain extrapolation (k = 1 or
+ * p = 0: the previous-step guess) and scales_dev may be NULL. */
+int ocmp_guess_predict(ocmp_guess_t g, int64_t n, int32_t k, const float* tab_dev, const uint8_t* free_dev,
+                       const double* scales_dev, int32_t base_order, double* x_dev, void* stream);
+/* training target T_i = (u^{n+1}_i - u^n_i - D_1 - ... - D_p) / S_{k-1} (0 at constrained dofs) */
+int ocmp_guess_target(int64_t n, int32_t k, const float* tab_dev, const uint8_t* free_dev, const double* scales_dev,
+                      int32_t base_order, const double* unext_dev, float* T_dev, void* stream);
+/* Residual loss of a prediction Y (ndof rows) against the target T of one stored step: with
+ * e = S (Y - T) on free dofs (S = *scale_dev = S_{k-1} of that step), loss = weight |(A e)_free|^2 /
+ * |b_free|^2, `weight` times the squared relative residual the guess would start the solve with;
+ * dY = d loss / dY = 2 weight S A^T (A e)_free / |b_free|^2. Needs a structurally symmetric pattern
+ * (A^T gathers through a transpose-position map the space builds on first use). */
+int ocmp_guess_residual_loss(ocmp_guess_t g, ocmp_matrix_t mat, const float* Y_dev, const float* T_dev,
+                             const double* scale_dev, const double* b_dev, double weight, double* loss_host,
+                             float* dY_dev, void* stream);
+/* y = A^T x with the FP64 values (structurally symmetric patterns) */
+int ocmp_spmv_transpose(ocmp_matrix_t mat, const double* x_dev, double* y_dev, void* stream);
 
 /* ---------------------------------------------------------------- allocation-free solve
  * No counterpart in the reference: an addition for callers that cannot call cudaMalloc when they

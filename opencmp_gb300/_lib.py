@@ -131,11 +131,13 @@ SIGNATURES = {
     'ocmp_guess_forward': [P, P, I64, P, P],
     'ocmp_guess_loss_grad': [P, P, P, I64, P, P, P],
     'ocmp_guess_adam_step': [P, C.c_float, P],
-    'ocmp_guess_scale': [P, I64, P, P, P, P],
-    'ocmp_guess_features': [I64, I32, P, P, P, P, I32, P],
-    'ocmp_guess_target': [I64, P, P, P, P, P],
-    'ocmp_guess_apply': [I64, P, P, P, P, P, P],
-    'ocmp_jacobi_residual': [P, P, P, P, P],
+    'ocmp_guess_backward': [P, P, P, I64, P, P],
+    'ocmp_guess_push': [I64, I32, I32, P, P, P],
+    'ocmp_guess_features': [P, I64, I32, P, P, P, P, P],
+    'ocmp_guess_predict': [P, I64, I32, P, P, P, I32, P, P],
+    'ocmp_guess_target': [I64, I32, P, P, P, I32, P, P, P],
+    'ocmp_guess_residual_loss': [P, P, P, P, P, P, D, P, P, P],
+    'ocmp_spmv_transpose': [P, P, P, P],
 }
 
 _lib = None

@@ -20,6 +20,7 @@
 #include <vector>
 
 #include "ocmp_internal.h"
+#include "ocmp_ff.cuh"
 #include "ocmp_spmv.cuh"
 
 namespace ocmp {
@@ -487,39 +488,9 @@ __global__ void __launch_bounds__(128) row_scatter_kernel(
 }
 
 // ---------------------------------------------------------------------------------------------
-// Double-float assembly (OCMP_MAT_DFLOAT). Values are unevaluated sums hi + lo of two floats;
-// products use an FMA-exact error term, sums an exact TwoSum of the high parts. Geometry stays FP64;
+// Double-float assembly (OCMP_MAT_DFLOAT): pair arithmetic from ocmp_ff.cuh. Geometry stays FP64;
 // the element terms and the row sums run on the FP32 pipes, and each CSR entry ends with one FP64
-// add. Floats are widened to doubles with integer operations (exact for normal numbers; subnormal
-// floats, below 1.2e-38, are flushed to zero).
-__device__ __forceinline__ void ff_add(float& sh, float& sl, float ph, float pl) {
-    const float s = __fadd_rn(sh, ph);
-    const float bb = __fsub_rn(s, sh);
-    const float err = __fadd_rn(__fsub_rn(sh, __fsub_rn(s, bb)), __fsub_rn(ph, bb));
-    sl = __fadd_rn(__fadd_rn(sl, pl), err);
-    sh = s;
-}
-__device__ __forceinline__ void ff_mul(float ah, float al, float bh, float bl, float& ph, float& pl) {
-    ph = __fmul_rn(ah, bh);
-    float e = __fmaf_rn(ah, bh, -ph);
-    e = __fmaf_rn(ah, bl, e);
-    pl = __fmaf_rn(al, bh, e);
-}
-__device__ __forceinline__ double f2d_exact(float f) {
-    const uint32_t b = __float_as_uint(f);
-    const uint32_t e = (b >> 23) & 0xffu;
-    const unsigned long long sgn = (unsigned long long)(b & 0x80000000u) << 32;
-    if (e == 0) return __longlong_as_double((long long)sgn);
-    if (e == 0xffu) return (double)f;
-    const unsigned long long d = sgn | ((unsigned long long)(e + 896u) << 52) | ((unsigned long long)(b & 0x7fffffu) << 29);
-    return __longlong_as_double((long long)d);
-}
-__device__ __forceinline__ double ff_to_double(float h, float l) { return f2d_exact(h) + f2d_exact(l); }
-__device__ __forceinline__ float2 ff_split(double x) {
-    const float h = __double2float_rn(x);
-    return make_float2(h, __double2float_rn(x - f2d_exact(h)));
-}
-
+// add.
 // Static element geometry of a mesh, once per space (the mesh does not move): |det J|,
 // |det J| grad(lam_p).grad(lam_q) (p <= q) and |det J| grad(lam_p), as (hi, lo) float pairs in
 // structure-of-arrays order (quantity k of element e at G[k * ne + e]).
@@ -560,14 +531,6 @@ __global__ void geo_ff_kernel(int64_t ne, const double* __restrict__ X, const in
         for (int r = 0; r < D; r++) G[(k++) * ne + e] = ff_split(g.adet * gl[p][r]);
 }
 
-// (ah + al)(bh + bl), renormalised so the pair can feed further products
-__device__ __forceinline__ float2 ff_prod(float2 a, float2 b) {
-    float ph, pl;
-    ff_mul(a.x, a.y, b.x, b.y, ph, pl);
-    const float s = __fadd_rn(ph, pl);
-    return make_float2(s, __fsub_rn(pl, __fsub_rn(s, ph)));
-}
-
 // Straight-line element matrices: the term tables of the H1 element types, written out at build
 // time as device code (ocmp_terms_gen.h, from ocmp_host.cpp's generator). Each product is
 // gterm(acc, F[g], coefficient) with g and the coefficient compile-time constants, so the factors
@@ -586,14 +549,21 @@ __device__ __forceinline__ void gterm(float& sh, float& sl, float2 f, float ch, 
 }
 #include "ocmp_terms_gen.h"
 
+// The block's element matrices are staged in shared memory (one padded record per thread, so the
+// half-warps' 8-byte writes fall in distinct banks) and written out as one contiguous run with
+// consecutive threads on consecutive addresses: full-line stores instead of 32 partial lines per
+// warp store.
+constexpr int kGenThreads = 64;
 template <int D, int L, int VAR>
-__global__ void __launch_bounds__(128) elem_gen_ff_kernel(int64_t ne, const float2* __restrict__ geo,
-                                                          const int32_t* __restrict__ conn, FormArgs a,
-                                                          float2* __restrict__ K) {
+__global__ void __launch_bounds__(kGenThreads) elem_gen_ff_kernel(int64_t ne, const float2* __restrict__ geo,
+                                                                  const int32_t* __restrict__ conn, FormArgs a,
+                                                                  float2* __restrict__ K) {
     using GT = GenTerms<D, L, VAR>;
-    constexpr int NP = D + 1, NS = NP * (NP + 1) / 2, LL = L * L;
-    const int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    if (e >= ne) return;
+    constexpr int NP = D + 1, NS = NP * (NP + 1) / 2, LL = L * L, PADLL = LL | 1;
+    extern __shared__ float2 kst[];
+    const int64_t e0 = blockIdx.x * (int64_t)blockDim.x;
+    const int64_t e = e0 + threadIdx.x;
+    if (e < ne) {
     float2 F[GT::NG];
 #pragma unroll
     for (int g = 0; g < GT::NG; g++) F[g] = make_float2(0.f, 0.f);
@@ -633,7 +603,15 @@ __global__ void __launch_bounds__(128) elem_gen_ff_kernel(int64_t ne, const floa
             }
         }
     }
-    GT::run(F, K + e * LL);
+    GT::run(F, kst + threadIdx.x * PADLL);
+    }
+    __syncthreads();
+    const int nb = (int)min((int64_t)blockDim.x, ne - e0);
+    float2* __restrict__ dst = K + e0 * LL;
+    for (int q = threadIdx.x; q < nb * LL; q += blockDim.x) {
+        const int t = q / LL;
+        dst[q] = kst[t * PADLL + (q - t * LL)];
+    }
 }
 
 template <int D, int L>
@@ -936,6 +914,81 @@ __global__ void __launch_bounds__(256) row_gather_warp_kernel(
     }
 }
 
+// ---------------------------------------------------------------------------------------------
+// Sorted segmented reduction for element-only assembly. Once per space (first use), for every CSR
+// entry the list of element-matrix entries that sum into it: row r takes its incidences (e, i) in
+// incidence order and, for each, the entries K_e[i][j] (flat index (e L + i) L + j) whose column slot
+// is the entry's position in the row. Row r's run starts at L * inc_ptr[r], since each incidence
+// adds L entries to its row. One thread per row; counters in a shared-memory stripe.
+template <int L>
+__global__ void __launch_bounds__(128) contrib_build_kernel(int64_t nd, const int32_t* __restrict__ rp,
+                                                            const int32_t* __restrict__ inc_ptr,
+                                                            const int32_t* __restrict__ inc,
+                                                            const uint8_t* __restrict__ slot, int ss, int stripe,
+                                                            int32_t* __restrict__ seg, int32_t* __restrict__ src) {
+    extern __shared__ int32_t cstr[];
+    const int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (r >= nd) return;
+    int32_t* cnt = cstr + (size_t)threadIdx.x * stripe;
+    const int32_t p0 = rp[r], rn = rp[r + 1] - p0;
+    for (int q = 0; q < rn; q++) cnt[q] = 0;
+    for (int32_t k = inc_ptr[r]; k < inc_ptr[r + 1]; k++) {
+        const int64_t flat = inc[k];
+        for (int j = 0; j < L; j++) cnt[slot[flat * ss + j]]++;
+    }
+    int32_t run = L * inc_ptr[r];
+    for (int q = 0; q < rn; q++) {
+        const int32_t c = cnt[q];
+        seg[p0 + q] = run;
+        cnt[q] = run;  // fill pointer
+        run += c;
+    }
+    for (int32_t k = inc_ptr[r]; k < inc_ptr[r + 1]; k++) {
+        const int64_t flat = inc[k];
+        for (int j = 0; j < L; j++) src[cnt[slot[flat * ss + j]]++] = (int32_t)(flat * L + j);
+    }
+}
+
+// One thread per CSR entry: the sum of its element-matrix entries in list order (FP64, or
+// double-float for FF with K as (hi, lo) float pairs), written once to every requested output.
+template <bool FF>
+__global__ void __launch_bounds__(256) csr_gather_kernel(int64_t nnz, const int32_t* __restrict__ seg,
+                                                         const int32_t* __restrict__ src, const void* __restrict__ Kv,
+                                                         const int32_t* __restrict__ col,
+                                                         const double* __restrict__ dinv,
+                                                         const float* __restrict__ dinv32, double* __restrict__ vals,
+                                                         float* __restrict__ vals32, double* __restrict__ svals64,
+                                                         float* __restrict__ svals32) {
+    const int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (k >= nnz) return;
+    const int32_t s0 = __ldg(seg + k), s1 = __ldg(seg + k + 1);
+    if (FF) {
+        const float2* __restrict__ K = reinterpret_cast<const float2*>(Kv);
+        float h = 0.f, l = 0.f;
+        for (int32_t q = s0; q < s1; q++) {
+            const float2 v = __ldg(K + __ldg(src + q));
+            ff_add(h, l, v.x, v.y);
+        }
+        const double vv = ff_to_double(h, l);
+        vals[k] = vv;
+        const float v32 = __fadd_rn(h, l);
+        if (vals32) vals32[k] = v32;
+        if (svals64) svals64[k] = vv * dinv[__ldg(col + k)];
+        if (svals32) svals32[k] = v32 * dinv32[__ldg(col + k)];
+    } else {
+        const double* __restrict__ K = reinterpret_cast<const double*>(Kv);
+        double acc = 0.0;
+        for (int32_t q = s0; q < s1; q++) acc += __ldg(K + __ldg(src + q));
+        vals[k] = acc;
+        if (vals32) vals32[k] = (float)acc;
+        if (svals64 || svals32) {
+            const double sv = acc * dinv[__ldg(col + k)];
+            if (svals64) svals64[k] = sv;
+            if (svals32) svals32[k] = (float)sv;
+        }
+    }
+}
+
 // Element right-hand sides: dt (f, phi_i) + mass (u_prev, phi_i) + boundary data.
 template <int D, int L>
 __global__ void rhs_elem_kernel(int64_t ne, const double* __restrict__ X, const int32_t* __restrict__ conn,
@@ -1055,6 +1108,55 @@ __global__ void rhs_elem_kernel(int64_t ne, const double* __restrict__ X, const 
     }
 #pragma unroll
     for (int i = 0; i < L; i++) Fe[e * L + i] = out[i];
+}
+
+// Mass-term right-hand side in double-float (the implicit time-step load mass (u_prev, phi_i) with
+// no source or boundary data). u_prev is split once per dof into (hi, lo) float pairs; then one
+// thread per (element, local row i), flat = e * L + i:
+//   Fe[flat] = (mass |det J|) (sum_j Rm_ij u_prev[dof(e, j)]), every product and sum in (hi, lo)
+// float pairs; the element's dof indices and values are shared through L1 by its L threads.
+__global__ void split_ff_kernel(int64_t n, const double* __restrict__ u, float2* __restrict__ u2) {
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i < n) u2[i] = ff_split(u[i]);
+}
+
+template <int L>
+__global__ void __launch_bounds__(256) rhs_mass_ff_kernel(int64_t nflat, const int32_t* __restrict__ dofs,
+                                                          const float2* __restrict__ geo, float2 mass,
+                                                          const float2* __restrict__ u2,
+                                                          const float2* __restrict__ Rmf, float2* __restrict__ Fe) {
+    const int64_t flat = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (flat >= nflat) return;
+    const int64_t e = flat / L;
+    const int i = (int)(flat - e * L);
+    float sh = 0.f, sl = 0.f;
+#pragma unroll
+    for (int j = 0; j < L; j++) {
+        const float2 u = __ldg(u2 + __ldg(dofs + e * L + j));
+        const float2 c = __ldg(Rmf + i * L + j);
+        float ph, pl;
+        ff_mul(c.x, c.y, u.x, u.y, ph, pl);
+        ff_add(sh, sl, ph, pl);
+    }
+    const float2 sc = ff_prod(mass, __ldg(geo + e));
+    float ph, pl;
+    ff_mul(sc.x, sc.y, sh, sl, ph, pl);
+    const float hs = __fadd_rn(ph, pl);
+    Fe[flat] = make_float2(hs, __fsub_rn(pl, __fsub_rn(hs, ph)));
+}
+
+// b[d] (+)= sum over the dof's incidences of the (hi, lo) element contributions, in incidence order
+__global__ void rhs_gather_ff_kernel(int64_t ndof, const int32_t* __restrict__ inc_ptr, const int32_t* __restrict__ inc,
+                                     const float2* __restrict__ Fe, double* __restrict__ b, int accumulate) {
+    const int64_t d = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (d >= ndof) return;
+    float h = 0.f, l = 0.f;
+    for (int k = inc_ptr[d]; k < inc_ptr[d + 1]; k++) {
+        const float2 v = __ldg(Fe + inc[k]);
+        ff_add(h, l, v.x, v.y);
+    }
+    const double acc = ff_to_double(h, l);
+    b[d] = accumulate ? b[d] + acc : acc;
 }
 
 __global__ void rhs_gather_kernel(int64_t ndof, const int32_t* __restrict__ inc_ptr, const int32_t* __restrict__ inc,
@@ -1179,11 +1281,14 @@ int assemble_impl(ocmp_matrix_s* m, const ocmp_form_t* f, cudaStream_t st) {
         bool done = false;
         if constexpr (GenTerms<D, L, 0>::value && GenTerms<D, L, 1>::value) {
             if (s->kind == OCMP_H1) {
+                const size_t gsm = sizeof(float2) * (size_t)kGenThreads * ((L * L) | 1);
+                OCMP_CUDA(cudaFuncSetAttribute(elem_gen_ff_kernel<D, L, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)gsm));
+                OCMP_CUDA(cudaFuncSetAttribute(elem_gen_ff_kernel<D, L, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)gsm));
                 if (var == 0)
-                    OCMP_LAUNCH(elem_gen_ff_kernel<D, L, 0><<<nblk(ne, 128), 128, 0, st>>>(ne, s->d_geo_ff, mesh->dconn, a,
+                    OCMP_LAUNCH(elem_gen_ff_kernel<D, L, 0><<<nblk(ne, kGenThreads), kGenThreads, gsm, st>>>(ne, s->d_geo_ff, mesh->dconn, a,
                                                                                            Kff));
                 else
-                    OCMP_LAUNCH(elem_gen_ff_kernel<D, L, 1><<<nblk(ne, 128), 128, 0, st>>>(ne, s->d_geo_ff, mesh->dconn, a,
+                    OCMP_LAUNCH(elem_gen_ff_kernel<D, L, 1><<<nblk(ne, kGenThreads), kGenThreads, gsm, st>>>(ne, s->d_geo_ff, mesh->dconn, a,
                                                                                            Kff));
                 done = true;
             }
@@ -1223,6 +1328,35 @@ int assemble_impl(ocmp_matrix_s* m, const ocmp_form_t* f, cudaStream_t st) {
     else if (m->dinv)
         OCMP_LAUNCH(diag_kernel<L><<<nblk(nd, 256), 256, 0, st>>>(nd, s->d_inc_ptr, s->d_inc, s->d_K, s->d_free, use_facets, efp,
                                                       s->d_efac, s->d_ebf_ptr, s->d_ebf, Ki, Kb, m->dinv));
+    if (!use_facets) {
+        // element-only assembly: sorted segmented reduction, one thread per CSR entry
+        if (!s->d_cseg) {
+            const int64_t ncon = ne * (int64_t)L * L;
+            if (ncon >= (int64_t)INT32_MAX) return fail(OCMP_ERR_UNSUPPORTED, "assembly: too many element entries");
+            OCMP_CUDA(cudaMalloc((void**)&s->d_cseg, sizeof(int32_t) * (size_t)(s->nnz + 1)));
+            OCMP_CUDA(cudaMalloc((void**)&s->d_csrc, sizeof(int32_t) * (size_t)ncon));
+            const int ct = 128;
+            const size_t csm = sizeof(int32_t) * (size_t)s->maxrow * ct;
+            OCMP_CUDA(cudaFuncSetAttribute(contrib_build_kernel<L>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)csm));
+            OCMP_LAUNCH(contrib_build_kernel<L><<<nblk(nd, ct), ct, csm, st>>>(nd, s->d_rowptr, s->d_inc_ptr, s->d_inc,
+                                                                          s->d_slot, s->slot_stride, s->maxrow,
+                                                                          s->d_cseg, s->d_csrc));
+            const int32_t last = (int32_t)ncon;
+            OCMP_CUDA(cudaMemcpyAsync(s->d_cseg + s->nnz, &last, sizeof(int32_t), cudaMemcpyHostToDevice, st));
+            OCMP_CUDA(cudaStreamSynchronize(st));
+        }
+        const void* Kc = dfl ? (const void*)Kff : (const void*)s->d_K;
+        if (dfl)
+            OCMP_LAUNCH(csr_gather_kernel<true><<<nblk(s->nnz, 256), 256, 0, st>>>(s->nnz, s->d_cseg, s->d_csrc, Kc, s->d_col,
+                                                                              m->dinv, m->dinv32, m->vals, m->vals32,
+                                                                              m->svals64, m->svals32));
+        else
+            OCMP_LAUNCH(csr_gather_kernel<false><<<nblk(s->nnz, 256), 256, 0, st>>>(s->nnz, s->d_cseg, s->d_csrc, Kc, s->d_col,
+                                                                               m->dinv, m->dinv32, m->vals, m->vals32,
+                                                                               m->svals64, m->svals32));
+        OCMP_CUDA(cudaGetLastError());
+        return OCMP_OK;
+    }
     if (!use_facets) {
         // element-only assembly: one warp per row (row_gather_warp_kernel)
         const int wt = 256, wpb = wt / 32;
@@ -1274,6 +1408,21 @@ int rhs_impl(ocmp_space_s* s, const ocmp_form_t* f, const ocmp_rhs_t* r, double*
     const ocmp_mesh_s* mesh = s->mesh;
     const int64_t ne = mesh->ne;
     FormArgs a = make_args(s, f);
+    // double-float mass load alone (no source, no boundary data): thread per (element, row)
+    const bool bnd = r->bval_mask != 0 || (s->kind == OCMP_L2 && f->nitsche_mask != 0);
+    if (r->dfloat && r->uprev && r->src_kind == OCMP_SRC_NONE && !bnd && s->d_geo_ff && s->d_Rm_ff) {
+        float2* Fe2 = reinterpret_cast<float2*>(s->d_Fe);
+        if (!s->d_u2) OCMP_CUDA(cudaMalloc((void**)&s->d_u2, sizeof(float2) * (size_t)s->ndof));
+        OCMP_LAUNCH(split_ff_kernel<<<nblk(s->ndof, 256), 256, 0, st>>>(s->ndof, r->uprev, s->d_u2));
+        const float mh = (float)r->mass;
+        const float2 m2 = make_float2(mh, (float)(r->mass - (double)mh));
+        OCMP_LAUNCH(rhs_mass_ff_kernel<L><<<nblk(ne * L, 256), 256, 0, st>>>(ne * L, s->d_dofs, s->d_geo_ff, m2, s->d_u2,
+                                                                        s->d_Rm_ff, Fe2));
+        OCMP_LAUNCH(rhs_gather_ff_kernel<<<nblk(s->ndof, 256), 256, 0, st>>>(s->ndof, s->d_inc_ptr, s->d_inc, Fe2, b,
+                                                                        r->accumulate));
+        OCMP_CUDA(cudaGetLastError());
+        return OCMP_OK;
+    }
     // per-label data travels by value through a small device buffer owned by the call's stream
     double* dvals = nullptr;
     OCMP_CUDA(cudaMallocAsync((void**)&dvals, sizeof(double) * 64, st));

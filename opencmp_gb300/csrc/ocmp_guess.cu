@@ -1,14 +1,25 @@
 // Learned Krylov initial guess (sm_103a): a small per-dof MLP, its training kernels and the
-// feature/guess kernels around it. No counterpart in the reference: OpenCMP starts CG/GMRes from
-// the previous step's solution (opencmp/models/base_model.py:925-937), which stays the fallback.
+// history/feature/prediction kernels around it. No counterpart in the reference: OpenCMP starts
+// CG/GMRes from the previous step's solution (opencmp/models/base_model.py:925-937).
+//
+// Guess. From the last k solutions h_0 = u^n, h_1 = u^{n-1}, ... (k <= 6) every dof forms the
+// backward differences D_j = nabla^j u^n (j = 1..k-1). The guess is
+//     x = u^n + D_1 + ... + D_p  +  S_{k-1} * y(X),      X = [D_1 / S_1, ..., D_{k-1} / S_{k-1}],
+// the degree-p Newton (backward-difference) extrapolation in time plus the network's correction,
+// where S_j is the root mean square of D_j over the free dofs. Without the network (or before it
+// is trusted) the guess is the extrapolation alone; with p = 0 it is OpenCMP's previous-step guess.
 //
 // Network: y = w3 . tanh(W2 tanh(W1 x + b1) + b2) + b3 + c . x, x in R^F (F <= 8), hidden width
-// H = 32, FP32; the linear skip c . x makes polynomial extrapolation in time exactly representable.
-// Per dof, x holds the last solution differences and the Jacobi-scaled residual of the previous-step
-// guess, all divided by the norm of that dof's differences; y predicts (u^{n+1} - u^n) / that norm.
+// H = 16, FP32. It starts with zero output (w3, b3, c = 0), so an untrained network leaves the
+// extrapolation unchanged.
 //
-// Training is deterministic: the weight gradients are sums over rows done in two fixed-order stages
-// (per-block partial sums in shared memory, then one pass over the blocks), followed by an Adam step.
+// Training minimises the initial residual the guess would give the solve: for a stored step with
+// target T = (u^{n+1} - base) / S_{k-1}, the error of the guess is e = S_{k-1} (y - T) and the loss
+// |A e|^2 / |b|^2 over the free rows (ocmp_guess_residual_loss). Its gradient with respect to y is
+// 2 S_{k-1} A^T A e / |b|^2, formed with A and its transpose (the pattern is structurally
+// symmetric; A^T x gathers through a transpose-position map), and back-propagated through the
+// network by ocmp_guess_backward. Gradients are deterministic: sums over rows run in two fixed-order
+// stages (per-block partial sums in shared memory, then one pass over the blocks).
 #include <cuda_runtime.h>
 
 #include <cmath>
@@ -16,14 +27,17 @@
 #include <vector>
 
 #include "ocmp_internal.h"
+#include "ocmp_ff.cuh"
 #include "ocmp_spmv.cuh"
 
 namespace ocmp {
 namespace {
 
-constexpr int kH = 32;
+constexpr int kH = 16;
 constexpr int kMaxF = 8;
+constexpr int kMaxK = 6;
 constexpr int kRowsPerBlock = 256;
+constexpr int kRedBlocks = 304;  // 2 x 152 SMs: fixed grid of the deterministic reductions
 
 struct Layout {
     int F;
@@ -41,6 +55,26 @@ __host__ __device__ inline Layout layout(int F) {
     L.c = L.b3 + 1;
     L.n = L.c + F;
     return L;
+}
+
+__device__ __forceinline__ double warp_sum_d(double v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+// true in every thread of the block that finishes last; resets the counter for the next launch
+__device__ __forceinline__ bool last_block(unsigned* cnt) {
+    __shared__ bool last;
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) last = atomicAdd(cnt, 1u) == gridDim.x - 1;
+    __syncthreads();
+    if (last) {
+        __threadfence();
+        if (threadIdx.x == 0) *cnt = 0;
+    }
+    return last;
 }
 
 // forward of one row; h1, h2 returned for the backward pass
@@ -66,6 +100,39 @@ __device__ __forceinline__ float mlp_row(const float* __restrict__ P, const Layo
     return y;
 }
 
+// tanh on the special-function unit (one MUFU.TANH instruction; absolute error below 1e-3): the
+// per-step prediction only; training and the forward/gradient kernels use tanhf
+__device__ __forceinline__ float tanh_fast(float x) {
+    float y;
+    asm("tanh.approx.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+
+// the same forward with F known at compile time and tanh_fast (the per-step prediction kernel)
+template <int F>
+__device__ __forceinline__ float mlp_row_f(const float* __restrict__ P, const float (&x)[F]) {
+    constexpr int W1 = 0, B1 = kH * F, W2 = B1 + kH, B2 = W2 + kH * kH, W3 = B2 + kH, B3 = W3 + kH, CC = B3 + 1;
+    float h1[kH];
+#pragma unroll
+    for (int j = 0; j < kH; j++) {
+        float a = P[B1 + j];
+#pragma unroll
+        for (int f = 0; f < F; f++) a = fmaf(P[W1 + j * F + f], x[f], a);
+        h1[j] = tanh_fast(a);
+    }
+    float y = P[B3];
+#pragma unroll
+    for (int j = 0; j < kH; j++) {
+        float a = P[B2 + j];
+#pragma unroll
+        for (int k = 0; k < kH; k++) a = fmaf(P[W2 + j * kH + k], h1[k], a);
+        y = fmaf(P[W3 + j], tanh_fast(a), y);
+    }
+#pragma unroll
+    for (int f = 0; f < F; f++) y = fmaf(P[CC + f], x[f], y);
+    return y;
+}
+
 __global__ void __launch_bounds__(kRowsPerBlock) mlp_forward_kernel(int64_t rows, int F, const float* __restrict__ Pg,
                                                                     const float* __restrict__ X, float* __restrict__ Y) {
     extern __shared__ float P[];
@@ -79,13 +146,16 @@ __global__ void __launch_bounds__(kRowsPerBlock) mlp_forward_kernel(int64_t rows
     Y[r] = mlp_row(P, L, x, h1, h2);
 }
 
-// Per row: forward, loss term (y - t)^2 / rows and the row's gradients; the block sums its rows'
-// parameter gradients in shared memory in row order (thread 0 walks the rows), then writes one
-// partial gradient vector per block. Loss partials likewise.
+// Per row: forward and the gradient of the row's loss term with respect to y, either
+//   mean squared error (T given): dy = 2 (y - t) / rows, loss term (y - t)^2 / rows, or
+//   an upstream gradient (dY given): dy = dY[r], no loss;
+// then the row's parameter gradients. The block sums its rows' parameter gradients in shared
+// memory in row order and writes one partial gradient vector per block. Loss partials likewise.
 __global__ void __launch_bounds__(kRowsPerBlock) mlp_grad_partial_kernel(int64_t rows, int F,
                                                                          const float* __restrict__ Pg,
                                                                          const float* __restrict__ X,
                                                                          const float* __restrict__ T,
+                                                                         const float* __restrict__ dY,
                                                                          float* __restrict__ Gpart,
                                                                          double* __restrict__ Lpart) {
     extern __shared__ double smd[];
@@ -108,10 +178,15 @@ __global__ void __launch_bounds__(kRowsPerBlock) mlp_grad_partial_kernel(int64_t
     if (valid) {
         for (int f = 0; f < F; f++) x[f] = X[r * F + f];
         const float y = mlp_row(P, L, x, h1, h2);
-        const float e = y - T[r];
-        dy = 2.f * e / (float)rows;
+        if (T) {
+            const float e = y - T[r];
+            dy = 2.f * e / (float)rows;
+            sloss[tid] = (double)e * (double)e / (double)rows;
+        } else {
+            dy = dY[r];
+            sloss[tid] = 0.0;
+        }
         sdy[tid] = dy;
-        sloss[tid] = (double)e * (double)e / (double)rows;
         float d2[kH];
 #pragma unroll
         for (int j = 0; j < kH; j++) d2[j] = dy * P[L.w3 + j] * (1.f - h2[j] * h2[j]);
@@ -204,104 +279,249 @@ __global__ void adam_kernel(int n, float* __restrict__ P, const float* __restric
     P[p] -= lr * (m / c1) / (sqrtf(v / c2) + eps);
 }
 
-// features at dof i: x = [d_0, d_1, ..., q] / s_i with d_j = h_j - h_{j+1} (h_0 = u^n) and the per-dof
-// scale s_i = |(d_0, d_1, ...)|_2 at that dof (floored at 1e-300); s_i is written to `scale`
-__global__ void features_kernel(int64_t n, int k, const double* __restrict__ h0, const double* __restrict__ h1,
-                                const double* __restrict__ h2, const double* __restrict__ h3,
-                                const double* __restrict__ q, double* __restrict__ scale, float* __restrict__ X,
-                                int F) {
+// ---- the history as a backward-difference table in double-float ---------------------------------
+// Row j of the table (n (hi, lo) float pairs, rows stored one after another) holds nabla^j u^n; row
+// 0 is u^n itself. Every operation on it runs on the FP32 pipes (this part's FP64 rate is 1/58 of
+// FP32): doubles are split into pairs with integer operations, differences and sums are TwoSum-exact
+// float-pair arithmetic (about 48 significant bits), and only the final guess is widened to FP64.
+
+__device__ __forceinline__ float2 tab_at(const float2* __restrict__ tab, int64_t n, int j, int64_t i) {
+    return __ldg(tab + (int64_t)j * n + i);
+}
+
+// push u^{n+1}: row 0 <- u^{n+1}; row j <- (new row j-1) - (old row j-1) for 0 < j < min(m + 1, K)
+__global__ void push_kernel(int64_t n, int K, int m, float2* __restrict__ tab, const double* __restrict__ u) {
     const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (i >= n) return;
-    const double* h[4] = {h0, h1, h2, h3};
-    double d[4];
-    double s2 = 0;
-    for (int j = 0; j + 1 < k; j++) {
-        d[j] = h[j][i] - h[j + 1][i];
-        s2 += d[j] * d[j];
-    }
-    const double s = fmax(sqrt(s2), 1e-300);
-    scale[i] = s;
-    const double inv = 1.0 / s;
-    int f = 0;
-    for (int j = 0; j + 1 < k && f < F; j++, f++) X[i * F + f] = (float)(d[j] * inv);
-    if (q && f < F) X[i * F + f++] = (float)fmax(-1e3, fmin(1e3, q[i] * inv));
-    for (; f < F; f++) X[i * F + f] = 0.f;
-}
-
-// training target t_i = (u^{n+1}_i - u^n_i) / s_i, clamped to [-10, 10]
-__global__ void target_kernel(int64_t n, const double* __restrict__ unext, const double* __restrict__ un,
-                              const double* __restrict__ scale, float* __restrict__ T) {
-    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    T[i] = (float)fmax(-10.0, fmin(10.0, (unext[i] - un[i]) / scale[i]));
-}
-
-// x = u^n + scale * y on free dofs (constrained dofs keep u^n)
-__global__ void apply_kernel(int64_t n, const double* __restrict__ un, const float* __restrict__ y,
-                             const double* __restrict__ scale, const uint8_t* __restrict__ freed, double* __restrict__ x) {
-    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    x[i] = un[i] + ((freed == nullptr || freed[i]) ? scale[i] * (double)y[i] : 0.0);
-}
-
-// scale = sqrt(mean((a - b)^2)) (floored at 1e-300), two fixed-order stages in one launch: the last
-// block to finish sums the per-block partials in block order.
-__global__ void rms_diff_kernel(int64_t n, const double* __restrict__ a, const double* __restrict__ b,
-                                double* __restrict__ part, unsigned* __restrict__ cnt, double* __restrict__ scale) {
-    double acc = 0;
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-        const double d = a[i] - b[i];
-        acc += d * d;
-    }
-    __shared__ double sh[32];
-    for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
-    if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = acc;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        double t = 0;
-        for (int w = 0; w < (int)(blockDim.x >> 5); w++) t += sh[w];
-        part[blockIdx.x] = t;
-    }
-    __shared__ bool last;
-    __threadfence();
-    __syncthreads();
-    if (threadIdx.x == 0) last = atomicAdd(cnt, 1u) == gridDim.x - 1;
-    __syncthreads();
-    if (!last || threadIdx.x != 0) return;
-    __threadfence();
-    double t = 0;
-    for (unsigned q = 0; q < gridDim.x; q++) t += __ldcg(part + q);
-    *cnt = 0;
-    const double r = sqrt(t / (double)(n > 0 ? n : 1));
-    scale[0] = r > 1e-300 ? r : 1e-300;
-}
-
-// q = D^-1 (b - A x) on free rows (0 elsewhere), FP64, TPR lanes per row (the SpMV row kernel)
-template <int TPR, int U>
-__global__ void __launch_bounds__(256) jacobi_resid_kernel(int64_t n, const int32_t* __restrict__ rp,
-                                                           const int32_t* __restrict__ col,
-                                                           const double* __restrict__ A,
-                                                           const double* __restrict__ dinv,
-                                                           const int32_t* __restrict__ diagpos,
-                                                           const uint8_t* __restrict__ freed,
-                                                           const double* __restrict__ b, const double* __restrict__ x,
-                                                           double* __restrict__ q) {
-    const int64_t r = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) / TPR;
-    const int lane = threadIdx.x % TPR;
-    int32_t a = 0, e = 0;
-    if (r < n) {
-        a = __ldg(rp + r);
-        e = __ldg(rp + r + 1);
-    }
-    const double ax = row_dot<double, double, TPR, U>(a, e, col, A, x, lane);
-    if (r < n && lane == 0) {
-        if (!freed[r]) {
-            q[r] = 0.0;
+    float2 cur = split_d(u[i]);
+    const int mn = m + 1 < K ? m + 1 : K;
+    for (int j = 0; j < mn; j++) {
+        float2* slot = tab + (int64_t)j * n + i;
+        if (j < m) {
+            const float2 old = *slot;
+            *slot = cur;
+            cur = ff_addn(cur, old, true);
         } else {
-            const double di = dinv ? dinv[r] : 1.0 / A[diagpos[r]];
-            q[r] = di * (b[r] - ax);
+            *slot = cur;
         }
     }
+}
+
+// S_j = sqrt(mean over free dofs of (row j)^2), j = 1..K-1 (from the high parts, floored at 1e-300),
+// into sc[j-1]; as floats 1 / S_j and S_j into ((float*)(sc + 8))[j-1] and [8 + j-1]. One launch of
+// kRedBlocks blocks, the last block summing the per-block partials in block order.
+template <int K>
+__global__ void __launch_bounds__(256) hist_scales_kernel(int64_t n, const float2* __restrict__ tab,
+                                                          const uint8_t* __restrict__ freed,
+                                                          double* __restrict__ part, unsigned* __restrict__ cnt,
+                                                          double* __restrict__ sc) {
+    constexpr int NQ = K;  // K-1 sums of squares + the free count
+    float acc[NQ];
+#pragma unroll
+    for (int q = 0; q < NQ; q++) acc[q] = 0.f;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        if (freed && !freed[i]) continue;
+#pragma unroll
+        for (int j = 1; j < K; j++) {
+            const float d = tab_at(tab, n, j, i).x;
+            acc[j - 1] = fmaf(d, d, acc[j - 1]);
+        }
+        acc[K - 1] += 1.f;
+    }
+    __shared__ double sh[NQ][8];
+#pragma unroll
+    for (int q = 0; q < NQ; q++) {
+        const double s = warp_sum_d((double)acc[q]);
+        if ((threadIdx.x & 31) == 0) sh[q][threadIdx.x >> 5] = s;
+    }
+    __syncthreads();
+    if (threadIdx.x < NQ) {
+        double t = 0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); w++) t += sh[threadIdx.x][w];
+        part[(int64_t)threadIdx.x * gridDim.x + blockIdx.x] = t;
+    }
+    if (!last_block(cnt)) return;
+    if (threadIdx.x < NQ) {
+        double t = 0;
+        for (unsigned b = 0; b < gridDim.x; b++) t += __ldcg(part + (int64_t)threadIdx.x * gridDim.x + b);
+        sh[threadIdx.x][0] = t;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        const double nf = fmax(sh[K - 1][0], 1.0);
+        float* fs = reinterpret_cast<float*>(sc + 8);
+        for (int j = 1; j < K; j++) {
+            const double S = fmax(sqrt(sh[j - 1][0] / nf), 1e-300);
+            sc[j - 1] = S;
+            fs[j - 1] = (float)(1.0 / S);
+            fs[8 + j - 1] = (float)S;
+        }
+    }
+}
+
+// X[i] = [D_1 / S_1, ..., D_{K-1} / S_{K-1}] (FP32, F = K-1 per row); zero rows at constrained dofs
+template <int K>
+__global__ void features_kernel(int64_t n, const float2* __restrict__ tab, const uint8_t* __restrict__ freed,
+                                const double* __restrict__ sc, float* __restrict__ X) {
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    constexpr int F = K - 1;
+    const float* __restrict__ inv = reinterpret_cast<const float*>(sc + 8);
+    const bool fr = freed == nullptr || freed[i];
+#pragma unroll
+    for (int j = 1; j < K; j++) X[i * F + j - 1] = fr ? tab_at(tab, n, j, i).x * inv[j - 1] : 0.f;
+}
+
+// x = u^n + D_1 + ... + D_base (+ S_{K-1} y(X) with the network) on free dofs, u^n elsewhere
+template <int K, bool NET>
+__global__ void __launch_bounds__(256) predict_kernel(int64_t n, const float2* __restrict__ tab,
+                                                      const uint8_t* __restrict__ freed,
+                                                      const double* __restrict__ sc, int base,
+                                                      const float* __restrict__ Pg, int np,
+                                                      double* __restrict__ x) {
+    extern __shared__ float P[];
+    if (NET) {
+        for (int k = threadIdx.x; k < np; k += blockDim.x) P[k] = Pg[k];
+        __syncthreads();
+    }
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    float2 D[K];
+#pragma unroll
+    for (int j = 0; j < K; j++) D[j] = tab_at(tab, n, j, i);
+    if (freed && !freed[i]) {
+        x[i] = ff_to_double(D[0].x, D[0].y);
+        return;
+    }
+    float2 v = D[0];
+#pragma unroll
+    for (int j = 1; j < K; j++)
+        if (j <= base) v = ff_addn(v, D[j], false);
+    if constexpr (NET && K >= 2) {
+        constexpr int F = K - 1;
+        const float* __restrict__ fs = reinterpret_cast<const float*>(sc + 8);
+        float xf[F];
+#pragma unroll
+        for (int j = 1; j <= F; j++) xf[j - 1] = D[j].x * fs[j - 1];
+        v = ff_addn(v, make_float2(fs[8 + F - 1] * mlp_row_f<F>(P, xf), 0.f), false);
+    }
+    x[i] = ff_to_double(v.x, v.y);
+}
+
+// training target T_i = (u^{n+1}_i - u^n_i - D_1 - ... - D_base) / S_{K-1} (0 at constrained dofs)
+template <int K>
+__global__ void target_kernel(int64_t n, const float2* __restrict__ tab, const uint8_t* __restrict__ freed,
+                              const double* __restrict__ sc, int base, const double* __restrict__ unext,
+                              float* __restrict__ T) {
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    if (freed && !freed[i]) {
+        T[i] = 0.f;
+        return;
+    }
+    float2 d = split_d(unext[i]);
+#pragma unroll
+    for (int j = 0; j < K; j++)
+        if (j <= base) d = ff_addn(d, tab_at(tab, n, j, i), true);
+    const float* __restrict__ fs = reinterpret_cast<const float*>(sc + 8);
+    T[i] = fmaxf(-1e6f, fminf(1e6f, __fadd_rn(d.x, d.y) * fs[K >= 2 ? K - 2 : 0]));
+}
+
+// e = S (Y - T) on free dofs, 0 elsewhere
+__global__ void guess_error_kernel(int64_t n, const float* __restrict__ Y, const float* __restrict__ T,
+                                   const double* __restrict__ scale, const uint8_t* __restrict__ freed,
+                                   double* __restrict__ e) {
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    e[i] = (freed == nullptr || freed[i]) ? scale[0] * ((double)Y[i] - (double)T[i]) : 0.0;
+}
+
+// v := v on free rows, 0 elsewhere; out[0] = |v_free|^2, out[1] = |b_free|^2 (deterministic)
+__global__ void __launch_bounds__(256) mask_norms_kernel(int64_t n, double* __restrict__ v,
+                                                         const double* __restrict__ b,
+                                                         const uint8_t* __restrict__ freed,
+                                                         double* __restrict__ part, unsigned* __restrict__ cnt,
+                                                         double* __restrict__ out) {
+    double av = 0, ab = 0;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        if (freed && !freed[i]) {
+            v[i] = 0.0;
+            continue;
+        }
+        const double vi = v[i], bi = b[i];
+        av += vi * vi;
+        ab += bi * bi;
+    }
+    __shared__ double sh[2][8];
+    av = warp_sum_d(av);
+    ab = warp_sum_d(ab);
+    if ((threadIdx.x & 31) == 0) {
+        sh[0][threadIdx.x >> 5] = av;
+        sh[1][threadIdx.x >> 5] = ab;
+    }
+    __syncthreads();
+    if (threadIdx.x < 2) {
+        double t = 0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); w++) t += sh[threadIdx.x][w];
+        part[(int64_t)threadIdx.x * gridDim.x + blockIdx.x] = t;
+    }
+    if (!last_block(cnt)) return;
+    if (threadIdx.x < 2) {
+        double t = 0;
+        for (unsigned b2 = 0; b2 < gridDim.x; b2++) t += __ldcg(part + (int64_t)threadIdx.x * gridDim.x + b2);
+        out[threadIdx.x] = t;
+    }
+}
+
+// dY_i = 2 wt S w_i / |b|^2 on free rows; loss = wt |A e|^2 / |b|^2 into nrm[2]
+__global__ void guess_dy_kernel(int64_t n, const double* __restrict__ w, const double* __restrict__ scale,
+                                const uint8_t* __restrict__ freed, double wt, double* __restrict__ nrm,
+                                float* __restrict__ dY) {
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    const double c = wt / (nrm[1] > 0 ? nrm[1] : 1.0);
+    if (i == 0) nrm[2] = c * nrm[0];
+    if (i >= n) return;
+    dY[i] = (freed == nullptr || freed[i]) ? (float)(2.0 * c * scale[0] * w[i]) : 0.f;
+}
+
+// transpose positions of a structurally symmetric CSR pattern: tpos[k] = position of (col[k], row)
+// in row col[k]; a missing mirror entry raises the flag
+__global__ void tpos_kernel(int64_t n, const int32_t* __restrict__ rp, const int32_t* __restrict__ col,
+                            int32_t* __restrict__ tpos, int* __restrict__ bad) {
+    const int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (r >= n) return;
+    for (int32_t k = rp[r]; k < rp[r + 1]; k++) {
+        const int32_t c = col[k];
+        int32_t lo = rp[c], hi = rp[c + 1] - 1, at = -1;
+        while (lo <= hi) {
+            const int32_t mid = (lo + hi) >> 1;
+            const int32_t v = col[mid];
+            if (v == (int32_t)r) {
+                at = mid;
+                break;
+            }
+            if (v < (int32_t)r) lo = mid + 1;
+            else hi = mid - 1;
+        }
+        tpos[k] = at < 0 ? k : at;
+        if (at < 0) *bad = 1;
+    }
+}
+
+// y = A^T x: row r gathers A[tpos[k]] x[col[k]] (the entries of column r), TPR lanes per row
+template <int TPR>
+__global__ void __launch_bounds__(256) spmv_t_kernel(int64_t n, const int32_t* __restrict__ rp,
+                                                     const int32_t* __restrict__ col,
+                                                     const int32_t* __restrict__ tpos, const double* __restrict__ A,
+                                                     const double* __restrict__ x, double* __restrict__ y) {
+    const int64_t r = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) / TPR;
+    const int lane = threadIdx.x % TPR;
+    double acc = 0;
+    if (r < n)
+        for (int32_t k = rp[r] + lane; k < rp[r + 1]; k += TPR) acc += __ldg(A + __ldg(tpos + k)) * __ldg(x + __ldg(col + k));
+#pragma unroll
+    for (int o = TPR / 2; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o, TPR);
+    if (r < n && lane == 0) y[r] = acc;
 }
 
 }  // namespace
@@ -321,12 +541,15 @@ struct ocmp_guess_s {
     double* loss = nullptr;
     int64_t part_rows = 0;  // capacity (rows) of the partial buffers
     int step = 0;
-    double* spart = nullptr;  // scale reduction partials
+    double* spart = nullptr;  // reduction partials (kRedBlocks x up to kMaxK)
     unsigned* scnt = nullptr;
+    double* nrm = nullptr;    // |A e|^2, |b|^2, loss
+    double* vecs = nullptr;   // residual-loss workspace: e, A e, A^T A e (3 n-vectors)
+    int64_t vec_n = 0;
 };
 
 static void guess_free(ocmp_guess_s* g) {
-    void* ps[] = {g->P, g->G, g->M, g->V, g->Gpart, g->Lpart, g->loss, g->spart, g->scnt};
+    void* ps[] = {g->P, g->G, g->M, g->V, g->Gpart, g->Lpart, g->loss, g->spart, g->scnt, g->nrm, g->vecs};
     for (void* p : ps) dfree(p);
 }
 
@@ -344,6 +567,61 @@ static int ensure_parts(ocmp_guess_s* g, int64_t rows) {
     return OCMP_OK;
 }
 
+static int ensure_vecs(ocmp_guess_s* g, int64_t n) {
+    if (n <= g->vec_n) return OCMP_OK;
+    dfree(g->vecs);
+    g->vecs = nullptr;
+    int st = dalloc(&g->vecs, (size_t)(3 * n));
+    if (st) return st;
+    g->vec_n = n;
+    return OCMP_OK;
+}
+
+static int ensure_tpos(ocmp_space_s* s, cudaStream_t st) {
+    if (s->d_tpos) return OCMP_OK;
+    int* bad = nullptr;
+    int rc = dalloc(&s->d_tpos, (size_t)s->nnz);
+    if (!rc) rc = dalloc(&bad, 1);
+    if (rc) {
+        dfree(bad);
+        return rc;
+    }
+    int hb = 0;
+    OCMP_CUDA(cudaMemsetAsync(bad, 0, sizeof(int), st));
+    OCMP_LAUNCH(tpos_kernel<<<(unsigned)((s->ndof + 255) / 256), 256, 0, st>>>(s->ndof, s->d_rowptr, s->d_col, s->d_tpos,
+                                                                           bad));
+    OCMP_CUDA(cudaMemcpyAsync(&hb, bad, sizeof(int), cudaMemcpyDeviceToHost, st));
+    OCMP_CUDA(cudaStreamSynchronize(st));
+    dfree(bad);
+    if (hb) {
+        dfree(s->d_tpos);
+        s->d_tpos = nullptr;
+        return fail(OCMP_ERR_UNSUPPORTED, "transpose product: the sparsity pattern is not structurally symmetric");
+    }
+    return OCMP_OK;
+}
+
+static int launch_spmv_t(ocmp_space_s* s, const double* A, const double* x, double* y, cudaStream_t st) {
+    int rc = ensure_tpos(s, st);
+    if (rc) return rc;
+    const int64_t n = s->ndof;
+    OCMP_LAUNCH(spmv_t_kernel<4><<<(unsigned)((n * 4 + 255) / 256), 256, 0, st>>>(n, s->d_rowptr, s->d_col, s->d_tpos, A, x,
+                                                                              y));
+    OCMP_CUDA(cudaGetLastError());
+    return OCMP_OK;
+}
+
+// K dispatch (history length 1..6) for a kernel template taking <int K>
+#define OCMP_K_DISPATCH(k, ...)                           \
+    switch (k) {                                          \
+    case 1: { constexpr int KK = 1; __VA_ARGS__; } break;  \
+    case 2: { constexpr int KK = 2; __VA_ARGS__; } break;  \
+    case 3: { constexpr int KK = 3; __VA_ARGS__; } break;  \
+    case 4: { constexpr int KK = 4; __VA_ARGS__; } break;  \
+    case 5: { constexpr int KK = 5; __VA_ARGS__; } break;  \
+    default: { constexpr int KK = 6; __VA_ARGS__; } break; \
+    }
+
 extern "C" {
 
 int ocmp_guess_create(int32_t n_features, uint64_t seed, ocmp_guess_t* out) {
@@ -357,12 +635,16 @@ int ocmp_guess_create(int32_t n_features, uint64_t seed, ocmp_guess_t* out) {
     if (!st) st = dalloc(&g->M, n);
     if (!st) st = dalloc(&g->V, n);
     if (!st) st = dalloc(&g->loss, 1);
+    if (!st) st = dalloc(&g->spart, (size_t)kRedBlocks * kMaxK);
+    if (!st) st = dalloc(&g->scnt, 1);
+    if (!st) st = dalloc(&g->nrm, 4);
     if (st) {
         guess_free(g);
         delete g;
         return st;
     }
-    // Xavier-uniform weights from a 64-bit LCG seeded by `seed`; zero biases; small output layer
+    // Xavier-uniform hidden weights from a 64-bit LCG seeded by `seed`; zero biases; zero output
+    // layer and linear skip, so the untrained network adds nothing to the extrapolation
     std::vector<float> h(n, 0.f);
     uint64_t s = seed * 6364136223846793005ull + 1442695040888963407ull;
     auto rnd = [&]() {
@@ -370,15 +652,14 @@ int ocmp_guess_create(int32_t n_features, uint64_t seed, ocmp_guess_t* out) {
         return (double)(s >> 11) * (1.0 / 9007199254740992.0);
     };
     const Layout& L = g->L;
-    const double a1 = std::sqrt(6.0 / (n_features + kH)), a2 = std::sqrt(6.0 / (2 * kH)), a3 = 0.1;
+    const double a1 = std::sqrt(6.0 / (n_features + kH)), a2 = std::sqrt(6.0 / (2 * kH));
     for (int k = 0; k < kH * n_features; k++) h[L.W1 + k] = (float)((2 * rnd() - 1) * a1);
     for (int k = 0; k < kH * kH; k++) h[L.W2 + k] = (float)((2 * rnd() - 1) * a2);
-    for (int k = 0; k < kH; k++) h[L.w3 + k] = (float)((2 * rnd() - 1) * a3);
-    if (n_features >= 1) h[L.c] = 1.f;  // start from the previous-difference guess u^n + (u^n - u^{n-1})
     std::vector<float> z(n, 0.f);
     if (cudaMemcpy(g->P, h.data(), sizeof(float) * n, cudaMemcpyHostToDevice) != cudaSuccess ||
         cudaMemcpy(g->M, z.data(), sizeof(float) * n, cudaMemcpyHostToDevice) != cudaSuccess ||
-        cudaMemcpy(g->V, z.data(), sizeof(float) * n, cudaMemcpyHostToDevice) != cudaSuccess) {
+        cudaMemcpy(g->V, z.data(), sizeof(float) * n, cudaMemcpyHostToDevice) != cudaSuccess ||
+        cudaMemset(g->scnt, 0, sizeof(unsigned)) != cudaSuccess) {
         guess_free(g);
         delete g;
         return fail(OCMP_ERR_CUDA, "ocmp_guess_create: upload failed");
@@ -418,23 +699,43 @@ int ocmp_guess_forward(ocmp_guess_t g, const float* X, int64_t rows, float* Y, v
     return OCMP_OK;
 }
 
-int ocmp_guess_loss_grad(ocmp_guess_t g, const float* X, const float* T, int64_t rows, double* loss_host,
-                         float* grad_host, void* stream) {
-    if (!g || !X || !T || rows <= 0) return fail(OCMP_ERR_ARG, "ocmp_guess_loss_grad: bad argument");
+static int grad_launch(ocmp_guess_t g, const float* X, const float* T, const float* dY, int64_t rows,
+                       cudaStream_t s) {
     int st = ensure_parts(g, rows);
     if (st) return st;
-    cudaStream_t s = (cudaStream_t)stream;
     const int nb = (int)((rows + kRowsPerBlock - 1) / kRowsPerBlock);
     const size_t smem = sizeof(double) * kRowsPerBlock + sizeof(float) * (g->L.n + kRowsPerBlock * (4 * kH + kMaxF + 1));
     OCMP_CUDA(cudaFuncSetAttribute(mlp_grad_partial_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    OCMP_LAUNCH(mlp_grad_partial_kernel<<<nb, kRowsPerBlock, smem, s>>>(rows, g->F, g->P, X, T, g->Gpart, g->Lpart));
+    OCMP_LAUNCH(mlp_grad_partial_kernel<<<nb, kRowsPerBlock, smem, s>>>(rows, g->F, g->P, X, T, dY, g->Gpart, g->Lpart));
     OCMP_LAUNCH(mlp_grad_reduce_kernel<<<(g->L.n + 255) / 256, 256, 0, s>>>(nb, g->L.n, g->Gpart, g->G, g->Lpart, (int64_t)nb,
                                                                 g->loss));
     OCMP_CUDA(cudaGetLastError());
+    return OCMP_OK;
+}
+
+int ocmp_guess_loss_grad(ocmp_guess_t g, const float* X, const float* T, int64_t rows, double* loss_host,
+                         float* grad_host, void* stream) {
+    if (!g || !X || !T || rows <= 0) return fail(OCMP_ERR_ARG, "ocmp_guess_loss_grad: bad argument");
+    cudaStream_t s = (cudaStream_t)stream;
+    int st = grad_launch(g, X, T, nullptr, rows, s);
+    if (st) return st;
     if (loss_host) {
         OCMP_CUDA(cudaMemcpyAsync(loss_host, g->loss, sizeof(double), cudaMemcpyDeviceToHost, s));
         OCMP_CUDA(cudaStreamSynchronize(s));
     }
+    if (grad_host) {
+        OCMP_CUDA(cudaMemcpyAsync(grad_host, g->G, sizeof(float) * g->L.n, cudaMemcpyDeviceToHost, s));
+        OCMP_CUDA(cudaStreamSynchronize(s));
+    }
+    return OCMP_OK;
+}
+
+int ocmp_guess_backward(ocmp_guess_t g, const float* X, const float* dY, int64_t rows, float* grad_host,
+                        void* stream) {
+    if (!g || !X || !dY || rows <= 0) return fail(OCMP_ERR_ARG, "ocmp_guess_backward: bad argument");
+    cudaStream_t s = (cudaStream_t)stream;
+    int st = grad_launch(g, X, nullptr, dY, rows, s);
+    if (st) return st;
     if (grad_host) {
         OCMP_CUDA(cudaMemcpyAsync(grad_host, g->G, sizeof(float) * g->L.n, cudaMemcpyDeviceToHost, s));
         OCMP_CUDA(cudaStreamSynchronize(s));
@@ -453,71 +754,97 @@ int ocmp_guess_adam_step(ocmp_guess_t g, float lr, void* stream) {
     return OCMP_OK;
 }
 
-int ocmp_guess_features(int64_t n, int32_t k, const double* const* hist, const double* q, double* scale,
-                        float* X, int32_t F, void* stream) {
-    if (!hist || !X || !scale || n < 0 || k < 2 || k > 4 || F < 1 || F > kMaxF)
-        return fail(OCMP_ERR_ARG, "ocmp_guess_features: bad argument");
-    for (int d = 0; d < k; d++)
-        if (!hist[d]) return fail(OCMP_ERR_ARG, "ocmp_guess_features: null history vector");
+int ocmp_guess_push(int64_t n, int32_t k, int32_t m, float* tab, const double* u, void* stream) {
+    if (!tab || !u || n < 0 || k < 1 || k > kMaxK || m < 0 || m > k)
+        return fail(OCMP_ERR_ARG, "ocmp_guess_push: bad argument (table of 1..6 rows, 0 <= m <= k)");
     if (n == 0) return OCMP_OK;
-    OCMP_LAUNCH(features_kernel<<<(unsigned)((n + 255) / 256), 256, 0, (cudaStream_t)stream>>>(
-        n, k, hist[0], k > 1 ? hist[1] : hist[0], k > 2 ? hist[2] : hist[0], k > 3 ? hist[3] : hist[0], q, scale, X,
-        F));
+    OCMP_LAUNCH(push_kernel<<<(unsigned)((n + 255) / 256), 256, 0, (cudaStream_t)stream>>>(
+        n, k, m, reinterpret_cast<float2*>(tab), u));
     OCMP_CUDA(cudaGetLastError());
     return OCMP_OK;
 }
 
-int ocmp_guess_apply(int64_t n, const double* un, const float* y, const double* scale, const uint8_t* freed,
-                     double* x, void* stream) {
-    if (!un || !y || !x || !scale || n < 0) return fail(OCMP_ERR_ARG, "ocmp_guess_apply: bad argument");
-    if (n == 0) return OCMP_OK;
-    OCMP_LAUNCH(apply_kernel<<<(unsigned)((n + 255) / 256), 256, 0, (cudaStream_t)stream>>>(n, un, y, scale, freed, x));
-    OCMP_CUDA(cudaGetLastError());
-    return OCMP_OK;
-}
-
-int ocmp_guess_target(int64_t n, const double* unext, const double* un, const double* scale, float* T,
-                      void* stream) {
-    if (!unext || !un || !scale || !T || n < 0) return fail(OCMP_ERR_ARG, "ocmp_guess_target: bad argument");
-    if (n == 0) return OCMP_OK;
-    OCMP_LAUNCH(target_kernel<<<(unsigned)((n + 255) / 256), 256, 0, (cudaStream_t)stream>>>(n, unext, un, scale, T));
-    OCMP_CUDA(cudaGetLastError());
-    return OCMP_OK;
-}
-
-int ocmp_guess_scale(ocmp_guess_t g, int64_t n, const double* a, const double* b, double* scale, void* stream) {
-    if (!g || !a || !b || !scale || n < 0) return fail(OCMP_ERR_ARG, "ocmp_guess_scale: bad argument");
-    const int nb = 304;
-    if (!g->spart) {
-        int st = dalloc(&g->spart, nb);
-        if (!st) st = dalloc(&g->scnt, 1);
-        if (st) return st;
-        OCMP_CUDA(cudaMemset(g->scnt, 0, sizeof(unsigned)));
-    }
-    OCMP_LAUNCH(rms_diff_kernel<<<nb, 256, 0, (cudaStream_t)stream>>>(n, a, b, g->spart, g->scnt, scale));
-    OCMP_CUDA(cudaGetLastError());
-    return OCMP_OK;
-}
-
-int ocmp_jacobi_residual(ocmp_matrix_t mat, const double* b, const double* x, double* q, void* stream) {
-    if (!mat || !b || !x || !q) return fail(OCMP_ERR_ARG, "ocmp_jacobi_residual: null argument");
-    const ocmp_space_s* s = mat->space;
-    const RowCfg rc = row_cfg(s);
-    const int64_t n = s->ndof;
-    const unsigned g = (unsigned)((n * rc.tpr + 255) / 256);
+int ocmp_guess_features(ocmp_guess_t g, int64_t n, int32_t k, const float* tab, const uint8_t* freed,
+                        double* scales, float* X, void* stream) {
+    if (!g || !tab || !scales || n < 0 || k < 2 || k > kMaxK)
+        return fail(OCMP_ERR_ARG, "ocmp_guess_features: bad argument (table of 2..6 rows)");
+    if (X && g->F != k - 1) return fail(OCMP_ERR_ARG, "ocmp_guess_features: the network takes F = k - 1 features");
     cudaStream_t st = (cudaStream_t)stream;
-#define JR(TPR, U)                                                                                                    \
-    OCMP_LAUNCH(jacobi_resid_kernel<TPR, U><<<g, 256, 0, st>>>(n, s->d_rowptr, s->d_col, mat->vals, mat->dinv, s->d_diag, s->d_free, \
-                                                   b, x, q))
-    if (rc.tpr == 2) JR(2, 4);
-    else if (rc.tpr == 4 && rc.u == 4) JR(4, 4);
-    else if (rc.tpr == 4) JR(4, 8);
-    else if (rc.tpr == 8 && rc.u == 4) JR(8, 4);
-    else if (rc.tpr == 8) JR(8, 8);
-    else JR(16, 8);
-#undef JR
+    const float2* T2 = reinterpret_cast<const float2*>(tab);
+    OCMP_K_DISPATCH(k, OCMP_LAUNCH(hist_scales_kernel<KK><<<kRedBlocks, 256, 0, st>>>(n, T2, freed, g->spart, g->scnt, scales)));
+    if (X && n > 0)
+        OCMP_K_DISPATCH(k, OCMP_LAUNCH(features_kernel<KK><<<(unsigned)((n + 255) / 256), 256, 0, st>>>(n, T2, freed, scales, X)));
     OCMP_CUDA(cudaGetLastError());
     return OCMP_OK;
+}
+
+int ocmp_guess_predict(ocmp_guess_t g, int64_t n, int32_t k, const float* tab, const uint8_t* freed,
+                       const double* scales, int32_t base_order, double* x, void* stream) {
+    if (!x || !tab || n < 0 || k < 1 || k > kMaxK || base_order < 0 || base_order > k - 1)
+        return fail(OCMP_ERR_ARG, "ocmp_guess_predict: bad argument (table of 1..6 rows, base order < k)");
+    if (g && (k < 2 || !scales || g->F != k - 1))
+        return fail(OCMP_ERR_ARG, "ocmp_guess_predict: the network needs k = F + 1 >= 2 and the history scales");
+    if (n == 0) return OCMP_OK;
+    cudaStream_t st = (cudaStream_t)stream;
+    const float2* T2 = reinterpret_cast<const float2*>(tab);
+    const unsigned nb = (unsigned)((n + 255) / 256);
+    if (g) {
+        OCMP_K_DISPATCH(k, OCMP_LAUNCH(predict_kernel<KK, true><<<nb, 256, sizeof(float) * g->L.n, st>>>(
+                               n, T2, freed, scales, base_order, g->P, g->L.n, x)));
+    } else {
+        OCMP_K_DISPATCH(k, OCMP_LAUNCH(predict_kernel<KK, false><<<nb, 256, 0, st>>>(n, T2, freed, scales, base_order,
+                                                                                nullptr, 0, x)));
+    }
+    OCMP_CUDA(cudaGetLastError());
+    return OCMP_OK;
+}
+
+int ocmp_guess_target(int64_t n, int32_t k, const float* tab, const uint8_t* freed, const double* scales,
+                      int32_t base_order, const double* unext, float* T, void* stream) {
+    if (!unext || !T || !scales || !tab || n < 0 || k < 2 || k > kMaxK || base_order < 0 || base_order > k - 1)
+        return fail(OCMP_ERR_ARG, "ocmp_guess_target: bad argument");
+    if (n == 0) return OCMP_OK;
+    cudaStream_t st = (cudaStream_t)stream;
+    const float2* T2 = reinterpret_cast<const float2*>(tab);
+    OCMP_K_DISPATCH(k, OCMP_LAUNCH(target_kernel<KK><<<(unsigned)((n + 255) / 256), 256, 0, st>>>(n, T2, freed, scales,
+                                                                                           base_order, unext, T)));
+    OCMP_CUDA(cudaGetLastError());
+    return OCMP_OK;
+}
+
+int ocmp_guess_residual_loss(ocmp_guess_t g, ocmp_matrix_t mat, const float* Y, const float* T, const double* scale,
+                             const double* b, double weight, double* loss_host, float* dY, void* stream) {
+    if (!g || !mat || !Y || !T || !scale || !b || !dY) return fail(OCMP_ERR_ARG, "ocmp_guess_residual_loss: null argument");
+    if (mat->B != 1) return fail(OCMP_ERR_ARG, "ocmp_guess_residual_loss: batched matrix");
+    ocmp_space_s* s = mat->space;
+    const int64_t n = s->ndof;
+    cudaStream_t st = (cudaStream_t)stream;
+    int rc = ensure_vecs(g, n);
+    if (!rc) rc = ensure_tpos(s, st);
+    if (rc) return rc;
+    double* e = g->vecs;
+    double* v = g->vecs + n;
+    double* w = g->vecs + 2 * n;
+    const unsigned nb = (unsigned)((n + 255) / 256);
+    OCMP_LAUNCH(guess_error_kernel<<<nb, 256, 0, st>>>(n, Y, T, scale, s->d_free, e));
+    rc = launch_spmv64(s, mat->vals, e, v, st);
+    if (rc) return rc;
+    OCMP_LAUNCH(mask_norms_kernel<<<kRedBlocks, 256, 0, st>>>(n, v, b, s->d_free, g->spart, g->scnt, g->nrm));
+    rc = launch_spmv_t(s, mat->vals, v, w, st);
+    if (rc) return rc;
+    OCMP_LAUNCH(guess_dy_kernel<<<nb, 256, 0, st>>>(n, w, scale, s->d_free, weight, g->nrm, dY));
+    OCMP_CUDA(cudaGetLastError());
+    if (loss_host) {
+        OCMP_CUDA(cudaMemcpyAsync(loss_host, g->nrm + 2, sizeof(double), cudaMemcpyDeviceToHost, st));
+        OCMP_CUDA(cudaStreamSynchronize(st));
+    }
+    return OCMP_OK;
+}
+
+int ocmp_spmv_transpose(ocmp_matrix_t mat, const double* x, double* y, void* stream) {
+    if (!mat || !x || !y) return fail(OCMP_ERR_ARG, "ocmp_spmv_transpose: null argument");
+    if (mat->B != 1) return fail(OCMP_ERR_ARG, "ocmp_spmv_transpose: batched matrix");
+    return launch_spmv_t(mat->space, mat->vals, x, y, (cudaStream_t)stream);
 }
 
 }  // extern "C"

@@ -128,9 +128,14 @@ struct ocmp_space_s {
     int32_t* d_ebf = nullptr;
     int32_t* d_lift_ptr = nullptr;  // ndof+1: per free row, CSR positions whose column is constrained
     int32_t* d_lift_pos = nullptr;
+    int32_t* d_tpos = nullptr;      // nnz: position of the mirror entry (col, row), built on first use
     double* d_Rc = nullptr;         // R_const
     float2* d_Rm_ff = nullptr;      // reference mass matrix as (hi, lo) float pairs
     float2* d_geo_ff = nullptr;     // static element geometry for the double-float element kernel
+    float2* d_u2 = nullptr;         // ndof: a vector split into (hi, lo) float pairs (right-hand sides)
+    int32_t* d_cseg = nullptr;      // nnz+1: per CSR entry, its run in d_csrc (built on first use)
+    int32_t* d_csrc = nullptr;      // ne*nloc^2: element-matrix entries (e*nloc + i)*nloc + j per CSR entry,
+                                    // in incidence order
     double* d_Rv = nullptr;         // R_vtx
     double* d_qw = nullptr;
     double* d_qphi = nullptr;

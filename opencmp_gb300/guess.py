@@ -1,19 +1,26 @@
 """Learned Krylov initial guess for implicit time stepping.
 
 OpenCMP starts each step's Krylov solve from the previous step's solution
-(``opencmp/models/base_model.py:925-937``). :class:`LearnedGuess` replaces that start by
-``u^n + scale * MLP(features)``, where, per dof, the features are the last k-1 solution differences
-and the Jacobi correction ``D^-1 (b - A u^n)`` of the previous-step guess, all divided by the norm
-of that dof's differences. The network (``ocmp_guess_*`` in ``csrc/ocmp_guess.cu``) is trained on
-trajectories the solver itself produced, with the library's own forward, backward and Adam
-kernels. The solve still runs to the same FP64 residual tolerance, so the guess only changes how
-many iterations that takes; if a prediction starts worse than the previous step's solution would
-have, the run falls back to the previous-step guess.
+(``opencmp/models/base_model.py:925-937``). :class:`LearnedGuess` starts it from
+
+    x = u^n + D_1 + ... + D_p  +  S_{k-1} * MLP(D_1 / S_1, ..., D_{k-1} / S_{k-1}),
+
+where D_j is the j-th backward difference in time of the last k solutions at a dof and S_j its
+root mean square over the free dofs: the degree-p extrapolation in time plus a per-dof network's
+correction (``ocmp_guess_*`` in ``csrc/ocmp_guess.cu``). The history is kept on the device as the
+table of backward differences itself, in double-float (pairs of FP32 values). The network is trained on trajectories
+the solver itself produced, with the library's own forward, backward and Adam kernels, to minimise
+the FP64 relative residual its guess leaves (|A e| / |b|, through A and its transpose).
+
+The extrapolation alone is the fallback: it is used until the history is full and the network is
+trained, and for the rest of a run once the judge (:meth:`LearnedGuess.judge`) sees the network's
+guess start a solve no better than the extrapolation did. The solve always runs to the same FP64
+residual tolerance, so the guess only changes how many iterations that takes.
 """
 from __future__ import annotations
 
 import ctypes as C
-from typing import List, Optional
+from typing import Dict, List
 
 import numpy as np
 import torch
@@ -21,9 +28,12 @@ import torch
 from . import _lib as LB
 from .fem import Matrix, Space, _ptr, _stream
 
+NET, PROBE, FALLBACK = 'network', 'probe', 'fallback'
+
 
 class GuessNet:
-    """The per-dof MLP (hidden width 32, FP32) and its Adam state on the device."""
+    """The per-dof MLP (hidden width 16, FP32) and its Adam state on the device. A new network has
+    zero output: its output layer and linear skip start at zero."""
 
     def __init__(self, n_features: int, seed: int = 0):
         h = C.c_void_p()
@@ -50,143 +60,168 @@ class GuessNet:
         LB.call('ocmp_guess_forward', self.h, _ptr(X), X.shape[0], _ptr(Y), _stream(stream))
 
     def loss_grad(self, X: torch.Tensor, T: torch.Tensor, want_grad: bool = False, stream=None):
+        """Mean squared error against T and its parameter gradient."""
         loss = C.c_double(0)
         g = np.empty(self.nparams, np.float32) if want_grad else None
         LB.call('ocmp_guess_loss_grad', self.h, _ptr(X), _ptr(T), X.shape[0], C.byref(loss),
                 _ptr(g) if want_grad else None, _stream(stream))
         return loss.value, g
 
+    def backward(self, X: torch.Tensor, dY: torch.Tensor, want_grad: bool = False, stream=None):
+        """Parameter gradient of sum_r dY_r y_r (kept on the device for :meth:`adam_step`)."""
+        g = np.empty(self.nparams, np.float32) if want_grad else None
+        LB.call('ocmp_guess_backward', self.h, _ptr(X), _ptr(dY), X.shape[0], _ptr(g) if want_grad else None,
+                _stream(stream))
+        return g
+
     def adam_step(self, lr: float, stream=None):
         LB.call('ocmp_guess_adam_step', self.h, C.c_float(lr), _stream(stream))
 
 
 class LearnedGuess:
-    """History of the last ``k`` solutions on the device and the network that extrapolates them."""
+    """History of the last ``k`` solutions on the device, the degree-``base_order`` extrapolation and
+    the network that corrects it (``k - 1`` features)."""
 
-    def __init__(self, space: Space, k: int = 4, use_residual: bool = True, seed: int = 0):
-        if not 2 <= k <= 4:
-            raise ValueError('k must be 2..4')
+    def __init__(self, space: Space, k: int = 5, base_order: int = 3, seed: int = 0):
+        if not 2 <= k <= 6:
+            raise ValueError('k must be 2..6')
+        if not 0 <= base_order < k:
+            raise ValueError('base_order must be 0..k-1')
         self.space = space
         self.n = space.ndof
         self.k = k
-        self.use_q = use_residual
-        self.F = (k - 1) + (1 if use_residual else 0)
+        self.base_order = base_order
+        self.F = k - 1
         self.net = GuessNet(self.F, seed)
         dev = 'cuda'
-        self.hist: List[torch.Tensor] = []
-        self._ring = [torch.zeros(self.n, dtype=torch.float64, device=dev) for _ in range(k)]
-        self._head = 0
+        self.m = 0  # valid rows of the difference table
+        self.tab = torch.zeros(k, self.n, 2, dtype=torch.float32, device=dev)
         self.X = torch.empty(self.n, self.F, dtype=torch.float32, device=dev)
         self.Y = torch.empty(self.n, dtype=torch.float32, device=dev)
-        self.q = torch.empty(self.n, dtype=torch.float64, device=dev)
-        self.scale = torch.ones(self.n, dtype=torch.float64, device=dev)
+        self.dY = torch.empty(self.n, dtype=torch.float32, device=dev)
+        self.scales = torch.ones(32, dtype=torch.float64, device=dev)
         self._free = torch.as_tensor(space.FreeDofs().astype(np.uint8), device=dev)
-        self.samples_X: List[torch.Tensor] = []
-        self.samples_T: List[torch.Tensor] = []
+        self.samples: List[Dict] = []
+        self.trained = False
         self.enabled = True
         self.judge_window = 3
-        self._base_it: List[int] = []
-        self._base_r0: List[float] = []
-        self._net_it: List[int] = []
         self.fallback_reason = None
+        self.reset_judge()
 
     # ---------------------------------------------------------------- history
     def reset(self):
-        self.hist = []
+        self.m = 0
 
-    def push(self, u: torch.Tensor):
-        """Record the newest solution (copied into the device ring)."""
-        buf = self._ring[self._head]
-        buf.copy_(u)
-        self._head = (self._head + 1) % self.k
-        self.hist = [buf] + self.hist[:self.k - 1]
+    def push(self, u: torch.Tensor, stream=None):
+        """Add the newest solution to the difference table."""
+        LB.call('ocmp_guess_push', self.n, self.k, self.m, _ptr(self.tab), _ptr(u), _stream(stream))
+        self.m = min(self.m + 1, self.k)
 
     @property
     def ready(self) -> bool:
-        return len(self.hist) >= self.k
+        return self.m >= self.k
 
-    # ---------------------------------------------------------------- features / prediction
-    def _features(self, A: Optional[Matrix], b: Optional[torch.Tensor], stream=None):
-        L = LB.load()
-        st = _stream(stream)
-        h = self.hist
-        qp = None
-        if self.use_q:
-            LB.check(L.ocmp_jacobi_residual(A.h, _ptr(b), _ptr(h[0]), _ptr(self.q), st))
-            qp = _ptr(self.q)
-        arr = (C.c_void_p * 4)(*[C.c_void_p(t.data_ptr()) for t in h[:self.k]] + [None] * (4 - self.k))
-        LB.check(L.ocmp_guess_features(self.n, self.k, arr, qp, _ptr(self.scale), _ptr(self.X), self.F, st))
+    # ---------------------------------------------------------------- prediction
+    def _scales(self, X=None, stream=None):
+        LB.call('ocmp_guess_features', self.net.h, self.n, self.k, _ptr(self.tab), _ptr(self._free),
+                _ptr(self.scales), _ptr(X), _stream(stream))
 
-    def predict(self, x: torch.Tensor, A: Optional[Matrix] = None, b: Optional[torch.Tensor] = None, stream=None):
-        """x = u^n + scale * MLP(features); falls back to x = u^n until the history is full."""
-        if not (self.ready and self.enabled):
-            x.copy_(self.hist[0] if self.hist else x)
-            return False
-        self._features(A, b, stream)
-        self.net.forward(self.X, self.Y, stream)
-        LB.check(LB.load().ocmp_guess_apply(self.n, _ptr(self.hist[0]), _ptr(self.Y), _ptr(self.scale),
-                                            _ptr(self._free), _ptr(x), _stream(stream)))
-        return True
+    def extrapolate(self, x: torch.Tensor, order=None, stream=None):
+        """The fallback: x = u^n + D_1 + ... + D_p with p = min(order, history - 1)."""
+        if self.m == 0:
+            raise RuntimeError('no history')
+        p = min(self.base_order if order is None else order, self.m - 1)
+        LB.call('ocmp_guess_predict', None, self.n, self.m, _ptr(self.tab), _ptr(self._free), None, p, _ptr(x),
+                _stream(stream))
 
-    def judge(self, info, used: bool):
-        """Convergence is the guess's judge. Steps solved from the previous-step guess set the
-        baseline (iterations, initial residual); the network is switched off for the rest of the run
-        if one of its guesses starts worse than that baseline, or if over ``judge_window`` steps it
-        does not reduce the Krylov iterations."""
-        if not used:
+    def predict(self, x: torch.Tensor, stream=None) -> str:
+        """Writes the guess into x; returns which guess it was: ``'network'``, ``'probe'`` (the
+        extrapolation, solved once after each judge reset to set the judge's baseline) or
+        ``'fallback'`` (the extrapolation)."""
+        if not (self.ready and self.enabled and self.trained):
+            self.extrapolate(x, stream=stream)
+            return FALLBACK
+        if self._probe_pending:
+            self.extrapolate(x, stream=stream)
+            self._probe_pending = False
+            return PROBE
+        self._scales(stream=stream)
+        LB.call('ocmp_guess_predict', self.net.h, self.n, self.k, _ptr(self.tab), _ptr(self._free),
+                _ptr(self.scales), self.base_order, _ptr(x), _stream(stream))
+        return NET
+
+    def judge(self, info, kind: str):
+        """Convergence is the guess's judge. The probe step, solved from the extrapolation, sets the
+        baseline (initial FP64 residual, iterations); the network is switched off for the rest of
+        the run if one of its guesses starts the solve with a larger residual than that, or if over
+        ``judge_window`` steps it does not save Krylov iterations (its evaluation costs time)."""
+        if kind == PROBE:
             self._base_it.append(info.iterations)
             self._base_r0.append(info.relres0)
             return
-        self._net_it.append(info.iterations)
-        if not self._base_it:
+        if kind != NET or not self._base_it:
             return
+        self._net_it.append(info.iterations)
         if info.relres0 > np.mean(self._base_r0):
-            self.enabled, self.fallback_reason = False, 'initial residual above the previous-step guess'
+            self.enabled, self.fallback_reason = False, 'initial residual above the extrapolation'
         elif len(self._net_it) >= self.judge_window and \
-                np.mean(self._net_it[-self.judge_window:]) >= np.mean(self._base_it[-self.judge_window:]):
-            self.enabled, self.fallback_reason = False, 'no fewer Krylov iterations than the previous-step guess'
+                np.mean(self._net_it[-self.judge_window:]) >= np.mean(self._base_it):
+            self.enabled, self.fallback_reason = False, 'no fewer Krylov iterations than the extrapolation'
 
     def reset_judge(self):
         self.enabled = True
+        self._probe_pending = True
         self._base_it, self._base_r0, self._net_it = [], [], []
         self.fallback_reason = None
 
     # ---------------------------------------------------------------- training
-    def collect(self, u_next: torch.Tensor, A: Optional[Matrix] = None, b: Optional[torch.Tensor] = None):
-        """Store one training sample: features at step n and target (u^{n+1} - u^n) / scale."""
+    def collect(self, u_next: torch.Tensor, A: Matrix, b: torch.Tensor):
+        """Store one training sample from a solved step: features and target of the history before
+        it, the step's matrix A (kept by reference: it must keep these values until training ends)
+        and right-hand side b. The sample's weight makes the extrapolation's loss 1."""
         if not self.ready:
             return
-        self._features(A, b)
+        X = torch.empty(self.n, self.F, dtype=torch.float32, device='cuda')
+        self._scales(X)
         T = torch.empty(self.n, dtype=torch.float32, device='cuda')
-        LB.check(LB.load().ocmp_guess_target(self.n, _ptr(u_next), _ptr(self.hist[0]), _ptr(self.scale), _ptr(T),
-                                             _stream(None)))
-        self.samples_X.append(self.X.clone())
-        self.samples_T.append(T)
+        LB.call('ocmp_guess_target', self.n, self.k, _ptr(self.tab), _ptr(self._free), _ptr(self.scales),
+                self.base_order, _ptr(u_next), _ptr(T), _stream(None))
+        smp = dict(X=X, T=T, S=self.scales[self.F - 1:self.F].clone(), A=A, b=b.clone(), w=1.0)
+        self.Y.zero_()
+        base = self._loss(smp, self.Y, want_grad=False)
+        smp['w'] = 1.0 / base if base > 0 else 1.0
+        smp['r0_extrap'] = float(np.sqrt(base))
+        self.samples.append(smp)
 
-    def train(self, steps: int = 300, batch: int = 1 << 17, lr: float = 3e-3, seed: int = 0) -> List[float]:
-        """Adam on random contiguous row windows of the stored samples; returns the loss history."""
-        if not self.samples_X:
+    def _loss(self, smp, Y, want_grad=True) -> float:
+        loss = C.c_double(0)
+        LB.call('ocmp_guess_residual_loss', self.net.h, smp['A'].h, _ptr(Y), _ptr(smp['T']), _ptr(smp['S']),
+                _ptr(smp['b']), smp['w'], C.byref(loss), _ptr(self.dY), _stream(None))
+        return loss.value
+
+    def train(self, steps: int = 300, lr: float = 3e-3, seed: int = 0) -> List[float]:
+        """Adam over the stored samples (one whole step per iteration, cosine learning rate) on the
+        weighted residual loss; returns the loss history (1 = the extrapolation's residual)."""
+        if not self.samples:
             raise RuntimeError('no training samples collected')
         rng = np.random.default_rng(seed)
         losses = []
         for it in range(steps):
-            s = int(rng.integers(len(self.samples_X)))
-            nb = min(batch, self.n)
-            off = int(rng.integers(0, self.n - nb + 1))
-            X = self.samples_X[s][off:off + nb]
-            T = self.samples_T[s][off:off + nb]
-            loss, _ = self.net.loss_grad(X, T)
+            smp = self.samples[int(rng.integers(len(self.samples)))]
+            self.net.forward(smp['X'], self.Y)
+            losses.append(self._loss(smp, self.Y))
+            self.net.backward(smp['X'], self.dY)
             self.net.adam_step(lr * (0.5 * (1 + np.cos(np.pi * it / steps))) + 1e-5)
-            losses.append(loss)
+        self.trained = True
         return losses
 
     def eval_loss(self) -> float:
-        """Mean loss of the network over every stored sample (all rows)."""
+        """Mean weighted residual loss of the network over the stored samples (1 = extrapolation)."""
         tot = 0.0
-        for X, T in zip(self.samples_X, self.samples_T):
-            tot += self.net.loss_grad(X, T)[0]
-        return tot / max(1, len(self.samples_X))
+        for smp in self.samples:
+            self.net.forward(smp['X'], self.Y)
+            tot += self._loss(smp, self.Y)
+        return tot / max(1, len(self.samples))
 
     def drop_samples(self):
-        self.samples_X.clear()
-        self.samples_T.clear()
+        self.samples.clear()

@@ -45,6 +45,13 @@ class Solver:
         self.check_error = config.get_item(['ERROR ANALYSIS', 'check_error'], bool)
         self.t = 0.0
         self.infos = []
+        # new [SOLVER] key: the Krylov start of each transient step, 'previous' (OpenCMP's: the last
+        # solution) or 'extrapolated' (cubic extrapolation in time of the last solutions, the
+        # fallback of the learned guess; used for fixed-step schemes, restarted when dt changes)
+        self.guess_mode = config.get_item(['SOLVER', 'initial_guess'], str).strip().lower()
+        if self.guess_mode not in ('previous', 'extrapolated'):
+            raise NotImplementedError('initial_guess {!r} is not on the GPU path (previous or extrapolated)'.format(
+                self.guess_mode))
 
     def _solve_var(self, v, theta: float, dt: float, t_new: float, t_old: float, transient: bool,
                    u_from=None, u_to=None):
@@ -54,6 +61,9 @@ class Solver:
         uprev = (v.u if u_from is None else u_from).clone() if transient else None
         if uprev is not None and u_to.data_ptr() != uprev.data_ptr():
             u_to.copy_(uprev)
+        g = self._guess(v, dt, uprev) if transient else None
+        if g is not None:
+            g.extrapolate(u_to)
         v.set_dirichlet(t_new, u_to)
         mass = 1.0 if transient else 0.0
         v.mat.assemble(m.form(v, mass, theta * dt, dt))
@@ -72,8 +82,25 @@ class Solver:
             del keep0
         info = v.solve(u_to)
         del keep
+        if g is not None:
+            g.push(u_to)
         self.infos.append(info)
         return info
+
+    def _guess(self, v, dt, uprev):
+        """The variable's extrapolation history (None for the previous-step guess); restarted from
+        u^n when the step size changes, since the extrapolation assumes equal steps."""
+        if self.guess_mode != 'extrapolated' or not getattr(self, 'fixed_step', False):
+            return None
+        from .guess import LearnedGuess
+        g = getattr(v, 'guess', None)
+        if g is None:
+            g = v.guess = LearnedGuess(v.space, k=4, base_order=3)
+        if getattr(v, 'guess_dt', None) != dt or g.m == 0:
+            g.reset()
+            g.push(uprev)
+            v.guess_dt = dt
+        return g
 
     def _step(self, theta: float, dt: float, t_new: float, t_old: float, transient: bool):
         if hasattr(self.model, 'step'):
@@ -98,6 +125,8 @@ class StationarySolver(Solver):
 
 
 class TransientMultiStepSolver(Solver):
+    fixed_step = True
+
     def __init__(self, model_class, config):
         super().__init__(model_class, config)
         self.scheme = config.get_item(['TRANSIENT', 'scheme'], str)
@@ -149,6 +178,8 @@ class AdaptiveSolver(TransientMultiStepSolver):
       two step   (adaptive_two_step.py): Crank-Nicolson predictor, implicit-Euler corrector (kept);
       three step (adaptive_three_step.py): one implicit-Euler step of dt against two of dt/2 (kept);
                  a rejected attempt repeats with dt/2 (base_adaptive_transient_RK.py)."""
+
+    fixed_step = False  # attempts of different dt: the step history does not extrapolate
 
     def __init__(self, model_class, config):
         Solver.__init__(self, model_class, config)

@@ -305,3 +305,25 @@ def test_config_copied_from_another_parser():
     assert c.get_item(['TRANSIENT', 'dt'], float) == 0.01
     assert c.get_dict(['FINITE ELEMENT SPACE', 'elements'], all_str=True)['b'] == 'H1'
     assert c.get_dict(['SOLVER', 'nonlinear_tolerance'])['absolute'] == 1e-8
+
+
+@pytest.mark.gpu
+def test_extrapolated_initial_guess_through_run(gpu_lib):
+    """The [SOLVER] initial_guess = extrapolated key on a transient reference fixture: the same
+    solution (both solves stop at the same FP64 relative residual) from fewer Krylov iterations
+    than OpenCMP's previous-step start."""
+    from opencmp_gb300.run import run
+    case = next(c.values[0] for c in CASES if not c.marks and c.values[0]['fixture'] == 'poisson_transient_coarse'
+                and _scheme(c.values[0]) == 'implicit euler')
+    res = {}
+    for mode in ('previous', 'extrapolated'):
+        cfg = _load(case)
+        if not cfg.has_section('SOLVER'):
+            cfg.add_section('SOLVER')
+        cfg['SOLVER']['initial_guess'] = mode
+        solver, sol = run('', cfg)
+        res[mode] = (sum(i.iterations for i in solver.infos), {k: v.u.cpu().numpy() for k, v in sol.items()},
+                     max(i.relres for i in solver.infos))
+    assert res['extrapolated'][0] < res['previous'][0]
+    for k, u in res['previous'][1].items():
+        assert np.linalg.norm(res['extrapolated'][1][k] - u) <= 1e-6 * np.linalg.norm(u) + 1e-12

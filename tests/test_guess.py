@@ -1,5 +1,6 @@
-"""Learned initial guess: GPU kernels against the NumPy oracle, and the gain of the trained network
-over the previous-step guess OpenCMP uses (opencmp/models/base_model.py:925-937)."""
+"""Learned initial guess: the NumPy oracle against finite differences and exact polynomials, the GPU
+kernels against the oracle, and what the trained network gains over the extrapolation it corrects
+and over the previous-step guess OpenCMP uses (opencmp/models/base_model.py:925-937)."""
 import numpy as np
 import pytest
 
@@ -21,6 +22,40 @@ def test_oracle_mlp_gradient_matches_finite_differences():
         Pm[p] -= eps
         fd = (mlp.loss_grad(Pp, X, T)[0] - mlp.loss_grad(Pm, X, T)[0]) / (2 * eps)
         assert abs(fd - g[p]) <= 1e-6 * max(1.0, abs(g[p]))
+    # the vector-Jacobian product with dY = d loss / dy is the same gradient
+    y, _ = mlp.forward(P, X)
+    assert np.allclose(mlp.backward(P, X, 2 * (y - T) / len(T)), g, rtol=1e-12, atol=1e-14)
+
+
+def test_oracle_residual_loss_gradient_matches_finite_differences():
+    from oracle import mlp
+    rng = np.random.default_rng(1)
+    n = 40
+    A = np.eye(n) * 4 + rng.standard_normal((n, n)) * (rng.random((n, n)) < 0.1)
+    free = rng.random(n) < 0.8
+    Y, T, b = rng.standard_normal(n), rng.standard_normal(n), rng.standard_normal(n)
+    S = 0.37
+    loss, g = mlp.residual_loss(A, Y, T, S, b, free, weight=2.5)
+    for i in range(n):
+        d = np.zeros(n)
+        d[i] = 1e-6
+        fd = (mlp.residual_loss(A, Y + d, T, S, b, free, 2.5)[0] - mlp.residual_loss(A, Y - d, T, S, b, free, 2.5)[0]) / 2e-6
+        assert abs(fd - g[i]) <= 1e-6 * max(1.0, abs(g[i]))
+
+
+def test_oracle_extrapolation_is_exact_for_polynomials():
+    """The degree-p backward-difference guess reproduces any degree-p polynomial in time."""
+    from oracle import mlp
+    rng = np.random.default_rng(2)
+    n = 30
+    coef = rng.standard_normal((4, n))
+    free = np.ones(n, bool)
+    for p in range(4):
+        cp = coef.copy()
+        cp[p + 1:] = 0
+        up = lambda t: sum(cp[q] * t ** q for q in range(4))
+        hist = [up(-j * 0.1) for j in range(p + 1)]
+        assert np.allclose(mlp.predict(None, hist, free, p), up(0.1), rtol=1e-12, atol=1e-12)
 
 
 @pytest.mark.gpu
@@ -31,6 +66,10 @@ def test_gpu_mlp_forward_and_gradients_match_oracle(gpu_lib):
     rng = np.random.default_rng(3)
     F = 4
     net = GuessNet(F, seed=5)
+    P0 = net.params()
+    lay = mlp.layout(F)
+    # a new network has zero output: output layer, bias and linear skip start at zero
+    assert not P0[lay['w3']:].any()
     P = (rng.standard_normal(net.nparams) * 0.3).astype(np.float32)
     net.set_params(P)
     assert np.array_equal(net.params(), P)
@@ -48,39 +87,135 @@ def test_gpu_mlp_forward_and_gradients_match_oracle(gpu_lib):
     # deterministic reductions: the same gradient bits twice
     _, g2 = net.loss_grad(Xd, Td, want_grad=True)
     assert g.tobytes() == g2.tobytes()
+    # back-propagation of an upstream gradient
+    dY = rng.standard_normal(3000).astype(np.float32) * 1e-2
+    gb = net.backward(Xd, torch.as_tensor(dY, device='cuda'), want_grad=True)
+    gbo = mlp.backward(P.astype(np.float64), X.astype(np.float64), dY.astype(np.float64))
+    assert np.abs(gb - gbo).max() <= 1e-4 * np.abs(gbo).max()
 
 
-def _transient(space, A, sv, guess, eps, steps, collect=False, use=False):
+def _history(space, steps=5, seed=0):
+    """A smooth synthetic history on the dofs of `space`: u(t) = sum_q c_q(x) t^q + a small sine."""
+    rng = np.random.default_rng(seed)
+    n = space.ndof
+    c = rng.standard_normal((5, n))
+    return [c[0] + c[1] * t + c[2] * t * t + 0.3 * c[3] * t ** 3 + 0.1 * np.sin(7 * t) * c[4]
+            for t in [-0.05 * j for j in range(steps)]]
+
+
+@pytest.mark.gpu
+def test_gpu_guess_kernels_match_oracle(gpu_lib):
+    """Scales, features, extrapolation, network prediction, training target, residual loss and the
+    transpose product against the oracle on a small P2 mesh."""
+    import ctypes as C
+    import torch
+    from opencmp_gb300 import fem, _lib as LB
+    from opencmp_gb300.fem import _ptr, _stream
+    from opencmp_gb300.guess import LearnedGuess
+    from oracle import mlp
+    m = M.unit_cube(4)
+    space = fem.Space(m, 'H1', 2, m.bc_names)
+    n = space.ndof
+    free = space.FreeDofs().astype(bool)
+    A = fem.Matrix(space)
+    A.assemble(fem.make_form(mass=1.0, diff=1e-2, dt=1e-3, wind=(1.0, 0.5, 0.25)))
+    rp, col = space.pattern()
+    import scipy.sparse as sp
+    Ah = sp.csr_matrix((A.values(), col, rp), shape=(n, n))
+    g = LearnedGuess(space, k=5, base_order=3, seed=1)
+    rng = np.random.default_rng(4)
+    P = (rng.standard_normal(g.net.nparams) * 0.2).astype(np.float32)
+    g.net.set_params(P)
+    hist = _history(space)
+    for h in reversed(hist):
+        g.push(torch.as_tensor(h, device='cuda'))
+    X = torch.empty(n, 4, dtype=torch.float32, device='cuda')
+    g._scales(X)
+    Xo, So = mlp.features(hist, free)
+    # the scales come from the FP32 high parts of the differences (FP32 partial sums)
+    assert np.allclose(g.scales[:4].cpu().numpy(), So, rtol=1e-5)
+    assert np.allclose(X.cpu().numpy(), Xo, rtol=1e-5, atol=1e-5)
+    x = torch.empty(n, dtype=torch.float64, device='cuda')
+    amax = max(np.abs(h).max() for h in hist)
+    for p in range(5):
+        g.extrapolate(x, order=p)
+        # double-float differences and sums: about 48 significant bits
+        assert np.abs(x.cpu().numpy() - mlp.predict(None, hist, free, p)).max() <= 1e-13 * amax
+    g.trained = True
+    g._probe_pending = False
+    assert g.predict(x) == 'network'
+    Sg4 = float(g.scales[3].item())
+    xo = mlp.predict(P.astype(np.float64), hist, free, 3)
+    yo, _ = mlp.forward(P.astype(np.float64), Xo.astype(np.float32).astype(np.float64))
+    # features and scale from the FP32 high parts: the network input moves by ~1e-6 relative
+    xo = mlp.predict(None, hist, free, 3) + Sg4 * yo * free
+    # the prediction kernel evaluates tanh on the special-function unit (absolute error < 1e-3):
+    # bound the network's output error layer by layer from the weights
+    W1, b1, W2, b2, w3, b3, c = mlp.unpack(P.astype(np.float64), 4)
+    e2 = np.abs(W2).sum(1) * 1e-3 + 1e-3
+    gW = np.abs(W1).sum(1) * 1e-5 * max(1.0, np.abs(Xo).max())
+    tol = So[-1] * (np.abs(w3) @ (e2 + np.abs(W2) @ gW) + np.abs(c).sum() * 1e-5 * np.abs(Xo).max()
+                    + 1e-5 * max(1.0, np.abs(yo).max())) + 1e-13 * amax
+    assert np.abs(x.cpu().numpy() - xo).max() <= tol
+    unext = hist[0] + 0.01 * rng.standard_normal(n)
+    T = torch.empty(n, dtype=torch.float32, device='cuda')
+    LB.call('ocmp_guess_target', n, 5, _ptr(g.tab), _ptr(g._free), _ptr(g.scales), 3,
+            _ptr(torch.as_tensor(unext, device='cuda')), _ptr(T), _stream(None))
+    Sg = g.scales[:4].cpu().numpy()
+    To = mlp.target(hist, free, 3, unext) * So[-1] / Sg[-1]
+    assert np.allclose(T.cpu().numpy(), To, rtol=1e-5, atol=1e-5 * np.abs(To).max())
+    Y = rng.standard_normal(n).astype(np.float32)
+    b = rng.standard_normal(n)
+    smp = dict(T=T, S=g.scales[3:4].clone(), A=A, b=torch.as_tensor(b, device='cuda'), w=0.7)
+    loss = g._loss(smp, torch.as_tensor(Y, device='cuda'))
+    lo, dyo = mlp.residual_loss(Ah, Y, T.cpu().numpy(), Sg[-1], b, free, 0.7)
+    assert abs(loss - lo) <= 1e-10 * lo
+    assert np.abs(g.dY.cpu().numpy() - dyo).max() <= 1e-6 * np.abs(dyo).max()
+    xt = torch.as_tensor(rng.standard_normal(n), device='cuda')
+    yt = torch.empty_like(xt)
+    LB.call('ocmp_spmv_transpose', A.h, _ptr(xt), _ptr(yt), _stream(None))
+    assert np.allclose(yt.cpu().numpy(), Ah.T @ xt.cpu().numpy(), rtol=1e-12, atol=1e-12)
+
+
+def _transient(space, A, sv, guess, eps, steps, mode, collect=None):
+    """mode 'previous' (OpenCMP's guess), 'extrapolation' (the fallback) or 'learned'."""
     import torch
     from opencmp_gb300 import fem
     form = fem.make_form(mass=1.0, diff=eps, dt=1e-3, wind=(1.0, 0.5, 0.25))
     A.assemble(form)
     sv.update()
-    X = space.mesh.coords
+    if collect is not None:
+        collect.assemble(form)
     u = torch.as_tensor(fem.interpolate_p2(space, lambda P: np.exp(-((P - 0.3) ** 2).sum(-1) / 0.02)),
                         device='cuda')
     b = torch.zeros_like(u)
     guess.reset()
+    guess.reset_judge()
     guess.push(u)
     stats = []
     for _ in range(steps):
         fem.assemble_rhs(space, form, fem.make_rhs(dt=1e-3, mass=1.0, uprev=u), b)
         x = torch.empty_like(u)
-        if use:
-            guess.predict(x, A, b)
-        else:
+        kind = 'previous'
+        if mode == 'previous':
             x.copy_(u)
+        elif mode == 'extrapolation':
+            guess.extrapolate(x)
+        else:
+            kind = guess.predict(x)
         info = sv.solve(b, x)
-        stats.append((info.iterations, info.relres0, info.relres))
-        if collect:
-            guess.collect(x, A, b)
+        if mode == 'learned':
+            guess.judge(info, kind)
+        stats.append((info.iterations, info.relres0, info.relres, kind))
+        if collect is not None:
+            guess.collect(x, collect, b)
         guess.push(x)
         u = x
     return stats
 
 
 @pytest.mark.gpu
-def test_trained_guess_beats_previous_step_guess(gpu_lib):
+def test_trained_guess_beats_extrapolation_and_previous_step(gpu_lib):
     """Trains on eps in {2e-3, 2e-2, 7e-2}, evaluates on held-out eps = 1e-2."""
     from opencmp_gb300 import fem
     from opencmp_gb300.guess import LearnedGuess
@@ -88,26 +223,36 @@ def test_trained_guess_beats_previous_step_guess(gpu_lib):
     space = fem.Space(m, 'H1', 2, m.bc_names)
     A = fem.Matrix(space, jacobi32=True, dfloat=True)
     sv = fem.KrylovSolver(A, method='GMRES', restart=30, precision='mixed', tol=1e-8, maxit=500, inner_tol=1e-4)
-    guess = LearnedGuess(space, k=4, use_residual=True, seed=0)
+    guess = LearnedGuess(space, k=5, base_order=3, seed=0)
+    keep = []
     for eps in (2e-3, 2e-2, 7e-2):
-        _transient(space, A, sv, guess, eps, 20, collect=True)
+        At = fem.Matrix(space)
+        keep.append(At)
+        _transient(space, A, sv, guess, eps, 20, 'extrapolation', collect=At)
     before = guess.eval_loss()
-    guess.train(steps=300, batch=1 << 14, lr=3e-3)
+    losses = guess.train(steps=300, lr=3e-3)
     after = guess.eval_loss()
-    # training starts from the linear-extrapolation network (linear skip = first difference)
+    # a new network leaves the extrapolation unchanged (weighted loss 1); training lowers it
+    assert abs(before - 1.0) < 1e-6
     assert after < before
-    base = _transient(space, A, sv, guess, 1e-2, 12)
-    learned = _transient(space, A, sv, guess, 1e-2, 12, use=True)
+    prev = _transient(space, A, sv, guess, 1e-2, 14, 'previous')
+    extr = _transient(space, A, sv, guess, 1e-2, 14, 'extrapolation')
+    learned = _transient(space, A, sv, guess, 1e-2, 14, 'learned')
     # every solve reaches the FP64 tolerance whatever the guess
-    assert max(s[2] for s in base + learned) <= 1e-8
-    it_base = np.mean([s[0] for s in base[4:]])
-    it_learn = np.mean([s[0] for s in learned[4:]])
-    r0_base = np.mean([s[1] for s in base[4:]])
-    r0_learn = np.mean([s[1] for s in learned[4:]])
-    print('iterations previous-step {:.1f} learned {:.1f}; relres0 {:.2e} -> {:.2e}'.format(
-        it_base, it_learn, r0_base, r0_learn))
-    # what the trained network gains: a smaller initial FP64 residual than the previous-step guess
-    assert r0_learn < 0.5 * r0_base
+    assert max(s[2] for s in prev + extr + learned) <= 1e-8
+    net = [s for s in learned if s[3] == 'network']
+    assert len(net) >= 6 and guess.enabled
+    r0 = {k: np.mean([s[1] for s in v[-6:]]) for k, v in (('previous', prev), ('extrapolation', extr), ('learned', net))}
+    it = {k: np.mean([s[0] for s in v[-6:]]) for k, v in (('previous', prev), ('extrapolation', extr), ('learned', net))}
+    print('training loss {:.3f} -> {:.3f} (last {:.3f}); relres0 previous {:.2e} extrapolation {:.2e} learned {:.2e}; '
+          'iterations {:.1f} / {:.1f} / {:.1f}'.format(before, after, np.mean(losses[-10:]), r0['previous'],
+                                                      r0['extrapolation'], r0['learned'], it['previous'],
+                                                      it['extrapolation'], it['learned']))
+    # what the trained network gains over its fallback (the cubic extrapolation) and over the
+    # previous-step guess
+    assert r0['learned'] < 0.9 * r0['extrapolation']
+    assert r0['learned'] < 1e-3 * r0['previous']
+    assert it['learned'] <= it['extrapolation'] <= it['previous']
 
 
 class _Info:
@@ -117,21 +262,19 @@ class _Info:
 
 def test_guess_judge_falls_back_without_gain():
     """Host-side judge logic (no GPU): the network is switched off when it stops paying."""
-    from opencmp_gb300.guess import LearnedGuess
+    from opencmp_gb300.guess import LearnedGuess, NET, PROBE, FALLBACK
     g = LearnedGuess.__new__(LearnedGuess)
     g.judge_window = 3
     g.reset_judge()
+    g.judge(_Info(9, 5e-7), FALLBACK)   # history not full yet: no baseline
+    g.judge(_Info(4, 3e-8), PROBE)
     for _ in range(3):
-        g.judge(_Info(18, 8e-3), used=False)
-    g.judge(_Info(12, 1e-3), used=True)
-    g.judge(_Info(13, 1e-3), used=True)
-    g.judge(_Info(12, 1e-3), used=True)
+        g.judge(_Info(3, 1e-8), NET)
     assert g.enabled
-    g.judge(_Info(25, 1e-3), used=True)
-    g.judge(_Info(25, 1e-3), used=True)
-    g.judge(_Info(25, 1e-3), used=True)
+    for _ in range(3):
+        g.judge(_Info(4, 2e-8), NET)
     assert not g.enabled and 'iterations' in g.fallback_reason
     g.reset_judge()
-    g.judge(_Info(18, 8e-3), used=False)
-    g.judge(_Info(10, 2e-2), used=True)
+    g.judge(_Info(4, 3e-8), PROBE)
+    g.judge(_Info(3, 5e-8), NET)
     assert not g.enabled and 'initial residual' in g.fallback_reason
