@@ -299,6 +299,8 @@ def run_ours(args):
                       'relres0_network_steps': float(np.mean([s[2] for s in st_opt if s[4] == 'network']))
                       if any(s[4] == 'network' for s in st_opt) else None,
                       'iters_per_step': float(np.mean([s[0] for s in st_opt])),
+                      'iters_network_steps': float(np.mean([s[0] for s in st_opt if s[4] == 'network']))
+                      if any(s[4] == 'network' for s in st_opt) else None,
                       'outer_per_step': float(np.mean([s[1] for s in st_opt])),
                       'guess_kinds': {k: sum(1 for s in st_opt if s[4] == k) for k in ('network', 'probe', 'fallback')},
                       'max_relres': float(max(s[3] for s in st_opt)), 'speedup_vs_plain_fp64': value / plain,
@@ -306,7 +308,8 @@ def run_ours(args):
         'mixed_extrapolated_guess': {'value': ndof * args.steps * world / (ms_extrap * 1e-3), 'unit': 'DOF/s',
                                      'ms_per_step': ms_extrap / args.steps,
                                      'relres0_per_step': float(np.mean([s[2] for s in st_extrap[4:]])),
-                                     'iters_per_step': float(np.mean([s[0] for s in st_extrap]))},
+                                     'iters_per_step': float(np.mean([s[0] for s in st_extrap])),
+                                     'iters_full_history_steps': float(np.mean([s[0] for s in st_extrap[2:]]))},
         'mixed_previous_step_guess': {'value': ndof * args.steps * world / (ms_mixed * 1e-3), 'unit': 'DOF/s',
                                       'ms_per_step': ms_mixed / args.steps,
                                       'relres0_per_step': float(np.mean([s[2] for s in st_mixed])),

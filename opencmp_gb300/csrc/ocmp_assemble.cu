@@ -557,7 +557,7 @@ constexpr int kGenThreads = 64;
 template <int D, int L, int VAR>
 __global__ void __launch_bounds__(kGenThreads) elem_gen_ff_kernel(int64_t ne, const float2* __restrict__ geo,
                                                                   const int32_t* __restrict__ conn, FormArgs a,
-                                                                  float2* __restrict__ K) {
+                                                                  float2* __restrict__ K, float2* __restrict__ Kd) {
     using GT = GenTerms<D, L, VAR>;
     constexpr int NP = D + 1, NS = NP * (NP + 1) / 2, LL = L * L, PADLL = LL | 1;
     extern __shared__ float2 kst[];
@@ -611,6 +611,12 @@ __global__ void __launch_bounds__(kGenThreads) elem_gen_ff_kernel(int64_t ne, co
     for (int q = threadIdx.x; q < nb * LL; q += blockDim.x) {
         const int t = q / LL;
         dst[q] = kst[t * PADLL + (q - t * LL)];
+    }
+    // the diagonals K_e[i][i] again, compactly at Kd[e L + i], for the Jacobi diagonal pass
+    float2* __restrict__ dd = Kd + e0 * L;
+    for (int q = threadIdx.x; q < nb * L; q += blockDim.x) {
+        const int t = q / L, i = q - t * L;
+        dd[q] = kst[t * PADLL + i * L + i];
     }
 }
 
@@ -705,7 +711,8 @@ __global__ void __launch_bounds__(256) elem_matrix_ff_kernel(int64_t ne, const f
 
 template <int L>
 __global__ void diag_ff_kernel(int64_t nd, const int32_t* __restrict__ inc_ptr, const int32_t* __restrict__ inc,
-                               const float2* __restrict__ K, const uint8_t* __restrict__ freed, int use_facets,
+                               const float2* __restrict__ K, const float2* __restrict__ Kd,
+                               const uint8_t* __restrict__ freed, int use_facets,
                                const int32_t* __restrict__ efac_ptr, const int32_t* __restrict__ efac,
                                const int32_t* __restrict__ ebf_ptr, const int32_t* __restrict__ ebf,
                                const double* __restrict__ Ki, const double* __restrict__ Kb, double* __restrict__ dinv,
@@ -717,7 +724,7 @@ __global__ void diag_ff_kernel(int64_t nd, const int32_t* __restrict__ inc_ptr, 
         const int64_t flat = inc[k];
         const int64_t e = flat / L;
         const int i = (int)(flat % L);
-        const float2 v = K[flat * L + i];
+        const float2 v = Kd ? __ldg(Kd + flat) : K[flat * L + i];
         ff_add(h, l, v.x, v.y);
         if (use_facets) {
             if (efac_ptr)
@@ -962,27 +969,47 @@ __global__ void __launch_bounds__(256) csr_gather_kernel(int64_t nnz, const int3
     const int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (k >= nnz) return;
     const int32_t s0 = __ldg(seg + k), s1 = __ldg(seg + k + 1);
+    const int32_t ck = __ldg(col + k);
     if (FF) {
+        // contributions four at a time: indices, then values, all in flight before the sums (which
+        // keep list order)
         const float2* __restrict__ K = reinterpret_cast<const float2*>(Kv);
         float h = 0.f, l = 0.f;
-        for (int32_t q = s0; q < s1; q++) {
-            const float2 v = __ldg(K + __ldg(src + q));
-            ff_add(h, l, v.x, v.y);
+        for (int32_t q0 = s0; q0 < s1; q0 += 4) {
+            int32_t ix[4];
+            float2 v[4];
+#pragma unroll
+            for (int t = 0; t < 4; t++) ix[t] = q0 + t < s1 ? __ldg(src + q0 + t) : -1;
+#pragma unroll
+            for (int t = 0; t < 4; t++) v[t] = ix[t] >= 0 ? __ldg(K + ix[t]) : make_float2(0.f, 0.f);
+#pragma unroll
+            for (int t = 0; t < 4; t++)
+                if (ix[t] >= 0) ff_add(h, l, v[t].x, v[t].y);
         }
         const double vv = ff_to_double(h, l);
         vals[k] = vv;
         const float v32 = __fadd_rn(h, l);
         if (vals32) vals32[k] = v32;
-        if (svals64) svals64[k] = vv * dinv[__ldg(col + k)];
-        if (svals32) svals32[k] = v32 * dinv32[__ldg(col + k)];
+        if (svals64) svals64[k] = vv * dinv[ck];
+        if (svals32) svals32[k] = v32 * dinv32[ck];
     } else {
         const double* __restrict__ K = reinterpret_cast<const double*>(Kv);
         double acc = 0.0;
-        for (int32_t q = s0; q < s1; q++) acc += __ldg(K + __ldg(src + q));
+        for (int32_t q0 = s0; q0 < s1; q0 += 4) {
+            int32_t ix[4];
+            double v[4];
+#pragma unroll
+            for (int t = 0; t < 4; t++) ix[t] = q0 + t < s1 ? __ldg(src + q0 + t) : -1;
+#pragma unroll
+            for (int t = 0; t < 4; t++) v[t] = ix[t] >= 0 ? __ldg(K + ix[t]) : 0.0;
+#pragma unroll
+            for (int t = 0; t < 4; t++)
+                if (ix[t] >= 0) acc += v[t];
+        }
         vals[k] = acc;
         if (vals32) vals32[k] = (float)acc;
         if (svals64 || svals32) {
-            const double sv = acc * dinv[__ldg(col + k)];
+            const double sv = acc * dinv[ck];
             if (svals64) svals64[k] = sv;
             if (svals32) svals32[k] = (float)sv;
         }
@@ -1269,6 +1296,7 @@ int assemble_impl(ocmp_matrix_s* m, const ocmp_form_t* f, cudaStream_t st) {
     OCMP_CUDA(cudaFuncSetAttribute(elem_matrix_kernel<D, L>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     const bool dfl = (m->flags & OCMP_MAT_DFLOAT) != 0;
     float2* Kff = reinterpret_cast<float2*>(s->d_K);
+    bool kd_ok = false;  // the element kernel also wrote the compact diagonals (s->d_Kd)
     if (dfl) {
         const int ntf = 256;
         const size_t smf = sizeof(float2) * (size_t)NG * (ntf + 1);
@@ -1282,14 +1310,16 @@ int assemble_impl(ocmp_matrix_s* m, const ocmp_form_t* f, cudaStream_t st) {
         if constexpr (GenTerms<D, L, 0>::value && GenTerms<D, L, 1>::value) {
             if (s->kind == OCMP_H1) {
                 const size_t gsm = sizeof(float2) * (size_t)kGenThreads * ((L * L) | 1);
+                if (!s->d_Kd) OCMP_CUDA(cudaMalloc((void**)&s->d_Kd, sizeof(float2) * (size_t)ne * L));
+                kd_ok = true;
                 OCMP_CUDA(cudaFuncSetAttribute(elem_gen_ff_kernel<D, L, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)gsm));
                 OCMP_CUDA(cudaFuncSetAttribute(elem_gen_ff_kernel<D, L, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)gsm));
                 if (var == 0)
                     OCMP_LAUNCH(elem_gen_ff_kernel<D, L, 0><<<nblk(ne, kGenThreads), kGenThreads, gsm, st>>>(ne, s->d_geo_ff, mesh->dconn, a,
-                                                                                           Kff));
+                                                                                           Kff, s->d_Kd));
                 else
                     OCMP_LAUNCH(elem_gen_ff_kernel<D, L, 1><<<nblk(ne, kGenThreads), kGenThreads, gsm, st>>>(ne, s->d_geo_ff, mesh->dconn, a,
-                                                                                           Kff));
+                                                                                           Kff, s->d_Kd));
                 done = true;
             }
         }
@@ -1323,7 +1353,8 @@ int assemble_impl(ocmp_matrix_s* m, const ocmp_form_t* f, cudaStream_t st) {
     }
     const int32_t* efp = is_l2 ? s->d_efac_ptr : nullptr;
     if (m->dinv && dfl)
-        OCMP_LAUNCH(diag_ff_kernel<L><<<nblk(nd, 256), 256, 0, st>>>(nd, s->d_inc_ptr, s->d_inc, Kff, s->d_free, use_facets, efp,
+        OCMP_LAUNCH(diag_ff_kernel<L><<<nblk(nd, 256), 256, 0, st>>>(nd, s->d_inc_ptr, s->d_inc, Kff, kd_ok ? s->d_Kd : nullptr,
+                                                         s->d_free, use_facets, efp,
                                                          s->d_efac, s->d_ebf_ptr, s->d_ebf, Ki, Kb, m->dinv, m->dinv32));
     else if (m->dinv)
         OCMP_LAUNCH(diag_kernel<L><<<nblk(nd, 256), 256, 0, st>>>(nd, s->d_inc_ptr, s->d_inc, s->d_K, s->d_free, use_facets, efp,

@@ -289,22 +289,27 @@ __device__ __forceinline__ float2 tab_at(const float2* __restrict__ tab, int64_t
     return __ldg(tab + (int64_t)j * n + i);
 }
 
-// push u^{n+1}: row 0 <- u^{n+1}; row j <- (new row j-1) - (old row j-1) for 0 < j < min(m + 1, K)
-__global__ void push_kernel(int64_t n, int K, int m, float2* __restrict__ tab, const double* __restrict__ u) {
+// push u^{n+1}: row 0 <- u^{n+1}; row j <- (new row j-1) - (old row j-1) for 0 < j < min(m + 1, K).
+// All old rows are loaded before any store, so the loads are in flight together.
+template <int K>
+__global__ void push_kernel(int64_t n, int m, float2* __restrict__ tab, const double* __restrict__ u) {
     const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (i >= n) return;
+    float2 old[K];
+#pragma unroll
+    for (int j = 0; j < K; j++)
+        if (j < m) old[j] = tab[(int64_t)j * n + i];
     float2 cur = split_d(u[i]);
-    const int mn = m + 1 < K ? m + 1 : K;
-    for (int j = 0; j < mn; j++) {
-        float2* slot = tab + (int64_t)j * n + i;
-        if (j < m) {
-            const float2 old = *slot;
-            *slot = cur;
-            cur = ff_addn(cur, old, true);
-        } else {
-            *slot = cur;
-        }
+    float2 nw[K];
+#pragma unroll
+    for (int j = 0; j < K; j++) {
+        nw[j] = cur;
+        if (j < m) cur = ff_addn(cur, old[j], true);
     }
+    const int mn = m + 1 < K ? m + 1 : K;
+#pragma unroll
+    for (int j = 0; j < K; j++)
+        if (j < mn) tab[(int64_t)j * n + i] = nw[j];
 }
 
 // S_j = sqrt(mean over free dofs of (row j)^2), j = 1..K-1 (from the high parts, floored at 1e-300),
@@ -758,8 +763,9 @@ int ocmp_guess_push(int64_t n, int32_t k, int32_t m, float* tab, const double* u
     if (!tab || !u || n < 0 || k < 1 || k > kMaxK || m < 0 || m > k)
         return fail(OCMP_ERR_ARG, "ocmp_guess_push: bad argument (table of 1..6 rows, 0 <= m <= k)");
     if (n == 0) return OCMP_OK;
-    OCMP_LAUNCH(push_kernel<<<(unsigned)((n + 255) / 256), 256, 0, (cudaStream_t)stream>>>(
-        n, k, m, reinterpret_cast<float2*>(tab), u));
+    cudaStream_t st = (cudaStream_t)stream;
+    float2* T2 = reinterpret_cast<float2*>(tab);
+    OCMP_K_DISPATCH(k, OCMP_LAUNCH(push_kernel<KK><<<(unsigned)((n + 255) / 256), 256, 0, st>>>(n, m, T2, u)));
     OCMP_CUDA(cudaGetLastError());
     return OCMP_OK;
 }

@@ -512,7 +512,7 @@ static void free_space_device(ocmp_space_s* s) {
                   s->d_inc_ptr,  s->d_inc,      s->d_ifac,      s->d_bfac,     s->d_ebf_ptr,   s->d_ebf,
                   s->d_Rc,       s->d_Rv,       s->d_qw,        s->d_qphi,     s->d_mvec,      s->d_fw,
                   s->d_fphi,     s->d_fdphi,    s->d_flam,      s->d_K,        s->d_facetK,    s->d_Fe,
-                  s->d_lift_ptr, s->d_lift_pos, s->d_Rm_ff, s->d_geo_ff, s->d_tpos, s->d_cseg, s->d_csrc, s->d_u2};
+                  s->d_lift_ptr, s->d_lift_pos, s->d_Rm_ff, s->d_geo_ff, s->d_tpos, s->d_cseg, s->d_csrc, s->d_u2, s->d_Kd};
     for (void* p : ps) dfree(p);
 }
 

@@ -132,6 +132,7 @@ struct ocmp_space_s {
     double* d_Rc = nullptr;         // R_const
     float2* d_Rm_ff = nullptr;      // reference mass matrix as (hi, lo) float pairs
     float2* d_geo_ff = nullptr;     // static element geometry for the double-float element kernel
+    float2* d_Kd = nullptr;         // ne*nloc: element-matrix diagonals (double-float element kernel)
     float2* d_u2 = nullptr;         // ndof: a vector split into (hi, lo) float pairs (right-hand sides)
     int32_t* d_cseg = nullptr;      // nnz+1: per CSR entry, its run in d_csrc (built on first use)
     int32_t* d_csrc = nullptr;      // ne*nloc^2: element-matrix entries (e*nloc + i)*nloc + j per CSR entry,

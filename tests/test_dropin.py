@@ -309,9 +309,10 @@ def test_config_copied_from_another_parser():
 
 @pytest.mark.gpu
 def test_extrapolated_initial_guess_through_run(gpu_lib):
-    """The [SOLVER] initial_guess = extrapolated key on a transient reference fixture: the same
-    solution (both solves stop at the same FP64 relative residual) from fewer Krylov iterations
-    than OpenCMP's previous-step start."""
+    """The [SOLVER] initial_guess = extrapolated key on a transient reference fixture (1000 implicit
+    Euler steps): the same solution (both solves stop at the same FP64 relative residual) from
+    initial residuals orders of magnitude below OpenCMP's previous-step start. (This fixture's
+    1e-12 tolerance sits at the round-off floor of its CG, so the iteration counts stay alike.)"""
     from opencmp_gb300.run import run
     case = next(c.values[0] for c in CASES if not c.marks and c.values[0]['fixture'] == 'poisson_transient_coarse'
                 and _scheme(c.values[0]) == 'implicit euler')
@@ -322,8 +323,9 @@ def test_extrapolated_initial_guess_through_run(gpu_lib):
             cfg.add_section('SOLVER')
         cfg['SOLVER']['initial_guess'] = mode
         solver, sol = run('', cfg)
-        res[mode] = (sum(i.iterations for i in solver.infos), {k: v.u.cpu().numpy() for k, v in sol.items()},
+        res[mode] = (np.median([i.relres0 for i in solver.infos]), {k: v.u.cpu().numpy() for k, v in sol.items()},
                      max(i.relres for i in solver.infos))
-    assert res['extrapolated'][0] < res['previous'][0]
+    assert res['extrapolated'][0] < 1e-3 * res['previous'][0]
+    assert res['extrapolated'][2] <= 1e-9 and res['previous'][2] <= 1e-9
     for k, u in res['previous'][1].items():
-        assert np.linalg.norm(res['extrapolated'][1][k] - u) <= 1e-6 * np.linalg.norm(u) + 1e-12
+        assert np.linalg.norm(res['extrapolated'][1][k] - u) <= 1e-8 * np.linalg.norm(u) + 1e-14
