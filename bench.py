@@ -135,8 +135,8 @@ def run_ours(args):
     }
 
     from opencmp_gb300.guess import LearnedGuess
-    # history of 5 solutions: cubic extrapolation in time (the fallback) + the network's correction
-    guess = LearnedGuess(space, k=5, base_order=3, seed=0)
+    # history of k solutions: degree-p extrapolation in time (the fallback) + the network's correction
+    guess = LearnedGuess(space, k=args.guess_k, base_order=args.guess_base, seed=0)
 
     launches = {}
 
@@ -292,9 +292,10 @@ def run_ours(args):
         'plain_fp64': {'value': plain, 'unit': 'DOF/s', 'ms_per_step': ms_plain / args.steps,
                        'relres0_per_step': plain_relres0[0],
                        'iters_per_step': float(np.mean([s[0] for s in st_plain]))},
-        'optimised': {'kind': 'double-float (FP32-pair) assembly, learned initial guess (cubic extrapolation in '
-                              'time + per-dof MLP correction trained on the solver\'s own trajectories), FP32 inner '
-                              'GMRES + FP64 iterative refinement',
+        'optimised': {'kind': 'double-float (FP32-pair) assembly, learned initial guess (degree-{} extrapolation '
+                              'in time over {} solutions + per-dof MLP correction trained on the solver\'s own '
+                              'trajectories), FP32 inner GMRES + FP64 iterative refinement'.format(args.guess_base,
+                                                                                                  args.guess_k),
                       'relres0_per_step': float(np.mean([s[2] for s in st_opt])),
                       'relres0_network_steps': float(np.mean([s[2] for s in st_opt if s[4] == 'network']))
                       if any(s[4] == 'network' for s in st_opt) else None,
@@ -315,7 +316,7 @@ def run_ours(args):
                                       'relres0_per_step': float(np.mean([s[2] for s in st_mixed])),
                                       'iters_per_step': float(np.mean([s[0] for s in st_mixed]))},
         'guess_training': {'eps': eps_train, 'steps_per_run': args.train_steps, 'adam_steps': args.train_iters,
-                           'loss': 'residual |A e|^2 / |b|^2 relative to the cubic extrapolation (1 = no gain)',
+                           'loss': 'residual |A e|^2 / |b|^2 relative to the extrapolation (1 = no gain)',
                            'loss_before': loss_before, 'loss_after': loss_after,
                            'loss_last_iters': float(np.mean(losses[-10:])), 'seconds': train_s},
         'e2e': {'value': e2e_val, 'unit': 'DOF/s', 'h2d_bytes_per_step': 8 * ndof, 'd2h_bytes_per_step': 8 * ndof},
@@ -587,6 +588,8 @@ def main():
     ap.add_argument('--train-runs', type=int, default=4)
     ap.add_argument('--train-steps', type=int, default=50)
     ap.add_argument('--train-iters', type=int, default=300)
+    ap.add_argument('--guess-k', type=int, default=5, help='history length of the learned guess (2..6)')
+    ap.add_argument('--guess-base', type=int, default=3, help='degree of the extrapolation it corrects')
     args = ap.parse_args()
     if args.impl == 'reference':
         run_reference(args)

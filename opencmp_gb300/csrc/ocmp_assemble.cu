@@ -541,6 +541,8 @@ struct GenTerms {
     static constexpr bool value = false;
     static constexpr int NG = 1;
     static __device__ __forceinline__ void run(const float2 (&)[1], float2*) {}
+    static __device__ __forceinline__ void run0(const float2 (&)[1], float2*) {}
+    static __device__ __forceinline__ void run1(const float2 (&)[1], float2*) {}
 };
 __device__ __forceinline__ void gterm(float& sh, float& sl, float2 f, float ch, float cl) {
     float ph, pl;
@@ -549,11 +551,13 @@ __device__ __forceinline__ void gterm(float& sh, float& sl, float2 f, float ch, 
 }
 #include "ocmp_terms_gen.h"
 
-// The block's element matrices are staged in shared memory (one padded record per thread, so the
-// half-warps' 8-byte writes fall in distinct banks) and written out as one contiguous run with
-// consecutive threads on consecutive addresses: full-line stores instead of 32 partial lines per
-// warp store.
+// Two threads per element, in different warps, each running half of the generated slots (run0 /
+// run1, balanced by term count) after computing the element's factors; the block's element matrices are staged in shared
+// memory (one padded record per element, so the half-warps' 8-byte writes spread over the banks)
+// and written out as one contiguous run with consecutive threads on consecutive addresses:
+// full-line stores instead of 32 partial lines per warp store.
 constexpr int kGenThreads = 64;
+constexpr int kGenElems = kGenThreads / 2;
 template <int D, int L, int VAR>
 __global__ void __launch_bounds__(kGenThreads) elem_gen_ff_kernel(int64_t ne, const float2* __restrict__ geo,
                                                                   const int32_t* __restrict__ conn, FormArgs a,
@@ -561,8 +565,9 @@ __global__ void __launch_bounds__(kGenThreads) elem_gen_ff_kernel(int64_t ne, co
     using GT = GenTerms<D, L, VAR>;
     constexpr int NP = D + 1, NS = NP * (NP + 1) / 2, LL = L * L, PADLL = LL | 1;
     extern __shared__ float2 kst[];
-    const int64_t e0 = blockIdx.x * (int64_t)blockDim.x;
-    const int64_t e = e0 + threadIdx.x;
+    const int64_t e0 = blockIdx.x * (int64_t)kGenElems;
+    const int el = threadIdx.x % kGenElems, part = threadIdx.x / kGenElems;  // one part per warp: no divergence
+    const int64_t e = e0 + el;
     if (e < ne) {
     float2 F[GT::NG];
 #pragma unroll
@@ -603,14 +608,30 @@ __global__ void __launch_bounds__(kGenThreads) elem_gen_ff_kernel(int64_t ne, co
             }
         }
     }
-    GT::run(F, kst + threadIdx.x * PADLL);
+    if (part == 0) GT::run0(F, kst + el * PADLL);
+    else GT::run1(F, kst + el * PADLL);
     }
     __syncthreads();
-    const int nb = (int)min((int64_t)blockDim.x, ne - e0);
+    const int nb = (int)min((int64_t)kGenElems, ne - e0);
+    // copy-out: each thread moves 4 consecutive pairs per round (two 16-byte stores), the loads of a
+    // round issued before its stores
     float2* __restrict__ dst = K + e0 * LL;
-    for (int q = threadIdx.x; q < nb * LL; q += blockDim.x) {
-        const int t = q / LL;
-        dst[q] = kst[t * PADLL + (q - t * LL)];
+    const int nq = nb * LL;
+    for (int q0 = 4 * threadIdx.x; q0 < nq; q0 += 4 * blockDim.x) {
+        float2 v[4];
+#pragma unroll
+        for (int t = 0; t < 4; t++) {
+            const int q = q0 + t, el2 = q / LL;
+            v[t] = q < nq ? kst[el2 * PADLL + (q - el2 * LL)] : make_float2(0.f, 0.f);
+        }
+        if (q0 + 3 < nq && ((reinterpret_cast<uintptr_t>(dst + q0) & 15) == 0)) {
+            reinterpret_cast<float4*>(dst + q0)[0] = make_float4(v[0].x, v[0].y, v[1].x, v[1].y);
+            reinterpret_cast<float4*>(dst + q0)[1] = make_float4(v[2].x, v[2].y, v[3].x, v[3].y);
+        } else {
+#pragma unroll
+            for (int t = 0; t < 4; t++)
+                if (q0 + t < nq) dst[q0 + t] = v[t];
+        }
     }
     // the diagonals K_e[i][i] again, compactly at Kd[e L + i], for the Jacobi diagonal pass
     float2* __restrict__ dd = Kd + e0 * L;
@@ -1139,37 +1160,40 @@ __global__ void rhs_elem_kernel(int64_t ne, const double* __restrict__ X, const 
 
 // Mass-term right-hand side in double-float (the implicit time-step load mass (u_prev, phi_i) with
 // no source or boundary data). u_prev is split once per dof into (hi, lo) float pairs; then one
-// thread per (element, local row i), flat = e * L + i:
-//   Fe[flat] = (mass |det J|) (sum_j Rm_ij u_prev[dof(e, j)]), every product and sum in (hi, lo)
-// float pairs; the element's dof indices and values are shared through L1 by its L threads.
+// thread per element:
+//   Fe[e L + i] = (mass |det J|) (sum_j Rm_ij u_prev[dof(e, j)]), every product and sum in (hi, lo)
+// float pairs.
 __global__ void split_ff_kernel(int64_t n, const double* __restrict__ u, float2* __restrict__ u2) {
     const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (i < n) u2[i] = ff_split(u[i]);
 }
 
 template <int L>
-__global__ void __launch_bounds__(256) rhs_mass_ff_kernel(int64_t nflat, const int32_t* __restrict__ dofs,
+__global__ void __launch_bounds__(128) rhs_mass_ff_kernel(int64_t ne, const int32_t* __restrict__ dofs,
                                                           const float2* __restrict__ geo, float2 mass,
                                                           const float2* __restrict__ u2,
                                                           const float2* __restrict__ Rmf, float2* __restrict__ Fe) {
-    const int64_t flat = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    if (flat >= nflat) return;
-    const int64_t e = flat / L;
-    const int i = (int)(flat - e * L);
-    float sh = 0.f, sl = 0.f;
+    const int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (e >= ne) return;
+    float2 u[L];
 #pragma unroll
-    for (int j = 0; j < L; j++) {
-        const float2 u = __ldg(u2 + __ldg(dofs + e * L + j));
-        const float2 c = __ldg(Rmf + i * L + j);
-        float ph, pl;
-        ff_mul(c.x, c.y, u.x, u.y, ph, pl);
-        ff_add(sh, sl, ph, pl);
-    }
+    for (int j = 0; j < L; j++) u[j] = __ldg(u2 + __ldg(dofs + e * L + j));
     const float2 sc = ff_prod(mass, __ldg(geo + e));
-    float ph, pl;
-    ff_mul(sc.x, sc.y, sh, sl, ph, pl);
-    const float hs = __fadd_rn(ph, pl);
-    Fe[flat] = make_float2(hs, __fsub_rn(pl, __fsub_rn(hs, ph)));
+#pragma unroll
+    for (int i = 0; i < L; i++) {
+        float sh = 0.f, sl = 0.f;
+#pragma unroll
+        for (int j = 0; j < L; j++) {
+            const float2 c = __ldg(Rmf + i * L + j);
+            float ph, pl;
+            ff_mul(c.x, c.y, u[j].x, u[j].y, ph, pl);
+            ff_add(sh, sl, ph, pl);
+        }
+        float ph, pl;
+        ff_mul(sc.x, sc.y, sh, sl, ph, pl);
+        const float hs = __fadd_rn(ph, pl);
+        Fe[e * L + i] = make_float2(hs, __fsub_rn(pl, __fsub_rn(hs, ph)));
+    }
 }
 
 // b[d] (+)= sum over the dof's incidences of the (hi, lo) element contributions, in incidence order
@@ -1309,16 +1333,16 @@ int assemble_impl(ocmp_matrix_s* m, const ocmp_form_t* f, cudaStream_t st) {
         bool done = false;
         if constexpr (GenTerms<D, L, 0>::value && GenTerms<D, L, 1>::value) {
             if (s->kind == OCMP_H1) {
-                const size_t gsm = sizeof(float2) * (size_t)kGenThreads * ((L * L) | 1);
+                const size_t gsm = sizeof(float2) * (size_t)kGenElems * ((L * L) | 1);
                 if (!s->d_Kd) OCMP_CUDA(cudaMalloc((void**)&s->d_Kd, sizeof(float2) * (size_t)ne * L));
                 kd_ok = true;
                 OCMP_CUDA(cudaFuncSetAttribute(elem_gen_ff_kernel<D, L, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)gsm));
                 OCMP_CUDA(cudaFuncSetAttribute(elem_gen_ff_kernel<D, L, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)gsm));
                 if (var == 0)
-                    OCMP_LAUNCH(elem_gen_ff_kernel<D, L, 0><<<nblk(ne, kGenThreads), kGenThreads, gsm, st>>>(ne, s->d_geo_ff, mesh->dconn, a,
+                    OCMP_LAUNCH(elem_gen_ff_kernel<D, L, 0><<<nblk(ne, kGenElems), kGenThreads, gsm, st>>>(ne, s->d_geo_ff, mesh->dconn, a,
                                                                                            Kff, s->d_Kd));
                 else
-                    OCMP_LAUNCH(elem_gen_ff_kernel<D, L, 1><<<nblk(ne, kGenThreads), kGenThreads, gsm, st>>>(ne, s->d_geo_ff, mesh->dconn, a,
+                    OCMP_LAUNCH(elem_gen_ff_kernel<D, L, 1><<<nblk(ne, kGenElems), kGenThreads, gsm, st>>>(ne, s->d_geo_ff, mesh->dconn, a,
                                                                                            Kff, s->d_Kd));
                 done = true;
             }
@@ -1447,8 +1471,8 @@ int rhs_impl(ocmp_space_s* s, const ocmp_form_t* f, const ocmp_rhs_t* r, double*
         OCMP_LAUNCH(split_ff_kernel<<<nblk(s->ndof, 256), 256, 0, st>>>(s->ndof, r->uprev, s->d_u2));
         const float mh = (float)r->mass;
         const float2 m2 = make_float2(mh, (float)(r->mass - (double)mh));
-        OCMP_LAUNCH(rhs_mass_ff_kernel<L><<<nblk(ne * L, 256), 256, 0, st>>>(ne * L, s->d_dofs, s->d_geo_ff, m2, s->d_u2,
-                                                                        s->d_Rm_ff, Fe2));
+        OCMP_LAUNCH(rhs_mass_ff_kernel<L><<<nblk(ne, 128), 128, 0, st>>>(ne, s->d_dofs, s->d_geo_ff, m2, s->d_u2,
+                                                                    s->d_Rm_ff, Fe2));
         OCMP_LAUNCH(rhs_gather_ff_kernel<<<nblk(s->ndof, 256), 256, 0, st>>>(s->ndof, s->d_inc_ptr, s->d_inc, Fe2, b,
                                                                         r->accumulate));
         OCMP_CUDA(cudaGetLastError());

@@ -1263,10 +1263,6 @@ int main(int argc, char** argv) {
         const int L = T.nloc, NP = D + 1, NS = NP * (NP + 1) / 2;
         for (int var = 0; var < 2; var++) {
             const int NG = 1 + NS + (var ? NP * NP : NP);
-            std::fprintf(o, "template <> struct GenTerms<%d, %d, %d> {\n    static constexpr bool value = true;\n"
-                            "    static constexpr int NG = %d;\n"
-                            "    static __device__ __forceinline__ void run(const float2 (&F)[%d], float2* __restrict__ Ke) {\n",
-                         D, L, var, NG, NG);
             const auto& off = T.slot_off[var];
             const auto& tg = T.term_g[var];
             const auto& tc = T.term_coef[var];
@@ -1281,9 +1277,23 @@ int main(int argc, char** argv) {
                                  acc, (int)tg[t], hb, lb);
                 }
             };
-            int slot = 0;
+            // the slots in (i <= j) order, and the slot where the terms reach half the total: run0
+            // writes the entries of the slots before it, run1 those from it on (two threads per element)
+            std::vector<int> si, sj;
             for (int i = 0; i < L; i++)
-                for (int j = i; j < L; j++, slot++) {
+                for (int j = i; j < L; j++) {
+                    si.push_back(i);
+                    sj.push_back(j);
+                }
+            const int nsl = (int)si.size();
+            const int total = off[4 * nsl];
+            int half = 0;
+            while (half < nsl && off[4 * half] < total / 2) half++;
+            auto emit_slots = [&](const char* name, int s0, int s1) {
+                std::fprintf(o, "    static __device__ __forceinline__ void %s(const float2 (&F)[%d], float2* __restrict__ Ke) {\n",
+                             name, NG);
+                for (int slot = s0; slot < s1; slot++) {
+                    const int i = si[slot], j = sj[slot];
                     const int o0 = off[4 * slot], o2 = off[4 * slot + 2], o3 = off[4 * slot + 3], o4 = off[4 * slot + 4];
                     std::fprintf(o, "        {\n        float sh = 0.f, sl = 0.f;\n");
                     emit("s", o0, o2);
@@ -1297,7 +1307,15 @@ int main(int argc, char** argv) {
                     }
                     std::fprintf(o, "        }\n");
                 }
-            std::fprintf(o, "    }\n};\n\n");
+                std::fprintf(o, "    }\n");
+            };
+            std::fprintf(o, "template <> struct GenTerms<%d, %d, %d> {\n    static constexpr bool value = true;\n"
+                            "    static constexpr int NG = %d;\n",
+                         D, L, var, NG);
+            emit_slots("run", 0, nsl);
+            emit_slots("run0", 0, half);
+            emit_slots("run1", half, nsl);
+            std::fprintf(o, "};\n\n");
         }
     }
     std::fclose(o);

@@ -1127,6 +1127,9 @@ int gm_run(const Ctx& c, const GmBufs<T>& B, const double* b, double* x, int max
     const int64_t ne = s->mesh->ne;
     const int L = s->nloc;
     const dim3 gg(G, NB), gs(nblk(n * TPR, 256), NB);
+    // The FP64 residual is bound by the FP64 pipe (1/58 of the FP32 rate here), not by HBM: half the
+    // lanes per row of the SpMV halves the FP64 shuffle-reduction adds it spends beside the FMAs.
+    constexpr int RTPR = TPR > 2 ? TPR / 2 : TPR;
     cudaStream_t ls = c.st;  // launch stream of the lambdas below (switched while capturing)
     auto block_apply = [&](int j, double* xo) {
         const unsigned nbk = nblk(ne * L, kThreads);
@@ -1172,7 +1175,7 @@ int gm_run(const Ctx& c, const GmBufs<T>& B, const double* b, double* x, int max
         } else {
             OCMP_LAUNCH(gm_combine<T><<<gg, 256, 0, ls>>>(n, m, B.V, sv->scale, sv->H, csg, sv->flags, B.dinv, x, nullptr, bt));
         }
-        OCMP_LAUNCH(gm_resid<T, TPR, U><<<gg, 256, 0, ls>>>(n, s->d_rowptr, s->d_col, sv->mat->vals, s->d_free, b, x, B.V,
+        OCMP_LAUNCH(gm_resid<T, RTPR, U><<<gg, 256, 0, ls>>>(n, s->d_rowptr, s->d_col, sv->mat->vals, s->d_free, b, x, B.V,
                                                   sv->part, sv->cnt, sv->st, sv->flags, sv->scale, csg, m, 1,
                                                   s->d_lift_ptr, s->d_lift_pos, bt));
     };
@@ -1185,7 +1188,7 @@ int gm_run(const Ctx& c, const GmBufs<T>& B, const double* b, double* x, int max
     // projection (|w_new|^2 < 1e-6 |w|^2); the mass-dominated systems here lose far less per step.
     OCMP_LAUNCH(gm_set_tols<<<1, 1, 0, c.st>>>(sv->st, sv->prm.tol, inner_tol, 1e-6, NB, bt.st));
     OCMP_CUDA(cudaMemsetAsync(sv->flags, 0, sizeof(int) * F_NFLAG * NB, c.st));
-    OCMP_LAUNCH(gm_resid<T, TPR, U><<<gg, 256, 0, c.st>>>(n, s->d_rowptr, s->d_col, sv->mat->vals, s->d_free, b, x, B.V, sv->part,
+    OCMP_LAUNCH(gm_resid<T, RTPR, U><<<gg, 256, 0, c.st>>>(n, s->d_rowptr, s->d_col, sv->mat->vals, s->d_free, b, x, B.V, sv->part,
                                               sv->cnt, sv->st, sv->flags, sv->scale, csg, m, 3, s->d_lift_ptr,
                                               s->d_lift_pos, bt));
     {

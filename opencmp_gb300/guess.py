@@ -105,6 +105,7 @@ class LearnedGuess:
         self.trained = False
         self.enabled = True
         self.judge_window = 3
+        self.probe_every = 8
         self.fallback_reason = None
         self.reset_judge()
 
@@ -136,41 +137,51 @@ class LearnedGuess:
 
     def predict(self, x: torch.Tensor, stream=None) -> str:
         """Writes the guess into x; returns which guess it was: ``'network'``, ``'probe'`` (the
-        extrapolation, solved once after each judge reset to set the judge's baseline) or
-        ``'fallback'`` (the extrapolation)."""
+        extrapolation, solved on alternate steps of the judge's evaluation window and every
+        ``probe_every``-th step after it) or ``'fallback'`` (the extrapolation)."""
         if not (self.ready and self.enabled and self.trained):
             self.extrapolate(x, stream=stream)
             return FALLBACK
-        if self._probe_pending:
+        self._count += 1
+        probe = self._probe_next if self._evaluating else self._count % self.probe_every == 0
+        if probe:
             self.extrapolate(x, stream=stream)
-            self._probe_pending = False
+            self._probe_next = False
             return PROBE
         self._scales(stream=stream)
         LB.call('ocmp_guess_predict', self.net.h, self.n, self.k, _ptr(self.tab), _ptr(self._free),
                 _ptr(self.scales), self.base_order, _ptr(x), _stream(stream))
+        self._probe_next = self._evaluating
         return NET
 
     def judge(self, info, kind: str):
-        """Convergence is the guess's judge. The probe step, solved from the extrapolation, sets the
-        baseline (initial FP64 residual, iterations); the network is switched off for the rest of
-        the run if one of its guesses starts the solve with a larger residual than that, or if over
-        ``judge_window`` steps it does not save Krylov iterations (its evaluation costs time)."""
+        """Convergence is the guess's judge. Over an evaluation window of ``2 judge_window`` steps
+        the network's guess alternates with the extrapolation (probe steps), and after it every
+        ``probe_every``-th step is a probe. The network is switched off for the rest of the run as
+        soon as its recent steps (the last ``2 judge_window``) do not take fewer Krylov iterations on
+        average than the recent probes (the last ``judge_window``), or if one of its guesses starts
+        a solve with a larger initial FP64 residual than the probes' mean."""
         if kind == PROBE:
             self._base_it.append(info.iterations)
             self._base_r0.append(info.relres0)
+        elif kind == NET:
+            self._net_it.append(info.iterations)
+            if self._base_r0 and info.relres0 > np.mean(self._base_r0[-self.judge_window:]):
+                self.enabled, self.fallback_reason = False, 'initial residual above the extrapolation'
+                return
+        else:
             return
-        if kind != NET or not self._base_it:
-            return
-        self._net_it.append(info.iterations)
-        if info.relres0 > np.mean(self._base_r0):
-            self.enabled, self.fallback_reason = False, 'initial residual above the extrapolation'
-        elif len(self._net_it) >= self.judge_window and \
-                np.mean(self._net_it[-self.judge_window:]) >= np.mean(self._base_it):
-            self.enabled, self.fallback_reason = False, 'no fewer Krylov iterations than the extrapolation'
+        W = self.judge_window
+        if len(self._net_it) >= W and len(self._base_it) >= W:
+            self._evaluating = False
+            if np.mean(self._net_it[-2 * W:]) >= np.mean(self._base_it[-W:]):
+                self.enabled, self.fallback_reason = False, 'no fewer Krylov iterations than the extrapolation'
 
     def reset_judge(self):
         self.enabled = True
-        self._probe_pending = True
+        self._evaluating = True
+        self._probe_next = True
+        self._count = 0
         self._base_it, self._base_r0, self._net_it = [], [], []
         self.fallback_reason = None
 
