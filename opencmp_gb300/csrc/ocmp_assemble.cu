@@ -613,25 +613,10 @@ __global__ void __launch_bounds__(kGenThreads) elem_gen_ff_kernel(int64_t ne, co
     }
     __syncthreads();
     const int nb = (int)min((int64_t)kGenElems, ne - e0);
-    // copy-out: each thread moves 4 consecutive pairs per round (two 16-byte stores), the loads of a
-    // round issued before its stores
     float2* __restrict__ dst = K + e0 * LL;
-    const int nq = nb * LL;
-    for (int q0 = 4 * threadIdx.x; q0 < nq; q0 += 4 * blockDim.x) {
-        float2 v[4];
-#pragma unroll
-        for (int t = 0; t < 4; t++) {
-            const int q = q0 + t, el2 = q / LL;
-            v[t] = q < nq ? kst[el2 * PADLL + (q - el2 * LL)] : make_float2(0.f, 0.f);
-        }
-        if (q0 + 3 < nq && ((reinterpret_cast<uintptr_t>(dst + q0) & 15) == 0)) {
-            reinterpret_cast<float4*>(dst + q0)[0] = make_float4(v[0].x, v[0].y, v[1].x, v[1].y);
-            reinterpret_cast<float4*>(dst + q0)[1] = make_float4(v[2].x, v[2].y, v[3].x, v[3].y);
-        } else {
-#pragma unroll
-            for (int t = 0; t < 4; t++)
-                if (q0 + t < nq) dst[q0 + t] = v[t];
-        }
+    for (int q = threadIdx.x; q < nb * LL; q += blockDim.x) {
+        const int t = q / LL;
+        dst[q] = kst[t * PADLL + (q - t * LL)];
     }
     // the diagonals K_e[i][i] again, compactly at Kd[e L + i], for the Jacobi diagonal pass
     float2* __restrict__ dd = Kd + e0 * L;
