@@ -347,9 +347,13 @@ def run_ins(args):
     """Lid-driven cavity (OpenCMP INS model): unit square 256 x 256 x 2, Taylor-Hood P2/P1, nu = 1e-3
     (Re = 1000 with lid speed 1), Euler IMEX steps dt = 1e-3 from rest (explicit convection,
     reassembly every step), GMRES(50) with the block-diagonal preconditioner (velocity Jacobi,
-    pressure Schur-complement diagonal) to 1e-8; plain FP64 against FP32 inner / FP64 refinement."""
+    pressure Schur-complement diagonal) to 1e-8. Every path runs the same first `ins_train` steps
+    untimed (the learned path collects its training samples there: the run's own first steps), then
+    times `steps` steps: plain FP64 (previous-step guess), FP32 inner / FP64 refinement with the
+    previous-step guess, with the extrapolated guess, and with the learned guess under its judge."""
     import torch
     from opencmp_gb300 import fem, mesh as M, build, _lib
+    from opencmp_gb300.guess import LearnedGuess
     build.build()
     torch.cuda.set_device(0)
     n = args.n_ins
@@ -361,55 +365,98 @@ def run_ins(args):
     A = th.matrix()
     dinv = torch.zeros(nd, dtype=torch.float64, device='cuda')
     b = torch.zeros_like(dinv)
-    solvers = {p: fem.KrylovSolver(A, method='GMRES', restart=50, precond='user', precision=p, tol=1e-8, maxit=20000,
-                                   inner_tol=1e-4) for p in ('fp64', 'mixed')}
+    solvers = {p: fem.KrylovSolver(A, method='GMRES', restart=50, precond='user', precision=p, tol=1e-8,
+                                   maxit=args.ins_maxit, inner_tol=1e-4) for p in ('fp64', 'mixed')}
+    guess = LearnedGuess(th.C, k=args.guess_k, base_order=args.guess_base, seed=0)
 
-    def step(sv, u, stats):
-        uprev = u.clone()
+    def bcs(u):
         for c, val in ((0, 1.0), (1, 0.0)):
             th.V.set_boundary({lab['bottom']: 0.0, lab['left']: 0.0, lab['right']: 0.0, lab['top']: val},
                               th.component(u, c))
+
+    def step(kind, u, stats, collect=False):
+        sv = solvers['fp64' if kind == 'fp64' else 'mixed']
+        uprev = u.clone()
         th.assemble(A, mass=1.0, nu=nu, dt=dt)
         th.assemble_rhs(b, dt=dt, mass=1.0, uprev=uprev, imex=uprev)
         th.block_diag(A, dinv)
         sv.set_diag(dinv)
         sv.update()
+        used = 'previous'
+        if kind == 'learned':
+            used = guess.predict(u)
+        elif kind == 'extrap':
+            guess.extrapolate(u)
+        bcs(u)
         info = sv.solve(b, u, raise_on_fail=False)
-        stats.append((info.iterations, info.relres, info.status))
+        if collect:
+            guess.collect(u, A, b)
+        if kind in ('learned', 'extrap'):
+            guess.push(u)
+            if kind == 'learned':
+                guess.judge(info, used)
+        stats.append((info.iterations, info.relres, info.status, info.relres0, used))
 
     res = {}
-    for p in ('fp64', 'mixed'):
+    train_info = {}
+    for p in ('fp64', 'mixed', 'extrap', 'learned'):
         u = torch.zeros(nd, dtype=torch.float64, device='cuda')
+        bcs(u)
         st = []
-        for _ in range(args.warmup):
-            step(solvers[p], u, st)
+        guess.reset()
+        guess.reset_judge()
+        guess.push(u)
+        t_tr = time.perf_counter()
+        for _ in range(args.ins_train):
+            # the same untimed start for every path; the learned path collects its training samples
+            # here (the run's own first steps, solved from the extrapolated guess; the IMEX matrix is
+            # the same every step, so the live matrix serves the residual loss)
+            step('extrap' if p in ('extrap', 'learned') else p, u, st, collect=p == 'learned')
+        if p == 'learned':
+            l_before = guess.eval_loss()
+            guess.train(steps=args.train_iters, lr=3e-3)
+            train_info = dict(samples=len(guess.samples), adam_steps=args.train_iters, loss_before=l_before,
+                              loss_after=guess.eval_loss(), seconds=time.perf_counter() - t_tr)
+            guess.drop_samples()
+            guess.reset_judge()
         st.clear()
         torch.cuda.synchronize()
         l0 = _lib.load().ocmp_launch_count()
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record()
         for _ in range(args.steps):
-            step(solvers[p], u, st)
+            step(p, u, st)
         e1.record()
         torch.cuda.synchronize()
         ms = e0.elapsed_time(e1)
         l2, dv = th.errors(u)
-        res[p] = dict(ms=ms, launches=int(_lib.load().ocmp_launch_count() - l0),
+        res[p] = dict(ms_per_step=ms / args.steps, value=nd * args.steps / (ms * 1e-3), unit='DOF/s',
+                      launches=int(_lib.load().ocmp_launch_count() - l0),
                       iters=float(np.mean([s[0] for s in st])), max_relres=float(max(s[1] for s in st)),
+                      relres0=float(np.mean([s[3] for s in st])),
                       converged=int(sum(1 for s in st if s[2] == 0)), u_l2=l2, div_l2=dv)
-    val = nd * args.steps / (res['mixed']['ms'] * 1e-3)
+        if p == 'learned':
+            res[p].update(guess_kinds={k: sum(1 for s in st if s[4] == k) for k in ('network', 'probe', 'fallback')},
+                          guess_enabled_at_end=bool(guess.enabled), guess_fallback=guess.fallback_reason)
+        print('ins {}: {:.2f} ms/step, {:.1f} iterations/step'.format(p, res[p]['ms_per_step'], res[p]['iters']),
+              file=sys.stderr, flush=True)
+    val = res['learned']['value']
     line = {'metric': METRIC + ' (INS lid-driven cavity)', 'value': val, 'unit': 'DOF/s', 'n_gpus': 1,
-            'steps': args.steps, 'warmup': args.warmup, 'ms_per_step': res['mixed']['ms'] / args.steps,
+            'steps': args.steps, 'warmup': args.ins_train, 'ms_per_step': res['learned']['ms_per_step'],
             'higher_is_better': True, 'scaling': 'weak', 'vs_baseline': None, 'dtype': 'f64+f32',
             'data': 'synthetic (generated structured mesh, cavity at rest)',
             'config': {'workload': 'INS lid-driven cavity {0}x{0}x2 tri, Taylor-Hood P2/P1, Re=1000, Euler IMEX '
                                    'dt=1e-3, GMRES(50) + block-diagonal (velocity Jacobi, pressure Schur '
-                                   'diagonal) to 1e-8'.format(n), 'ndof': nd, 'nnz': th.nnz,
-                       'l2': 'inputs larger than L2 (no flush)'},
-            'plain_fp64': dict(res['fp64'], value=nd * args.steps / (res['fp64']['ms'] * 1e-3), unit='DOF/s'),
-            'optimised': dict(res['mixed'], kind='FP32 inner GMRES + FP64 iterative refinement'),
-            'gpu_launches': res['mixed']['launches'],
-            'learned_guess': 'not applied to INS in this build'}
+                                   'diagonal) to 1e-8; steps {1}..{2} from rest timed'.format(
+                                       n, args.ins_train + 1, args.ins_train + args.steps),
+                       'ndof': nd, 'nnz': th.nnz, 'l2': 'inputs larger than L2 (no flush)'},
+            'plain_fp64': res['fp64'], 'mixed_previous_step_guess': res['mixed'],
+            'mixed_extrapolated_guess': res['extrap'],
+            'optimised': dict(res['learned'], kind='FP32 inner GMRES + FP64 refinement, learned guess (degree-{} '
+                                                   'extrapolation + network trained on the run\'s first {} steps)'
+                              .format(args.guess_base, args.ins_train)),
+            'speedup_vs_plain_fp64': res['fp64']['ms_per_step'] / res['learned']['ms_per_step'],
+            'guess_training': train_info, 'gpu_launches': res['learned']['launches']}
     print(json.dumps(line), flush=True)
 
 
@@ -583,6 +630,8 @@ def main():
     ap.add_argument('--no-cpu', action='store_true')
     ap.add_argument('--config', default='transient3d', choices=['transient3d', 'batched', 'ins'])
     ap.add_argument('--n-ins', type=int, default=256)
+    ap.add_argument('--ins-train', type=int, default=100, help='untimed first INS steps (training samples)')
+    ap.add_argument('--ins-maxit', type=int, default=1000, help='GMRES iteration cap per INS step')
     ap.add_argument('--instances', type=int, default=512)
     ap.add_argument('--restart-batch', type=int, default=50)
     ap.add_argument('--train-runs', type=int, default=4)

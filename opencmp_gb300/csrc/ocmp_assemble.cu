@@ -543,6 +543,8 @@ struct GenTerms {
     static __device__ __forceinline__ void run(const float2 (&)[1], float2*) {}
     static __device__ __forceinline__ void run0(const float2 (&)[1], float2*) {}
     static __device__ __forceinline__ void run1(const float2 (&)[1], float2*) {}
+    static __device__ __forceinline__ void run2(const float2 (&)[1], float2*) {}
+    static __device__ __forceinline__ void run3(const float2 (&)[1], float2*) {}
 };
 __device__ __forceinline__ void gterm(float& sh, float& sl, float2 f, float ch, float cl) {
     float ph, pl;
@@ -551,15 +553,15 @@ __device__ __forceinline__ void gterm(float& sh, float& sl, float2 f, float ch, 
 }
 #include "ocmp_terms_gen.h"
 
-// Two threads per element, in different warps, each running half of the generated slots (run0 /
-// run1, balanced by term count) after computing the element's factors; the block's element matrices are staged in shared
+// NPART threads per element (one warp per part: NPART = 2 is launched), each running its share of
+// the generated slots (run0 .. run3: quarters balanced by term count) after computing the element's
+// factors; the block's element matrices are staged in shared
 // memory (one padded record per element, so the half-warps' 8-byte writes spread over the banks)
 // and written out as one contiguous run with consecutive threads on consecutive addresses:
 // full-line stores instead of 32 partial lines per warp store.
-constexpr int kGenThreads = 64;
-constexpr int kGenElems = kGenThreads / 2;
-template <int D, int L, int VAR>
-__global__ void __launch_bounds__(kGenThreads) elem_gen_ff_kernel(int64_t ne, const float2* __restrict__ geo,
+constexpr int kGenElems = 32;
+template <int D, int L, int VAR, int NPART>
+__global__ void __launch_bounds__(32 * NPART) elem_gen_ff_kernel(int64_t ne, const float2* __restrict__ geo,
                                                                   const int32_t* __restrict__ conn, FormArgs a,
                                                                   float2* __restrict__ K, float2* __restrict__ Kd) {
     using GT = GenTerms<D, L, VAR>;
@@ -608,8 +610,22 @@ __global__ void __launch_bounds__(kGenThreads) elem_gen_ff_kernel(int64_t ne, co
             }
         }
     }
-    if (part == 0) GT::run0(F, kst + el * PADLL);
-    else GT::run1(F, kst + el * PADLL);
+    if (NPART == 1) {
+        GT::run(F, kst + el * PADLL);
+    } else if (NPART == 2) {
+        if (part == 0) {
+            GT::run0(F, kst + el * PADLL);
+            GT::run1(F, kst + el * PADLL);
+        } else {
+            GT::run2(F, kst + el * PADLL);
+            GT::run3(F, kst + el * PADLL);
+        }
+    } else {
+        if (part == 0) GT::run0(F, kst + el * PADLL);
+        else if (part == 1) GT::run1(F, kst + el * PADLL);
+        else if (part == 2) GT::run2(F, kst + el * PADLL);
+        else GT::run3(F, kst + el * PADLL);
+    }
     }
     __syncthreads();
     const int nb = (int)min((int64_t)kGenElems, ne - e0);
@@ -1321,14 +1337,16 @@ int assemble_impl(ocmp_matrix_s* m, const ocmp_form_t* f, cudaStream_t st) {
                 const size_t gsm = sizeof(float2) * (size_t)kGenElems * ((L * L) | 1);
                 if (!s->d_Kd) OCMP_CUDA(cudaMalloc((void**)&s->d_Kd, sizeof(float2) * (size_t)ne * L));
                 kd_ok = true;
-                OCMP_CUDA(cudaFuncSetAttribute(elem_gen_ff_kernel<D, L, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)gsm));
-                OCMP_CUDA(cudaFuncSetAttribute(elem_gen_ff_kernel<D, L, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)gsm));
-                if (var == 0)
-                    OCMP_LAUNCH(elem_gen_ff_kernel<D, L, 0><<<nblk(ne, kGenElems), kGenThreads, gsm, st>>>(ne, s->d_geo_ff, mesh->dconn, a,
-                                                                                           Kff, s->d_Kd));
-                else
-                    OCMP_LAUNCH(elem_gen_ff_kernel<D, L, 1><<<nblk(ne, kGenElems), kGenThreads, gsm, st>>>(ne, s->d_geo_ff, mesh->dconn, a,
-                                                                                           Kff, s->d_Kd));
+#define OCMP_GEN(V)                                                                                                 \
+    do {                                                                                                            \
+        OCMP_CUDA(cudaFuncSetAttribute(elem_gen_ff_kernel<D, L, V, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, \
+                                       (int)gsm));                                                                  \
+        OCMP_LAUNCH(elem_gen_ff_kernel<D, L, V, 2><<<nblk(ne, kGenElems), 64, gsm, st>>>(ne, s->d_geo_ff, mesh->dconn,  \
+                                                                                      a, Kff, s->d_Kd));            \
+    } while (0)
+                if (var == 0) OCMP_GEN(0);
+                else OCMP_GEN(1);
+#undef OCMP_GEN
                 done = true;
             }
         }

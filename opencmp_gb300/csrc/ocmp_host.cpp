@@ -1277,8 +1277,8 @@ int main(int argc, char** argv) {
                                  acc, (int)tg[t], hb, lb);
                 }
             };
-            // the slots in (i <= j) order, and the slot where the terms reach half the total: run0
-            // writes the entries of the slots before it, run1 those from it on (two threads per element)
+            // the slots in (i <= j) order, split where the terms reach each quarter of the total:
+            // run0 .. run3 write the entries of one quarter each (four threads per element)
             std::vector<int> si, sj;
             for (int i = 0; i < L; i++)
                 for (int j = i; j < L; j++) {
@@ -1287,8 +1287,13 @@ int main(int argc, char** argv) {
                 }
             const int nsl = (int)si.size();
             const int total = off[4 * nsl];
-            int half = 0;
-            while (half < nsl && off[4 * half] < total / 2) half++;
+            // slot boundaries at each quarter of the terms
+            int cut[5] = {0, 0, 0, 0, nsl};
+            for (int q = 1; q < 4; q++) {
+                int c = cut[q - 1];
+                while (c < nsl && off[4 * c] < (int64_t)total * q / 4) c++;
+                cut[q] = c;
+            }
             auto emit_slots = [&](const char* name, int s0, int s1) {
                 std::fprintf(o, "    static __device__ __forceinline__ void %s(const float2 (&F)[%d], float2* __restrict__ Ke) {\n",
                              name, NG);
@@ -1313,8 +1318,10 @@ int main(int argc, char** argv) {
                             "    static constexpr int NG = %d;\n",
                          D, L, var, NG);
             emit_slots("run", 0, nsl);
-            emit_slots("run0", 0, half);
-            emit_slots("run1", half, nsl);
+            emit_slots("run0", cut[0], cut[1]);
+            emit_slots("run1", cut[1], cut[2]);
+            emit_slots("run2", cut[2], cut[3]);
+            emit_slots("run3", cut[3], cut[4]);
             std::fprintf(o, "};\n\n");
         }
     }
