@@ -1,16 +1,20 @@
 // Assembly kernels of libopencmp_gpu.so (sm_103a).
 //
-// Matrix assembly (FP64 throughout; GB300 runs FP64 at 1/58 of its FP32 rate, so the FP64 work
-// per element is kept small and the data movement coalesced):
-//   1. elem_matrix_kernel  one thread per element: Jacobian, |det J|, barycentric gradients, the
-//                     element factors (mass, G_ab = grad lam_a . grad lam_b, wind projections),
-//                     then the sparse barycentric term list K[slot] += F[g] * coef in shared memory
-//                     (symmetric parts for i <= j only), written out coalesced as K[e][i][j];
-//   2. diag_kernel    (only when Jacobi-scaled outputs are requested) the diagonal of each row;
-//   3. row_scatter_kernel  one thread per CSR row: sums the element-matrix row slices K[e][i][:]
-//                     of its incident elements (and facet-matrix rows) into the row through the
-//                     byte-sized slot table, then writes the row once: FP64 values, and optionally
-//                     an FP32 copy and the Jacobi-scaled A D^-1 in FP64 / FP32.
+// Matrix assembly (GB300 runs FP64 at 1/58 of its FP32 rate, so the FP64 work per element is kept
+// small, or moved to double-float pairs on the FP32 pipes, and the data movement coalesced):
+//   1. element matrices K[e][i][j]: elem_matrix_kernel (FP64, one thread per element: Jacobian,
+//                     |det J|, barycentric gradients, the element factors, then the sparse
+//                     barycentric term list) or, in double-float, elem_gen_ff_kernel (build-time
+//                     generated straight-line code on the static element geometry, staged through
+//                     shared memory for full-line stores; elem_matrix_ff_kernel for element types
+//                     without generated code);
+//   2. diag_kernel / diag_ff_kernel (when Jacobi-scaled outputs are requested): the row diagonals;
+//   3. element-only forms: the sorted segmented reduction csr_gather_kernel, one thread per CSR
+//                     entry summing its list of element-matrix entries (built once per space by
+//                     contrib_build_kernel); forms with facet terms: row_scatter_kernel, one
+//                     thread per CSR row gathering element and facet matrix rows through the
+//                     byte-sized slot table. Either writes each entry once: FP64 values, and
+//                     optionally an FP32 copy and the Jacobi-scaled A D^-1 in FP64 / FP32.
 // Every CSR value is produced by one thread in a fixed order: bit-reproducible, no atomics.
 // Facet matrices (DG skeleton terms, boundary terms) are computed by quadrature because their
 // integrands (max(w.n, 0)) are not polynomial.
@@ -849,100 +853,6 @@ __global__ void __launch_bounds__(128) row_scatter_ff_kernel(
     }
 }
 
-// Warp-per-row gather for element-only assembly (no facet terms). Lanes are split into G = 32 / L
-// groups; group g takes incidences k0 + g, k0 + g + G, ... of the row, loading each one's row slice
-// (L values, coalesced) and slot bytes, and adds them into its own accumulator stripe in shared
-// memory (a slice's slots are distinct, so the lanes of a group never collide). The G stripes are
-// then summed in group order and the row written with consecutive lanes on consecutive entries.
-// The summation order is fixed by the incidence list, so the values are deterministic.
-template <int L, bool FF>
-__global__ void __launch_bounds__(256) row_gather_warp_kernel(
-    int64_t r0, int64_t r1, const int32_t* __restrict__ rp, const int32_t* __restrict__ col,
-    const int32_t* __restrict__ inc_ptr, const int32_t* __restrict__ inc, const void* __restrict__ Kv,
-    const uint8_t* __restrict__ slot, int ss, int stripe, const double* __restrict__ dinv,
-    const float* __restrict__ dinv32, double* __restrict__ vals, float* __restrict__ vals32,
-    double* __restrict__ svals64, float* __restrict__ svals32) {
-    constexpr int G = 32 / L > 0 ? 32 / L : 1;
-    extern __shared__ double wacc[];
-    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    const int g = lane / L, j = lane % L;
-    const bool act = g < G;
-    double* __restrict__ base_acc = wacc + (size_t)w * stripe * G;
-    double* __restrict__ acc = base_acc + (size_t)(act ? g : 0) * stripe;
-    float2* __restrict__ acc2 = reinterpret_cast<float2*>(acc);
-    const int64_t wpb = blockDim.x >> 5;
-    for (int64_t r = r0 + blockIdx.x * wpb + w; r < r1; r += (int64_t)gridDim.x * wpb) {
-        const int32_t base = rp[r], rn = rp[r + 1] - base;
-        for (int q = lane; q < rn * G; q += 32) base_acc[(q / rn) * stripe + q % rn] = 0.0;
-        __syncwarp();
-        const int32_t k0 = inc_ptr[r], k1 = inc_ptr[r + 1];
-        double v = 0.0;
-        int sl = 0;
-        bool have = act && k0 + g < k1;
-        if (have) {
-            const int64_t flat = inc[k0 + g];
-            v = FF ? __longlong_as_double(__ldg(reinterpret_cast<const long long*>(Kv) + flat * L + j))
-                   : __ldg(reinterpret_cast<const double*>(Kv) + flat * L + j);
-            sl = __ldg(slot + flat * ss + j);
-        }
-        for (int32_t kb = k0; kb < k1; kb += G) {
-            // issue the next round's loads before this round's adds
-            double vn = 0.0;
-            int sln = 0;
-            const bool hn = act && kb + G + g < k1;
-            if (hn) {
-                const int64_t flat = inc[kb + G + g];
-                vn = FF ? __longlong_as_double(__ldg(reinterpret_cast<const long long*>(Kv) + flat * L + j))
-                        : __ldg(reinterpret_cast<const double*>(Kv) + flat * L + j);
-                sln = __ldg(slot + flat * ss + j);
-            }
-            if (have) {
-                if (FF) {
-                    const long long bits = __double_as_longlong(v);
-                    const float vh = __int_as_float((int)(bits & 0xffffffffll)), vl = __int_as_float((int)(bits >> 32));
-                    float2 a2 = acc2[sl];
-                    ff_add(a2.x, a2.y, vh, vl);
-                    acc2[sl] = a2;
-                } else {
-                    acc[sl] += v;
-                }
-            }
-            v = vn;
-            sl = sln;
-            have = hn;
-        }
-        __syncwarp();
-        for (int q = lane; q < rn; q += 32) {
-            if (FF) {
-                float2 a2 = reinterpret_cast<const float2*>(base_acc)[q];
-#pragma unroll
-                for (int gg = 1; gg < G; gg++) {
-                    const float2 b2 = reinterpret_cast<const float2*>(base_acc + (size_t)gg * stripe)[q];
-                    ff_add(a2.x, a2.y, b2.x, b2.y);
-                }
-                const double vv = ff_to_double(a2.x, a2.y);
-                vals[base + q] = vv;
-                const float v32 = __fadd_rn(a2.x, a2.y);
-                if (vals32) vals32[base + q] = v32;
-                if (svals64) svals64[base + q] = vv * dinv[col[base + q]];
-                if (svals32) svals32[base + q] = v32 * dinv32[col[base + q]];
-            } else {
-                double vv = base_acc[q];
-#pragma unroll
-                for (int gg = 1; gg < G; gg++) vv += base_acc[(size_t)gg * stripe + q];
-                vals[base + q] = vv;
-                if (vals32) vals32[base + q] = (float)vv;
-                if (svals64 || svals32) {
-                    const double sv = vv * dinv[col[base + q]];
-                    if (svals64) svals64[base + q] = sv;
-                    if (svals32) svals32[base + q] = (float)sv;
-                }
-            }
-        }
-        __syncwarp();
-    }
-}
-
 // ---------------------------------------------------------------------------------------------
 // Sorted segmented reduction for element-only assembly. Once per space (first use), for every CSR
 // entry the list of element-matrix entries that sum into it: row r takes its incidences (e, i) in
@@ -1412,27 +1322,6 @@ int assemble_impl(ocmp_matrix_s* m, const ocmp_form_t* f, cudaStream_t st) {
             OCMP_LAUNCH(csr_gather_kernel<false><<<nblk(s->nnz, 256), 256, 0, st>>>(s->nnz, s->d_cseg, s->d_csrc, Kc, s->d_col,
                                                                                m->dinv, m->dinv32, m->vals, m->vals32,
                                                                                m->svals64, m->svals32));
-        OCMP_CUDA(cudaGetLastError());
-        return OCMP_OK;
-    }
-    if (!use_facets) {
-        // element-only assembly: one warp per row (row_gather_warp_kernel)
-        const int wt = 256, wpb = wt / 32;
-        const int stripe = s->maxrow;
-        const int G = 32 / L > 0 ? 32 / L : 1;
-        const size_t wsm = sizeof(double) * (size_t)stripe * G * wpb;
-        auto kern = dfl ? row_gather_warp_kernel<L, true> : row_gather_warp_kernel<L, false>;
-        OCMP_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)wsm));
-        int dev = 0, sms = 152, per = 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        OCMP_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kern, wt, wsm));
-        const int64_t want = (nd + wpb - 1) / wpb;
-        const unsigned grid = (unsigned)std::max<int64_t>(1, std::min<int64_t>(want, (int64_t)std::max(per, 1) * sms));
-        const void* Kv = dfl ? (const void*)Kff : (const void*)s->d_K;
-        OCMP_LAUNCH(kern<<<grid, wt, wsm, st>>>(0, nd, s->d_rowptr, s->d_col, s->d_inc_ptr, s->d_inc, Kv, s->d_slot,
-                                              s->slot_stride, stripe, m->dinv, m->dinv32, m->vals, m->vals32,
-                                              m->svals64, m->svals32));
         OCMP_CUDA(cudaGetLastError());
         return OCMP_OK;
     }
