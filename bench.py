@@ -93,6 +93,23 @@ class Clocks:
                 'reasons': reasons, 'samples': len(sm)}
 
 
+def max_over_ranks(x: float, device: str = 'cuda') -> float:
+    """The largest of the ranks' values (the slowest replica's time); x itself on a single process."""
+    import torch
+    import torch.distributed as dist
+    if not (dist.is_available() and dist.is_initialized()) or dist.get_world_size() == 1:
+        return x
+    t = torch.tensor([x], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def whole_job_rate(units_per_rank: int, steps: int, world: int, ms: float) -> float:
+    """Units per second of the whole job: every replica processes `units_per_rank` per step; the
+    time is the slowest replica's (weak scaling, no collective on the data path)."""
+    return units_per_rank * steps * world / (ms * 1e-3)
+
+
 def run_ours(args):
     import torch
     import torch.distributed as dist
@@ -197,11 +214,7 @@ def run_ours(args):
         torch.cuda.nvtx.range_pop()
         ev1.record()
         torch.cuda.synchronize()
-        ms = ev0.elapsed_time(ev1)
-        if world > 1:
-            t = torch.tensor([ms], device='cuda')
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-            ms = float(t.item())
+        ms = max_over_ranks(ev0.elapsed_time(ev1))
         return ms, stats
 
     # training of the guess network on trajectories the solver produces (not timed): eps drawn
@@ -277,9 +290,9 @@ def run_ours(args):
     g_avg = g_ms / max(g_launches, 1)
     g_achieved = g_bytes / (g_avg * 1e-3) / 1e9 if g_launches else None
 
-    value = ndof * args.steps * world / (ms_opt * 1e-3)
-    plain = ndof * args.steps * world / (ms_plain * 1e-3)
-    e2e_val = ndof * args.steps * world / (ms_e2e * 1e-3)
+    value = whole_job_rate(ndof, args.steps, world, ms_opt)
+    plain = whole_job_rate(ndof, args.steps, world, ms_plain)
+    e2e_val = whole_job_rate(ndof, args.steps, world, ms_e2e)
     line = {
         'metric': METRIC, 'value': value, 'unit': 'DOF/s', 'n_gpus': world, 'steps': args.steps, 'warmup': args.warmup,
         'ms_per_step': ms_opt / args.steps, 'higher_is_better': True, 'scaling': 'weak', 'vs_baseline': None,
