@@ -538,13 +538,12 @@ __global__ void geo_ff_kernel(int64_t ne, const double* __restrict__ X, const in
 // Straight-line element matrices: the term tables of the H1 element types, written out at build
 // time as device code (ocmp_terms_gen.h, from ocmp_host.cpp's generator). Each product is
 // gterm(acc, F[g], coefficient) with g and the coefficient compile-time constants, so the factors
-// stay in registers; the sums are the same double-float operations in the same order as
-// elem_matrix_ff_kernel, entry (j, i) written with (i, j) as the term tables pair them.
+// stay in registers; entry (j, i) is written with (i, j), sharing the symmetric part, as the term
+// tables pair them (the roundings can differ from elem_matrix_ff_kernel's by ~1e-15 relative).
 template <int D, int L, int VAR>
 struct GenTerms {
     static constexpr bool value = false;
     static constexpr int NG = 1;
-    static __device__ __forceinline__ void run(const float2 (&)[1], float2*) {}
     static __device__ __forceinline__ void run0(const float2 (&)[1], float2*) {}
     static __device__ __forceinline__ void run1(const float2 (&)[1], float2*) {}
     static __device__ __forceinline__ void run2(const float2 (&)[1], float2*) {}
@@ -557,15 +556,15 @@ __device__ __forceinline__ void gterm(float& sh, float& sl, float2 f, float ch, 
 }
 #include "ocmp_terms_gen.h"
 
-// NPART threads per element (one warp per part: NPART = 2 is launched), each running its share of
-// the generated slots (run0 .. run3: quarters balanced by term count) after computing the element's
-// factors; the block's element matrices are staged in shared
-// memory (one padded record per element, so the half-warps' 8-byte writes spread over the banks)
-// and written out as one contiguous run with consecutive threads on consecutive addresses:
-// full-line stores instead of 32 partial lines per warp store.
+// Two threads per element, in two warps: each runs half of the generated slots (run0 + run1 or
+// run2 + run3, quarters balanced by term count) after computing the element's factors; the block's
+// element matrices are staged in shared memory (one padded record per element, so the half-warps'
+// 8-byte writes spread over the banks) and written out as one contiguous run with consecutive
+// threads on consecutive addresses: full-line stores instead of 32 partial lines per warp store.
+// (One or four threads per element time the same or slower.)
 constexpr int kGenElems = 32;
-template <int D, int L, int VAR, int NPART>
-__global__ void __launch_bounds__(32 * NPART) elem_gen_ff_kernel(int64_t ne, const float2* __restrict__ geo,
+template <int D, int L, int VAR>
+__global__ void __launch_bounds__(2 * kGenElems) elem_gen_ff_kernel(int64_t ne, const float2* __restrict__ geo,
                                                                   const int32_t* __restrict__ conn, FormArgs a,
                                                                   float2* __restrict__ K, float2* __restrict__ Kd) {
     using GT = GenTerms<D, L, VAR>;
@@ -614,21 +613,12 @@ __global__ void __launch_bounds__(32 * NPART) elem_gen_ff_kernel(int64_t ne, con
             }
         }
     }
-    if (NPART == 1) {
-        GT::run(F, kst + el * PADLL);
-    } else if (NPART == 2) {
-        if (part == 0) {
-            GT::run0(F, kst + el * PADLL);
-            GT::run1(F, kst + el * PADLL);
-        } else {
-            GT::run2(F, kst + el * PADLL);
-            GT::run3(F, kst + el * PADLL);
-        }
+    if (part == 0) {
+        GT::run0(F, kst + el * PADLL);
+        GT::run1(F, kst + el * PADLL);
     } else {
-        if (part == 0) GT::run0(F, kst + el * PADLL);
-        else if (part == 1) GT::run1(F, kst + el * PADLL);
-        else if (part == 2) GT::run2(F, kst + el * PADLL);
-        else GT::run3(F, kst + el * PADLL);
+        GT::run2(F, kst + el * PADLL);
+        GT::run3(F, kst + el * PADLL);
     }
     }
     __syncthreads();
@@ -1249,9 +1239,10 @@ int assemble_impl(ocmp_matrix_s* m, const ocmp_form_t* f, cudaStream_t st) {
                 kd_ok = true;
 #define OCMP_GEN(V)                                                                                                 \
     do {                                                                                                            \
-        OCMP_CUDA(cudaFuncSetAttribute(elem_gen_ff_kernel<D, L, V, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, \
+        OCMP_CUDA(cudaFuncSetAttribute(elem_gen_ff_kernel<D, L, V>, cudaFuncAttributeMaxDynamicSharedMemorySize,    \
                                        (int)gsm));                                                                  \
-        OCMP_LAUNCH(elem_gen_ff_kernel<D, L, V, 2><<<nblk(ne, kGenElems), 64, gsm, st>>>(ne, s->d_geo_ff, mesh->dconn,  \
+        OCMP_LAUNCH(elem_gen_ff_kernel<D, L, V><<<nblk(ne, kGenElems), 2 * kGenElems, gsm, st>>>(ne, s->d_geo_ff,      \
+                                                                                              mesh->dconn,          \
                                                                                       a, Kff, s->d_Kd));            \
     } while (0)
                 if (var == 0) OCMP_GEN(0);

@@ -1244,8 +1244,9 @@ int ocmp_spmv_axpby(ocmp_matrix_t m, double alpha, const double* x, double beta,
 
 #ifdef OCMP_TERM_GENERATOR
 // Build-time generator (opencmp_gb300/build.py): writes, for the H1 element types of the
-// double-float path, the element-matrix term tables of build_terms as straight-line device code,
-// one function per (dimension, local size, wind variant). With every factor index and coefficient
+// double-float path, the element-matrix term tables of build_terms as straight-line device code:
+// per (dimension, local size, wind variant) four functions, each writing the entries of a quarter
+// of the symmetric slots (quarters balanced by term count). With every factor index and coefficient
 // a compile-time constant, the factors live in registers and the products need no table loads.
 #include <cstdio>
 
@@ -1317,7 +1318,6 @@ int main(int argc, char** argv) {
             std::fprintf(o, "template <> struct GenTerms<%d, %d, %d> {\n    static constexpr bool value = true;\n"
                             "    static constexpr int NG = %d;\n",
                          D, L, var, NG);
-            emit_slots("run", 0, nsl);
             emit_slots("run0", cut[0], cut[1]);
             emit_slots("run1", cut[1], cut[2]);
             emit_slots("run2", cut[2], cut[3]);
