@@ -1,12 +1,15 @@
 """Benchmark: transient 3D convection-diffusion, the OpenCMP hot path on one GB300.
 
-Workload (one "step" = one implicit-Euler time step, exactly what OpenCMP's transient loop does
-per step: reassemble the bilinear and linear forms, refresh the preconditioner, Krylov-solve to a
-1e-8 FP64 relative residual starting from the previous step's solution):
+Workload (one "step" = one implicit-Euler time step, what OpenCMP's transient loop does per step:
+reassemble the bilinear and linear forms, refresh the preconditioner, Krylov-solve to a 1e-8 FP64
+relative residual from the step's initial guess):
   unit cube, 64^3 cubes x 6 tetrahedra (1,572,864 tets), H1 order 2 (2,146,689 dofs), Dirichlet 0 on
   all faces, eps = 1e-2, w = (1, 0.5, 0.25), dt = 1e-3, u0 = Gaussian (sigma 0.1 at (0.25,0.25,0.25)).
-Metric: DOF/s = dofs x steps / time. `value` is the optimised path (FP32-inner GMRES with FP64
-refinement); `plain_fp64` is the plain FP64 GPU path on the same steps.
+Metric: DOF/s = dofs x steps / time. `value` is the optimised path: double-float assembly, FP32-inner
+GMRES with FP64 refinement, and the learned initial guess (cubic extrapolation in time plus a network
+trained on the solver's own trajectories, kept only while its convergence judge sees it save
+iterations). `plain_fp64` is the plain FP64 GPU path (previous-step guess, OpenCMP's) on the same
+steps; `mixed_previous_step_guess` and `mixed_extrapolated_guess` separate the two gains.
 Inputs are resident in HBM and larger than L2 (the matrix alone is ~730 MB), so no L2 flush.
 
 --impl reference: the CPU restatement of the same step (the oracle: C + OpenMP, all host
