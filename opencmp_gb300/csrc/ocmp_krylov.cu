@@ -1716,7 +1716,7 @@ int ocmp_solve(ocmp_solver_t sv, const double* b, double* x, void* stream, ocmp_
 // afford cudaFree's implicit device synchronisation. ocmp_solve_cg_noalloc serves them: it runs the
 // same FP64 Jacobi-preconditioned CG as ocmp_solve with method OCMP_CG, but its workspace (five
 // n-vectors, reduction partials, scalars and flags) lives in the file-scope device arrays below,
-// which the driver allocates once per device when this library is loaded and keeps until exit.
+// which the CUDA driver allocates once per device when this library is loaded and keeps until exit.
 // The caller passes only the assembled matrix, the right-hand side and the initial guess/result.
 namespace {
 
