@@ -29,6 +29,7 @@ from . import _lib as LB
 from . import fem
 from .config import ConfigParser, Expr, load_sub_config, parse, value_map
 from .mesh import load_mesh
+from .saddle import SaddleSolver
 
 
 def _scalar_at(v, t) -> Optional[float]:
@@ -397,8 +398,12 @@ class INS(Model):
     """Incompressible Navier-Stokes (opencmp/models/ins.py) on Taylor-Hood spaces: velocity order
     ``interpolant_order``, pressure one lower, velocity Dirichlet data per label, the Oseen
     linearisation (Picard iteration on the wind, ins.py:323-355) or IMEX (explicit convection,
-    ins.py:302-314). The system is solved by GMRES with the block-diagonal preconditioner of
-    ocmp_th_block_diag (velocity Jacobi, pressure Schur-complement diagonal)."""
+    ins.py:302-314). Where OpenCMP factorises the system (ins.py with its direct default), the
+    transient systems here are solved by flexible GMRES with the Cahouet-Chabard preconditioner
+    (``saddle.SaddleSolver``: velocity Jacobi, pressure Laplacian CG plus pressure mass diagonal),
+    whose iteration counts do not grow with the mesh. ``[SOLVER] preconditioner = local`` and the
+    stationary systems use GMRES with the block-diagonal preconditioner of ocmp_th_block_diag
+    (velocity Jacobi, pressure Schur-complement diagonal)."""
 
     components = ['u', 'p']
 
@@ -427,10 +432,9 @@ class INS(Model):
         self.th = fem.TaylorHood(self.mesh, k, list(self.dirichlet), gmesh=self.gmesh)
         th = self.th
         self.A = th.matrix()
-        P = self.solver_params
-        self.solver = fem.KrylovSolver(self.A, method='GMRES', restart=max(P['restart'], 50), precond='user',
-                                       precision=P['precision'], tol=P['tol'], maxit=P['maxit'],
-                                       inner_tol=P['inner_tol'])
+        self.local_precond = self.config.get_item(['SOLVER', 'preconditioner'], str) == 'local'
+        self.solver = None   # block-diagonal GMRES, made on first use
+        self.saddle = None   # Cahouet-Chabard FGMRES, made on first use
         dev = 'cuda'
         self.u = torch.zeros(th.ndof, dtype=torch.float64, device=dev)
         self.b = torch.zeros_like(self.u)
@@ -490,12 +494,31 @@ class INS(Model):
         v = _vec_at(f, np.zeros((1, 2)), t)[0]
         return (float(v[0]), float(v[1])), None
 
-    def _solve(self):
+    def _solve(self, mass: float, dt: float, tcoef: Optional[float] = None):
+        """Solve the system just assembled into A (mass coefficient `mass`, time step dt, divergence
+        factor tcoef, default dt) for u; a stop at the iteration cap is accepted at the round-off
+        floor (1e-9) when the requested tolerance is below it."""
+        P = self.solver_params
+        accept = 1e-9 if P['tol'] <= 1e-12 else P['tol']
+        if mass > 0.0 and not self.local_precond:
+            if self.saddle is None:
+                self.saddle = SaddleSolver(self.th, self.A, restart=max(P['restart'], 50), tol=P['tol'],
+                                           maxit=P['maxit'], precision=P['precision'])
+            self.saddle.update(mass=mass, dt=dt, nu=self.kv, tcoef=tcoef)
+            info = self.saddle.solve(self.b, self.u, raise_on_fail=False)
+            if info.status != LB.OK and not (info.status == LB.NOT_CONVERGED and np.isfinite(info.relres)
+                                             and info.relres <= accept):
+                raise LB.OcmpError(info.status, 'INS solve: relative residual {:.3e} after {} FGMRES iterations'
+                                   .format(info.relres, info.iterations))
+            return info
+        if self.solver is None:
+            self.solver = fem.KrylovSolver(self.A, method='GMRES', restart=max(P['restart'], 50), precond='user',
+                                           precision=P['precision'], tol=P['tol'], maxit=P['maxit'],
+                                           inner_tol=P['inner_tol'])
         self.th.block_diag(self.A, self.dinv)
         self.solver.set_diag(self.dinv)
         self.solver.update()
-        return checked_solve(self.solver, self.b, self.u, 1e-9 if self.solver_params['tol'] <= 1e-12 else
-                             self.solver_params['tol'])
+        return checked_solve(self.solver, self.b, self.u, accept)
 
     def _push(self):
         self.hist = [self.u.clone()] + self.hist[:-1]
@@ -509,7 +532,7 @@ class INS(Model):
         self.set_dirichlet(t_new)
         th.assemble(self.A, mass=1.0, nu=self.kv, dt=dt)
         th.assemble_rhs(self.b, dt=dt, src=f, src_qp=fq, mass=1.0, uprev=uprev)
-        infos.append(self._solve())
+        infos.append(self._solve(1.0, dt))
         self._push()
 
     def step(self, theta, dt, t_new, t_old, transient, infos):
@@ -533,7 +556,7 @@ class INS(Model):
                 self.Kv = th.matrix()
             th.assemble(self.Kv, mass=0.0, nu=self.kv, dt=dt, tcoef=0.0)
             LB.call('ocmp_spmv_axpby', self.Kv.h, -1.0, fem._ptr(u1), 1.0, fem._ptr(self.b), None)
-            infos.append(self._solve())
+            infos.append(self._solve(1.0, dt, 2.0 * dt))
             self._push()
             return
         if self.linearize == 'IMEX' and self.scheme == 'SBDF':
@@ -546,14 +569,14 @@ class INS(Model):
             th.assemble_rhs(self.b, dt=dt, src=f, src_qp=fq, mass=1.0, uprev=comb, imex=uprev, imex_coef=3.0)
             th.assemble_rhs(self.b, dt=dt, imex=u1, imex_coef=-3.0, accumulate=True)
             th.assemble_rhs(self.b, dt=dt, imex=u2, imex_coef=1.0, accumulate=True)
-            infos.append(self._solve())
+            infos.append(self._solve(11.0 / 6.0, dt))
             self._push()
             return
         if self.linearize == 'IMEX':
             self.set_dirichlet(t_new)
             th.assemble(self.A, mass=mass, nu=self.kv, dt=dt)
             th.assemble_rhs(self.b, dt=dt, src=f, src_qp=fq, mass=mass, uprev=uprev, imex=uprev)
-            infos.append(self._solve())
+            infos.append(self._solve(mass, dt))
             self._push()
             return
         area = float(self.mesh_area())
@@ -561,7 +584,7 @@ class INS(Model):
             self.set_dirichlet(t_new)
             th.assemble(self.A, mass=mass, nu=self.kv, dt=dt, wind=self.W)
             th.assemble_rhs(self.b, dt=dt, src=f, src_qp=fq, mass=mass, uprev=uprev)
-            infos.append(self._solve())
+            infos.append(self._solve(mass, dt))
             d = self.u - self.W
             err, _ = th.errors(d)
             unorm, _ = th.errors(self.u)
