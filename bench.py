@@ -429,12 +429,17 @@ def run_ins(args):
             # here (the run's own first steps, solved from the extrapolated guess; the IMEX matrix is
             # the same every step, so the live matrix serves the residual loss)
             step('extrap' if p in ('extrap', 'learned') else p, u, st, collect=p == 'learned')
-        if p == 'learned':
+        if p == 'learned' and guess.samples:
             l_before = guess.eval_loss()
             guess.train(steps=args.train_iters, lr=3e-3)
             train_info = dict(samples=len(guess.samples), adam_steps=args.train_iters, loss_before=l_before,
                               loss_after=guess.eval_loss(), seconds=time.perf_counter() - t_tr)
             guess.drop_samples()
+            guess.reset_judge()
+        elif p == 'learned':
+            # samples start once the history holds guess_k steps: with fewer untimed steps the
+            # network keeps its zero output and the learned path is the extrapolation
+            train_info = dict(samples=0, adam_steps=0)
             guess.reset_judge()
         st.clear()
         torch.cuda.synchronize()
@@ -652,7 +657,8 @@ def main():
     ap.add_argument('--no-cpu', action='store_true')
     ap.add_argument('--config', default='transient3d', choices=['transient3d', 'batched', 'ins'])
     ap.add_argument('--n-ins', type=int, default=256)
-    ap.add_argument('--ins-train', type=int, default=100, help='untimed first INS steps (training samples)')
+    ap.add_argument('--ins-train', type=int, default=100,
+                    help='untimed first INS steps (training samples from step guess_k + 1 on)')
     ap.add_argument('--ins-maxit', type=int, default=1000, help='FGMRES iteration cap per INS step')
     ap.add_argument('--instances', type=int, default=512)
     ap.add_argument('--restart-batch', type=int, default=50)
