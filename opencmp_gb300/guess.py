@@ -212,17 +212,29 @@ class LearnedGuess:
 
     def train(self, steps: int = 300, lr: float = 3e-3, seed: int = 0) -> List[float]:
         """Adam over the stored samples (one whole step per iteration, cosine learning rate) on the
-        weighted residual loss; returns the loss history (1 = the extrapolation's residual)."""
+        weighted residual loss; returns the loss history (1 = the extrapolation's residual).
+
+        The mean loss over all samples is evaluated ten times along the way, and the parameters with
+        the lowest one are kept, the untrained network (mean loss 1) included: on few samples from a
+        fast transient the steps can overshoot, and training then never ends worse than the
+        extrapolation on its own samples."""
         if not self.samples:
             raise RuntimeError('no training samples collected')
         rng = np.random.default_rng(seed)
         losses = []
+        best_p, best = self.net.params(), self.eval_loss()
+        every = max(1, steps // 10)
         for it in range(steps):
             smp = self.samples[int(rng.integers(len(self.samples)))]
             self.net.forward(smp['X'], self.Y)
             losses.append(self._loss(smp, self.Y))
             self.net.backward(smp['X'], self.dY)
             self.net.adam_step(lr * (0.5 * (1 + np.cos(np.pi * it / steps))) + 1e-5)
+            if (it + 1) % every == 0 or it + 1 == steps:
+                cur = self.eval_loss()
+                if cur < best:
+                    best_p, best = self.net.params(), cur
+        self.net.set_params(best_p)
         self.trained = True
         return losses
 

@@ -286,3 +286,48 @@ def test_guess_judge_falls_back_without_gain():
     g.judge(_Info(4, 3e-8), PROBE)
     g.judge(_Info(3, 5e-8), NET)
     assert not g.enabled and 'initial residual' in g.fallback_reason
+
+
+def test_training_keeps_the_best_parameters():
+    """Host-side training loop (no GPU): when the Adam steps overshoot, train() ends on the
+    checkpoint with the lowest mean loss, the untrained network (loss 1) included."""
+    from opencmp_gb300.guess import LearnedGuess
+
+    class Net:
+        def __init__(self):
+            self.p = np.zeros(3, np.float32)
+
+        def params(self):
+            return self.p.copy()
+
+        def set_params(self, p):
+            self.p = np.asarray(p, np.float32).copy()
+
+        def forward(self, X, Y):
+            pass
+
+        def backward(self, X, dY):
+            pass
+
+        def adam_step(self, lr):
+            self.p = self.p + 1.0
+
+    def run(curve, steps=20):
+        g = LearnedGuess.__new__(LearnedGuess)
+        g.samples = [{'X': None}]
+        g.net, g.Y, g.dY = Net(), None, None
+        g._loss = lambda smp, Y: curve(float(g.net.p[0]))
+        g.eval_loss = lambda: curve(float(g.net.p[0]))
+        g.train(steps=steps)
+        return float(g.net.p[0]), g.trained
+
+    # the loss rises from the start: the untrained parameters are kept
+    assert run(lambda s: 1.0 + s) == (0.0, True)
+    # the loss falls to its lowest at 8 steps and rises again: the checkpoint at 8 (every 2 steps)
+    assert run(lambda s: 1.0 + (s - 8.0) ** 2 / 100.0 - 0.64) == (8.0, True)
+    # the loss falls all the way: the last parameters
+    assert run(lambda s: 1.0 / (1.0 + s)) == (20.0, True)
+    with pytest.raises(RuntimeError):
+        g = LearnedGuess.__new__(LearnedGuess)
+        g.samples = []
+        g.train()
