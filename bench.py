@@ -14,6 +14,9 @@ Inputs are resident in HBM and larger than L2 (the matrix alone is ~730 MB), so 
 
 --impl reference: the CPU restatement of the same step (the oracle: C + OpenMP, all host
 threads) on a bounded sample, the 32^3 x 6 mesh (274,625 dofs), since NGSolve cannot run here.
+--config batched: 512 steady 2D convection-diffusion instances of mixed mesh sizes and orders.
+--config ins: the Navier-Stokes lid-driven cavity (Taylor-Hood, Euler IMEX, flexible GMRES with the
+Cahouet-Chabard pressure preconditioner).
 """
 from __future__ import annotations
 
