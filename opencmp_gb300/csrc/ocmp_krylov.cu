@@ -240,20 +240,6 @@ __global__ void block_jacobi_setup(int64_t ne, const int32_t* __restrict__ rp, c
         }
 }
 
-// v_j = w * inv ; z = P v_j (Jacobi fused; block-Jacobi done by block_prec afterwards)
-template <class T>
-__global__ void scale_prec(int64_t n, const T* __restrict__ w, const double* __restrict__ st, T* __restrict__ v,
-                           const T* __restrict__ dinv, T* __restrict__ z, const int* __restrict__ flags) {
-    if (flags[F_CONV]) return;
-    const T inv = (T)st[S_INV];
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-        const T vi = w[i] * inv;
-        v[i] = vi;
-        if (dinv) z[i] = dinv[i] * vi;
-        else if (z != v) z[i] = vi;
-    }
-}
-
 template <class T, int L>
 __global__ void block_prec(int64_t ne, const T* __restrict__ Binv, const T* __restrict__ v, T* __restrict__ z,
                            const int* __restrict__ flags) {
@@ -266,169 +252,6 @@ __global__ void block_prec(int64_t ne, const T* __restrict__ Binv, const T* __re
 #pragma unroll
     for (int j = 0; j < L; j++) acc += Binv[(e * L + i) * L + j] * v[e * L + j];
     z[t] = acc;
-}
-
-// partials of  V_k . w  for k in [k0, k0 + 8) (k <= j) and, in chunk 0, w . w
-template <class T>
-__global__ void mdot_kernel(int64_t n, int j, const T* __restrict__ V, const T* __restrict__ w,
-                            double* __restrict__ part, int nb, const int* __restrict__ flags, int gate) {
-    if (flags[F_CONV] || (gate >= 0 && flags[gate] == 0)) return;
-    const int k0 = blockIdx.y * 8;
-    T acc[9];
-#pragma unroll
-    for (int k = 0; k < 9; k++) acc[k] = 0;
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-        const T wi = w[i];
-#pragma unroll
-        for (int k = 0; k < 8; k++)
-            if (k0 + k <= j) acc[k] += V[(int64_t)(k0 + k) * n + i] * wi;
-        if (k0 == 0) acc[8] += wi * wi;
-    }
-#pragma unroll
-    for (int k = 0; k < 8; k++)
-        if (k0 + k <= j) {
-            double s = block_sum(acc[k]);
-            if (threadIdx.x == 0) part[(int64_t)(k0 + k) * nb + blockIdx.x] = s;
-        }
-    if (k0 == 0) {
-        double s = block_sum(acc[8]);
-        if (threadIdx.x == 0) part[(int64_t)(j + 1) * nb + blockIdx.x] = s;
-    }
-}
-
-// w -= sum_k h[k] V_k (k <= j); partial of |w|^2 into slot 0
-template <class T>
-__global__ void axpy_norm_kernel(int64_t n, int j, const T* __restrict__ V, const double* __restrict__ h,
-                                 T* __restrict__ w, double* __restrict__ part, const int* __restrict__ flags,
-                                 int gate) {
-    if (flags[F_CONV] || (gate >= 0 && flags[gate] == 0)) return;
-    __shared__ T hs[130];
-    for (int k = threadIdx.x; k <= j; k += blockDim.x) hs[k] = (T)h[k];
-    __syncthreads();
-    T acc = 0;
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-        T wi = w[i];
-        for (int k = 0; k <= j; k++) wi -= hs[k] * V[(int64_t)k * n + i];
-        w[i] = wi;
-        acc += wi * wi;
-    }
-    double s = block_sum(acc);
-    if (threadIdx.x == 0) part[blockIdx.x] = s;
-}
-
-// after the first orthogonalisation: decide on a second pass ("twice is enough" test)
-__global__ void reorth_check(const double* __restrict__ red, int j, double* st, int* flags) {
-    if (flags[F_CONV]) return;
-    const double nw2 = red[j + 1];  // |w|^2 before orthogonalisation
-    st[S_NW2] = nw2;
-    flags[F_REORTH] = 0;
-}
-__global__ void reorth_decide(const double* __restrict__ hn2, double* st, int* flags) {
-    if (flags[F_CONV]) return;
-    st[S_HN2] = hn2[0];
-    flags[F_REORTH] = (hn2[0] < 0.49 * st[S_NW2]) ? 1 : 0;
-}
-
-// Hessenberg column j from h (first pass) and h2 (second pass, gated), Givens rotations,
-// residual estimate, flags.
-__global__ void givens_kernel(int m, int j, double* __restrict__ H, const double* __restrict__ h,
-                              const double* __restrict__ h2, const double* __restrict__ hn2b, double* st, int* flags,
-                              double* __restrict__ cs_sn_g) {
-    if (flags[F_CONV]) return;
-    double* cs = cs_sn_g;
-    double* sn = cs_sn_g + m;
-    double* g = cs_sn_g + 2 * m;
-    const bool re = flags[F_REORTH] != 0;
-    double hn2 = re ? hn2b[0] : st[S_HN2];
-    for (int k = 0; k <= j; k++) H[k * m + j] = h[k] + (re ? h2[k] : 0.0);
-    double hn = sqrt(fmax(hn2, 0.0));
-    H[(j + 1) * m + j] = hn;
-    for (int k = 0; k < j; k++) {
-        const double a = H[k * m + j], b = H[(k + 1) * m + j];
-        H[k * m + j] = cs[k] * a + sn[k] * b;
-        H[(k + 1) * m + j] = -sn[k] * a + cs[k] * b;
-    }
-    const double a = H[j * m + j], b = H[(j + 1) * m + j];
-    const double d = sqrt(a * a + b * b);
-    flags[F_ITERS] += 1;
-    flags[F_JDONE] = j + 1;
-    if (!isfinite(d) || !isfinite(hn)) {
-        flags[F_NONFIN] = 1;
-        flags[F_CONV] = 1;
-        flags[F_JDONE] = j;  // drop the bad column
-        return;
-    }
-    if (d == 0.0) {
-        flags[F_BREAK] = 1;
-        flags[F_CONV] = 1;
-        flags[F_JDONE] = j;
-        return;
-    }
-    cs[j] = a / d;
-    sn[j] = b / d;
-    H[j * m + j] = d;
-    H[(j + 1) * m + j] = 0;
-    g[j + 1] = -sn[j] * g[j];
-    g[j] = cs[j] * g[j];
-    const double res = fabs(g[j + 1]) / st[S_NB];
-    st[S_RES] = res;
-    st[S_INV] = hn > 0 ? 1.0 / hn : 0.0;
-    if (res <= st[S_TOL] || hn == 0.0) flags[F_CONV] = 1;
-}
-
-// start of a cycle: beta = |r|, g = beta e1, inv = 1/beta; converged if beta/nb <= tol
-__global__ void cycle_start(const double* __restrict__ red, double* st, int* flags, double* __restrict__ cs_sn_g,
-                            int m) {
-    const double beta = sqrt(fmax(red[0], 0.0));
-    st[S_BETA] = beta;
-    double* g = cs_sn_g + 2 * m;
-    for (int k = 0; k <= m; k++) g[k] = 0;
-    g[0] = beta;
-    st[S_INV] = beta > 0 ? 1.0 / beta : 0.0;
-    st[S_RES] = beta / st[S_NB];
-    flags[F_JDONE] = 0;
-    flags[F_REORTH] = 0;
-    if (!isfinite(beta)) {
-        flags[F_NONFIN] = 1;
-        flags[F_CONV] = 1;
-    } else
-        flags[F_CONV] = (beta / st[S_NB] <= st[S_TOL]) ? 1 : 0;
-}
-
-// y = H^-1 g over the completed columns, then coefficients stored in y
-__global__ void trisolve_kernel(int m, const double* __restrict__ H, const double* __restrict__ cs_sn_g,
-                                double* __restrict__ y, const int* flags) {
-    const int jd = flags[F_JDONE];
-    const double* g = cs_sn_g + 2 * m;
-    for (int k = jd - 1; k >= 0; k--) {
-        double acc = g[k];
-        for (int l = k + 1; l < jd; l++) acc -= H[k * m + l] * y[l];
-        y[k] = acc / H[k * m + k];
-    }
-}
-
-// u = sum_k y_k V_k  (k < jdone)
-template <class T>
-__global__ void combine_kernel(int64_t n, const T* __restrict__ V, const double* __restrict__ y,
-                               const int* __restrict__ flags, T* __restrict__ u) {
-    __shared__ T ys[130];
-    const int jd = flags[F_JDONE];
-    for (int k = threadIdx.x; k < jd; k += blockDim.x) ys[k] = (T)y[k];
-    __syncthreads();
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-        T acc = 0;
-        for (int k = 0; k < jd; k++) acc += ys[k] * V[(int64_t)k * n + i];
-        u[i] = acc;
-    }
-}
-
-// x += P u  (Jacobi fused; for block-Jacobi the caller applied the blocks into z already)
-template <class TX, class T>
-__global__ void xupdate_kernel(int64_t n, const T* __restrict__ u, const T* __restrict__ dinv, TX* __restrict__ x) {
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-        const T z = dinv ? dinv[i] * u[i] : u[i];
-        x[i] += (TX)z;
-    }
 }
 
 // ---- CG pieces
@@ -1082,11 +905,6 @@ __global__ void gm_scale_matrix(int64_t n, const int32_t* __restrict__ rp, const
 __global__ void gm_cast(int64_t n, const double* __restrict__ a, float* __restrict__ b) {
     const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (i < n) b[i] = (float)a[i];
-}
-
-__global__ void gm_copy(int64_t n, const double* __restrict__ a, double* __restrict__ b) {
-    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    if (i < n) b[i] = a[i];
 }
 
 __global__ void gm_set_tols(double* st, double tol, double inner, double eta2, int nb, int64_t stride) {
