@@ -207,3 +207,46 @@ def test_gpu_saddle_solver_matches_oracle(gpu_lib, oracle, precision):
         assert info.inner_iterations > 0
         its.append(info.iterations)
     assert its[1] <= 1.25 * its[0] + 5 and its[1] <= 200, its
+
+
+def test_fgmres_edge_cases():
+    """Host FGMRES on small dense systems (CPU tensors): an exact preconditioner converges in one
+    iteration (lucky breakdown, |w| = 0); a zero operator reports BREAKDOWN and leaves x alone;
+    constrained entries of x are kept; a zero right-hand side with a zero free part returns at once."""
+    import torch
+    from opencmp_gb300 import _lib as LB
+    from opencmp_gb300.saddle import fgmres
+    rng = np.random.default_rng(1)
+    n = 12
+    A = rng.standard_normal((n, n)) + n * np.eye(n)
+    free = np.ones(n, bool)
+    free[[0, 5]] = False
+    b = torch.from_numpy(rng.standard_normal(n))
+    x = torch.zeros(n, dtype=torch.float64)
+    x[0], x[5] = 2.0, -1.0
+    fr = torch.from_numpy(free)
+
+    def mv(v, out):
+        out.copy_(torch.from_numpy(A @ v.numpy()))
+
+    # exact inverse of the free block as the preconditioner
+    Aff = A[np.ix_(free, free)]
+    Affi = np.linalg.inv(Aff)
+
+    def exact(r, z):
+        zn = np.zeros(n)
+        zn[free] = Affi @ r.numpy()[free]
+        z.copy_(torch.from_numpy(zn))
+    info = fgmres(mv, exact, b, x, fr, restart=10, tol=1e-12)
+    assert info.status == LB.OK and info.iterations == 1 and info.relres <= 1e-12
+    assert x[0] == 2.0 and x[5] == -1.0
+    xs = x.numpy()
+    assert np.allclose(A[free] @ xs, b.numpy()[free], rtol=0, atol=1e-10)
+    # zero operator: breakdown, x untouched
+    x2 = torch.zeros(n, dtype=torch.float64)
+    info2 = fgmres(lambda v, out: out.zero_(), lambda r, z: z.copy_(r * fr), b, x2, fr, restart=10, tol=1e-8)
+    assert info2.status == LB.BREAKDOWN and info2.iterations == 1 and float(x2.abs().max()) == 0.0
+    # zero right-hand side and zero free part: already converged (relres 0 over a unit norm)
+    x3 = torch.zeros(n, dtype=torch.float64)
+    info3 = fgmres(mv, exact, torch.zeros(n, dtype=torch.float64), x3, torch.ones(n, dtype=torch.bool), tol=1e-8)
+    assert info3.status == LB.OK and info3.iterations == 0 and info3.relres == 0.0
