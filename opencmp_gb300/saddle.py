@@ -41,6 +41,7 @@ import numpy as np
 import torch
 
 from . import _lib as LB
+from . import fem
 
 
 class FGMRESInfo:
@@ -164,8 +165,6 @@ class SaddleSolver:
 
     def __init__(self, th, A, restart: int = 50, tol: float = 1e-8, maxit: int = 2000, inner_tol: float = 0.1,
                  inner_maxit: int = 1000, precision: str = 'fp64', eps_p: float = 1e-10):
-        from . import fem
-        self.fem = fem
         self.th, self.A = th, A
         self.restart, self.tol, self.maxit = restart, tol, maxit
         self.inner_tol, self.inner_maxit = inner_tol, inner_maxit
@@ -189,7 +188,6 @@ class SaddleSolver:
         """(Re)assemble L_p + delta M_p and its inner CG solver when delta changes."""
         if self.delta == delta:
             return
-        fem = self.fem
         self.Lp.assemble(fem.make_form(mass=delta, diff=1.0))
         self.inner = fem.KrylovSolver(self.Lp, method='CG', precond='jacobi', precision=self.precision,
                                       tol=self.inner_tol, maxit=self.inner_maxit, inner_tol=self.inner_tol)
