@@ -330,17 +330,20 @@ int ocmp_spmv_transpose(ocmp_matrix_t mat, const double* x_dev, double* y_dev, v
 
 /* ---------------------------------------------------------------- allocation-free solve
  * No counterpart in the reference: an addition for callers that cannot call cudaMalloc when they
- * solve (a stream being captured into a CUDA graph in global capture mode, a host whose device
- * memory belongs to another allocator's fixed pool, a loop that cannot take cudaFree's implicit
- * device synchronisation). Same FP64 Jacobi-preconditioned CG as ocmp_solve with OCMP_CG, on the
- * free dofs of `mat`, to the same relative-residual definition; it allocates nothing. Its
- * workspace is a static device array of 41 MiB that every GPU which loads this library holds until
- * the process exits; systems with more than OCMP_NOALLOC_MAX_NDOF dofs are rejected with
- * OCMP_ERR_ARG. The first call on each device looks up that array's device address
- * (cudaGetSymbolAddress) with the device current: make that first call before any stream capture.
- * All calls share the one workspace and it keeps the last call's contents (the call resets what
- * must start at zero): calls whose work overlaps on the GPU (different streams or threads) race,
- * so serialise them. */
+ * solve - a host whose device memory belongs to another allocator's fixed pool (a fresh cudaMalloc
+ * would take memory that pool has already claimed, or fail), or a loop that cannot take the
+ * implicit device-wide synchronisation of cudaFree. Same FP64 Jacobi-preconditioned CG as
+ * ocmp_solve with OCMP_CG, on the free dofs of `mat`, to the same relative-residual definition; it
+ * allocates nothing (no cudaMalloc, cudaFree or allocating library call). Its workspace is a static
+ * device array of 41 MiB that every GPU which loads this library holds until the process exits;
+ * systems with more than OCMP_NOALLOC_MAX_NDOF dofs are rejected with OCMP_ERR_ARG, batched
+ * matrices (B > 1) with OCMP_ERR_UNSUPPORTED. The first call on each device looks up that array's
+ * device address (cudaGetSymbolAddress) with the device current. All calls share the one workspace
+ * and it keeps the last call's contents (each call resets what must start at zero): calls whose
+ * work overlaps on the GPU (different streams or threads) race, so serialise them. The host reads
+ * the convergence flags every 8 iterations through a blocking copy into its own stack memory (no
+ * pinned buffer is allocated for it), and the call returns OCMP_ERR_UNSUPPORTED on a stream that is
+ * being captured, since those reads would invalidate the capture. */
 #define OCMP_NOALLOC_MAX_NDOF 1048576
 int ocmp_solve_cg_noalloc(ocmp_matrix_t mat, const double* b_dev, double* x_dev, double tol, int32_t maxit,
                           void* stream, ocmp_solve_info_t* info);

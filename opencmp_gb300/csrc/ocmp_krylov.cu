@@ -1528,10 +1528,10 @@ int ocmp_solve(ocmp_solver_t sv, const double* b, double* x, void* stream, ocmp_
 }  // extern "C"
 
 // ---------------------------------------------------------------------------------------------
-// Allocation-free CG. Some callers cannot call cudaMalloc at the moment they need a solve: code
-// that runs while a stream is being captured into a CUDA graph in global capture mode, hosts whose
-// device memory belongs to another allocator's fixed pool, and latency-bound loops that cannot
-// afford cudaFree's implicit device synchronisation. ocmp_solve_cg_noalloc serves them: it runs the
+// Allocation-free CG. Some callers cannot call cudaMalloc at the moment they need a solve: hosts
+// whose device memory belongs to another allocator's fixed pool (cudaMalloc would take memory that
+// pool has already claimed, or fail), and loops that cannot take the implicit device-wide
+// synchronisation of cudaFree. ocmp_solve_cg_noalloc serves them: it runs the
 // same FP64 Jacobi-preconditioned CG as ocmp_solve with method OCMP_CG, but its workspace (five
 // n-vectors, reduction partials, scalars and flags) lives in the file-scope device arrays below,
 // which the CUDA driver allocates once per device when this library is loaded and keeps until exit.
@@ -1578,6 +1578,16 @@ int noalloc_scratch(double** scratch, int** flags) {
 extern "C" int ocmp_solve_cg_noalloc(ocmp_matrix_t mat, const double* b, double* x, double tol, int32_t maxit,
                                      void* stream, ocmp_solve_info_t* info) {
     if (!mat || !b || !x) return fail(OCMP_ERR_ARG, "ocmp_solve_cg_noalloc: null argument");
+    if (mat->B != 1) return fail(OCMP_ERR_UNSUPPORTED, "ocmp_solve_cg_noalloc: batched matrices are not supported");
+    {
+        // the solve reads its convergence flags on the host (stream synchronisation, device-to-host
+        // copies); on a stream under capture those calls would invalidate the caller's capture
+        cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+        OCMP_CUDA(cudaStreamIsCapturing((cudaStream_t)stream, &cs));
+        if (cs != cudaStreamCaptureStatusNone)
+            return fail(OCMP_ERR_UNSUPPORTED, "ocmp_solve_cg_noalloc: the stream is being captured; the solve "
+                                              "synchronises with the host and cannot run under capture");
+    }
     ocmp_space_s* s = mat->space;
     const int64_t n = s->ndof;
     if (n > kNoAllocMaxN)

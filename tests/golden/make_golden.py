@@ -1,7 +1,7 @@
 """Generates the golden fixtures under tests/golden/ from the OpenCMP reference tree.
 
-Run in a container where the reference is mounted (default path /root/reference, or pass it as
-the first argument). The reference's Python package cannot be imported there (NGSolve and
+Run where the OpenCMP source tree is available: pass its path as the first argument, or set
+OPENCMP_REFERENCE. The reference's Python package cannot be imported there (NGSolve and
 pyparsing are absent), so the fixtures are its test inputs and pinned numbers, read as data:
 
 * unit_square_coarse.npz - pytests/mesh_files/unit_square_coarse.vol (the mesh both the
@@ -34,7 +34,10 @@ FIXTURES = ['poisson/transient_coarse', 'poisson/h_convergence', 'mcins/diffusio
 MESHES = ['unit_square_coarse.vol', 'square.msh', 'coarse_large_square_4bcs.vol']
 
 
-def main(ref='/root/reference'):
+def main(ref=None):
+    ref = ref or os.environ.get('OPENCMP_REFERENCE')
+    if not ref:
+        raise SystemExit('usage: make_golden.py <path of the OpenCMP source tree> (or set OPENCMP_REFERENCE)')
     m = load_mesh(os.path.join(ref, 'pytests/mesh_files/unit_square_coarse.vol'))
     np.savez(os.path.join(HERE, 'unit_square_coarse.npz'), coords=m.coords, elements=m.elements,
              bfacets=m.bfacets, blabels=m.blabels, bc_names=np.array(m.bc_names))
