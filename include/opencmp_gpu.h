@@ -55,7 +55,7 @@ enum { OCMP_H1 = 0, OCMP_L2 = 1, OCMP_COMPOUND = 2 };  /* compound: the Taylor-H
 enum { OCMP_WIND_NONE = 0, OCMP_WIND_CONST = 1, OCMP_WIND_VERTEX = 2 };
 enum { OCMP_SRC_NONE = 0, OCMP_SRC_CONST = 1, OCMP_SRC_QP = 2 };
 enum { OCMP_CG = 0, OCMP_GMRES = 1 };
-enum { OCMP_PRE_NONE = 0, OCMP_PRE_JACOBI = 1, OCMP_PRE_BLOCK_JACOBI = 2, OCMP_PRE_USER = 3 };
+enum { OCMP_PRE_NONE = 0, OCMP_PRE_JACOBI = 1, OCMP_PRE_BLOCK_JACOBI = 2, OCMP_PRE_USER = 3, OCMP_PRE_STRIP = 4 };
 enum { OCMP_FP64 = 0, OCMP_MIXED = 1 };
 
 typedef struct ocmp_mesh_s* ocmp_mesh_t;
@@ -221,11 +221,49 @@ int ocmp_solver_set_graph(ocmp_solver_t solver, int32_t on);
 /* OCMP_PRE_USER: the inverse diagonal (ndof, device) applied as the preconditioner; copied, and
  * taken over by the next ocmp_solver_update. */
 int ocmp_solver_set_diag(ocmp_solver_t solver, const double* dinv_dev, void* stream);
-/* Time every GMRES SpMV launch with CUDA events on its stream (single solves, outside graphs);
- * ocmp_solver_spmv_stats returns the launches timed and their total milliseconds since the timing
- * was switched on. No counterpart in the reference (measurement). */
+/* Time every GMRES SpMV launch with CUDA events on its stream (single solves, outside graphs; up to
+ * 4096 launches per solve); ocmp_solver_spmv_stats returns the launches that did the product (not
+ * those queued past convergence, which return at once) and their total milliseconds since the
+ * timing was switched on. No counterpart in the reference (measurement). */
 int ocmp_solver_spmv_timing(ocmp_solver_t solver, int32_t on);
 int ocmp_solver_spmv_stats(ocmp_solver_t solver, int64_t* launches, double* total_ms);
+
+/* ---------------------------------------------------------------- strip direct preconditioner
+ * OCMP_PRE_STRIP replaces the sparse direct solve of opencmp/models/base_model.py:906-922
+ * (a.mat.Inverse(freedofs, 'pardiso' | 'umfpack'), then gfu += inv (L - A gfu)) by an exact block
+ * factorisation used as the preconditioner of GMRES, whose FP64 residual decides convergence. The
+ * dofs are cut into consecutive strips over which the matrix is block tridiagonal (greedy over the
+ * row bandwidth: number the dofs so that the matrix is banded, e.g. the element-major L2 dofs of a
+ * structured mesh whose elements run row by row); each strip's Schur complement is inverted
+ * explicitly in FP32 by block Gauss-Jordan with 128 x 128 pivot tiles, and a preconditioner
+ * application is one forward and one backward sweep of dense matrix-vector products. Built by
+ * ocmp_solver_create (OCMP_ERR_UNSUPPORTED when the pattern has no such strips or a strip exceeds
+ * 16384 dofs), factorised by ocmp_solver_create and every ocmp_solver_update; GMRES only.
+ * ocmp_solver_strip_stats reports the last factorisation. No counterpart in the reference beyond
+ * the direct solve it replaces. */
+typedef struct {
+    int64_t nstrips;         /* strips                                                             */
+    int64_t max_strip;       /* largest strip, padded to a multiple of 128                          */
+    int64_t bytes;           /* device memory of the factorisation                                  */
+    double factor_ms;        /* wall time of the last factorisation on its stream (CUDA events)     */
+    double gemm_ms;          /* time inside the dense products (0 unless ocmp_solver_strip_timing)  */
+    double gemm_flops;       /* flops of those products                                             */
+    int32_t singular_tiles;  /* pivot tiles that met a zero or non-finite pivot                     */
+    int32_t gemm_kind;       /* 0: FP32 SIMT products, 1: tensor-core (tcgen05, 3xTF32) products    */
+} ocmp_strip_stats_t;
+int ocmp_solver_strip_stats(ocmp_solver_t solver, ocmp_strip_stats_t* out);
+/* time every dense product of the next factorisations with CUDA events (measurement) */
+int ocmp_solver_strip_timing(ocmp_solver_t solver, int32_t on);
+/* dense products of the next factorisations: 0 FP32 SIMT (the default), 1 tensor cores */
+int ocmp_solver_strip_gemm(ocmp_solver_t solver, int32_t kind);
+/* C = beta C + alpha A B^T in FP32, row-major, K contiguous in A (M x K) and B (N x K): the dense
+ * product of the strip factorisation, exposed for tests and measurement. kind 0: FP32 SIMT (K a
+ * multiple of 16); kind 1: tcgen05 tensor cores, TF32 products with the 3xTF32 split for FP32
+ * accuracy, operands staged by TMA (K a multiple of 32, operands 16-byte aligned). M and N are
+ * multiples of 128. Synchronises the stream for kind 1 (it reads the kernel's wait flag). No
+ * counterpart in the reference. */
+int ocmp_dense_gemm_nt(int32_t kind, int32_t M, int32_t N, int32_t K, const float* A, int64_t lda, const float* B,
+                       int64_t ldb, float* C, int64_t ldc, float alpha, float beta, void* stream);
 
 /* ---------------------------------------------------------------- incompressible Navier-Stokes
  * Taylor-Hood system of OpenCMP's INS model (opencmp/models/ins.py) on triangles: velocity H1

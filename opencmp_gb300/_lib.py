@@ -18,7 +18,7 @@ H1, L2, COMPOUND = 0, 1, 2
 WIND_NONE, WIND_CONST, WIND_VERTEX = 0, 1, 2
 SRC_NONE, SRC_CONST, SRC_QP = 0, 1, 2
 CG, GMRES = 0, 1
-PRE_NONE, PRE_JACOBI, PRE_BLOCK_JACOBI, PRE_USER = 0, 1, 2, 3
+PRE_NONE, PRE_JACOBI, PRE_BLOCK_JACOBI, PRE_USER, PRE_STRIP = 0, 1, 2, 3, 4
 FP64, MIXED = 0, 1
 
 
@@ -68,6 +68,12 @@ class SolveParams(C.Structure):
 class SolveInfo(C.Structure):
     _fields_ = [('status', C.c_int32), ('iterations', C.c_int32), ('outer_iterations', C.c_int32),
                 ('relres0', C.c_double), ('relres', C.c_double)]
+
+
+class StripStats(C.Structure):
+    _fields_ = [('nstrips', C.c_int64), ('max_strip', C.c_int64), ('bytes', C.c_int64), ('factor_ms', C.c_double),
+                ('gemm_ms', C.c_double), ('gemm_flops', C.c_double), ('singular_tiles', C.c_int32),
+                ('gemm_kind', C.c_int32)]
 
 
 P = C.c_void_p
@@ -124,6 +130,10 @@ SIGNATURES = {
     'ocmp_solver_update': [P, P],
     'ocmp_solve': [P, P, P, P, C.POINTER(SolveInfo)],
     'ocmp_solve_cg_noalloc': [P, P, P, D, I32, P, C.POINTER(SolveInfo)],
+    'ocmp_solver_strip_stats': [P, C.POINTER(StripStats)],
+    'ocmp_solver_strip_timing': [P, I32],
+    'ocmp_solver_strip_gemm': [P, I32],
+    'ocmp_dense_gemm_nt': [I32, I32, I32, I32, P, I64, P, I64, P, I64, C.c_float, C.c_float, P],
     'ocmp_guess_create': [I32, C.c_uint64, C.POINTER(P)],
     'ocmp_guess_destroy': [P],
     'ocmp_guess_nparams': [P],

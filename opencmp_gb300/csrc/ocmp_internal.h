@@ -179,6 +179,25 @@ int launch_l2_error(ocmp_space_s* s, const double* u, const double* fq, double f
 int launch_spmv64(const ocmp_space_s* s, const double* vals, const double* x, double* y, cudaStream_t st);
 int launch_spmv_axpby(const ocmp_space_s* s, const double* vals, double alpha, const double* x, double beta, double* y,
                       cudaStream_t st);
+// strip direct preconditioner (ocmp_strip.cu)
+struct Strip;
+int strip_create(const ocmp_space_s* s, Strip** out);
+void strip_destroy(Strip* p);
+int strip_factor(Strip* p, const ocmp_space_s* s, const double* vals, cudaStream_t st);
+// z = M^-1 (sc v), sc = scale[j] (scale != null) or 1; z may alias v; kernels return at once when
+// flags[0] (the solver's convergence flag) is set
+template <class T>
+int strip_apply(Strip* p, const ocmp_space_s* s, const double* vals, const T* v, const double* scale, int j, T* z,
+                const int* flags, cudaStream_t st);
+template <class T>
+int strip_add(int64_t n, const T* z, double* x, cudaStream_t st);
+void strip_stats(const Strip* p, ocmp_strip_stats_t* out);
+void strip_set_timing(Strip* p, bool on);
+void strip_set_gemm(Strip* p, int kind);
+// C = beta C + alpha A B^T on the tensor cores (ocmp_tcgemm.cu): FP32 operands, 3xTF32 products;
+// M, N multiples of 128, K of 32; *err set when a bounded wait gave up
+int tc_gemm_nt(int M, int N, int K, const float* A, int64_t lda, const float* B, int64_t ldb, float* C, int64_t ldc,
+               float alpha, float beta, int* err, cudaStream_t st);
 int autotune_spmv(ocmp_space_s* s, const double* vals, const double* x, double* y, cudaStream_t st, int reps,
                   int* best_tpr, int* best_u, float* best_ms);
 }  // namespace ocmp

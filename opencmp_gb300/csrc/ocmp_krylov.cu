@@ -42,6 +42,7 @@ struct ocmp_solver_s {
     double* udiag = nullptr;    // caller's inverse diagonal (OCMP_PRE_USER)
     bool udiag_set = false;
     double* Binv = nullptr;     // block Jacobi (L2 element blocks)
+    ocmp::Strip* strip = nullptr;  // strip direct preconditioner (OCMP_PRE_STRIP)
     double* V = nullptr;        // (m+1) x n
     double* w = nullptr;
     double* z = nullptr;
@@ -82,6 +83,8 @@ struct ocmp_solver_s {
     bool time_spmv = false;
     std::vector<cudaEvent_t> tev;
     size_t tev_used = 0;
+    int* worklog = nullptr;     // per timed launch: 1 if it ran (not past convergence), written by the kernel
+    int worklog_cap = 0;
     int64_t spmv_launches = 0;
     double spmv_ms = 0;
     cudaStream_t gstream = nullptr;   // capture/launch stream when the caller passes the default stream
@@ -740,7 +743,7 @@ __global__ void __launch_bounds__(256) gm_spmv(int64_t n, int j, const int32_t* 
                                                const int32_t* __restrict__ col, const T* __restrict__ A,
                                                const uint8_t* __restrict__ freed, const T* __restrict__ xin,
                                                int xin_is_basis, T* __restrict__ V, const double* __restrict__ scale,
-                                               const int* __restrict__ flags, Bat bt) {
+                                               const int* __restrict__ flags, Bat bt, int* __restrict__ worked) {
     const int64_t ib = blockIdx.y;
     A += ib * bt.nnz;
     xin += ib * (xin_is_basis ? bt.V : bt.n);
@@ -748,7 +751,10 @@ __global__ void __launch_bounds__(256) gm_spmv(int64_t n, int j, const int32_t* 
     scale += ib * bt.scale;
     flags += ib * bt.flags;
 
-    if (flags[F_CONV]) return;
+    const bool done = flags[F_CONV] != 0;
+    // timed launches log whether they did the product or returned at once past convergence
+    if (worked && blockIdx.x == 0 && blockIdx.y == 0 && threadIdx.x == 0) *worked = done ? 0 : 1;
+    if (done) return;
     const int64_t r = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) / TPR;
     const int lane = threadIdx.x % TPR;
     int32_t a = 0, e = 0;
@@ -850,7 +856,14 @@ __global__ void __launch_bounds__(256) gm_combine(int64_t n, int m, const T* __r
     __shared__ double y[130];
     __shared__ T c[130];
     const int jd = flags[F_JDONE];
-    if (jd == 0) return;
+    if (jd == 0) {
+        // no completed column: the correction is zero (the preconditioner input must not keep the
+        // last iteration's vector)
+        if (u)
+            for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+                u[i] = (T)0;
+        return;
+    }
     if (threadIdx.x == 0) {
         const double* g = csg + 2 * m;
         for (int k = jd - 1; k >= 0; k--) {
@@ -923,7 +936,8 @@ struct GmBufs {
     const T* dinv;     // for the final x update (Jacobi), or null
     const T* Binv;     // block Jacobi, or null
     T* V;
-    T* z;              // block Jacobi workspace
+    T* z;              // block Jacobi / strip workspace
+    Strip* strip;      // strip direct preconditioner, or null
 };
 
 // Host driver of the fused GMRES over a batch of sv->B systems (B = 1 for a single solve).
@@ -945,6 +959,7 @@ int gm_run(const Ctx& c, const GmBufs<T>& B, const double* b, double* x, int max
     const int nbp = G;
     double* red2 = sv->red + (m + 4);
     const bool block = B.Binv != nullptr;
+    const bool strip = B.strip != nullptr;
     const int64_t ne = s->mesh->ne;
     const int L = s->nloc;
     const dim3 gg(G, NB), gs(nblk(n * TPR, 256), NB);
@@ -966,8 +981,12 @@ int gm_run(const Ctx& c, const GmBufs<T>& B, const double* b, double* x, int max
         if (block) {
             block_apply(j, nullptr);
             xin = B.z;
+        } else if (strip) {
+            // z = M^-1 (scale_j V_j); every sweep kernel returns at once after convergence
+            strip_apply<T>(B.strip, s, sv->mat->vals, B.V + (int64_t)j * n, sv->scale, j, B.z, sv->flags, ls);
+            xin = B.z;
         }
-        const bool timing = sv->time_spmv && ls == c.st;
+        const bool timing = sv->time_spmv && ls == c.st && sv->worklog && (int)(sv->tev_used / 2) < sv->worklog_cap;
         if (timing) {
             while (sv->tev.size() < sv->tev_used + 2) {
                 cudaEvent_t e;
@@ -976,8 +995,9 @@ int gm_run(const Ctx& c, const GmBufs<T>& B, const double* b, double* x, int max
             }
             cudaEventRecord(sv->tev[sv->tev_used], ls);
         }
-        OCMP_LAUNCH(gm_spmv<T, TPR, U><<<gs, 256, 0, ls>>>(n, j, s->d_rowptr, s->d_col, B.A, s->d_free, xin, block ? 0 : 1, B.V,
-                                                 sv->scale, sv->flags, bt));
+        OCMP_LAUNCH(gm_spmv<T, TPR, U><<<gs, 256, 0, ls>>>(n, j, s->d_rowptr, s->d_col, B.A, s->d_free, xin, (block || strip) ? 0 : 1, B.V,
+                                                 sv->scale, sv->flags, bt,
+                                                 timing ? sv->worklog + sv->tev_used / 2 : nullptr));
         if (timing) {
             cudaEventRecord(sv->tev[sv->tev_used + 1], ls);
             sv->tev_used += 2;
@@ -993,6 +1013,10 @@ int gm_run(const Ctx& c, const GmBufs<T>& B, const double* b, double* x, int max
         if (block) {
             OCMP_LAUNCH(gm_combine<T><<<gg, 256, 0, ls>>>(n, m, B.V, sv->scale, sv->H, csg, sv->flags, nullptr, x, B.z, bt));
             block_apply(0, x);
+        } else if (strip) {
+            OCMP_LAUNCH(gm_combine<T><<<gg, 256, 0, ls>>>(n, m, B.V, sv->scale, sv->H, csg, sv->flags, nullptr, x, B.z, bt));
+            strip_apply<T>(B.strip, s, sv->mat->vals, B.z, nullptr, 0, B.z, nullptr, ls);
+            strip_add<T>(n, B.z, x, ls);
         } else {
             OCMP_LAUNCH(gm_combine<T><<<gg, 256, 0, ls>>>(n, m, B.V, sv->scale, sv->H, csg, sv->flags, B.dinv, x, nullptr, bt));
         }
@@ -1132,10 +1156,12 @@ static void free_solver(ocmp_solver_s* sv) {
                   sv->V32,  sv->w32,  sv->z32, sv->r32,   sv->p32, sv->d32,   sv->part, sv->pspmv,  sv->red,
                   sv->st,   sv->H,    sv->flags, sv->As64, sv->As32, sv->scale, sv->cnt};
     for (void* q : ps) dfree(q);
+    if (sv->strip) strip_destroy(sv->strip);
     if (sv->hflags) cudaFreeHost(sv->hflags);
     if (sv->gexec) cudaGraphExecDestroy(sv->gexec);
     if (sv->gstream) cudaStreamDestroy(sv->gstream);
     for (cudaEvent_t e : sv->tev) cudaEventDestroy(e);
+    dfree(sv->worklog);
     for (cudaEvent_t e : sv->gev)
         if (e) cudaEventDestroy(e);
 }
@@ -1145,7 +1171,7 @@ extern "C" {
 int ocmp_solver_create(ocmp_matrix_t mat, const ocmp_solve_params_t* prm, ocmp_solver_t* out) {
     if (!mat || !prm || !out) return fail(OCMP_ERR_ARG, "ocmp_solver_create: null argument");
     if (prm->method != OCMP_CG && prm->method != OCMP_GMRES) return fail(OCMP_ERR_ARG, "ocmp_solver_create: method");
-    if (prm->precond < OCMP_PRE_NONE || prm->precond > OCMP_PRE_USER)
+    if (prm->precond < OCMP_PRE_NONE || prm->precond > OCMP_PRE_STRIP)
         return fail(OCMP_ERR_ARG, "ocmp_solver_create: precond");
     if (prm->precision == OCMP_MIXED && prm->method == OCMP_CG && !mat->vals32)
         return fail(OCMP_ERR_ARG, "ocmp_solver_create: mixed-precision CG needs a matrix created with OCMP_MAT_FP32");
@@ -1154,11 +1180,15 @@ int ocmp_solver_create(ocmp_matrix_t mat, const ocmp_solve_params_t* prm, ocmp_s
     ocmp_space_s* s = mat->space;
     if (prm->precond == OCMP_PRE_BLOCK_JACOBI && (s->kind != OCMP_L2 || (s->nloc != 3 && s->nloc != 6 && s->nloc != 10)))
         return fail(OCMP_ERR_UNSUPPORTED, "ocmp_solver_create: block Jacobi is built for L2 element blocks");
+    if (prm->precond == OCMP_PRE_STRIP && (prm->method != OCMP_GMRES || mat->B != 1))
+        return fail(OCMP_ERR_UNSUPPORTED, "ocmp_solver_create: the strip preconditioner is built for GMRES on one matrix");
     auto* sv = new ocmp_solver_s();
     sv->mat = mat;
     sv->s = s;
     sv->prm = *prm;
     if (sv->prm.check_every <= 0) sv->prm.check_every = 8;
+    // a strip-preconditioned iteration costs two full sweeps: read the flags after every one
+    if (prm->precond == OCMP_PRE_STRIP) sv->prm.check_every = 1;
     const int64_t n = sv->n = s->ndof;
     const int NB = sv->B = mat->B;
     if (NB > 1 && (prm->method != OCMP_GMRES || prm->precond == OCMP_PRE_BLOCK_JACOBI)) {
@@ -1216,6 +1246,7 @@ int ocmp_solver_create(ocmp_matrix_t mat, const ocmp_solve_params_t* prm, ocmp_s
         else A(&sv->p, n);
     }
     if (blk) A(&sv->Binv, (size_t)s->mesh->ne * s->nloc * s->nloc);
+    if (!st && prm->precond == OCMP_PRE_STRIP) st = strip_create(s, &sv->strip);
     if (mixed) {
         A(&sv->dinv32, (size_t)n * NB);
         A(&sv->w32, n);
@@ -1304,6 +1335,10 @@ int ocmp_solver_update(ocmp_solver_t sv, void* stream) {
         default: break;
         }
     }
+    if (sv->strip) {
+        const int r = strip_factor(sv->strip, s, sv->mat->vals, st);
+        if (r) return r;
+    }
     if (sv->As64 || sv->As32) {
         const double* d = sv->prm.precond == OCMP_PRE_JACOBI || sv->prm.precond == OCMP_PRE_USER ? sv->dinv : nullptr;
         const dim3 g(nblk(n, kThreads), NB);
@@ -1330,6 +1365,11 @@ int ocmp_solver_spmv_timing(ocmp_solver_t sv, int32_t on) {
     sv->time_spmv = on != 0;
     sv->spmv_launches = 0;
     sv->spmv_ms = 0;
+    if (on && !sv->worklog) {
+        const int st = dalloc(&sv->worklog, 4096);
+        if (st) return st;
+        sv->worklog_cap = 4096;
+    }
     return OCMP_OK;
 }
 
@@ -1344,11 +1384,35 @@ int ocmp_solver_set_graph(ocmp_solver_t sv, int32_t on) {
     if (!sv) return fail(OCMP_ERR_ARG, "ocmp_solver_set_graph: null solver");
     if (on && sv->prm.method != OCMP_GMRES)
         return fail(OCMP_ERR_UNSUPPORTED, "ocmp_solver_set_graph: graphs are built for GMRES");
+    if (on && sv->strip)
+        return fail(OCMP_ERR_UNSUPPORTED, "ocmp_solver_set_graph: the strip preconditioner runs without graphs");
     sv->use_graph = on != 0;
     if (!on && sv->gexec) {
         cudaGraphExecDestroy(sv->gexec);
         sv->gexec = nullptr;
     }
+    return OCMP_OK;
+}
+
+int ocmp_solver_strip_stats(ocmp_solver_t sv, ocmp_strip_stats_t* out) {
+    if (!sv || !out) return fail(OCMP_ERR_ARG, "ocmp_solver_strip_stats: null argument");
+    if (!sv->strip) return fail(OCMP_ERR_ARG, "ocmp_solver_strip_stats: solver not created with OCMP_PRE_STRIP");
+    strip_stats(sv->strip, out);
+    return OCMP_OK;
+}
+
+int ocmp_solver_strip_timing(ocmp_solver_t sv, int32_t on) {
+    if (!sv) return fail(OCMP_ERR_ARG, "ocmp_solver_strip_timing: null solver");
+    if (!sv->strip) return fail(OCMP_ERR_ARG, "ocmp_solver_strip_timing: solver not created with OCMP_PRE_STRIP");
+    strip_set_timing(sv->strip, on != 0);
+    return OCMP_OK;
+}
+
+int ocmp_solver_strip_gemm(ocmp_solver_t sv, int32_t kind) {
+    if (!sv) return fail(OCMP_ERR_ARG, "ocmp_solver_strip_gemm: null solver");
+    if (!sv->strip) return fail(OCMP_ERR_ARG, "ocmp_solver_strip_gemm: solver not created with OCMP_PRE_STRIP");
+    if (kind != 0 && kind != 1) return fail(OCMP_ERR_ARG, "ocmp_solver_strip_gemm: kind is 0 (SIMT) or 1 (tensor cores)");
+    strip_set_gemm(sv->strip, kind);
     return OCMP_OK;
 }
 
@@ -1368,10 +1432,10 @@ int ocmp_solve_batch(ocmp_solver_t sv, const double* b, double* x, void* stream,
     std::vector<int> its(NB, 0);
     int cyc = 0, st;
     if (!mixed) {
-        GmBufs<double> B{sv->K64, jac ? sv->dinv : nullptr, nullptr, sv->V, sv->z};
+        GmBufs<double> B{sv->K64, jac ? sv->dinv : nullptr, nullptr, sv->V, sv->z, nullptr};
         st = gm_dispatch<double>(c, B, b, x, P.maxit, 0.0, its.data(), &cyc, r0.data());
     } else {
-        GmBufs<float> B{sv->K32, jac ? sv->dinv32 : nullptr, nullptr, sv->V32, sv->z32};
+        GmBufs<float> B{sv->K32, jac ? sv->dinv32 : nullptr, nullptr, sv->V32, sv->z32, nullptr};
         st = gm_dispatch<float>(c, B, b, x, P.maxit, P.inner_tol > 0 ? P.inner_tol : 1e-4, its.data(), &cyc,
                                 r0.data());
     }
@@ -1420,10 +1484,10 @@ int ocmp_solve(ocmp_solver_t sv, const double* b, double* x, void* stream, ocmp_
         const bool jac = P.precond == OCMP_PRE_JACOBI || P.precond == OCMP_PRE_USER;
         if (sv->B != 1) return fail(OCMP_ERR_ARG, "ocmp_solve: batched matrix, use ocmp_solve_batch");
         if (!mixed) {
-            GmBufs<double> B{sv->K64, jac ? sv->dinv : nullptr, sv->Binv, sv->V, sv->z};
+            GmBufs<double> B{sv->K64, jac ? sv->dinv : nullptr, sv->Binv, sv->V, sv->z, sv->strip};
             st = gm_dispatch<double>(c, B, b, x, P.maxit, 0.0, &iters, &outer, &relres0);
         } else {
-            GmBufs<float> B{sv->K32, jac ? sv->dinv32 : nullptr, sv->Binv32, sv->V32, sv->z32};
+            GmBufs<float> B{sv->K32, jac ? sv->dinv32 : nullptr, sv->Binv32, sv->V32, sv->z32, sv->strip};
             st = gm_dispatch<float>(c, B, b, x, P.maxit, P.inner_tol > 0 ? P.inner_tol : 1e-4, &iters, &outer,
                                     &relres0);
         }
@@ -1442,11 +1506,19 @@ int ocmp_solve(ocmp_solver_t sv, const double* b, double* x, void* stream, ocmp_
             OCMP_CUDA(cudaStreamSynchronize(c.st));
             relres = hst[S_RES];
         }
-        for (size_t k = 0; k + 1 < sv->tev_used; k += 2) {
-            float ms = 0;
-            OCMP_CUDA(cudaEventElapsedTime(&ms, sv->tev[k], sv->tev[k + 1]));
-            sv->spmv_ms += ms;
-            sv->spmv_launches++;
+        if (sv->tev_used) {
+            // only the launches that did the product count (those queued past convergence return
+            // at once and read no matrix)
+            std::vector<int> wk(sv->tev_used / 2, 0);
+            OCMP_CUDA(cudaMemcpyAsync(wk.data(), sv->worklog, sizeof(int) * wk.size(), cudaMemcpyDeviceToHost, c.st));
+            OCMP_CUDA(cudaStreamSynchronize(c.st));
+            for (size_t k = 0; k + 1 < sv->tev_used; k += 2) {
+                if (!wk[k / 2]) continue;
+                float ms = 0;
+                OCMP_CUDA(cudaEventElapsedTime(&ms, sv->tev[k], sv->tev[k + 1]));
+                sv->spmv_ms += ms;
+                sv->spmv_launches++;
+            }
         }
         sv->tev_used = 0;
     } else {

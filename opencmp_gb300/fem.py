@@ -297,7 +297,7 @@ class KrylovSolver:
         p.restart = restart
         p.precond = {'none': LB.PRE_NONE, 'jacobi': LB.PRE_JACOBI, 'local': LB.PRE_JACOBI,
                      'block_jacobi': LB.PRE_BLOCK_JACOBI, 'block': LB.PRE_BLOCK_JACOBI,
-                     'user': LB.PRE_USER}[str(precond).lower()]
+                     'user': LB.PRE_USER, 'strip': LB.PRE_STRIP, 'direct': LB.PRE_STRIP}[str(precond).lower()]
         p.precision = LB.MIXED if str(precision).lower() == 'mixed' else LB.FP64
         p.tol, p.maxit, p.inner_tol, p.check_every = tol, maxit, inner_tol, check_every
         self.params = p
@@ -326,6 +326,20 @@ class KrylovSolver:
         n, ms = C.c_int64(0), C.c_double(0)
         LB.call('ocmp_solver_spmv_stats', self.h, C.byref(n), C.byref(ms))
         return n.value, ms.value
+
+    def strip_stats(self) -> dict:
+        """Sizes and timings of the last strip factorisation (precond='strip')."""
+        o = LB.StripStats()
+        LB.call('ocmp_solver_strip_stats', self.h, C.byref(o))
+        return {k: getattr(o, k) for k, _ in LB.StripStats._fields_}
+
+    def strip_gemm(self, kind: str):
+        """Dense products of the next strip factorisations: 'simt' (FP32 FMA) or 'tensor' (tcgen05)."""
+        LB.call('ocmp_solver_strip_gemm', self.h, {'simt': 0, 'tensor': 1}[kind])
+
+    def strip_timing(self, on: bool = True):
+        """Time every dense product of the next strip factorisations with CUDA events."""
+        LB.call('ocmp_solver_strip_timing', self.h, int(on))
 
     def set_graph(self, on: bool = True):
         """Replay each restart cycle from a captured CUDA graph (GMRES)."""
