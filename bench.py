@@ -13,7 +13,8 @@ steps; `mixed_previous_step_guess` and `mixed_extrapolated_guess` separate the t
 Inputs are resident in HBM and larger than L2 (the matrix alone is ~730 MB), so no L2 flush.
 
 --impl reference: the CPU restatement of the same step (the oracle: C + OpenMP, all host
-threads) on a bounded sample, the 32^3 x 6 mesh (274,625 dofs), since NGSolve cannot run here.
+threads; NGSolve cannot run here) on the same mesh, the same steps after the same warm-up, from the
+previous-step guess OpenCMP uses.
 --config batched: 512 steady 2D convection-diffusion instances of mixed mesh sizes and orders.
 --config ins: the Navier-Stokes lid-driven cavity (Taylor-Hood, Euler IMEX, flexible GMRES with the
 Cahouet-Chabard pressure preconditioner).
@@ -37,6 +38,8 @@ sys.path.insert(0, ROOT)
 EPS, WIND, DT = 1e-2, (1.0, 0.5, 0.25), 1e-3
 GAUSS = dict(c=(0.25, 0.25, 0.25), s=0.1)
 METRIC = 'DOF/s to 1e-8 FP64 rel. residual: mixed+batched+learned vs plain FP64, 1 GB300'
+WORKLOAD = ('transient 3D convection-diffusion, unit cube {}^3 x 6 tets, H1 p=2, eps=1e-2, w=(1,0.5,0.25), implicit '
+            'Euler dt=1e-3, full reassembly every step, GMRES({}) + Jacobi to 1e-8 FP64 relative residual')
 # DRAM bytes per matrix entry (dram__bytes_read.sum + dram__bytes_write.sum per launch / nnz) of the
 # dominant kernel, gm_spmv<float>, from an ncu capture on the 48^3 x 6 case (nnz 25,755,265; two
 # launches: 221.7 and 222.0 MB); the traffic of a launch is this figure times the launch's nnz
@@ -303,9 +306,8 @@ def run_ours(args):
         'metric': METRIC, 'value': value, 'unit': 'DOF/s', 'n_gpus': world, 'steps': args.steps, 'warmup': args.warmup,
         'ms_per_step': ms_opt / args.steps, 'higher_is_better': True, 'scaling': 'weak', 'vs_baseline': None,
         'dtype': 'f64+f32', 'data': 'synthetic (generated structured mesh, Gaussian initial condition)',
-        'config': {'workload': 'transient 3D convection-diffusion, unit cube {}^3 x 6 tets, H1 p=2, implicit Euler'
-                               ' dt=1e-3, GMRES({}) + Jacobi to 1e-8 FP64 relative residual, previous-step guess,'
-                               ' full reassembly every step'.format(n, args.restart),
+        'config': {'workload': WORKLOAD.format(n, args.restart) + ', optimised path: double-float assembly, '
+                               'learned initial guess under its judge, FP32 inner GMRES + FP64 refinement',
                    'ndof': ndof, 'nnz': nnz, 'parallelism': 'replicas' if world > 1 else 'single GPU',
                    'l2': 'inputs larger than L2 (no flush)'},
         'plain_fp64': {'value': plain, 'unit': 'DOF/s', 'ms_per_step': ms_plain / args.steps,
@@ -355,7 +357,7 @@ def run_ours(args):
         'setup_s': setup_s,
     }
     if rank == 0 and world == 1 and not args.no_cpu:
-        line['cpu_baseline'] = cpu_baseline(args.cpu_n)
+        line['cpu_baseline'] = cpu_baseline(args.cpu_n if args.cpu_n > 0 else n)
     if rank == 0:
         print(json.dumps(line), flush=True)
     if world > 1:
@@ -591,8 +593,177 @@ def run_batched(args):
     print(json.dumps(line), flush=True)
 
 
-def cpu_step_sample(n_cpu, steps):
-    """The oracle's implicit-Euler step (assembly + GMRES/Jacobi to 1e-8) on the n_cpu^3 x 6 mesh."""
+def run_dg2d(args):
+    """Config 2: steady 2D convection-diffusion, unit square 256 x 256 x 2 triangles, DG order 2
+    (786,432 dofs), eps = 1e-3, rotating wind w = (-(y-0.5), x-0.5), Gaussian source (sigma 0.05 at
+    (0.3, 0.5)), DG Dirichlet 0, interior penalty 10. One step = assemble the matrix and the
+    right-hand side, factorise the strip direct preconditioner, GMRES to a 1e-8 FP64 relative
+    residual from zero (OpenCMP's direct solve of this system, base_model.py:906-922, refactorises
+    on every call too). `value`: FP32 inner GMRES + FP64 refinement, strip inverses built with the
+    tensor-core products; `plain_fp64`: FP64 GMRES with the same preconditioner built with FP32 SIMT
+    products. The configuration's own GMRES(50) + block Jacobi is run once for the record: it
+    stagnates on this closed-streamline problem."""
+    import torch
+    from opencmp_gb300 import fem, mesh as M, build, _lib
+    build.build()
+    torch.cuda.set_device(0)
+    n = args.n_dg
+    m = M.unit_square(n)
+    sp = fem.Space(m, 'L2', 2)
+    X = m.coords
+    W = torch.as_tensor(np.ascontiguousarray(np.stack([-(X[:, 1] - 0.5), X[:, 0] - 0.5], 1)), device='cuda')
+    allb = m.label_mask(m.bc_names)
+    form = fem.make_form(diff=1e-3, dt=1.0, wind_vtx=W, dg=True, ipc=10.0, nitsche_mask=allb)
+    Xq = sp.quad_points()
+    fq = torch.as_tensor(np.exp(-((Xq[..., 0] - 0.3) ** 2 + (Xq[..., 1] - 0.5) ** 2) / (2 * 0.05 ** 2)), device='cuda')
+    rhs = fem.make_rhs(src_qp=fq, gval={k: 0.0 for k in range(len(m.bc_names))})
+    nd, nnz = sp.ndof, sp.nnz
+    A = fem.Matrix(sp)
+    b = torch.zeros(nd, dtype=torch.float64, device='cuda')
+    A.assemble(form)
+    fem.assemble_rhs(sp, form, rhs, b)
+    paths = {'tensor_mixed': ('mixed', 'tensor'), 'simt_fp64': ('fp64', 'simt')}
+    solvers = {}
+    for k, (prec, kind) in paths.items():
+        sv = fem.KrylovSolver(A, method='GMRES', restart=50, precond='strip', precision=prec, tol=1e-8, maxit=200)
+        sv.strip_gemm(kind)
+        solvers[k] = sv
+    peak = None
+    try:
+        with open(os.path.join(ROOT, 'MEASURED_PEAKS.json')) as fh:
+            pk = json.load(fh)
+        peak, peak_kind = float(pk['bf16_tflops']), 'measured'
+    except Exception:
+        peak, peak_kind = 1900.0, 'fallback'
+
+    def step(sv, x, e2e=None):
+        if e2e is not None:
+            b_host, x_host = e2e
+        A.assemble(form)
+        fem.assemble_rhs(sp, form, rhs, b)
+        sv.update()
+        x.zero_()
+        info = sv.solve(b, x, raise_on_fail=False)
+        if e2e is not None:
+            x_host.copy_(x, non_blocking=True)
+        return info
+
+    res = {}
+    x = torch.zeros_like(b)
+    for k, sv in solvers.items():
+        for _ in range(args.warmup):
+            step(sv, x)
+        torch.cuda.synchronize()
+        l0 = _lib.load().ocmp_launch_count()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        infos = []
+        e0.record()
+        for _ in range(args.steps):
+            infos.append(step(sv, x))
+        e1.record()
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / args.steps
+        res[k] = dict(value=nd / (ms * 1e-3), unit='DOF/s', ms_per_step=ms, launches=int(_lib.load().ocmp_launch_count() - l0),
+                      iters=float(np.mean([i.iterations for i in infos])),
+                      max_relres=float(max(i.relres for i in infos)),
+                      converged=int(sum(1 for i in infos if i.status == 0)))
+        print('dg2d {}: {:.1f} ms/step, {:.1f} iterations'.format(k, ms, res[k]['iters']), file=sys.stderr, flush=True)
+    # the optimised path end to end: the right-hand side's source data from pinned host memory, the
+    # solution back to it, every step
+    sv = solvers['tensor_mixed']
+    fq_host = fq.cpu().pin_memory()
+    x_host = torch.empty(nd, dtype=torch.float64, pin_memory=True)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(args.steps):
+        fq.copy_(fq_host, non_blocking=True)
+        step(sv, x, e2e=(None, x_host))
+        torch.cuda.current_stream().synchronize()
+    e1.record()
+    torch.cuda.synchronize()
+    ms_e2e = e0.elapsed_time(e1) / args.steps
+    # dense products of one factorisation, timed per launch with CUDA events (the tile inversions,
+    # panels and sweeps are the rest of the factorisation time)
+    gem = {}
+    for k, sv in solvers.items():
+        sv.strip_timing(True)
+        sv.update()
+        st = sv.strip_stats()
+        sv.strip_timing(False)
+        gem[k] = dict(st, tflops=st['gemm_flops'] / (st['gemm_ms'] * 1e-3) / 1e12 if st['gemm_ms'] else None)
+    # the configuration's own preconditioner, once, for the record
+    bj = fem.KrylovSolver(A, method='GMRES', restart=50, precond='block_jacobi', precision='fp64', tol=1e-8,
+                          maxit=args.bj_iters)
+    xb = torch.zeros_like(b)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    ib = bj.solve(b, xb, raise_on_fail=False)
+    torch.cuda.synchronize()
+    t_bj = time.perf_counter() - t0
+    tc = gem['tensor_mixed']
+    # FLOP/s of the tensor-core products against the measured dense BF16 rate (TF32 runs at half of
+    # it on this part, and the 3xTF32 split issues three products per FP32 product counted here)
+    line = {'metric': METRIC + ' (steady DG convection-diffusion)', 'value': res['tensor_mixed']['value'],
+            'unit': 'DOF/s', 'n_gpus': 1, 'steps': args.steps, 'warmup': args.warmup,
+            'ms_per_step': res['tensor_mixed']['ms_per_step'], 'higher_is_better': True, 'scaling': 'weak',
+            'vs_baseline': None, 'dtype': 'f64+f32+tf32', 'data': 'synthetic (generated structured mesh)',
+            'config': {'workload': 'steady 2D convection-diffusion, unit square {0}x{0}x2 tri, DG p=2, eps=1e-3, '
+                                   'rotating wind, Gaussian source, DG Dirichlet 0; assembly + strip direct '
+                                   'preconditioner factorisation + GMRES(50) to 1e-8 FP64 relative residual '
+                                   'per step'.format(n),
+                       'ndof': nd, 'nnz': nnz, 'l2': 'strip inverses ({:.1f} GB) larger than L2 (no flush)'.format(
+                           tc['bytes'] / 1e9)},
+            'optimised': dict(res['tensor_mixed'], kind='FP32 inner GMRES + FP64 refinement, strip inverses in FP32 '
+                                                        'built with tcgen05 3xTF32 products'),
+            'plain_fp64': dict(res['simt_fp64'], kind='FP64 GMRES, strip inverses in FP32 built with FP32 SIMT '
+                                                      'products'),
+            'block_jacobi_fp64': {'kind': 'FP64 GMRES(50) + block Jacobi (the configuration\'s own preconditioner)',
+                                  'iterations': ib.iterations, 'relres_reached': ib.relres, 'status': ib.status,
+                                  'seconds': t_bj},
+            'factorisation': gem,
+            'e2e': {'value': nd / (ms_e2e * 1e-3), 'unit': 'DOF/s', 'h2d_bytes_per_step': 8 * fq.numel(),
+                    'd2h_bytes_per_step': 8 * nd},
+            'roofline': {'bound': 'tensor', 'kernel': 'tc_gemm_nt_kernel (tcgen05 kind::tf32, 3xTF32, TMA-staged)',
+                         'achieved': tc['tflops'], 'peak': peak, 'peak_kind': peak_kind + ' bf16 dense (burst)',
+                         'unit': 'TFLOP/s', 'frac': tc['tflops'] / peak if tc['tflops'] else None,
+                         'flops': 'FP32-equivalent 2 M N K per product (the three TF32 products of the split '
+                                  'are not counted)',
+                         'traffic': None},
+            'gpu_launches': res['tensor_mixed']['launches']}
+    if not args.no_cpu:
+        line['cpu_baseline'] = dg2d_cpu_baseline(args.dg_cpu_n)
+    print(json.dumps(line), flush=True)
+
+
+def dg2d_cpu_baseline(n_cpu):
+    """The reference's default for this call, a sparse direct solve (scipy spsolve, SuperLU), after
+    the oracle's assembly, on the n_cpu x n_cpu x 2 mesh."""
+    import scipy.sparse.linalg as spla
+    from oracle import oracle as O
+    from opencmp_gb300 import mesh as M
+    O.build()
+    O.lib().or_set_threads(os.cpu_count() or 1)
+    m = M.unit_square(n_cpu)
+    X = m.coords
+    W = np.ascontiguousarray(np.stack([-(X[:, 1] - 0.5), X[:, 0] - 0.5], 1))
+    o = O.Space(m, O.L2, 2, 0)
+    allb = m.label_mask(m.bc_names)
+    of = O.make_form(diff=1e-3, dt=1.0, wind_vtx=W, dg=True, ipc=10.0, nitsche_mask=allb)
+    t0 = time.perf_counter()
+    A = o.assemble(of)
+    bo = o.rhs(of, O.make_rhs(src_kind=O.SRC_GAUSS, src=(1.0, 0.3, 0.5, 0.0, 0.05)))
+    x = spla.spsolve(o.csr(A).tocsc(), bo)
+    dt = time.perf_counter() - t0
+    return {'value': o.ndof / dt, 'unit': 'DOF/s', 'cores': 1, 'kind': 'port',
+            'sample': 'oracle assembly (OpenMP) + scipy spsolve (SuperLU, one thread) on the {0}x{0}x2 mesh ({1} '
+                      'dofs), relres {2:.1e}'.format(n_cpu, o.ndof, o.relres(A, bo, x))}
+
+
+def cpu_steps(n_cpu, warmup, steps):
+    """The oracle's implicit-Euler step (full reassembly + GMRES(30)/Jacobi to 1e-8 from the
+    previous-step guess, OpenCMP's start) on the n_cpu^3 x 6 mesh, all host threads: `warmup`
+    untimed steps from the Gaussian start, then `steps` timed ones."""
     from oracle import oracle as O
     from opencmp_gb300 import mesh as M
     O.build()
@@ -602,15 +773,24 @@ def cpu_step_sample(n_cpu, steps):
     s = O.Space(m, O.H1, 2, m.label_mask(m.bc_names))
     f = O.make_form(mass=1.0, diff=EPS, dt=DT, wind=WIND)
     u = _interp_p2_oracle(s, m)
-    t0 = time.perf_counter()
-    for _ in range(steps):
+    iters = []
+
+    def one(u):
         A = s.assemble(f)
         b = s.rhs(f, O.make_rhs(dt=DT, mass=1.0, uprev=u))
         x = u.copy()
-        s.gmres(A, b, x, restart=30, precond=1, tol=1e-8, maxit=2000)
-        u = x
+        it, _ = s.gmres(A, b, x, restart=30, precond=1, tol=1e-8, maxit=2000)
+        iters.append(it)
+        return x
+
+    for _ in range(warmup):
+        u = one(u)
+    iters.clear()
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        u = one(u)
     dt = time.perf_counter() - t0
-    return s.ndof, dt, threads
+    return s.ndof, dt, threads, float(np.mean(iters)) if iters else 0.0
 
 
 def _interp_p2_oracle(s, m):
@@ -618,27 +798,34 @@ def _interp_p2_oracle(s, m):
     return interpolate_p2_arrays(m.coords, s.sorted_conn(), s.dofs(), s.ndof, gaussian)
 
 
-def cpu_baseline(n_cpu):
-    ndof, dt, threads = cpu_step_sample(n_cpu, 1)
-    return {'value': ndof / dt, 'unit': 'DOF/s', 'cores': threads, 'kind': 'port',
-            'sample': 'one implicit-Euler step (assembly + GMRES(30)/Jacobi to 1e-8) on the {}^3 x 6 tet mesh '
-                      '({} dofs), C oracle with OpenMP'.format(n_cpu, ndof)}
+def cpu_baseline(n_cpu, warmup=1, steps=2):
+    ndof, dt, threads, its = cpu_steps(n_cpu, warmup, steps)
+    return {'value': ndof * steps / dt, 'unit': 'DOF/s', 'cores': threads, 'kind': 'port',
+            'sample': 'implicit-Euler steps {}..{} from the Gaussian start (full reassembly + GMRES(30)/Jacobi to '
+                      '1e-8 from the previous-step guess, {:.1f} iterations per step) on the {}^3 x 6 tet mesh ({} '
+                      'dofs), C oracle with OpenMP'.format(warmup + 1, warmup + steps, its, n_cpu, ndof)}
 
 
 def run_reference(args):
+    """The reference arm: OpenCMP's own algorithm for this step (NGSolve cannot be installed here, so
+    its CPU restatement, the oracle) on the same mesh, the same steps after the same warm-up, from
+    the previous-step guess OpenCMP uses, on all host cores."""
     rank = int(os.environ.get('RANK', '0'))
     if rank != 0:
         return
-    ndof, dt, threads = cpu_step_sample(args.cpu_n, max(1, args.steps // 10) if args.steps > 0 else 1)
-    steps = max(1, args.steps // 10) if args.steps > 0 else 1
+    steps = max(1, args.steps)
+    ndof, dt, threads, its = cpu_steps(args.n, args.warmup, steps)
     v = ndof * steps / dt
-    line = {'metric': METRIC, 'value': v, 'unit': 'DOF/s', 'n_gpus': 0, 'steps': steps, 'warmup': 0,
+    line = {'metric': METRIC, 'value': v, 'unit': 'DOF/s', 'n_gpus': 0, 'steps': steps, 'warmup': args.warmup,
             'ms_per_step': dt / steps * 1e3, 'higher_is_better': True, 'scaling': 'weak', 'vs_baseline': None,
-            'dtype': 'f64', 'data': 'synthetic', 'impl': 'reference',
-            'config': {'workload': 'transient 3D convection-diffusion, implicit Euler step, H1 p=2 (CPU sample on '
-                                   'the {}^3 x 6 mesh, {} dofs)'.format(args.cpu_n, ndof)},
+            'dtype': 'f64', 'data': 'synthetic (generated structured mesh, Gaussian initial condition)',
+            'impl': 'reference',
+            'config': {'workload': WORKLOAD.format(args.n, 30) + ', previous-step guess',
+                       'ndof': ndof, 'l2': 'inputs larger than L2 (no flush)'},
             'cpu_baseline': {'value': v, 'unit': 'DOF/s', 'cores': threads, 'kind': 'port',
-                             'sample': '{} step(s) on {} dofs'.format(steps, ndof)},
+                             'sample': 'steps {}..{} from the Gaussian start on {} dofs, {:.1f} GMRES iterations per '
+                                       'step, C oracle with OpenMP'.format(args.warmup + 1, args.warmup + steps,
+                                                                          ndof, its)},
             'e2e': {'value': v, 'unit': 'DOF/s', 'h2d_bytes_per_step': 0, 'd2h_bytes_per_step': 0}}
     print(json.dumps(line), flush=True)
 
@@ -650,7 +837,7 @@ def main():
     ap.add_argument('--warmup', type=int, default=3)
     ap.add_argument('--impl', default='ours', choices=['ours', 'reference'])
     ap.add_argument('--n', type=int, default=64)
-    ap.add_argument('--cpu-n', type=int, default=32)
+    ap.add_argument('--cpu-n', type=int, default=0, help='mesh of the cpu_baseline sample (0: the workload\'s)')
     ap.add_argument('--restart', type=int, default=30)
     ap.add_argument('--inner-tol', type=float, default=1e-4)
     # GMRES iterations between the host's convergence checks, per path at its measured best: the plain
@@ -658,7 +845,10 @@ def main():
     ap.add_argument('--check-every', type=int, default=8, help='plain FP64 path')
     ap.add_argument('--check-every-mixed', type=int, default=6, help='mixed-precision paths')
     ap.add_argument('--no-cpu', action='store_true')
-    ap.add_argument('--config', default='transient3d', choices=['transient3d', 'batched', 'ins'])
+    ap.add_argument('--config', default='transient3d', choices=['transient3d', 'batched', 'ins', 'dg2d'])
+    ap.add_argument('--n-dg', type=int, default=256)
+    ap.add_argument('--dg-cpu-n', type=int, default=128, help='mesh of the dg2d cpu_baseline sample')
+    ap.add_argument('--bj-iters', type=int, default=2000, help='block-Jacobi GMRES budget of the dg2d record')
     ap.add_argument('--n-ins', type=int, default=256)
     ap.add_argument('--ins-train', type=int, default=100,
                     help='untimed first INS steps (training samples from step guess_k + 1 on)')
@@ -677,6 +867,8 @@ def main():
         run_ins(args)
     elif args.config == 'batched':
         run_batched(args)
+    elif args.config == 'dg2d':
+        run_dg2d(args)
     else:
         run_ours(args)
 

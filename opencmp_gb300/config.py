@@ -26,7 +26,8 @@ CONFIG_DEFAULTS: Dict[str, Dict[str, Any]] = {
                'linear_max_iterations': 100, 'linearization_method': 'Oseen', 'nonlinear_solver': 'default',
                'nonlinear_tolerance': {'absolute': 0.0, 'relative': 'REQUIRED'}, 'nonlinear_max_iterations': 10,
                # GPU path (new keys; absent from OpenCMP's table)
-               'gpu_precision': 'fp64', 'gpu_restart': 50, 'initial_guess': 'previous'},
+               'gpu_precision': 'fp64', 'gpu_restart': 50, 'initial_guess': 'previous',
+               'learned_train_steps': 20, 'learned_train_iters': 300},
     'TRANSIENT': {'transient': False, 'scheme': 'implicit euler', 'time_range': [0.0, 5.0], 'dt': 0.001,
                   'dt_tolerance': {'absolute': 0.0, 'relative': 'REQUIRED'}, 'dt_range': [1e-6, 0.1],
                   'maximum_rejected_solves': 1000},

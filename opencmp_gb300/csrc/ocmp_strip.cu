@@ -8,18 +8,25 @@
 // elements). Block elimination over the strips (the block Thomas algorithm) needs, per strip,
 //     S_k = A_kk - A_k,k-1 S_{k-1}^-1 A_k-1,k,      G_k = S_k^-1,
 // and a solve is a forward sweep y_k = G_k (b_k - A_k,k-1 y_k-1) and a backward sweep
-// x_k = y_k - G_k A_k,k+1 x_k+1. Every G_k is kept explicitly (FP32, dense, padded to a multiple of
-// 128), so each sweep step is one dense matrix-vector product instead of two triangular solves.
+// x_k = y_k - G_k A_k,k+1 x_k+1. Every G_k is kept explicitly (FP32, dense), so each sweep step is
+// one dense matrix-vector product instead of two triangular solves; the sweeps of a
+// preconditioner application are replayed from a CUDA graph.
 //
-// Factorisation of strip k, all in FP32 on the device:
-//  1. S_k is scattered from the CSR rows of the strip (constrained rows and columns dropped, unit
-//     diagonal there and on the padding).
-//  2. Schur update through the interface only: I = rows of strip k coupled to strip k-1, J = rows of
-//     strip k-1 coupled to strip k; S_k[I,I] -= A[I,J] G_k-1[J,J] A[J,I] as two dense products.
-//  3. Block Gauss-Jordan inversion in place with 128 x 128 diagonal-tile pivots (each tile inverted
-//     with partial pivoting inside it): per tile one small inversion, two panel kernels and one
-//     rank-128 update S -= C R^T of the whole strip, the dominant flops.
-// The dense products are C = beta C + alpha A B^T with both operands K-contiguous (gemm_nt).
+// Within a strip the dofs are ordered [N | I]: I = the dofs coupled to the previous strip (the
+// only rows and columns the Schur update A_k,k-1 S_{k-1}^-1 A_k-1,k touches), N = the rest, each
+// part padded to a multiple of 128 with decoupled unit rows. G_k is the block Gauss-Jordan inverse
+// of S_k with 128 x 128 diagonal-tile pivots (each tile inverted with partial pivoting inside it):
+// per tile one small inversion, two panel kernels and one rank-128 update of the whole strip, the
+// dominant flops. Since the Schur update only adds to the II block, the N pivots can be eliminated
+// before it:
+//   phase 1 (side streams, all strips independent): fill S_k, eliminate its N tiles;
+//   phase 2 (the caller's stream, strip after strip): S_k[I,I] -= A[I,J] G_k-1[J,J] A[J,I] (two
+//     dense products over the interface, J = the dofs of strip k-1 coupled to strip k), then
+//     eliminate the I tiles.
+// On a structured triangle mesh half of each strip's elements touch the previous row of elements,
+// so phase 2, the sequential chain, does half of the pivot tiles.
+// The dense products are C = beta C + alpha A B^T with both operands K-contiguous: FP32 SIMT
+// (sgemm_nt) or the tensor cores (tc_gemm_nt, ocmp_tcgemm.cu).
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -32,19 +39,30 @@
 namespace ocmp {
 
 constexpr int kNb = 128;   // Gauss-Jordan tile and padding granule
+constexpr int kSide = 3;   // side streams of phase 1
+
+struct StripWork {
+    float* P = nullptr;    // pivot-tile inverse, kNb x kNb
+    float* Ck = nullptr;   // column panel, mp_max x kNb
+    float* Rt = nullptr;   // row panel (transposed), mp_max x kNb
+};
 
 struct Strip {
     int K = 0;
     std::vector<int64_t> s;          // K + 1 strip boundaries
-    std::vector<int> m, mp;          // strip sizes and padded sizes
+    std::vector<int> m, mp;          // strip sizes and padded sizes (nNp + nIp)
+    std::vector<int> nN, nNp, nI, nJ;
     std::vector<int64_t> goff;       // offsets of G_k in d_G (floats)
-    std::vector<int> nI, nJ;         // interface sizes: I_k (k >= 1) and J_k (k <= K-2)
+    std::vector<int64_t> poff;       // offsets of strip k's permutation in d_perm
     std::vector<int64_t> ioff, joff; // offsets into d_I / d_J
     int mp_max = 0, nIp_max = 0, nJp_max = 0;
-    int32_t* d_I = nullptr;          // local indices of I_k, strip after strip
-    int32_t* d_J = nullptr;          // local indices of J_k
-    int32_t* d_Iinv = nullptr;       // per dof: its position in I of its strip, or -1
-    int32_t* d_Jinv = nullptr;       // per dof: its position in J of its strip, or -1
+    int32_t* d_perm = nullptr;       // per strip position: local dof, -1 on padding
+    int32_t* d_I = nullptr;          // I_k as positions in strip k's order (nNp + a)
+    int32_t* d_J = nullptr;          // J_k as positions in strip k's order
+    int32_t* jrow = nullptr;         // J_k as local dofs
+    int32_t* d_pinv = nullptr;       // per dof: its position in its strip's order
+    int32_t* d_Iinv = nullptr;       // per dof: its index in I of its strip, or -1
+    int32_t* d_Jinv = nullptr;       // per dof: its index in J of its strip, or -1
     int32_t* d_lo_ptr = nullptr;     // per dof: CSR positions whose column lies in the previous strip
     int32_t* d_lo_pos = nullptr;
     int32_t* d_hi_ptr = nullptr;     // per dof: CSR positions whose column lies in the next strip
@@ -55,13 +73,22 @@ struct Strip {
     float* d_Gjj = nullptr;
     float* d_Tt = nullptr;
     float* d_U = nullptr;
-    float* d_P = nullptr;            // Gauss-Jordan panels
-    float* d_Ck = nullptr;
-    float* d_Rt = nullptr;
+    StripWork work[kSide + 1];       // [0]: the caller's stream, [1..]: side streams
     float* d_r = nullptr;            // solve scratch (one strip)
     int* d_flag = nullptr;           // [0] pivot tiles that were singular or non-finite, [1] a tensor-core
                                      // product whose bounded wait gave up
     int64_t bytes = 0;
+    cudaStream_t side[kSide] = {};
+    cudaEvent_t ev_start = nullptr;
+    std::vector<cudaEvent_t> ev_phase1;
+    // sweeps replayed from graphs: [0] gated on the solver's convergence flag, [1] not gated
+    cudaStream_t cap = nullptr;
+    cudaGraphExec_t gexec[2] = {nullptr, nullptr};
+    unsigned long long gkernels[2] = {0, 0};
+    const void* g_z[2] = {nullptr, nullptr};
+    const int* g_flags[2] = {nullptr, nullptr};
+    const double* g_vals[2] = {nullptr, nullptr};
+    int g_type[2] = {0, 0};
     // statistics of the last factorisation
     bool timing = false;
     std::vector<cudaEvent_t> ev;
@@ -158,28 +185,34 @@ __global__ void __launch_bounds__(256) sgemm_nt(int M, int N, int K, const float
     }
 }
 
+
 // ------------------------------------------------------------------ strip assembly
-// S (mp x mp, zeroed) <- the strip's diagonal block; unit diagonal on constrained rows and padding
-__global__ void k_fill_strip(int m, int mp, int64_t s0, const int32_t* __restrict__ rp, const int32_t* __restrict__ col,
-                             const double* __restrict__ vals, const uint8_t* __restrict__ freed, float* __restrict__ S) {
+// S (mp x mp, zeroed) <- the strip's diagonal block in the strip's [N | I] order; unit diagonal on
+// constrained rows and on the padding. pinv: per dof its position in its strip's order.
+__global__ void k_fill_strip(int mp, int64_t s0, const int32_t* __restrict__ perm, const int32_t* __restrict__ pinv,
+                             const int32_t* __restrict__ rp, const int32_t* __restrict__ col,
+                             const double* __restrict__ vals, const uint8_t* __restrict__ freed, int64_t s1,
+                             float* __restrict__ S) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= mp) return;
     float* row = S + (int64_t)i * mp;
-    if (i >= m || !freed[s0 + i]) {
+    const int ld = perm[i];
+    if (ld < 0 || !freed[s0 + ld]) {
         row[i] = 1.f;
         return;
     }
-    const int64_t r = s0 + i;
+    const int64_t r = s0 + ld;
     for (int32_t k = rp[r]; k < rp[r + 1]; k++) {
         const int64_t c = col[k];
-        if (c >= s0 && c < s0 + m && freed[c]) row[c - s0] = (float)vals[k];
+        if (c >= s0 && c < s1 && freed[c]) row[pinv[c]] = (float)vals[k];
     }
 }
 
 // Interface blocks of the boundary between strip k-1 (start sp) and strip k (start s0):
 // Cc[a, b] = A[I_a, J_b] (rows of strip k, columns of strip k-1) and Bt[a, b] = A[J_b, I_a].
-__global__ void k_fill_iface(int nI, int nJ, int nJp, int64_t s0, int64_t sp, const int32_t* __restrict__ I,
-                             const int32_t* __restrict__ J, const int32_t* __restrict__ Iinv,
+// Irow / Jrow: the local dofs of I_k and J_k-1.
+__global__ void k_fill_iface(int nI, int nJ, int nJp, int64_t s0, int64_t sp, const int32_t* __restrict__ Irow,
+                             const int32_t* __restrict__ Jrow, const int32_t* __restrict__ Iinv,
                              const int32_t* __restrict__ Jinv, const int32_t* __restrict__ lo_ptr,
                              const int32_t* __restrict__ lo_pos, const int32_t* __restrict__ hi_ptr,
                              const int32_t* __restrict__ hi_pos, const int32_t* __restrict__ col,
@@ -187,7 +220,7 @@ __global__ void k_fill_iface(int nI, int nJ, int nJp, int64_t s0, int64_t sp, co
                              float* __restrict__ Bt) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t < nI) {
-        const int64_t r = s0 + I[t];
+        const int64_t r = s0 + Irow[t];
         if (!freed[r]) return;
         for (int32_t q = lo_ptr[r]; q < lo_ptr[r + 1]; q++) {
             const int32_t k = lo_pos[q];
@@ -197,7 +230,7 @@ __global__ void k_fill_iface(int nI, int nJ, int nJp, int64_t s0, int64_t sp, co
         }
     } else if (t < nI + nJ) {
         const int bj = t - nI;
-        const int64_t r = sp + J[bj];
+        const int64_t r = sp + Jrow[bj];
         if (!freed[r]) return;
         for (int32_t q = hi_ptr[r]; q < hi_ptr[r + 1]; q++) {
             const int32_t k = hi_pos[q];
@@ -208,7 +241,7 @@ __global__ void k_fill_iface(int nI, int nJ, int nJp, int64_t s0, int64_t sp, co
     }
 }
 
-// Gjj[a, b] = G[J_a, J_b] (zero padding)
+// Gjj[a, b] = G[J_a, J_b] (positions in the previous strip's order; zero padding)
 __global__ void k_gather_gjj(int nJ, int nJp, const int32_t* __restrict__ J, const float* __restrict__ G, int mpG,
                              float* __restrict__ Gjj) {
     const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
@@ -217,105 +250,101 @@ __global__ void k_gather_gjj(int nJ, int nJp, const int32_t* __restrict__ J, con
     Gjj[t] = (a < nJ && b < nJ) ? G[(int64_t)J[a] * mpG + J[b]] : 0.f;
 }
 
-// S[I_a, I_c] -= U[a, c]
-__global__ void k_scatter_sub(int nI, int nIp, const int32_t* __restrict__ I, const float* __restrict__ U, int mp,
-                              float* __restrict__ S) {
+// S[nNp + a, nNp + c] -= U[a, c]: the I block is contiguous in the strip's order
+__global__ void k_sub_block(int nI, int nIp, int nNp, const float* __restrict__ U, int mp, float* __restrict__ S) {
     const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (t >= (int64_t)nI * nI) return;
     const int a = (int)(t / nI), c = (int)(t % nI);
-    S[(int64_t)I[a] * mp + I[c]] -= U[(int64_t)a * nIp + c];
+    S[(int64_t)(nNp + a) * mp + nNp + c] -= U[(int64_t)a * nIp + c];
 }
 
 // ------------------------------------------------------------------ block Gauss-Jordan
 // P <- inverse of the tile S[t0:t0+128, t0:t0+128] by Gauss-Jordan with partial pivoting inside
-// the tile. A zero or non-finite pivot is counted in *flag and replaced by a tiny value.
+// the tile, one barrier per pivot: every warp finds the pivot itself, and each step reads one
+// shared-memory copy of the tile and writes the other. A zero or non-finite pivot is counted in
+// *flag and replaced by a tiny value.
 constexpr int kTileThreads = 1024;
+constexpr int kTileLD = kNb + 1;
+constexpr int kTileSmem = 2 * kNb * kTileLD * (int)sizeof(float);
 __global__ void __launch_bounds__(kTileThreads) k_tile_inv(const float* __restrict__ S, int mp, int t0,
                                                            float* __restrict__ P, int* __restrict__ flag) {
     extern __shared__ float sm[];
-    constexpr int LD = kNb + 1;
-    float* a = sm;                      // kNb x LD
-    float* f = sm + kNb * LD;           // column k before the update
     __shared__ int piv[kNb];
-    __shared__ int sp;
-    __shared__ float sd;
-    const int tid = threadIdx.x;
+    __shared__ int cperm[kNb];
+    const int tid = threadIdx.x, lane = tid & 31;
+    float* buf0 = sm;
+    float* buf1 = sm + kNb * kTileLD;
     for (int e = tid; e < kNb * kNb; e += kTileThreads) {
         const int r = e / kNb, c = e % kNb;
-        a[r * LD + c] = S[(int64_t)(t0 + r) * mp + t0 + c];
+        buf0[r * kTileLD + c] = S[(int64_t)(t0 + r) * mp + t0 + c];
     }
     __syncthreads();
+    const int c = tid & (kNb - 1), r0 = tid >> 7;  // column c, rows r0 + 8 j
+    int cur = 0;
     for (int k = 0; k < kNb; k++) {
-        if (tid < 32) {
-            float best = -1.f;
-            int bi = k;
-            for (int i = k + tid; i < kNb; i += 32) {
-                const float v = fabsf(a[i * LD + k]);
-                if (v > best) {
-                    best = v;
-                    bi = i;
-                }
+        const float* a = cur ? buf1 : buf0;
+        float* o = cur ? buf0 : buf1;
+        float best = -1.f;
+        int bi = kNb;
+        for (int i = k + lane; i < kNb; i += 32) {
+            const float v = fabsf(a[i * kTileLD + k]);
+            if (v > best) {
+                best = v;
+                bi = i;
             }
+        }
 #pragma unroll
-            for (int o = 16; o > 0; o >>= 1) {
-                const float ob = __shfl_down_sync(0xffffffffu, best, o);
-                const int oi = __shfl_down_sync(0xffffffffu, bi, o);
-                if (ob > best || (ob == best && oi < bi)) {
-                    best = ob;
-                    bi = oi;
-                }
-            }
-            if (tid == 0) {
-                sp = bi;
-                piv[k] = bi;
+        for (int off = 16; off > 0; off >>= 1) {
+            const float ob = __shfl_xor_sync(0xffffffffu, best, off);
+            const int oi = __shfl_xor_sync(0xffffffffu, bi, off);
+            if (ob > best || (ob == best && oi < bi)) {
+                best = ob;
+                bi = oi;
             }
         }
-        __syncthreads();
-        const int p = sp;
-        if (p != k && tid < kNb) {
-            const float t = a[k * LD + tid];
-            a[k * LD + tid] = a[p * LD + tid];
-            a[p * LD + tid] = t;
+        const int p = bi < kNb ? bi : k;
+        if (tid == 0) piv[k] = p;
+        float pv = a[p * kTileLD + k];
+        if (!(fabsf(pv) > 0.f) || !isfinite(pv)) {
+            if (tid == 0) atomicAdd(flag, 1);
+            pv = 1e-30f;
         }
-        __syncthreads();
-        if (tid == 0) {
-            float d = a[k * LD + k];
-            if (!(fabsf(d) > 0.f) || !isfinite(d)) {
-                atomicAdd(flag, 1);
-                d = 1e-30f;
+        const float d = 1.f / pv;
+        const float nk = (c == k ? 1.f : a[p * kTileLD + c]) * d;   // the new pivot row at column c
+#pragma unroll 4
+        for (int j = 0; j < kNb / 8; j++) {
+            const int r = r0 + 8 * j;
+            float v;
+            if (r == k) {
+                v = nk;
+            } else {
+                const int rs = r == p ? k : r;   // rows k and p trade places
+                const float f = a[rs * kTileLD + k];
+                const float prev = c == k ? 0.f : a[rs * kTileLD + c];
+                v = prev - f * nk;
             }
-            sd = 1.f / d;
+            o[r * kTileLD + c] = v;
         }
         __syncthreads();
-        if (tid < kNb) {
-            f[tid] = a[tid * LD + k];
-            const float v = tid == k ? 1.f : a[k * LD + tid];
-            a[k * LD + tid] = v * sd;
-        }
-        __syncthreads();
-        for (int e = tid; e < kNb * kNb; e += kTileThreads) {
-            const int r = e / kNb, c = e % kNb;
-            if (r == k) continue;
-            const float prev = c == k ? 0.f : a[r * LD + c];
-            a[r * LD + c] = prev - f[r] * a[k * LD + c];
-        }
-        __syncthreads();
+        cur ^= 1;
     }
-    // undo the row interchanges: swap columns in reverse order
-    for (int k = kNb - 1; k >= 0; k--) {
-        const int p = piv[k];
-        if (p != k && tid < kNb) {
-            const float t = a[tid * LD + k];
-            a[tid * LD + k] = a[tid * LD + p];
-            a[tid * LD + p] = t;
+    // the row interchanges come back as column interchanges in reverse order
+    if (tid == 0) {
+        for (int i = 0; i < kNb; i++) cperm[i] = i;
+        for (int k = kNb - 1; k >= 0; k--) {
+            const int t = cperm[k];
+            cperm[k] = cperm[piv[k]];
+            cperm[piv[k]] = t;
         }
-        __syncthreads();
     }
-    for (int e = tid; e < kNb * kNb; e += kTileThreads) P[e] = a[(e / kNb) * LD + e % kNb];
+    __syncthreads();
+    const float* a = cur ? buf1 : buf0;
+    for (int e = tid; e < kNb * kNb; e += kTileThreads) P[e] = a[(e / kNb) * kTileLD + cperm[e % kNb]];
 }
 
 // For the 32 columns c0..c0+31: Rt[c, r] = sum_l P[r, l] S[t0 + l, c] (the pivot rows times P, stored
 // transposed), and for the 32 rows c0..c0+31: Ck[i, l] = S[i, t0 + l], zero on the pivot rows.
+constexpr int kPrepSmem = (kNb * kNb + kNb * 33) * (int)sizeof(float);
 __global__ void __launch_bounds__(256) k_panel_prep(const float* __restrict__ S, int mp, int t0,
                                                     const float* __restrict__ P, float* __restrict__ Rt,
                                                     float* __restrict__ Ck) {
@@ -328,7 +357,6 @@ __global__ void __launch_bounds__(256) k_panel_prep(const float* __restrict__ S,
         const int l = e / 32, j = e % 32;
         Sc[l * 33 + j] = S[(int64_t)(t0 + l) * mp + c0 + j];
     }
-    // Ck rows
     for (int e = tid; e < 32 * kNb; e += 256) {
         const int i = c0 + e / kNb, l = e % kNb;
         Ck[(int64_t)i * kNb + l] = (i >= t0 && i < t0 + kNb) ? 0.f : S[(int64_t)i * mp + t0 + l];
@@ -339,9 +367,9 @@ __global__ void __launch_bounds__(256) k_panel_prep(const float* __restrict__ S,
 #pragma unroll
     for (int q = 0; q < 16; q++) acc[q] = 0.f;
     for (int l = 0; l < kNb; l++) {
-        const float s = Sc[l * 33 + j];
+        const float sv = Sc[l * 33 + j];
 #pragma unroll
-        for (int q = 0; q < 16; q++) acc[q] = fmaf(Ps[(rw + 8 * q) * kNb + l], s, acc[q]);
+        for (int q = 0; q < 16; q++) acc[q] = fmaf(Ps[(rw + 8 * q) * kNb + l], sv, acc[q]);
     }
 #pragma unroll
     for (int q = 0; q < 16; q++) Rt[(int64_t)(c0 + j) * kNb + rw + 8 * q] = acc[q];
@@ -349,6 +377,7 @@ __global__ void __launch_bounds__(256) k_panel_prep(const float* __restrict__ S,
 
 // After the rank-128 update: S[i, t0 + l] = -(Ck P)[i, l] for the non-pivot rows i of this block's 32
 // rows; S[t0 + r, c] = Rt[c, r] for this block's 32 columns c outside the tile, P inside it.
+constexpr int kFinishSmem = (kNb * kNb + 32 * (kNb + 1)) * (int)sizeof(float);
 __global__ void __launch_bounds__(256) k_panel_finish(float* __restrict__ S, int mp, int t0,
                                                       const float* __restrict__ P, const float* __restrict__ Rt,
                                                       const float* __restrict__ Ck) {
@@ -357,9 +386,9 @@ __global__ void __launch_bounds__(256) k_panel_finish(float* __restrict__ S, int
     float* Cs = sm + kNb * kNb;      // 32 x (kNb + 1)
     const int tid = threadIdx.x, c0 = blockIdx.x * 32;
     for (int e = tid; e < kNb * kNb; e += 256) Ps[e] = P[e];
-    for (int e = tid; e < 32 * kNb; e += 256) Cs[(e / kNb) * (kNb + 1) + e % kNb] = Ck[(int64_t)(c0 + e / kNb) * kNb + e % kNb];
+    for (int e = tid; e < 32 * kNb; e += 256)
+        Cs[(e / kNb) * (kNb + 1) + e % kNb] = Ck[(int64_t)(c0 + e / kNb) * kNb + e % kNb];
     __syncthreads();
-    // column block: row i = c0 + ii, column l; thread: l = tid & 127, rows ii = (tid >> 7) + 2 q
     {
         const int l = tid & (kNb - 1), r0 = tid >> 7;
         for (int ii = r0; ii < 32; ii += 2) {
@@ -370,7 +399,6 @@ __global__ void __launch_bounds__(256) k_panel_finish(float* __restrict__ S, int
             S[(int64_t)i * mp + t0 + l] = -acc;
         }
     }
-    // row block
     for (int e = tid; e < 32 * kNb; e += 256) {
         const int jj = e / kNb, r = e % kNb;
         const int c = c0 + jj;
@@ -380,69 +408,76 @@ __global__ void __launch_bounds__(256) k_panel_finish(float* __restrict__ S, int
 }
 
 // ------------------------------------------------------------------ sweeps
-// forward right-hand side of strip [s0, s0 + m): r_i = sc v_i - sum A[i, c] z_c over the entries
-// whose column lies in the previous strip (z holds that strip's y); zero on constrained rows and
-// on the padding up to mp
+// z = sc v with sc = scale[j] (the GMRES basis vector into the preconditioner's input)
 template <class T>
-__global__ void k_fwd_rhs(int m, int mp, int64_t s0, const int32_t* __restrict__ lo_ptr,
-                          const int32_t* __restrict__ lo_pos, const int32_t* __restrict__ col,
-                          const double* __restrict__ vals, const uint8_t* __restrict__ freed, const T* __restrict__ v,
-                          const double* __restrict__ scale, int j, const T* __restrict__ z, float* __restrict__ r,
-                          const int* __restrict__ flags) {
+__global__ void k_scale_copy(int64_t n, const T* __restrict__ v, const double* __restrict__ scale, int j,
+                             T* __restrict__ z, const int* __restrict__ flags) {
     if (flags && flags[0]) return;
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= mp) return;
-    if (i >= m) {
-        r[i] = 0.f;
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i < n) z[i] = (T)((double)v[i] * scale[j]);
+}
+
+// forward right-hand side of strip [s0, s1) in the strip's order: r_p = z_i - sum A[i, c] z_c over
+// the entries whose column lies in the previous strip (z holds that strip's y, and this strip's
+// input); zero on constrained rows and on the padding
+template <class T>
+__global__ void k_fwd_rhs(int mp, int64_t s0, const int32_t* __restrict__ perm, const int32_t* __restrict__ lo_ptr,
+                          const int32_t* __restrict__ lo_pos, const int32_t* __restrict__ col,
+                          const double* __restrict__ vals, const uint8_t* __restrict__ freed, const T* __restrict__ z,
+                          float* __restrict__ r, const int* __restrict__ flags) {
+    if (flags && flags[0]) return;
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= mp) return;
+    const int ld = perm[p];
+    if (ld < 0 || !freed[s0 + ld]) {
+        r[p] = 0.f;
         return;
     }
-    const int64_t row = s0 + i;
-    if (!freed[row]) {
-        r[i] = 0.f;
-        return;
-    }
-    const double sc = scale ? scale[j] : 1.0;
-    float acc = (float)(sc * (double)v[row]);
+    const int64_t row = s0 + ld;
+    float acc = (float)z[row];
     for (int32_t q = lo_ptr[row]; q < lo_ptr[row + 1]; q++) {
         const int32_t k = lo_pos[q];
         const int32_t c = col[k];
         if (freed[c]) acc -= (float)vals[k] * (float)z[c];
     }
-    r[i] = acc;
+    r[p] = acc;
 }
 
-// backward right-hand side: r_i = sum A[i, c] z_c over the entries in the next strip
+// backward right-hand side: r_p = sum A[i, c] z_c over the entries in the next strip
 template <class T>
-__global__ void k_bwd_rhs(int m, int mp, int64_t s0, const int32_t* __restrict__ hi_ptr,
+__global__ void k_bwd_rhs(int mp, int64_t s0, const int32_t* __restrict__ perm, const int32_t* __restrict__ hi_ptr,
                           const int32_t* __restrict__ hi_pos, const int32_t* __restrict__ col,
                           const double* __restrict__ vals, const uint8_t* __restrict__ freed, const T* __restrict__ z,
                           float* __restrict__ r, const int* __restrict__ flags) {
     if (flags && flags[0]) return;
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= mp) return;
-    if (i >= m || !freed[s0 + i]) {
-        r[i] = 0.f;
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= mp) return;
+    const int ld = perm[p];
+    if (ld < 0 || !freed[s0 + ld]) {
+        r[p] = 0.f;
         return;
     }
-    const int64_t row = s0 + i;
+    const int64_t row = s0 + ld;
     float acc = 0.f;
     for (int32_t q = hi_ptr[row]; q < hi_ptr[row + 1]; q++) {
         const int32_t k = hi_pos[q];
         const int32_t c = col[k];
         if (freed[c]) acc += (float)vals[k] * (float)z[c];
     }
-    r[i] = acc;
+    r[p] = acc;
 }
 
-// z_i = (G r)_i (mode 0) or z_i -= (G r)_i (mode 1) for the strip's m rows; a warp per row, 16-byte
-// loads (mp is a multiple of 128)
+// z_i = (G r)_p (mode 0) or z_i -= (G r)_p (mode 1), i = the local dof at position p; a warp per
+// row, 16-byte loads (mp is a multiple of 128)
 template <class T>
-__global__ void __launch_bounds__(256) k_strip_gemv(int m, int mp, const float* __restrict__ G,
-                                                    const float* __restrict__ r, T* __restrict__ z, int mode,
-                                                    const int* __restrict__ flags) {
+__global__ void __launch_bounds__(256) k_strip_gemv(int mp, int64_t s0, const int32_t* __restrict__ perm,
+                                                    const float* __restrict__ G, const float* __restrict__ r,
+                                                    T* __restrict__ z, int mode, const int* __restrict__ flags) {
     if (flags && flags[0]) return;
     const int row = blockIdx.x * 8 + (threadIdx.x >> 5), lane = threadIdx.x & 31;
-    if (row >= m) return;
+    if (row >= mp) return;
+    const int ld = perm[row];
+    if (ld < 0) return;
     const float4* g = reinterpret_cast<const float4*>(G + (int64_t)row * mp);
     const float4* rv = reinterpret_cast<const float4*>(r);
     float acc = 0.f;
@@ -457,30 +492,43 @@ __global__ void __launch_bounds__(256) k_strip_gemv(int m, int mp, const float* 
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
     if (lane == 0) {
-        if (mode == 0) z[row] = (T)acc;
-        else z[row] = (T)((float)z[row] - acc);
+        T* zi = z + s0 + ld;
+        if (mode == 0) *zi = (T)acc;
+        else *zi = (T)((float)*zi - acc);
     }
 }
 
 template <class T>
-__global__ void k_add_to(int64_t n, const T* __restrict__ z, double* __restrict__ x, const int* __restrict__ flags) {
+__global__ void k_add_to(int64_t n, const T* __restrict__ z, double* __restrict__ x) {
     const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (i < n) x[i] += (double)z[i];
 }
 
 // ------------------------------------------------------------------ host helpers
 void strip_free(Strip* p) {
-    void* ps[] = {p->d_I, p->d_J, p->d_Iinv, p->d_Jinv, p->d_lo_ptr, p->d_lo_pos, p->d_hi_ptr, p->d_hi_pos, p->d_G,
-                  p->d_Bt, p->d_Cc, p->d_Gjj, p->d_Tt, p->d_U, p->d_P, p->d_Ck, p->d_Rt, p->d_r, p->d_flag};
+    void* ps[] = {p->d_perm, p->d_I, p->d_J, p->jrow, p->d_pinv, p->d_Iinv, p->d_Jinv, p->d_lo_ptr, p->d_lo_pos, p->d_hi_ptr,
+                  p->d_hi_pos, p->d_G, p->d_Bt, p->d_Cc, p->d_Gjj, p->d_Tt, p->d_U, p->d_r, p->d_flag};
     for (void* q : ps) dfree(q);
+    for (auto& w : p->work) {
+        dfree(w.P);
+        dfree(w.Ck);
+        dfree(w.Rt);
+    }
     for (cudaEvent_t e : p->ev) cudaEventDestroy(e);
+    for (cudaEvent_t e : p->ev_phase1) cudaEventDestroy(e);
     for (cudaEvent_t e : p->fev)
         if (e) cudaEventDestroy(e);
+    if (p->ev_start) cudaEventDestroy(p->ev_start);
+    for (cudaStream_t q : p->side)
+        if (q) cudaStreamDestroy(q);
+    for (cudaGraphExec_t g : p->gexec)
+        if (g) cudaGraphExecDestroy(g);
+    if (p->cap) cudaStreamDestroy(p->cap);
 }
 
 int gemm(Strip* p, int M, int N, int K, const float* A, int64_t lda, const float* B, int64_t ldb, float* C, int64_t ldc,
          float alpha, float beta, cudaStream_t st) {
-    if (M % GB || N % GB || K % GK || M <= 0 || N <= 0 || K <= 0)
+    if (M % GB || N % GB || K % 32 || M <= 0 || N <= 0 || K <= 0)
         return fail(OCMP_ERR_ARG, "strip gemm: sizes must be multiples of the tile");
     const bool t = p->timing;
     if (t) {
@@ -503,6 +551,18 @@ int gemm(Strip* p, int M, int N, int K, const float* A, int64_t lda, const float
         p->ev_used += 2;
     }
     p->gemm_flops_pending += 2.0 * M * N * (double)K;
+    return OCMP_OK;
+}
+
+// Gauss-Jordan over the pivot tiles [t_begin, t_end) of S (mp x mp) on stream st with workspace w
+int gj_tiles(Strip* p, float* S, int mp, int t_begin, int t_end, const StripWork& w, cudaStream_t st) {
+    for (int t0 = t_begin; t0 < t_end; t0 += kNb) {
+        OCMP_LAUNCH(k_tile_inv<<<1, kTileThreads, kTileSmem, st>>>(S, mp, t0, w.P, p->d_flag));
+        OCMP_LAUNCH(k_panel_prep<<<mp / 32, 256, kPrepSmem, st>>>(S, mp, t0, w.P, w.Rt, w.Ck));
+        const int r = gemm(p, mp, mp, kNb, w.Ck, kNb, w.Rt, kNb, S, mp, -1.f, 1.f, st);
+        if (r) return r;
+        OCMP_LAUNCH(k_panel_finish<<<mp / 32, 256, kFinishSmem, st>>>(S, mp, t0, w.P, w.Rt, w.Ck));
+    }
     return OCMP_OK;
 }
 
@@ -551,65 +611,91 @@ int strip_create(const ocmp_space_s* s, Strip** out) {
             }
         }
     }
+    // interface sets: I_k = dofs of strip k coupled to strip k-1 (by their row or their column),
+    // J_k = dofs of strip k coupled to strip k+1
     p->m.resize(K);
-    p->mp.resize(K);
-    p->goff.resize(K + 1);
-    int64_t total = 0;
+    p->nN.resize(K);
+    p->nNp.resize(K);
+    p->nI.assign(K, 0);
+    p->nJ.assign(K, 0);
+    std::vector<std::vector<char>> inI(K), inJ(K);
     for (int k = 0; k < K; k++) {
         p->m[k] = (int)(p->s[k + 1] - p->s[k]);
-        p->mp[k] = pad(p->m[k]);
+        inI[k].assign(p->m[k], 0);
+        inJ[k].assign(p->m[k], 0);
+    }
+    for (int k = 0; k < K; k++) {
+        const int64_t s0 = p->s[k], s1 = p->s[k + 1];
+        for (int64_t r = s0; r < s1; r++)
+            for (int64_t q = rp[r]; q < rp[r + 1]; q++) {
+                const int64_t c = col[q];
+                if (c < s0) {
+                    inI[k][r - s0] = 1;
+                    inJ[k - 1][c - p->s[k - 1]] = 1;
+                } else if (c >= s1) {
+                    inJ[k][r - s0] = 1;
+                    inI[k + 1][c - s1] = 1;
+                }
+            }
+    }
+    p->mp.resize(K);
+    p->goff.resize(K + 1);
+    p->poff.resize(K + 1);
+    p->ioff.assign(K + 1, 0);
+    p->joff.assign(K + 1, 0);
+    std::vector<int32_t> perm, pinv(n, -1), Ipos, Jpos, Iinv(n, -1), Jinv(n, -1);
+    int64_t total = 0;
+    for (int k = 0; k < K; k++) {
+        const int m = p->m[k];
+        const int64_t s0 = p->s[k];
+        std::vector<int32_t> Nl, Il;
+        for (int i = 0; i < m; i++) (inI[k][i] ? Il : Nl).push_back(i);
+        p->nN[k] = (int)Nl.size();
+        p->nNp[k] = pad(p->nN[k]);
+        p->nI[k] = (int)Il.size();
+        p->mp[k] = p->nNp[k] + pad(p->nI[k]);
         p->goff[k] = total;
         total += (int64_t)p->mp[k] * p->mp[k];
+        p->poff[k] = (int64_t)perm.size();
         p->mp_max = std::max(p->mp_max, p->mp[k]);
+        std::vector<int32_t> pm(p->mp[k], -1);
+        for (int q = 0; q < p->nN[k]; q++) pm[q] = Nl[q];
+        for (int q = 0; q < p->nI[k]; q++) pm[p->nNp[k] + q] = Il[q];
+        for (int q = 0; q < p->mp[k]; q++)
+            if (pm[q] >= 0) pinv[s0 + pm[q]] = q;
+        perm.insert(perm.end(), pm.begin(), pm.end());
+        p->ioff[k] = (int64_t)Ipos.size();
+        for (int q = 0; q < p->nI[k]; q++) {
+            Iinv[s0 + Il[q]] = q;
+            Ipos.push_back(Il[q]);         // local dofs (fill_iface); their positions are nNp + q
+        }
+        p->joff[k] = (int64_t)Jpos.size();
+        for (int i = 0; i < m; i++)
+            if (inJ[k][i]) {
+                Jinv[s0 + i] = p->nJ[k]++;
+                Jpos.push_back(i);
+            }
+        p->nIp_max = std::max(p->nIp_max, pad(p->nI[k]));
+        p->nJp_max = std::max(p->nJp_max, pad(p->nJ[k]));
     }
     p->goff[K] = total;
+    p->poff[K] = (int64_t)perm.size();
+    p->ioff[K] = (int64_t)Ipos.size();
+    p->joff[K] = (int64_t)Jpos.size();
     if (p->mp_max > 16384) {
         const int mm = p->mp_max;
         delete p;
         return fail(OCMP_ERR_UNSUPPORTED, "strip preconditioner: a strip of " + std::to_string(mm) +
                                               " dofs exceeds the 16384-dof limit (number the dofs so the matrix is banded)");
     }
-    // interface sets and coupling lists
-    std::vector<int32_t> I, J, Iinv(n, -1), Jinv(n, -1);
+    // J_k as positions in strip k's order (the Schur update gathers G_k[J, J]); the local dofs stay in
+    // Jrow for the interface fill
+    std::vector<int32_t> Jp(Jpos.size());
+    for (int k = 0; k < K; k++)
+        for (int64_t q = p->joff[k]; q < p->joff[k + 1]; q++) Jp[q] = pinv[p->s[k] + Jpos[q]];
     std::vector<int32_t> lo_ptr(n + 1, 0), hi_ptr(n + 1, 0), lo_pos, hi_pos;
-    p->nI.assign(K, 0);
-    p->nJ.assign(K, 0);
-    p->ioff.assign(K + 1, 0);
-    p->joff.assign(K + 1, 0);
     for (int k = 0; k < K; k++) {
         const int64_t s0 = p->s[k], s1 = p->s[k + 1];
-        std::vector<char> inI(p->m[k], 0), inJ(p->m[k], 0);
-        for (int64_t r = s0; r < s1; r++) {
-            for (int64_t q = rp[r]; q < rp[r + 1]; q++) {
-                const int64_t c = col[q];
-                if (c < s0) inI[r - s0] = 1;
-                if (c >= s1) inJ[r - s0] = 1;
-            }
-        }
-        // column sides (structurally unsymmetric patterns): columns of this strip reached from the
-        // neighbours' rows belong to the interface too
-        if (k > 0)
-            for (int64_t r = p->s[k - 1]; r < s0; r++)
-                for (int64_t q = rp[r]; q < rp[r + 1]; q++)
-                    if (col[q] >= s0) inI[col[q] - s0] = 1;
-        if (k + 1 < K)
-            for (int64_t r = s1; r < p->s[k + 2]; r++)
-                for (int64_t q = rp[r]; q < rp[r + 1]; q++)
-                    if (col[q] < s1) inJ[col[q] - s0] = 1;
-        p->ioff[k] = (int64_t)I.size();
-        p->joff[k] = (int64_t)J.size();
-        for (int i = 0; i < p->m[k]; i++) {
-            if (inI[i]) {
-                Iinv[s0 + i] = p->nI[k]++;
-                I.push_back(i);
-            }
-            if (inJ[i]) {
-                Jinv[s0 + i] = p->nJ[k]++;
-                J.push_back(i);
-            }
-        }
-        p->nIp_max = std::max(p->nIp_max, pad(p->nI[k]));
-        p->nJp_max = std::max(p->nJp_max, pad(p->nJ[k]));
         for (int64_t r = s0; r < s1; r++) {
             for (int64_t q = rp[r]; q < rp[r + 1]; q++) {
                 if (col[q] < s0) lo_pos.push_back((int32_t)q);
@@ -619,11 +705,8 @@ int strip_create(const ocmp_space_s* s, Strip** out) {
             hi_ptr[r + 1] = (int32_t)hi_pos.size();
         }
     }
-    p->ioff[K] = (int64_t)I.size();
-    p->joff[K] = (int64_t)J.size();
     const int ifp = std::max(p->nIp_max, p->nJp_max);
-    const int64_t need = total * 4 + (int64_t)3 * ifp * ifp * 4 + (int64_t)2 * ifp * ifp * 4 +
-                         (int64_t)p->mp_max * kNb * 8 + kNb * kNb * 4;
+    const int64_t need = total * 4 + (int64_t)5 * ifp * ifp * 4 + (int64_t)(kSide + 1) * (2 * p->mp_max * kNb + kNb * kNb) * 4;
     size_t fr = 0, tot = 0;
     cudaMemGetInfo(&fr, &tot);
     if ((size_t)need > fr) {
@@ -635,14 +718,18 @@ int strip_create(const ocmp_space_s* s, Strip** out) {
     auto U = [&](auto** d, const auto& h) {
         if (!st) st = upload(d, h.data(), h.size());
     };
-    U(&p->d_I, I);
-    U(&p->d_J, J);
+    U(&p->d_perm, perm);
+    U(&p->d_pinv, pinv);
+    U(&p->d_I, Ipos);
+    U(&p->d_J, Jp);
     U(&p->d_Iinv, Iinv);
     U(&p->d_Jinv, Jinv);
     U(&p->d_lo_ptr, lo_ptr);
     U(&p->d_lo_pos, lo_pos);
     U(&p->d_hi_ptr, hi_ptr);
     U(&p->d_hi_pos, hi_pos);
+    p->bytes = total * 4 + (int64_t)(perm.size() + Ipos.size() + Jp.size() + 3 * n + 2 * (n + 1) + lo_pos.size() +
+                                     hi_pos.size()) * 4;
     auto A = [&](auto** d, size_t cnt) {
         if (!st) st = dalloc(d, cnt);
     };
@@ -652,23 +739,34 @@ int strip_create(const ocmp_space_s* s, Strip** out) {
     A(&p->d_Gjj, (size_t)ifp * ifp);
     A(&p->d_Tt, (size_t)ifp * ifp);
     A(&p->d_U, (size_t)ifp * ifp);
-    A(&p->d_P, (size_t)kNb * kNb);
-    A(&p->d_Ck, (size_t)p->mp_max * kNb);
-    A(&p->d_Rt, (size_t)p->mp_max * kNb);
+    for (auto& w : p->work) {
+        A(&w.P, (size_t)kNb * kNb);
+        A(&w.Ck, (size_t)p->mp_max * kNb);
+        A(&w.Rt, (size_t)p->mp_max * kNb);
+    }
     A(&p->d_r, (size_t)p->mp_max);
     A(&p->d_flag, 2);
-    if (!st && cudaEventCreate(&p->fev[0]) != cudaSuccess) st = fail(OCMP_ERR_CUDA, "cudaEventCreate");
-    if (!st && cudaEventCreate(&p->fev[1]) != cudaSuccess) st = fail(OCMP_ERR_CUDA, "cudaEventCreate");
+    U(&p->jrow, Jpos);
+    p->bytes += (int64_t)Jpos.size() * 4;
+    if (!st && (cudaEventCreateWithFlags(&p->fev[0], cudaEventDefault) != cudaSuccess ||
+                cudaEventCreateWithFlags(&p->fev[1], cudaEventDefault) != cudaSuccess ||
+                cudaEventCreateWithFlags(&p->ev_start, cudaEventDisableTiming) != cudaSuccess))
+        st = fail(OCMP_ERR_CUDA, "cudaEventCreate");
+    for (int q = 0; q < kSide && !st; q++)
+        if (cudaStreamCreateWithFlags(&p->side[q], cudaStreamNonBlocking) != cudaSuccess)
+            st = fail(OCMP_ERR_CUDA, "cudaStreamCreateWithFlags");
+    if (!st && cudaStreamCreateWithFlags(&p->cap, cudaStreamNonBlocking) != cudaSuccess)
+        st = fail(OCMP_ERR_CUDA, "cudaStreamCreateWithFlags");
+    p->ev_phase1.assign(K, nullptr);
+    for (int k = 0; k < K && !st; k++)
+        if (cudaEventCreateWithFlags(&p->ev_phase1[k], cudaEventDisableTiming) != cudaSuccess)
+            st = fail(OCMP_ERR_CUDA, "cudaEventCreate");
     if (!st) {
-        const int tsm = (kNb * (kNb + 1) + kNb) * (int)sizeof(float);
-        const int psm = (kNb * kNb + kNb * 33) * (int)sizeof(float);
-        const int fsm = (kNb * kNb + 32 * (kNb + 1)) * (int)sizeof(float);
-        if (cudaFuncSetAttribute(k_tile_inv, cudaFuncAttributeMaxDynamicSharedMemorySize, tsm) != cudaSuccess ||
-            cudaFuncSetAttribute(k_panel_prep, cudaFuncAttributeMaxDynamicSharedMemorySize, psm) != cudaSuccess ||
-            cudaFuncSetAttribute(k_panel_finish, cudaFuncAttributeMaxDynamicSharedMemorySize, fsm) != cudaSuccess)
+        if (cudaFuncSetAttribute(k_tile_inv, cudaFuncAttributeMaxDynamicSharedMemorySize, kTileSmem) != cudaSuccess ||
+            cudaFuncSetAttribute(k_panel_prep, cudaFuncAttributeMaxDynamicSharedMemorySize, kPrepSmem) != cudaSuccess ||
+            cudaFuncSetAttribute(k_panel_finish, cudaFuncAttributeMaxDynamicSharedMemorySize, kFinishSmem) != cudaSuccess)
             st = fail(OCMP_ERR_CUDA, "strip preconditioner: shared-memory attribute");
     }
-    p->bytes = total * 4 + (int64_t)(I.size() + J.size() + 2 * n + 2 * (n + 1) + lo_pos.size() + hi_pos.size()) * 4;
     if (st) {
         strip_free(p);
         delete p;
@@ -690,39 +788,45 @@ int strip_factor(Strip* p, const ocmp_space_s* s, const double* vals, cudaStream
     p->gemm_flops_pending = 0;
     OCMP_CUDA(cudaEventRecord(p->fev[0], st));
     OCMP_CUDA(cudaMemsetAsync(p->d_flag, 0, 2 * sizeof(int), st));
-    const int tsm = (kNb * (kNb + 1) + kNb) * (int)sizeof(float);
-    const int psm = (kNb * kNb + kNb * 33) * (int)sizeof(float);
-    const int fsm = (kNb * kNb + 32 * (kNb + 1)) * (int)sizeof(float);
+    OCMP_CUDA(cudaEventRecord(p->ev_start, st));
+    for (int q = 0; q < kSide; q++) OCMP_CUDA(cudaStreamWaitEvent(p->side[q], p->ev_start, 0));
+    // phase 1: fill every strip and eliminate its N pivots, strips spread over the side streams
     for (int k = 0; k < K; k++) {
-        const int m = p->m[k], mp = p->mp[k];
+        const int q = k % kSide;
+        cudaStream_t ss = p->side[q];
+        const int mp = p->mp[k];
+        float* S = p->d_G + p->goff[k];
+        OCMP_CUDA(cudaMemsetAsync(S, 0, sizeof(float) * (size_t)mp * mp, ss));
+        OCMP_LAUNCH(k_fill_strip<<<nblk(mp, 128), 128, 0, ss>>>(mp, p->s[k], p->d_perm + p->poff[k], p->d_pinv, s->d_rowptr,
+                                                               s->d_col, vals, s->d_free, p->s[k + 1], S));
+        int r = gj_tiles(p, S, mp, 0, p->nNp[k], p->work[1 + q], ss);
+        if (r) return r;
+        OCMP_CUDA(cudaEventRecord(p->ev_phase1[k], ss));
+    }
+    // phase 2 on the caller's stream, strip after strip: the Schur update from the previous strip's
+    // inverse, then the I pivots
+    for (int k = 0; k < K; k++) {
+        OCMP_CUDA(cudaStreamWaitEvent(st, p->ev_phase1[k], 0));
+        const int mp = p->mp[k];
         const int64_t s0 = p->s[k];
         float* S = p->d_G + p->goff[k];
-        OCMP_CUDA(cudaMemsetAsync(S, 0, sizeof(float) * (size_t)mp * mp, st));
-        OCMP_LAUNCH(k_fill_strip<<<nblk(mp, 128), 128, 0, st>>>(m, mp, s0, s->d_rowptr, s->d_col, vals, s->d_free, S));
         if (k > 0 && p->nI[k] > 0 && p->nJ[k - 1] > 0) {
             const int nI = p->nI[k], nJ = p->nJ[k - 1], nIp = pad(nI), nJp = pad(nJ);
-            const int mpp = p->mp[k - 1];
             OCMP_CUDA(cudaMemsetAsync(p->d_Cc, 0, sizeof(float) * (size_t)nIp * nJp, st));
             OCMP_CUDA(cudaMemsetAsync(p->d_Bt, 0, sizeof(float) * (size_t)nIp * nJp, st));
             OCMP_LAUNCH(k_fill_iface<<<nblk(nI + nJ, 128), 128, 0, st>>>(
-                nI, nJ, nJp, s0, p->s[k - 1], p->d_I + p->ioff[k], p->d_J + p->joff[k - 1], p->d_Iinv, p->d_Jinv,
+                nI, nJ, nJp, s0, p->s[k - 1], p->d_I + p->ioff[k], p->jrow + p->joff[k - 1], p->d_Iinv, p->d_Jinv,
                 p->d_lo_ptr, p->d_lo_pos, p->d_hi_ptr, p->d_hi_pos, s->d_col, vals, s->d_free, p->d_Cc, p->d_Bt));
             OCMP_LAUNCH(k_gather_gjj<<<nblk((int64_t)nJp * nJp, 256), 256, 0, st>>>(
-                nJ, nJp, p->d_J + p->joff[k - 1], p->d_G + p->goff[k - 1], mpp, p->d_Gjj));
+                nJ, nJp, p->d_J + p->joff[k - 1], p->d_G + p->goff[k - 1], p->mp[k - 1], p->d_Gjj));
             // Tt = Bt Gjj^T (= (G_JJ A_JI)^T), U = Cc Tt^T
             int r = gemm(p, nIp, nJp, nJp, p->d_Bt, nJp, p->d_Gjj, nJp, p->d_Tt, nJp, 1.f, 0.f, st);
             if (!r) r = gemm(p, nIp, nIp, nJp, p->d_Cc, nJp, p->d_Tt, nJp, p->d_U, nIp, 1.f, 0.f, st);
             if (r) return r;
-            OCMP_LAUNCH(k_scatter_sub<<<nblk((int64_t)nI * nI, 256), 256, 0, st>>>(nI, nIp, p->d_I + p->ioff[k], p->d_U,
-                                                                                  mp, S));
+            OCMP_LAUNCH(k_sub_block<<<nblk((int64_t)nI * nI, 256), 256, 0, st>>>(nI, nIp, p->nNp[k], p->d_U, mp, S));
         }
-        for (int t0 = 0; t0 < mp; t0 += kNb) {
-            OCMP_LAUNCH(k_tile_inv<<<1, kTileThreads, tsm, st>>>(S, mp, t0, p->d_P, p->d_flag));
-            OCMP_LAUNCH(k_panel_prep<<<mp / 32, 256, psm, st>>>(S, mp, t0, p->d_P, p->d_Rt, p->d_Ck));
-            int r = gemm(p, mp, mp, kNb, p->d_Ck, kNb, p->d_Rt, kNb, S, mp, -1.f, 1.f, st);
-            if (r) return r;
-            OCMP_LAUNCH(k_panel_finish<<<mp / 32, 256, fsm, st>>>(S, mp, t0, p->d_P, p->d_Rt, p->d_Ck));
-        }
+        int r = gj_tiles(p, S, mp, p->nNp[k], mp, p->work[0], st);
+        if (r) return r;
     }
     OCMP_CUDA(cudaGetLastError());
     OCMP_CUDA(cudaEventRecord(p->fev[1], st));
@@ -732,8 +836,7 @@ int strip_factor(Strip* p, const ocmp_space_s* s, const double* vals, cudaStream
     float ms = 0;
     OCMP_CUDA(cudaEventElapsedTime(&ms, p->fev[0], p->fev[1]));
     p->factor_ms = ms;
-    const int flag = flags[0];
-    p->singular = flag;
+    p->singular = flags[0];
     if (flags[1]) return fail(OCMP_TIMEOUT, "strip preconditioner: a tensor-core product gave up a bounded wait");
     p->gemm_flops = p->gemm_flops_pending;
     p->gemm_ms = 0;
@@ -742,29 +845,69 @@ int strip_factor(Strip* p, const ocmp_space_s* s, const double* vals, cudaStream
         OCMP_CUDA(cudaEventElapsedTime(&e, p->ev[q], p->ev[q + 1]));
         p->gemm_ms += e;
     }
-    if (flag) return fail(OCMP_BREAKDOWN, "strip preconditioner: " + std::to_string(flag) +
-                                              " zero or non-finite pivots in the strip factorisation");
+    if (flags[0]) return fail(OCMP_BREAKDOWN, "strip preconditioner: " + std::to_string(flags[0]) +
+                                                  " zero or non-finite pivots in the strip factorisation");
     return OCMP_OK;
 }
+
+namespace {
+// the two sweeps, in place on z (input: the vector to precondition)
+template <class T>
+void sweeps(Strip* p, const ocmp_space_s* s, const double* vals, T* z, const int* flags, cudaStream_t st) {
+    const int K = p->K;
+    for (int k = 0; k < K; k++) {
+        const int mp = p->mp[k];
+        const int32_t* pm = p->d_perm + p->poff[k];
+        OCMP_LAUNCH(k_fwd_rhs<T><<<nblk(mp, 256), 256, 0, st>>>(mp, p->s[k], pm, p->d_lo_ptr, p->d_lo_pos, s->d_col,
+                                                               vals, s->d_free, z, p->d_r, flags));
+        OCMP_LAUNCH(k_strip_gemv<T><<<nblk(mp, 8), 256, 0, st>>>(mp, p->s[k], pm, p->d_G + p->goff[k], p->d_r, z, 0,
+                                                                flags));
+    }
+    for (int k = K - 2; k >= 0; k--) {
+        const int mp = p->mp[k];
+        const int32_t* pm = p->d_perm + p->poff[k];
+        OCMP_LAUNCH(k_bwd_rhs<T><<<nblk(mp, 256), 256, 0, st>>>(mp, p->s[k], pm, p->d_hi_ptr, p->d_hi_pos, s->d_col,
+                                                               vals, s->d_free, z, p->d_r, flags));
+        OCMP_LAUNCH(k_strip_gemv<T><<<nblk(mp, 8), 256, 0, st>>>(mp, p->s[k], pm, p->d_G + p->goff[k], p->d_r, z, 1,
+                                                                flags));
+    }
+}
+}  // namespace
 
 template <class T>
 int strip_apply(Strip* p, const ocmp_space_s* s, const double* vals, const T* v, const double* scale, int j, T* z,
                 const int* flags, cudaStream_t st) {
-    const int K = p->K;
-    for (int k = 0; k < K; k++) {
-        const int m = p->m[k], mp = p->mp[k];
-        const int64_t s0 = p->s[k];
-        OCMP_LAUNCH(k_fwd_rhs<T><<<nblk(mp, 256), 256, 0, st>>>(m, mp, s0, p->d_lo_ptr, p->d_lo_pos, s->d_col, vals,
-                                                               s->d_free, v, scale, j, z, p->d_r, flags));
-        OCMP_LAUNCH(k_strip_gemv<T><<<nblk(m, 8), 256, 0, st>>>(m, mp, p->d_G + p->goff[k], p->d_r, z + s0, 0, flags));
+    const int64_t n = s->ndof;
+    if (v != z) {
+        if (scale) OCMP_LAUNCH(k_scale_copy<T><<<nblk(n, 256), 256, 0, st>>>(n, v, scale, j, z, flags));
+        else OCMP_CUDA(cudaMemcpyAsync(z, v, sizeof(T) * n, cudaMemcpyDeviceToDevice, st));
     }
-    for (int k = K - 2; k >= 0; k--) {
-        const int m = p->m[k], mp = p->mp[k];
-        const int64_t s0 = p->s[k];
-        OCMP_LAUNCH(k_bwd_rhs<T><<<nblk(mp, 256), 256, 0, st>>>(m, mp, s0, p->d_hi_ptr, p->d_hi_pos, s->d_col, vals,
-                                                               s->d_free, z, p->d_r, flags));
-        OCMP_LAUNCH(k_strip_gemv<T><<<nblk(m, 8), 256, 0, st>>>(m, mp, p->d_G + p->goff[k], p->d_r, z + s0, 1, flags));
+    // the sweeps (4 launches per strip) replay from a graph captured on first use for this
+    // (vector, flag, matrix) on the library's own stream
+    const int gi = flags ? 0 : 1;
+    const int type = sizeof(T) == 8 ? 1 : 2;
+    if (!p->gexec[gi] || p->g_z[gi] != z || p->g_flags[gi] != flags || p->g_vals[gi] != vals || p->g_type[gi] != type) {
+        if (p->gexec[gi]) {
+            cudaGraphExecDestroy(p->gexec[gi]);
+            p->gexec[gi] = nullptr;
+        }
+        cudaGraph_t g;
+        const unsigned long long l0 = g_launches.load();
+        OCMP_CUDA(cudaStreamBeginCapture(p->cap, cudaStreamCaptureModeThreadLocal));
+        sweeps<T>(p, s, vals, z, flags, p->cap);
+        OCMP_CUDA(cudaStreamEndCapture(p->cap, &g));
+        p->gkernels[gi] = g_launches.load() - l0;
+        g_launches.fetch_sub(p->gkernels[gi]);
+        cudaError_t e = cudaGraphInstantiate(&p->gexec[gi], g, 0);
+        cudaGraphDestroy(g);
+        if (e != cudaSuccess) return cuda_fail(e, "cudaGraphInstantiate (strip sweeps)");
+        p->g_z[gi] = z;
+        p->g_flags[gi] = flags;
+        p->g_vals[gi] = vals;
+        p->g_type[gi] = type;
     }
+    OCMP_CUDA(cudaGraphLaunch(p->gexec[gi], st));
+    g_launches.fetch_add(p->gkernels[gi]);
     return OCMP_OK;
 }
 template int strip_apply<double>(Strip*, const ocmp_space_s*, const double*, const double*, const double*, int,
@@ -774,7 +917,7 @@ template int strip_apply<float>(Strip*, const ocmp_space_s*, const double*, cons
 
 template <class T>
 int strip_add(int64_t n, const T* z, double* x, cudaStream_t st) {
-    OCMP_LAUNCH(k_add_to<T><<<nblk(n, 256), 256, 0, st>>>(n, z, x, nullptr));
+    OCMP_LAUNCH(k_add_to<T><<<nblk(n, 256), 256, 0, st>>>(n, z, x));
     return OCMP_OK;
 }
 template int strip_add<double>(int64_t, const double*, double*, cudaStream_t);
@@ -825,7 +968,3 @@ extern "C" int ocmp_dense_gemm_nt(int32_t kind, int32_t M, int32_t N, int32_t K,
     if (!r && h) r = fail(OCMP_TIMEOUT, "ocmp_dense_gemm_nt: a bounded wait of the tensor-core product gave up");
     return r;
 }
-
-namespace ocmp {
-
-}  // namespace ocmp

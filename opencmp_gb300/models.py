@@ -27,6 +27,7 @@ import torch
 
 from . import _lib as LB
 from . import fem
+from . import forms
 from .config import ConfigParser, Expr, load_sub_config, parse, value_map
 from .mesh import load_mesh
 from .saddle import SaddleSolver
@@ -81,18 +82,20 @@ class Variable:
         dnames = list(self.dirichlet) if self.kind == 'H1' else []
         self.space = fem.Space(model.mesh, self.kind, model.interp_ord, dnames, gmesh=model.gmesh)
         P = dict(model.solver_params)
+        direct_dg = False
         if P['method'] == 'auto':
-            # a direct solve in OpenCMP: CG where the operator is symmetric positive definite
+            # a direct solve in OpenCMP: CG where the operator is symmetric positive definite, else
+            # GMRES; for DG spaces GMRES preconditioned by the strip direct factorisation (the
+            # counterpart of the sparse LU OpenCMP refactorises each step) where the pattern allows
             P['method'] = 'CG' if model.symmetric(self) else 'GMRES'
+            direct_dg = P['method'] == 'GMRES' and self.kind == 'L2'
         if P['method'] == 'CG' and P['precision'] == 'mixed':
             P['precision'] = 'fp64'
         if P['method'] == 'CG' and P['precond'] == 'block_jacobi':
             P['precond'] = 'jacobi'            # CG is built with a diagonal preconditioner
         self.params = P
-        self.mat = fem.Matrix(self.space, jacobi64=P['precision'] == 'fp64', jacobi32=P['precision'] == 'mixed')
-        self.solver = fem.KrylovSolver(self.mat, method=P['method'], restart=P['restart'], precond=P['precond'],
-                                       precision=P['precision'], tol=P['tol'], maxit=P['maxit'],
-                                       inner_tol=P['inner_tol'])
+        self.mat = fem.Matrix(self.space, jacobi64=P['precision'] == 'fp64' and P['precond'] == 'jacobi',
+                              jacobi32=P['precision'] == 'mixed' and P['precond'] == 'jacobi')
         # A direct solve in OpenCMP is accurate to the conditioning of the system; here a Krylov
         # solve that stops short of 1e-12 at the FP64 round-off floor is accepted below 1e-9.
         self.accept = 1e-9 if model.solver_params['tol'] <= 1e-12 else P['tol']
@@ -100,6 +103,23 @@ class Variable:
         n = self.space.ndof
         self.u = torch.zeros(n, dtype=torch.float64, device='cuda')
         self.b = torch.zeros(n, dtype=torch.float64, device='cuda')
+        # the NGSolve-side objects OpenCMP's Model/Solver methods pass around (forms.py)
+        self.gfu = forms.GridFunction(self.space, self.u)
+        self.a = forms.BilinearForm(self.space, self.mat)
+        self.a.var = self
+        self.L = forms.LinearForm(self.space, self.b)
+        if direct_dg:
+            P['precond'] = 'strip'
+            try:
+                self.pre = model.construct_preconditioners([self.a])[0]
+            except LB.OcmpError as e:
+                if e.status not in (LB.ERR_UNSUPPORTED, LB.ERR_NOMEM):
+                    raise
+                P['precond'] = model.solver_params['precond']
+                self.pre = model.construct_preconditioners([self.a])[0]
+        else:
+            self.pre = model.construct_preconditioners([self.a])[0]
+        self.solver = self.pre.solver
         self._qp = None
         self._fq = None
         self._flab = None
@@ -192,7 +212,9 @@ class Variable:
         self.u.copy_(x)
 
     def solve(self, x: Optional[torch.Tensor] = None):
-        return checked_solve(self.solver, self.b, self.u if x is None else x, self.accept)
+        """Model.solve_single_step for this variable's system, into x (default: the solution)."""
+        gfu = self.gfu if x is None or x.data_ptr() == self.u.data_ptr() else forms.GridFunction(self.space, x)
+        return self.model.solve_single_step([self.a], [self.L], [self.pre], gfu)
 
     def source(self, t: float):
         """(constant, quadrature-point tensor) of the source; one of them is None."""
@@ -255,7 +277,8 @@ class Model:
             method = 'GMRES'
         else:
             raise ValueError('No linear solver specified.')
-        precond = {'default': 'jacobi', 'local': 'jacobi', 'None': 'none', 'block_jacobi': 'block_jacobi'}.get(pre)
+        precond = {'default': 'jacobi', 'local': 'jacobi', 'None': 'none', 'block_jacobi': 'block_jacobi',
+                   'direct': 'strip'}.get(pre)
         if precond is None:
             raise NotImplementedError('preconditioner {!r} is not on the GPU path'.format(pre))
         if self.DG and pre == 'default':
@@ -264,6 +287,33 @@ class Model:
         return dict(method=method, precond=precond, tol=max(tol, 1e-12), maxit=max(maxit, 1000),
                     precision='mixed' if prec == 'mixed' else 'fp64',
                     restart=c.get_item(['SOLVER', 'gpu_restart'], int), inner_tol=1e-4)
+
+    # ---------------------------------------------------------------- OpenCMP's solve hooks
+    def construct_preconditioners(self, a_assembled: List[forms.BilinearForm]) -> List[forms.Preconditioner]:
+        """One preconditioner per assembled bilinear form (base_model.py:365-383): the [SOLVER]
+        preconditioner ('local' = point Jacobi, 'direct' = the strip direct factorisation, ...) in
+        the Krylov method, precision and tolerances the form's variable solves with."""
+        out = []
+        for a in a_assembled:
+            P = a.var.params
+            out.append(forms.Preconditioner(a, P['precond'], method=P['method'], precision=P['precision'],
+                                            tol=P['tol'], maxit=P['maxit'], restart=P['restart'],
+                                            inner_tol=P['inner_tol']))
+        return out
+
+    def solve_single_step(self, a_lst: List[forms.BilinearForm], L_lst: List[forms.LinearForm],
+                          precond_lst: List[forms.Preconditioner], gfu: forms.GridFunction, time_step: int = 0):
+        """One linear solve of the step's system (base_model.py:868-884): linear_solve with the
+        forms of this time step."""
+        return self.linear_solve(a_lst[time_step], L_lst[time_step], precond_lst[time_step], gfu)
+
+    def linear_solve(self, a_assembled: forms.BilinearForm, L_assembled: forms.LinearForm,
+                     precond: forms.Preconditioner, gfu: forms.GridFunction):
+        """Solve A x = L on the free dofs (base_model.py:886-947): gfu.vec holds the Dirichlet values
+        and the initial guess and receives the solution. Returns the solve's info (OpenCMP returns
+        nothing; the info carries iterations and the FP64 relative residual)."""
+        accept = getattr(getattr(a_assembled, 'var', None), 'accept', precond.solver.params.tol)
+        return checked_solve(precond.solver, L_assembled.vec, gfu.vec, accept)
 
     def symmetric(self, var: Variable) -> bool:
         """Whether the variable's operator is symmetric (no convection)."""

@@ -46,12 +46,17 @@ class Solver:
         self.t = 0.0
         self.infos = []
         # new [SOLVER] key: the Krylov start of each transient step, 'previous' (OpenCMP's: the last
-        # solution) or 'extrapolated' (cubic extrapolation in time of the last solutions, the
-        # fallback of the learned guess; used for fixed-step schemes, restarted when dt changes)
+        # solution), 'extrapolated' (cubic extrapolation in time of the last solutions, the
+        # fallback of the learned guess) or 'learned' (that extrapolation plus the correction of a
+        # network trained on the run's own first `learned_train_steps` steps once the history is
+        # full, kept only while its convergence judge sees it save Krylov iterations); the last two
+        # for fixed-step schemes, restarted when dt changes
         self.guess_mode = config.get_item(['SOLVER', 'initial_guess'], str).strip().lower()
-        if self.guess_mode not in ('previous', 'extrapolated'):
-            raise NotImplementedError('initial_guess {!r} is not on the GPU path (previous or extrapolated)'.format(
-                self.guess_mode))
+        if self.guess_mode not in ('previous', 'extrapolated', 'learned'):
+            raise NotImplementedError('initial_guess {!r} is not on the GPU path (previous, extrapolated or '
+                                      'learned)'.format(self.guess_mode))
+        self.learn_steps = config.get_item(['SOLVER', 'learned_train_steps'], int)
+        self.learn_iters = config.get_item(['SOLVER', 'learned_train_iters'], int)
 
     def _solve_var(self, v, theta: float, dt: float, t_new: float, t_old: float, transient: bool,
                    u_from=None, u_to=None):
@@ -62,14 +67,23 @@ class Solver:
         if uprev is not None and u_to.data_ptr() != uprev.data_ptr():
             u_to.copy_(uprev)
         g = self._guess(v, dt, uprev) if transient else None
+        used = None
         if g is not None:
-            g.extrapolate(u_to)
+            if self.guess_mode == 'learned':
+                used = g.predict(u_to)
+            else:
+                g.extrapolate(u_to)
         v.set_dirichlet(t_new, u_to)
         mass = 1.0 if transient else 0.0
-        v.mat.assemble(m.form(v, mass, theta * dt, dt))
-        v.solver.update()
+        # _assemble (base_solver.py:368-377): the bilinear and linear forms of this step, then the
+        # preconditioner update
+        form = m.form(v, mass, theta * dt, dt)
         r, keep = m.rhs(v, t_new, theta * dt, mass=mass, uprev=uprev)
-        fem.assemble_rhs(v.space, m.form(v, mass, theta * dt, dt), r, v.b)
+        v.a.form = form
+        v.L._assemble = lambda vec: fem.assemble_rhs(v.space, form, r, vec)
+        v.a.Assemble()
+        v.L.Assemble()
+        v.pre.Update()
         if transient and theta < 1.0:
             # (1 - theta) [L(t^n) - dt K_ode u^n]
             r0, keep0 = m.rhs(v, t_old, (1.0 - theta) * dt, accumulate=True)
@@ -83,19 +97,38 @@ class Solver:
         info = v.solve(u_to)
         del keep
         if g is not None:
+            if self.guess_mode == 'learned':
+                self._learn(v, g, u_to, info, used)
             g.push(u_to)
         self.infos.append(info)
         return info
 
+    def _learn(self, v, g, u_new, info, used):
+        """Learned guess: collect the run's first steps as training samples (each keeps a copy of
+        its step's matrix for the residual loss), train once they are in, then let the judge
+        decide after every step whether the network's guess still saves iterations."""
+        if not g.trained:
+            if g.ready and len(g.samples) < self.learn_steps:
+                A = fem.Matrix(v.space)
+                A.device_values()[0].copy_(v.mat.device_values()[0])
+                g.collect(u_new, A, v.b)
+            if len(g.samples) >= self.learn_steps:
+                g.train(steps=self.learn_iters, lr=3e-3)
+                g.drop_samples()
+                g.reset_judge()
+            return
+        g.judge(info, used)
+
     def _guess(self, v, dt, uprev):
         """The variable's extrapolation history (None for the previous-step guess); restarted from
         u^n when the step size changes, since the extrapolation assumes equal steps."""
-        if self.guess_mode != 'extrapolated' or not getattr(self, 'fixed_step', False):
+        if self.guess_mode == 'previous' or not getattr(self, 'fixed_step', False):
             return None
         from .guess import LearnedGuess
         g = getattr(v, 'guess', None)
         if g is None:
-            g = v.guess = LearnedGuess(v.space, k=4, base_order=3)
+            # the learned guess reads 4 backward differences (5 solutions); the plain extrapolation 3
+            g = v.guess = LearnedGuess(v.space, k=5 if self.guess_mode == 'learned' else 4, base_order=3)
         if getattr(v, 'guess_dt', None) != dt or g.m == 0:
             g.reset()
             g.push(uprev)

@@ -329,3 +329,86 @@ def test_extrapolated_initial_guess_through_run(gpu_lib):
     assert res['extrapolated'][2] <= 1e-9 and res['previous'][2] <= 1e-9
     for k, u in res['previous'][1].items():
         assert np.linalg.norm(res['extrapolated'][1][k] - u) <= 1e-8 * np.linalg.norm(u) + 1e-14
+
+
+@pytest.mark.gpu
+def test_learned_initial_guess_through_run(gpu_lib):
+    """[SOLVER] initial_guess = learned on the same transient reference fixture: the network is
+    trained on the run's own first steps (once the history holds five solutions), then starts the
+    later solves under its convergence judge. Every step still meets the solver tolerance and the
+    solution is the one from OpenCMP's previous-step start to 1e-8 (the run that meets the
+    fixture's error bound in test_reference_test_through_run)."""
+    from opencmp_gb300.run import run
+    case = next(c.values[0] for c in CASES if not c.marks and c.values[0]['fixture'] == 'poisson_transient_coarse'
+                and _scheme(c.values[0]) == 'implicit euler')
+    res = {}
+    for mode in ('previous', 'learned'):
+        cfg = _load(case)
+        if not cfg.has_section('SOLVER'):
+            cfg.add_section('SOLVER')
+        cfg['SOLVER']['initial_guess'] = mode
+        cfg['SOLVER']['learned_train_steps'] = '12'
+        cfg['SOLVER']['learned_train_iters'] = '60'
+        solver, sol = run('', cfg)
+        res[mode] = (solver, {k: v.u.cpu().numpy() for k, v in sol.items()}, sol)
+    solver, u_l, sol = res['learned']
+    assert max(i.relres for i in solver.infos) <= 1e-9
+    guesses = [getattr(v, 'guess', None) for v in sol.values()]
+    assert guesses and all(g is not None and g.trained for g in guesses)
+    # after training the judge ran: the network either still starts solves or was switched off
+    # with its reason recorded
+    assert all(g.enabled or g.fallback_reason for g in guesses)
+    for k, u in res['previous'][1].items():
+        assert np.linalg.norm(u_l[k] - u) <= 1e-8 * np.linalg.norm(u) + 1e-14
+
+
+@pytest.mark.gpu
+def test_model_subclass_through_opencmp_hooks(gpu_lib):
+    """A Model subclass written against OpenCMP's method API (construct_preconditioners,
+    solve_single_step, linear_solve: opencmp/models/base_model.py:365-383, 868-947), registered in
+    models_dict and run through run(): the hooks receive the NGSolve stand-ins (device GridFunction,
+    BilinearForm, LinearForm, Preconditioner), a user-side residual check on those handles holds,
+    and the solution is bit for bit the built-in model's."""
+    import torch
+    from opencmp_gb300 import forms, models
+    from opencmp_gb300.run import run
+    case = next(c.values[0] for c in CASES if not c.marks and c.values[0]['fixture'] == 'poisson_transient_coarse'
+                and _scheme(c.values[0]) == 'implicit euler')
+    calls = {'pre': 0, 'single': 0, 'solve': 0}
+
+    class HookedPoisson(models.Poisson):
+        def construct_preconditioners(self, a_assembled):
+            calls['pre'] += 1
+            assert all(isinstance(a, forms.BilinearForm) for a in a_assembled)
+            return super().construct_preconditioners(a_assembled)
+
+        def solve_single_step(self, a_lst, L_lst, precond_lst, gfu, time_step=0):
+            calls['single'] += 1
+            return super().solve_single_step(a_lst, L_lst, precond_lst, gfu, time_step)
+
+        def linear_solve(self, a_assembled, L_assembled, precond, gfu):
+            calls['solve'] += 1
+            assert isinstance(precond, forms.Preconditioner) and isinstance(L_assembled, forms.LinearForm)
+            assert gfu.vec.is_cuda and gfu.space.ndof == gfu.vec.numel()
+            info = super().linear_solve(a_assembled, L_assembled, precond, gfu)
+            # the user's own check on the handles: ||(L - A gfu)_free|| against ||L_free||
+            y = torch.empty_like(gfu.vec)
+            a_assembled.mat.mult(gfu.vec, y)
+            free = torch.as_tensor(gfu.space.FreeDofs(), device='cuda')
+            r = torch.linalg.vector_norm((L_assembled.vec - y)[free]).item()
+            assert r <= 1e-6 * max(torch.linalg.vector_norm(L_assembled.vec[free]).item(), 1e-300)
+            return info
+
+    models.models_dict['HookedPoisson'] = HookedPoisson
+    try:
+        sols = {}
+        for name in ('Poisson', 'HookedPoisson'):
+            cfg = _load(case)
+            cfg['OTHER']['model'] = name
+            solver, sol = run('', cfg)
+            sols[name] = ({k: v.u.cpu().numpy() for k, v in sol.items()}, len(solver.infos))
+    finally:
+        del models.models_dict['HookedPoisson']
+    assert calls['pre'] == 1 and calls['single'] == calls['solve'] == sols['HookedPoisson'][1] > 0
+    for k, u in sols['Poisson'][0].items():
+        assert np.array_equal(u, sols['HookedPoisson'][0][k])
