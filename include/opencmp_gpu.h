@@ -250,6 +250,8 @@ typedef struct {
     double gemm_flops;       /* flops of those products                                             */
     int32_t singular_tiles;  /* pivot tiles that met a zero or non-finite pivot                     */
     int32_t gemm_kind;       /* 0: FP32 SIMT products, 1: tensor-core (tcgen05, 3xTF32) products    */
+    double tile_ms;          /* time in the pivot-tile inversions (with ocmp_solver_strip_timing)   */
+    double panel_ms;         /* time in the panel kernels (with ocmp_solver_strip_timing)           */
 } ocmp_strip_stats_t;
 int ocmp_solver_strip_stats(ocmp_solver_t solver, ocmp_strip_stats_t* out);
 /* time every dense product of the next factorisations with CUDA events (measurement) */

@@ -73,7 +73,7 @@ class SolveInfo(C.Structure):
 class StripStats(C.Structure):
     _fields_ = [('nstrips', C.c_int64), ('max_strip', C.c_int64), ('bytes', C.c_int64), ('factor_ms', C.c_double),
                 ('gemm_ms', C.c_double), ('gemm_flops', C.c_double), ('singular_tiles', C.c_int32),
-                ('gemm_kind', C.c_int32)]
+                ('gemm_kind', C.c_int32), ('tile_ms', C.c_double), ('panel_ms', C.c_double)]
 
 
 P = C.c_void_p

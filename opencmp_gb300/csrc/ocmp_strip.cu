@@ -93,6 +93,8 @@ struct Strip {
     bool timing = false;
     std::vector<cudaEvent_t> ev;
     size_t ev_used = 0;
+    std::vector<int> ev_tag;            // per event pair: 0 product, 1 tile inversion, 2 panels
+    double part_ms[3] = {0, 0, 0};
     cudaEvent_t fev[2] = {nullptr, nullptr};
     double factor_ms = 0, gemm_ms = 0, gemm_flops = 0, gemm_flops_pending = 0;
     int singular = 0;
@@ -260,36 +262,44 @@ __global__ void k_sub_block(int nI, int nIp, int nNp, const float* __restrict__ 
 
 // ------------------------------------------------------------------ block Gauss-Jordan
 // P <- inverse of the tile S[t0:t0+128, t0:t0+128] by Gauss-Jordan with partial pivoting inside
-// the tile, one barrier per pivot: every warp finds the pivot itself, and each step reads one
-// shared-memory copy of the tile and writes the other. A zero or non-finite pivot is counted in
-// *flag and replaced by a tiny value.
+// the tile. The tile stays in registers (thread t holds column t % 128 of rows t / 128 + 8 j) and
+// rows are never moved: step k takes as pivot the largest |a_rk| over the rows not yet used, and
+// the row and column permutation is applied when the result is written (P[step(r)][piv(c)] =
+// M[r][c]). Per step the owners of column k publish it and the owners of the pivot row publish
+// that row (double-buffered in shared memory), two barriers per step. A zero or non-finite pivot
+// is counted in *flag and replaced by a tiny value.
 constexpr int kTileThreads = 1024;
-constexpr int kTileLD = kNb + 1;
-constexpr int kTileSmem = 2 * kNb * kTileLD * (int)sizeof(float);
+constexpr int kTileSmem = 0;
 __global__ void __launch_bounds__(kTileThreads) k_tile_inv(const float* __restrict__ S, int mp, int t0,
                                                            float* __restrict__ P, int* __restrict__ flag) {
-    extern __shared__ float sm[];
+    __shared__ float colk[2][kNb];
+    __shared__ float prow[2][kNb];
+    __shared__ int used[kNb];
     __shared__ int piv[kNb];
-    __shared__ int cperm[kNb];
-    const int tid = threadIdx.x, lane = tid & 31;
-    float* buf0 = sm;
-    float* buf1 = sm + kNb * kTileLD;
-    for (int e = tid; e < kNb * kNb; e += kTileThreads) {
-        const int r = e / kNb, c = e % kNb;
-        buf0[r * kTileLD + c] = S[(int64_t)(t0 + r) * mp + t0 + c];
-    }
+    __shared__ int step[kNb];
+    const int tid = threadIdx.x, c = tid & (kNb - 1), r0 = tid >> 7, lane = tid & 31;
+    constexpr int R = kNb / 8;   // rows per thread
+    float v[R];
+#pragma unroll
+    for (int j = 0; j < R; j++) v[j] = S[(int64_t)(t0 + r0 + 8 * j) * mp + t0 + c];
+    if (tid < kNb) used[tid] = 0;
     __syncthreads();
-    const int c = tid & (kNb - 1), r0 = tid >> 7;  // column c, rows r0 + 8 j
-    int cur = 0;
     for (int k = 0; k < kNb; k++) {
-        const float* a = cur ? buf1 : buf0;
-        float* o = cur ? buf0 : buf1;
+        const int b = k & 1;
+        if (c == k) {
+#pragma unroll
+            for (int j = 0; j < R; j++) colk[b][r0 + 8 * j] = v[j];
+        }
+        __syncthreads();
+        // every warp finds the pivot itself: the largest |a_rk| over the unused rows (lowest r on ties)
         float best = -1.f;
         int bi = kNb;
-        for (int i = k + lane; i < kNb; i += 32) {
-            const float v = fabsf(a[i * kTileLD + k]);
-            if (v > best) {
-                best = v;
+#pragma unroll
+        for (int q = 0; q < kNb / 32; q++) {
+            const int i = lane + 32 * q;
+            const float a = used[i] ? -1.f : fabsf(colk[b][i]);
+            if (a > best) {
+                best = a;
                 bi = i;
             }
         }
@@ -302,44 +312,46 @@ __global__ void __launch_bounds__(kTileThreads) k_tile_inv(const float* __restri
                 bi = oi;
             }
         }
-        const int p = bi < kNb ? bi : k;
-        if (tid == 0) piv[k] = p;
-        float pv = a[p * kTileLD + k];
+        int p = bi;
+        if (p >= kNb) {   // every remaining |a_rk| is NaN: take the first unused row
+            p = 0;
+            while (p < kNb - 1 && used[p]) p++;
+        }
+        float pv = colk[b][p];
         if (!(fabsf(pv) > 0.f) || !isfinite(pv)) {
             if (tid == 0) atomicAdd(flag, 1);
             pv = 1e-30f;
         }
         const float d = 1.f / pv;
-        const float nk = (c == k ? 1.f : a[p * kTileLD + c]) * d;   // the new pivot row at column c
-#pragma unroll 4
-        for (int j = 0; j < kNb / 8; j++) {
-            const int r = r0 + 8 * j;
-            float v;
-            if (r == k) {
-                v = nk;
-            } else {
-                const int rs = r == p ? k : r;   // rows k and p trade places
-                const float f = a[rs * kTileLD + k];
-                const float prev = c == k ? 0.f : a[rs * kTileLD + c];
-                v = prev - f * nk;
-            }
-            o[r * kTileLD + c] = v;
+        if (r0 == (p & 7)) {
+            // v[p >> 3] without dynamic register indexing
+            float x = 0.f;
+#pragma unroll
+            for (int j = 0; j < R; j++)
+                if (j == (p >> 3)) x = v[j];
+            prow[b][c] = (c == k ? 1.f : x) * d;
         }
         __syncthreads();
-        cur ^= 1;
-    }
-    // the row interchanges come back as column interchanges in reverse order
-    if (tid == 0) {
-        for (int i = 0; i < kNb; i++) cperm[i] = i;
-        for (int k = kNb - 1; k >= 0; k--) {
-            const int t = cperm[k];
-            cperm[k] = cperm[piv[k]];
-            cperm[piv[k]] = t;
+        if (tid == 0) {
+            used[p] = 1;
+            piv[k] = p;
+            step[p] = k;
+        }
+        const float pr = prow[b][c];
+#pragma unroll
+        for (int j = 0; j < R; j++) {
+            const int r = r0 + 8 * j;
+            if (r == p) v[j] = pr;
+            else v[j] = (c == k ? 0.f : v[j]) - colk[b][r] * pr;
         }
     }
     __syncthreads();
-    const float* a = cur ? buf1 : buf0;
-    for (int e = tid; e < kNb * kNb; e += kTileThreads) P[e] = a[(e / kNb) * kTileLD + cperm[e % kNb]];
+    const int pc = piv[c];
+#pragma unroll
+    for (int j = 0; j < R; j++) {
+        const int r = r0 + 8 * j;
+        P[step[r] * kNb + pc] = v[j];
+    }
 }
 
 // For the 32 columns c0..c0+31: Rt[c, r] = sum_l P[r, l] S[t0 + l, c] (the pivot rows times P, stored
@@ -526,19 +538,32 @@ void strip_free(Strip* p) {
     if (p->cap) cudaStreamDestroy(p->cap);
 }
 
+// timing of the factorisation's kernels by class (ocmp_solver_strip_timing): an event pair around
+// each launch on its stream
+int tbegin(Strip* p, cudaStream_t st) {
+    if (!p->timing) return OCMP_OK;
+    while (p->ev.size() < p->ev_used + 2) {
+        cudaEvent_t e;
+        OCMP_CUDA(cudaEventCreate(&e));
+        p->ev.push_back(e);
+    }
+    OCMP_CUDA(cudaEventRecord(p->ev[p->ev_used], st));
+    return OCMP_OK;
+}
+int tend(Strip* p, cudaStream_t st, int tag) {
+    if (!p->timing) return OCMP_OK;
+    OCMP_CUDA(cudaEventRecord(p->ev[p->ev_used + 1], st));
+    p->ev_used += 2;
+    p->ev_tag.push_back(tag);
+    return OCMP_OK;
+}
+
 int gemm(Strip* p, int M, int N, int K, const float* A, int64_t lda, const float* B, int64_t ldb, float* C, int64_t ldc,
          float alpha, float beta, cudaStream_t st) {
     if (M % GB || N % GB || K % 32 || M <= 0 || N <= 0 || K <= 0)
         return fail(OCMP_ERR_ARG, "strip gemm: sizes must be multiples of the tile");
     const bool t = p->timing;
-    if (t) {
-        while (p->ev.size() < p->ev_used + 2) {
-            cudaEvent_t e;
-            OCMP_CUDA(cudaEventCreate(&e));
-            p->ev.push_back(e);
-        }
-        OCMP_CUDA(cudaEventRecord(p->ev[p->ev_used], st));
-    }
+    if (t && tbegin(p, st)) return OCMP_ERR_CUDA;
     if (p->gemm_kind == 1) {
         const int r = tc_gemm_nt(M, N, K, A, lda, B, ldb, C, ldc, alpha, beta, p->d_flag + 1, st);
         if (r) return r;
@@ -546,10 +571,7 @@ int gemm(Strip* p, int M, int N, int K, const float* A, int64_t lda, const float
         const dim3 g(N / GB, M / GB);
         OCMP_LAUNCH(sgemm_nt<<<g, 256, 0, st>>>(M, N, K, A, lda, B, ldb, C, ldc, alpha, beta));
     }
-    if (t) {
-        OCMP_CUDA(cudaEventRecord(p->ev[p->ev_used + 1], st));
-        p->ev_used += 2;
-    }
+    if (t && tend(p, st, 0)) return OCMP_ERR_CUDA;
     p->gemm_flops_pending += 2.0 * M * N * (double)K;
     return OCMP_OK;
 }
@@ -557,11 +579,17 @@ int gemm(Strip* p, int M, int N, int K, const float* A, int64_t lda, const float
 // Gauss-Jordan over the pivot tiles [t_begin, t_end) of S (mp x mp) on stream st with workspace w
 int gj_tiles(Strip* p, float* S, int mp, int t_begin, int t_end, const StripWork& w, cudaStream_t st) {
     for (int t0 = t_begin; t0 < t_end; t0 += kNb) {
+        int r = tbegin(p, st);
         OCMP_LAUNCH(k_tile_inv<<<1, kTileThreads, kTileSmem, st>>>(S, mp, t0, w.P, p->d_flag));
+        if (!r) r = tend(p, st, 1);
+        if (!r) r = tbegin(p, st);
         OCMP_LAUNCH(k_panel_prep<<<mp / 32, 256, kPrepSmem, st>>>(S, mp, t0, w.P, w.Rt, w.Ck));
-        const int r = gemm(p, mp, mp, kNb, w.Ck, kNb, w.Rt, kNb, S, mp, -1.f, 1.f, st);
-        if (r) return r;
+        if (!r) r = tend(p, st, 2);
+        if (!r) r = gemm(p, mp, mp, kNb, w.Ck, kNb, w.Rt, kNb, S, mp, -1.f, 1.f, st);
+        if (!r) r = tbegin(p, st);
         OCMP_LAUNCH(k_panel_finish<<<mp / 32, 256, kFinishSmem, st>>>(S, mp, t0, w.P, w.Rt, w.Ck));
+        if (!r) r = tend(p, st, 2);
+        if (r) return r;
     }
     return OCMP_OK;
 }
@@ -785,6 +813,7 @@ void strip_destroy(Strip* p) {
 int strip_factor(Strip* p, const ocmp_space_s* s, const double* vals, cudaStream_t st) {
     const int K = p->K;
     p->ev_used = 0;
+    p->ev_tag.clear();
     p->gemm_flops_pending = 0;
     OCMP_CUDA(cudaEventRecord(p->fev[0], st));
     OCMP_CUDA(cudaMemsetAsync(p->d_flag, 0, 2 * sizeof(int), st));
@@ -840,11 +869,13 @@ int strip_factor(Strip* p, const ocmp_space_s* s, const double* vals, cudaStream
     if (flags[1]) return fail(OCMP_TIMEOUT, "strip preconditioner: a tensor-core product gave up a bounded wait");
     p->gemm_flops = p->gemm_flops_pending;
     p->gemm_ms = 0;
+    for (double& x : p->part_ms) x = 0;
     for (size_t q = 0; q + 1 < p->ev_used; q += 2) {
         float e = 0;
         OCMP_CUDA(cudaEventElapsedTime(&e, p->ev[q], p->ev[q + 1]));
-        p->gemm_ms += e;
+        p->part_ms[p->ev_tag[q / 2]] += e;
     }
+    p->gemm_ms = p->part_ms[0];
     if (flags[0]) return fail(OCMP_BREAKDOWN, "strip preconditioner: " + std::to_string(flags[0]) +
                                                   " zero or non-finite pivots in the strip factorisation");
     return OCMP_OK;
@@ -932,6 +963,8 @@ void strip_stats(const Strip* p, ocmp_strip_stats_t* o) {
     o->gemm_flops = p->gemm_flops;
     o->singular_tiles = p->singular;
     o->gemm_kind = p->gemm_kind;
+    o->tile_ms = p->part_ms[1];
+    o->panel_ms = p->part_ms[2];
 }
 
 void strip_set_timing(Strip* p, bool on) { p->timing = on; }

@@ -11,7 +11,8 @@
 //              3-stage shared-memory ring (cp.async.bulk.tensor, mbarrier completion);
 //   warps 2-5  split the staged boxes into their low parts (x - trunc_tf32(x), same swizzled layout,
 //              elementwise), then run the epilogue: tcgen05.ld of the accumulator (each warp its 32
-//              TMEM lanes = rows), C read, scaled, written;
+//              TMEM lanes = rows) into a staging tile in the idle stage buffers, then C read, scaled
+//              and written row by row (512 contiguous bytes per row and warp instruction);
 //   warp 1     allocates 128 TMEM columns, and one thread issues the tcgen05.mma.kind::tf32
 //              instructions (M = 128, N = 128, K = 8) and the tcgen05.commit arrivals that free the
 //              stages and signal the epilogue.
@@ -225,9 +226,12 @@ __global__ void __launch_bounds__(kTcThreads, 1)
         }
         if (ok && mbar_wait(accum_b, 0, abort)) {
             asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-            const int q = warp & 3;                 // TMEM lanes 32q..32q+31 = rows of the tile
-            const int64_t row = (int64_t)m0 + 32 * q + lane;
-            float* crow = C + row * ldc + n0;
+            // TMEM lanes 32q..32q+31 are the tile's rows; each thread takes its row's 128 columns
+            // into a staging tile in the (now idle) stage buffers, then the warp writes C row by
+            // row, 512 contiguous bytes per row
+            const int q = warp & 3;
+            constexpr int SLD = TBN + 4;            // 16-byte aligned rows, conflict-free float4 writes
+            float* stg = reinterpret_cast<float*>(gbase) + q * (32 * SLD);
 #pragma unroll 1
             for (int c0 = 0; c0 < TBN; c0 += 32) {
                 uint32_t r[32];
@@ -245,15 +249,22 @@ __global__ void __launch_bounds__(kTcThreads, 1)
                     : "memory");
                 asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 #pragma unroll
-                for (int v = 0; v < 32; v += 4) {
-                    float4* p = reinterpret_cast<float4*>(crow + c0 + v);
-                    float4 o = beta != 0.f ? *p : make_float4(0.f, 0.f, 0.f, 0.f);
-                    o.x = alpha * __uint_as_float(r[v + 0]) + beta * o.x;
-                    o.y = alpha * __uint_as_float(r[v + 1]) + beta * o.y;
-                    o.z = alpha * __uint_as_float(r[v + 2]) + beta * o.z;
-                    o.w = alpha * __uint_as_float(r[v + 3]) + beta * o.w;
-                    *p = o;
-                }
+                for (int v = 0; v < 32; v += 4)
+                    *reinterpret_cast<float4*>(stg + lane * SLD + c0 + v) =
+                        make_float4(__uint_as_float(r[v]), __uint_as_float(r[v + 1]), __uint_as_float(r[v + 2]),
+                                    __uint_as_float(r[v + 3]));
+            }
+            __syncwarp();
+#pragma unroll 4
+            for (int rr = 0; rr < 32; rr++) {
+                const float4 a = *reinterpret_cast<const float4*>(stg + rr * SLD + 4 * lane);
+                float4* p = reinterpret_cast<float4*>(C + ((int64_t)m0 + 32 * q + rr) * ldc + n0) + lane;
+                float4 o = beta != 0.f ? *p : make_float4(0.f, 0.f, 0.f, 0.f);
+                o.x = alpha * a.x + beta * o.x;
+                o.y = alpha * a.y + beta * o.y;
+                o.z = alpha * a.z + beta * o.z;
+                o.w = alpha * a.w + beta * o.w;
+                *p = o;
             }
         } else if (ok) {
             give_up();
