@@ -178,7 +178,12 @@ int ocmp_l2_error(ocmp_space_t space, const double* u_dev, const double* fq_dev,
  * OCMP_MAT_DFLOAT assembles the element matrices and their sums in double-float arithmetic (pairs of
  * FP32 values, about 48 significant bits) on the FP32 pipes, finishing each CSR entry with one FP64
  * addition; the FP64 values agree with the native FP64 assembly to about 1e-14 relative. */
-enum { OCMP_MAT_FP32 = 1, OCMP_MAT_JACOBI64 = 2, OCMP_MAT_JACOBI32 = 4, OCMP_MAT_DFLOAT = 8 };
+enum { OCMP_MAT_FP32 = 1, OCMP_MAT_JACOBI64 = 2, OCMP_MAT_JACOBI32 = 4, OCMP_MAT_DFLOAT = 8, OCMP_MAT_SELL32 = 16 };
+/* OCMP_MAT_SELL32 (with OCMP_MAT_JACOBI32, single matrices): the FP32 Jacobi-scaled values are
+ * written in the space's SELL-32 order instead of CSR order (slices of 32 rows, each row padded to
+ * its slice's width in 4-entry chunks, chunk-major within a slice, zero padding), the layout the
+ * FP32 GMRES SpMV reads with 16-byte loads, a warp per slice; ocmp_matrix_scaled_values then
+ * returns them in that order. */
 int ocmp_matrix_create(ocmp_space_t space, int32_t flags, ocmp_matrix_t* out);
 /* nbatch independent matrices on the space's pattern (instances of a batch of problems that differ
  * only in their coefficients); values are stored instance after instance. */

@@ -444,7 +444,7 @@ __global__ void __launch_bounds__(128) row_scatter_kernel(
     const int32_t* __restrict__ efac, const uint8_t* __restrict__ fslot, const int32_t* __restrict__ ebf_ptr,
     const int32_t* __restrict__ ebf, const double* __restrict__ Ki, const double* __restrict__ Kb,
     const double* __restrict__ dinv, double* __restrict__ vals, float* __restrict__ vals32,
-    double* __restrict__ svals64, float* __restrict__ svals32) {
+    double* __restrict__ svals64, float* __restrict__ svals32, const int32_t* __restrict__ spos) {
     extern __shared__ double acc[];
     const int NTP = blockDim.x + 1, tid = threadIdx.x;
     const int64_t r = r0 + blockIdx.x * (int64_t)blockDim.x + tid;
@@ -486,7 +486,7 @@ __global__ void __launch_bounds__(128) row_scatter_kernel(
         if (svals64 || svals32) {
             const double sv = v * dinv[col[base + q]];
             if (svals64) svals64[base + q] = sv;
-            if (svals32) svals32[base + q] = (float)sv;
+            if (svals32) svals32[spos ? spos[base + q] : base + q] = (float)sv;
         }
     }
 }
@@ -770,7 +770,8 @@ __global__ void __launch_bounds__(128) row_scatter_ff_kernel(
     const int32_t* __restrict__ efac, const uint8_t* __restrict__ fslot, const int32_t* __restrict__ ebf_ptr,
     const int32_t* __restrict__ ebf, const double* __restrict__ Ki, const double* __restrict__ Kb,
     const double* __restrict__ dinv, const float* __restrict__ dinv32, double* __restrict__ vals,
-    float* __restrict__ vals32, double* __restrict__ svals64, float* __restrict__ svals32) {
+    float* __restrict__ vals32, double* __restrict__ svals64, float* __restrict__ svals32,
+    const int32_t* __restrict__ spos) {
     extern __shared__ float2 acc2[];
     const int NTP = blockDim.x + 1, tid = threadIdx.x;
     const int64_t r = r0 + blockIdx.x * (int64_t)blockDim.x + tid;
@@ -839,7 +840,7 @@ __global__ void __launch_bounds__(128) row_scatter_ff_kernel(
         const float v32 = __fadd_rn(a2.x, a2.y);
         if (vals32) vals32[base + q] = v32;
         if (svals64) svals64[base + q] = v * dinv[col[base + q]];
-        if (svals32) svals32[base + q] = v32 * dinv32[col[base + q]];
+        if (svals32) svals32[spos ? spos[base + q] : base + q] = v32 * dinv32[col[base + q]];
     }
 }
 
@@ -887,7 +888,7 @@ __global__ void __launch_bounds__(256) csr_gather_kernel(int64_t nnz, const int3
                                                          const double* __restrict__ dinv,
                                                          const float* __restrict__ dinv32, double* __restrict__ vals,
                                                          float* __restrict__ vals32, double* __restrict__ svals64,
-                                                         float* __restrict__ svals32) {
+                                                         float* __restrict__ svals32, const int32_t* __restrict__ spos) {
     const int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (k >= nnz) return;
     const int32_t s0 = __ldg(seg + k), s1 = __ldg(seg + k + 1);
@@ -913,7 +914,7 @@ __global__ void __launch_bounds__(256) csr_gather_kernel(int64_t nnz, const int3
         const float v32 = __fadd_rn(h, l);
         if (vals32) vals32[k] = v32;
         if (svals64) svals64[k] = vv * dinv[ck];
-        if (svals32) svals32[k] = v32 * dinv32[ck];
+        if (svals32) svals32[spos ? __ldg(spos + k) : k] = v32 * dinv32[ck];
     } else {
         const double* __restrict__ K = reinterpret_cast<const double*>(Kv);
         double acc = 0.0;
@@ -933,7 +934,7 @@ __global__ void __launch_bounds__(256) csr_gather_kernel(int64_t nnz, const int3
         if (svals64 || svals32) {
             const double sv = acc * dinv[ck];
             if (svals64) svals64[k] = sv;
-            if (svals32) svals32[k] = (float)sv;
+            if (svals32) svals32[spos ? __ldg(spos + k) : k] = (float)sv;
         }
     }
 }
@@ -1287,6 +1288,8 @@ int assemble_impl(ocmp_matrix_s* m, const ocmp_form_t* f, cudaStream_t st) {
     else if (m->dinv)
         OCMP_LAUNCH(diag_kernel<L><<<nblk(nd, 256), 256, 0, st>>>(nd, s->d_inc_ptr, s->d_inc, s->d_K, s->d_free, use_facets, efp,
                                                       s->d_efac, s->d_ebf_ptr, s->d_ebf, Ki, Kb, m->dinv));
+    // the FP32 Jacobi-scaled values in the SELL-32 order (OCMP_MAT_SELL32)
+    const int32_t* spos = (m->flags & OCMP_MAT_SELL32) ? s->d_sell_pos : nullptr;
     if (!use_facets) {
         // element-only assembly: sorted segmented reduction, one thread per CSR entry
         if (!s->d_cseg) {
@@ -1308,11 +1311,11 @@ int assemble_impl(ocmp_matrix_s* m, const ocmp_form_t* f, cudaStream_t st) {
         if (dfl)
             OCMP_LAUNCH(csr_gather_kernel<true><<<nblk(s->nnz, 256), 256, 0, st>>>(s->nnz, s->d_cseg, s->d_csrc, Kc, s->d_col,
                                                                               m->dinv, m->dinv32, m->vals, m->vals32,
-                                                                              m->svals64, m->svals32));
+                                                                              m->svals64, m->svals32, spos));
         else
             OCMP_LAUNCH(csr_gather_kernel<false><<<nblk(s->nnz, 256), 256, 0, st>>>(s->nnz, s->d_cseg, s->d_csrc, Kc, s->d_col,
                                                                                m->dinv, m->dinv32, m->vals, m->vals32,
-                                                                               m->svals64, m->svals32));
+                                                                               m->svals64, m->svals32, spos));
         OCMP_CUDA(cudaGetLastError());
         return OCMP_OK;
     }
@@ -1330,12 +1333,12 @@ int assemble_impl(ocmp_matrix_s* m, const ocmp_form_t* f, cudaStream_t st) {
             OCMP_LAUNCH(row_scatter_ff_kernel<L><<<nblk(r1 - r0, rt), rt, rsm, st>>>(
                 r0, r1, s->d_rowptr, s->d_col, s->d_inc_ptr, s->d_inc, Kff, s->d_slot, s->slot_stride, use_facets,
                 efp, s->d_efac, s->d_fslot, s->d_ebf_ptr, s->d_ebf, Ki, Kb, m->dinv, m->dinv32, m->vals, m->vals32,
-                m->svals64, m->svals32));
+                m->svals64, m->svals32, spos));
         else
             OCMP_LAUNCH(row_scatter_kernel<L><<<nblk(r1 - r0, rt), rt, rsm, st>>>(
                 r0, r1, s->d_rowptr, s->d_col, s->d_inc_ptr, s->d_inc, s->d_K, s->d_slot, s->slot_stride, use_facets,
                 efp, s->d_efac, s->d_fslot, s->d_ebf_ptr, s->d_ebf, Ki, Kb, m->dinv, m->vals, m->vals32, m->svals64,
-                m->svals32));
+                m->svals32, spos));
     }
     OCMP_CUDA(cudaGetLastError());
     return OCMP_OK;

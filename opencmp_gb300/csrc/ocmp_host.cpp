@@ -443,6 +443,56 @@ static void build_tables(int kind, int D, int p, ocmp_tables& T) {
 
 using namespace ocmp;
 
+namespace ocmp {
+// SELL-32 layout of the space's pattern (see ocmp_space_s), built once on the host
+int space_build_sell(ocmp_space_s* s) {
+    if (s->d_sell_off) return OCMP_OK;
+    const int64_t n = s->ndof, ns = (n + 31) / 32;
+    std::vector<int32_t> off(ns + 1), pos(s->nnz);
+    int64_t tot = 0;
+    for (int64_t sl = 0; sl < ns; sl++) {
+        int64_t w = 0;
+        for (int64_t r = sl * 32; r < std::min(n, sl * 32 + 32); r++)
+            w = std::max<int64_t>(w, (s->rowptr[r + 1] - s->rowptr[r] + 3) / 4);
+        off[sl] = (int32_t)tot;
+        tot += w * 128;
+        if (tot >= (int64_t)INT32_MAX) return fail(OCMP_ERR_UNSUPPORTED, "SELL-32 layout: too many entries");
+    }
+    off[ns] = (int32_t)tot;
+    std::vector<int32_t> colv(tot, 0);
+    for (int64_t sl = 0; sl < ns; sl++) {
+        const int64_t w = (off[sl + 1] - off[sl]) / 128;
+        for (int lane = 0; lane < 32; lane++) {
+            const int64_t r = sl * 32 + lane;
+            if (r >= n) continue;                           // past the last row: column 0, value 0
+            for (int64_t e = 0; e < 4 * w; e++) {
+                const int64_t q = off[sl] + ((e / 4) * 32 + lane) * 4 + e % 4;
+                const int64_t k = s->rowptr[r] + e;
+                if (k < s->rowptr[r + 1]) {
+                    colv[q] = s->col[k];
+                    pos[k] = (int32_t)q;
+                } else {
+                    colv[q] = (int32_t)r;                   // padding: the row itself, value 0
+                }
+            }
+        }
+    }
+    int st = upload(&s->d_sell_off, off.data(), off.size());
+    if (!st) st = upload(&s->d_sell_col, colv.data(), colv.size());
+    if (!st) st = upload(&s->d_sell_pos, pos.data(), pos.size());
+    if (st) {
+        dfree(s->d_sell_off);
+        dfree(s->d_sell_col);
+        dfree(s->d_sell_pos);
+        s->d_sell_off = s->d_sell_col = s->d_sell_pos = nullptr;
+        return st;
+    }
+    s->sell_slices = ns;
+    s->sell_nent = tot;
+    return OCMP_OK;
+}
+}  // namespace ocmp
+
 extern "C" {
 
 int ocmp_abi_version(void) { return OCMP_ABI_VERSION; }
@@ -512,7 +562,8 @@ static void free_space_device(ocmp_space_s* s) {
                   s->d_inc_ptr,  s->d_inc,      s->d_ifac,      s->d_bfac,     s->d_ebf_ptr,   s->d_ebf,
                   s->d_Rc,       s->d_Rv,       s->d_qw,        s->d_qphi,     s->d_mvec,      s->d_fw,
                   s->d_fphi,     s->d_fdphi,    s->d_flam,      s->d_K,        s->d_facetK,    s->d_Fe,
-                  s->d_lift_ptr, s->d_lift_pos, s->d_Rm_ff, s->d_geo_ff, s->d_tpos, s->d_cseg, s->d_csrc, s->d_u2, s->d_Kd};
+                  s->d_lift_ptr, s->d_lift_pos, s->d_Rm_ff, s->d_geo_ff, s->d_tpos, s->d_cseg, s->d_csrc, s->d_u2, s->d_Kd,
+                  s->d_sell_off, s->d_sell_col, s->d_sell_pos};
     for (void* p : ps) dfree(p);
 }
 
@@ -1133,10 +1184,20 @@ int ocmp_matrix_create_batch(ocmp_space_t s, int32_t nbatch, int32_t flags, ocmp
     m->flags = flags;
     m->B = nbatch;
     const size_t nz = (size_t)s->nnz * nbatch, nd = (size_t)s->ndof * nbatch;
-    int st = dalloc(&m->vals, nz);
+    if ((flags & OCMP_MAT_SELL32) && (!(flags & OCMP_MAT_JACOBI32) || nbatch != 1 || s->kind == OCMP_COMPOUND)) {
+        delete m;
+        return fail(OCMP_ERR_ARG, "ocmp_matrix_create: OCMP_MAT_SELL32 needs OCMP_MAT_JACOBI32 on a single matrix");
+    }
+    int st = (flags & OCMP_MAT_SELL32) ? space_build_sell(s) : OCMP_OK;
+    if (!st) st = dalloc(&m->vals, nz);
     if (!st && (flags & OCMP_MAT_FP32)) st = dalloc(&m->vals32, nz);
     if (!st && (flags & OCMP_MAT_JACOBI64)) st = dalloc(&m->svals64, nz);
-    if (!st && (flags & OCMP_MAT_JACOBI32)) st = dalloc(&m->svals32, nz);
+    if (!st && (flags & OCMP_MAT_JACOBI32)) {
+        const size_t n32 = (flags & OCMP_MAT_SELL32) ? (size_t)s->sell_nent : nz;
+        st = dalloc(&m->svals32, n32);
+        if (!st && (flags & OCMP_MAT_SELL32) && cudaMemset(m->svals32, 0, sizeof(float) * n32) != cudaSuccess)
+            st = OCMP_ERR_CUDA;
+    }
     if (!st && (flags & (OCMP_MAT_JACOBI64 | OCMP_MAT_JACOBI32))) st = dalloc(&m->dinv, nd);
     if (!st && (flags & OCMP_MAT_JACOBI32)) st = dalloc(&m->dinv32, nd);
     if (!st) st = cudaMemset(m->vals, 0, sizeof(double) * nz) == cudaSuccess ? 0 : OCMP_ERR_CUDA;

@@ -149,6 +149,13 @@ struct ocmp_space_s {
     double* d_K = nullptr;          // ne*nloc^2 element matrices (FP64, or (hi, lo) float pairs)
     double* d_facetK = nullptr;     // nif*(2 nloc)^2 + nbf*nloc^2 facet matrices
     double* d_Fe = nullptr;         // ne*nloc element right-hand sides
+    // SELL-32 layout of the pattern (built on first use by a matrix with OCMP_MAT_SELL32): slices of
+    // 32 rows, each row padded to its slice's width in 4-entry chunks; entry (slice s, chunk c, row
+    // lane l, e) at sell_off[s] + (c * 32 + l) * 4 + e
+    int64_t sell_slices = 0, sell_nent = 0;
+    int32_t* d_sell_off = nullptr;  // slices + 1
+    int32_t* d_sell_col = nullptr;  // sell_nent columns (padding: the row itself, or 0 past the last row)
+    int32_t* d_sell_pos = nullptr;  // nnz: the SELL position of each CSR entry
 };
 
 // Matrix outputs selected at creation (ocmp_matrix_create's flags): the FP64 values always; an FP32
@@ -198,6 +205,7 @@ void strip_set_gemm(Strip* p, int kind);
 // M, N multiples of 128, K of 32; *err set when a bounded wait gave up
 int tc_gemm_nt(int M, int N, int K, const float* A, int64_t lda, const float* B, int64_t ldb, float* C, int64_t ldc,
                float alpha, float beta, int* err, cudaStream_t st);
+int space_build_sell(ocmp_space_s* s);
 int autotune_spmv(ocmp_space_s* s, const double* vals, const double* x, double* y, cudaStream_t st, int reps,
                   int* best_tpr, int* best_u, float* best_ms);
 }  // namespace ocmp

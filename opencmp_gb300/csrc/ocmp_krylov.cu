@@ -18,6 +18,7 @@
 #include <cmath>
 #include <mutex>
 #include <string>
+#include <type_traits>
 
 #include "ocmp_internal.h"
 #include "ocmp_spmv.cuh"
@@ -85,6 +86,8 @@ struct ocmp_solver_s {
     size_t tev_used = 0;
     int* worklog = nullptr;     // per timed launch: 1 if it ran (not past convergence), written by the kernel
     int worklog_cap = 0;
+    // the FP32 Krylov matrix is the assembly's SELL-32 copy (OCMP_MAT_SELL32, borrowed)
+    bool sell = false;
     int64_t spmv_launches = 0;
     double spmv_ms = 0;
     cudaStream_t gstream = nullptr;   // capture/launch stream when the caller passes the default stream
@@ -769,6 +772,53 @@ __global__ void __launch_bounds__(256) gm_spmv(int64_t n, int j, const int32_t* 
     }
 }
 
+// The same product from the SELL-32 copy: a warp per slice of 32 rows, a lane per row, 16-byte loads
+// of column indices and values, two chunks (8 entries) in flight before their gathers. The grid is
+// a fixed number of waves that stride over the slices, so that a launch queued past convergence
+// retires at once.
+__global__ void __launch_bounds__(256) gm_spmv_sell(int64_t n, int64_t nslices, int j, const int32_t* __restrict__ off,
+                                                    const int32_t* __restrict__ scol, const float* __restrict__ sval,
+                                                    const uint8_t* __restrict__ freed, const float* __restrict__ xin,
+                                                    int xin_is_basis, float* __restrict__ V,
+                                                    const double* __restrict__ scale, const int* __restrict__ flags,
+                                                    int* __restrict__ worked) {
+    const bool done = flags[F_CONV] != 0;
+    if (worked && blockIdx.x == 0 && threadIdx.x == 0) *worked = done ? 0 : 1;
+    if (done) return;
+    const int lane = threadIdx.x & 31;
+    const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    const float sc = xin_is_basis ? (float)scale[j] : 1.f;
+    for (int64_t sl = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5; sl < nslices; sl += nw) {
+        const int32_t o0 = off[sl], w = (off[sl + 1] - o0) >> 7;   // chunks of 4 entries per row
+        const int4* C = reinterpret_cast<const int4*>(scol + o0) + lane;
+        const float4* A = reinterpret_cast<const float4*>(sval + o0) + lane;
+        float acc0 = 0.f, acc1 = 0.f;
+        int c = 0;
+        for (; c + 1 < w; c += 2) {
+            const int4 c0 = __ldg(C + c * 32), c1 = __ldg(C + (c + 1) * 32);
+            const float4 a0 = __ldg(A + c * 32), a1 = __ldg(A + (c + 1) * 32);
+            acc0 = fmaf(a0.x, __ldg(xin + c0.x), acc0);
+            acc1 = fmaf(a1.x, __ldg(xin + c1.x), acc1);
+            acc0 = fmaf(a0.y, __ldg(xin + c0.y), acc0);
+            acc1 = fmaf(a1.y, __ldg(xin + c1.y), acc1);
+            acc0 = fmaf(a0.z, __ldg(xin + c0.z), acc0);
+            acc1 = fmaf(a1.z, __ldg(xin + c1.z), acc1);
+            acc0 = fmaf(a0.w, __ldg(xin + c0.w), acc0);
+            acc1 = fmaf(a1.w, __ldg(xin + c1.w), acc1);
+        }
+        if (c < w) {
+            const int4 c0 = __ldg(C + c * 32);
+            const float4 a0 = __ldg(A + c * 32);
+            acc0 = fmaf(a0.x, __ldg(xin + c0.x), acc0);
+            acc0 = fmaf(a0.y, __ldg(xin + c0.y), acc0);
+            acc0 = fmaf(a0.z, __ldg(xin + c0.z), acc0);
+            acc0 = fmaf(a0.w, __ldg(xin + c0.w), acc0);
+        }
+        const int64_t r = sl * 32 + lane;
+        if (r < n) V[(int64_t)(j + 1) * n + r] = freed[r] ? (acc0 + acc1) * sc : 0.f;
+    }
+}
+
 // w -= sum_k h_k v_k; |w|^2; then (finishing block) Hessenberg column + Givens, or the request for
 // a second pass. pass 1 reads h from red (d_k = V_k . w, |w|^2 in red[j+1]); pass 2 from red2.
 template <class T>
@@ -995,9 +1045,21 @@ int gm_run(const Ctx& c, const GmBufs<T>& B, const double* b, double* x, int max
             }
             cudaEventRecord(sv->tev[sv->tev_used], ls);
         }
-        OCMP_LAUNCH(gm_spmv<T, TPR, U><<<gs, 256, 0, ls>>>(n, j, s->d_rowptr, s->d_col, B.A, s->d_free, xin, (block || strip) ? 0 : 1, B.V,
-                                                 sv->scale, sv->flags, bt,
-                                                 timing ? sv->worklog + sv->tev_used / 2 : nullptr));
+        int* wlog = timing ? sv->worklog + sv->tev_used / 2 : nullptr;
+        bool done_sell = false;
+        if constexpr (std::is_same<T, float>::value) {
+            if (sv->sell && B.A == sv->K32 && NB == 1) {
+                const unsigned gsl = (unsigned)std::min<int64_t>(nblk(s->sell_slices * 32, 256), 2 * kGridCap);
+                OCMP_LAUNCH(gm_spmv_sell<<<gsl, 256, 0, ls>>>(n, s->sell_slices, j, s->d_sell_off, s->d_sell_col, B.A,
+                                                              s->d_free, xin, (block || strip) ? 0 : 1, B.V, sv->scale,
+                                                              sv->flags, wlog));
+                done_sell = true;
+            }
+        }
+        if (!done_sell)
+            OCMP_LAUNCH(gm_spmv<T, TPR, U><<<gs, 256, 0, ls>>>(n, j, s->d_rowptr, s->d_col, B.A, s->d_free, xin,
+                                                             (block || strip) ? 0 : 1, B.V, sv->scale, sv->flags, bt,
+                                                             wlog));
         if (timing) {
             cudaEventRecord(sv->tev[sv->tev_used + 1], ls);
             sv->tev_used += 2;
@@ -1274,6 +1336,7 @@ int ocmp_solver_create(ocmp_matrix_t mat, const ocmp_solve_params_t* prm, ocmp_s
     }
     sv->K64 = sv->borrow ? mat->svals64 : sv->As64;
     sv->K32 = sv->borrow ? mat->svals32 : sv->As32;
+    sv->sell = sv->borrow && mixed && (mat->flags & OCMP_MAT_SELL32) && s->d_sell_off != nullptr;
     A(&sv->flags, (size_t)F_NFLAG * NB);
     if (!st && cudaMemset(sv->cnt, 0, sizeof(unsigned) * 8 * NB) != cudaSuccess) st = fail(OCMP_ERR_CUDA, "cudaMemset");
     if (!st && cudaMemset(sv->st, 0, sizeof(double) * S_NSLOT * NB) != cudaSuccess)

@@ -193,7 +193,7 @@ def make_rhs(dt=1.0, src_const=None, src_qp: Optional[torch.Tensor] = None, mass
     return r
 
 
-MAT_FP32, MAT_JACOBI64, MAT_JACOBI32, MAT_DFLOAT = 1, 2, 4, 8
+MAT_FP32, MAT_JACOBI64, MAT_JACOBI32, MAT_DFLOAT, MAT_SELL32 = 1, 2, 4, 8, 16
 
 
 class Matrix:
@@ -203,11 +203,11 @@ class Matrix:
     on the FP32 pipes (about 1e-14 relative to the native FP64 assembly)."""
 
     def __init__(self, space: Space, fp32: bool = False, jacobi64: bool = False, jacobi32: bool = False,
-                 dfloat: bool = False, batch: int = 1):
+                 dfloat: bool = False, batch: int = 1, sell: bool = False):
         self.space = space
         h = C.c_void_p()
         flags = (MAT_FP32 if fp32 else 0) | (MAT_JACOBI64 if jacobi64 else 0) | (MAT_JACOBI32 if jacobi32 else 0) \
-            | (MAT_DFLOAT if dfloat else 0)
+            | (MAT_DFLOAT if dfloat else 0) | (MAT_SELL32 if sell else 0)
         self.batch = batch
         LB.call('ocmp_matrix_create_batch', space.h, batch, flags, C.byref(h))
         self.h = h
