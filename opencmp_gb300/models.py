@@ -288,6 +288,25 @@ class Model:
                     precision='mixed' if prec == 'mixed' else 'fp64',
                     restart=c.get_item(['SOLVER', 'gpu_restart'], int), inner_tol=1e-4)
 
+    @classmethod
+    def name(cls) -> str:
+        """The model's name in file names: the class name in lower case, a trailing 'dim' removed
+        (base_model.py:648-662)."""
+        n = cls.__name__.lower()
+        return n[:-3] if n.endswith('dim') else n
+
+    # ---------------------------------------------------------------- state for solution files
+    def state(self) -> Dict[str, np.ndarray]:
+        """The solution, variable by variable (the content of a solution file)."""
+        return {name: v.u.cpu().numpy() for name, v in self.vars.items()}
+
+    def load_state(self, st: Dict[str, np.ndarray]):
+        """Restore a state written by state() as the initial condition (base_model.py:218-221)."""
+        for name, v in self.vars.items():
+            if name not in st or st[name].size != v.u.numel():
+                raise ValueError('the checkpoint holds no {}-dof solution of {!r}'.format(v.u.numel(), name))
+            v.u.copy_(torch.as_tensor(st[name]))
+
     # ---------------------------------------------------------------- OpenCMP's solve hooks
     def construct_preconditioners(self, a_assembled: List[forms.BilinearForm]) -> List[forms.Preconditioner]:
         """One preconditioner per assembled bilinear form (base_model.py:365-383): the [SOLVER]
@@ -506,6 +525,17 @@ class INS(Model):
         if self._qp is None:
             self._qp = self.th.quad_points()
         return self._qp
+
+    def state(self):
+        return {'u_p': self.u.cpu().numpy()}
+
+    def load_state(self, st):
+        if 'u_p' not in st or st['u_p'].size != self.u.numel():
+            raise ValueError('the checkpoint holds no {}-dof Taylor-Hood solution'.format(self.u.numel()))
+        self.u.copy_(torch.as_tensor(st['u_p']))
+        self.W.copy_(self.u)
+        for h in self.hist:
+            h.copy_(self.u)
 
     def _project(self, vu, vp):
         """Initial condition: L2 projection of each velocity component and of the pressure."""

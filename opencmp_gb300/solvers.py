@@ -27,6 +27,7 @@ import torch
 
 from . import _lib as LB
 from . import fem
+from . import saving
 from .config import ConfigParser
 from .fem import _ptr, _stream
 
@@ -39,8 +40,18 @@ IMEX = {'euler IMEX': 1, 'CNLF': 2, 'SBDF': 3}
 class Solver:
     def __init__(self, model_class, config: ConfigParser):
         self.config = config
+        # restart (base_solver.py:150-213): the checkpoint's time starts time_range, its solution
+        # replaces the initial condition
+        transient = config.get_item(['TRANSIENT', 'transient'], bool)
+        order = IMEX.get(config.get_item(['TRANSIENT', 'scheme'], str), 1) if transient else 1
+        self.restart_file = saving.resolve_restart(config, model_class.name(), order)
         self.model = model_class(config)
         self.model.setup()
+        if self.restart_file is not None:
+            self.model.load_state(saving.read_sol(str(self.restart_file)))
+        self.saver = saving.SolutionFileSaver(self.model, config) \
+            if config.get_item(['VISUALIZATION', 'save_to_file'], bool) else None
+        self.num_iters = 0
         self.transient = config.get_item(['TRANSIENT', 'transient'], bool)
         self.check_error = config.get_item(['ERROR ANALYSIS', 'check_error'], bool)
         self.t = 0.0
@@ -187,14 +198,20 @@ class TransientMultiStepSolver(Solver):
     def solve(self):
         """The time loop of base_solver.py:801-865: step until t reaches the end of the range
         (np.isclose), the step shortened to land on the end time (base_solver.py:379-420), printing
-        the error metrics after every step when check_error is set."""
+        the error metrics after every step when check_error is set, and writing the solution files
+        the save frequency asks for (base_solver.py:562-586; the initial condition first)."""
         t1 = self.t_range[1]
+        if self.saver is not None:
+            self.saver.save(self.t)
         while self.t < t1 and not np.isclose(self.t, t1):
             t_old = self.t
             dt = min(self.dt if self._next_dt is None else self._next_dt, t1 - t_old)
             self._next_dt = None
             self.t = t_old + dt
             self._step(self.theta, dt, self.t, t_old, True)
+            self.num_iters += 1
+            if self.saver is not None:
+                self.saver.after_step(self.num_iters, self.t, self.t_range[0], dt)
             if self.check_error:
                 self.report()
         return self.model.vars
@@ -255,6 +272,8 @@ class AdaptiveSolver(TransientMultiStepSolver):
     def solve(self):
         t1 = self.t_range[1]
         rejects = 0
+        if self.saver is not None:
+            self.saver.save(self.t)
         while self.t < t1 and not np.isclose(self.t, t1):
             dt = min(self.dt, t1 - self.t)
             sols = self._attempt(dt, self.t)
@@ -273,6 +292,9 @@ class AdaptiveSolver(TransientMultiStepSolver):
                 for name, (kept, _) in sols.items():
                     self.model.vars[name].u.copy_(kept)
                 self.t += dt
+                self.num_iters += 1
+                if self.saver is not None:
+                    self.saver.after_step(self.num_iters, self.t, self.t_range[0], dt)
                 rest = t1 - self.t
                 self.dt = min(dt_err, self.dt_range[1], rest if rest > 0 else dt_err)
                 rejects = 0

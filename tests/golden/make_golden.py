@@ -12,7 +12,8 @@ pyparsing are absent), so the fixtures are its test inputs and pinned numbers, r
 * square.npz, coarse_large_square_4bcs.npz - pytests/mesh_files/square.msh (the purely convective
   MCINS test's mesh) and coarse_large_square_4bcs.vol (the transient INS test's);
 * fixtures/<group>_<case>/ - the run directories of the full-system tests the GPU path runs
-  (config plus bc/ic/model/ref_sol sub-configs), copied as data. The tests point their mesh file
+  (config plus bc/ic/model/ref_sol sub-configs), copied as data; restart_transient_poisson is the
+  run directory of the restart test (pytests/full_system/restart/test_restart.py). The tests point their mesh file
   and run_dir at this tree before running them.
 """
 import ast
@@ -30,7 +31,7 @@ from opencmp_gb300.mesh import load_mesh  # noqa: E402
 
 
 FIXTURES = ['poisson/transient_coarse', 'poisson/h_convergence', 'mcins/diffusion', 'mcins/diffusion_convection',
-            'mcins/purely_convective', 'ins/sinusoidal_transient']
+            'mcins/purely_convective', 'ins/sinusoidal_transient', 'restart/transient_poisson']
 MESHES = ['unit_square_coarse.vol', 'square.msh', 'coarse_large_square_4bcs.vol']
 
 
