@@ -120,7 +120,9 @@ typedef struct {
     double tol;              /* on || (b - A x)_free ||_2 / || (b - A x_D)_free ||_2 (FP64)       */
     int32_t maxit;           /* total Krylov iterations                                             */
     double inner_tol;        /* mixed: relative reduction asked of each inner solve               */
-    int32_t check_every;     /* host reads the convergence flag every k iterations (>= 1)          */
+    int32_t check_every;     /* host reads the convergence flag every k iterations (>= 1; 0: 8); -1:
+                                GMRES checks first one iteration before the previous solve's count,
+                                then after every iteration                                          */
 } ocmp_solve_params_t;
 
 typedef struct {

@@ -88,6 +88,7 @@ struct ocmp_solver_s {
     int worklog_cap = 0;
     // the FP32 Krylov matrix is the assembly's SELL-32 copy (OCMP_MAT_SELL32, borrowed)
     bool sell = false;
+    int last_iters = 0;         // iterations of the last GMRES solve (adaptive host checks)
     int64_t spmv_launches = 0;
     double spmv_ms = 0;
     cudaStream_t gstream = nullptr;   // capture/launch stream when the caller passes the default stream
@@ -1106,6 +1107,8 @@ int gm_run(const Ctx& c, const GmBufs<T>& B, const double* b, double* x, int max
     }
     int it = 0, cyc = 0;
     const bool graph = sv->use_graph;
+    const bool adaptive = sv->prm.check_every < 0;
+    int next_check = std::max(1, sv->last_iters - 1);
     // Stream capture is not allowed on the legacy default stream: capture and replay on the
     // solver's own stream instead, ordered after and before the caller's work with events.
     Ctx cg = c;
@@ -1158,9 +1161,13 @@ int gm_run(const Ctx& c, const GmBufs<T>& B, const double* b, double* x, int max
             for (int j = 0; j < m; j++) {
                 iteration(j);
                 it++;
-                if (((j + 1) % std::max(1, sv->prm.check_every)) == 0 || it >= maxit) {
+                // fixed interval, or (check_every < 0) the first check one iteration before the
+                // previous solve's count and then after every iteration
+                const bool check = adaptive ? it >= next_check : ((j + 1) % std::max(1, sv->prm.check_every)) == 0;
+                if (check || it >= maxit) {
                     if (read_flags(c)) return OCMP_ERR_CUDA;
                     if (all(F_CONV) || it >= maxit) break;
+                    next_check = it + 1;
                 }
             }
             finish_cycle();
@@ -1170,6 +1177,7 @@ int gm_run(const Ctx& c, const GmBufs<T>& B, const double* b, double* x, int max
     }
     OCMP_CUDA(cudaGetLastError());
     for (int q = 0; q < NB; q++) iters[q] = sv->hflags[q * F_NFLAG + F_ITERS];
+    sv->last_iters = iters[0];
     *cycles = cyc;
     return OCMP_OK;
 }
@@ -1248,7 +1256,7 @@ int ocmp_solver_create(ocmp_matrix_t mat, const ocmp_solve_params_t* prm, ocmp_s
     sv->mat = mat;
     sv->s = s;
     sv->prm = *prm;
-    if (sv->prm.check_every <= 0) sv->prm.check_every = 8;
+    if (sv->prm.check_every == 0) sv->prm.check_every = 8;
     // a strip-preconditioned iteration costs two full sweeps: read the flags after every one
     if (prm->precond == OCMP_PRE_STRIP) sv->prm.check_every = 1;
     const int64_t n = sv->n = s->ndof;

@@ -79,7 +79,10 @@ struct Strip {
                                      // product whose bounded wait gave up
     int64_t bytes = 0;
     cudaStream_t side[kSide] = {};
+    cudaStream_t chain = nullptr;    // phase 2, at the highest stream priority so that the side streams'
+                                     // products never hold the chain's kernels back
     cudaEvent_t ev_start = nullptr;
+    cudaEvent_t ev_done = nullptr;
     std::vector<cudaEvent_t> ev_phase1;
     // sweeps replayed from graphs: [0] gated on the solver's convergence flag, [1] not gated
     cudaStream_t cap = nullptr;
@@ -265,57 +268,60 @@ __global__ void k_sub_block(int nI, int nIp, int nNp, const float* __restrict__ 
 // the tile. The tile stays in registers (thread t holds column t % 128 of rows t / 128 + 8 j) and
 // rows are never moved: step k takes as pivot the largest |a_rk| over the rows not yet used, and
 // the row and column permutation is applied when the result is written (P[step(r)][piv(c)] =
-// M[r][c]). Per step the owners of column k publish it and the owners of the pivot row publish
-// that row (double-buffered in shared memory), two barriers per step. A zero or non-finite pivot
-// is counted in *flag and replaced by a tiny value.
+// M[r][c]). Per step the eight owners of column k publish it with their best unused row, every
+// thread reduces the eight candidates, the owners of the pivot row publish that row
+// (double-buffered in shared memory): two barriers per step. A zero or non-finite pivot is
+// counted in *flag and replaced by a tiny value.
 constexpr int kTileThreads = 1024;
 constexpr int kTileSmem = 0;
 __global__ void __launch_bounds__(kTileThreads) k_tile_inv(const float* __restrict__ S, int mp, int t0,
                                                            float* __restrict__ P, int* __restrict__ flag) {
     __shared__ float colk[2][kNb];
     __shared__ float prow[2][kNb];
-    __shared__ int used[kNb];
+    __shared__ float cval[2][8];
+    __shared__ int crow[2][8];
     __shared__ int piv[kNb];
     __shared__ int step[kNb];
-    const int tid = threadIdx.x, c = tid & (kNb - 1), r0 = tid >> 7, lane = tid & 31;
+    const int tid = threadIdx.x, c = tid & (kNb - 1), r0 = tid >> 7;
     constexpr int R = kNb / 8;   // rows per thread
     float v[R];
 #pragma unroll
     for (int j = 0; j < R; j++) v[j] = S[(int64_t)(t0 + r0 + 8 * j) * mp + t0 + c];
-    if (tid < kNb) used[tid] = 0;
-    __syncthreads();
+    unsigned usedmask = 0;       // which of this thread's rows have been pivots
     for (int k = 0; k < kNb; k++) {
         const int b = k & 1;
         if (c == k) {
+            float best = -1.f;
+            int bi = kNb;
 #pragma unroll
-            for (int j = 0; j < R; j++) colk[b][r0 + 8 * j] = v[j];
+            for (int j = 0; j < R; j++) {
+                colk[b][r0 + 8 * j] = v[j];
+                const float a = (usedmask >> j) & 1u ? -1.f : fabsf(v[j]);
+                if (a > best) {
+                    best = a;
+                    bi = r0 + 8 * j;
+                }
+            }
+            cval[b][r0] = best;
+            crow[b][r0] = bi;
         }
         __syncthreads();
-        // every warp finds the pivot itself: the largest |a_rk| over the unused rows (lowest r on ties)
-        float best = -1.f;
-        int bi = kNb;
+        float best = cval[b][0];
+        int p = crow[b][0];
 #pragma unroll
-        for (int q = 0; q < kNb / 32; q++) {
-            const int i = lane + 32 * q;
-            const float a = used[i] ? -1.f : fabsf(colk[b][i]);
-            if (a > best) {
+        for (int g = 1; g < 8; g++) {
+            const float a = cval[b][g];
+            const int r = crow[b][g];
+            if (a > best || (a == best && r < p)) {
                 best = a;
-                bi = i;
+                p = r;
             }
         }
+        if (p >= kNb) {   // every remaining |a_rk| is NaN: take the smallest unused row
+            p = kNb;
 #pragma unroll
-        for (int off = 16; off > 0; off >>= 1) {
-            const float ob = __shfl_xor_sync(0xffffffffu, best, off);
-            const int oi = __shfl_xor_sync(0xffffffffu, bi, off);
-            if (ob > best || (ob == best && oi < bi)) {
-                best = ob;
-                bi = oi;
-            }
-        }
-        int p = bi;
-        if (p >= kNb) {   // every remaining |a_rk| is NaN: take the first unused row
-            p = 0;
-            while (p < kNb - 1 && used[p]) p++;
+            for (int g = 0; g < 8; g++) p = min(p, crow[b][g] < kNb ? crow[b][g] : kNb);
+            if (p >= kNb) p = k;
         }
         float pv = colk[b][p];
         if (!(fabsf(pv) > 0.f) || !isfinite(pv)) {
@@ -330,10 +336,10 @@ __global__ void __launch_bounds__(kTileThreads) k_tile_inv(const float* __restri
             for (int j = 0; j < R; j++)
                 if (j == (p >> 3)) x = v[j];
             prow[b][c] = (c == k ? 1.f : x) * d;
+            usedmask |= 1u << (p >> 3);
         }
         __syncthreads();
         if (tid == 0) {
-            used[p] = 1;
             piv[k] = p;
             step[p] = k;
         }
@@ -531,6 +537,8 @@ void strip_free(Strip* p) {
     for (cudaEvent_t e : p->fev)
         if (e) cudaEventDestroy(e);
     if (p->ev_start) cudaEventDestroy(p->ev_start);
+    if (p->ev_done) cudaEventDestroy(p->ev_done);
+    if (p->chain) cudaStreamDestroy(p->chain);
     for (cudaStream_t q : p->side)
         if (q) cudaStreamDestroy(q);
     for (cudaGraphExec_t g : p->gexec)
@@ -785,6 +793,13 @@ int strip_create(const ocmp_space_s* s, Strip** out) {
             st = fail(OCMP_ERR_CUDA, "cudaStreamCreateWithFlags");
     if (!st && cudaStreamCreateWithFlags(&p->cap, cudaStreamNonBlocking) != cudaSuccess)
         st = fail(OCMP_ERR_CUDA, "cudaStreamCreateWithFlags");
+    if (!st) {
+        int lo = 0, hi = 0;
+        if (cudaDeviceGetStreamPriorityRange(&lo, &hi) != cudaSuccess ||
+            cudaStreamCreateWithPriority(&p->chain, cudaStreamNonBlocking, hi) != cudaSuccess ||
+            cudaEventCreateWithFlags(&p->ev_done, cudaEventDisableTiming) != cudaSuccess)
+            st = fail(OCMP_ERR_CUDA, "strip preconditioner: chain stream");
+    }
     p->ev_phase1.assign(K, nullptr);
     for (int k = 0; k < K && !st; k++)
         if (cudaEventCreateWithFlags(&p->ev_phase1[k], cudaEventDisableTiming) != cudaSuccess)
@@ -819,6 +834,8 @@ int strip_factor(Strip* p, const ocmp_space_s* s, const double* vals, cudaStream
     OCMP_CUDA(cudaMemsetAsync(p->d_flag, 0, 2 * sizeof(int), st));
     OCMP_CUDA(cudaEventRecord(p->ev_start, st));
     for (int q = 0; q < kSide; q++) OCMP_CUDA(cudaStreamWaitEvent(p->side[q], p->ev_start, 0));
+    cudaStream_t cs = p->chain;
+    OCMP_CUDA(cudaStreamWaitEvent(cs, p->ev_start, 0));
     // phase 1: fill every strip and eliminate its N pivots, strips spread over the side streams
     for (int k = 0; k < K; k++) {
         const int q = k % kSide;
@@ -832,32 +849,34 @@ int strip_factor(Strip* p, const ocmp_space_s* s, const double* vals, cudaStream
         if (r) return r;
         OCMP_CUDA(cudaEventRecord(p->ev_phase1[k], ss));
     }
-    // phase 2 on the caller's stream, strip after strip: the Schur update from the previous strip's
+    // phase 2 on the chain stream, strip after strip: the Schur update from the previous strip's
     // inverse, then the I pivots
     for (int k = 0; k < K; k++) {
-        OCMP_CUDA(cudaStreamWaitEvent(st, p->ev_phase1[k], 0));
+        OCMP_CUDA(cudaStreamWaitEvent(cs, p->ev_phase1[k], 0));
         const int mp = p->mp[k];
         const int64_t s0 = p->s[k];
         float* S = p->d_G + p->goff[k];
         if (k > 0 && p->nI[k] > 0 && p->nJ[k - 1] > 0) {
             const int nI = p->nI[k], nJ = p->nJ[k - 1], nIp = pad(nI), nJp = pad(nJ);
-            OCMP_CUDA(cudaMemsetAsync(p->d_Cc, 0, sizeof(float) * (size_t)nIp * nJp, st));
-            OCMP_CUDA(cudaMemsetAsync(p->d_Bt, 0, sizeof(float) * (size_t)nIp * nJp, st));
-            OCMP_LAUNCH(k_fill_iface<<<nblk(nI + nJ, 128), 128, 0, st>>>(
+            OCMP_CUDA(cudaMemsetAsync(p->d_Cc, 0, sizeof(float) * (size_t)nIp * nJp, cs));
+            OCMP_CUDA(cudaMemsetAsync(p->d_Bt, 0, sizeof(float) * (size_t)nIp * nJp, cs));
+            OCMP_LAUNCH(k_fill_iface<<<nblk(nI + nJ, 128), 128, 0, cs>>>(
                 nI, nJ, nJp, s0, p->s[k - 1], p->d_I + p->ioff[k], p->jrow + p->joff[k - 1], p->d_Iinv, p->d_Jinv,
                 p->d_lo_ptr, p->d_lo_pos, p->d_hi_ptr, p->d_hi_pos, s->d_col, vals, s->d_free, p->d_Cc, p->d_Bt));
-            OCMP_LAUNCH(k_gather_gjj<<<nblk((int64_t)nJp * nJp, 256), 256, 0, st>>>(
+            OCMP_LAUNCH(k_gather_gjj<<<nblk((int64_t)nJp * nJp, 256), 256, 0, cs>>>(
                 nJ, nJp, p->d_J + p->joff[k - 1], p->d_G + p->goff[k - 1], p->mp[k - 1], p->d_Gjj));
             // Tt = Bt Gjj^T (= (G_JJ A_JI)^T), U = Cc Tt^T
-            int r = gemm(p, nIp, nJp, nJp, p->d_Bt, nJp, p->d_Gjj, nJp, p->d_Tt, nJp, 1.f, 0.f, st);
-            if (!r) r = gemm(p, nIp, nIp, nJp, p->d_Cc, nJp, p->d_Tt, nJp, p->d_U, nIp, 1.f, 0.f, st);
+            int r = gemm(p, nIp, nJp, nJp, p->d_Bt, nJp, p->d_Gjj, nJp, p->d_Tt, nJp, 1.f, 0.f, cs);
+            if (!r) r = gemm(p, nIp, nIp, nJp, p->d_Cc, nJp, p->d_Tt, nJp, p->d_U, nIp, 1.f, 0.f, cs);
             if (r) return r;
-            OCMP_LAUNCH(k_sub_block<<<nblk((int64_t)nI * nI, 256), 256, 0, st>>>(nI, nIp, p->nNp[k], p->d_U, mp, S));
+            OCMP_LAUNCH(k_sub_block<<<nblk((int64_t)nI * nI, 256), 256, 0, cs>>>(nI, nIp, p->nNp[k], p->d_U, mp, S));
         }
-        int r = gj_tiles(p, S, mp, p->nNp[k], mp, p->work[0], st);
+        int r = gj_tiles(p, S, mp, p->nNp[k], mp, p->work[0], cs);
         if (r) return r;
     }
     OCMP_CUDA(cudaGetLastError());
+    OCMP_CUDA(cudaEventRecord(p->ev_done, cs));
+    OCMP_CUDA(cudaStreamWaitEvent(st, p->ev_done, 0));
     OCMP_CUDA(cudaEventRecord(p->fev[1], st));
     int flags[2] = {0, 0};
     OCMP_CUDA(cudaMemcpyAsync(flags, p->d_flag, 2 * sizeof(int), cudaMemcpyDeviceToHost, st));
