@@ -55,7 +55,8 @@ enum { OCMP_H1 = 0, OCMP_L2 = 1, OCMP_COMPOUND = 2 };  /* compound: the Taylor-H
 enum { OCMP_WIND_NONE = 0, OCMP_WIND_CONST = 1, OCMP_WIND_VERTEX = 2 };
 enum { OCMP_SRC_NONE = 0, OCMP_SRC_CONST = 1, OCMP_SRC_QP = 2 };
 enum { OCMP_CG = 0, OCMP_GMRES = 1 };
-enum { OCMP_PRE_NONE = 0, OCMP_PRE_JACOBI = 1, OCMP_PRE_BLOCK_JACOBI = 2, OCMP_PRE_USER = 3, OCMP_PRE_STRIP = 4 };
+enum { OCMP_PRE_NONE = 0, OCMP_PRE_JACOBI = 1, OCMP_PRE_BLOCK_JACOBI = 2, OCMP_PRE_USER = 3, OCMP_PRE_STRIP = 4,
+       OCMP_PRE_CAHOUET_CHABARD = 5 };
 enum { OCMP_FP64 = 0, OCMP_MIXED = 1 };
 
 typedef struct ocmp_mesh_s* ocmp_mesh_t;
@@ -314,6 +315,19 @@ int ocmp_th_nq(ocmp_th_t th);
 int ocmp_th_quad_points(ocmp_th_t th, double* xyz_host);                       /* ne*nq*2 */
 int ocmp_th_assemble(ocmp_th_t th, ocmp_matrix_t mat, const ocmp_th_form_t* form, void* stream);
 int ocmp_th_assemble_rhs(ocmp_th_t th, const ocmp_th_rhs_t* rhs, double* b_dev, void* stream);
+/* GMRES with OCMP_PRE_CAHOUET_CHABARD on a compound Taylor-Hood matrix [u | p]: the solve of the
+ * saddle-point system OpenCMP hands to a sparse direct solver (ins.py with linear_solver = default).
+ * The preconditioner is velocity point Jacobi (vdinv: nu entries, 0 on constrained rows) and on the
+ * pressure block the Cahouet-Chabard approximation of the inverse Schur complement,
+ *   z_p = -(alpha S^-1 r_p + beta mpinv r_p) / tc^2,   S = L_p + delta M_p  (the matrix pop),
+ * alpha the mass coefficient, beta = dt nu, tc the factor of the divergence terms, mpinv the inverse
+ * pressure-mass diagonal. S^-1 is applied exactly by the strip direct factorisation of pop, built on
+ * the first call and refactorised when `refactor` is nonzero (pop's values changed); the other
+ * arguments are copied on every call. No counterpart in the reference beyond the solve it
+ * replaces. */
+int ocmp_solver_set_cahouet_chabard(ocmp_solver_t solver, ocmp_matrix_t pop, const double* vdinv_dev,
+                                    const double* mpinv_dev, int64_t nu, double alpha, double beta, double tc,
+                                    int32_t refactor, void* stream);
 /* Inverse of the block-diagonal preconditioner: 1/a_ii on free velocity rows; on pressure rows
  * -1/(|a_ii| + sum_j a_ij^2 / |a_jj|) over free velocity columns j (the diagonal of the Schur
  * complement B diag(A)^-1 B^T); 0 on constrained rows. */

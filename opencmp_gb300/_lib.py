@@ -18,7 +18,7 @@ H1, L2, COMPOUND = 0, 1, 2
 WIND_NONE, WIND_CONST, WIND_VERTEX = 0, 1, 2
 SRC_NONE, SRC_CONST, SRC_QP = 0, 1, 2
 CG, GMRES = 0, 1
-PRE_NONE, PRE_JACOBI, PRE_BLOCK_JACOBI, PRE_USER, PRE_STRIP = 0, 1, 2, 3, 4
+PRE_NONE, PRE_JACOBI, PRE_BLOCK_JACOBI, PRE_USER, PRE_STRIP, PRE_CAHOUET_CHABARD = 0, 1, 2, 3, 4, 5
 FP64, MIXED = 0, 1
 
 
@@ -132,6 +132,7 @@ SIGNATURES = {
     'ocmp_solve_cg_noalloc': [P, P, P, D, I32, P, C.POINTER(SolveInfo)],
     'ocmp_solver_strip_stats': [P, C.POINTER(StripStats)],
     'ocmp_solver_strip_timing': [P, I32],
+    'ocmp_solver_set_cahouet_chabard': [P, P, P, P, I64, D, D, D, I32, P],
     'ocmp_solver_strip_gemm': [P, I32],
     'ocmp_dense_gemm_nt': [I32, I32, I32, I32, P, I64, P, I64, P, I64, C.c_float, C.c_float, P],
     'ocmp_guess_create': [I32, C.c_uint64, C.POINTER(P)],

@@ -31,6 +31,21 @@ struct Bat {
 };
 }  // namespace ocmp
 
+// Cahouet-Chabard block preconditioner of a Taylor-Hood saddle-point system [u | p]
+// (OCMP_PRE_CAHOUET_CHABARD): velocity point Jacobi, and on the pressure block
+// z_p = -(alpha S^-1 r_p + beta M_p,diag^-1 r_p) / tc^2 with S = L_p + delta M_p solved exactly by the
+// strip direct factorisation of the pressure operator.
+struct CCPre {
+    ocmp::Strip* strip = nullptr;
+    ocmp_matrix_s* pop = nullptr;   // the pressure operator S (pressure space)
+    int64_t nu = 0, np = 0;         // velocity dofs (all components) and pressure dofs
+    double alpha = 1, beta = 0, tc = 1;
+    double* vdinv = nullptr;        // nu
+    double* mpinv = nullptr;        // np
+    double* zp64 = nullptr;         // np: pressure-solve vector
+    float* zp32 = nullptr;
+};
+
 struct ocmp_solver_s {
     ocmp_matrix_s* mat = nullptr;
     ocmp_space_s* s = nullptr;
@@ -44,6 +59,7 @@ struct ocmp_solver_s {
     bool udiag_set = false;
     double* Binv = nullptr;     // block Jacobi (L2 element blocks)
     ocmp::Strip* strip = nullptr;  // strip direct preconditioner (OCMP_PRE_STRIP)
+    CCPre* cc = nullptr;           // Cahouet-Chabard data (OCMP_PRE_CAHOUET_CHABARD), once set
     double* V = nullptr;        // (m+1) x n
     double* w = nullptr;
     double* z = nullptr;
@@ -981,6 +997,44 @@ __global__ void gm_set_tols(double* st, double tol, double inner, double eta2, i
     }
 }
 
+// Cahouet-Chabard, part 1: z_u = sc D_u^-1 v_u, zp = sc v_p (the pressure solve's right-hand side)
+template <class T>
+__global__ void cc_pre1(int64_t nu, int64_t np, const T* __restrict__ v, const double* __restrict__ scale, int j,
+                        const double* __restrict__ vdinv, T* __restrict__ z, T* __restrict__ zp,
+                        const int* __restrict__ flags) {
+    if (flags && flags[F_CONV]) return;
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    const double sc = scale ? scale[j] : 1.0;
+    if (i < nu) z[i] = (T)(sc * vdinv[i] * (double)v[i]);
+    else if (i < nu + np) zp[i - nu] = (T)(sc * (double)v[i]);
+}
+// part 2: z_p = -(alpha S^-1 (sc v_p) + beta M^-1 (sc v_p)) / tc^2 (S^-1 applied in place on zp)
+template <class T>
+__global__ void cc_pre2(int64_t nu, int64_t np, const T* __restrict__ v, const double* __restrict__ scale, int j,
+                        const double* __restrict__ mpinv, const T* __restrict__ zp, T* __restrict__ z, double alpha,
+                        double beta, double tc, const int* __restrict__ flags) {
+    if (flags && flags[F_CONV]) return;
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= np) return;
+    const double sc = scale ? scale[j] : 1.0;
+    const double vp = sc * (double)v[nu + i];
+    z[nu + i] = (T)(-(alpha * (double)zp[i] + beta * mpinv[i] * vp) / (tc * tc));
+}
+
+template <class T>
+int cc_apply(CCPre* cc, const T* v, const double* scale, int j, T* z, const int* flags, cudaStream_t st) {
+    T* zp = nullptr;
+    if constexpr (std::is_same<T, float>::value) zp = cc->zp32;
+    else zp = cc->zp64;
+    OCMP_LAUNCH(cc_pre1<T><<<nblk(cc->nu + cc->np, kThreads), kThreads, 0, st>>>(cc->nu, cc->np, v, scale, j, cc->vdinv,
+                                                                              z, zp, flags));
+    int r = strip_apply<T>(cc->strip, cc->pop->space, cc->pop->vals, zp, nullptr, 0, zp, flags, st);
+    if (r) return r;
+    OCMP_LAUNCH(cc_pre2<T><<<nblk(cc->np, kThreads), kThreads, 0, st>>>(cc->nu, cc->np, v, scale, j, cc->mpinv, zp, z,
+                                                                     cc->alpha, cc->beta, cc->tc, flags));
+    return OCMP_OK;
+}
+
 template <class T>
 struct GmBufs {
     const T* A;        // Krylov matrix (scaled or plain)
@@ -989,6 +1043,7 @@ struct GmBufs {
     T* V;
     T* z;              // block Jacobi / strip workspace
     Strip* strip;      // strip direct preconditioner, or null
+    CCPre* cc;         // Cahouet-Chabard preconditioner, or null
 };
 
 // Host driver of the fused GMRES over a batch of sv->B systems (B = 1 for a single solve).
@@ -1011,6 +1066,7 @@ int gm_run(const Ctx& c, const GmBufs<T>& B, const double* b, double* x, int max
     double* red2 = sv->red + (m + 4);
     const bool block = B.Binv != nullptr;
     const bool strip = B.strip != nullptr;
+    const bool ccp = B.cc != nullptr;
     const int64_t ne = s->mesh->ne;
     const int L = s->nloc;
     const dim3 gg(G, NB), gs(nblk(n * TPR, 256), NB);
@@ -1036,6 +1092,9 @@ int gm_run(const Ctx& c, const GmBufs<T>& B, const double* b, double* x, int max
             // z = M^-1 (scale_j V_j); every sweep kernel returns at once after convergence
             strip_apply<T>(B.strip, s, sv->mat->vals, B.V + (int64_t)j * n, sv->scale, j, B.z, sv->flags, ls);
             xin = B.z;
+        } else if (ccp) {
+            cc_apply<T>(B.cc, B.V + (int64_t)j * n, sv->scale, j, B.z, sv->flags, ls);
+            xin = B.z;
         }
         const bool timing = sv->time_spmv && ls == c.st && sv->worklog && (int)(sv->tev_used / 2) < sv->worklog_cap;
         if (timing) {
@@ -1052,14 +1111,14 @@ int gm_run(const Ctx& c, const GmBufs<T>& B, const double* b, double* x, int max
             if (sv->sell && B.A == sv->K32 && NB == 1) {
                 const unsigned gsl = (unsigned)std::min<int64_t>(nblk(s->sell_slices * 32, 256), 2 * kGridCap);
                 OCMP_LAUNCH(gm_spmv_sell<<<gsl, 256, 0, ls>>>(n, s->sell_slices, j, s->d_sell_off, s->d_sell_col, B.A,
-                                                              s->d_free, xin, (block || strip) ? 0 : 1, B.V, sv->scale,
+                                                              s->d_free, xin, (block || strip || ccp) ? 0 : 1, B.V, sv->scale,
                                                               sv->flags, wlog));
                 done_sell = true;
             }
         }
         if (!done_sell)
             OCMP_LAUNCH(gm_spmv<T, TPR, U><<<gs, 256, 0, ls>>>(n, j, s->d_rowptr, s->d_col, B.A, s->d_free, xin,
-                                                             (block || strip) ? 0 : 1, B.V, sv->scale, sv->flags, bt,
+                                                             (block || strip || ccp) ? 0 : 1, B.V, sv->scale, sv->flags, bt,
                                                              wlog));
         if (timing) {
             cudaEventRecord(sv->tev[sv->tev_used + 1], ls);
@@ -1079,6 +1138,10 @@ int gm_run(const Ctx& c, const GmBufs<T>& B, const double* b, double* x, int max
         } else if (strip) {
             OCMP_LAUNCH(gm_combine<T><<<gg, 256, 0, ls>>>(n, m, B.V, sv->scale, sv->H, csg, sv->flags, nullptr, x, B.z, bt));
             strip_apply<T>(B.strip, s, sv->mat->vals, B.z, nullptr, 0, B.z, nullptr, ls);
+            strip_add<T>(n, B.z, x, ls);
+        } else if (ccp) {
+            OCMP_LAUNCH(gm_combine<T><<<gg, 256, 0, ls>>>(n, m, B.V, sv->scale, sv->H, csg, sv->flags, nullptr, x, B.z, bt));
+            cc_apply<T>(B.cc, B.z, nullptr, 0, B.z, nullptr, ls);
             strip_add<T>(n, B.z, x, ls);
         } else {
             OCMP_LAUNCH(gm_combine<T><<<gg, 256, 0, ls>>>(n, m, B.V, sv->scale, sv->H, csg, sv->flags, B.dinv, x, nullptr, bt));
@@ -1227,6 +1290,14 @@ static void free_solver(ocmp_solver_s* sv) {
                   sv->st,   sv->H,    sv->flags, sv->As64, sv->As32, sv->scale, sv->cnt};
     for (void* q : ps) dfree(q);
     if (sv->strip) strip_destroy(sv->strip);
+    if (sv->cc) {
+        if (sv->cc->strip) strip_destroy(sv->cc->strip);
+        dfree(sv->cc->vdinv);
+        dfree(sv->cc->mpinv);
+        dfree(sv->cc->zp64);
+        dfree(sv->cc->zp32);
+        delete sv->cc;
+    }
     if (sv->hflags) cudaFreeHost(sv->hflags);
     if (sv->gexec) cudaGraphExecDestroy(sv->gexec);
     if (sv->gstream) cudaStreamDestroy(sv->gstream);
@@ -1241,7 +1312,7 @@ extern "C" {
 int ocmp_solver_create(ocmp_matrix_t mat, const ocmp_solve_params_t* prm, ocmp_solver_t* out) {
     if (!mat || !prm || !out) return fail(OCMP_ERR_ARG, "ocmp_solver_create: null argument");
     if (prm->method != OCMP_CG && prm->method != OCMP_GMRES) return fail(OCMP_ERR_ARG, "ocmp_solver_create: method");
-    if (prm->precond < OCMP_PRE_NONE || prm->precond > OCMP_PRE_STRIP)
+    if (prm->precond < OCMP_PRE_NONE || prm->precond > OCMP_PRE_CAHOUET_CHABARD)
         return fail(OCMP_ERR_ARG, "ocmp_solver_create: precond");
     if (prm->precision == OCMP_MIXED && prm->method == OCMP_CG && !mat->vals32)
         return fail(OCMP_ERR_ARG, "ocmp_solver_create: mixed-precision CG needs a matrix created with OCMP_MAT_FP32");
@@ -1250,8 +1321,10 @@ int ocmp_solver_create(ocmp_matrix_t mat, const ocmp_solve_params_t* prm, ocmp_s
     ocmp_space_s* s = mat->space;
     if (prm->precond == OCMP_PRE_BLOCK_JACOBI && (s->kind != OCMP_L2 || (s->nloc != 3 && s->nloc != 6 && s->nloc != 10)))
         return fail(OCMP_ERR_UNSUPPORTED, "ocmp_solver_create: block Jacobi is built for L2 element blocks");
-    if (prm->precond == OCMP_PRE_STRIP && (prm->method != OCMP_GMRES || mat->B != 1))
-        return fail(OCMP_ERR_UNSUPPORTED, "ocmp_solver_create: the strip preconditioner is built for GMRES on one matrix");
+    if ((prm->precond == OCMP_PRE_STRIP || prm->precond == OCMP_PRE_CAHOUET_CHABARD) &&
+        (prm->method != OCMP_GMRES || mat->B != 1))
+        return fail(OCMP_ERR_UNSUPPORTED, "ocmp_solver_create: the strip and Cahouet-Chabard preconditioners are built "
+                                          "for GMRES on one matrix");
     auto* sv = new ocmp_solver_s();
     sv->mat = mat;
     sv->s = s;
@@ -1455,12 +1528,66 @@ int ocmp_solver_set_graph(ocmp_solver_t sv, int32_t on) {
     if (!sv) return fail(OCMP_ERR_ARG, "ocmp_solver_set_graph: null solver");
     if (on && sv->prm.method != OCMP_GMRES)
         return fail(OCMP_ERR_UNSUPPORTED, "ocmp_solver_set_graph: graphs are built for GMRES");
-    if (on && sv->strip)
-        return fail(OCMP_ERR_UNSUPPORTED, "ocmp_solver_set_graph: the strip preconditioner runs without graphs");
+    if (on && (sv->strip || sv->prm.precond == OCMP_PRE_CAHOUET_CHABARD))
+        return fail(OCMP_ERR_UNSUPPORTED, "ocmp_solver_set_graph: the strip preconditioners run without graphs");
     sv->use_graph = on != 0;
     if (!on && sv->gexec) {
         cudaGraphExecDestroy(sv->gexec);
         sv->gexec = nullptr;
+    }
+    return OCMP_OK;
+}
+
+int ocmp_solver_set_cahouet_chabard(ocmp_solver_t sv, ocmp_matrix_t pop, const double* vdinv, const double* mpinv,
+                                    int64_t nu, double alpha, double beta, double tc, int32_t refactor,
+                                    void* stream) {
+    if (!sv || !pop || !vdinv || !mpinv) return fail(OCMP_ERR_ARG, "ocmp_solver_set_cahouet_chabard: null argument");
+    if (sv->prm.precond != OCMP_PRE_CAHOUET_CHABARD)
+        return fail(OCMP_ERR_ARG, "ocmp_solver_set_cahouet_chabard: solver not created with OCMP_PRE_CAHOUET_CHABARD");
+    const int64_t np = pop->space->ndof;
+    if (nu < 0 || nu + np != sv->n || pop->B != 1)
+        return fail(OCMP_ERR_ARG, "ocmp_solver_set_cahouet_chabard: velocity + pressure dofs must make the system");
+    if (!(tc != 0.0)) return fail(OCMP_ERR_ARG, "ocmp_solver_set_cahouet_chabard: tc must not be zero");
+    cudaStream_t st = (cudaStream_t)stream;
+    CCPre* cc = sv->cc;
+    if (cc && cc->pop != pop) {
+        if (cc->strip) strip_destroy(cc->strip);
+        cc->strip = nullptr;
+        cc->pop = pop;
+        refactor = 1;
+    }
+    if (!cc) {
+        cc = new CCPre();
+        cc->pop = pop;
+        cc->np = np;
+        int r = dalloc(&cc->vdinv, (size_t)std::max<int64_t>(nu, 1));
+        if (!r) r = dalloc(&cc->mpinv, (size_t)np);
+        if (!r) r = dalloc(&cc->zp64, (size_t)np);
+        if (!r) r = dalloc(&cc->zp32, (size_t)np);
+        if (r) {
+            dfree(cc->vdinv);
+            dfree(cc->mpinv);
+            dfree(cc->zp64);
+            delete cc;
+            return r;
+        }
+        sv->cc = cc;
+        refactor = 1;
+    }
+    cc->nu = nu;
+    cc->np = np;
+    cc->alpha = alpha;
+    cc->beta = beta;
+    cc->tc = tc;
+    if (nu) OCMP_CUDA(cudaMemcpyAsync(cc->vdinv, vdinv, sizeof(double) * nu, cudaMemcpyDeviceToDevice, st));
+    OCMP_CUDA(cudaMemcpyAsync(cc->mpinv, mpinv, sizeof(double) * np, cudaMemcpyDeviceToDevice, st));
+    if (!cc->strip) {
+        const int r = strip_create(pop->space, &cc->strip);
+        if (r) return r;
+    }
+    if (refactor) {
+        const int r = strip_factor(cc->strip, pop->space, pop->vals, st);
+        if (r) return r;
     }
     return OCMP_OK;
 }
@@ -1503,10 +1630,10 @@ int ocmp_solve_batch(ocmp_solver_t sv, const double* b, double* x, void* stream,
     std::vector<int> its(NB, 0);
     int cyc = 0, st;
     if (!mixed) {
-        GmBufs<double> B{sv->K64, jac ? sv->dinv : nullptr, nullptr, sv->V, sv->z, nullptr};
+        GmBufs<double> B{sv->K64, jac ? sv->dinv : nullptr, nullptr, sv->V, sv->z, nullptr, nullptr};
         st = gm_dispatch<double>(c, B, b, x, P.maxit, 0.0, its.data(), &cyc, r0.data());
     } else {
-        GmBufs<float> B{sv->K32, jac ? sv->dinv32 : nullptr, nullptr, sv->V32, sv->z32, nullptr};
+        GmBufs<float> B{sv->K32, jac ? sv->dinv32 : nullptr, nullptr, sv->V32, sv->z32, nullptr, nullptr};
         st = gm_dispatch<float>(c, B, b, x, P.maxit, P.inner_tol > 0 ? P.inner_tol : 1e-4, its.data(), &cyc,
                                 r0.data());
     }
@@ -1555,10 +1682,14 @@ int ocmp_solve(ocmp_solver_t sv, const double* b, double* x, void* stream, ocmp_
         const bool jac = P.precond == OCMP_PRE_JACOBI || P.precond == OCMP_PRE_USER;
         if (sv->B != 1) return fail(OCMP_ERR_ARG, "ocmp_solve: batched matrix, use ocmp_solve_batch");
         if (!mixed) {
-            GmBufs<double> B{sv->K64, jac ? sv->dinv : nullptr, sv->Binv, sv->V, sv->z, sv->strip};
+            if (P.precond == OCMP_PRE_CAHOUET_CHABARD && !sv->cc)
+                return fail(OCMP_ERR_ARG, "ocmp_solve: set the Cahouet-Chabard data (ocmp_solver_set_cahouet_chabard)");
+            GmBufs<double> B{sv->K64, jac ? sv->dinv : nullptr, sv->Binv, sv->V, sv->z, sv->strip, sv->cc};
             st = gm_dispatch<double>(c, B, b, x, P.maxit, 0.0, &iters, &outer, &relres0);
         } else {
-            GmBufs<float> B{sv->K32, jac ? sv->dinv32 : nullptr, sv->Binv32, sv->V32, sv->z32, sv->strip};
+            if (P.precond == OCMP_PRE_CAHOUET_CHABARD && !sv->cc)
+                return fail(OCMP_ERR_ARG, "ocmp_solve: set the Cahouet-Chabard data (ocmp_solver_set_cahouet_chabard)");
+            GmBufs<float> B{sv->K32, jac ? sv->dinv32 : nullptr, sv->Binv32, sv->V32, sv->z32, sv->strip, sv->cc};
             st = gm_dispatch<float>(c, B, b, x, P.maxit, P.inner_tol > 0 ? P.inner_tol : 1e-4, &iters, &outer,
                                     &relres0);
         }

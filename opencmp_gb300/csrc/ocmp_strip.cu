@@ -632,6 +632,21 @@ int strip_create(const ocmp_space_s* s, Strip** out) {
         nxt = std::min<int64_t>(n, std::max<int64_t>(nxt, p->s.back() + 1));
         p->s.push_back(nxt);
     }
+    // consecutive strips merge (the block-tridiagonal structure survives) until a strip holds at
+    // least kMergeMin dofs: narrow bands (a P1 Laplacian's band is one row of vertices) would
+    // otherwise give many small strips, whose sweeps are launch-bound
+    {
+        constexpr int64_t kMergeMin = 1024, kMergeMax = 4096;
+        std::vector<int64_t> merged{0};
+        size_t q = 1;
+        while (q < p->s.size()) {
+            int64_t end = p->s[q++];
+            while (q < p->s.size() && end - merged.back() < kMergeMin && p->s[q] - merged.back() <= kMergeMax)
+                end = p->s[q++];
+            merged.push_back(end);
+        }
+        p->s.swap(merged);
+    }
     p->K = (int)p->s.size() - 1;
     const int K = p->K;
     // every row must reach only its own and the neighbouring strips

@@ -297,7 +297,8 @@ class KrylovSolver:
         p.restart = restart
         p.precond = {'none': LB.PRE_NONE, 'jacobi': LB.PRE_JACOBI, 'local': LB.PRE_JACOBI,
                      'block_jacobi': LB.PRE_BLOCK_JACOBI, 'block': LB.PRE_BLOCK_JACOBI,
-                     'user': LB.PRE_USER, 'strip': LB.PRE_STRIP, 'direct': LB.PRE_STRIP}[str(precond).lower()]
+                     'user': LB.PRE_USER, 'strip': LB.PRE_STRIP, 'direct': LB.PRE_STRIP,
+                     'cahouet_chabard': LB.PRE_CAHOUET_CHABARD}[str(precond).lower()]
         p.precision = LB.MIXED if str(precision).lower() == 'mixed' else LB.FP64
         p.tol, p.maxit, p.inner_tol, p.check_every = tol, maxit, inner_tol, check_every
         self.params = p
@@ -332,6 +333,14 @@ class KrylovSolver:
         o = LB.StripStats()
         LB.call('ocmp_solver_strip_stats', self.h, C.byref(o))
         return {k: getattr(o, k) for k, _ in LB.StripStats._fields_}
+
+    def set_cahouet_chabard(self, pop: 'Matrix', vdinv: torch.Tensor, mpinv: torch.Tensor, alpha: float, beta: float,
+                            tc: float, refactor: bool, stream=None):
+        """Data of precond='cahouet_chabard' (ocmp_solver_set_cahouet_chabard): the pressure operator
+        pop, the inverse velocity diagonal (its length is the velocity dofs), the inverse pressure-mass
+        diagonal and the coefficients; pop is factorised on the first call and when refactor is set."""
+        LB.call('ocmp_solver_set_cahouet_chabard', self.h, pop.h, _ptr(vdinv), _ptr(mpinv), vdinv.numel(), alpha,
+                beta, tc, int(refactor), _stream(stream))
 
     def strip_gemm(self, kind: str):
         """Dense products of the next strip factorisations: 'simt' (FP32 FMA) or 'tensor' (tcgen05)."""

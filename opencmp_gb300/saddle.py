@@ -26,11 +26,14 @@ therefore
     z_p = -(alpha (L_p + delta M_p)^-1 r_p + beta D(M_p)^-1 r_p) / tc^2,   delta = alpha eps / tc,
 
 where delta makes the preconditioner exact on constant pressures (the one mode that L_p does not
-see and that the eps term alone fixes). (L_p + delta M_p)^-1 is applied by an inexact Jacobi-CG
-solve on the pressure space (``ocmp_solve``), so the outer iteration is flexible GMRES (Saad 1993),
-which stores the preconditioned directions. The outer matrix products and the inner CG are the
-library's kernels; the Arnoldi vector algebra of the outer loop (a few hundred iterations per
-solve, against thousands of inner CG iterations) runs as torch tensor operations.
+see and that the eps term alone fixes).
+
+Two implementations. The default runs entirely in the library (``SaddleSolver(impl='library')``):
+GMRES with OCMP_PRE_CAHOUET_CHABARD, the Laplacian solve applied exactly by the strip direct
+factorisation of the pressure operator, so the preconditioner is fixed and plain GMRES suffices.
+The host implementation (``impl='host'``) applies (L_p + delta M_p)^-1 by an inexact Jacobi-CG
+solve (``ocmp_solve``) and therefore runs flexible GMRES (Saad 1993), which stores the
+preconditioned directions; its Arnoldi algebra runs as torch tensor operations.
 """
 from __future__ import annotations
 
@@ -154,17 +157,26 @@ def _diag_positions(space) -> np.ndarray:
 
 
 class SaddleSolver:
-    """FGMRES(m) with the Cahouet-Chabard block-diagonal preconditioner for a Taylor-Hood system
+    """GMRES(m) with the Cahouet-Chabard block-diagonal preconditioner for a Taylor-Hood system
     (``fem.TaylorHood``) assembled into ``A``.
 
-    Per outer iteration: one compound SpMV (``ocmp_spmv``), velocity Jacobi, and one Jacobi-CG solve
-    of (L_p + delta M_p) z = r_p on the pressure space to the relative tolerance ``inner_tol``
-    (``ocmp_solve``; ``precision='mixed'`` runs it as FP32 CG with FP64 refinement). The outer
-    iteration, its residuals and the convergence test are FP64.
+    ``impl='library'`` (the default): the library's GMRES with OCMP_PRE_CAHOUET_CHABARD, the whole
+    iteration on the device. The pressure block's Laplacian solve is exact: the strip direct
+    factorisation of L_p + sigma M_p, sigma = max(delta, 1), computed in FP32 once per pressure
+    operator (delta alone would leave the FP32 factorisation singular on the constant pressure, the
+    mode the outer FP64 GMRES resolves; sigma = 1 keeps the operator's condition near 1/h^2).
+    ``precision='mixed'`` runs the inner GMRES in FP32 with FP64 refinement.
+
+    ``impl='host'``: flexible GMRES on the host (``fgmres``), whose pressure block is an inexact
+    Jacobi-CG solve of (L_p + delta M_p) z = r_p to ``inner_tol`` (``ocmp_solve``), the outer
+    Arnoldi algebra in torch.
     """
 
     def __init__(self, th, A, restart: int = 50, tol: float = 1e-8, maxit: int = 2000, inner_tol: float = 0.1,
-                 inner_maxit: int = 1000, precision: str = 'fp64', eps_p: float = 1e-10):
+                 inner_maxit: int = 1000, precision: str = 'fp64', eps_p: float = 1e-10, impl: str = 'library'):
+        if impl not in ('library', 'host'):
+            raise ValueError("impl is 'library' or 'host'")
+        self.impl = impl
         self.th, self.A = th, A
         self.restart, self.tol, self.maxit = restart, tol, maxit
         self.inner_tol, self.inner_maxit = inner_tol, inner_maxit
@@ -183,24 +195,41 @@ class SaddleSolver:
         self.zp = torch.zeros(th.np, dtype=torch.float64, device='cuda')
         self.inner_iterations = 0
         self.coef = (1.0, 0.0, 1.0)
+        self.lib = None
+        if impl == 'library':
+            self.lib = fem.KrylovSolver(A, method='GMRES', restart=restart, precond='cahouet_chabard',
+                                        precision=precision, tol=tol, maxit=maxit, inner_tol=1e-4, check_every=1)
 
-    def _pressure_operator(self, delta: float):
-        """(Re)assemble L_p + delta M_p and its inner CG solver when delta changes."""
+    def _pressure_operator(self, delta: float) -> bool:
+        """(Re)assemble the pressure operator and, on the host path, its inner CG solver when delta
+        changes; True when it changed."""
         if self.delta == delta:
-            return
-        self.Lp.assemble(fem.make_form(mass=delta, diff=1.0))
-        self.inner = fem.KrylovSolver(self.Lp, method='CG', precond='jacobi', precision=self.precision,
-                                      tol=self.inner_tol, maxit=self.inner_maxit, inner_tol=self.inner_tol)
+            return False
+        if self.impl == 'library':
+            self.Lp.assemble(fem.make_form(mass=max(delta, 1.0), diff=1.0))
+        else:
+            self.Lp.assemble(fem.make_form(mass=delta, diff=1.0))
+            self.inner = fem.KrylovSolver(self.Lp, method='CG', precond='jacobi', precision=self.precision,
+                                          tol=self.inner_tol, maxit=self.inner_maxit, inner_tol=self.inner_tol)
         self.delta = delta
+        return True
 
     def update(self, mass: float, dt: float, nu: float, tcoef: Optional[float] = None):
         """Take the coefficients of the system just assembled into A: the mass coefficient alpha,
         beta = dt nu, and tc = tcoef (default dt); refresh the velocity Jacobi diagonal."""
         tc = dt if tcoef is None else tcoef
         self.coef = (float(mass), float(dt) * float(nu), float(tc))
+        changed = False
         if mass > 0.0:
-            self._pressure_operator(mass * self.eps_p / tc)
+            changed = self._pressure_operator(mass * self.eps_p / tc)
         self.th.block_diag(self.A, self.dinv)
+        if self.lib is not None:
+            if mass <= 0.0:
+                raise NotImplementedError('the library saddle-point solve needs a mass term (transient systems)')
+            self.lib.update()
+            n2 = self.nu2
+            self.lib.set_cahouet_chabard(self.Lp, self.dinv[:n2].contiguous(), self.mp_dinv, self.coef[0],
+                                         self.coef[1], self.coef[2], changed)
 
     def precond(self, r: torch.Tensor, z: torch.Tensor):
         alpha, beta, tc = self.coef
@@ -228,8 +257,12 @@ class SaddleSolver:
         """Solve A x = b on the free dofs from the initial guess x (its constrained entries hold the
         Dirichlet values)."""
         self.inner_iterations = 0
-        info = fgmres(self.matvec, self.precond, b, x, self.free, restart=self.restart, tol=self.tol,
-                      maxit=self.maxit)
+        if self.lib is not None:
+            li = self.lib.solve(b, x, raise_on_fail=False)
+            info = FGMRESInfo(li.status, li.iterations, li.outer_iterations, li.relres0, li.relres)
+        else:
+            info = fgmres(self.matvec, self.precond, b, x, self.free, restart=self.restart, tol=self.tol,
+                          maxit=self.maxit)
         info.inner_iterations = self.inner_iterations
         if raise_on_fail and info.status != LB.OK:
             raise LB.OcmpError(info.status, 'FGMRES (Cahouet-Chabard): relative residual {:.3e} after {} '
