@@ -306,4 +306,4 @@ def test_sell32_krylov_matrix_matches_csr(gpu_lib):
         out[sell] = (x.cpu().numpy(), info.iterations)
     # near the FP32 round-off floor the refinement's inner cycles differ with the summation order
     assert abs(out[True][1] - out[False][1]) <= max(2, 0.15 * out[False][1]), (out[True][1], out[False][1])
-    assert np.linalg.norm(out[True][0] - out[False][0]) <= 1e-9 * np.linalg.norm(out[False][0])
+    assert np.linalg.norm(out[True][0] - out[False][0]) <= 1e-8 * np.linalg.norm(out[False][0])
