@@ -260,12 +260,22 @@ typedef struct {
     int32_t gemm_kind;       /* 0: FP32 SIMT products, 1: tensor-core (tcgen05, 3xTF32) products    */
     double tile_ms;          /* time in the pivot-tile inversions (with ocmp_solver_strip_timing)   */
     double panel_ms;         /* time in the panel kernels (with ocmp_solver_strip_timing)           */
+    int32_t fast_strips;     /* strips whose non-interface block splits into groups of <= 32 dofs   */
+    int32_t schulz_strips;   /* of those, interface inverses by Newton-Schulz from the previous one */
+    int32_t schulz_iterations; /* Newton-Schulz steps in total                                      */
+    int32_t schulz_fallbacks;  /* Newton-Schulz attempts that fell back to Gauss-Jordan             */
 } ocmp_strip_stats_t;
 int ocmp_solver_strip_stats(ocmp_solver_t solver, ocmp_strip_stats_t* out);
 /* time every dense product of the next factorisations with CUDA events (measurement) */
 int ocmp_solver_strip_timing(ocmp_solver_t solver, int32_t on);
 /* dense products of the next factorisations: 0 FP32 SIMT (the default), 1 tensor cores */
 int ocmp_solver_strip_gemm(ocmp_solver_t solver, int32_t kind);
+/* on (the default): a strip whose non-interface dofs N fall into independent groups of at most 32
+ * (a row of DG elements: the elements that do not touch the previous row) inverts those groups one
+ * warp each, forms the interface Schur complement with one dense product and inverts it by
+ * Newton-Schulz iteration started from the previous strip's inverse (Gauss-Jordan when that start
+ * does not converge); off: block Gauss-Jordan over every strip's 128 x 128 tiles */
+int ocmp_solver_strip_schulz(ocmp_solver_t solver, int32_t on);
 /* C = beta C + alpha A B^T in FP32, row-major, K contiguous in A (M x K) and B (N x K): the dense
  * product of the strip factorisation, exposed for tests and measurement. kind 0: FP32 SIMT (K a
  * multiple of 16); kind 1: tcgen05 tensor cores, TF32 products with the 3xTF32 split for FP32

@@ -73,7 +73,9 @@ class SolveInfo(C.Structure):
 class StripStats(C.Structure):
     _fields_ = [('nstrips', C.c_int64), ('max_strip', C.c_int64), ('bytes', C.c_int64), ('factor_ms', C.c_double),
                 ('gemm_ms', C.c_double), ('gemm_flops', C.c_double), ('singular_tiles', C.c_int32),
-                ('gemm_kind', C.c_int32), ('tile_ms', C.c_double), ('panel_ms', C.c_double)]
+                ('gemm_kind', C.c_int32), ('tile_ms', C.c_double), ('panel_ms', C.c_double),
+                ('fast_strips', C.c_int32), ('schulz_strips', C.c_int32), ('schulz_iterations', C.c_int32),
+                ('schulz_fallbacks', C.c_int32)]
 
 
 P = C.c_void_p
@@ -134,6 +136,7 @@ SIGNATURES = {
     'ocmp_solver_strip_timing': [P, I32],
     'ocmp_solver_set_cahouet_chabard': [P, P, P, P, I64, D, D, D, I32, P],
     'ocmp_solver_strip_gemm': [P, I32],
+    'ocmp_solver_strip_schulz': [P, I32],
     'ocmp_dense_gemm_nt': [I32, I32, I32, I32, P, I64, P, I64, P, I64, C.c_float, C.c_float, P],
     'ocmp_guess_create': [I32, C.c_uint64, C.POINTER(P)],
     'ocmp_guess_destroy': [P],

@@ -201,6 +201,7 @@ int strip_add(int64_t n, const T* z, double* x, cudaStream_t st);
 void strip_stats(const Strip* p, ocmp_strip_stats_t* out);
 void strip_set_timing(Strip* p, bool on);
 void strip_set_gemm(Strip* p, int kind);
+void strip_set_schulz(Strip* p, bool on);
 // C = beta C + alpha A B^T on the tensor cores (ocmp_tcgemm.cu): FP32 operands, 3xTF32 products;
 // M, N multiples of 128, K of 32; *err set when a bounded wait gave up
 int tc_gemm_nt(int M, int N, int K, const float* A, int64_t lda, const float* B, int64_t ldb, float* C, int64_t ldc,

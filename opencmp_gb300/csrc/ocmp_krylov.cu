@@ -1614,6 +1614,13 @@ int ocmp_solver_strip_gemm(ocmp_solver_t sv, int32_t kind) {
     return OCMP_OK;
 }
 
+int ocmp_solver_strip_schulz(ocmp_solver_t sv, int32_t on) {
+    if (!sv) return fail(OCMP_ERR_ARG, "ocmp_solver_strip_schulz: null solver");
+    if (!sv->strip) return fail(OCMP_ERR_ARG, "ocmp_solver_strip_schulz: solver not created with OCMP_PRE_STRIP");
+    strip_set_schulz(sv->strip, on != 0);
+    return OCMP_OK;
+}
+
 // Batched GMRES solve of all B systems of the solver's matrix: b and x hold B vectors of ndof.
 int ocmp_solve_batch(ocmp_solver_t sv, const double* b, double* x, void* stream, ocmp_solve_info_t* infos) {
     if (!sv || !b || !x) return fail(OCMP_ERR_ARG, "ocmp_solve_batch: null argument");

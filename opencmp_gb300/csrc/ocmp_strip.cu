@@ -4,8 +4,8 @@
 //
 // The dofs are cut into consecutive strips [s_k, s_k+1) chosen so that the matrix is block
 // tridiagonal over them: strip k's rows reach no further than strip k+1 (greedy over the row
-// bandwidth; a structured mesh whose elements are numbered row by row gives one strip per row of
-// elements). Block elimination over the strips (the block Thomas algorithm) needs, per strip,
+// bandwidth, or, when the pattern repeats with a period, uniform strips of that period: one row of
+// elements of a structured mesh numbered row by row). Block elimination over the strips (the block Thomas algorithm) needs, per strip,
 //     S_k = A_kk - A_k,k-1 S_{k-1}^-1 A_k-1,k,      G_k = S_k^-1,
 // and a solve is a forward sweep y_k = G_k (b_k - A_k,k-1 y_k-1) and a backward sweep
 // x_k = y_k - G_k A_k,k+1 x_k+1. Every G_k is kept explicitly (FP32, dense), so each sweep step is
@@ -20,17 +20,27 @@
 // dominant flops. Since the Schur update only adds to the II block, the N pivots can be eliminated
 // before it:
 //   phase 1 (side streams, all strips independent): fill S_k, eliminate its N tiles;
-//   phase 2 (the caller's stream, strip after strip): S_k[I,I] -= A[I,J] G_k-1[J,J] A[J,I] (two
-//     dense products over the interface, J = the dofs of strip k-1 coupled to strip k), then
-//     eliminate the I tiles.
+//   phase 2 (the chain stream, strip after strip): S_k[I,I] -= A[I,J] G_k-1[J,J] A[J,I] (J = the
+//     dofs of strip k-1 coupled to strip k; A[I,J] and A[J,I] hold a few entries per row, so the
+//     update is two sparse-times-dense kernels over per-dof coupling lists), then eliminate the I
+//     tiles.
 // On a structured triangle mesh half of each strip's elements touch the previous row of elements,
 // so phase 2, the sequential chain, does half of the pivot tiles.
+// Newton-Schulz path, for a strip whose N dofs fall into independent groups of at most 32 (the
+// elements of a row of DG elements that do not touch the previous row): phase 1 inverts the groups
+// (a warp each) and forms the interface complement W0 = S_II - S_IN S_NN^-1 S_NI with one dense
+// product; phase 2 subtracts the Schur update from W0 and inverts it by Newton-Schulz iteration
+// started from the previous strip's interface inverse (two steps on a uniform DG mesh), then
+// assembles G_k from the 2 x 2 block inverse with three dense products.
 // The dense products are C = beta C + alpha A B^T with both operands K-contiguous: FP32 SIMT
 // (sgemm_nt) or the tensor cores (tc_gemm_nt, ocmp_tcgemm.cu).
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <array>
 #include <cmath>
+#include <cstring>
+#include <numeric>
 #include <string>
 #include <vector>
 
@@ -61,23 +71,25 @@ struct Strip {
     int32_t* d_J = nullptr;          // J_k as positions in strip k's order
     int32_t* jrow = nullptr;         // J_k as local dofs
     int32_t* d_pinv = nullptr;       // per dof: its position in its strip's order
-    int32_t* d_Iinv = nullptr;       // per dof: its index in I of its strip, or -1
-    int32_t* d_Jinv = nullptr;       // per dof: its index in J of its strip, or -1
     int32_t* d_lo_ptr = nullptr;     // per dof: CSR positions whose column lies in the previous strip
     int32_t* d_lo_pos = nullptr;
     int32_t* d_hi_ptr = nullptr;     // per dof: CSR positions whose column lies in the next strip
     int32_t* d_hi_pos = nullptr;
     float* d_G = nullptr;            // the explicit strip inverses
-    float* d_Bt = nullptr;           // interface scratch
-    float* d_Cc = nullptr;
-    float* d_Gjj = nullptr;
-    float* d_Tt = nullptr;
-    float* d_U = nullptr;
+    // per I dof (over all strips, indexed like d_I): its couplings to the previous strip's J, as
+    // entries [cptr[i], cptr[i+1]) of (index b in J, CSR position of A[I_i, J_b], of A[J_b, I_i])
+    int32_t* d_cptr = nullptr;
+    int32_t* d_cb = nullptr;
+    int32_t* d_crow = nullptr;
+    int32_t* d_ccol = nullptr;
+    int cmax = 0;                    // longest list
+    float* d_T = nullptr;            // Schur update scratch: T = G_k-1[J, J] A[J, I] (nJ x nIp)
     StripWork work[kSide + 1];       // [0]: the caller's stream, [1..]: side streams
     float* d_r = nullptr;            // solve scratch (one strip)
     int* d_flag = nullptr;           // [0] pivot tiles that were singular or non-finite, [1] a tensor-core
                                      // product whose bounded wait gave up
     int64_t bytes = 0;
+    int64_t schur_flops_pending = 0;
     cudaStream_t side[kSide] = {};
     cudaStream_t chain = nullptr;    // phase 2, at the highest stream priority so that the side streams'
                                      // products never hold the chain's kernels back
@@ -102,6 +114,28 @@ struct Strip {
     double factor_ms = 0, gemm_ms = 0, gemm_flops = 0, gemm_flops_pending = 0;
     int singular = 0;
     int gemm_kind = 0;               // 0: FP32 SIMT, 1: tensor cores (3xTF32)
+    // Newton-Schulz path (strips whose N dofs form small independent groups, e.g. the elements of a
+    // row of DG elements that do not touch the previous row)
+    std::vector<char> fast;          // per strip
+    std::vector<int64_t> gofs;       // per strip: first group in d_gptr
+    std::vector<int> ngrp;           // per strip: groups
+    int32_t* d_gptr = nullptr;       // group offsets into d_gidx (concatenated per strip, each ends with its total)
+    int32_t* d_gidx = nullptr;       // group members: positions in the strip's order (all in N)
+    float* d_Yt[kSide] = {};         // phase 1 scratch per side stream: Y^T
+    float* d_Xa = nullptr;           // chain scratch: Newton-Schulz iterates, residual, transposes
+    float* d_Xb = nullptr;
+    float* d_R = nullptr;
+    float* d_Rt = nullptr;
+    float* d_Xt = nullptr;
+    float* d_Wcur = nullptr;         // the last interface inverse (d_Xa or d_Xb): the next strip's start
+    int wprev_n = 0;                 // its padded size (0: none)
+    bool schulz = true;              // Newton-Schulz path on (off: block Gauss-Jordan throughout)
+    float* d_T1 = nullptr;
+    float* d_Zt = nullptr;
+    unsigned* d_rmax = nullptr;
+    unsigned* h_rmax = nullptr;      // pinned
+    int nfast = 0;
+    int ns_iters = 0, ns_strips = 0, ns_fallbacks = 0;
 };
 
 namespace {
@@ -213,54 +247,46 @@ __global__ void k_fill_strip(int mp, int64_t s0, const int32_t* __restrict__ per
     }
 }
 
-// Interface blocks of the boundary between strip k-1 (start sp) and strip k (start s0):
-// Cc[a, b] = A[I_a, J_b] (rows of strip k, columns of strip k-1) and Bt[a, b] = A[J_b, I_a].
-// Irow / Jrow: the local dofs of I_k and J_k-1.
-__global__ void k_fill_iface(int nI, int nJ, int nJp, int64_t s0, int64_t sp, const int32_t* __restrict__ Irow,
-                             const int32_t* __restrict__ Jrow, const int32_t* __restrict__ Iinv,
-                             const int32_t* __restrict__ Jinv, const int32_t* __restrict__ lo_ptr,
-                             const int32_t* __restrict__ lo_pos, const int32_t* __restrict__ hi_ptr,
-                             const int32_t* __restrict__ hi_pos, const int32_t* __restrict__ col,
-                             const double* __restrict__ vals, const uint8_t* __restrict__ freed, float* __restrict__ Cc,
-                             float* __restrict__ Bt) {
-    const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t < nI) {
-        const int64_t r = s0 + Irow[t];
-        if (!freed[r]) return;
-        for (int32_t q = lo_ptr[r]; q < lo_ptr[r + 1]; q++) {
-            const int32_t k = lo_pos[q];
-            const int64_t c = col[k];
-            const int b = Jinv[c];
-            if (freed[c] && b >= 0) Cc[(int64_t)t * nJp + b] = (float)vals[k];
-        }
-    } else if (t < nI + nJ) {
-        const int bj = t - nI;
-        const int64_t r = sp + Jrow[bj];
-        if (!freed[r]) return;
-        for (int32_t q = hi_ptr[r]; q < hi_ptr[r + 1]; q++) {
-            const int32_t k = hi_pos[q];
-            const int64_t c = col[k];
-            const int a = Iinv[c];
-            if (freed[c] && a >= 0) Bt[(int64_t)a * nJp + bj] = (float)vals[k];
+// Schur update of strip k (rows and columns of its I block, I dofs at global s0 + Irow[i]) from the
+// previous strip's inverse G (its J dofs at positions Jp, local dofs Jrow, strip start sp):
+//   T[b, c] = sum_{(d, A[J_d, I_c]) in list(c)} G[J_b, J_d] A[J_d, I_c]           (k_schur_t)
+//   S[I_a, I_c] -= sum_{(b, A[I_a, J_b]) in list(a)} A[I_a, J_b] T[b, c]           (k_schur_u)
+// An entry counts only when both its row and its column dof are free (the constrained rows and
+// columns of the strips are unit rows and columns).
+__global__ void k_schur_t(int nI, int nIp, int64_t s0, int64_t sp, const int32_t* __restrict__ Irow,
+                          const int32_t* __restrict__ Jrow, const int32_t* __restrict__ Jp,
+                          const int32_t* __restrict__ cptr, const int32_t* __restrict__ cb,
+                          const int32_t* __restrict__ ccol, const double* __restrict__ vals,
+                          const uint8_t* __restrict__ freed, const float* __restrict__ G, int mpG,
+                          float* __restrict__ T) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x, b = blockIdx.y;
+    if (c >= nIp) return;
+    float acc = 0.f;
+    if (c < nI && freed[s0 + Irow[c]]) {
+        const float* g = G + (int64_t)Jp[b] * mpG;
+        for (int32_t e = cptr[c]; e < cptr[c + 1]; e++) {
+            const int d = cb[e];
+            const int32_t q = ccol[e];
+            if (q >= 0 && freed[sp + Jrow[d]]) acc = fmaf(g[Jp[d]], (float)vals[q], acc);
         }
     }
+    T[(int64_t)b * nIp + c] = acc;
 }
 
-// Gjj[a, b] = G[J_a, J_b] (positions in the previous strip's order; zero padding)
-__global__ void k_gather_gjj(int nJ, int nJp, const int32_t* __restrict__ J, const float* __restrict__ G, int mpG,
-                             float* __restrict__ Gjj) {
-    const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    if (t >= (int64_t)nJp * nJp) return;
-    const int a = (int)(t / nJp), b = (int)(t % nJp);
-    Gjj[t] = (a < nJ && b < nJ) ? G[(int64_t)J[a] * mpG + J[b]] : 0.f;
-}
-
-// S[nNp + a, nNp + c] -= U[a, c]: the I block is contiguous in the strip's order
-__global__ void k_sub_block(int nI, int nIp, int nNp, const float* __restrict__ U, int mp, float* __restrict__ S) {
-    const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    if (t >= (int64_t)nI * nI) return;
-    const int a = (int)(t / nI), c = (int)(t % nI);
-    S[(int64_t)(nNp + a) * mp + nNp + c] -= U[(int64_t)a * nIp + c];
+__global__ void k_schur_u(int nI, int nIp, int nNp, int64_t s0, int64_t sp, const int32_t* __restrict__ Irow,
+                          const int32_t* __restrict__ Jrow, const int32_t* __restrict__ cptr,
+                          const int32_t* __restrict__ cb, const int32_t* __restrict__ crow,
+                          const double* __restrict__ vals, const uint8_t* __restrict__ freed,
+                          const float* __restrict__ T, float* __restrict__ S, int mp) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x, a = blockIdx.y;
+    if (c >= nI || !freed[s0 + Irow[a]]) return;
+    float acc = 0.f;
+    for (int32_t e = cptr[a]; e < cptr[a + 1]; e++) {
+        const int b = cb[e];
+        const int32_t q = crow[e];
+        if (q >= 0 && freed[sp + Jrow[b]]) acc = fmaf((float)vals[q], T[(int64_t)b * nIp + c], acc);
+    }
+    S[(int64_t)(nNp + a) * mp + nNp + c] -= acc;
 }
 
 // ------------------------------------------------------------------ block Gauss-Jordan
@@ -425,6 +451,159 @@ __global__ void __launch_bounds__(256) k_panel_finish(float* __restrict__ S, int
     }
 }
 
+// ------------------------------------------------------------------ Newton-Schulz path
+// Inverse of each small group of N dofs (b <= 32), a warp per group, in place in the strip: the
+// group's block is held in shared memory (lane c owns column c), Gauss-Jordan with partial pivoting
+// over the group's rows, rows never moved (as in k_tile_inv).
+constexpr int kGroupWarps = 8;
+__global__ void __launch_bounds__(32 * kGroupWarps) k_group_inv(float* __restrict__ S, int mp, const int32_t* __restrict__ gptr,
+                                                                const int32_t* __restrict__ gidx, int ngroups,
+                                                                int* __restrict__ flag) {
+    __shared__ float tile[kGroupWarps][32][33];
+    __shared__ int pivs[kGroupWarps][32], steps[kGroupWarps][32];
+    const int wl = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int grp = blockIdx.x * kGroupWarps + wl;
+    if (grp >= ngroups) return;
+    const int g0 = gptr[grp], b = gptr[grp + 1] - g0;
+    const int32_t* g = gidx + g0;
+    float(*t)[33] = tile[wl];
+    const int myg = lane < b ? g[lane] : 0;
+    for (int r = 0; r < b; r++) t[r][lane] = lane < b ? S[(int64_t)g[r] * mp + myg] : 0.f;
+    __syncwarp();
+    unsigned used = 0;
+    for (int k = 0; k < b; k++) {
+        // candidates: the unused rows (a NaN entry counts as 0, so every lane agrees on the pivot)
+        float a = -1.f;
+        int bi = 32;
+        if (lane < b && !((used >> lane) & 1u)) {
+            a = fabsf(t[lane][k]);
+            if (!(a >= 0.f)) a = 0.f;
+            bi = lane;
+        }
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) {
+            const float oa = __shfl_xor_sync(0xffffffffu, a, off);
+            const int oi = __shfl_xor_sync(0xffffffffu, bi, off);
+            if (oa > a || (oa == a && oi < bi)) {
+                a = oa;
+                bi = oi;
+            }
+        }
+        const int p = bi < b ? bi : 0;   // b - k >= 1 rows are unused, so bi < b
+        float pv = t[p][k];
+        if (!(fabsf(pv) > 0.f) || !isfinite(pv)) {
+            if (lane == 0) atomicAdd(flag, 1);
+            pv = 1e-30f;
+        }
+        const float d = 1.f / pv;
+        const float colk = lane < b ? t[lane][k] : 0.f;   // column k, row `lane`
+        const float nk = lane < b ? (lane == k ? 1.f : t[p][lane]) * d : 0.f;
+        __syncwarp();
+        for (int r = 0; r < b; r++) {
+            const float f = __shfl_sync(0xffffffffu, colk, r);
+            if (lane < b) t[r][lane] = r == p ? nk : (lane == k ? 0.f : t[r][lane]) - f * nk;
+        }
+        if (lane == 0) {
+            pivs[wl][k] = p;
+            steps[wl][p] = k;
+        }
+        used |= 1u << p;
+        __syncwarp();
+    }
+    if (lane < b) {
+        const int pc = g[pivs[wl][lane]];
+        for (int r = 0; r < b; r++) S[(int64_t)g[steps[wl][r]] * mp + pc] = t[r][lane];
+    }
+}
+
+// Y = X S_NI in place (rows of each group, columns of I): a block per group, a thread per column
+__global__ void __launch_bounds__(128) k_group_y(float* __restrict__ S, int mp, int nNp, int nIp,
+                                                 const int32_t* __restrict__ gptr, const int32_t* __restrict__ gidx) {
+    __shared__ float X[32][33];
+    __shared__ int gs[32];
+    __shared__ float sv[32][129];
+    const int grp = blockIdx.x, tid = threadIdx.x;
+    const int g0 = gptr[grp], b = gptr[grp + 1] - g0;
+    if (tid < b) gs[tid] = gidx[g0 + tid];
+    __syncthreads();
+    for (int e = tid; e < b * b; e += 128) X[e / b][e % b] = S[(int64_t)gs[e / b] * mp + gs[e % b]];
+    __syncthreads();
+    for (int c0 = 0; c0 < nIp; c0 += 128) {
+        const int c = c0 + tid;
+        for (int q = 0; q < b; q++) sv[q][tid] = S[(int64_t)gs[q] * mp + nNp + c];
+        for (int r = 0; r < b; r++) {
+            float acc = 0.f;
+            for (int q = 0; q < b; q++) acc = fmaf(X[r][q], sv[q][tid], acc);
+            S[(int64_t)gs[r] * mp + nNp + c] = acc;
+        }
+    }
+}
+
+// S_IN <- Z = -S_IN X in place (rows i of I, the N columns of each group): a block per group and
+// 128 rows, a thread per row, which reads its row's group entries before writing them
+__global__ void __launch_bounds__(128) k_group_z(float* __restrict__ S, int mp, int nNp, int nIp,
+                                                 const int32_t* __restrict__ gptr, const int32_t* __restrict__ gidx) {
+    __shared__ float X[32][33];
+    __shared__ int gs[32];
+    const int grp = blockIdx.x, tid = threadIdx.x;
+    const int g0 = gptr[grp], b = gptr[grp + 1] - g0;
+    if (tid < b) gs[tid] = gidx[g0 + tid];
+    __syncthreads();
+    for (int e = tid; e < b * b; e += 128) X[e / b][e % b] = S[(int64_t)gs[e / b] * mp + gs[e % b]];
+    __syncthreads();
+    const int i = blockIdx.y * 128 + tid;
+    if (i >= nIp) return;
+    float* row = S + (int64_t)(nNp + i) * mp;
+    float sv[32];
+#pragma unroll
+    for (int q = 0; q < 32; q++) sv[q] = q < b ? row[gs[q < b ? q : 0]] : 0.f;
+    for (int r = 0; r < b; r++) {
+        float acc = 0.f;
+#pragma unroll
+        for (int q = 0; q < 32; q++)
+            if (q < b) acc = fmaf(sv[q], X[q][r], acc);
+        row[gs[r]] = -acc;
+    }
+}
+
+// dst (cols x rows, leading dimension ldd) = src^T (rows x cols, leading dimension lds); 32 x 32 tiles
+__global__ void k_transpose(const float* __restrict__ src, int64_t lds, int rows, int cols, float* __restrict__ dst,
+                            int64_t ldd) {
+    __shared__ float tl[32][33];
+    const int bx = blockIdx.x * 32, by = blockIdx.y * 32, tx = threadIdx.x, ty = threadIdx.y;
+    for (int j = ty; j < 32; j += 8) {
+        const int r = by + j, c = bx + tx;
+        tl[j][tx] = (r < rows && c < cols) ? src[(int64_t)r * lds + c] : 0.f;
+    }
+    __syncthreads();
+    for (int j = ty; j < 32; j += 8) {
+        const int r = bx + j, c = by + tx;   // dst row = src column
+        if (r < cols && c < rows) dst[(int64_t)r * ldd + c] = tl[tx][j];
+    }
+}
+
+// dst = scale * src (rows x cols, leading dimensions) or, with src == null, the identity
+__global__ void k_copy2d(const float* __restrict__ src, int64_t lds, int rows, int cols, float* __restrict__ dst,
+                         int64_t ldd, float scale) {
+    const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (t >= (int64_t)rows * cols) return;
+    const int r = (int)(t / cols), c = (int)(t % cols);
+    dst[(int64_t)r * ldd + c] = src ? scale * src[(int64_t)r * lds + c] : (r == c ? 1.f : 0.f);
+}
+
+// *out = max over rows of sum |A[r, :]| (the infinity norm; non-negative floats order like their
+// bits, NaN above all): a warp per row
+__global__ void k_infnorm(const float* __restrict__ A, int64_t lda, int rows, int cols, unsigned* __restrict__ out) {
+    const int r = blockIdx.x * 8 + (threadIdx.x >> 5), lane = threadIdx.x & 31;
+    if (r >= rows) return;
+    const float* a = A + (int64_t)r * lda;
+    float sm = 0.f;
+    for (int c = lane; c < cols; c += 32) sm += fabsf(a[c]);
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) sm += __shfl_xor_sync(0xffffffffu, sm, off);
+    if (lane == 0) atomicMax(out, sm == sm ? __float_as_uint(sm) : 0x7FFFFFFFu);
+}
+
 // ------------------------------------------------------------------ sweeps
 // z = sc v with sc = scale[j] (the GMRES basis vector into the preconditioner's input)
 template <class T>
@@ -524,14 +703,18 @@ __global__ void k_add_to(int64_t n, const T* __restrict__ z, double* __restrict_
 
 // ------------------------------------------------------------------ host helpers
 void strip_free(Strip* p) {
-    void* ps[] = {p->d_perm, p->d_I, p->d_J, p->jrow, p->d_pinv, p->d_Iinv, p->d_Jinv, p->d_lo_ptr, p->d_lo_pos, p->d_hi_ptr,
-                  p->d_hi_pos, p->d_G, p->d_Bt, p->d_Cc, p->d_Gjj, p->d_Tt, p->d_U, p->d_r, p->d_flag};
+    void* ps[] = {p->d_perm, p->d_I, p->d_J, p->jrow, p->d_pinv, p->d_lo_ptr, p->d_lo_pos, p->d_hi_ptr,
+                  p->d_hi_pos, p->d_G, p->d_cptr, p->d_cb, p->d_crow, p->d_ccol, p->d_T, p->d_r, p->d_flag};
     for (void* q : ps) dfree(q);
     for (auto& w : p->work) {
         dfree(w.P);
         dfree(w.Ck);
         dfree(w.Rt);
     }
+    void* qs[] = {p->d_gptr, p->d_gidx, p->d_Xa, p->d_Xb, p->d_R, p->d_Rt, p->d_Xt, p->d_T1, p->d_Zt, p->d_rmax};
+    for (void* q : qs) dfree(q);
+    for (float* q : p->d_Yt) dfree(q);
+    if (p->h_rmax) cudaFreeHost(p->h_rmax);
     for (cudaEvent_t e : p->ev) cudaEventDestroy(e);
     for (cudaEvent_t e : p->ev_phase1) cudaEventDestroy(e);
     for (cudaEvent_t e : p->fev)
@@ -602,6 +785,109 @@ int gj_tiles(Strip* p, float* S, int mp, int t_begin, int t_end, const StripWork
     return OCMP_OK;
 }
 
+int transpose(const float* src, int64_t lds, int rows, int cols, float* dst, int64_t ldd, cudaStream_t st) {
+    const dim3 g(nblk(cols, 32), nblk(rows, 32)), b(32, 8);
+    OCMP_LAUNCH(k_transpose<<<g, b, 0, st>>>(src, lds, rows, cols, dst, ldd));
+    return OCMP_OK;
+}
+int copy2d(const float* src, int64_t lds, int rows, int cols, float* dst, int64_t ldd, float scale, cudaStream_t st) {
+    OCMP_LAUNCH(k_copy2d<<<nblk((int64_t)rows * cols, 256), 256, 0, st>>>(src, lds, rows, cols, dst, ldd, scale));
+    return OCMP_OK;
+}
+
+// Phase 1 of a strip whose N block is block diagonal (groups of at most 32 positions): X = S_NN^-1
+// group by group, S_NI <- Y = X S_NI, S_II <- W0 = S_II - S_IN Y (one dense product), S_IN <- Z =
+// -S_IN X. The strip then holds [[X, Y], [Z, W0]].
+int phase1_groups(Strip* p, int k, float* S, int q, cudaStream_t ss) {
+    const int mp = p->mp[k], nNp = p->nNp[k], nIp = mp - nNp, ng = p->ngrp[k];
+    const int32_t* gp = p->d_gptr + p->gofs[k];
+    int r = tbegin(p, ss);
+    OCMP_LAUNCH(k_group_inv<<<nblk(ng, kGroupWarps), 32 * kGroupWarps, 0, ss>>>(S, mp, gp, p->d_gidx, ng, p->d_flag));
+    if (!r) r = tend(p, ss, 1);
+    OCMP_LAUNCH(k_group_y<<<ng, 128, 0, ss>>>(S, mp, nNp, nIp, gp, p->d_gidx));
+    if (!r) r = transpose(S + nNp, mp, nNp, nIp, p->d_Yt[q], nNp, ss);
+    if (!r) r = gemm(p, nIp, nIp, nNp, S + (int64_t)nNp * mp, mp, p->d_Yt[q], nNp, S + (int64_t)nNp * mp + nNp, mp, -1.f,
+                     1.f, ss);
+    if (r) return r;
+    OCMP_LAUNCH(k_group_z<<<dim3(ng, nblk(nIp, 128)), 128, 0, ss>>>(S, mp, nNp, nIp, gp, p->d_gidx));
+    return OCMP_OK;
+}
+
+// Inverse of the interface Schur complement W = S_II (n x n, leading dimension mp) into a buffer
+// of the chain (returned in *X, its transpose in d_Xt). Newton-Schulz X <- X + X R, R = I - W X,
+// started from the previous strip's inverse (the interface complements of neighbouring strips of a
+// row-by-row structured mesh are close). The step squares R, so with rho = ||R||_inf read back
+// after each product: rho <= kSchulzTol: X is taken; rho^2 <= kSchulzTol: one more step is taken
+// unchecked; a step that does not reduce rho (or a non-finite rho, or kSchulzMax steps) falls back
+// to block Gauss-Jordan on a copy of W, as does a strip without a start of its size.
+constexpr float kSchulzTol = 1e-5f;
+constexpr int kSchulzMax = 8;
+int invert_interface(Strip* p, const float* W, int mp, int n, float** X, cudaStream_t cs) {
+    float* cur = p->d_Wcur;
+    float* nxt = cur == p->d_Xa ? p->d_Xb : p->d_Xa;
+    bool ok = false;
+    if (p->schulz && cur && p->wprev_n == n) {
+        float rprev = INFINITY;
+        for (int it = 0; it < kSchulzMax; it++) {
+            int r = transpose(cur, n, n, n, p->d_Xt, n, cs);
+            if (!r) r = copy2d(nullptr, 0, n, n, p->d_R, n, 1.f, cs);
+            if (!r) r = gemm(p, n, n, n, W, mp, p->d_Xt, n, p->d_R, n, -1.f, 1.f, cs);
+            if (r) return r;
+            OCMP_CUDA(cudaMemsetAsync(p->d_rmax, 0, sizeof(unsigned), cs));
+            OCMP_LAUNCH(k_infnorm<<<nblk(n, 8), 256, 0, cs>>>(p->d_R, n, n, n, p->d_rmax));
+            OCMP_CUDA(cudaMemcpyAsync(p->h_rmax, p->d_rmax, sizeof(unsigned), cudaMemcpyDeviceToHost, cs));
+            OCMP_CUDA(cudaStreamSynchronize(cs));
+            float rho;
+            std::memcpy(&rho, p->h_rmax, sizeof(float));
+            if (!std::isfinite(rho) || rho >= rprev) break;
+            if (rho <= kSchulzTol) {
+                ok = true;
+                break;
+            }
+            rprev = rho;
+            r = transpose(p->d_R, n, n, n, p->d_Rt, n, cs);
+            if (!r) r = copy2d(cur, n, n, n, nxt, n, 1.f, cs);
+            if (!r) r = gemm(p, n, n, n, cur, n, p->d_Rt, n, nxt, n, 1.f, 1.f, cs);
+            if (r) return r;
+            std::swap(cur, nxt);
+            p->ns_iters++;
+            if (rho * rho <= kSchulzTol) {
+                ok = true;
+                if ((r = transpose(cur, n, n, n, p->d_Xt, n, cs))) return r;
+                break;
+            }
+        }
+        if (ok) p->ns_strips++;
+        else p->ns_fallbacks++;
+    }
+    if (!ok) {
+        if (!cur) cur = p->d_Xa;
+        int r = copy2d(W, mp, n, n, cur, n, 1.f, cs);
+        if (!r) r = gj_tiles(p, cur, n, 0, n, p->work[0], cs);
+        if (!r) r = transpose(cur, n, n, n, p->d_Xt, n, cs);
+        if (r) return r;
+    }
+    p->d_Wcur = cur;
+    p->wprev_n = n;
+    *X = cur;
+    return OCMP_OK;
+}
+
+// Phase 2 of a block-diagonal-N strip after the Schur update: with X_I = W^-1 (W = S_II),
+//   G_II = X_I, G_IN = X_I Z, G_NI = -T, G_NN = X - T Z, T = Y X_I.
+int phase2_groups(Strip* p, int k, float* S, cudaStream_t cs) {
+    const int mp = p->mp[k], nNp = p->nNp[k], n = mp - nNp;
+    float* Wi = nullptr;
+    int r = invert_interface(p, S + (int64_t)nNp * mp + nNp, mp, n, &Wi, cs);
+    if (!r) r = gemm(p, nNp, n, n, S + nNp, mp, p->d_Xt, n, p->d_T1, n, 1.f, 0.f, cs);
+    if (!r) r = transpose(S + (int64_t)nNp * mp, mp, n, nNp, p->d_Zt, n, cs);
+    if (!r) r = gemm(p, nNp, nNp, n, p->d_T1, n, p->d_Zt, n, S, mp, -1.f, 1.f, cs);
+    if (!r) r = gemm(p, n, nNp, n, Wi, n, p->d_Zt, n, S + (int64_t)nNp * mp, mp, 1.f, 0.f, cs);
+    if (!r) r = copy2d(p->d_T1, n, nNp, n, S + nNp, mp, -1.f, cs);
+    if (!r) r = copy2d(Wi, n, n, n, S + (int64_t)nNp * mp + nNp, mp, 1.f, cs);
+    return r;
+}
+
 }  // namespace
 
 int strip_create(const ocmp_space_s* s, Strip** out) {
@@ -631,6 +917,46 @@ int strip_create(const ocmp_space_s* s, Strip** out) {
         }
         nxt = std::min<int64_t>(n, std::max<int64_t>(nxt, p->s.back() + 1));
         p->s.push_back(nxt);
+    }
+    // uniform strips when the pattern repeats with a period w (a structured mesh numbered row by
+    // row of elements): strips of exactly w dofs, each one row, make neighbouring strips' Schur
+    // complements alike (the Newton-Schulz start relies on it) where the greedy strips drift
+    // against the rows. w: the smallest width from half to twice the greedy one for which the
+    // rows of a sample match the rows w further on (same column offsets) and the uniform strips
+    // are block tridiagonal.
+    if (p->s.size() > 4) {
+        std::vector<int64_t> wd;
+        for (size_t q = 2; q + 1 < p->s.size(); q++) wd.push_back(p->s[q] - p->s[q - 1]);
+        std::nth_element(wd.begin(), wd.begin() + wd.size() / 2, wd.end());
+        const int64_t wg = wd[wd.size() / 2];
+        auto same = [&](int64_t r, int64_t w) {
+            const int64_t r2 = r + w;
+            if (rp[r + 1] - rp[r] != rp[r2 + 1] - rp[r2]) return false;
+            for (int64_t e = 0; e < rp[r + 1] - rp[r]; e++)
+                if ((int64_t)col[rp[r2] + e] - r2 != (int64_t)col[rp[r] + e] - r) return false;
+            return true;
+        };
+        auto valid = [&](int64_t w) {
+            for (int64_t r = 0; r < n; r++) {
+                const int64_t k = r / w;
+                if (mn[r] < (k - 1) * w || mx[r] >= (k + 2) * w) return false;
+            }
+            return true;
+        };
+        constexpr int kSample = 64;
+        for (int64_t w = std::max<int64_t>(1, wg / 2); w <= 2 * wg && 3 * w <= n; w++) {
+            int hits = 0;
+            for (int q = 0; q < kSample; q++) {
+                const int64_t r = (n - w - 1) * (2 * q + 1) / (2 * kSample);
+                hits += same(r, w);
+            }
+            if (hits * 8 < kSample * 7 || !valid(w)) continue;
+            std::vector<int64_t> u;
+            for (int64_t b = 0; b < n; b += w) u.push_back(b);
+            u.push_back(n);
+            p->s.swap(u);
+            break;
+        }
     }
     // consecutive strips merge (the block-tridiagonal structure survives) until a strip holds at
     // least kMergeMin dofs: narrow bands (a P1 Laplacian's band is one row of vertices) would
@@ -744,6 +1070,62 @@ int strip_create(const ocmp_space_s* s, Strip** out) {
     std::vector<int32_t> Jp(Jpos.size());
     for (int k = 0; k < K; k++)
         for (int64_t q = p->joff[k]; q < p->joff[k + 1]; q++) Jp[q] = pinv[p->s[k] + Jpos[q]];
+    // strips whose N positions split into independent groups of at most 32 (union-find over the
+    // pattern inside the strip, constrained dofs included, so the groups hold for any constraints),
+    // packed greedily into warps' worth; the padding of N joins as single positions
+    p->fast.assign(K, 0);
+    p->gofs.assign(K + 1, 0);
+    p->ngrp.assign(K, 0);
+    std::vector<int32_t> gptr{0}, gidx;
+    for (int k = 0; k < K; k++) {
+        p->gofs[k] = (int64_t)gptr.size() - 1;
+        const int nN = p->nN[k];
+        if (nN == 0 || p->nI[k] == 0) continue;
+        const int64_t s0 = p->s[k], s1 = p->s[k + 1];
+        std::vector<int> par(nN);
+        std::iota(par.begin(), par.end(), 0);
+        auto find = [&](int a) {
+            while (par[a] != a) a = par[a] = par[par[a]];
+            return a;
+        };
+        for (int q = 0; q < nN; q++) {
+            const int64_t r = s0 + perm[p->poff[k] + q];
+            for (int64_t e = rp[r]; e < rp[r + 1]; e++) {
+                const int64_t c = col[e];
+                if (c < s0 || c >= s1) continue;
+                const int pc = pinv[c];
+                if (pc < nN) {
+                    const int a = find(q), b = find(pc);
+                    if (a != b) par[std::max(a, b)] = std::min(a, b);
+                }
+            }
+        }
+        std::vector<std::vector<int32_t>> comp(nN);
+        bool small = true;
+        for (int q = 0; q < nN && small; q++) {
+            auto& c = comp[find(q)];
+            c.push_back(q);
+            small = c.size() <= 32;
+        }
+        if (!small) continue;
+        for (int q = nN; q < p->nNp[k]; q++) comp.push_back({q});
+        const size_t g0 = gptr.size();
+        int fill = 0;
+        for (const auto& c : comp) {
+            if (c.empty()) continue;
+            if (fill + (int)c.size() > 32) {
+                gptr.push_back((int32_t)gidx.size());
+                fill = 0;
+            }
+            gidx.insert(gidx.end(), c.begin(), c.end());
+            fill += (int)c.size();
+        }
+        gptr.push_back((int32_t)gidx.size());
+        p->ngrp[k] = (int)(gptr.size() - g0);
+        p->fast[k] = 1;
+        p->nfast++;
+    }
+    p->gofs[K] = (int64_t)gptr.size() - 1;
     std::vector<int32_t> lo_ptr(n + 1, 0), hi_ptr(n + 1, 0), lo_pos, hi_pos;
     for (int k = 0; k < K; k++) {
         const int64_t s0 = p->s[k], s1 = p->s[k + 1];
@@ -756,8 +1138,44 @@ int strip_create(const ocmp_space_s* s, Strip** out) {
             hi_ptr[r + 1] = (int32_t)hi_pos.size();
         }
     }
-    const int ifp = std::max(p->nIp_max, p->nJp_max);
-    const int64_t need = total * 4 + (int64_t)5 * ifp * ifp * 4 + (int64_t)(kSide + 1) * (2 * p->mp_max * kNb + kNb * kNb) * 4;
+    // coupling lists of the I dofs to the previous strip's J dofs (the Schur update's sparse factors)
+    std::vector<int32_t> cptr{0}, cb, crow, ccol;
+    for (int k = 0; k < K; k++) {
+        const int64_t s0 = p->s[k];
+        std::vector<std::vector<std::array<int32_t, 3>>> lists(p->nI[k]);
+        if (k > 0) {
+            auto entry = [&](int a, int32_t b) -> std::array<int32_t, 3>& {
+                for (auto& e : lists[a])
+                    if (e[0] == b) return e;
+                lists[a].push_back({b, -1, -1});
+                return lists[a].back();
+            };
+            for (int a = 0; a < p->nI[k]; a++) {
+                const int64_t r = s0 + Ipos[p->ioff[k] + a];
+                for (int64_t q = rp[r]; q < rp[r + 1]; q++)
+                    if (col[q] < s0) entry(a, Jinv[col[q]])[1] = (int32_t)q;
+            }
+            const int64_t sp = p->s[k - 1];
+            for (int64_t d = sp; d < s0; d++)
+                for (int64_t q = rp[d]; q < rp[d + 1]; q++)
+                    if (col[q] >= s0 && col[q] < p->s[k + 1]) entry(Iinv[col[q]], Jinv[d])[2] = (int32_t)q;
+        }
+        for (auto& l : lists) {
+            std::sort(l.begin(), l.end());
+            for (auto& e : l) {
+                cb.push_back(e[0]);
+                crow.push_back(e[1]);
+                ccol.push_back(e[2]);
+            }
+            cptr.push_back((int32_t)cb.size());
+            p->cmax = std::max(p->cmax, (int)l.size());
+        }
+    }
+    const int64_t fast_floats = p->nfast ? (int64_t)5 * p->nIp_max * p->nIp_max +
+                                                (int64_t)(2 + kSide) * p->mp_max * p->nIp_max
+                                          : 0;
+    const int64_t need = total * 4 + (int64_t)p->nJp_max * p->nIp_max * 4 +
+                         (int64_t)(kSide + 1) * (2 * p->mp_max * kNb + kNb * kNb) * 4 + fast_floats * 4;
     size_t fr = 0, tot = 0;
     cudaMemGetInfo(&fr, &tot);
     if ((size_t)need > fr) {
@@ -773,23 +1191,22 @@ int strip_create(const ocmp_space_s* s, Strip** out) {
     U(&p->d_pinv, pinv);
     U(&p->d_I, Ipos);
     U(&p->d_J, Jp);
-    U(&p->d_Iinv, Iinv);
-    U(&p->d_Jinv, Jinv);
     U(&p->d_lo_ptr, lo_ptr);
     U(&p->d_lo_pos, lo_pos);
     U(&p->d_hi_ptr, hi_ptr);
     U(&p->d_hi_pos, hi_pos);
-    p->bytes = total * 4 + (int64_t)(perm.size() + Ipos.size() + Jp.size() + 3 * n + 2 * (n + 1) + lo_pos.size() +
+    p->bytes = total * 4 + (int64_t)(perm.size() + Ipos.size() + Jp.size() + n + 2 * (n + 1) + lo_pos.size() +
                                      hi_pos.size()) * 4;
     auto A = [&](auto** d, size_t cnt) {
         if (!st) st = dalloc(d, cnt);
     };
     A(&p->d_G, (size_t)total);
-    A(&p->d_Bt, (size_t)ifp * ifp);
-    A(&p->d_Cc, (size_t)ifp * ifp);
-    A(&p->d_Gjj, (size_t)ifp * ifp);
-    A(&p->d_Tt, (size_t)ifp * ifp);
-    A(&p->d_U, (size_t)ifp * ifp);
+    U(&p->d_cptr, cptr);
+    U(&p->d_cb, cb);
+    U(&p->d_crow, crow);
+    U(&p->d_ccol, ccol);
+    p->bytes += (int64_t)(cptr.size() + 3 * cb.size()) * 4;
+    A(&p->d_T, (size_t)std::max(1, p->nJp_max * p->nIp_max));
     for (auto& w : p->work) {
         A(&w.P, (size_t)kNb * kNb);
         A(&w.Ck, (size_t)p->mp_max * kNb);
@@ -797,6 +1214,23 @@ int strip_create(const ocmp_space_s* s, Strip** out) {
     }
     A(&p->d_r, (size_t)p->mp_max);
     A(&p->d_flag, 2);
+    if (p->nfast) {
+        const size_t i2 = (size_t)p->nIp_max * p->nIp_max, mi = (size_t)p->mp_max * p->nIp_max;
+        U(&p->d_gptr, gptr);
+        U(&p->d_gidx, gidx);
+        A(&p->d_Xa, i2);
+        A(&p->d_Xb, i2);
+        A(&p->d_R, i2);
+        A(&p->d_Rt, i2);
+        A(&p->d_Xt, i2);
+        A(&p->d_T1, mi);
+        A(&p->d_Zt, mi);
+        for (float*& y : p->d_Yt) A(&y, mi);
+        A(&p->d_rmax, 1);
+        if (!st && cudaMallocHost((void**)&p->h_rmax, sizeof(unsigned)) != cudaSuccess)
+            st = fail(OCMP_ERR_NOMEM, "strip preconditioner: pinned flag");
+        p->bytes += (int64_t)(gptr.size() + gidx.size()) * 4;
+    }
     U(&p->jrow, Jpos);
     p->bytes += (int64_t)Jpos.size() * 4;
     if (!st && (cudaEventCreateWithFlags(&p->fev[0], cudaEventDefault) != cudaSuccess ||
@@ -845,6 +1279,9 @@ int strip_factor(Strip* p, const ocmp_space_s* s, const double* vals, cudaStream
     p->ev_used = 0;
     p->ev_tag.clear();
     p->gemm_flops_pending = 0;
+    p->ns_iters = p->ns_strips = p->ns_fallbacks = 0;
+    p->d_Wcur = nullptr;
+    p->wprev_n = 0;
     OCMP_CUDA(cudaEventRecord(p->fev[0], st));
     OCMP_CUDA(cudaMemsetAsync(p->d_flag, 0, 2 * sizeof(int), st));
     OCMP_CUDA(cudaEventRecord(p->ev_start, st));
@@ -860,7 +1297,8 @@ int strip_factor(Strip* p, const ocmp_space_s* s, const double* vals, cudaStream
         OCMP_CUDA(cudaMemsetAsync(S, 0, sizeof(float) * (size_t)mp * mp, ss));
         OCMP_LAUNCH(k_fill_strip<<<nblk(mp, 128), 128, 0, ss>>>(mp, p->s[k], p->d_perm + p->poff[k], p->d_pinv, s->d_rowptr,
                                                                s->d_col, vals, s->d_free, p->s[k + 1], S));
-        int r = gj_tiles(p, S, mp, 0, p->nNp[k], p->work[1 + q], ss);
+        const int r = p->schulz && p->fast[k] ? phase1_groups(p, k, S, q, ss)
+                                              : gj_tiles(p, S, mp, 0, p->nNp[k], p->work[1 + q], ss);
         if (r) return r;
         OCMP_CUDA(cudaEventRecord(p->ev_phase1[k], ss));
     }
@@ -872,21 +1310,19 @@ int strip_factor(Strip* p, const ocmp_space_s* s, const double* vals, cudaStream
         const int64_t s0 = p->s[k];
         float* S = p->d_G + p->goff[k];
         if (k > 0 && p->nI[k] > 0 && p->nJ[k - 1] > 0) {
-            const int nI = p->nI[k], nJ = p->nJ[k - 1], nIp = pad(nI), nJp = pad(nJ);
-            OCMP_CUDA(cudaMemsetAsync(p->d_Cc, 0, sizeof(float) * (size_t)nIp * nJp, cs));
-            OCMP_CUDA(cudaMemsetAsync(p->d_Bt, 0, sizeof(float) * (size_t)nIp * nJp, cs));
-            OCMP_LAUNCH(k_fill_iface<<<nblk(nI + nJ, 128), 128, 0, cs>>>(
-                nI, nJ, nJp, s0, p->s[k - 1], p->d_I + p->ioff[k], p->jrow + p->joff[k - 1], p->d_Iinv, p->d_Jinv,
-                p->d_lo_ptr, p->d_lo_pos, p->d_hi_ptr, p->d_hi_pos, s->d_col, vals, s->d_free, p->d_Cc, p->d_Bt));
-            OCMP_LAUNCH(k_gather_gjj<<<nblk((int64_t)nJp * nJp, 256), 256, 0, cs>>>(
-                nJ, nJp, p->d_J + p->joff[k - 1], p->d_G + p->goff[k - 1], p->mp[k - 1], p->d_Gjj));
-            // Tt = Bt Gjj^T (= (G_JJ A_JI)^T), U = Cc Tt^T
-            int r = gemm(p, nIp, nJp, nJp, p->d_Bt, nJp, p->d_Gjj, nJp, p->d_Tt, nJp, 1.f, 0.f, cs);
-            if (!r) r = gemm(p, nIp, nIp, nJp, p->d_Cc, nJp, p->d_Tt, nJp, p->d_U, nIp, 1.f, 0.f, cs);
-            if (r) return r;
-            OCMP_LAUNCH(k_sub_block<<<nblk((int64_t)nI * nI, 256), 256, 0, cs>>>(nI, nIp, p->nNp[k], p->d_U, mp, S));
+            const int nI = p->nI[k], nJ = p->nJ[k - 1], nIp = pad(nI);
+            const int64_t sp = p->s[k - 1];
+            const int32_t* Irow = p->d_I + p->ioff[k];
+            const int32_t* Jrow = p->jrow + p->joff[k - 1];
+            const int32_t* cp = p->d_cptr + p->ioff[k];
+            OCMP_LAUNCH(k_schur_t<<<dim3(nblk(nIp, 128), nJ), 128, 0, cs>>>(
+                nI, nIp, s0, sp, Irow, Jrow, p->d_J + p->joff[k - 1], cp, p->d_cb, p->d_ccol, vals, s->d_free,
+                p->d_G + p->goff[k - 1], p->mp[k - 1], p->d_T));
+            OCMP_LAUNCH(k_schur_u<<<dim3(nblk(nI, 128), nI), 128, 0, cs>>>(nI, nIp, p->nNp[k], s0, sp, Irow, Jrow, cp,
+                                                                          p->d_cb, p->d_crow, vals, s->d_free, p->d_T,
+                                                                          S, mp));
         }
-        int r = gj_tiles(p, S, mp, p->nNp[k], mp, p->work[0], cs);
+        const int r = p->schulz && p->fast[k] ? phase2_groups(p, k, S, cs) : gj_tiles(p, S, mp, p->nNp[k], mp, p->work[0], cs);
         if (r) return r;
     }
     OCMP_CUDA(cudaGetLastError());
@@ -999,10 +1435,15 @@ void strip_stats(const Strip* p, ocmp_strip_stats_t* o) {
     o->gemm_kind = p->gemm_kind;
     o->tile_ms = p->part_ms[1];
     o->panel_ms = p->part_ms[2];
+    o->fast_strips = p->schulz ? p->nfast : 0;
+    o->schulz_strips = p->ns_strips;
+    o->schulz_iterations = p->ns_iters;
+    o->schulz_fallbacks = p->ns_fallbacks;
 }
 
 void strip_set_timing(Strip* p, bool on) { p->timing = on; }
 void strip_set_gemm(Strip* p, int kind) { p->gemm_kind = kind; }
+void strip_set_schulz(Strip* p, bool on) { p->schulz = on; }
 
 }  // namespace ocmp
 

@@ -346,6 +346,11 @@ class KrylovSolver:
         """Dense products of the next strip factorisations: 'simt' (FP32 FMA) or 'tensor' (tcgen05)."""
         LB.call('ocmp_solver_strip_gemm', self.h, {'simt': 0, 'tensor': 1}[kind])
 
+    def strip_schulz(self, on: bool = True):
+        """Newton-Schulz interface inverses in the next strip factorisations (on by default; off:
+        block Gauss-Jordan over every strip)."""
+        LB.call('ocmp_solver_strip_schulz', self.h, int(on))
+
     def strip_timing(self, on: bool = True):
         """Time every dense product of the next strip factorisations with CUDA events."""
         LB.call('ocmp_solver_strip_timing', self.h, int(on))

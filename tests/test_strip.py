@@ -116,3 +116,35 @@ def test_strip_preconditioner_refuses_cg_and_unbanded(gpu_lib):
     with pytest.raises(_lib.OcmpError) as e:
         fem.KrylovSolver(A, method='CG', precond='strip')
     assert e.value.status in (_lib.ERR_UNSUPPORTED, _lib.ERR_ARG)
+
+
+@pytest.mark.parametrize('kind', ['simt', 'tensor'])
+def test_strip_newton_schulz_matches_gauss_jordan(gpu_lib, kind):
+    """At 96 x 96 every strip is one row of DG elements: its non-interface dofs (the elements that
+    do not touch the previous row) are independent 6-dof groups, and the interface inverse comes
+    from Newton-Schulz started at the previous strip's. The factorisation with that path and the
+    block Gauss-Jordan one precondition GMRES to the same solution in as many iterations, give or
+    take two."""
+    import torch
+    from opencmp_gb300 import fem
+    sp, A, b = _cd_system(96)
+    sols, iters, stats = {}, {}, {}
+    for on in (False, True):
+        sv = fem.KrylovSolver(A, method='GMRES', restart=50, precond='strip', precision='fp64', tol=1e-10, maxit=200)
+        sv.strip_gemm(kind)
+        sv.strip_schulz(on)
+        sv.update()
+        x = torch.zeros_like(b)
+        info = sv.solve(b, x)
+        assert info.status == 0 and info.relres <= 1e-10
+        stats[on] = sv.strip_stats()
+        assert stats[on]['singular_tiles'] == 0
+        sols[on], iters[on] = x.cpu().numpy(), info.iterations
+    st = stats[True]
+    assert stats[False]['fast_strips'] == 0 and stats[False]['schulz_strips'] == 0
+    assert st['fast_strips'] >= st['nstrips'] - 2, st
+    assert st['schulz_strips'] >= st['fast_strips'] - 2 and st['schulz_fallbacks'] <= 2, st
+    assert st['schulz_iterations'] <= 6 * st['schulz_strips'], st
+    d = np.linalg.norm(sols[True] - sols[False]) / np.linalg.norm(sols[False])
+    assert d <= 1e-8, d
+    assert abs(iters[True] - iters[False]) <= 2, iters
