@@ -71,10 +71,6 @@ struct Strip {
     int32_t* d_J = nullptr;          // J_k as positions in strip k's order
     int32_t* jrow = nullptr;         // J_k as local dofs
     int32_t* d_pinv = nullptr;       // per dof: its position in its strip's order
-    int32_t* d_lo_ptr = nullptr;     // per dof: CSR positions whose column lies in the previous strip
-    int32_t* d_lo_pos = nullptr;
-    int32_t* d_hi_ptr = nullptr;     // per dof: CSR positions whose column lies in the next strip
-    int32_t* d_hi_pos = nullptr;
     float* d_G = nullptr;            // the explicit strip inverses
     // per I dof (over all strips, indexed like d_I): its couplings to the previous strip's J, as
     // entries [cptr[i], cptr[i+1]) of (index b in J, CSR position of A[I_i, J_b], of A[J_b, I_i])
@@ -86,6 +82,18 @@ struct Strip {
     float* d_T = nullptr;            // Schur update scratch: T = G_k-1[J, J] A[J, I] (nJ x nIp)
     StripWork work[kSide + 1];       // [0]: the caller's stream, [1..]: side streams
     float* d_r = nullptr;            // solve scratch (one strip)
+    // ELL coupling lists of the sweeps' right-hand sides: per strip, the forward list (columns in
+    // the previous strip) then the backward one (columns in the next), entry-major; the values and
+    // the free rows' dofs are refreshed by every factorisation
+    std::vector<int64_t> eoff;       // per strip: first entry
+    std::vector<int> elo, ehi;       // per strip: widths
+    int32_t* d_prow = nullptr;       // per position (over all strips): its dof, -1 on padding
+    int32_t* d_rdof = nullptr;       // per position: its dof if free, else -1
+    int32_t* d_erow = nullptr;
+    int32_t* d_ecol = nullptr;       // per entry: the column's dof, -1 on padding
+    int32_t* d_epos = nullptr;       // per entry: its CSR position, -1 on padding
+    float* d_ev = nullptr;           // per entry: the value, 0 where the row or the column is constrained
+    int64_t nell = 0, npos = 0;
     int* d_flag = nullptr;           // [0] pivot tiles that were singular or non-finite, [1] a tensor-core
                                      // product whose bounded wait gave up
     int64_t bytes = 0;
@@ -121,14 +129,15 @@ struct Strip {
     std::vector<int> ngrp;           // per strip: groups
     int32_t* d_gptr = nullptr;       // group offsets into d_gidx (concatenated per strip, each ends with its total)
     int32_t* d_gidx = nullptr;       // group members: positions in the strip's order (all in N)
+    int32_t* d_gcomp = nullptr;      // per member: its component within the group (start << 8 | size)
     float* d_Yt[kSide] = {};         // phase 1 scratch per side stream: Y^T
     float* d_Xa = nullptr;           // chain scratch: Newton-Schulz iterates, residual, transposes
     float* d_Xb = nullptr;
     float* d_R = nullptr;
     float* d_Rt = nullptr;
     float* d_Xt = nullptr;
-    float* d_Wcur = nullptr;         // the last interface inverse (d_Xa or d_Xb): the next strip's start
-    int wprev_n = 0;                 // its padded size (0: none)
+    float* d_H[3] = {};              // the last three interface inverses, newest first (Newton-Schulz starts)
+    int h_n[3] = {0, 0, 0};          // their padded sizes (0: none)
     bool schulz = true;              // Newton-Schulz path on (off: block Gauss-Jordan throughout)
     float* d_T1 = nullptr;
     float* d_Zt = nullptr;
@@ -253,40 +262,63 @@ __global__ void k_fill_strip(int mp, int64_t s0, const int32_t* __restrict__ per
 //   S[I_a, I_c] -= sum_{(b, A[I_a, J_b]) in list(a)} A[I_a, J_b] T[b, c]           (k_schur_u)
 // An entry counts only when both its row and its column dof are free (the constrained rows and
 // columns of the strips are unit rows and columns).
-__global__ void k_schur_t(int nI, int nIp, int64_t s0, int64_t sp, const int32_t* __restrict__ Irow,
-                          const int32_t* __restrict__ Jrow, const int32_t* __restrict__ Jp,
-                          const int32_t* __restrict__ cptr, const int32_t* __restrict__ cb,
-                          const int32_t* __restrict__ ccol, const double* __restrict__ vals,
-                          const uint8_t* __restrict__ freed, const float* __restrict__ G, int mpG,
-                          float* __restrict__ T) {
-    const int c = blockIdx.x * blockDim.x + threadIdx.x, b = blockIdx.y;
+constexpr int kSchurRows = 8;   // rows b of T per thread in k_schur_t
+__global__ void __launch_bounds__(128) k_schur_t(int nI, int nJ, int nIp, int64_t s0, int64_t sp,
+                                                 const int32_t* __restrict__ Irow, const int32_t* __restrict__ Jrow,
+                                                 const int32_t* __restrict__ Jp, const int32_t* __restrict__ cptr,
+                                                 const int32_t* __restrict__ cb, const int32_t* __restrict__ ccol,
+                                                 const double* __restrict__ vals, const uint8_t* __restrict__ freed,
+                                                 const float* __restrict__ G, int mpG, float* __restrict__ T) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x, b0 = blockIdx.y * kSchurRows;
     if (c >= nIp) return;
-    float acc = 0.f;
+    const float* grow[kSchurRows];
+#pragma unroll
+    for (int u = 0; u < kSchurRows; u++) grow[u] = G + (int64_t)Jp[min(b0 + u, nJ - 1)] * mpG;
+    float acc[kSchurRows];
+#pragma unroll
+    for (int u = 0; u < kSchurRows; u++) acc[u] = 0.f;
     if (c < nI && freed[s0 + Irow[c]]) {
-        const float* g = G + (int64_t)Jp[b] * mpG;
         for (int32_t e = cptr[c]; e < cptr[c + 1]; e++) {
             const int d = cb[e];
             const int32_t q = ccol[e];
-            if (q >= 0 && freed[sp + Jrow[d]]) acc = fmaf(g[Jp[d]], (float)vals[q], acc);
+            if (q < 0 || !freed[sp + Jrow[d]]) continue;
+            const float v = (float)vals[q];
+            const int jc = Jp[d];
+#pragma unroll
+            for (int u = 0; u < kSchurRows; u++) acc[u] = fmaf(grow[u][jc], v, acc[u]);
         }
     }
-    T[(int64_t)b * nIp + c] = acc;
+#pragma unroll
+    for (int u = 0; u < kSchurRows; u++)
+        if (b0 + u < nJ) T[(int64_t)(b0 + u) * nIp + c] = acc[u];
 }
 
-__global__ void k_schur_u(int nI, int nIp, int nNp, int64_t s0, int64_t sp, const int32_t* __restrict__ Irow,
-                          const int32_t* __restrict__ Jrow, const int32_t* __restrict__ cptr,
-                          const int32_t* __restrict__ cb, const int32_t* __restrict__ crow,
-                          const double* __restrict__ vals, const uint8_t* __restrict__ freed,
-                          const float* __restrict__ T, float* __restrict__ S, int mp) {
-    const int c = blockIdx.x * blockDim.x + threadIdx.x, a = blockIdx.y;
+// four columns c per thread (T's rows are 16-byte aligned: nIp is a multiple of 128)
+__global__ void __launch_bounds__(128) k_schur_u(int nI, int nIp, int nNp, int64_t s0, int64_t sp,
+                                                 const int32_t* __restrict__ Irow, const int32_t* __restrict__ Jrow,
+                                                 const int32_t* __restrict__ cptr, const int32_t* __restrict__ cb,
+                                                 const int32_t* __restrict__ crow, const double* __restrict__ vals,
+                                                 const uint8_t* __restrict__ freed, const float* __restrict__ T,
+                                                 float* __restrict__ S, int mp) {
+    const int c = 4 * (blockIdx.x * blockDim.x + threadIdx.x), a = blockIdx.y;
     if (c >= nI || !freed[s0 + Irow[a]]) return;
-    float acc = 0.f;
+    float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
     for (int32_t e = cptr[a]; e < cptr[a + 1]; e++) {
         const int b = cb[e];
         const int32_t q = crow[e];
-        if (q >= 0 && freed[sp + Jrow[b]]) acc = fmaf((float)vals[q], T[(int64_t)b * nIp + c], acc);
+        if (q < 0 || !freed[sp + Jrow[b]]) continue;
+        const float v = (float)vals[q];
+        const float4 t = *reinterpret_cast<const float4*>(T + (int64_t)b * nIp + c);
+        acc.x = fmaf(v, t.x, acc.x);
+        acc.y = fmaf(v, t.y, acc.y);
+        acc.z = fmaf(v, t.z, acc.z);
+        acc.w = fmaf(v, t.w, acc.w);
     }
-    S[(int64_t)(nNp + a) * mp + nNp + c] -= acc;
+    float* srow = S + (int64_t)(nNp + a) * mp + nNp + c;
+    const float av[4] = {acc.x, acc.y, acc.z, acc.w};
+#pragma unroll
+    for (int u = 0; u < 4; u++)
+        if (c + u < nI) srow[u] -= av[u];
 }
 
 // ------------------------------------------------------------------ block Gauss-Jordan
@@ -452,14 +484,19 @@ __global__ void __launch_bounds__(256) k_panel_finish(float* __restrict__ S, int
 }
 
 // ------------------------------------------------------------------ Newton-Schulz path
-// Inverse of each small group of N dofs (b <= 32), a warp per group, in place in the strip: the
-// group's block is held in shared memory (lane c owns column c), Gauss-Jordan with partial pivoting
-// over the group's rows, rows never moved (as in k_tile_inv).
+// Inverse of each small group of N dofs (b <= 32 positions, packed from independent components),
+// a warp per group, in place in the strip. Lane c owns column c of the group's block in shared
+// memory; gcomp gives each position its component (start << 8 | size) within the group, and every
+// component is eliminated on its own lanes at the same time: Gauss-Jordan with partial pivoting
+// over the component's rows (each lane of a component scans them for the pivot, so all agree),
+// rows never moved (as in k_tile_inv).
 constexpr int kGroupWarps = 8;
 __global__ void __launch_bounds__(32 * kGroupWarps) k_group_inv(float* __restrict__ S, int mp, const int32_t* __restrict__ gptr,
-                                                                const int32_t* __restrict__ gidx, int ngroups,
+                                                                const int32_t* __restrict__ gidx,
+                                                                const int32_t* __restrict__ gcomp, int ngroups,
                                                                 int* __restrict__ flag) {
     __shared__ float tile[kGroupWarps][32][33];
+    __shared__ float colk[kGroupWarps][32];
     __shared__ int pivs[kGroupWarps][32], steps[kGroupWarps][32];
     const int wl = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int grp = blockIdx.x * kGroupWarps + wl;
@@ -467,75 +504,82 @@ __global__ void __launch_bounds__(32 * kGroupWarps) k_group_inv(float* __restric
     const int g0 = gptr[grp], b = gptr[grp + 1] - g0;
     const int32_t* g = gidx + g0;
     float(*t)[33] = tile[wl];
-    const int myg = lane < b ? g[lane] : 0;
-    for (int r = 0; r < b; r++) t[r][lane] = lane < b ? S[(int64_t)g[r] * mp + myg] : 0.f;
+    const bool in = lane < b;
+    const int cw = in ? gcomp[g0 + lane] : 0;
+    const int cs = cw >> 8, cn = in ? (cw & 255) : 0;
+    if (in) {
+        const int myg = g[lane];
+        for (int r = cs; r < cs + cn; r++) t[r][lane] = S[(int64_t)g[r] * mp + myg];
+    }
+    int maxn = cn;
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) maxn = max(maxn, __shfl_xor_sync(0xffffffffu, maxn, off));
     __syncwarp();
     unsigned used = 0;
-    for (int k = 0; k < b; k++) {
-        // candidates: the unused rows (a NaN entry counts as 0, so every lane agrees on the pivot)
-        float a = -1.f;
-        int bi = 32;
-        if (lane < b && !((used >> lane) & 1u)) {
-            a = fabsf(t[lane][k]);
-            if (!(a >= 0.f)) a = 0.f;
-            bi = lane;
-        }
-#pragma unroll
-        for (int off = 16; off > 0; off >>= 1) {
-            const float oa = __shfl_xor_sync(0xffffffffu, a, off);
-            const int oi = __shfl_xor_sync(0xffffffffu, bi, off);
-            if (oa > a || (oa == a && oi < bi)) {
-                a = oa;
-                bi = oi;
+    for (int k = 0; k < maxn; k++) {
+        const bool act = k < cn;
+        const int pc = cs + k;
+        int p = cs;
+        float nk = 0.f;
+        if (act) {
+            float best = -1.f;
+            for (int r = cs; r < cs + cn; r++) {
+                if ((used >> r) & 1u) continue;
+                float a = fabsf(t[r][pc]);
+                if (!(a >= 0.f)) a = 0.f;
+                if (a > best) {
+                    best = a;
+                    p = r;
+                }
             }
+            float pv = t[p][pc];
+            if (!(fabsf(pv) > 0.f) || !isfinite(pv)) {
+                if (lane == pc) atomicAdd(flag, 1);
+                pv = 1e-30f;
+            }
+            nk = (lane == pc ? 1.f : t[p][lane]) / pv;
+            colk[wl][lane] = t[lane][pc];   // row `lane` is in this component
         }
-        const int p = bi < b ? bi : 0;   // b - k >= 1 rows are unused, so bi < b
-        float pv = t[p][k];
-        if (!(fabsf(pv) > 0.f) || !isfinite(pv)) {
-            if (lane == 0) atomicAdd(flag, 1);
-            pv = 1e-30f;
-        }
-        const float d = 1.f / pv;
-        const float colk = lane < b ? t[lane][k] : 0.f;   // column k, row `lane`
-        const float nk = lane < b ? (lane == k ? 1.f : t[p][lane]) * d : 0.f;
         __syncwarp();
-        for (int r = 0; r < b; r++) {
-            const float f = __shfl_sync(0xffffffffu, colk, r);
-            if (lane < b) t[r][lane] = r == p ? nk : (lane == k ? 0.f : t[r][lane]) - f * nk;
+        if (act) {
+            for (int r = cs; r < cs + cn; r++)
+                t[r][lane] = r == p ? nk : (lane == pc ? 0.f : t[r][lane]) - colk[wl][r] * nk;
+            if (lane == pc) {
+                pivs[wl][pc] = p;
+                steps[wl][p] = pc;
+            }
+            used |= 1u << p;
         }
-        if (lane == 0) {
-            pivs[wl][k] = p;
-            steps[wl][p] = k;
-        }
-        used |= 1u << p;
         __syncwarp();
     }
-    if (lane < b) {
-        const int pc = g[pivs[wl][lane]];
-        for (int r = 0; r < b; r++) S[(int64_t)g[steps[wl][r]] * mp + pc] = t[r][lane];
+    if (in) {
+        const int pcol = g[pivs[wl][lane]];
+        for (int r = cs; r < cs + cn; r++) S[(int64_t)g[steps[wl][r]] * mp + pcol] = t[r][lane];
     }
 }
 
-// Y = X S_NI in place (rows of each group, columns of I): a block per group, a thread per column
-__global__ void __launch_bounds__(128) k_group_y(float* __restrict__ S, int mp, int nNp, int nIp,
+// Y = X S_NI in place (rows of each group, columns of I): a block per group and 128 columns, a
+// thread per column (X is zero between the group's components)
+__global__ void __launch_bounds__(128) k_group_y(float* __restrict__ S, int mp, int nNp,
                                                  const int32_t* __restrict__ gptr, const int32_t* __restrict__ gidx) {
     __shared__ float X[32][33];
     __shared__ int gs[32];
-    __shared__ float sv[32][129];
     const int grp = blockIdx.x, tid = threadIdx.x;
     const int g0 = gptr[grp], b = gptr[grp + 1] - g0;
     if (tid < b) gs[tid] = gidx[g0 + tid];
     __syncthreads();
     for (int e = tid; e < b * b; e += 128) X[e / b][e % b] = S[(int64_t)gs[e / b] * mp + gs[e % b]];
     __syncthreads();
-    for (int c0 = 0; c0 < nIp; c0 += 128) {
-        const int c = c0 + tid;
-        for (int q = 0; q < b; q++) sv[q][tid] = S[(int64_t)gs[q] * mp + nNp + c];
-        for (int r = 0; r < b; r++) {
-            float acc = 0.f;
-            for (int q = 0; q < b; q++) acc = fmaf(X[r][q], sv[q][tid], acc);
-            S[(int64_t)gs[r] * mp + nNp + c] = acc;
-        }
+    const int c = nNp + blockIdx.y * 128 + tid;
+    float sv[32];
+#pragma unroll
+    for (int q = 0; q < 32; q++) sv[q] = q < b ? S[(int64_t)gs[q < b ? q : 0] * mp + c] : 0.f;
+    for (int r = 0; r < b; r++) {
+        float acc = 0.f;
+#pragma unroll
+        for (int q = 0; q < 32; q++)
+            if (q < b) acc = fmaf(X[r][q], sv[q], acc);
+        S[(int64_t)gs[r] * mp + c] = acc;
     }
 }
 
@@ -591,6 +635,18 @@ __global__ void k_copy2d(const float* __restrict__ src, int64_t lds, int rows, i
     dst[(int64_t)r * ldd + c] = src ? scale * src[(int64_t)r * lds + c] : (r == c ? 1.f : 0.f);
 }
 
+// X0 = c1 H1 + c2 H2 + c3 H3 over n4 float4s (c3 = 0: H3 unused)
+__global__ void k_extrap(int64_t n4, const float4* __restrict__ h1, const float4* __restrict__ h2,
+                         const float4* __restrict__ h3, float c1, float c2, float c3, float4* __restrict__ x) {
+    const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (t >= n4) return;
+    const float4 a = h1[t];
+    const float4 b = h2 ? h2[t] : make_float4(0.f, 0.f, 0.f, 0.f);
+    const float4 c = h3 ? h3[t] : make_float4(0.f, 0.f, 0.f, 0.f);
+    x[t] = make_float4(c1 * a.x + c2 * b.x + c3 * c.x, c1 * a.y + c2 * b.y + c3 * c.y, c1 * a.z + c2 * b.z + c3 * c.z,
+                       c1 * a.w + c2 * b.w + c3 * c.w);
+}
+
 // *out = max over rows of sum |A[r, :]| (the infinity norm; non-negative floats order like their
 // bits, NaN above all): a warp per row
 __global__ void k_infnorm(const float* __restrict__ A, int64_t lda, int rows, int cols, unsigned* __restrict__ out) {
@@ -614,77 +670,60 @@ __global__ void k_scale_copy(int64_t n, const T* __restrict__ v, const double* _
     if (i < n) z[i] = (T)((double)v[i] * scale[j]);
 }
 
-// forward right-hand side of strip [s0, s1) in the strip's order: r_p = z_i - sum A[i, c] z_c over
-// the entries whose column lies in the previous strip (z holds that strip's y, and this strip's
-// input); zero on constrained rows and on the padding
+// right-hand side of a strip step in the strip's order, from its ELL list (L entries per position,
+// entry-major: entry e of position q at e * mp + q): forward r_q = z_i - sum A[i, c] z_c over the
+// previous strip's columns, backward r_q = sum A[i, c] z_c over the next strip's; zero on
+// constrained rows and on the padding (rdof = -1)
 template <class T>
-__global__ void k_fwd_rhs(int mp, int64_t s0, const int32_t* __restrict__ perm, const int32_t* __restrict__ lo_ptr,
-                          const int32_t* __restrict__ lo_pos, const int32_t* __restrict__ col,
-                          const double* __restrict__ vals, const uint8_t* __restrict__ freed, const T* __restrict__ z,
-                          float* __restrict__ r, const int* __restrict__ flags) {
+__global__ void k_strip_rhs(int mp, int L, int fwd, const int32_t* __restrict__ rdof, const int32_t* __restrict__ ecol,
+                            const float* __restrict__ ev, const T* __restrict__ z, float* __restrict__ r,
+                            const int* __restrict__ flags) {
     if (flags && flags[0]) return;
-    const int p = blockIdx.x * blockDim.x + threadIdx.x;
-    if (p >= mp) return;
-    const int ld = perm[p];
-    if (ld < 0 || !freed[s0 + ld]) {
-        r[p] = 0.f;
-        return;
-    }
-    const int64_t row = s0 + ld;
-    float acc = (float)z[row];
-    for (int32_t q = lo_ptr[row]; q < lo_ptr[row + 1]; q++) {
-        const int32_t k = lo_pos[q];
-        const int32_t c = col[k];
-        if (freed[c]) acc -= (float)vals[k] * (float)z[c];
-    }
-    r[p] = acc;
-}
-
-// backward right-hand side: r_p = sum A[i, c] z_c over the entries in the next strip
-template <class T>
-__global__ void k_bwd_rhs(int mp, int64_t s0, const int32_t* __restrict__ perm, const int32_t* __restrict__ hi_ptr,
-                          const int32_t* __restrict__ hi_pos, const int32_t* __restrict__ col,
-                          const double* __restrict__ vals, const uint8_t* __restrict__ freed, const T* __restrict__ z,
-                          float* __restrict__ r, const int* __restrict__ flags) {
-    if (flags && flags[0]) return;
-    const int p = blockIdx.x * blockDim.x + threadIdx.x;
-    if (p >= mp) return;
-    const int ld = perm[p];
-    if (ld < 0 || !freed[s0 + ld]) {
-        r[p] = 0.f;
-        return;
-    }
-    const int64_t row = s0 + ld;
+    const int q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= mp) return;
+    const int row = rdof[q];
     float acc = 0.f;
-    for (int32_t q = hi_ptr[row]; q < hi_ptr[row + 1]; q++) {
-        const int32_t k = hi_pos[q];
-        const int32_t c = col[k];
-        if (freed[c]) acc += (float)vals[k] * (float)z[c];
+    for (int e = 0; e < L; e++) {
+        const int cc = ecol[(int64_t)e * mp + q];
+        if (cc >= 0) acc = fmaf(ev[(int64_t)e * mp + q], (float)z[cc], acc);
     }
-    r[p] = acc;
+    r[q] = row < 0 ? 0.f : (fwd ? (float)z[row] - acc : acc);
 }
 
-// z_i = (G r)_p (mode 0) or z_i -= (G r)_p (mode 1), i = the local dof at position p; a warp per
-// row, 16-byte loads (mp is a multiple of 128)
+// z_i = (G r)_p (mode 0) or z_i -= (G r)_p (mode 1), i = the local dof at position p. A block of
+// 8 warps takes 8 rows, a warp per row; r is staged in shared memory, and each lane keeps eight
+// 16-byte loads of G in flight (streamed past L1). mp is a multiple of 128.
+constexpr int kGemvDepth = 8;
 template <class T>
 __global__ void __launch_bounds__(256) k_strip_gemv(int mp, int64_t s0, const int32_t* __restrict__ perm,
                                                     const float* __restrict__ G, const float* __restrict__ r,
                                                     T* __restrict__ z, int mode, const int* __restrict__ flags) {
+    extern __shared__ float4 rs[];
     if (flags && flags[0]) return;
+    const int nq = mp / 4;
+    const float4* r4 = reinterpret_cast<const float4*>(r);
+    for (int i = threadIdx.x; i < nq; i += blockDim.x) rs[i] = r4[i];
+    __syncthreads();
     const int row = blockIdx.x * 8 + (threadIdx.x >> 5), lane = threadIdx.x & 31;
     if (row >= mp) return;
     const int ld = perm[row];
     if (ld < 0) return;
     const float4* g = reinterpret_cast<const float4*>(G + (int64_t)row * mp);
-    const float4* rv = reinterpret_cast<const float4*>(r);
     float acc = 0.f;
-    for (int q = lane; q < mp / 4; q += 32) {
-        const float4 a = __ldg(g + q);
-        const float4 b = __ldg(rv + q);
-        acc = fmaf(a.x, b.x, acc);
-        acc = fmaf(a.y, b.y, acc);
-        acc = fmaf(a.z, b.z, acc);
-        acc = fmaf(a.w, b.w, acc);
+    for (int q0 = lane; q0 < nq; q0 += 32 * kGemvDepth) {
+        float4 a[kGemvDepth];
+#pragma unroll
+        for (int u = 0; u < kGemvDepth; u++)
+            if (q0 + 32 * u < nq) a[u] = __ldcs(g + q0 + 32 * u);
+#pragma unroll
+        for (int u = 0; u < kGemvDepth; u++)
+            if (q0 + 32 * u < nq) {
+                const float4 b = rs[q0 + 32 * u];
+                acc = fmaf(a[u].x, b.x, acc);
+                acc = fmaf(a[u].y, b.y, acc);
+                acc = fmaf(a[u].z, b.z, acc);
+                acc = fmaf(a[u].w, b.w, acc);
+            }
     }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
@@ -701,17 +740,35 @@ __global__ void k_add_to(int64_t n, const T* __restrict__ z, double* __restrict_
     if (i < n) x[i] += (double)z[i];
 }
 
+// the ELL right-hand-side values and the free rows' dofs of every strip, after an assembly
+__global__ void k_ell_refresh(int64_t nent, const int32_t* __restrict__ erow, const int32_t* __restrict__ ecol,
+                              const int32_t* __restrict__ epos, const double* __restrict__ vals,
+                              const uint8_t* __restrict__ freed, float* __restrict__ ev, int64_t npos,
+                              const int32_t* __restrict__ prow, int32_t* __restrict__ rdof) {
+    const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (t < nent) {
+        const int32_t q = epos[t];
+        ev[t] = (q >= 0 && freed[erow[t]] && freed[ecol[t]]) ? (float)vals[q] : 0.f;
+    }
+    if (t < npos) {
+        const int32_t d = prow[t];
+        rdof[t] = (d >= 0 && freed[d]) ? d : -1;
+    }
+}
+
 // ------------------------------------------------------------------ host helpers
 void strip_free(Strip* p) {
-    void* ps[] = {p->d_perm, p->d_I, p->d_J, p->jrow, p->d_pinv, p->d_lo_ptr, p->d_lo_pos, p->d_hi_ptr,
-                  p->d_hi_pos, p->d_G, p->d_cptr, p->d_cb, p->d_crow, p->d_ccol, p->d_T, p->d_r, p->d_flag};
+    void* ps[] = {p->d_perm, p->d_I, p->d_J, p->jrow, p->d_pinv, p->d_G, p->d_cptr, p->d_cb, p->d_crow, p->d_ccol, p->d_T, p->d_r, p->d_flag};
     for (void* q : ps) dfree(q);
     for (auto& w : p->work) {
         dfree(w.P);
         dfree(w.Ck);
         dfree(w.Rt);
     }
-    void* qs[] = {p->d_gptr, p->d_gidx, p->d_Xa, p->d_Xb, p->d_R, p->d_Rt, p->d_Xt, p->d_T1, p->d_Zt, p->d_rmax};
+    void* qs2[] = {p->d_prow, p->d_rdof, p->d_erow, p->d_ecol, p->d_epos, p->d_ev};
+    for (void* q : qs2) dfree(q);
+    void* qs[] = {p->d_gptr, p->d_gidx, p->d_gcomp, p->d_Xa, p->d_Xb, p->d_R, p->d_Rt, p->d_Xt, p->d_T1, p->d_Zt, p->d_rmax,
+                  p->d_H[0], p->d_H[1], p->d_H[2]};
     for (void* q : qs) dfree(q);
     for (float* q : p->d_Yt) dfree(q);
     if (p->h_rmax) cudaFreeHost(p->h_rmax);
@@ -802,9 +859,10 @@ int phase1_groups(Strip* p, int k, float* S, int q, cudaStream_t ss) {
     const int mp = p->mp[k], nNp = p->nNp[k], nIp = mp - nNp, ng = p->ngrp[k];
     const int32_t* gp = p->d_gptr + p->gofs[k];
     int r = tbegin(p, ss);
-    OCMP_LAUNCH(k_group_inv<<<nblk(ng, kGroupWarps), 32 * kGroupWarps, 0, ss>>>(S, mp, gp, p->d_gidx, ng, p->d_flag));
+    OCMP_LAUNCH(k_group_inv<<<nblk(ng, kGroupWarps), 32 * kGroupWarps, 0, ss>>>(S, mp, gp, p->d_gidx, p->d_gcomp, ng,
+                                                                              p->d_flag));
     if (!r) r = tend(p, ss, 1);
-    OCMP_LAUNCH(k_group_y<<<ng, 128, 0, ss>>>(S, mp, nNp, nIp, gp, p->d_gidx));
+    OCMP_LAUNCH(k_group_y<<<dim3(ng, nIp / 128), 128, 0, ss>>>(S, mp, nNp, gp, p->d_gidx));
     if (!r) r = transpose(S + nNp, mp, nNp, nIp, p->d_Yt[q], nNp, ss);
     if (!r) r = gemm(p, nIp, nIp, nNp, S + (int64_t)nNp * mp, mp, p->d_Yt[q], nNp, S + (int64_t)nNp * mp + nNp, mp, -1.f,
                      1.f, ss);
@@ -815,18 +873,29 @@ int phase1_groups(Strip* p, int k, float* S, int q, cudaStream_t ss) {
 
 // Inverse of the interface Schur complement W = S_II (n x n, leading dimension mp) into a buffer
 // of the chain (returned in *X, its transpose in d_Xt). Newton-Schulz X <- X + X R, R = I - W X,
-// started from the previous strip's inverse (the interface complements of neighbouring strips of a
-// row-by-row structured mesh are close). The step squares R, so with rho = ||R||_inf read back
-// after each product: rho <= kSchulzTol: X is taken; rho^2 <= kSchulzTol: one more step is taken
-// unchecked; a step that does not reduce rho (or a non-finite rho, or kSchulzMax steps) falls back
-// to block Gauss-Jordan on a copy of W, as does a strip without a start of its size.
+// started from the previous strips' interface inverses extrapolated along the strips (quadratic
+// from three, linear from two, the last one alone; the interface complements of the strips of a
+// row-by-row structured mesh vary smoothly from row to row). The step squares R, so with
+// rho = ||R||_inf read back after each product: rho <= kSchulzTol: X is taken; rho^2 <= kSchulzTol:
+// one more step is taken unchecked; a step that does not reduce rho (or a non-finite rho, or
+// kSchulzMax steps) falls back to block Gauss-Jordan on a copy of W, as does a strip without a
+// previous inverse of its size.
 constexpr float kSchulzTol = 1e-5f;
 constexpr int kSchulzMax = 8;
 int invert_interface(Strip* p, const float* W, int mp, int n, float** X, cudaStream_t cs) {
-    float* cur = p->d_Wcur;
-    float* nxt = cur == p->d_Xa ? p->d_Xb : p->d_Xa;
+    float* cur = p->d_Xa;
+    float* nxt = p->d_Xb;
+    int hist = 0;
+    while (hist < 3 && p->h_n[hist] == n) hist++;
     bool ok = false;
-    if (p->schulz && cur && p->wprev_n == n) {
+    if (p->schulz && hist > 0) {
+        const int64_t n4 = (int64_t)n * n / 4;
+        const float c[3][3] = {{1.f, 0.f, 0.f}, {2.f, -1.f, 0.f}, {3.f, -3.f, 1.f}};
+        const float* cc = c[hist - 1];
+        OCMP_LAUNCH(k_extrap<<<nblk(n4, 256), 256, 0, cs>>>(
+            n4, reinterpret_cast<const float4*>(p->d_H[0]), hist > 1 ? reinterpret_cast<const float4*>(p->d_H[1]) : nullptr,
+            hist > 2 ? reinterpret_cast<const float4*>(p->d_H[2]) : nullptr, cc[0], cc[1], cc[2],
+            reinterpret_cast<float4*>(cur)));
         float rprev = INFINITY;
         for (int it = 0; it < kSchulzMax; it++) {
             int r = transpose(cur, n, n, n, p->d_Xt, n, cs);
@@ -861,14 +930,20 @@ int invert_interface(Strip* p, const float* W, int mp, int n, float** X, cudaStr
         else p->ns_fallbacks++;
     }
     if (!ok) {
-        if (!cur) cur = p->d_Xa;
         int r = copy2d(W, mp, n, n, cur, n, 1.f, cs);
         if (!r) r = gj_tiles(p, cur, n, 0, n, p->work[0], cs);
         if (!r) r = transpose(cur, n, n, n, p->d_Xt, n, cs);
         if (r) return r;
     }
-    p->d_Wcur = cur;
-    p->wprev_n = n;
+    // the new inverse joins the history, the oldest buffer taking it
+    float* h = p->d_H[2];
+    p->d_H[2] = p->d_H[1];
+    p->d_H[1] = p->d_H[0];
+    p->d_H[0] = h;
+    p->h_n[2] = p->h_n[1];
+    p->h_n[1] = p->h_n[0];
+    p->h_n[0] = n;
+    OCMP_CUDA(cudaMemcpyAsync(h, cur, sizeof(float) * (size_t)n * n, cudaMemcpyDeviceToDevice, cs));
     *X = cur;
     return OCMP_OK;
 }
@@ -1076,7 +1151,7 @@ int strip_create(const ocmp_space_s* s, Strip** out) {
     p->fast.assign(K, 0);
     p->gofs.assign(K + 1, 0);
     p->ngrp.assign(K, 0);
-    std::vector<int32_t> gptr{0}, gidx;
+    std::vector<int32_t> gptr{0}, gidx, gcomp;
     for (int k = 0; k < K; k++) {
         p->gofs[k] = (int64_t)gptr.size() - 1;
         const int nN = p->nN[k];
@@ -1118,6 +1193,7 @@ int strip_create(const ocmp_space_s* s, Strip** out) {
                 fill = 0;
             }
             gidx.insert(gidx.end(), c.begin(), c.end());
+            for (size_t e = 0; e < c.size(); e++) gcomp.push_back((fill << 8) | (int32_t)c.size());
             fill += (int)c.size();
         }
         gptr.push_back((int32_t)gidx.size());
@@ -1171,7 +1247,7 @@ int strip_create(const ocmp_space_s* s, Strip** out) {
             p->cmax = std::max(p->cmax, (int)l.size());
         }
     }
-    const int64_t fast_floats = p->nfast ? (int64_t)5 * p->nIp_max * p->nIp_max +
+    const int64_t fast_floats = p->nfast ? (int64_t)8 * p->nIp_max * p->nIp_max +
                                                 (int64_t)(2 + kSide) * p->mp_max * p->nIp_max
                                           : 0;
     const int64_t need = total * 4 + (int64_t)p->nJp_max * p->nIp_max * 4 +
@@ -1191,12 +1267,7 @@ int strip_create(const ocmp_space_s* s, Strip** out) {
     U(&p->d_pinv, pinv);
     U(&p->d_I, Ipos);
     U(&p->d_J, Jp);
-    U(&p->d_lo_ptr, lo_ptr);
-    U(&p->d_lo_pos, lo_pos);
-    U(&p->d_hi_ptr, hi_ptr);
-    U(&p->d_hi_pos, hi_pos);
-    p->bytes = total * 4 + (int64_t)(perm.size() + Ipos.size() + Jp.size() + n + 2 * (n + 1) + lo_pos.size() +
-                                     hi_pos.size()) * 4;
+    p->bytes = total * 4 + (int64_t)(perm.size() + Ipos.size() + Jp.size() + n) * 4;
     auto A = [&](auto** d, size_t cnt) {
         if (!st) st = dalloc(d, cnt);
     };
@@ -1214,25 +1285,88 @@ int strip_create(const ocmp_space_s* s, Strip** out) {
     }
     A(&p->d_r, (size_t)p->mp_max);
     A(&p->d_flag, 2);
+    {
+        // ELL coupling lists of the sweeps' right-hand sides
+        std::vector<int64_t> eoff(K + 1, 0);
+        std::vector<int> elo(K, 0), ehi(K, 0);
+        std::vector<int32_t> prow, erow, ecol, epos;
+        for (int k = 0; k < K; k++) {
+            const int mpk = p->mp[k];
+            const int64_t s0 = p->s[k];
+            for (int q = 0; q < mpk; q++) {
+                const int ld = perm[p->poff[k] + q];
+                prow.push_back(ld < 0 ? -1 : (int32_t)(s0 + ld));
+                if (ld < 0) continue;
+                const int64_t r = s0 + ld;
+                elo[k] = std::max(elo[k], lo_ptr[r + 1] - lo_ptr[r]);
+                ehi[k] = std::max(ehi[k], hi_ptr[r + 1] - hi_ptr[r]);
+            }
+            eoff[k] = (int64_t)erow.size();
+            for (int part = 0; part < 2; part++) {
+                const int L = part == 0 ? elo[k] : ehi[k];
+                const std::vector<int32_t>& ptr = part == 0 ? lo_ptr : hi_ptr;
+                const std::vector<int32_t>& pos = part == 0 ? lo_pos : hi_pos;
+                for (int e = 0; e < L; e++)
+                    for (int q = 0; q < mpk; q++) {
+                        const int ld = perm[p->poff[k] + q];
+                        const int64_t r = ld < 0 ? -1 : s0 + ld;
+                        const bool has = ld >= 0 && ptr[r] + e < ptr[r + 1];
+                        const int32_t cp = has ? pos[ptr[r] + e] : -1;
+                        erow.push_back(ld < 0 ? 0 : (int32_t)r);
+                        ecol.push_back(has ? col[cp] : -1);
+                        epos.push_back(cp);
+                    }
+            }
+        }
+        eoff[K] = (int64_t)erow.size();
+        p->eoff = eoff;
+        p->elo = elo;
+        p->ehi = ehi;
+        p->nell = (int64_t)erow.size();
+        p->npos = (int64_t)prow.size();
+        U(&p->d_prow, prow);
+        U(&p->d_erow, erow);
+        U(&p->d_ecol, ecol);
+        U(&p->d_epos, epos);
+        A(&p->d_rdof, prow.size());
+        A(&p->d_ev, std::max<size_t>(1, erow.size()));
+        p->bytes += (int64_t)(prow.size() * 2 + erow.size() * 4) * 4;
+    }
     if (p->nfast) {
         const size_t i2 = (size_t)p->nIp_max * p->nIp_max, mi = (size_t)p->mp_max * p->nIp_max;
         U(&p->d_gptr, gptr);
         U(&p->d_gidx, gidx);
+        U(&p->d_gcomp, gcomp);
         A(&p->d_Xa, i2);
         A(&p->d_Xb, i2);
         A(&p->d_R, i2);
         A(&p->d_Rt, i2);
         A(&p->d_Xt, i2);
+        for (float*& h : p->d_H) A(&h, i2);
         A(&p->d_T1, mi);
         A(&p->d_Zt, mi);
         for (float*& y : p->d_Yt) A(&y, mi);
         A(&p->d_rmax, 1);
         if (!st && cudaMallocHost((void**)&p->h_rmax, sizeof(unsigned)) != cudaSuccess)
             st = fail(OCMP_ERR_NOMEM, "strip preconditioner: pinned flag");
-        p->bytes += (int64_t)(gptr.size() + gidx.size()) * 4;
+        p->bytes += (int64_t)(gptr.size() + 2 * gidx.size()) * 4;
     }
     U(&p->jrow, Jpos);
     p->bytes += (int64_t)Jpos.size() * 4;
+    // every buffer a kernel of the factorisation or the sweeps dereferences must exist
+    if (!st) {
+        const void* need_ptr[] = {p->d_perm, p->d_pinv, p->d_G, p->d_cptr, p->d_T, p->d_r, p->d_flag, p->d_prow, p->d_rdof,
+                                  p->d_ev, p->work[0].P, p->work[0].Ck, p->work[0].Rt};
+        bool ok = std::all_of(std::begin(need_ptr), std::end(need_ptr), [](const void* q) { return q != nullptr; });
+        if (p->nfast) {
+            const void* fast_ptr[] = {p->d_gptr, p->d_gidx, p->d_gcomp, p->d_Xa, p->d_Xb, p->d_R, p->d_Rt, p->d_Xt,
+                                      p->d_H[0], p->d_H[1], p->d_H[2], p->d_T1, p->d_Zt, p->d_Yt[0], p->d_Yt[1],
+                                      p->d_Yt[2], p->d_rmax, p->h_rmax};
+            ok = ok && std::all_of(std::begin(fast_ptr), std::end(fast_ptr), [](const void* q) { return q != nullptr; });
+        }
+        if (p->nell) ok = ok && p->d_erow && p->d_ecol && p->d_epos;
+        if (!ok) st = fail(OCMP_ERR_NOMEM, "strip preconditioner: a work buffer was not allocated");
+    }
     if (!st && (cudaEventCreateWithFlags(&p->fev[0], cudaEventDefault) != cudaSuccess ||
                 cudaEventCreateWithFlags(&p->fev[1], cudaEventDefault) != cudaSuccess ||
                 cudaEventCreateWithFlags(&p->ev_start, cudaEventDisableTiming) != cudaSuccess))
@@ -1256,7 +1390,11 @@ int strip_create(const ocmp_space_s* s, Strip** out) {
     if (!st) {
         if (cudaFuncSetAttribute(k_tile_inv, cudaFuncAttributeMaxDynamicSharedMemorySize, kTileSmem) != cudaSuccess ||
             cudaFuncSetAttribute(k_panel_prep, cudaFuncAttributeMaxDynamicSharedMemorySize, kPrepSmem) != cudaSuccess ||
-            cudaFuncSetAttribute(k_panel_finish, cudaFuncAttributeMaxDynamicSharedMemorySize, kFinishSmem) != cudaSuccess)
+            cudaFuncSetAttribute(k_panel_finish, cudaFuncAttributeMaxDynamicSharedMemorySize, kFinishSmem) != cudaSuccess ||
+            cudaFuncSetAttribute(k_strip_gemv<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, 4 * p->mp_max) !=
+                cudaSuccess ||
+            cudaFuncSetAttribute(k_strip_gemv<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, 4 * p->mp_max) !=
+                cudaSuccess)
             st = fail(OCMP_ERR_CUDA, "strip preconditioner: shared-memory attribute");
     }
     if (st) {
@@ -1280,10 +1418,14 @@ int strip_factor(Strip* p, const ocmp_space_s* s, const double* vals, cudaStream
     p->ev_tag.clear();
     p->gemm_flops_pending = 0;
     p->ns_iters = p->ns_strips = p->ns_fallbacks = 0;
-    p->d_Wcur = nullptr;
-    p->wprev_n = 0;
+    for (int& h : p->h_n) h = 0;
     OCMP_CUDA(cudaEventRecord(p->fev[0], st));
     OCMP_CUDA(cudaMemsetAsync(p->d_flag, 0, 2 * sizeof(int), st));
+    {
+        const int64_t nt = std::max(p->nell, p->npos);
+        OCMP_LAUNCH(k_ell_refresh<<<nblk(nt, 256), 256, 0, st>>>(p->nell, p->d_erow, p->d_ecol, p->d_epos, vals, s->d_free,
+                                                                  p->d_ev, p->npos, p->d_prow, p->d_rdof));
+    }
     OCMP_CUDA(cudaEventRecord(p->ev_start, st));
     for (int q = 0; q < kSide; q++) OCMP_CUDA(cudaStreamWaitEvent(p->side[q], p->ev_start, 0));
     cudaStream_t cs = p->chain;
@@ -1315,13 +1457,15 @@ int strip_factor(Strip* p, const ocmp_space_s* s, const double* vals, cudaStream
             const int32_t* Irow = p->d_I + p->ioff[k];
             const int32_t* Jrow = p->jrow + p->joff[k - 1];
             const int32_t* cp = p->d_cptr + p->ioff[k];
-            OCMP_LAUNCH(k_schur_t<<<dim3(nblk(nIp, 128), nJ), 128, 0, cs>>>(
-                nI, nIp, s0, sp, Irow, Jrow, p->d_J + p->joff[k - 1], cp, p->d_cb, p->d_ccol, vals, s->d_free,
+            OCMP_LAUNCH(k_schur_t<<<dim3(nblk(nIp, 128), nblk(nJ, kSchurRows)), 128, 0, cs>>>(
+                nI, nJ, nIp, s0, sp, Irow, Jrow, p->d_J + p->joff[k - 1], cp, p->d_cb, p->d_ccol, vals, s->d_free,
                 p->d_G + p->goff[k - 1], p->mp[k - 1], p->d_T));
-            OCMP_LAUNCH(k_schur_u<<<dim3(nblk(nI, 128), nI), 128, 0, cs>>>(nI, nIp, p->nNp[k], s0, sp, Irow, Jrow, cp,
-                                                                          p->d_cb, p->d_crow, vals, s->d_free, p->d_T,
-                                                                          S, mp));
+            OCMP_LAUNCH(k_schur_u<<<dim3(nblk(nI, 4 * 128), nI), 128, 0, cs>>>(nI, nIp, p->nNp[k], s0, sp, Irow, Jrow,
+                                                                              cp, p->d_cb, p->d_crow, vals, s->d_free,
+                                                                              p->d_T, S, mp));
         }
+        if (!p->fast[k])
+            for (int& h : p->h_n) h = 0;
         const int r = p->schulz && p->fast[k] ? phase2_groups(p, k, S, cs) : gj_tiles(p, S, mp, p->nNp[k], mp, p->work[0], cs);
         if (r) return r;
     }
@@ -1354,23 +1498,19 @@ int strip_factor(Strip* p, const ocmp_space_s* s, const double* vals, cudaStream
 namespace {
 // the two sweeps, in place on z (input: the vector to precondition)
 template <class T>
-void sweeps(Strip* p, const ocmp_space_s* s, const double* vals, T* z, const int* flags, cudaStream_t st) {
+void sweeps(Strip* p, T* z, const int* flags, cudaStream_t st) {
     const int K = p->K;
-    for (int k = 0; k < K; k++) {
-        const int mp = p->mp[k];
-        const int32_t* pm = p->d_perm + p->poff[k];
-        OCMP_LAUNCH(k_fwd_rhs<T><<<nblk(mp, 256), 256, 0, st>>>(mp, p->s[k], pm, p->d_lo_ptr, p->d_lo_pos, s->d_col,
-                                                               vals, s->d_free, z, p->d_r, flags));
-        OCMP_LAUNCH(k_strip_gemv<T><<<nblk(mp, 8), 256, 0, st>>>(mp, p->s[k], pm, p->d_G + p->goff[k], p->d_r, z, 0,
-                                                                flags));
-    }
-    for (int k = K - 2; k >= 0; k--) {
-        const int mp = p->mp[k];
-        const int32_t* pm = p->d_perm + p->poff[k];
-        OCMP_LAUNCH(k_bwd_rhs<T><<<nblk(mp, 256), 256, 0, st>>>(mp, p->s[k], pm, p->d_hi_ptr, p->d_hi_pos, s->d_col,
-                                                               vals, s->d_free, z, p->d_r, flags));
-        OCMP_LAUNCH(k_strip_gemv<T><<<nblk(mp, 8), 256, 0, st>>>(mp, p->s[k], pm, p->d_G + p->goff[k], p->d_r, z, 1,
-                                                                flags));
+    for (int pass = 0; pass < 2; pass++) {
+        for (int step = 0; step < (pass == 0 ? K : K - 1); step++) {
+            const int k = pass == 0 ? step : K - 2 - step;
+            const int mp = p->mp[k];
+            const int L = pass == 0 ? p->elo[k] : p->ehi[k];
+            const int64_t e0 = p->eoff[k] + (pass == 0 ? 0 : (int64_t)p->elo[k] * mp);
+            OCMP_LAUNCH(k_strip_rhs<T><<<nblk(mp, 128), 128, 0, st>>>(mp, L, pass == 0, p->d_rdof + p->poff[k],
+                                                                     p->d_ecol + e0, p->d_ev + e0, z, p->d_r, flags));
+            OCMP_LAUNCH(k_strip_gemv<T><<<nblk(mp, 8), 256, sizeof(float) * mp, st>>>(
+                mp, p->s[k], p->d_perm + p->poff[k], p->d_G + p->goff[k], p->d_r, z, pass, flags));
+        }
     }
 }
 }  // namespace
@@ -1395,7 +1535,7 @@ int strip_apply(Strip* p, const ocmp_space_s* s, const double* vals, const T* v,
         cudaGraph_t g;
         const unsigned long long l0 = g_launches.load();
         OCMP_CUDA(cudaStreamBeginCapture(p->cap, cudaStreamCaptureModeThreadLocal));
-        sweeps<T>(p, s, vals, z, flags, p->cap);
+        sweeps<T>(p, z, flags, p->cap);
         OCMP_CUDA(cudaStreamEndCapture(p->cap, &g));
         p->gkernels[gi] = g_launches.load() - l0;
         g_launches.fetch_sub(p->gkernels[gi]);
