@@ -523,10 +523,15 @@ def run_ins(args):
 
 
 def run_batched(args):
-    """512 independent steady 2D convection-diffusion problems (one step = assemble + solve all)."""
+    """Config 4: 512 independent steady 2D convection-diffusion problems of 12 (mesh, order) classes
+    (n in {16, 32, 64, 128}, H1 p in {1, 2, 3}). One step = assemble every instance (one batched
+    assembly per class) and solve all of them with one solver group: every GMRES kernel launched once
+    over all 512 uneven instances (ocmp_group_solve), FP32 inner GMRES + FP64 refinement, one restart
+    cycle replayed from a CUDA graph. Recorded beside it: the same classes as 12 batched solves on 12
+    host threads and streams, and the plain FP64 loop over instances."""
     import concurrent.futures as cf
     import torch
-    from opencmp_gb300 import fem, mesh as M, build
+    from opencmp_gb300 import fem, mesh as M, build, _lib
     build.build()
     torch.cuda.set_device(0)
     rng = np.random.default_rng(0)
@@ -553,25 +558,90 @@ def run_batched(args):
         fem.assemble_rhs(sp, forms[0], fem.make_rhs(src_const=1.0), b1)
         sv = fem.KrylovSolver(A, method='GMRES', restart=args.restart_batch, precision='mixed', tol=tol,
                               maxit=20000, inner_tol=1e-4)
-        sv.set_graph(True)
         C.append(dict(n=n, p=p, idx=idx, space=sp, forms=forms, A=A, b=b1.repeat(len(idx)),
-                      x=torch.zeros(len(idx) * sp.ndof, dtype=torch.float64, device='cuda'), sv=sv,
-                      stream=torch.cuda.Stream()))
+                      x=torch.zeros(len(idx) * sp.ndof, dtype=torch.float64, device='cuda'), sv=sv))
     total_dofs = sum(c['space'].ndof * len(c['idx']) for c in C)
+    group = fem.KrylovGroup([c['sv'] for c in C])
+    bs = [c['b'] for c in C]
+    xs = [c['x'] for c in C]
+
+    def group_step():
+        for c in C:
+            c['A'].assemble_batch(c['forms'])
+            c['sv'].update()
+            c['x'].zero_()
+        return group.solve(bs, xs, raise_on_fail=False)
+
+    for _ in range(args.warmup):
+        group_step()
+    torch.cuda.synchronize()
+    l0 = _lib.load().ocmp_launch_count()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(args.steps):
+        infos = group_step()
+    e1.record()
+    torch.cuda.synchronize()
+    t_b = e0.elapsed_time(e1) * 1e-3 / args.steps
+    launches = int(_lib.load().ocmp_launch_count() - l0)
+    # end to end: right-hand sides from pinned host memory, solutions back to it, every step
+    b_host = [b.cpu().pin_memory() for b in bs]
+    x_host = [torch.empty(x.numel(), dtype=torch.float64, pin_memory=True) for x in xs]
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        for b, bh in zip(bs, b_host):
+            b.copy_(bh, non_blocking=True)
+        group_step()
+        for x, xh in zip(xs, x_host):
+            xh.copy_(x, non_blocking=True)
+        torch.cuda.synchronize()
+    t_e2e = (time.perf_counter() - t0) / args.steps
+    # algorithmic HBM bytes of the Krylov iterations each instance ran (FP32 SpMV: 4-byte value and
+    # column per entry, x read, y written; classical Gram-Schmidt step j of a GMRES(m) cycle: about
+    # 2 j + 4 vector passes, j averaging m / 2) and of its FP64 residuals (one per cycle: 12 bytes
+    # per entry and 24 per row)
+    mm = args.restart_batch
+    alg = 0.0
+    k = 0
+    for c in C:
+        nd, nz = c['space'].ndof, c['space'].nnz
+        for _ in c['idx']:
+            it = infos[k].iterations
+            cyc = max(1, -(-it // mm))
+            alg += it * (8.0 * nz + 8.0 * nd + 4.0 * (mm + 4) * nd) + cyc * (12.0 * nz + 24.0 * nd)
+            k += 1
+    try:
+        with open(os.path.join(ROOT, 'MEASURED_PEAKS.json')) as fh:
+            peak, peak_kind = float(json.load(fh)['hbm_gbs']), 'measured'
+    except Exception:
+        peak, peak_kind = 6800.0, 'fallback'
+    achieved = alg / t_b / 1e9
+
+    # the same classes as 12 batched solves on 12 host threads (one stream each), for the record
+    for c in C:
+        c['stream'] = torch.cuda.Stream()
 
     def run_class(c):
         with torch.cuda.stream(c['stream']):
             c['A'].assemble_batch(c['forms'], stream=c['stream'])
             c['sv'].update(stream=c['stream'])
             c['x'].zero_()
-            return c['sv'].solve_batch(c['b'], c['x'], stream=c['stream'])
+            return c['sv'].solve_batch(c['b'], c['x'], stream=c['stream'], raise_on_fail=False)
 
     pool = cf.ThreadPoolExecutor(max_workers=len(C))
 
-    def batched_step():
+    def class_step():
         res = list(pool.map(run_class, C))
         torch.cuda.synchronize()
         return res
+
+    class_step()
+    t0 = time.perf_counter()
+    for _ in range(max(1, min(args.steps, 3))):
+        cres = class_step()
+    t_c = (time.perf_counter() - t0) / max(1, min(args.steps, 3))
+    cinf = [i for r in cres for i in r]
 
     # plain FP64 loop over instances: one matrix, one GMRES solve at a time
     plain = []
@@ -582,47 +652,56 @@ def run_batched(args):
         plain.append((c, A1, sv1, torch.zeros(c['space'].ndof, dtype=torch.float64, device='cuda')))
 
     def plain_step():
-        infos = []
+        out = []
         for c, A1, sv1, x1 in plain:
             b1 = c['b'][:c['space'].ndof]
             for f in c['forms']:
                 A1.assemble(f)
                 sv1.update()
                 x1.zero_()
-                infos.append(sv1.solve(b1, x1))
+                out.append(sv1.solve(b1, x1, raise_on_fail=False))
         torch.cuda.synchronize()
-        return infos
+        return out
 
-    for _ in range(args.warmup):
-        batched_step()
     plain_step()
-    t0 = time.perf_counter()
-    for _ in range(args.steps):
-        res = batched_step()
-    t_b = (time.perf_counter() - t0) / args.steps
     t0 = time.perf_counter()
     psteps = max(1, min(args.steps, 3))
     for _ in range(psteps):
         pinf = plain_step()
     t_p = (time.perf_counter() - t0) / psteps
-    infos = [i for r in res for i in r]
     line = {'metric': METRIC + ' (batched instances)', 'value': total_dofs / t_b, 'unit': 'DOF/s', 'n_gpus': 1,
             'steps': args.steps, 'warmup': args.warmup, 'ms_per_step': t_b * 1e3, 'higher_is_better': True,
             'scaling': 'weak', 'vs_baseline': None, 'dtype': 'f64+f32', 'data': 'synthetic',
             'config': {'workload': '{} steady 2D convection-diffusion instances, n in {{16,32,64,128}}, H1 p in {{1,2,3}}, '
                                    'eps log-uniform [1e-3,1], |w|=1, f=1, Dirichlet 0, seed 0; GMRES({}) + Jacobi to '
-                                   '1e-8'.format(N, args.restart_batch),
-                       'classes': len(C), 'total_dofs': total_dofs},
-            'optimised': {'kind': 'batched kernels per (mesh, order) class, one stream per class, FP32 inner GMRES + '
-                                  'FP64 refinement, restart cycles replayed from CUDA graphs',
+                                   '1e-8; assembly + solve per step'.format(N, args.restart_batch),
+                       'classes': len(C), 'total_dofs': total_dofs,
+                       'l2': 'instances and bases exceed L2 together (no flush)'},
+            'optimised': {'kind': 'one solver group over all instances: every GMRES kernel launched once for all {} '
+                                  'uneven instances, FP32 inner GMRES + FP64 refinement, restart cycle from a CUDA '
+                                  'graph'.format(N),
                           'max_relres': float(max(i.relres for i in infos)),
                           'converged': int(sum(1 for i in infos if i.status == 0)),
-                          'iters_mean': float(np.mean([i.iterations for i in infos]))},
+                          'iters_mean': float(np.mean([i.iterations for i in infos])),
+                          'iters_max': int(max(i.iterations for i in infos))},
+            'per_class_threads': {'value': total_dofs / t_c, 'unit': 'DOF/s', 'ms_per_step': t_c * 1e3,
+                                  'kind': '12 batched solves (one per class) on 12 host threads and streams',
+                                  'converged': int(sum(1 for i in cinf if i.status == 0))},
             'plain_fp64': {'value': total_dofs / t_p, 'unit': 'DOF/s', 'ms_per_step': t_p * 1e3,
                            'kind': 'loop over instances, FP64 GMRES',
                            'converged': int(sum(1 for i in pinf if i.status == 0)),
                            'iters_mean': float(np.mean([i.iterations for i in pinf]))},
-            'speedup_vs_plain_fp64': t_p / t_b}
+            'speedup_vs_plain_fp64': t_p / t_b,
+            'e2e': {'value': total_dofs / t_e2e, 'unit': 'DOF/s',
+                    'h2d_bytes_per_step': int(sum(8 * b.numel() for b in bs)),
+                    'd2h_bytes_per_step': int(sum(8 * x.numel() for x in xs))},
+            'roofline': {'bound': 'hbm', 'kernel': 'whole group solve (gx_spmv, gx_dots, gx_orth, gx_combine, gx_resid)',
+                         'achieved': achieved, 'peak': peak, 'unit': 'GB/s', 'frac': achieved / peak,
+                         'peak_kind': peak_kind + ' HBM copy',
+                         'bytes': 'algorithmic bytes of the iterations each instance ran, over the step time '
+                                  '(assembly included in the time)',
+                         'traffic': None},
+            'gpu_launches': launches}
     print(json.dumps(line), flush=True)
 
 

@@ -223,6 +223,26 @@ int ocmp_solve(ocmp_solver_t solver, const double* b_dev, double* x_dev, void* s
  * blockIdx.y) and instances that have converged return immediately. */
 int ocmp_solve_batch(ocmp_solver_t solver, const double* b_dev, double* x_dev, void* stream,
                      ocmp_solve_info_t* infos);
+/* Solver groups: uneven instances in one kernel sequence. The instances of several GMRES solvers
+ * (each a single or batched matrix of its own space: different sizes, orders and patterns) are
+ * solved together: every kernel of the GMRES iteration is launched once over all of them, a fixed
+ * grid striding over a device list of (instance, block) pairs of the instances still iterating
+ * (each instance's share proportional to its rows, the rows per thread of its SpMV from its
+ * space's autotuned choice; the list shrinks after every restart cycle), one restart cycle
+ * replayed from a CUDA graph. Each instance keeps its own Krylov space, tolerance and
+ * convergence test; converged instances return at the top of every kernel. No kernel waits on
+ * another block: reductions end in the last block to finish. Members must be GMRES with point
+ * Jacobi (or no) preconditioning, CSR Krylov matrices, and share restart, precision and maxit.
+ * ocmp_group_solve takes one right-hand side and solution array per member (its instances one
+ * after another) and fills infos for every instance in member order. The group borrows the
+ * members' buffers: do not solve a member on its own while its group is in use. Replaces the
+ * per-instance loop over opencmp/solvers solve calls (one Solver.solve per run directory) with one
+ * call; no counterpart in the reference beyond that loop. */
+typedef struct ocmp_group_s* ocmp_group_t;
+int ocmp_group_create(const ocmp_solver_t* solvers, int32_t count, ocmp_group_t* out);
+int ocmp_group_solve(ocmp_group_t group, const double* const* b_dev, double* const* x_dev, void* stream,
+                     ocmp_solve_info_t* infos);
+int ocmp_group_destroy(ocmp_group_t group);
 /* Replay each GMRES restart cycle (m iterations, the x update and the next FP64 residual) from a
  * CUDA graph captured on first use (re-captured when b, x or the stream change). */
 int ocmp_solver_set_graph(ocmp_solver_t solver, int32_t on);

@@ -105,6 +105,9 @@ SIGNATURES = {
     'ocmp_matrix_create_batch': [P, I32, I32, C.POINTER(P)],
     'ocmp_assemble_matrix_batch': [P, P, P],
     'ocmp_solve_batch': [P, P, P, P, P],
+    'ocmp_group_create': [C.POINTER(P), I32, C.POINTER(P)],
+    'ocmp_group_solve': [P, C.POINTER(P), C.POINTER(P), P, P],
+    'ocmp_group_destroy': [P],
     'ocmp_solver_set_graph': [P, I32],
     'ocmp_matrix_destroy': [P],
     'ocmp_matrix_values': [P, C.POINTER(P), C.POINTER(P)],

@@ -29,6 +29,32 @@ namespace ocmp {
 struct Bat {
     int64_t n, nnz, V, part, st, flags, scale, H, red, cnt;
 };
+// One instance of a solver group (ocmp_group_*): its system and its slice of its member solver's
+// GMRES buffers. The group's kernels stride a fixed grid over a list of (instance, block) pairs
+// of the instances still iterating: block k of gbn (reduction kernels) or of sbn (SpMV).
+struct GInst {
+    int64_t n;
+    const int32_t* rp;
+    const int32_t* col;
+    const uint8_t* freed;
+    const int32_t* lift_ptr;
+    const int32_t* lift_pos;
+    const double* A64;   // FP64 matrix values (residuals)
+    const void* K;       // Krylov matrix values (T)
+    const void* dinv;    // T: D^-1 of the final update, or null
+    void* V;             // T: (m + 1) x n basis
+    double* part;
+    unsigned* cnt;
+    double* st;
+    int* flags;
+    double* scale;
+    double* H;           // Hessenberg, then cos/sin/g
+    double* red;
+    const double* b;
+    double* x;
+    int gbn, sbn;
+    int cfg;             // SpMV rows: 0 (2, 4), 1 (4, 4), 2 (4, 8), 3 (8, 4), 4 (8, 8), 5 (16, 8) threads per row, loads in flight
+};
 }  // namespace ocmp
 
 // Cahouet-Chabard block preconditioner of a Taylor-Hood saddle-point system [u | p]
@@ -112,6 +138,29 @@ struct ocmp_solver_s {
     const double* g_b = nullptr;
     const double* g_x = nullptr;
     cudaStream_t g_stream = nullptr;
+};
+
+// A group of GMRES solvers whose instances (every system of every member, members of different
+// sizes and patterns) are solved by one kernel sequence.
+struct ocmp_group_s {
+    std::vector<ocmp_solver_s*> members;
+    std::vector<int> first;          // per member: its first instance
+    int ninst = 0, m = 0, maxit = 0;
+    bool mixed = false;
+    std::vector<ocmp::GInst> h_inst;
+    ocmp::GInst* d_inst = nullptr;
+    int2* d_glist = nullptr;         // (instance, block) pairs of the active instances: reduction kernels
+    int2* d_slist = nullptr;         // the same for the SpMV
+    int* d_nact = nullptr;           // [0] pairs in d_glist, [1] in d_slist
+    int2* h_glist = nullptr;         // pinned staging of the lists
+    int2* h_slist = nullptr;
+    int* h_nact = nullptr;
+    int gtot = 0, stot = 0;          // pairs of all instances
+    int grid[2][6] = {};             // resident grid per kernel and precision: [FP32, FP64][spmv, dots, orth,
+                                     // combine, resid, -]
+    cudaStream_t gstream = nullptr;  // capture stream
+    cudaGraphExec_t gexec = nullptr; // one restart cycle over all instances
+    unsigned long long graph_kernels = 0;
 };
 
 namespace ocmp {
@@ -517,12 +566,13 @@ __device__ __forceinline__ double warp_sum(double v) {
     return v;
 }
 
-// true in every thread of the block that finishes last; resets the counter for the next launch
-__device__ __forceinline__ bool finish_last(unsigned* cnt) {
+// true in every thread of the block that finishes last of nblocks; resets the counter for the next
+// launch
+__device__ __forceinline__ bool finish_last(unsigned* cnt, unsigned nblocks) {
     __shared__ bool last;
     __threadfence();
     __syncthreads();
-    if (threadIdx.x == 0) last = atomicAdd(cnt, 1u) == gridDim.x - 1;
+    if (threadIdx.x == 0) last = atomicAdd(cnt, 1u) == nblocks - 1;
     __syncthreads();
     if (last) {
         __threadfence();
@@ -587,32 +637,24 @@ __device__ void givens_step(int m, int j, double hn, double* __restrict__ H, dou
 // mode 2: measure only (S_RES)
 // mode 3: mode 0 and mode 1 in the same pass (the first cycle of a solve); the lift A_fD x_D is
 //         summed over the precomputed lift list only
+// (the kernel bodies below take the block's index bx within its instance and the instance's block
+// count gx in place of blockIdx.x / gridDim.x: the batched kernels pass those, the group kernels
+// an instance's share of a grid over several instances)
 template <class T, int TPR, int U>
-__global__ void __launch_bounds__(256) gm_resid(int64_t n, const int32_t* __restrict__ rp,
-                                                const int32_t* __restrict__ col, const double* __restrict__ A,
-                                                const uint8_t* __restrict__ freed, const double* __restrict__ b,
-                                                const double* __restrict__ x, T* __restrict__ V0,
-                                                double* __restrict__ part, unsigned* __restrict__ cnt, double* st,
-                                                int* flags, double* scale, double* csg, int m, int mode,
-                                                const int32_t* __restrict__ lift_ptr,
-                                                const int32_t* __restrict__ lift_pos, Bat bt) {
-    const int64_t ib = blockIdx.y;
-    A += ib * bt.nnz;
-    b += ib * bt.n;
-    x += ib * bt.n;
-    if (V0) V0 += ib * bt.V;
-    part += ib * bt.part;
-    cnt += ib * bt.cnt;
-    st += ib * bt.st;
-    flags += ib * bt.flags;
-    scale += ib * bt.scale;
-    csg += ib * bt.H;
+__device__ __forceinline__ void gm_resid_body(int bx, int gx, int64_t n, const int32_t* __restrict__ rp,
+                                              const int32_t* __restrict__ col, const double* __restrict__ A,
+                                              const uint8_t* __restrict__ freed, const double* __restrict__ b,
+                                              const double* __restrict__ x, T* __restrict__ V0,
+                                              double* __restrict__ part, unsigned* __restrict__ cnt, double* st,
+                                              int* flags, double* scale, double* csg, int m, int mode,
+                                              const int32_t* __restrict__ lift_ptr,
+                                              const int32_t* __restrict__ lift_pos) {
     if (mode == 1 && flags[F_OUTER]) return;  // this instance has converged
 
     constexpr int RT = 256 / TPR;
     const int lane = threadIdx.x % TPR;
     double acc = 0, accd = 0;
-    for (int64_t t0 = (int64_t)blockIdx.x * RT; t0 < n; t0 += (int64_t)gridDim.x * RT) {
+    for (int64_t t0 = (int64_t)bx * RT; t0 < n; t0 += (int64_t)gx * RT) {
         const int64_t r = t0 + threadIdx.x / TPR;
         int32_t a = 0, e = 0;
         if (r < n) {
@@ -662,16 +704,16 @@ __global__ void __launch_bounds__(256) gm_resid(int64_t n, const int32_t* __rest
             t += sh[w];
             td += shd[w];
         }
-        part[blockIdx.x] = t;
-        part[gridDim.x + blockIdx.x] = td;
+        part[bx] = t;
+        part[gx + bx] = td;
     }
-    if (!finish_last(cnt)) return;
+    if (!finish_last(cnt, gx)) return;
     __shared__ double tot, totd;
     if (threadIdx.x < 32) {
         double q = 0, qd = 0;
-        for (int bb = threadIdx.x; bb < (int)gridDim.x; bb += 32) {
+        for (int bb = threadIdx.x; bb < gx; bb += 32) {
             q += __ldcg(part + bb);
-            qd += __ldcg(part + gridDim.x + bb);
+            qd += __ldcg(part + gx + bb);
         }
         q = warp_sum(q);
         qd = warp_sum(qd);
@@ -719,26 +761,35 @@ __global__ void __launch_bounds__(256) gm_resid(int64_t n, const int32_t* __rest
     st[S_TARGET] = fmax(kTargetMargin * st[S_OUTERTOL] * st[S_NB], st[S_INNER] * beta);
 }
 
+template <class T, int TPR, int U>
+__global__ void __launch_bounds__(256) gm_resid(int64_t n, const int32_t* __restrict__ rp,
+                                                const int32_t* __restrict__ col, const double* __restrict__ A,
+                                                const uint8_t* __restrict__ freed, const double* __restrict__ b,
+                                                const double* __restrict__ x, T* __restrict__ V0,
+                                                double* __restrict__ part, unsigned* __restrict__ cnt, double* st,
+                                                int* flags, double* scale, double* csg, int m, int mode,
+                                                const int32_t* __restrict__ lift_ptr,
+                                                const int32_t* __restrict__ lift_pos, Bat bt) {
+    const int64_t ib = blockIdx.y;
+    gm_resid_body<T, TPR, U>(blockIdx.x, gridDim.x, n, rp, col, A + ib * bt.nnz, freed, b + ib * bt.n, x + ib * bt.n,
+                             V0 ? V0 + ib * bt.V : nullptr, part + ib * bt.part, cnt + ib * bt.cnt, st + ib * bt.st,
+                             flags + ib * bt.flags, scale + ib * bt.scale, csg + ib * bt.H, m, mode, lift_ptr, lift_pos);
+}
+
 // d_k = V_k . w for k <= j, and |w|^2 as d_{j+1} when with_norm; w = V[j+1]. The second
 // Gram-Schmidt pass (gated = 1) runs only when F_REORTH is set.
 template <class T>
-__global__ void __launch_bounds__(256) gm_dots(int64_t n, int j, const T* __restrict__ V, double* __restrict__ part,
-                                               int nbp, unsigned* __restrict__ cnt, double* __restrict__ red,
-                                               const int* __restrict__ flags, int gated, int with_norm, Bat bt) {
-    const int64_t ib = blockIdx.y;
-    V += ib * bt.V;
-    part += ib * bt.part;
-    cnt += ib * bt.cnt;
-    red += ib * bt.red;
-    flags += ib * bt.flags;
-
+__device__ __forceinline__ void gm_dots_body(int bx, int gx, int64_t n, int j, const T* __restrict__ V,
+                                             double* __restrict__ part, int nbp, unsigned* __restrict__ cnt,
+                                             double* __restrict__ red, const int* __restrict__ flags, int gated,
+                                             int with_norm) {
     if (flags[F_CONV] || (gated && !flags[F_REORTH])) return;
     const T* __restrict__ w = V + (int64_t)(j + 1) * n;
     const int warp = threadIdx.x >> 5, lane32 = threadIdx.x & 31;
     const int nk = j + 1 + (with_norm ? 1 : 0);
     // a block sweeps a contiguous slab of rows; warp w owns k = w, w + 8, ...
-    const int64_t slab = ((n + gridDim.x - 1) / gridDim.x + 31) / 32 * 32;
-    const int64_t i0 = (int64_t)blockIdx.x * slab, i1 = min(n, i0 + slab);
+    const int64_t slab = ((n + gx - 1) / gx + 31) / 32 * 32;
+    const int64_t i0 = (int64_t)bx * slab, i1 = min(n, i0 + slab);
     for (int k = warp; k < nk; k += 8) {
         const T* __restrict__ vk = k <= j ? V + (int64_t)k * n : w;
         T s0 = 0, s1 = 0, s2 = 0, s3 = 0;
@@ -751,31 +802,28 @@ __global__ void __launch_bounds__(256) gm_dots(int64_t n, int j, const T* __rest
         }
         for (; i < i1; i += 32) s0 += vk[i] * w[i];
         const double sm = warp_sum((double)s0 + (double)s1 + (double)s2 + (double)s3);
-        if (lane32 == 0) part[(int64_t)k * nbp + blockIdx.x] = sm;
+        if (lane32 == 0) part[(int64_t)k * nbp + bx] = sm;
     }
-    if (!finish_last(cnt)) return;
-    finish_sums(part, nbp, gridDim.x, nk, red);
+    if (!finish_last(cnt, gx)) return;
+    finish_sums(part, nbp, gx, nk, red);
+}
+
+template <class T>
+__global__ void __launch_bounds__(256) gm_dots(int64_t n, int j, const T* __restrict__ V, double* __restrict__ part,
+                                               int nbp, unsigned* __restrict__ cnt, double* __restrict__ red,
+                                               const int* __restrict__ flags, int gated, int with_norm, Bat bt) {
+    const int64_t ib = blockIdx.y;
+    gm_dots_body<T>(blockIdx.x, gridDim.x, n, j, V + ib * bt.V, part + ib * bt.part, nbp, cnt + ib * bt.cnt,
+                    red + ib * bt.red, flags + ib * bt.flags, gated, with_norm);
 }
 
 // plain masked SpMV of the Krylov matrix into the next basis slot: V[j+1] = sc * (A_s x_in)_free
 template <class T, int TPR, int U>
-__global__ void __launch_bounds__(256) gm_spmv(int64_t n, int j, const int32_t* __restrict__ rp,
-                                               const int32_t* __restrict__ col, const T* __restrict__ A,
-                                               const uint8_t* __restrict__ freed, const T* __restrict__ xin,
-                                               int xin_is_basis, T* __restrict__ V, const double* __restrict__ scale,
-                                               const int* __restrict__ flags, Bat bt, int* __restrict__ worked) {
-    const int64_t ib = blockIdx.y;
-    A += ib * bt.nnz;
-    xin += ib * (xin_is_basis ? bt.V : bt.n);
-    V += ib * bt.V;
-    scale += ib * bt.scale;
-    flags += ib * bt.flags;
-
-    const bool done = flags[F_CONV] != 0;
-    // timed launches log whether they did the product or returned at once past convergence
-    if (worked && blockIdx.x == 0 && blockIdx.y == 0 && threadIdx.x == 0) *worked = done ? 0 : 1;
-    if (done) return;
-    const int64_t r = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) / TPR;
+__device__ __forceinline__ void gm_spmv_body(int bx, int64_t n, int j, const int32_t* __restrict__ rp,
+                                             const int32_t* __restrict__ col, const T* __restrict__ A,
+                                             const uint8_t* __restrict__ freed, const T* __restrict__ xin,
+                                             int xin_is_basis, T* __restrict__ V, const double* __restrict__ scale) {
+    const int64_t r = (bx * (int64_t)blockDim.x + threadIdx.x) / TPR;
     const int lane = threadIdx.x % TPR;
     int32_t a = 0, e = 0;
     if (r < n) {
@@ -787,6 +835,21 @@ __global__ void __launch_bounds__(256) gm_spmv(int64_t n, int j, const int32_t* 
         const T sc = xin_is_basis ? (T)scale[j] : (T)1;
         V[(int64_t)(j + 1) * n + r] = freed[r] ? y * sc : (T)0;
     }
+}
+
+template <class T, int TPR, int U>
+__global__ void __launch_bounds__(256) gm_spmv(int64_t n, int j, const int32_t* __restrict__ rp,
+                                               const int32_t* __restrict__ col, const T* __restrict__ A,
+                                               const uint8_t* __restrict__ freed, const T* __restrict__ xin,
+                                               int xin_is_basis, T* __restrict__ V, const double* __restrict__ scale,
+                                               const int* __restrict__ flags, Bat bt, int* __restrict__ worked) {
+    const int64_t ib = blockIdx.y;
+    const bool done = flags[ib * bt.flags + F_CONV] != 0;
+    // timed launches log whether they did the product or returned at once past convergence
+    if (worked && blockIdx.x == 0 && blockIdx.y == 0 && threadIdx.x == 0) *worked = done ? 0 : 1;
+    if (done) return;
+    gm_spmv_body<T, TPR, U>(blockIdx.x, n, j, rp, col, A + ib * bt.nnz, freed, xin + ib * (xin_is_basis ? bt.V : bt.n),
+                            xin_is_basis, V + ib * bt.V, scale + ib * bt.scale);
 }
 
 // The same product from the SELL-32 copy: a warp per slice of 32 rows, a lane per row, 16-byte loads
@@ -839,29 +902,18 @@ __global__ void __launch_bounds__(256) gm_spmv_sell(int64_t n, int64_t nslices, 
 // w -= sum_k h_k v_k; |w|^2; then (finishing block) Hessenberg column + Givens, or the request for
 // a second pass. pass 1 reads h from red (d_k = V_k . w, |w|^2 in red[j+1]); pass 2 from red2.
 template <class T>
-__global__ void __launch_bounds__(256) gm_orth(int64_t n, int j, int m, T* __restrict__ V,
-                                               const double* __restrict__ red, double* __restrict__ part,
-                                               unsigned* __restrict__ cnt, double* __restrict__ H,
-                                               double* __restrict__ csg, double* st, int* flags, double* scale,
-                                               int pass, Bat bt) {
-    const int64_t ib = blockIdx.y;
-    V += ib * bt.V;
-    red += ib * bt.red;
-    part += ib * bt.part;
-    cnt += ib * bt.cnt;
-    H += ib * bt.H;
-    csg += ib * bt.H;
-    st += ib * bt.st;
-    flags += ib * bt.flags;
-    scale += ib * bt.scale;
-
+__device__ __forceinline__ void gm_orth_body(int bx, int gx, int64_t n, int j, int m, T* __restrict__ V,
+                                             const double* __restrict__ red, double* __restrict__ part,
+                                             unsigned* __restrict__ cnt, double* __restrict__ H,
+                                             double* __restrict__ csg, double* st, int* flags, double* scale,
+                                             int pass) {
     if (flags[F_CONV] || (pass == 2 && !flags[F_REORTH])) return;
     __shared__ T coef[130];
     for (int k = threadIdx.x; k <= j; k += blockDim.x) coef[k] = (T)(red[k] * scale[k] * scale[k]);
     __syncthreads();
     T* __restrict__ w = V + (int64_t)(j + 1) * n;
     double acc = 0;
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    for (int64_t i = bx * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gx * blockDim.x) {
         T wi = w[i];
         for (int k = 0; k <= j; k++) wi -= coef[k] * V[(int64_t)k * n + i];
         w[i] = wi;
@@ -874,13 +926,13 @@ __global__ void __launch_bounds__(256) gm_orth(int64_t n, int j, int m, T* __res
     if (threadIdx.x == 0) {
         double t = 0;
         for (int q = 0; q < (int)(blockDim.x >> 5); q++) t += sh[q];
-        part[blockIdx.x] = t;
+        part[bx] = t;
     }
-    if (!finish_last(cnt)) return;
+    if (!finish_last(cnt, gx)) return;
     __shared__ double hn2;
     if (threadIdx.x < 32) {
         double q = 0;
-        for (int b = threadIdx.x; b < (int)gridDim.x; b += 32) q += __ldcg(part + b);
+        for (int b = threadIdx.x; b < gx; b += 32) q += __ldcg(part + b);
         q = warp_sum(q);
         if (threadIdx.x == 0) hn2 = q;
     }
@@ -901,25 +953,27 @@ __global__ void __launch_bounds__(256) gm_orth(int64_t n, int j, int m, T* __res
     givens_step(m, j, isfinite(hn2) ? sqrt(fmax(hn2, 0.0)) : (double)NAN, H, csg, st, flags, scale);
 }
 
+template <class T>
+__global__ void __launch_bounds__(256) gm_orth(int64_t n, int j, int m, T* __restrict__ V,
+                                               const double* __restrict__ red, double* __restrict__ part,
+                                               unsigned* __restrict__ cnt, double* __restrict__ H,
+                                               double* __restrict__ csg, double* st, int* flags, double* scale,
+                                               int pass, Bat bt) {
+    const int64_t ib = blockIdx.y;
+    gm_orth_body<T>(blockIdx.x, gridDim.x, n, j, m, V + ib * bt.V, red + ib * bt.red, part + ib * bt.part,
+                    cnt + ib * bt.cnt, H + ib * bt.H, csg + ib * bt.H, st + ib * bt.st, flags + ib * bt.flags,
+                    scale + ib * bt.scale, pass);
+}
+
 // x += P (sum_k y_k v_k) with y = H^-1 g over the completed columns (each block solves the small
 // triangular system itself). P = D^-1 (dinv != null), identity, or (u != null) the sum is written
 // to u for a block-Jacobi application by the caller.
 template <class T>
-__global__ void __launch_bounds__(256) gm_combine(int64_t n, int m, const T* __restrict__ V,
-                                                  const double* __restrict__ scale, const double* __restrict__ H,
-                                                  const double* __restrict__ csg, const int* __restrict__ flags,
-                                                  const T* __restrict__ dinv, double* __restrict__ x,
-                                                  T* __restrict__ u, Bat bt) {
-    const int64_t ib = blockIdx.y;
-    V += ib * bt.V;
-    scale += ib * bt.scale;
-    H += ib * bt.H;
-    csg += ib * bt.H;
-    flags += ib * bt.flags;
-    if (dinv) dinv += ib * bt.n;
-    x += ib * bt.n;
-    if (u) u += ib * bt.n;
-
+__device__ __forceinline__ void gm_combine_body(int bx, int gx, int64_t n, int m, const T* __restrict__ V,
+                                                const double* __restrict__ scale, const double* __restrict__ H,
+                                                const double* __restrict__ csg, const int* __restrict__ flags,
+                                                const T* __restrict__ dinv, double* __restrict__ x,
+                                                T* __restrict__ u) {
     __shared__ double y[130];
     __shared__ T c[130];
     const int jd = flags[F_JDONE];
@@ -927,8 +981,7 @@ __global__ void __launch_bounds__(256) gm_combine(int64_t n, int m, const T* __r
         // no completed column: the correction is zero (the preconditioner input must not keep the
         // last iteration's vector)
         if (u)
-            for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
-                u[i] = (T)0;
+            for (int64_t i = bx * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gx * blockDim.x) u[i] = (T)0;
         return;
     }
     if (threadIdx.x == 0) {
@@ -941,12 +994,24 @@ __global__ void __launch_bounds__(256) gm_combine(int64_t n, int m, const T* __r
         for (int k = 0; k < jd; k++) c[k] = (T)(y[k] * scale[k]);
     }
     __syncthreads();
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    for (int64_t i = bx * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gx * blockDim.x) {
         T acc = 0;
         for (int k = 0; k < jd; k++) acc += c[k] * V[(int64_t)k * n + i];
         if (u) u[i] = acc;
         else x[i] += (double)(dinv ? dinv[i] * acc : acc);
     }
+}
+
+template <class T>
+__global__ void __launch_bounds__(256) gm_combine(int64_t n, int m, const T* __restrict__ V,
+                                                  const double* __restrict__ scale, const double* __restrict__ H,
+                                                  const double* __restrict__ csg, const int* __restrict__ flags,
+                                                  const T* __restrict__ dinv, double* __restrict__ x,
+                                                  T* __restrict__ u, Bat bt) {
+    const int64_t ib = blockIdx.y;
+    gm_combine_body<T>(blockIdx.x, gridDim.x, n, m, V + ib * bt.V, scale + ib * bt.scale, H + ib * bt.H,
+                       csg + ib * bt.H, flags + ib * bt.flags, dinv ? dinv + ib * bt.n : nullptr, x + ib * bt.n,
+                       u ? u + ib * bt.n : nullptr);
 }
 
 template <class T, int L>
@@ -1277,6 +1342,195 @@ int gm_norms(const Ctx& c, const double* b, const double* x, int mode) {
 #undef GM_R
     OCMP_CUDA(cudaGetLastError());
     return OCMP_OK;
+}
+
+// ---------------------------------------------------------------------------------------------
+// Group kernels: the GMRES kernel bodies above over the (instance, block) pairs of a group's active
+// instances, a fixed grid striding over the list (its length is read from the device, so one
+// captured graph serves every active set). A barrier ends each pair: the bodies keep state in
+// shared memory.
+#define OCMP_GX_LOOP(list, which)                                                                                      \
+    for (int vb = blockIdx.x; vb < nact[which]; vb += gridDim.x) {                                                     \
+        const int2 e = list[vb];                                                                                       \
+        const GInst& d = I[e.x];                                                                                       \
+        const int bx = e.y;
+#define OCMP_GX_END                                                                                                    \
+        __syncthreads();                                                                                               \
+    }
+
+template <class T>
+__global__ void __launch_bounds__(256) gx_resid(const GInst* __restrict__ I, const int2* __restrict__ list,
+                                                const int* __restrict__ nact, int m, int mode) {
+    OCMP_GX_LOOP(list, 0)
+    T* V0 = (mode == 1 || mode == 3) ? (T*)d.V : nullptr;
+    double* csg = d.H + (int64_t)(m + 1) * m;
+#define OCMP_GX_RESID(TPR, U)                                                                                          \
+    gm_resid_body<T, TPR, U>(bx, d.gbn, d.n, d.rp, d.col, d.A64, d.freed, d.b, d.x, V0, d.part, d.cnt, d.st, d.flags,   \
+                             d.scale, csg, m, mode, d.lift_ptr, d.lift_pos)
+    switch (d.cfg) {
+    case 0:
+    case 1: OCMP_GX_RESID(2, 4); break;
+    case 2: OCMP_GX_RESID(2, 8); break;
+    case 3: OCMP_GX_RESID(4, 4); break;
+    case 4: OCMP_GX_RESID(4, 8); break;
+    default: OCMP_GX_RESID(8, 8); break;
+    }
+#undef OCMP_GX_RESID
+    OCMP_GX_END
+}
+
+template <class T>
+__global__ void __launch_bounds__(256) gx_spmv(const GInst* __restrict__ I, const int2* __restrict__ list,
+                                               const int* __restrict__ nact, int j) {
+    OCMP_GX_LOOP(list, 1)
+    if (!d.flags[F_CONV]) {
+        T* V = (T*)d.V;
+        const T* K = (const T*)d.K;
+        const T* xin = V + (int64_t)j * d.n;
+        switch (d.cfg) {
+        case 0: gm_spmv_body<T, 2, 4>(bx, d.n, j, d.rp, d.col, K, d.freed, xin, 1, V, d.scale); break;
+        case 1: gm_spmv_body<T, 4, 4>(bx, d.n, j, d.rp, d.col, K, d.freed, xin, 1, V, d.scale); break;
+        case 2: gm_spmv_body<T, 4, 8>(bx, d.n, j, d.rp, d.col, K, d.freed, xin, 1, V, d.scale); break;
+        case 3: gm_spmv_body<T, 8, 4>(bx, d.n, j, d.rp, d.col, K, d.freed, xin, 1, V, d.scale); break;
+        case 4: gm_spmv_body<T, 8, 8>(bx, d.n, j, d.rp, d.col, K, d.freed, xin, 1, V, d.scale); break;
+        default: gm_spmv_body<T, 16, 8>(bx, d.n, j, d.rp, d.col, K, d.freed, xin, 1, V, d.scale); break;
+        }
+    }
+    }   // no barrier needed: the SpMV body keeps nothing in shared memory
+}
+
+// pass 1: dots into red (counter 0), pass 2: gated dots into red + m + 4 (counter 2)
+template <class T>
+__global__ void __launch_bounds__(256) gx_dots(const GInst* __restrict__ I, const int2* __restrict__ list,
+                                               const int* __restrict__ nact, int j, int m, int pass) {
+    OCMP_GX_LOOP(list, 0)
+    gm_dots_body<T>(bx, d.gbn, d.n, j, (const T*)d.V, d.part, d.gbn, d.cnt + (pass == 1 ? 0 : 2),
+                    d.red + (pass == 1 ? 0 : m + 4), d.flags, pass == 1 ? 0 : 1, pass == 1 ? 1 : 0);
+    OCMP_GX_END
+}
+
+template <class T>
+__global__ void __launch_bounds__(256) gx_orth(const GInst* __restrict__ I, const int2* __restrict__ list,
+                                               const int* __restrict__ nact, int j, int m, int pass) {
+    OCMP_GX_LOOP(list, 0)
+    gm_orth_body<T>(bx, d.gbn, d.n, j, m, (T*)d.V, d.red + (pass == 1 ? 0 : m + 4), d.part,
+                    d.cnt + (pass == 1 ? 1 : 3), d.H, d.H + (int64_t)(m + 1) * m, d.st, d.flags, d.scale, pass);
+    OCMP_GX_END
+}
+
+template <class T>
+__global__ void __launch_bounds__(256) gx_combine(const GInst* __restrict__ I, const int2* __restrict__ list,
+                                                  const int* __restrict__ nact, int m) {
+    OCMP_GX_LOOP(list, 0)
+    gm_combine_body<T>(bx, d.gbn, d.n, m, (const T*)d.V, d.scale, d.H, d.H + (int64_t)(m + 1) * m, d.flags,
+                       (const T*)d.dinv, d.x, nullptr);
+    OCMP_GX_END
+}
+#undef OCMP_GX_LOOP
+#undef OCMP_GX_END
+
+constexpr int kGroupRows = 2048;   // rows per reduction block of a group instance
+
+// Host driver of a group solve: the fused GMRES of gm_run over every instance of every member, one
+// launch per kernel of the iteration for all of them; one restart cycle (m iterations, the x
+// update and the next FP64 residual) is captured once into a CUDA graph and replayed (the kernels
+// read the right-hand sides and solutions through the descriptors, so the graph serves every
+// solve), the host reading the members' flags between cycles. Converged instances return at the
+// top of every kernel.
+template <class T>
+int group_run(ocmp_group_s* g, cudaStream_t st, std::vector<int>& its, std::vector<double>& r0, int* cycles) {
+    const int m = g->m;
+    auto read_all = [&]() -> int {
+        for (ocmp_solver_s* sv : g->members)
+            OCMP_CUDA(cudaMemcpyAsync(sv->hflags, sv->flags, sizeof(int) * F_NFLAG * sv->B, cudaMemcpyDeviceToHost, st));
+        OCMP_CUDA(cudaStreamSynchronize(st));
+        return OCMP_OK;
+    };
+    auto all_outer = [&]() {
+        for (ocmp_solver_s* sv : g->members)
+            for (int q = 0; q < sv->B; q++)
+                if (!sv->hflags[q * F_NFLAG + F_OUTER] && !sv->hflags[q * F_NFLAG + F_NONFIN]) return false;
+        return true;
+    };
+    // each kernel's grid is what stays resident at once (a larger grid would leave a second wave
+    // waiting for the first to stride through the whole list)
+    const int* gr = g->grid[std::is_same<T, double>::value ? 1 : 0];
+    auto G = [&](int k, int tot) { return (unsigned)std::max(1, std::min(gr[k], tot)); };
+    auto cycle = [&](cudaStream_t ls) {
+        for (int j = 0; j < m; j++) {
+            OCMP_LAUNCH(gx_spmv<T><<<G(0, g->stot), 256, 0, ls>>>(g->d_inst, g->d_slist, g->d_nact, j));
+            OCMP_LAUNCH(gx_dots<T><<<G(1, g->gtot), 256, 0, ls>>>(g->d_inst, g->d_glist, g->d_nact, j, m, 1));
+            OCMP_LAUNCH(gx_orth<T><<<G(2, g->gtot), 256, 0, ls>>>(g->d_inst, g->d_glist, g->d_nact, j, m, 1));
+            OCMP_LAUNCH(gx_dots<T><<<G(1, g->gtot), 256, 0, ls>>>(g->d_inst, g->d_glist, g->d_nact, j, m, 2));
+            OCMP_LAUNCH(gx_orth<T><<<G(2, g->gtot), 256, 0, ls>>>(g->d_inst, g->d_glist, g->d_nact, j, m, 2));
+        }
+        OCMP_LAUNCH(gx_combine<T><<<G(3, g->gtot), 256, 0, ls>>>(g->d_inst, g->d_glist, g->d_nact, m));
+        OCMP_LAUNCH(gx_resid<T><<<G(4, g->gtot), 256, 0, ls>>>(g->d_inst, g->d_glist, g->d_nact, m, 1));
+    };
+    // the (instance, block) lists of the instances still iterating, after the flags were read
+    auto set_active = [&](bool all_inst) -> int {
+        int ng = 0, ns = 0;
+        for (size_t i = 0; i < g->members.size(); i++) {
+            ocmp_solver_s* sv = g->members[i];
+            for (int q = 0; q < sv->B; q++) {
+                if (!all_inst && (sv->hflags[q * F_NFLAG + F_OUTER] || sv->hflags[q * F_NFLAG + F_NONFIN])) continue;
+                const int k = g->first[i] + q;
+                const GInst& d = g->h_inst[k];
+                for (int bb = 0; bb < d.gbn; bb++) g->h_glist[ng++] = make_int2(k, bb);
+                for (int bb = 0; bb < d.sbn; bb++) g->h_slist[ns++] = make_int2(k, bb);
+            }
+        }
+        g->h_nact[0] = ng;
+        g->h_nact[1] = ns;
+        if (ng) OCMP_CUDA(cudaMemcpyAsync(g->d_glist, g->h_glist, sizeof(int2) * ng, cudaMemcpyHostToDevice, st));
+        if (ns) OCMP_CUDA(cudaMemcpyAsync(g->d_slist, g->h_slist, sizeof(int2) * ns, cudaMemcpyHostToDevice, st));
+        OCMP_CUDA(cudaMemcpyAsync(g->d_nact, g->h_nact, 2 * sizeof(int), cudaMemcpyHostToDevice, st));
+        return OCMP_OK;
+    };
+    for (ocmp_solver_s* sv : g->members) {
+        const double inner = g->mixed ? (sv->prm.inner_tol > 0 ? sv->prm.inner_tol : 1e-4) : 0.0;
+        OCMP_LAUNCH(gm_set_tols<<<1, 1, 0, st>>>(sv->st, sv->prm.tol, inner, 1e-6, sv->B, sv->bat.st));
+        OCMP_CUDA(cudaMemsetAsync(sv->flags, 0, sizeof(int) * F_NFLAG * sv->B, st));
+    }
+    if (set_active(true)) return OCMP_ERR_CUDA;
+    OCMP_LAUNCH(gx_resid<T><<<G(4, g->gtot), 256, 0, st>>>(g->d_inst, g->d_glist, g->d_nact, m, 3));
+    {
+        if (read_all()) return OCMP_ERR_CUDA;
+        for (size_t i = 0; i < g->members.size(); i++) {
+            ocmp_solver_s* sv = g->members[i];
+            std::vector<double> sth((size_t)S_NSLOT * sv->B);
+            OCMP_CUDA(cudaMemcpy(sth.data(), sv->st, sizeof(double) * sth.size(), cudaMemcpyDeviceToHost));
+            for (int q = 0; q < sv->B; q++) r0[g->first[i] + q] = sth[(size_t)q * S_NSLOT + S_RES];
+        }
+    }
+    if (!g->gexec) {
+        if (!g->gstream) OCMP_CUDA(cudaStreamCreateWithFlags(&g->gstream, cudaStreamNonBlocking));
+        cudaGraph_t gph;
+        const unsigned long long l0 = g_launches.load();
+        OCMP_CUDA(cudaStreamBeginCapture(g->gstream, cudaStreamCaptureModeThreadLocal));
+        cycle(g->gstream);
+        OCMP_CUDA(cudaStreamEndCapture(g->gstream, &gph));
+        g->graph_kernels = g_launches.load() - l0;
+        g_launches.fetch_sub(g->graph_kernels);
+        cudaError_t e = cudaGraphInstantiate(&g->gexec, gph, 0);
+        cudaGraphDestroy(gph);
+        if (e != cudaSuccess) return cuda_fail(e, "cudaGraphInstantiate (group cycle)");
+    }
+    int it = 0, cyc = 0;
+    while (!all_outer() && it < g->maxit) {
+        if (set_active(false)) return OCMP_ERR_CUDA;
+        OCMP_CUDA(cudaGraphLaunch(g->gexec, st));
+        g_launches.fetch_add(g->graph_kernels);
+        it += m;
+        cyc++;
+        if (read_all()) return OCMP_ERR_CUDA;
+    }
+    for (size_t i = 0; i < g->members.size(); i++) {
+        ocmp_solver_s* sv = g->members[i];
+        for (int q = 0; q < sv->B; q++) its[g->first[i] + q] = sv->hflags[q * F_NFLAG + F_ITERS];
+    }
+    *cycles = cyc;
+    return set_active(true);   // every instance again, for the final residuals
 }
 
 }  // namespace
@@ -1804,6 +2058,170 @@ int ocmp_solve(ocmp_solver_t sv, const double* b, double* x, void* stream, ocmp_
     else if (status == OCMP_NOT_CONVERGED) set_error("ocmp_solve: iteration cap reached before the tolerance");
     else if (status == OCMP_BREAKDOWN) set_error("ocmp_solve: Krylov breakdown");
     return status;
+}
+
+
+int ocmp_group_create(const ocmp_solver_t* solvers, int32_t count, ocmp_group_t* out) {
+    if (!solvers || count <= 0 || !out) return fail(OCMP_ERR_ARG, "ocmp_group_create: no solvers");
+    *out = nullptr;
+    auto* g = new ocmp_group_s();
+    for (int i = 0; i < count; i++) {
+        ocmp_solver_s* sv = solvers[i];
+        const ocmp_solve_params_t& P = sv ? sv->prm : ocmp_solve_params_t{};
+        const char* why = nullptr;
+        if (!sv) why = "null solver";
+        else if (P.method != OCMP_GMRES) why = "members must be GMRES solvers";
+        else if (P.precond != OCMP_PRE_JACOBI && P.precond != OCMP_PRE_USER && P.precond != OCMP_PRE_NONE)
+            why = "members must use point Jacobi (or no) preconditioning";
+        else if (sv->sell) why = "members' FP32 Krylov matrices must be in CSR order (no OCMP_MAT_SELL32)";
+        else if (i > 0 && (sv->m != g->m || (P.precision == OCMP_MIXED) != g->mixed || P.maxit != g->maxit))
+            why = "members must share the restart, the precision and the iteration cap";
+        if (why) {
+            delete g;
+            return fail(OCMP_ERR_UNSUPPORTED, std::string("ocmp_group_create: ") + why);
+        }
+        if (i == 0) {
+            g->m = sv->m;
+            g->mixed = P.precision == OCMP_MIXED;
+            g->maxit = P.maxit;
+        }
+        g->members.push_back(sv);
+        g->first.push_back(g->ninst);
+        const ocmp_space_s* s = sv->s;
+        const RowCfg rc = row_cfg(s);
+        const int cfg = rc.tpr == 2 ? 0 : rc.tpr == 4 ? (rc.u == 4 ? 1 : 2) : rc.tpr == 8 ? (rc.u == 4 ? 3 : 4) : 5;
+        const int tpr = cfg == 0 ? 2 : cfg <= 2 ? 4 : cfg <= 4 ? 8 : 16;
+        const int64_t n = sv->n, m = sv->m;
+        const Bat& bt = sv->bat;
+        const size_t ts = g->mixed ? sizeof(float) : sizeof(double);
+        const bool jac = P.precond == OCMP_PRE_JACOBI || P.precond == OCMP_PRE_USER;
+        for (int q = 0; q < sv->B; q++) {
+            GInst d{};
+            d.n = n;
+            d.rp = s->d_rowptr;
+            d.col = s->d_col;
+            d.freed = s->d_free;
+            d.lift_ptr = s->d_lift_ptr;
+            d.lift_pos = s->d_lift_pos;
+            d.A64 = sv->mat->vals + q * s->nnz;
+            const char* K = g->mixed ? (const char*)sv->K32 : (const char*)sv->K64;
+            d.K = K + ts * q * s->nnz;
+            const char* dv = jac ? (g->mixed ? (const char*)sv->dinv32 : (const char*)sv->dinv) : nullptr;
+            d.dinv = dv ? dv + ts * q * n : nullptr;
+            char* V = g->mixed ? (char*)sv->V32 : (char*)sv->V;
+            d.V = V + ts * q * (m + 1) * n;
+            d.part = sv->part + q * bt.part;
+            d.cnt = sv->cnt + q * bt.cnt;
+            d.st = sv->st + q * bt.st;
+            d.flags = sv->flags + q * bt.flags;
+            d.scale = sv->scale + q * bt.scale;
+            d.H = sv->H + q * bt.H;
+            d.red = sv->red + q * bt.red;
+            // reduction blocks in proportion to the rows (the partial sums fit the member's layout,
+            // sized for sv->grid blocks)
+            d.gbn = (int)std::max<int64_t>(1, std::min<int64_t>(sv->grid, (n + kGroupRows - 1) / kGroupRows));
+            d.sbn = (int)nblk(n * tpr, 256);
+            d.cfg = cfg;
+            g->gtot += d.gbn;
+            g->stot += d.sbn;
+            g->h_inst.push_back(d);
+            g->ninst++;
+        }
+    }
+    {
+        int dev = 0, sms = 152;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        const void* ks[2][5] = {{(const void*)gx_spmv<float>, (const void*)gx_dots<float>, (const void*)gx_orth<float>,
+                                 (const void*)gx_combine<float>, (const void*)gx_resid<float>},
+                                {(const void*)gx_spmv<double>, (const void*)gx_dots<double>,
+                                 (const void*)gx_orth<double>, (const void*)gx_combine<double>,
+                                 (const void*)gx_resid<double>}};
+        for (int t = 0; t < 2; t++)
+            for (int k = 0; k < 5; k++) {
+                int nb = 0;
+                if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, ks[t][k], 256, 0) != cudaSuccess || nb < 1) nb = 1;
+                g->grid[t][k] = nb * sms;
+            }
+    }
+    int st = dalloc(&g->d_glist, (size_t)g->gtot);
+    if (!st) st = dalloc(&g->d_slist, (size_t)g->stot);
+    if (!st) st = dalloc(&g->d_nact, 2);
+    if (!st) st = dalloc(&g->d_inst, (size_t)g->ninst);
+    if (!st && (cudaMallocHost((void**)&g->h_glist, sizeof(int2) * g->gtot) != cudaSuccess ||
+                cudaMallocHost((void**)&g->h_slist, sizeof(int2) * g->stot) != cudaSuccess ||
+                cudaMallocHost((void**)&g->h_nact, 2 * sizeof(int)) != cudaSuccess))
+        st = fail(OCMP_ERR_NOMEM, "ocmp_group_create: pinned lists");
+    if (st) {
+        ocmp_group_destroy(g);
+        return st;
+    }
+    *out = g;
+    return OCMP_OK;
+}
+
+int ocmp_group_destroy(ocmp_group_t g) {
+    if (!g) return OCMP_OK;
+    dfree(g->d_glist);
+    dfree(g->d_slist);
+    dfree(g->d_nact);
+    dfree(g->d_inst);
+    if (g->h_glist) cudaFreeHost(g->h_glist);
+    if (g->h_slist) cudaFreeHost(g->h_slist);
+    if (g->h_nact) cudaFreeHost(g->h_nact);
+    if (g->gexec) cudaGraphExecDestroy(g->gexec);
+    if (g->gstream) cudaStreamDestroy(g->gstream);
+    delete g;
+    return OCMP_OK;
+}
+
+int ocmp_group_solve(ocmp_group_t g, const double* const* b, double* const* x, void* stream, ocmp_solve_info_t* infos) {
+    if (!g || !b || !x) return fail(OCMP_ERR_ARG, "ocmp_group_solve: null argument");
+    cudaStream_t st = (cudaStream_t)stream;
+    for (size_t i = 0; i < g->members.size(); i++) {
+        ocmp_solver_s* sv = g->members[i];
+        if (!b[i] || !x[i]) return fail(OCMP_ERR_ARG, "ocmp_group_solve: null right-hand side or solution");
+        for (int q = 0; q < sv->B; q++) {
+            GInst& d = g->h_inst[g->first[i] + q];
+            d.b = b[i] + q * sv->n;
+            d.x = x[i] + q * sv->n;
+        }
+    }
+    OCMP_CUDA(cudaMemcpyAsync(g->d_inst, g->h_inst.data(), sizeof(GInst) * g->ninst, cudaMemcpyHostToDevice, st));
+    std::vector<int> its(g->ninst, 0);
+    std::vector<double> r0(g->ninst, 0.0);
+    int cyc = 0;
+    int r = g->mixed ? group_run<float>(g, st, its, r0, &cyc) : group_run<double>(g, st, its, r0, &cyc);
+    if (r) return r;
+    // the FP64 residual of every returned x
+    const unsigned gg = (unsigned)std::max(1, std::min(g->grid[g->mixed ? 0 : 1][4], g->gtot));
+    if (g->mixed) OCMP_LAUNCH(gx_resid<float><<<gg, 256, 0, st>>>(g->d_inst, g->d_glist, g->d_nact, g->m, 2));
+    else OCMP_LAUNCH(gx_resid<double><<<gg, 256, 0, st>>>(g->d_inst, g->d_glist, g->d_nact, g->m, 2));
+    OCMP_CUDA(cudaGetLastError());
+    int worst = OCMP_OK;
+    for (size_t i = 0; i < g->members.size(); i++) {
+        ocmp_solver_s* sv = g->members[i];
+        std::vector<double> sth((size_t)S_NSLOT * sv->B);
+        OCMP_CUDA(cudaMemcpyAsync(sth.data(), sv->st, sizeof(double) * sth.size(), cudaMemcpyDeviceToHost, st));
+        OCMP_CUDA(cudaStreamSynchronize(st));
+        for (int q = 0; q < sv->B; q++) {
+            const int k = g->first[i] + q;
+            const double rr = sth[(size_t)q * S_NSLOT + S_RES];
+            int status = OCMP_OK;
+            if (sv->hflags[q * F_NFLAG + F_NONFIN] || !std::isfinite(rr)) status = OCMP_ERR_NONFINITE;
+            else if (rr > sv->prm.tol) status = sv->hflags[q * F_NFLAG + F_BREAK] ? OCMP_BREAKDOWN : OCMP_NOT_CONVERGED;
+            if (infos) {
+                infos[k].status = status;
+                infos[k].iterations = its[k];
+                infos[k].outer_iterations = cyc;
+                infos[k].relres0 = r0[k];
+                infos[k].relres = rr;
+            }
+            if (status != OCMP_OK && worst == OCMP_OK) worst = status;
+        }
+    }
+    if (worst != OCMP_OK) set_error("ocmp_group_solve: at least one system did not reach the tolerance");
+    return worst;
 }
 
 }  // extern "C"

@@ -376,6 +376,39 @@ class KrylovSolver:
         return info
 
 
+class KrylovGroup:
+    """GMRES over the instances of several solvers at once (``ocmp_group_*``): uneven sizes, orders
+    and patterns in one kernel sequence. The members (``KrylovSolver``, single or batched matrices)
+    must be GMRES with point Jacobi, share restart, precision and maxit, and stay alive with the
+    group; their own ``update()`` refreshes what the group solves with."""
+
+    def __init__(self, solvers):
+        self.solvers = list(solvers)
+        arr = (C.c_void_p * len(self.solvers))(*[s.h for s in self.solvers])
+        h = C.c_void_p()
+        LB.call('ocmp_group_create', arr, len(self.solvers), C.byref(h))
+        self.h = h
+        self.ninst = sum(s.mat.batch for s in self.solvers)
+
+    def __del__(self):
+        if getattr(self, 'h', None) and LB._lib is not None:
+            LB._lib.ocmp_group_destroy(self.h)
+            self.h = None
+
+    def solve(self, bs, xs, stream=None, raise_on_fail=True):
+        """bs, xs: one device tensor per member (its instances one after another); returns the
+        SolveInfo of every instance in member order."""
+        if len(bs) != len(self.solvers) or len(xs) != len(self.solvers):
+            raise ValueError('one right-hand side and one solution per member')
+        pb = (C.c_void_p * len(bs))(*[_ptr(b) for b in bs])
+        px = (C.c_void_p * len(xs))(*[_ptr(x) for x in xs])
+        infos = (LB.SolveInfo * self.ninst)()
+        st = LB.load().ocmp_group_solve(self.h, pb, px, _stream(stream), infos)
+        if raise_on_fail:
+            LB.check(st)
+        return list(infos)
+
+
 _EDGES = {2: [(0, 1), (0, 2), (1, 2)], 3: [(0, 1), (0, 2), (0, 3), (1, 2), (1, 3), (2, 3)]}
 
 
