@@ -400,13 +400,13 @@ def run_ours(args):
 def run_ins(args):
     """Lid-driven cavity (OpenCMP INS model): unit square 256 x 256 x 2, Taylor-Hood P2/P1, nu = 1e-3
     (Re = 1000 with lid speed 1; the lid's corners at rest, so that the discrete lid does not leak),
-    Euler IMEX steps dt = 1e-3 from rest (explicit convection, reassembly every step), FGMRES(50)
-    with the Cahouet-Chabard block-diagonal preconditioner (velocity Jacobi; pressure: a Jacobi-CG
-    solve with the pressure Laplacian to 0.1 plus the pressure mass diagonal) to 1e-8. Every path
-    runs the same first `ins_train` steps untimed (the learned path collects its training samples
-    there: the run's own first steps), then times `steps` steps: plain FP64 (previous-step guess),
-    FP32 inner pressure CG with the previous-step guess, with the extrapolated guess, and with the
-    learned guess under its judge."""
+    Euler IMEX steps dt = 1e-3 from rest (explicit convection, reassembly every step), the library's
+    GMRES(50) with the Cahouet-Chabard block-diagonal preconditioner (velocity Jacobi; pressure: the
+    strip direct solve of L_p + max(delta, 1) M_p plus the pressure-mass diagonal) to 1e-8. Every
+    path runs the same first `ins_train` steps untimed (the learned path collects its training
+    samples there: the run's own first steps), then times `steps` steps: plain FP64 GMRES
+    (previous-step guess), FP32 inner GMRES + FP64 refinement with the previous-step guess, with the
+    extrapolated guess, and with the learned guess under its judge."""
     import torch
     from opencmp_gb300 import fem, mesh as M, build, _lib
     from opencmp_gb300.guess import LearnedGuess
@@ -442,6 +442,9 @@ def run_ins(args):
             used = guess.predict(u)
         elif kind == 'extrap':
             guess.extrapolate(u)
+        if kind in ('learned', 'extrap'):
+            # the undetermined constant pressure stays where the previous step left it
+            sv.match_pressure_mean(u, uprev)
         bcs(u)
         info = sv.solve(b, u, raise_on_fail=False)
         if collect:
@@ -454,6 +457,7 @@ def run_ins(args):
 
     res = {}
     train_info = {}
+    spmv_live, e2e_ms = (0, 0.0), float('nan')
     for p in ('fp64', 'mixed', 'extrap', 'learned'):
         u = torch.zeros(nd, dtype=torch.float64, device='cuda')
         bcs(u)
@@ -480,6 +484,9 @@ def run_ins(args):
             train_info = dict(samples=0, adam_steps=0)
             guess.reset_judge()
         st.clear()
+        lib_sv = solvers['fp64' if p == 'fp64' else 'mixed'].lib
+        if p == 'learned' and lib_sv is not None:
+            lib_sv.spmv_timing(True)
         torch.cuda.synchronize()
         l0 = _lib.load().ocmp_launch_count()
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -489,6 +496,21 @@ def run_ins(args):
         e1.record()
         torch.cuda.synchronize()
         ms = e0.elapsed_time(e1)
+        if p == 'learned' and lib_sv is not None:
+            spmv_live = lib_sv.spmv_stats()
+            lib_sv.spmv_timing(False)
+            # end to end: the solution back to pinned host memory after every step (the step's
+            # inputs are the device-resident state; the boundary data is constant)
+            u_host = torch.empty(nd, dtype=torch.float64, pin_memory=True)
+            ue = u.clone()
+            ste = []
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            for _ in range(args.steps):
+                step(p, ue, ste)
+                u_host.copy_(ue, non_blocking=True)
+                torch.cuda.current_stream().synchronize()
+            e2e_ms = (time.perf_counter() - t0) * 1e3 / args.steps
         l2, dv = th.errors(u)
         res[p] = dict(ms_per_step=ms / args.steps, value=nd * args.steps / (ms * 1e-3), unit='DOF/s',
                       launches=int(_lib.load().ocmp_launch_count() - l0),
@@ -502,22 +524,39 @@ def run_ins(args):
         print('ins {}: {:.2f} ms/step, {:.1f} iterations/step'.format(p, res[p]['ms_per_step'], res[p]['iters']),
               file=sys.stderr, flush=True)
     val = res['learned']['value']
+    try:
+        with open(os.path.join(ROOT, 'MEASURED_PEAKS.json')) as fh:
+            peak, peak_kind = float(json.load(fh)['hbm_gbs']), 'measured HBM copy'
+    except Exception:
+        peak, peak_kind = 6800.0, 'fallback HBM'
+    nnz_ins = th.nnz
+    g_bytes = 8 * nnz_ins + 4 * (nd + 1) + 9 * nd
+    g_launches, g_ms = spmv_live
+    g_avg = g_ms / max(g_launches, 1)
+    g_achieved = g_bytes / (g_avg * 1e-3) / 1e9 if g_launches else None
     line = {'metric': METRIC + ' (INS lid-driven cavity)', 'value': val, 'unit': 'DOF/s', 'n_gpus': 1,
             'steps': args.steps, 'warmup': args.ins_train, 'ms_per_step': res['learned']['ms_per_step'],
             'higher_is_better': True, 'scaling': 'weak', 'vs_baseline': None, 'dtype': 'f64+f32',
             'data': 'synthetic (generated structured mesh, cavity at rest)',
             'config': {'workload': 'INS lid-driven cavity {0}x{0}x2 tri, Taylor-Hood P2/P1, Re=1000, Euler IMEX '
-                                   'dt=1e-3, lid corners at rest, FGMRES(50) + Cahouet-Chabard (velocity '
-                                   'Jacobi, pressure Laplacian CG to 0.1 + pressure mass diagonal) to 1e-8; '
-                                   'steps {1}..{2} from rest timed'.format(
+                                   'dt=1e-3, lid corners at rest, GMRES(50) + Cahouet-Chabard (velocity '
+                                   'Jacobi, pressure: strip direct solve of the pressure Laplacian + mass '
+                                   'diagonal) to 1e-8; steps {1}..{2} from rest timed'.format(
                                        n, args.ins_train + 1, args.ins_train + args.steps),
                        'ndof': nd, 'nnz': th.nnz, 'l2': 'inputs larger than L2 (no flush)'},
             'plain_fp64': res['fp64'], 'mixed_previous_step_guess': res['mixed'],
             'mixed_extrapolated_guess': res['extrap'],
-            'optimised': dict(res['learned'], kind='FP32 inner pressure CG, learned guess (degree-{} '
+            'optimised': dict(res['learned'], kind='FP32 inner GMRES + FP64 refinement, learned guess (degree-{} '
                                                    'extrapolation + network trained on the run\'s first {} steps)'
                               .format(args.guess_base, args.ins_train)),
             'speedup_vs_plain_fp64': res['fp64']['ms_per_step'] / res['learned']['ms_per_step'],
+            'e2e': {'value': nd / (e2e_ms * 1e-3), 'unit': 'DOF/s', 'h2d_bytes_per_step': 0,
+                    'd2h_bytes_per_step': 8 * nd},
+            'roofline': {'bound': 'hbm', 'kernel': 'gm_spmv<float> (FP32 Krylov SpMV of the saddle-point system, CSR)',
+                         'achieved': g_achieved, 'peak': peak, 'peak_kind': peak_kind, 'unit': 'GB/s',
+                         'frac': g_achieved / peak if g_achieved else None, 'traffic': None,
+                         'algorithmic_bytes': g_bytes, 'avg_launch_ms': g_avg, 'launches_timed': g_launches,
+                         'timing': 'CUDA events around every launch in the timed steps of the optimised path'},
             'guess_training': train_info, 'gpu_launches': res['learned']['launches']}
     print(json.dumps(line), flush=True)
 
@@ -575,6 +614,12 @@ def run_batched(args):
     for _ in range(args.warmup):
         group_step()
     torch.cuda.synchronize()
+    if args.group_only:
+        # a profiling run: the group solve only
+        for _ in range(args.steps):
+            group_step()
+        torch.cuda.synchronize()
+        return
     l0 = _lib.load().ocmp_launch_count()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     e0.record()
@@ -735,6 +780,10 @@ def run_dg2d(args):
     A.assemble(form)
     fem.assemble_rhs(sp, form, rhs, b)
     paths = {'tensor_fp64': ('fp64', 'tensor'), 'simt_fp64': ('fp64', 'simt'), 'tensor_mixed': ('mixed', 'tensor')}
+    if args.dg_paths != 'all':
+        # a profiling run: only the listed paths, no comparison record
+        keep = args.dg_paths.split(',')
+        paths = {k: v for k, v in paths.items() if k in keep}
     solvers = {}
     for k, (prec, kind) in paths.items():
         sv = fem.KrylovSolver(A, method='GMRES', restart=50, precond='strip', precision=prec, tol=1e-8, maxit=200)
@@ -780,6 +829,8 @@ def run_dg2d(args):
                       max_relres=float(max(i.relres for i in infos)),
                       converged=int(sum(1 for i in infos if i.status == 0)))
         print('dg2d {}: {:.1f} ms/step, {:.1f} iterations'.format(k, ms, res[k]['iters']), file=sys.stderr, flush=True)
+    if args.dg_paths != 'all':
+        return
     # the optimised path end to end: the right-hand side's source data from pinned host memory, the
     # solution back to it, every step
     sv = solvers['tensor_fp64']
@@ -965,6 +1016,9 @@ def main():
     ap.add_argument('--n-dg', type=int, default=256)
     ap.add_argument('--dg-cpu-n', type=int, default=128, help='mesh of the dg2d cpu_baseline sample')
     ap.add_argument('--bj-iters', type=int, default=2000, help='block-Jacobi GMRES budget of the dg2d record')
+    ap.add_argument('--dg-paths', default='all',
+                    help='dg2d: comma-separated subset of tensor_fp64,simt_fp64,tensor_mixed to run alone (profiling)')
+    ap.add_argument('--group-only', action='store_true', help='batched: run the group solve only (profiling)')
     ap.add_argument('--n-ins', type=int, default=256)
     ap.add_argument('--ins-train', type=int, default=100,
                     help='untimed first INS steps (training samples from step guess_k + 1 on)')

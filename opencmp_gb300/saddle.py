@@ -250,6 +250,17 @@ class SaddleSolver:
             zp.mul_(beta)
         zp.mul_(-1.0 / (tc * tc))
 
+    def match_pressure_mean(self, u: torch.Tensor, ref: torch.Tensor):
+        """Shift the pressure part of u so that its pressure-mass-weighted mean equals ref's. The
+        constant pressure is determined only by the 1e-10 p q term, so a guess extrapolated in time
+        carries whatever the previous steps left in it, amplified by the extrapolation; left alone it
+        grows from step to step until the FP32 inner iteration loses the pressure gradients to
+        cancellation. The shift changes the residual by far less than the tolerance."""
+        n2 = self.nu2
+        w = 1.0 / self.mp_dinv
+        du = torch.dot(w, u[n2:] - ref[n2:]) / w.sum()
+        u[n2:] -= du
+
     def matvec(self, v: torch.Tensor, out: torch.Tensor):
         self.A.mult(v, out)
 
