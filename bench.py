@@ -41,9 +41,10 @@ METRIC = 'DOF/s to 1e-8 FP64 rel. residual: mixed+batched+learned vs plain FP64,
 WORKLOAD = ('transient 3D convection-diffusion, unit cube {}^3 x 6 tets, H1 p=2, eps=1e-2, w=(1,0.5,0.25), implicit '
             'Euler dt=1e-3, full reassembly every step, GMRES({}) + Jacobi to 1e-8 FP64 relative residual')
 # DRAM bytes per matrix entry (dram__bytes_read.sum + dram__bytes_write.sum per launch / nnz) of the
-# dominant kernel, gm_spmv<float>, from an ncu capture on the 48^3 x 6 case (nnz 25,755,265; two
-# launches: 221.7 and 222.0 MB); the traffic of a launch is this figure times the launch's nnz
-TRAFFIC_PER_NNZ = {'gm_spmv_float': 8.615}
+# dominant kernel from ncu captures on the 48^3 x 6 case (nnz 25,755,265): gm_spmv<float> on the CSR
+# copy (two launches: 221.7 and 222.0 MB), gm_spmv_sell on the SELL-32 copy (251.7 and 251.4 MB; the
+# slices' padding is the difference); the traffic of a launch is this figure times the launch's nnz
+TRAFFIC_PER_NNZ = {'gm_spmv_float': 8.615, 'gm_spmv_sell': 9.768}
 # DRAM bytes moved by one reassembly of the optimised path (element kernel, diagonal pass, gather;
 # ncu on the 48^3 x 6 case: 645 + 95 + 1,428 MB) per algorithmic byte of that case
 ASSEMBLY_TRAFFIC_RATIO = 2168.0 / 227.0

@@ -266,7 +266,9 @@ int ocmp_solver_spmv_stats(ocmp_solver_t solver, int64_t* launches, double* tota
  * explicitly in FP32 by block Gauss-Jordan with 128 x 128 pivot tiles, and a preconditioner
  * application is one forward and one backward sweep of dense matrix-vector products. Built by
  * ocmp_solver_create (OCMP_ERR_UNSUPPORTED when the pattern has no such strips or a strip exceeds
- * 16384 dofs), factorised by ocmp_solver_create and every ocmp_solver_update; GMRES only.
+ * 16384 dofs) and factorised by every ocmp_solver_update (not by ocmp_solver_create: OpenCMP
+ * builds its preconditioners before the first assembly); ocmp_solve refuses a strip solver that
+ * has not been factorised since its last failure. GMRES only.
  * ocmp_solver_strip_stats reports the last factorisation. No counterpart in the reference beyond
  * the direct solve it replaces. */
 typedef struct {

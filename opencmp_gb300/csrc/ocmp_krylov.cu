@@ -85,6 +85,7 @@ struct ocmp_solver_s {
     bool udiag_set = false;
     double* Binv = nullptr;     // block Jacobi (L2 element blocks)
     ocmp::Strip* strip = nullptr;  // strip direct preconditioner (OCMP_PRE_STRIP)
+    bool strip_ready = false;       // factorised by ocmp_solver_update since the last failure
     CCPre* cc = nullptr;           // Cahouet-Chabard data (OCMP_PRE_CAHOUET_CHABARD), once set
     double* V = nullptr;        // (m+1) x n
     double* w = nullptr;
@@ -1683,7 +1684,9 @@ int ocmp_solver_create(ocmp_matrix_t mat, const ocmp_solve_params_t* prm, ocmp_s
         delete sv;
         return st;
     }
-    if (prm->precond != OCMP_PRE_USER) st = ocmp_solver_update(sv, nullptr);  // USER: after ocmp_solver_set_diag
+    // USER: after ocmp_solver_set_diag; STRIP: after the matrix is assembled (OpenCMP builds its
+    // preconditioners before the first assembly and updates them after every one)
+    if (prm->precond != OCMP_PRE_USER && prm->precond != OCMP_PRE_STRIP) st = ocmp_solver_update(sv, nullptr);
     if (st) {
         free_solver(sv);
         delete sv;
@@ -1734,8 +1737,10 @@ int ocmp_solver_update(ocmp_solver_t sv, void* stream) {
         }
     }
     if (sv->strip) {
+        sv->strip_ready = false;
         const int r = strip_factor(sv->strip, s, sv->mat->vals, st);
         if (r) return r;
+        sv->strip_ready = true;
     }
     if (sv->As64 || sv->As32) {
         const double* d = sv->prm.precond == OCMP_PRE_JACOBI || sv->prm.precond == OCMP_PRE_USER ? sv->dinv : nullptr;
@@ -1942,6 +1947,9 @@ int ocmp_solve(ocmp_solver_t sv, const double* b, double* x, void* stream, ocmp_
     if (gm) {
         const bool jac = P.precond == OCMP_PRE_JACOBI || P.precond == OCMP_PRE_USER;
         if (sv->B != 1) return fail(OCMP_ERR_ARG, "ocmp_solve: batched matrix, use ocmp_solve_batch");
+        if (sv->strip && !sv->strip_ready)
+            return fail(OCMP_ERR_ARG, "ocmp_solve: the strip preconditioner is not factorised (call ocmp_solver_update "
+                                      "after assembling the matrix)");
         if (!mixed) {
             if (P.precond == OCMP_PRE_CAHOUET_CHABARD && !sv->cc)
                 return fail(OCMP_ERR_ARG, "ocmp_solve: set the Cahouet-Chabard data (ocmp_solver_set_cahouet_chabard)");

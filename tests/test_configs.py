@@ -86,6 +86,7 @@ def _cd_dg(fem, n, precision, restart=50, tol=1e-10, maxit=40000, raise_on_fail=
     x = torch.zeros_like(b)
     sv = fem.KrylovSolver(A, method='GMRES', restart=restart, precond=precond, precision=precision, tol=tol,
                           maxit=maxit, inner_tol=1e-4)
+    sv.update()                         # Preconditioner.Update() after the assembly, as OpenCMP does
     info = sv.solve(b, x, raise_on_fail=raise_on_fail)
     _cd_dg.last_solver = sv
     return m, sp, x, info, W

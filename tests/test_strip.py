@@ -118,6 +118,26 @@ def test_strip_preconditioner_refuses_cg_and_unbanded(gpu_lib):
     assert e.value.status in (_lib.ERR_UNSUPPORTED, _lib.ERR_ARG)
 
 
+def test_strip_preconditioner_built_before_assembly(gpu_lib):
+    """OpenCMP's order (base_model.py:365-383, base_solver.py:368-377): the preconditioner is built on
+    a matrix that is not assembled yet and updated after every assembly. Building it does not
+    factorise; a solve before the first update is refused; after assembly and update the solve
+    converges."""
+    import torch
+    from opencmp_gb300 import fem, _lib
+    sp, A, b = _cd_system(16)
+    A0 = fem.Matrix(sp)
+    sv = fem.KrylovSolver(A0, method='GMRES', restart=50, precond='strip', precision='fp64', tol=1e-10, maxit=200)
+    x = torch.zeros_like(b)
+    with pytest.raises(_lib.OcmpError) as e:
+        sv.solve(b, x)
+    assert e.value.status == _lib.ERR_ARG
+    A0.device_values()[0].copy_(A.device_values()[0])
+    sv.update()
+    info = sv.solve(b, x)
+    assert info.status == 0 and info.relres <= 1e-10 and info.iterations <= 20
+
+
 @pytest.mark.parametrize('kind', ['simt', 'tensor'])
 def test_strip_newton_schulz_matches_gauss_jordan(gpu_lib, kind):
     """At 96 x 96 every strip is one row of DG elements: its non-interface dofs (the elements that
