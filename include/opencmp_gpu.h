@@ -181,7 +181,24 @@ int ocmp_l2_error(ocmp_space_t space, const double* u_dev, const double* fq_dev,
  * OCMP_MAT_DFLOAT assembles the element matrices and their sums in double-float arithmetic (pairs of
  * FP32 values, about 48 significant bits) on the FP32 pipes, finishing each CSR entry with one FP64
  * addition; the FP64 values agree with the native FP64 assembly to about 1e-14 relative. */
-enum { OCMP_MAT_FP32 = 1, OCMP_MAT_JACOBI64 = 2, OCMP_MAT_JACOBI32 = 4, OCMP_MAT_DFLOAT = 8, OCMP_MAT_SELL32 = 16 };
+enum {
+    OCMP_MAT_FP32 = 1,
+    OCMP_MAT_JACOBI64 = 2,
+    OCMP_MAT_JACOBI32 = 4,
+    OCMP_MAT_DFLOAT = 8,
+    OCMP_MAT_SELL32 = 16,
+    OCMP_MAT_TWO_PASS = 32
+};
+/* Element-only forms on H1 spaces assembled with OCMP_MAT_DFLOAT (generated element code: P1/P2
+ * tetrahedra, P1..P3 triangles) run as one pipelined launch, the element ring: element matrices of
+ * consecutive element chunks go into a ring of chunk slots sized to stay in L2 and are summed into
+ * the CSR entries (and the diagonal) as soon as every element a row needs is written, so they do not
+ * round-trip through DRAM. The values are identical, bit for bit, to those of the two-pass assembly
+ * (all element matrices to memory, then the sorted segmented gather). The ring is planned on the
+ * first such assembly from the dof numbering; where the numbering spreads a row's elements too
+ * widely for the ring, the two-pass assembly runs instead. OCMP_MAT_TWO_PASS always takes the
+ * two-pass assembly. The ring, like the element-matrix buffer, is per space: assemblies of matrices
+ * on one space must not overlap on the GPU. */
 /* OCMP_MAT_SELL32 (with OCMP_MAT_JACOBI32, single matrices): the FP32 Jacobi-scaled values are
  * written in the space's SELL-32 order instead of CSR order (slices of 32 rows, each row padded to
  * its slice's width in 4-entry chunks, chunk-major within a slice, zero padding), the layout the

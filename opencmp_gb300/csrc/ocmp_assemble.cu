@@ -544,10 +544,10 @@ template <int D, int L, int VAR>
 struct GenTerms {
     static constexpr bool value = false;
     static constexpr int NG = 1;
-    static __device__ __forceinline__ void run0(const float2 (&)[1], float2*) {}
-    static __device__ __forceinline__ void run1(const float2 (&)[1], float2*) {}
-    static __device__ __forceinline__ void run2(const float2 (&)[1], float2*) {}
-    static __device__ __forceinline__ void run3(const float2 (&)[1], float2*) {}
+    template <class ST> static __device__ __forceinline__ void run0(const float2 (&)[1], ST&) {}
+    template <class ST> static __device__ __forceinline__ void run1(const float2 (&)[1], ST&) {}
+    template <class ST> static __device__ __forceinline__ void run2(const float2 (&)[1], ST&) {}
+    template <class ST> static __device__ __forceinline__ void run3(const float2 (&)[1], ST&) {}
 };
 __device__ __forceinline__ void gterm(float& sh, float& sl, float2 f, float ch, float cl) {
     float ph, pl;
@@ -556,27 +556,15 @@ __device__ __forceinline__ void gterm(float& sh, float& sl, float2 f, float ch, 
 }
 #include "ocmp_terms_gen.h"
 
-// Two threads per element, in two warps: each runs half of the generated slots (run0 + run1 or
-// run2 + run3, quarters balanced by term count) after computing the element's factors; the block's
-// element matrices are staged in shared memory (one padded record per element, so the half-warps'
-// 8-byte writes spread over the banks) and written out as one contiguous run with consecutive
-// threads on consecutive addresses: full-line stores instead of 32 partial lines per warp store.
-// (One or four threads per element time the same or slower.)
-constexpr int kGenElems = 32;
-template <int D, int L, int VAR>
-__global__ void __launch_bounds__(2 * kGenElems) elem_gen_ff_kernel(int64_t ne, const float2* __restrict__ geo,
-                                                                  const int32_t* __restrict__ conn, FormArgs a,
-                                                                  float2* __restrict__ K, float2* __restrict__ Kd) {
-    using GT = GenTerms<D, L, VAR>;
-    constexpr int NP = D + 1, NS = NP * (NP + 1) / 2, LL = L * L, PADLL = LL | 1;
-    extern __shared__ float2 kst[];
-    const int64_t e0 = blockIdx.x * (int64_t)kGenElems;
-    const int el = threadIdx.x % kGenElems, part = threadIdx.x / kGenElems;  // one part per warp: no divergence
-    const int64_t e = e0 + el;
-    if (e < ne) {
-    float2 F[GT::NG];
+// The factors of the generated element code for element e: F[0] = mass |det J|, F[1 + pq] =
+// dt eps |det J| grad(lam_p).grad(lam_q), then the convection factors -dt |det J| w.grad(lam_p)
+// (constant wind, VAR 0) or -dt |det J| w(v).grad(lam_p) per vertex v (vertex wind, VAR 1).
+template <int D, int L, int VAR, int NG>
+__device__ __forceinline__ void gen_factors(int64_t e, int64_t ne, const float2* __restrict__ geo,
+                                            const int32_t* __restrict__ conn, const FormArgs& a, float2 (&F)[NG]) {
+    constexpr int NP = D + 1, NS = NP * (NP + 1) / 2;
 #pragma unroll
-    for (int g = 0; g < GT::NG; g++) F[g] = make_float2(0.f, 0.f);
+    for (int g = 0; g < NG; g++) F[g] = make_float2(0.f, 0.f);
     const float2 cm = ff_split(a.mass), cs = ff_split(a.dt * a.diff), cw = ff_split(-a.dt);
     F[0] = ff_prod(cm, __ldg(geo + e));
 #pragma unroll
@@ -613,12 +601,36 @@ __global__ void __launch_bounds__(2 * kGenElems) elem_gen_ff_kernel(int64_t ne, 
             }
         }
     }
+}
+
+// Two threads per element, in two warps: each runs half of the generated slots (run0 + run1 or
+// run2 + run3, quarters balanced by term count) after computing the element's factors; the block's
+// element matrices are staged in shared memory (one padded record per element, so the half-warps'
+// 8-byte writes spread over the banks) and written out as one contiguous run with consecutive
+// threads on consecutive addresses: full-line stores instead of 32 partial lines per warp store.
+// (One or four threads per element time the same or slower.)
+constexpr int kGenElems = 32;
+template <int D, int L, int VAR>
+__global__ void __launch_bounds__(2 * kGenElems) elem_gen_ff_kernel(int64_t ne, const float2* __restrict__ geo,
+                                                                  const int32_t* __restrict__ conn, FormArgs a,
+                                                                  float2* __restrict__ K, float2* __restrict__ Kd) {
+    using GT = GenTerms<D, L, VAR>;
+    constexpr int LL = L * L, PADLL = LL | 1;
+    extern __shared__ float2 kst[];
+    const int64_t e0 = blockIdx.x * (int64_t)kGenElems;
+    const int el = threadIdx.x % kGenElems, part = threadIdx.x / kGenElems;  // one part per warp: no divergence
+    const int64_t e = e0 + el;
+    if (e < ne) {
+    float2 F[GT::NG];
+    gen_factors<D, L, VAR>(e, ne, geo, conn, a, F);
+    float2* __restrict__ rec = kst + el * PADLL;
+    auto st = [rec](int idx, float2 v) { rec[idx] = v; };
     if (part == 0) {
-        GT::run0(F, kst + el * PADLL);
-        GT::run1(F, kst + el * PADLL);
+        GT::run0(F, st);
+        GT::run1(F, st);
     } else {
-        GT::run2(F, kst + el * PADLL);
-        GT::run3(F, kst + el * PADLL);
+        GT::run2(F, st);
+        GT::run3(F, st);
     }
     }
     __syncthreads();
@@ -940,6 +952,279 @@ __global__ void __launch_bounds__(256) csr_gather_kernel(int64_t nnz, const int3
 }
 
 // Element right-hand sides: dt (f, phi_i) + mass (u_prev, phi_i) + boundary data.
+// ---------------------------------------------------------------------------------------------
+// Element ring: pipelined assembly of element-only forms in double-float (H1 spaces with generated
+// element code), one persistent launch that works through a list of tiles in a fixed order, taking
+// them one at a time from an atomic ticket:
+//   E  element tile: 128 elements of chunk c (CE consecutive elements) write their element matrices
+//      into ring slot c mod R in structure-of-arrays order (entry (i, j) of element e at
+//      slot + (i L + j) CE + e mod CE: consecutive lanes, consecutive addresses);
+//   D  diagonal tile (up to 256 consecutive rows): each row's sum of K_e[i][i] over its incidences,
+//      then D^-1 in FP64 and FP32;
+//   G  row tile (the same rows): every CSR entry of the rows, the sum of its element-matrix entries
+//      in incidence order (the lists of the two-pass gather, each entry's element found through the
+//      row's incidence list: 2 bytes per entry), then the FP64 value, the FP32 copies and A D^-1
+//      (SELL-32 positions computed from the row and the entry's place in it).
+// Stages: a row tile's D stage is the last chunk its rows' elements lie in, its G stage the last D
+// stage among its rows' columns. Tickets go by rounds t = 0, 1, ...: the E tiles of chunk t, the D
+// tiles of stage t - 1, the G tiles of stage t - 2. A tile waits (thread 0, bounded spin on per-stage
+// completion counters) only for tiles with smaller tickets: D for the chunks it reads, G for those
+// and for the D stages of its columns, E(t) for every D and G tile reading chunk t - R, the chunk
+// whose slot it overwrites (R is chosen on the host so that those tickets come at least two rounds
+// earlier). A tile a running block holds therefore never waits for a tile no running block holds,
+// and the launch finishes. The ring is sized to half of L2 and accessed with an L2 evict-last
+// policy, then discarded from L2: element matrices do not round-trip through DRAM. The sums are the
+// two-pass assembly's, term for term and in the same order, so the values are bit-identical.
+constexpr int kRingThreads = 256;
+constexpr int kRingElems = 128;   // elements per element tile (two threads each, as elem_gen_ff_kernel)
+constexpr int kRingRows = 256;    // rows per diagonal / row tile (at most)
+constexpr unsigned kRingSpin = 1u << 20;  // polls before a wait gives up (with the back-off, about a second)
+
+struct RingArgs {
+    int64_t ne;
+    const float2* geo;
+    const int32_t* conn;
+    FormArgs a;
+    float2* ring;
+    int ce_shift, rmask;            // CE = 1 << ce_shift elements per chunk, R = rmask + 1 slots
+    int nchunk, nitems;
+    const int4* items;              // in ticket order: {kind (0 E, 1 D, 2 G), stage, E: first element / D, G: tile, 0}
+    const int32_t* tile_row;        // row tiles: first rows (ntiles + 1)
+    const int4* tile_wait;          // per row tile: {first chunk read, D stage, first D stage of the columns, G stage}
+    const int2* chunk_wait;         // per chunk j: the stages [lo, hi] of the D and G tiles that read it
+    const int32_t* rowptr;
+    const int32_t* col;
+    const int32_t* inc_ptr;
+    const int32_t* inc;
+    const int32_t* seg;             // per CSR entry, its run in con (the two-pass gather's runs)
+    const uint16_t* con;            // per contribution: (place of the element in the row's incidences) << 4 | j
+    const uint8_t* freed;
+    const int32_t* sell_off;        // SELL-32 slice offsets for svals32, or null (CSR order)
+    double* vals;
+    float* vals32;
+    double* svals64;
+    float* svals32;
+    double* dinv;
+    float* dinv32;
+    unsigned* cnt;                  // [0] ticket, [1] error flag, then done tiles per stage: E, D, G (nchunk each)
+    const int32_t* need;            // tiles per stage: E, D, G (nchunk each)
+};
+
+__device__ __forceinline__ unsigned ld_acquire_u32(const unsigned* p) {
+    unsigned v;
+    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+__device__ __forceinline__ uint64_t l2_evict_last_policy() {
+    uint64_t p;
+    asm volatile("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;" : "=l"(p));
+    return p;
+}
+__device__ __forceinline__ void st_ring(float2* p, float2 v, uint64_t pol) {
+    asm volatile("st.global.L2::cache_hint.v2.f32 [%0], {%1, %2}, %3;" ::"l"(p), "f"(v.x), "f"(v.y), "l"(pol)
+                 : "memory");
+}
+__device__ __forceinline__ float2 ld_ring(const float2* p, uint64_t pol) {
+    float2 v;
+    asm volatile("ld.global.cg.L2::cache_hint.v2.f32 {%0, %1}, [%2], %3;" : "=f"(v.x), "=f"(v.y) : "l"(p), "l"(pol)
+                 : "memory");
+    return v;
+}
+template <int L>
+__device__ __forceinline__ const float2* ring_at(const RingArgs& g, int32_t e, int idx) {
+    const int64_t slot = (e >> g.ce_shift) & g.rmask;
+    return g.ring + ((slot * (L * L) + idx) << g.ce_shift) + (e & ((1 << g.ce_shift) - 1));
+}
+
+// Waits (one thread) until every tile of kind `kind` and stages lo..hi is done; on giving up it sets
+// the error flag and returns, so the launch always ends.
+__device__ void ring_wait(const RingArgs& g, int kind, int lo, int hi) {
+    if (ld_acquire_u32(g.cnt + 1)) return;
+    const unsigned* done = g.cnt + 2 + (int64_t)kind * g.nchunk;
+    const int32_t* need = g.need + (int64_t)kind * g.nchunk;
+    lo = max(lo, 0);
+    hi = min(hi, g.nchunk - 1);
+    for (int s = lo; s <= hi; s++) {
+        const unsigned want = (unsigned)__ldg(need + s);
+        unsigned it = 0;
+        while (ld_acquire_u32(done + s) < want) {
+            // after one wait has given up, every later wait returns at once
+            if (++it >= kRingSpin || (it % 1024 == 0 && ld_acquire_u32(g.cnt + 1))) {
+                atomicOr(g.cnt + 1, 1u);
+                return;
+            }
+            __nanosleep(it < 64 ? 32 : 256);
+        }
+    }
+}
+
+template <int D, int L, int VAR>
+__global__ void __launch_bounds__(kRingThreads, 2) ring_assemble_kernel(RingArgs g) {
+    using GT = GenTerms<D, L, VAR>;
+    __shared__ int4 s_it;
+    __shared__ int32_t s_rp[kRingRows + 1], s_ip[kRingRows + 1];
+    const int tid = threadIdx.x;
+    const uint64_t pol = l2_evict_last_policy();
+    for (;;) {
+        if (tid == 0) {
+            const unsigned t = atomicAdd(g.cnt, 1u);
+            int4 it = make_int4(-1, 0, 0, 0);
+            if (t < (unsigned)g.nitems) {
+                it = __ldg(g.items + t);
+                if (it.x == 0) {
+                    // the slot's previous chunk must have been read by all its D and G tiles
+                    const int j = it.y - (g.rmask + 1);
+                    if (j >= 0) {
+                        const int2 w = __ldg(g.chunk_wait + j);
+                        ring_wait(g, 1, w.x, w.y);
+                        ring_wait(g, 2, w.x, w.y);
+                    }
+                } else {
+                    const int4 w = __ldg(g.tile_wait + it.z);
+                    ring_wait(g, 0, w.x, w.y);               // the chunks its rows' elements lie in
+                    if (it.x == 2) ring_wait(g, 1, w.z, w.w);  // the diagonals of its columns
+                }
+                __threadfence();
+            }
+            s_it = it;
+        }
+        __syncthreads();
+        const int4 it = s_it;
+        if (it.x < 0) return;
+        if (it.x == 0) {
+            // element tile: warp w holds elements (w / 2) * 32 + lane, half (w % 2) of the slots
+            const int w = tid >> 5, lane = tid & 31;
+            const int64_t e = (int64_t)it.z + (w >> 1) * 32 + lane;
+            if (e < g.ne) {
+                float2 F[GT::NG];
+                gen_factors<D, L, VAR>(e, g.ne, g.geo, g.conn, g.a, F);
+                float2* slot = g.ring + (((int64_t)(it.y & g.rmask) * (L * L)) << g.ce_shift) +
+                               (e & ((1 << g.ce_shift) - 1));
+                const int sh = g.ce_shift;
+                auto st = [slot, sh, pol](int idx, float2 v) { st_ring(slot + ((int64_t)idx << sh), v, pol); };
+                if ((w & 1) == 0) {
+                    GT::run0(F, st);
+                    GT::run1(F, st);
+                } else {
+                    GT::run2(F, st);
+                    GT::run3(F, st);
+                }
+            }
+        } else if (it.x == 1) {
+            // diagonal tile: one thread per row, incidences four at a time
+            const int32_t r0 = __ldg(g.tile_row + it.z), r1 = __ldg(g.tile_row + it.z + 1);
+            const int32_t r = r0 + tid;
+            if (r < r1 && g.dinv) {
+                float h = 0.f, l = 0.f;
+                const int32_t k0 = __ldg(g.inc_ptr + r), k1 = __ldg(g.inc_ptr + r + 1);
+                for (int32_t k = k0; k < k1; k += 4) {
+                    int32_t fl[4];
+                    float2 v[4];
+#pragma unroll
+                    for (int t = 0; t < 4; t++) fl[t] = k + t < k1 ? __ldg(g.inc + k + t) : -1;
+#pragma unroll
+                    for (int t = 0; t < 4; t++) {
+                        v[t] = make_float2(0.f, 0.f);
+                        if (fl[t] >= 0) {
+                            const int32_t e = fl[t] / L, i = fl[t] - e * L;
+                            v[t] = ld_ring(ring_at<L>(g, e, i * (L + 1)), pol);
+                        }
+                    }
+#pragma unroll
+                    for (int t = 0; t < 4; t++)
+                        if (fl[t] >= 0) ff_add(h, l, v[t].x, v[t].y);
+                }
+                const double d = ff_to_double(h, l);
+                const double di = (__ldg(g.freed + r) && d != 0.0) ? 1.0 / d : 0.0;
+                g.dinv[r] = di;
+                if (g.dinv32) g.dinv32[r] = (float)di;
+            }
+        } else {
+            // row tile: one thread per CSR entry
+            const int32_t r0 = __ldg(g.tile_row + it.z), r1 = __ldg(g.tile_row + it.z + 1);
+            const int nr = r1 - r0;
+            for (int q = tid; q <= nr; q += kRingThreads) {
+                s_rp[q] = __ldg(g.rowptr + r0 + q);
+                s_ip[q] = __ldg(g.inc_ptr + r0 + q);
+            }
+            __syncthreads();
+            const int32_t kb = s_rp[0], ke = s_rp[nr];
+            for (int32_t k = kb + tid; k < ke; k += kRingThreads) {
+                int lo = 0, hi = nr;  // s_rp[lo] <= k < s_rp[hi]
+                while (hi - lo > 1) {
+                    const int mid = (lo + hi) >> 1;
+                    if (s_rp[mid] <= k) lo = mid;
+                    else hi = mid;
+                }
+                const int32_t r = r0 + lo, q = k - s_rp[lo], ib = s_ip[lo];
+                const int32_t c0 = __ldcs(g.seg + k), c1 = __ldcs(g.seg + k + 1);
+                const int32_t ck = __ldcs(g.col + k);
+                float h = 0.f, l = 0.f;
+                for (int32_t c = c0; c < c1; c += 4) {
+                    uint32_t cc[4];
+                    int32_t fl[4];
+                    float2 v[4];
+#pragma unroll
+                    for (int t = 0; t < 4; t++) cc[t] = c + t < c1 ? (uint32_t)__ldcs(g.con + c + t) : 0xffffffffu;
+#pragma unroll
+                    for (int t = 0; t < 4; t++) fl[t] = cc[t] != 0xffffffffu ? __ldg(g.inc + ib + (cc[t] >> 4)) : -1;
+#pragma unroll
+                    for (int t = 0; t < 4; t++) {
+                        v[t] = make_float2(0.f, 0.f);
+                        if (fl[t] >= 0) {
+                            const int32_t e = fl[t] / L, i = fl[t] - e * L;
+                            v[t] = ld_ring(ring_at<L>(g, e, i * L + (int)(cc[t] & 15u)), pol);
+                        }
+                    }
+#pragma unroll
+                    for (int t = 0; t < 4; t++)
+                        if (fl[t] >= 0) ff_add(h, l, v[t].x, v[t].y);
+                }
+                const double vv = ff_to_double(h, l);
+                __stcs(g.vals + k, vv);
+                const float v32 = __fadd_rn(h, l);
+                if (g.vals32) __stcs(g.vals32 + k, v32);
+                if (g.svals64) __stcs(g.svals64 + k, vv * __ldcg(g.dinv + ck));
+                if (g.svals32) {
+                    const int64_t pos = g.sell_off ? (int64_t)__ldg(g.sell_off + (r >> 5)) +
+                                                         (((q >> 2) * 32 + (r & 31)) * 4 + (q & 3))
+                                                   : (int64_t)k;
+                    __stcs(g.svals32 + pos, v32 * __ldcg(g.dinv32 + ck));
+                }
+            }
+        }
+        __syncthreads();
+        if (tid == 0) {
+            __threadfence();
+            atomicAdd(g.cnt + 2 + (int64_t)it.x * g.nchunk + it.y, 1u);
+        }
+    }
+}
+
+// Drops the ring's lines from L2 without writing them back (their contents are dead after the
+// assembly), so they do not hold L2 under the evict-last policy afterwards.
+__global__ void ring_discard_kernel(char* ring, int64_t lines) {
+    for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < lines; q += (int64_t)gridDim.x * blockDim.x)
+        asm volatile("discard.global.L2 [%0], 128;" ::"l"(ring + q * 128) : "memory");
+}
+
+// Per contribution of the two-pass gather's lists (src = (e L + i) L + j in CSR order), its 2-byte
+// form for the ring: the place of incidence e L + i in row r's incidence list, and j.
+template <int L>
+__global__ void ring_con_kernel(int64_t nd, const int32_t* __restrict__ rp, const int32_t* __restrict__ seg,
+                                const int32_t* __restrict__ src, const int32_t* __restrict__ inc_ptr,
+                                const int32_t* __restrict__ inc, uint16_t* __restrict__ con) {
+    const int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (r >= nd) return;
+    const int32_t i0 = inc_ptr[r], i1 = inc_ptr[r + 1];
+    for (int32_t c = seg[rp[r]]; c < seg[rp[r + 1]]; c++) {
+        const int32_t s = src[c], ei = s / L, j = s - ei * L;
+        int32_t kl = 0;
+        while (i0 + kl < i1 && inc[i0 + kl] != ei) kl++;
+        con[c] = (uint16_t)((kl << 4) | j);
+    }
+}
+
 template <int D, int L>
 __global__ void rhs_elem_kernel(int64_t ne, const double* __restrict__ X, const int32_t* __restrict__ conn,
                                 const int32_t* __restrict__ dofs, FormArgs a, double dt, int src_kind, double src_const,
@@ -1208,6 +1493,274 @@ FormArgs make_args(const ocmp_space_s* s, const ocmp_form_t* f) {
 
 inline unsigned nblk(int64_t n, int t) { return (unsigned)((n + t - 1) / t); }
 
+// The sorted segmented reduction's lists (once per space, and again if the element ring released
+// the element indices): per CSR entry its run start (d_cseg), per contribution its flat
+// element-matrix index (d_csrc).
+template <int L>
+int ensure_contrib(ocmp_space_s* s, cudaStream_t st) {
+    if (s->d_cseg && s->d_csrc) return OCMP_OK;
+    const int64_t ne = s->mesh->ne, nd = s->ndof;
+    const int64_t ncon = ne * (int64_t)L * L;
+    if (ncon >= (int64_t)INT32_MAX) return fail(OCMP_ERR_UNSUPPORTED, "assembly: too many element entries");
+    if (!s->d_cseg) OCMP_CUDA(cudaMalloc((void**)&s->d_cseg, sizeof(int32_t) * (size_t)(s->nnz + 1)));
+    if (!s->d_csrc) OCMP_CUDA(cudaMalloc((void**)&s->d_csrc, sizeof(int32_t) * (size_t)ncon));
+    const int ct = 128;
+    const size_t csm = sizeof(int32_t) * (size_t)s->maxrow * ct;
+    OCMP_CUDA(cudaFuncSetAttribute(contrib_build_kernel<L>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)csm));
+    OCMP_LAUNCH(contrib_build_kernel<L><<<nblk(nd, ct), ct, csm, st>>>(nd, s->d_rowptr, s->d_inc_ptr, s->d_inc, s->d_slot,
+                                                                  s->slot_stride, s->maxrow, s->d_cseg, s->d_csrc));
+    const int32_t last = (int32_t)ncon;
+    OCMP_CUDA(cudaMemcpyAsync(s->d_cseg + s->nnz, &last, sizeof(int32_t), cudaMemcpyHostToDevice, st));
+    OCMP_CUDA(cudaStreamSynchronize(st));
+    return OCMP_OK;
+}
+
+}  // namespace
+// ---------------------------------------------------------------------------------------------
+// Element ring: the plan (host, once per space) and the launch.
+struct RingPlan {
+    int ce_shift = 0, R = 0, nchunk = 0, nitems = 0, ntiles = 0, grid = 0, L = 0;
+    size_t ring_bytes = 0;
+    float2* ring = nullptr;
+    int4* items = nullptr;
+    int32_t* tile_row = nullptr;
+    int4* tile_wait = nullptr;
+    int2* chunk_wait = nullptr;
+    int32_t* need = nullptr;
+    unsigned* cnt = nullptr;
+    uint16_t* con = nullptr;
+};
+
+void ring_destroy(RingPlan* p) {
+    if (!p) return;
+    void* ps[] = {p->ring, p->items, p->tile_row, p->tile_wait, p->chunk_wait, p->need, p->cnt, p->con};
+    for (void* q : ps)
+        if (q) cudaFree(q);
+    delete p;
+}
+
+namespace {
+
+template <class T>
+int ring_upload(T** d, const std::vector<T>& h) {
+    if (cudaMalloc((void**)d, sizeof(T) * std::max<size_t>(1, h.size())) != cudaSuccess)
+        return fail(OCMP_ERR_NOMEM, "element ring: cudaMalloc");
+    if (!h.empty() && cudaMemcpy(*d, h.data(), sizeof(T) * h.size(), cudaMemcpyHostToDevice) != cudaSuccess)
+        return fail(OCMP_ERR_CUDA, "element ring: cudaMemcpy");
+    return OCMP_OK;
+}
+
+// The schedule for chunks of 1 << ce_shift elements (host). Returns false when the ring it needs
+// exceeds `budget` bytes.
+struct RingSchedule {
+    int R = 0, nchunk = 0;
+    size_t ring_bytes = 0;
+    std::vector<int4> items, tile_wait;
+    std::vector<int32_t> tile_row, need;
+    std::vector<int2> chunk_wait;
+};
+
+bool ring_schedule(const ocmp_space_s* s, int L, const std::vector<int32_t>& inc_ptr,
+                   const std::vector<int32_t>& inc, int ce_shift, size_t budget, RingSchedule& S) {
+    const int64_t ne = s->mesh->ne, nd = s->ndof;
+    const int64_t CE = (int64_t)1 << ce_shift;
+    const int nchunk = (int)((ne + CE - 1) / CE);
+    // the chunks a row's elements lie in
+    std::vector<int32_t> cmin(nd, INT32_MAX), cmax(nd, -1);
+    for (int64_t r = 0; r < nd; r++)
+        for (int32_t k = inc_ptr[r]; k < inc_ptr[r + 1]; k++) {
+            const int32_t c = (int32_t)((inc[k] / L) >> ce_shift);
+            cmin[r] = std::min(cmin[r], c);
+            cmax[r] = std::max(cmax[r], c);
+        }
+    // row tiles: up to kRingRows consecutive rows, not across the space's row ranges (vertex rows,
+    // then edge and interior rows: each range runs through the mesh on its own)
+    std::vector<int32_t> trow;
+    for (size_t q = 0; q + 1 < s->row_ranges.size(); q++)
+        for (int64_t r = s->row_ranges[q]; r < s->row_ranges[q + 1]; r += kRingRows) trow.push_back((int32_t)r);
+    trow.push_back((int32_t)nd);
+    const int nt = (int)trow.size() - 1;
+    std::vector<int32_t> elo(nt), dst(nt), dlo(nt), gst(nt), dst_row(nd);
+    for (int b = 0; b < nt; b++) {
+        int32_t lo = INT32_MAX, hi = -1;
+        for (int32_t r = trow[b]; r < trow[b + 1]; r++) {
+            lo = std::min(lo, cmin[r]);
+            hi = std::max(hi, cmax[r]);
+        }
+        if (hi < 0) return false;  // a row without elements
+        elo[b] = lo;
+        dst[b] = hi;
+        for (int32_t r = trow[b]; r < trow[b + 1]; r++) dst_row[r] = hi;
+    }
+    for (int b = 0; b < nt; b++) {
+        int32_t lo = INT32_MAX, hi = -1;
+        for (int64_t k = s->rowptr[trow[b]]; k < s->rowptr[trow[b + 1]]; k++) {
+            lo = std::min(lo, dst_row[s->col[k]]);
+            hi = std::max(hi, dst_row[s->col[k]]);
+        }
+        dlo[b] = lo;
+        gst[b] = hi;
+    }
+    // the last stage reading each chunk, and the ring length that keeps every overwrite two rounds
+    // behind its readers
+    std::vector<int32_t> last(nchunk, -1);
+    for (int b = 0; b < nt; b++)
+        for (int32_t j = elo[b]; j <= dst[b]; j++) last[j] = std::max(last[j], gst[b]);
+    int lag = 0;
+    for (int j = 0; j < nchunk; j++) lag = std::max(lag, last[j] - j);
+    int R = 4;
+    while (R < lag + 4) R *= 2;
+    const size_t bytes = (size_t)R * (size_t)CE * L * L * sizeof(float2);
+    if (bytes > budget) return false;
+    S.R = R;
+    S.nchunk = nchunk;
+    S.ring_bytes = bytes;
+    S.tile_row = trow;
+    S.tile_wait.resize(nt);
+    for (int b = 0; b < nt; b++) S.tile_wait[b] = make_int4(elo[b], dst[b], dlo[b], gst[b]);
+    S.chunk_wait.resize(nchunk);
+    for (int j = 0; j < nchunk; j++) S.chunk_wait[j] = make_int2(j, last[j]);
+    S.need.assign((size_t)3 * nchunk, 0);
+    std::vector<std::vector<int32_t>> dby(nchunk), gby(nchunk);
+    for (int b = 0; b < nt; b++) {
+        dby[dst[b]].push_back(b);
+        gby[gst[b]].push_back(b);
+        S.need[nchunk + dst[b]]++;
+        S.need[2 * nchunk + gst[b]]++;
+    }
+    for (int t = 0; t < nchunk + 2; t++) {
+        if (t < nchunk)
+            for (int64_t e = (int64_t)t * CE; e < std::min(ne, (int64_t)(t + 1) * CE); e += kRingElems) {
+                S.items.push_back(make_int4(0, t, (int32_t)e, 0));
+                S.need[t]++;
+            }
+        if (t >= 1 && t - 1 < nchunk)
+            for (int32_t b : dby[t - 1]) S.items.push_back(make_int4(1, t - 1, b, 0));
+        if (t >= 2)
+            for (int32_t b : gby[t - 2]) S.items.push_back(make_int4(2, t - 2, b, 0));
+    }
+    return true;
+}
+
+// Plans the ring for space s (first use): on success s->ring holds the device tables, else the
+// space is marked for the two-pass assembly.
+template <int L>
+int ring_plan(ocmp_space_s* s, cudaStream_t st) {
+    s->ring_state = -1;
+    const int64_t ne = s->mesh->ne, nd = s->ndof;
+    if ((int64_t)ne * L >= INT32_MAX || ne * (int64_t)L * L >= INT32_MAX) return OCMP_OK;
+    // the incidence lists, in the order the space stores them (ascending element)
+    std::vector<int32_t> inc_ptr(nd + 1, 0), inc((size_t)ne * L);
+    for (int64_t i = 0; i < ne * L; i++) inc_ptr[s->dofs[i] + 1]++;
+    for (int64_t i = 0; i < nd; i++) inc_ptr[i + 1] += inc_ptr[i];
+    {
+        std::vector<int32_t> fill(inc_ptr.begin(), inc_ptr.end() - 1);
+        for (int64_t i = 0; i < ne * L; i++) inc[fill[s->dofs[i]]++] = (int32_t)i;
+    }
+    for (int64_t r = 0; r < nd; r++)
+        if (inc_ptr[r + 1] - inc_ptr[r] > 4095 || inc_ptr[r + 1] == inc_ptr[r]) return OCMP_OK;
+    int dev = 0, l2 = 0, sms = 0;
+    OCMP_CUDA(cudaGetDevice(&dev));
+    OCMP_CUDA(cudaDeviceGetAttribute(&l2, cudaDevAttrL2CacheSize, dev));
+    OCMP_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    const size_t budget = (size_t)l2 / 2;
+    RingSchedule S;
+    int shift = -1;
+    for (int sh : {11, 10, 9})
+        if (ring_schedule(s, L, inc_ptr, inc, sh, budget, S)) {
+            shift = sh;
+            break;
+        }
+    if (shift < 0) return OCMP_OK;
+    auto* p = new RingPlan();
+    p->ce_shift = shift;
+    p->R = S.R;
+    p->nchunk = S.nchunk;
+    p->nitems = (int)S.items.size();
+    p->ntiles = (int)S.tile_row.size() - 1;
+    p->ring_bytes = S.ring_bytes;
+    p->L = L;
+    int r = OCMP_OK;
+    if (cudaMalloc((void**)&p->ring, S.ring_bytes) != cudaSuccess) r = fail(OCMP_ERR_NOMEM, "element ring: cudaMalloc");
+    if (!r) r = ring_upload(&p->items, S.items);
+    if (!r) r = ring_upload(&p->tile_row, S.tile_row);
+    if (!r) r = ring_upload(&p->tile_wait, S.tile_wait);
+    if (!r) r = ring_upload(&p->chunk_wait, S.chunk_wait);
+    if (!r) r = ring_upload(&p->need, S.need);
+    if (!r && cudaMalloc((void**)&p->cnt, sizeof(unsigned) * (2 + 3 * (size_t)S.nchunk)) != cudaSuccess)
+        r = fail(OCMP_ERR_NOMEM, "element ring: cudaMalloc");
+    // the 2-byte contribution lists, from the two-pass gather's lists (built here if needed, then
+    // released: the ring keeps only the run starts)
+    if (!r) r = ensure_contrib<L>(s, st);
+    if (!r && cudaMalloc((void**)&p->con, sizeof(uint16_t) * (size_t)(ne * L * L)) != cudaSuccess)
+        r = fail(OCMP_ERR_NOMEM, "element ring: cudaMalloc");
+    if (!r) {
+        OCMP_LAUNCH(ring_con_kernel<L><<<nblk(nd, 128), 128, 0, st>>>(nd, s->d_rowptr, s->d_cseg, s->d_csrc, s->d_inc_ptr,
+                                                                      s->d_inc, p->con));
+        if (cudaStreamSynchronize(st) != cudaSuccess) r = fail(OCMP_ERR_CUDA, "element ring: contribution lists");
+    }
+    if (r) {
+        ring_destroy(p);
+        return r;
+    }
+    cudaFree(s->d_csrc);
+    s->d_csrc = nullptr;
+    s->ring = p;
+    s->ring_state = 1;
+    return OCMP_OK;
+}
+
+template <int D, int L, int VAR>
+int ring_launch(ocmp_matrix_s* m, const FormArgs& a, cudaStream_t st) {
+    ocmp_space_s* s = m->space;
+    RingPlan* p = s->ring;
+    if (!p->grid) {
+        int dev = 0, sms = 0, per = 0;
+        OCMP_CUDA(cudaGetDevice(&dev));
+        OCMP_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+        OCMP_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, ring_assemble_kernel<D, L, VAR>, kRingThreads, 0));
+        p->grid = std::max(1, per) * sms;
+    }
+    RingArgs g;
+    g.ne = s->mesh->ne;
+    g.geo = s->d_geo_ff;
+    g.conn = s->mesh->dconn;
+    g.a = a;
+    g.ring = p->ring;
+    g.ce_shift = p->ce_shift;
+    g.rmask = p->R - 1;
+    g.nchunk = p->nchunk;
+    g.nitems = p->nitems;
+    g.items = p->items;
+    g.tile_row = p->tile_row;
+    g.tile_wait = p->tile_wait;
+    g.chunk_wait = p->chunk_wait;
+    g.rowptr = s->d_rowptr;
+    g.col = s->d_col;
+    g.inc_ptr = s->d_inc_ptr;
+    g.inc = s->d_inc;
+    g.seg = s->d_cseg;
+    g.con = p->con;
+    g.freed = s->d_free;
+    g.sell_off = (m->flags & OCMP_MAT_SELL32) ? s->d_sell_off : nullptr;
+    g.vals = m->vals;
+    g.vals32 = m->vals32;
+    g.svals64 = m->svals64;
+    g.svals32 = m->svals32;
+    g.dinv = m->dinv;
+    g.dinv32 = m->dinv32;
+    g.cnt = p->cnt;
+    g.need = p->need;
+    OCMP_CUDA(cudaMemsetAsync(p->cnt, 0, sizeof(unsigned) * (2 + 3 * (size_t)p->nchunk), st));
+    OCMP_LAUNCH(ring_assemble_kernel<D, L, VAR><<<p->grid, kRingThreads, 0, st>>>(g));
+    const int64_t lines = (int64_t)(p->ring_bytes / 128);
+    OCMP_LAUNCH(ring_discard_kernel<<<(unsigned)std::min<int64_t>(nblk(lines, 256), 1184), 256, 0, st>>>(
+        reinterpret_cast<char*>(p->ring), lines));
+    OCMP_CUDA(cudaGetLastError());
+    return OCMP_OK;
+}
+
+
 template <int D, int L>
 int assemble_impl(ocmp_matrix_s* m, const ocmp_form_t* f, cudaStream_t st) {
     ocmp_space_s* s = m->space;
@@ -1234,6 +1787,15 @@ int assemble_impl(ocmp_matrix_s* m, const ocmp_form_t* f, cudaStream_t st) {
         }
         bool done = false;
         if constexpr (GenTerms<D, L, 0>::value && GenTerms<D, L, 1>::value) {
+            // element-only forms: the pipelined element ring, where the numbering allows it
+            const uint32_t bm = f->outflow_mask | f->wn_mask;
+            if (s->kind == OCMP_H1 && !(bm != 0 && s->nbf > 0) && !(m->flags & OCMP_MAT_TWO_PASS)) {
+                if (s->ring_state == 0) {
+                    const int r = ring_plan<L>(s, st);
+                    if (r) return r;
+                }
+                if (s->ring_state == 1) return var == 0 ? ring_launch<D, L, 0>(m, a, st) : ring_launch<D, L, 1>(m, a, st);
+            }
             if (s->kind == OCMP_H1) {
                 const size_t gsm = sizeof(float2) * (size_t)kGenElems * ((L * L) | 1);
                 if (!s->d_Kd) OCMP_CUDA(cudaMalloc((void**)&s->d_Kd, sizeof(float2) * (size_t)ne * L));
@@ -1292,20 +1854,9 @@ int assemble_impl(ocmp_matrix_s* m, const ocmp_form_t* f, cudaStream_t st) {
     const int32_t* spos = (m->flags & OCMP_MAT_SELL32) ? s->d_sell_pos : nullptr;
     if (!use_facets) {
         // element-only assembly: sorted segmented reduction, one thread per CSR entry
-        if (!s->d_cseg) {
-            const int64_t ncon = ne * (int64_t)L * L;
-            if (ncon >= (int64_t)INT32_MAX) return fail(OCMP_ERR_UNSUPPORTED, "assembly: too many element entries");
-            OCMP_CUDA(cudaMalloc((void**)&s->d_cseg, sizeof(int32_t) * (size_t)(s->nnz + 1)));
-            OCMP_CUDA(cudaMalloc((void**)&s->d_csrc, sizeof(int32_t) * (size_t)ncon));
-            const int ct = 128;
-            const size_t csm = sizeof(int32_t) * (size_t)s->maxrow * ct;
-            OCMP_CUDA(cudaFuncSetAttribute(contrib_build_kernel<L>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)csm));
-            OCMP_LAUNCH(contrib_build_kernel<L><<<nblk(nd, ct), ct, csm, st>>>(nd, s->d_rowptr, s->d_inc_ptr, s->d_inc,
-                                                                          s->d_slot, s->slot_stride, s->maxrow,
-                                                                          s->d_cseg, s->d_csrc));
-            const int32_t last = (int32_t)ncon;
-            OCMP_CUDA(cudaMemcpyAsync(s->d_cseg + s->nnz, &last, sizeof(int32_t), cudaMemcpyHostToDevice, st));
-            OCMP_CUDA(cudaStreamSynchronize(st));
+        {
+            const int r = ensure_contrib<L>(s, st);
+            if (r) return r;
         }
         const void* Kc = dfl ? (const void*)Kff : (const void*)s->d_K;
         if (dfl)

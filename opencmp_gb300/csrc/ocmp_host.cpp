@@ -565,6 +565,8 @@ static void free_space_device(ocmp_space_s* s) {
                   s->d_lift_ptr, s->d_lift_pos, s->d_Rm_ff, s->d_geo_ff, s->d_tpos, s->d_cseg, s->d_csrc, s->d_u2, s->d_Kd,
                   s->d_sell_off, s->d_sell_col, s->d_sell_pos};
     for (void* p : ps) dfree(p);
+    ocmp::ring_destroy(s->ring);
+    s->ring = nullptr;
 }
 
 int ocmp_space_create(ocmp_mesh_t mesh, int32_t kind, int32_t order, uint32_t dirichlet_mask, ocmp_space_t* out) {
@@ -1307,7 +1309,8 @@ int ocmp_spmv_axpby(ocmp_matrix_t m, double alpha, const double* x, double beta,
 // Build-time generator (opencmp_gb300/build.py): writes, for the H1 element types of the
 // double-float path, the element-matrix term tables of build_terms as straight-line device code:
 // per (dimension, local size, wind variant) four functions, each writing the entries of a quarter
-// of the symmetric slots (quarters balanced by term count). With every factor index and coefficient
+// of the symmetric slots (quarters balanced by term count) through a store functor st(index, value),
+// index = i * nloc + j, so one generated body serves any element-matrix layout. With every factor index and coefficient
 // a compile-time constant, the factors live in registers and the products need no table loads.
 #include <cstdio>
 
@@ -1357,7 +1360,7 @@ int main(int argc, char** argv) {
                 cut[q] = c;
             }
             auto emit_slots = [&](const char* name, int s0, int s1) {
-                std::fprintf(o, "    static __device__ __forceinline__ void %s(const float2 (&F)[%d], float2* __restrict__ Ke) {\n",
+                std::fprintf(o, "    template <class ST>\n    static __device__ __forceinline__ void %s(const float2 (&F)[%d], ST& st) {\n",
                              name, NG);
                 for (int slot = s0; slot < s1; slot++) {
                     const int i = si[slot], j = sj[slot];
@@ -1366,11 +1369,11 @@ int main(int argc, char** argv) {
                     emit("s", o0, o2);
                     std::fprintf(o, "        float ah = sh, al = sl;\n");
                     emit("a", o2, o3);
-                    std::fprintf(o, "        Ke[%d] = make_float2(ah, al);\n", i * L + j);
+                    std::fprintf(o, "        st(%d, make_float2(ah, al));\n", i * L + j);
                     if (j != i) {
                         std::fprintf(o, "        float bh = sh, bl = sl;\n");
                         emit("b", o3, o4);
-                        std::fprintf(o, "        Ke[%d] = make_float2(bh, bl);\n", j * L + i);
+                        std::fprintf(o, "        st(%d, make_float2(bh, bl));\n", j * L + i);
                     }
                     std::fprintf(o, "        }\n");
                 }
