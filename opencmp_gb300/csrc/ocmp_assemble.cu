@@ -954,67 +954,52 @@ __global__ void __launch_bounds__(256) csr_gather_kernel(int64_t nnz, const int3
 // Element right-hand sides: dt (f, phi_i) + mass (u_prev, phi_i) + boundary data.
 // ---------------------------------------------------------------------------------------------
 // Element ring: pipelined assembly of element-only forms in double-float (H1 spaces with generated
-// element code), one persistent launch that works through a list of tiles in a fixed order, taking
-// them one at a time from an atomic ticket:
-//   E  element tile: 128 elements of chunk c (CE consecutive elements) write their element matrices
-//      into ring slot c mod R in structure-of-arrays order (entry (i, j) of element e at
-//      slot + (i L + j) CE + e mod CE: consecutive lanes, consecutive addresses);
-//   D  diagonal tile (up to 256 consecutive rows): each row's sum of K_e[i][i] over its incidences,
-//      then D^-1 in FP64 and FP32;
-//   G  row tile (the same rows): every CSR entry of the rows, the sum of its element-matrix entries
-//      in incidence order (the lists of the two-pass gather, each entry's element found through the
-//      row's incidence list: 2 bytes per entry), then the FP64 value, the FP32 copies and A D^-1
-//      (SELL-32 positions computed from the row and the entry's place in it).
-// Stages: a row tile's D stage is the last chunk its rows' elements lie in, its G stage the last D
-// stage among its rows' columns. Tickets go by rounds t = 0, 1, ...: the E tiles of chunk t, the D
-// tiles of stage t - 1, the G tiles of stage t - 2. A tile waits (thread 0, bounded spin on per-stage
-// completion counters) only for tiles with smaller tickets: D for the chunks it reads, G for those
-// and for the D stages of its columns, E(t) for every D and G tile reading chunk t - R, the chunk
-// whose slot it overwrites (R is chosen on the host so that those tickets come at least two rounds
-// earlier). A tile a running block holds therefore never waits for a tile no running block holds,
-// and the launch finishes. The ring is sized to half of L2 and accessed with an L2 evict-last
-// policy, then discarded from L2: element matrices do not round-trip through DRAM. The sums are the
-// two-pass assembly's, term for term and in the same order, so the values are bit-identical.
-constexpr int kRingThreads = 256;
-constexpr int kRingElems = 128;   // elements per element tile (two threads each, as elem_gen_ff_kernel)
+// element code). The elements are cut into chunks of CE consecutive elements and the rows into
+// tiles of up to 256 consecutive rows. Per chunk c three kinds of kernel run as nodes of one CUDA
+// graph:
+//   E(c)  the element matrices of chunk c into ring slot c mod R (element-major records, staged in
+//         shared memory for full-line stores, as elem_gen_ff_kernel);
+//   D(s)  the row tiles whose elements end in chunk s (their D stage): per row, the sum of its
+//         incidences' K_e[i][i] from the ring, then D^-1 in FP64 and FP32;
+//   G(s)  the row tiles whose columns' D stages end at s (their G stage): one thread per CSR entry,
+//         the sum of its element-matrix entries from the ring in the two-pass gather's order, then
+//         the FP64 value, the FP32 copies and A D^-1.
+// Graph edges: D(s) after the E chunks its rows read; G(s) after those and after the D stages of
+// its columns; E(c) after every D and G node that reads chunk c - R, the slot it overwrites (R is
+// larger than the widest stage distance, so the graph has no cycle). Independent nodes run
+// concurrently, so element work of later chunks overlaps the gathers of earlier ones, and every
+// kernel has the occupancy of its own register and shared-memory needs. The ring (R CE L^2 float
+// pairs) is sized to at most half of L2 and stored and read with an L2 evict-last policy, then
+// dropped from L2: element matrices do not round-trip through DRAM. The sums are the two-pass
+// assembly's, term for term and in the same order, so the values are bit-identical.
 constexpr int kRingRows = 256;    // rows per diagonal / row tile (at most)
-constexpr unsigned kRingSpin = 1u << 20;  // polls before a wait gives up (with the back-off, about a second)
 
-struct RingArgs {
-    int64_t ne;
-    const float2* geo;
-    const int32_t* conn;
+// Per-assembly arguments (the form and the matrix outputs), written on the device by
+// ring_args_kernel ahead of each graph launch.
+struct RingDev {
     FormArgs a;
-    float2* ring;
-    int ce_shift, rmask;            // CE = 1 << ce_shift elements per chunk, R = rmask + 1 slots
-    int nchunk, nitems;
-    const int4* items;              // in ticket order: {kind (0 E, 1 D, 2 G), stage, E: first element / D, G: tile, 0}
-    const int32_t* tile_row;        // row tiles: first rows (ntiles + 1)
-    const int4* tile_wait;          // per row tile: {first chunk read, D stage, first D stage of the columns, G stage}
-    const int2* chunk_wait;         // per chunk j: the stages [lo, hi] of the D and G tiles that read it
-    const int32_t* rowptr;
-    const int32_t* col;
-    const int32_t* inc_ptr;
-    const int32_t* inc;
-    const int32_t* seg;             // per CSR entry, its run in con (the two-pass gather's runs)
-    const uint16_t* con;            // per contribution: (place of the element in the row's incidences) << 4 | j
-    const uint8_t* freed;
-    const int32_t* sell_off;        // SELL-32 slice offsets for svals32, or null (CSR order)
     double* vals;
     float* vals32;
     double* svals64;
     float* svals32;
+    const int32_t* spos;
     double* dinv;
     float* dinv32;
-    unsigned* cnt;                  // [0] ticket, [1] error flag, then done tiles per stage: E, D, G (nchunk each)
-    const int32_t* need;            // tiles per stage: E, D, G (nchunk each)
 };
 
-__device__ __forceinline__ unsigned ld_acquire_u32(const unsigned* p) {
-    unsigned v;
-    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
-    return v;
+// Ring position of element-matrix entry src = (e L + i) L + j: chunk c = e / CE holds slot c mod R,
+// so the entry sits at src - (c / R) R CE L^2 (c / R by multiply-high: exact for c < 2^16).
+struct RingMap {
+    int ce_shift;
+    unsigned magic;   // ceil(2^32 / R)
+    int64_t span;     // R CE L^2
+};
+template <int L>
+__device__ __forceinline__ int64_t ring_off(const RingMap& m, int32_t src) {
+    const unsigned c = (unsigned)(src / (L * L)) >> m.ce_shift;
+    return (int64_t)src - (int64_t)__umulhi(c, m.magic) * m.span;
 }
+
 __device__ __forceinline__ uint64_t l2_evict_last_policy() {
     uint64_t p;
     asm volatile("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;" : "=l"(p));
@@ -1026,178 +1011,116 @@ __device__ __forceinline__ void st_ring(float2* p, float2 v, uint64_t pol) {
 }
 __device__ __forceinline__ float2 ld_ring(const float2* p, uint64_t pol) {
     float2 v;
-    asm volatile("ld.global.cg.L2::cache_hint.v2.f32 {%0, %1}, [%2], %3;" : "=f"(v.x), "=f"(v.y) : "l"(p), "l"(pol)
-                 : "memory");
+    asm volatile("ld.global.nc.L2::cache_hint.v2.f32 {%0, %1}, [%2], %3;" : "=f"(v.x), "=f"(v.y) : "l"(p), "l"(pol));
     return v;
 }
-template <int L>
-__device__ __forceinline__ const float2* ring_at(const RingArgs& g, int32_t e, int idx) {
-    const int64_t slot = (e >> g.ce_shift) & g.rmask;
-    return g.ring + ((slot * (L * L) + idx) << g.ce_shift) + (e & ((1 << g.ce_shift) - 1));
-}
 
-// Waits (one thread) until every tile of kind `kind` and stages lo..hi is done; on giving up it sets
-// the error flag and returns, so the launch always ends.
-__device__ void ring_wait(const RingArgs& g, int kind, int lo, int hi) {
-    if (ld_acquire_u32(g.cnt + 1)) return;
-    const unsigned* done = g.cnt + 2 + (int64_t)kind * g.nchunk;
-    const int32_t* need = g.need + (int64_t)kind * g.nchunk;
-    lo = max(lo, 0);
-    hi = min(hi, g.nchunk - 1);
-    for (int s = lo; s <= hi; s++) {
-        const unsigned want = (unsigned)__ldg(need + s);
-        unsigned it = 0;
-        while (ld_acquire_u32(done + s) < want) {
-            // after one wait has given up, every later wait returns at once
-            if (++it >= kRingSpin || (it % 1024 == 0 && ld_acquire_u32(g.cnt + 1))) {
-                atomicOr(g.cnt + 1, 1u);
-                return;
-            }
-            __nanosleep(it < 64 ? 32 : 256);
+__global__ void ring_args_kernel(RingDev* dev, RingDev v) { *dev = v; }
+
+template <int D, int L, int VAR>
+__global__ void __launch_bounds__(2 * kGenElems) ring_elem_kernel(const RingDev* __restrict__ dev, int64_t ne,
+                                                                const float2* __restrict__ geo,
+                                                                const int32_t* __restrict__ conn, int64_t e_begin,
+                                                                int64_t e_end, float2* __restrict__ slot) {
+    using GT = GenTerms<D, L, VAR>;
+    constexpr int LL = L * L, PADLL = LL | 1;
+    extern __shared__ float2 kst[];
+    const int64_t e0 = e_begin + blockIdx.x * (int64_t)kGenElems;
+    const int el = threadIdx.x % kGenElems, part = threadIdx.x / kGenElems;
+    const int64_t e = e0 + el;
+    if (e < e_end) {
+        const FormArgs a = dev->a;
+        float2 F[GT::NG];
+        gen_factors<D, L, VAR>(e, ne, geo, conn, a, F);
+        float2* __restrict__ rec = kst + el * PADLL;
+        auto st = [rec](int idx, float2 v) { rec[idx] = v; };
+        if (part == 0) {
+            GT::run0(F, st);
+            GT::run1(F, st);
+        } else {
+            GT::run2(F, st);
+            GT::run3(F, st);
         }
+    }
+    __syncthreads();
+    const uint64_t pol = l2_evict_last_policy();
+    const int nb = (int)min((int64_t)kGenElems, e_end - e0);
+    float2* __restrict__ dst = slot + (e0 - e_begin) * LL;
+    for (int q = threadIdx.x; q < nb * LL; q += blockDim.x) {
+        const int t = q / LL;
+        st_ring(dst + q, kst[t * PADLL + (q - t * LL)], pol);
     }
 }
 
-template <int D, int L, int VAR>
-__global__ void __launch_bounds__(kRingThreads, 2) ring_assemble_kernel(RingArgs g) {
-    using GT = GenTerms<D, L, VAR>;
-    __shared__ int4 s_it;
-    __shared__ int32_t s_rp[kRingRows + 1], s_ip[kRingRows + 1];
-    const int tid = threadIdx.x;
+// One block per row tile (rows [t.x, t.y)), one thread per row: incidences four at a time.
+template <int L>
+__global__ void __launch_bounds__(kRingRows) ring_diag_kernel(const RingDev* __restrict__ dev,
+                                                             const int2* __restrict__ tiles, RingMap mp,
+                                                             const float2* __restrict__ ring,
+                                                             const int32_t* __restrict__ inc_ptr,
+                                                             const int32_t* __restrict__ inc,
+                                                             const uint8_t* __restrict__ freed) {
+    const int2 t = tiles[blockIdx.x];
+    const int32_t r = t.x + threadIdx.x;
+    double* __restrict__ dinv = dev->dinv;
+    if (r >= t.y || !dinv) return;
+    float* __restrict__ dinv32 = dev->dinv32;
     const uint64_t pol = l2_evict_last_policy();
-    for (;;) {
-        if (tid == 0) {
-            const unsigned t = atomicAdd(g.cnt, 1u);
-            int4 it = make_int4(-1, 0, 0, 0);
-            if (t < (unsigned)g.nitems) {
-                it = __ldg(g.items + t);
-                if (it.x == 0) {
-                    // the slot's previous chunk must have been read by all its D and G tiles
-                    const int j = it.y - (g.rmask + 1);
-                    if (j >= 0) {
-                        const int2 w = __ldg(g.chunk_wait + j);
-                        ring_wait(g, 1, w.x, w.y);
-                        ring_wait(g, 2, w.x, w.y);
-                    }
-                } else {
-                    const int4 w = __ldg(g.tile_wait + it.z);
-                    ring_wait(g, 0, w.x, w.y);               // the chunks its rows' elements lie in
-                    if (it.x == 2) ring_wait(g, 1, w.z, w.w);  // the diagonals of its columns
-                }
-                __threadfence();
-            }
-            s_it = it;
-        }
-        __syncthreads();
-        const int4 it = s_it;
-        if (it.x < 0) return;
-        if (it.x == 0) {
-            // element tile: warp w holds elements (w / 2) * 32 + lane, half (w % 2) of the slots
-            const int w = tid >> 5, lane = tid & 31;
-            const int64_t e = (int64_t)it.z + (w >> 1) * 32 + lane;
-            if (e < g.ne) {
-                float2 F[GT::NG];
-                gen_factors<D, L, VAR>(e, g.ne, g.geo, g.conn, g.a, F);
-                float2* slot = g.ring + (((int64_t)(it.y & g.rmask) * (L * L)) << g.ce_shift) +
-                               (e & ((1 << g.ce_shift) - 1));
-                const int sh = g.ce_shift;
-                auto st = [slot, sh, pol](int idx, float2 v) { st_ring(slot + ((int64_t)idx << sh), v, pol); };
-                if ((w & 1) == 0) {
-                    GT::run0(F, st);
-                    GT::run1(F, st);
-                } else {
-                    GT::run2(F, st);
-                    GT::run3(F, st);
-                }
-            }
-        } else if (it.x == 1) {
-            // diagonal tile: one thread per row, incidences four at a time
-            const int32_t r0 = __ldg(g.tile_row + it.z), r1 = __ldg(g.tile_row + it.z + 1);
-            const int32_t r = r0 + tid;
-            if (r < r1 && g.dinv) {
-                float h = 0.f, l = 0.f;
-                const int32_t k0 = __ldg(g.inc_ptr + r), k1 = __ldg(g.inc_ptr + r + 1);
-                for (int32_t k = k0; k < k1; k += 4) {
-                    int32_t fl[4];
-                    float2 v[4];
+    float h = 0.f, l = 0.f;
+    const int32_t k0 = __ldg(inc_ptr + r), k1 = __ldg(inc_ptr + r + 1);
+    for (int32_t k = k0; k < k1; k += 4) {
+        int32_t fl[4];
+        float2 v[4];
 #pragma unroll
-                    for (int t = 0; t < 4; t++) fl[t] = k + t < k1 ? __ldg(g.inc + k + t) : -1;
+        for (int q = 0; q < 4; q++) fl[q] = k + q < k1 ? __ldg(inc + k + q) : -1;
 #pragma unroll
-                    for (int t = 0; t < 4; t++) {
-                        v[t] = make_float2(0.f, 0.f);
-                        if (fl[t] >= 0) {
-                            const int32_t e = fl[t] / L, i = fl[t] - e * L;
-                            v[t] = ld_ring(ring_at<L>(g, e, i * (L + 1)), pol);
-                        }
-                    }
+        for (int q = 0; q < 4; q++)
+            v[q] = fl[q] >= 0 ? ld_ring(ring + ring_off<L>(mp, fl[q] * L + fl[q] % L), pol) : make_float2(0.f, 0.f);
 #pragma unroll
-                    for (int t = 0; t < 4; t++)
-                        if (fl[t] >= 0) ff_add(h, l, v[t].x, v[t].y);
-                }
-                const double d = ff_to_double(h, l);
-                const double di = (__ldg(g.freed + r) && d != 0.0) ? 1.0 / d : 0.0;
-                g.dinv[r] = di;
-                if (g.dinv32) g.dinv32[r] = (float)di;
-            }
-        } else {
-            // row tile: one thread per CSR entry
-            const int32_t r0 = __ldg(g.tile_row + it.z), r1 = __ldg(g.tile_row + it.z + 1);
-            const int nr = r1 - r0;
-            for (int q = tid; q <= nr; q += kRingThreads) {
-                s_rp[q] = __ldg(g.rowptr + r0 + q);
-                s_ip[q] = __ldg(g.inc_ptr + r0 + q);
-            }
-            __syncthreads();
-            const int32_t kb = s_rp[0], ke = s_rp[nr];
-            for (int32_t k = kb + tid; k < ke; k += kRingThreads) {
-                int lo = 0, hi = nr;  // s_rp[lo] <= k < s_rp[hi]
-                while (hi - lo > 1) {
-                    const int mid = (lo + hi) >> 1;
-                    if (s_rp[mid] <= k) lo = mid;
-                    else hi = mid;
-                }
-                const int32_t r = r0 + lo, q = k - s_rp[lo], ib = s_ip[lo];
-                const int32_t c0 = __ldcs(g.seg + k), c1 = __ldcs(g.seg + k + 1);
-                const int32_t ck = __ldcs(g.col + k);
-                float h = 0.f, l = 0.f;
-                for (int32_t c = c0; c < c1; c += 4) {
-                    uint32_t cc[4];
-                    int32_t fl[4];
-                    float2 v[4];
+        for (int q = 0; q < 4; q++)
+            if (fl[q] >= 0) ff_add(h, l, v[q].x, v[q].y);
+    }
+    const double d = ff_to_double(h, l);
+    const double di = (__ldg(freed + r) && d != 0.0) ? 1.0 / d : 0.0;
+    dinv[r] = di;
+    if (dinv32) dinv32[r] = (float)di;
+}
+
+// One thread per CSR entry of the block's entry range [b.x, b.y): csr_gather_kernel's double-float
+// sum, with the element-matrix entries read from the ring.
+template <int L>
+__global__ void __launch_bounds__(256) ring_gather_kernel(const RingDev* __restrict__ dev,
+                                                         const int2* __restrict__ blocks, RingMap mp,
+                                                         const float2* __restrict__ ring,
+                                                         const int32_t* __restrict__ seg,
+                                                         const int32_t* __restrict__ src,
+                                                         const int32_t* __restrict__ col) {
+    const int2 b = blocks[blockIdx.x];
+    const int32_t k = b.x + threadIdx.x;
+    if (k >= b.y) return;
+    const uint64_t pol = l2_evict_last_policy();
+    const int32_t s0 = __ldcs(seg + k), s1 = __ldcs(seg + k + 1);
+    float h = 0.f, l = 0.f;
+    for (int32_t q0 = s0; q0 < s1; q0 += 4) {
+        int32_t ix[4];
+        float2 v[4];
 #pragma unroll
-                    for (int t = 0; t < 4; t++) cc[t] = c + t < c1 ? (uint32_t)__ldcs(g.con + c + t) : 0xffffffffu;
+        for (int t = 0; t < 4; t++) ix[t] = q0 + t < s1 ? __ldcs(src + q0 + t) : -1;
 #pragma unroll
-                    for (int t = 0; t < 4; t++) fl[t] = cc[t] != 0xffffffffu ? __ldg(g.inc + ib + (cc[t] >> 4)) : -1;
+        for (int t = 0; t < 4; t++) v[t] = ix[t] >= 0 ? ld_ring(ring + ring_off<L>(mp, ix[t]), pol) : make_float2(0.f, 0.f);
 #pragma unroll
-                    for (int t = 0; t < 4; t++) {
-                        v[t] = make_float2(0.f, 0.f);
-                        if (fl[t] >= 0) {
-                            const int32_t e = fl[t] / L, i = fl[t] - e * L;
-                            v[t] = ld_ring(ring_at<L>(g, e, i * L + (int)(cc[t] & 15u)), pol);
-                        }
-                    }
-#pragma unroll
-                    for (int t = 0; t < 4; t++)
-                        if (fl[t] >= 0) ff_add(h, l, v[t].x, v[t].y);
-                }
-                const double vv = ff_to_double(h, l);
-                __stcs(g.vals + k, vv);
-                const float v32 = __fadd_rn(h, l);
-                if (g.vals32) __stcs(g.vals32 + k, v32);
-                if (g.svals64) __stcs(g.svals64 + k, vv * __ldcg(g.dinv + ck));
-                if (g.svals32) {
-                    const int64_t pos = g.sell_off ? (int64_t)__ldg(g.sell_off + (r >> 5)) +
-                                                         (((q >> 2) * 32 + (r & 31)) * 4 + (q & 3))
-                                                   : (int64_t)k;
-                    __stcs(g.svals32 + pos, v32 * __ldcg(g.dinv32 + ck));
-                }
-            }
-        }
-        __syncthreads();
-        if (tid == 0) {
-            __threadfence();
-            atomicAdd(g.cnt + 2 + (int64_t)it.x * g.nchunk + it.y, 1u);
-        }
+        for (int t = 0; t < 4; t++)
+            if (ix[t] >= 0) ff_add(h, l, v[t].x, v[t].y);
+    }
+    const RingDev* d = dev;
+    const double vv = ff_to_double(h, l);
+    __stcs(d->vals + k, vv);
+    const float v32 = __fadd_rn(h, l);
+    if (d->vals32) __stcs(d->vals32 + k, v32);
+    if (d->svals64 || d->svals32) {
+        const int32_t ck = __ldcs(col + k);
+        if (d->svals64) __stcs(d->svals64 + k, vv * __ldg(d->dinv + ck));
+        if (d->svals32) __stcs(d->svals32 + (d->spos ? __ldg(d->spos + k) : k), v32 * __ldg(d->dinv32 + ck));
     }
 }
 
@@ -1206,23 +1129,6 @@ __global__ void __launch_bounds__(kRingThreads, 2) ring_assemble_kernel(RingArgs
 __global__ void ring_discard_kernel(char* ring, int64_t lines) {
     for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < lines; q += (int64_t)gridDim.x * blockDim.x)
         asm volatile("discard.global.L2 [%0], 128;" ::"l"(ring + q * 128) : "memory");
-}
-
-// Per contribution of the two-pass gather's lists (src = (e L + i) L + j in CSR order), its 2-byte
-// form for the ring: the place of incidence e L + i in row r's incidence list, and j.
-template <int L>
-__global__ void ring_con_kernel(int64_t nd, const int32_t* __restrict__ rp, const int32_t* __restrict__ seg,
-                                const int32_t* __restrict__ src, const int32_t* __restrict__ inc_ptr,
-                                const int32_t* __restrict__ inc, uint16_t* __restrict__ con) {
-    const int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    if (r >= nd) return;
-    const int32_t i0 = inc_ptr[r], i1 = inc_ptr[r + 1];
-    for (int32_t c = seg[rp[r]]; c < seg[rp[r + 1]]; c++) {
-        const int32_t s = src[c], ei = s / L, j = s - ei * L;
-        int32_t kl = 0;
-        while (i0 + kl < i1 && inc[i0 + kl] != ei) kl++;
-        con[c] = (uint16_t)((kl << 4) | j);
-    }
 }
 
 template <int D, int L>
@@ -1517,23 +1423,26 @@ int ensure_contrib(ocmp_space_s* s, cudaStream_t st) {
 
 }  // namespace
 // ---------------------------------------------------------------------------------------------
-// Element ring: the plan (host, once per space) and the launch.
+// Element ring: the plan (host, once per space), the graph (once per space and wind variant) and
+// the launch.
 struct RingPlan {
-    int ce_shift = 0, R = 0, nchunk = 0, nitems = 0, ntiles = 0, grid = 0, L = 0;
+    int ce_shift = 0, R = 0, nchunk = 0, L = 0;
     size_t ring_bytes = 0;
     float2* ring = nullptr;
-    int4* items = nullptr;
-    int32_t* tile_row = nullptr;
-    int4* tile_wait = nullptr;
-    int2* chunk_wait = nullptr;
-    int32_t* need = nullptr;
-    unsigned* cnt = nullptr;
-    uint16_t* con = nullptr;
+    RingDev* dev = nullptr;
+    int2* dtiles = nullptr;          // row ranges of the D nodes' tiles, stage after stage
+    int2* gblocks = nullptr;         // entry ranges (<= 256 entries) of the G nodes, stage after stage
+    std::vector<int> doff, goff;     // per stage: first tile / block (nchunk + 1)
+    std::vector<int32_t> dlo_e, glo_e, ghi_e, glo_d, last;  // per stage: chunks / stages waited on
+    cudaGraphExec_t exec[2] = {nullptr, nullptr};
+    int nodes[2] = {0, 0};
 };
 
 void ring_destroy(RingPlan* p) {
     if (!p) return;
-    void* ps[] = {p->ring, p->items, p->tile_row, p->tile_wait, p->chunk_wait, p->need, p->cnt, p->con};
+    for (cudaGraphExec_t e : p->exec)
+        if (e) cudaGraphExecDestroy(e);
+    void* ps[] = {p->ring, p->dev, p->dtiles, p->gblocks};
     for (void* q : ps)
         if (q) cudaFree(q);
     delete p;
@@ -1550,14 +1459,14 @@ int ring_upload(T** d, const std::vector<T>& h) {
     return OCMP_OK;
 }
 
-// The schedule for chunks of 1 << ce_shift elements (host). Returns false when the ring it needs
-// exceeds `budget` bytes.
+// The schedule for chunks of 1 << ce_shift elements. Returns false when the ring it needs exceeds
+// `budget` bytes.
 struct RingSchedule {
     int R = 0, nchunk = 0;
     size_t ring_bytes = 0;
-    std::vector<int4> items, tile_wait;
-    std::vector<int32_t> tile_row, need;
-    std::vector<int2> chunk_wait;
+    std::vector<int2> dtiles, gblocks;
+    std::vector<int> doff, goff;
+    std::vector<int32_t> dlo_e, glo_e, ghi_e, glo_d, last;
 };
 
 bool ring_schedule(const ocmp_space_s* s, int L, const std::vector<int32_t>& inc_ptr,
@@ -1565,6 +1474,7 @@ bool ring_schedule(const ocmp_space_s* s, int L, const std::vector<int32_t>& inc
     const int64_t ne = s->mesh->ne, nd = s->ndof;
     const int64_t CE = (int64_t)1 << ce_shift;
     const int nchunk = (int)((ne + CE - 1) / CE);
+    if (nchunk >= (1 << 16)) return false;
     // the chunks a row's elements lie in
     std::vector<int32_t> cmin(nd, INT32_MAX), cmax(nd, -1);
     for (int64_t r = 0; r < nd; r++)
@@ -1574,7 +1484,7 @@ bool ring_schedule(const ocmp_space_s* s, int L, const std::vector<int32_t>& inc
             cmax[r] = std::max(cmax[r], c);
         }
     // row tiles: up to kRingRows consecutive rows, not across the space's row ranges (vertex rows,
-    // then edge and interior rows: each range runs through the mesh on its own)
+    // then the rest: each range runs through the mesh on its own)
     std::vector<int32_t> trow;
     for (size_t q = 0; q + 1 < s->row_ranges.size(); q++)
         for (int64_t r = s->row_ranges[q]; r < s->row_ranges[q + 1]; r += kRingRows) trow.push_back((int32_t)r);
@@ -1601,54 +1511,56 @@ bool ring_schedule(const ocmp_space_s* s, int L, const std::vector<int32_t>& inc
         dlo[b] = lo;
         gst[b] = hi;
     }
-    // the last stage reading each chunk, and the ring length that keeps every overwrite two rounds
-    // behind its readers
+    // the last stage reading each chunk; the ring must outlast the widest distance
     std::vector<int32_t> last(nchunk, -1);
     for (int b = 0; b < nt; b++)
         for (int32_t j = elo[b]; j <= dst[b]; j++) last[j] = std::max(last[j], gst[b]);
     int lag = 0;
     for (int j = 0; j < nchunk; j++) lag = std::max(lag, last[j] - j);
-    int R = 4;
-    while (R < lag + 4) R *= 2;
+    const int R = lag + 2;   // one chunk of slack beyond the minimum (lag + 1)
     const size_t bytes = (size_t)R * (size_t)CE * L * L * sizeof(float2);
     if (bytes > budget) return false;
     S.R = R;
     S.nchunk = nchunk;
     S.ring_bytes = bytes;
-    S.tile_row = trow;
-    S.tile_wait.resize(nt);
-    for (int b = 0; b < nt; b++) S.tile_wait[b] = make_int4(elo[b], dst[b], dlo[b], gst[b]);
-    S.chunk_wait.resize(nchunk);
-    for (int j = 0; j < nchunk; j++) S.chunk_wait[j] = make_int2(j, last[j]);
-    S.need.assign((size_t)3 * nchunk, 0);
+    S.last = last;
+    // nodes per stage: D tiles (row ranges), G blocks (<= 256 entries of one tile), and what they wait on
     std::vector<std::vector<int32_t>> dby(nchunk), gby(nchunk);
     for (int b = 0; b < nt; b++) {
         dby[dst[b]].push_back(b);
         gby[gst[b]].push_back(b);
-        S.need[nchunk + dst[b]]++;
-        S.need[2 * nchunk + gst[b]]++;
     }
-    for (int t = 0; t < nchunk + 2; t++) {
-        if (t < nchunk)
-            for (int64_t e = (int64_t)t * CE; e < std::min(ne, (int64_t)(t + 1) * CE); e += kRingElems) {
-                S.items.push_back(make_int4(0, t, (int32_t)e, 0));
-                S.need[t]++;
-            }
-        if (t >= 1 && t - 1 < nchunk)
-            for (int32_t b : dby[t - 1]) S.items.push_back(make_int4(1, t - 1, b, 0));
-        if (t >= 2)
-            for (int32_t b : gby[t - 2]) S.items.push_back(make_int4(2, t - 2, b, 0));
+    S.doff.assign(1, 0);
+    S.goff.assign(1, 0);
+    S.dlo_e.assign(nchunk, INT32_MAX);
+    S.glo_e.assign(nchunk, INT32_MAX);
+    S.ghi_e.assign(nchunk, -1);
+    S.glo_d.assign(nchunk, INT32_MAX);
+    for (int st = 0; st < nchunk; st++) {
+        for (int32_t b : dby[st]) {
+            S.dtiles.push_back(make_int2(trow[b], trow[b + 1]));
+            S.dlo_e[st] = std::min(S.dlo_e[st], elo[b]);
+        }
+        for (int32_t b : gby[st]) {
+            const int32_t k0 = (int32_t)s->rowptr[trow[b]], k1 = (int32_t)s->rowptr[trow[b + 1]];
+            for (int32_t k = k0; k < k1; k += 256) S.gblocks.push_back(make_int2(k, std::min(k1, k + 256)));
+            S.glo_e[st] = std::min(S.glo_e[st], elo[b]);
+            S.ghi_e[st] = std::max(S.ghi_e[st], dst[b]);
+            S.glo_d[st] = std::min(S.glo_d[st], dlo[b]);
+        }
+        S.doff.push_back((int)S.dtiles.size());
+        S.goff.push_back((int)S.gblocks.size());
     }
     return true;
 }
 
-// Plans the ring for space s (first use): on success s->ring holds the device tables, else the
-// space is marked for the two-pass assembly.
+// Plans the ring for space s (first use): on success s->ring holds the ring and the node lists,
+// else the space is marked for the two-pass assembly.
 template <int L>
 int ring_plan(ocmp_space_s* s, cudaStream_t st) {
     s->ring_state = -1;
     const int64_t ne = s->mesh->ne, nd = s->ndof;
-    if ((int64_t)ne * L >= INT32_MAX || ne * (int64_t)L * L >= INT32_MAX) return OCMP_OK;
+    if (ne * (int64_t)L * L >= INT32_MAX) return OCMP_OK;
     // the incidence lists, in the order the space stores them (ascending element)
     std::vector<int32_t> inc_ptr(nd + 1, 0), inc((size_t)ne * L);
     for (int64_t i = 0; i < ne * L; i++) inc_ptr[s->dofs[i] + 1]++;
@@ -1657,105 +1569,164 @@ int ring_plan(ocmp_space_s* s, cudaStream_t st) {
         std::vector<int32_t> fill(inc_ptr.begin(), inc_ptr.end() - 1);
         for (int64_t i = 0; i < ne * L; i++) inc[fill[s->dofs[i]]++] = (int32_t)i;
     }
-    for (int64_t r = 0; r < nd; r++)
-        if (inc_ptr[r + 1] - inc_ptr[r] > 4095 || inc_ptr[r + 1] == inc_ptr[r]) return OCMP_OK;
-    int dev = 0, l2 = 0, sms = 0;
+    int dev = 0, l2 = 0;
     OCMP_CUDA(cudaGetDevice(&dev));
     OCMP_CUDA(cudaDeviceGetAttribute(&l2, cudaDevAttrL2CacheSize, dev));
-    OCMP_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
     const size_t budget = (size_t)l2 / 2;
     RingSchedule S;
     int shift = -1;
-    for (int sh : {11, 10, 9})
+    for (int sh : {13, 12, 11, 10})
         if (ring_schedule(s, L, inc_ptr, inc, sh, budget, S)) {
             shift = sh;
             break;
         }
     if (shift < 0) return OCMP_OK;
+    {
+        const int r = ensure_contrib<L>(s, st);
+        if (r) return r;
+    }
     auto* p = new RingPlan();
     p->ce_shift = shift;
     p->R = S.R;
     p->nchunk = S.nchunk;
-    p->nitems = (int)S.items.size();
-    p->ntiles = (int)S.tile_row.size() - 1;
     p->ring_bytes = S.ring_bytes;
     p->L = L;
+    p->doff = S.doff;
+    p->goff = S.goff;
+    p->dlo_e = S.dlo_e;
+    p->glo_e = S.glo_e;
+    p->ghi_e = S.ghi_e;
+    p->glo_d = S.glo_d;
+    p->last = S.last;
     int r = OCMP_OK;
     if (cudaMalloc((void**)&p->ring, S.ring_bytes) != cudaSuccess) r = fail(OCMP_ERR_NOMEM, "element ring: cudaMalloc");
-    if (!r) r = ring_upload(&p->items, S.items);
-    if (!r) r = ring_upload(&p->tile_row, S.tile_row);
-    if (!r) r = ring_upload(&p->tile_wait, S.tile_wait);
-    if (!r) r = ring_upload(&p->chunk_wait, S.chunk_wait);
-    if (!r) r = ring_upload(&p->need, S.need);
-    if (!r && cudaMalloc((void**)&p->cnt, sizeof(unsigned) * (2 + 3 * (size_t)S.nchunk)) != cudaSuccess)
-        r = fail(OCMP_ERR_NOMEM, "element ring: cudaMalloc");
-    // the 2-byte contribution lists, from the two-pass gather's lists (built here if needed, then
-    // released: the ring keeps only the run starts)
-    if (!r) r = ensure_contrib<L>(s, st);
-    if (!r && cudaMalloc((void**)&p->con, sizeof(uint16_t) * (size_t)(ne * L * L)) != cudaSuccess)
-        r = fail(OCMP_ERR_NOMEM, "element ring: cudaMalloc");
-    if (!r) {
-        OCMP_LAUNCH(ring_con_kernel<L><<<nblk(nd, 128), 128, 0, st>>>(nd, s->d_rowptr, s->d_cseg, s->d_csrc, s->d_inc_ptr,
-                                                                      s->d_inc, p->con));
-        if (cudaStreamSynchronize(st) != cudaSuccess) r = fail(OCMP_ERR_CUDA, "element ring: contribution lists");
-    }
+    if (!r && cudaMalloc((void**)&p->dev, sizeof(RingDev)) != cudaSuccess) r = fail(OCMP_ERR_NOMEM, "element ring: cudaMalloc");
+    if (!r) r = ring_upload(&p->dtiles, S.dtiles);
+    if (!r) r = ring_upload(&p->gblocks, S.gblocks);
     if (r) {
         ring_destroy(p);
         return r;
     }
-    cudaFree(s->d_csrc);
-    s->d_csrc = nullptr;
     s->ring = p;
     s->ring_state = 1;
     return OCMP_OK;
+}
+
+// The graph of one space and wind variant: E, D and G nodes per chunk with their edges, and a last
+// node dropping the ring from L2.
+template <int D, int L, int VAR>
+int ring_graph(ocmp_space_s* s, RingPlan* p) {
+    constexpr int LL = L * L;
+    const int C = p->nchunk, R = p->R;
+    const int64_t ne = s->mesh->ne, CE = (int64_t)1 << p->ce_shift;
+    RingMap mp;
+    mp.ce_shift = p->ce_shift;
+    mp.magic = (unsigned)((((uint64_t)1 << 32) + (uint64_t)R - 1) / (uint64_t)R);
+    mp.span = (int64_t)R * CE * LL;
+    cudaGraph_t g = nullptr;
+    OCMP_CUDA(cudaGraphCreate(&g, 0));
+    std::vector<cudaGraphNode_t> En(C, nullptr), Dn(C, nullptr), Gn(C, nullptr), all;
+    int r = OCMP_OK, nodes = 0;
+    auto add = [&](cudaGraphNode_t* out, const void* fn, unsigned grid, unsigned block, unsigned smem, void** args,
+                   const std::vector<cudaGraphNode_t>& deps) {
+        if (r) return;
+        cudaKernelNodeParams kp{};
+        kp.func = const_cast<void*>(fn);
+        kp.gridDim = dim3(grid);
+        kp.blockDim = dim3(block);
+        kp.sharedMemBytes = smem;
+        kp.kernelParams = args;
+        if (cudaGraphAddKernelNode(out, g, deps.empty() ? nullptr : deps.data(), deps.size(), &kp) != cudaSuccess)
+            r = fail(OCMP_ERR_CUDA, "element ring: cudaGraphAddKernelNode");
+        else
+            nodes++;
+    };
+    const RingDev* dev = p->dev;
+    const float2* geo = s->d_geo_ff;
+    const int32_t* conn = s->mesh->dconn;
+    const float2* ring = p->ring;
+    const size_t gsm = sizeof(float2) * (size_t)kGenElems * (LL | 1);
+    std::vector<cudaGraphNode_t> deps;
+    for (int t = 0; t < C && !r; t++) {
+        // E(t): after the readers of the chunk its slot held before (t - R)
+        deps.clear();
+        const int j = t - R;
+        if (j >= 0)
+            for (int st = j; st <= p->last[j]; st++) {
+                if (Dn[st]) deps.push_back(Dn[st]);
+                if (Gn[st]) deps.push_back(Gn[st]);
+            }
+        {
+            int64_t e_begin = (int64_t)t * CE, e_end = std::min(ne, e_begin + CE);
+            float2* slot = p->ring + (int64_t)(t % R) * CE * LL;
+            void* args[] = {(void*)&dev, (void*)&ne, (void*)&geo, (void*)&conn, (void*)&e_begin, (void*)&e_end,
+                            (void*)&slot};
+            add(&En[t], (const void*)ring_elem_kernel<D, L, VAR>, (unsigned)((e_end - e_begin + kGenElems - 1) / kGenElems),
+                2 * kGenElems, (unsigned)gsm, args, deps);
+        }
+        // D(t): after the chunks its rows read
+        if (p->doff[t + 1] > p->doff[t]) {
+            deps.clear();
+            for (int c = p->dlo_e[t]; c <= t; c++) deps.push_back(En[c]);
+            const int2* tiles = p->dtiles + p->doff[t];
+            const int32_t* inc_ptr = s->d_inc_ptr;
+            const int32_t* inc = s->d_inc;
+            const uint8_t* freed = s->d_free;
+            void* args[] = {(void*)&dev, (void*)&tiles, (void*)&mp, (void*)&ring, (void*)&inc_ptr, (void*)&inc, (void*)&freed};
+            add(&Dn[t], (const void*)ring_diag_kernel<L>, (unsigned)(p->doff[t + 1] - p->doff[t]), kRingRows, 0, args, deps);
+            all.push_back(Dn[t]);
+        }
+        // G(t): after the chunks its rows read and the diagonals of its columns
+        if (p->goff[t + 1] > p->goff[t]) {
+            deps.clear();
+            for (int c = p->glo_e[t]; c <= p->ghi_e[t]; c++) deps.push_back(En[c]);
+            for (int c = p->glo_d[t]; c <= t; c++)
+                if (Dn[c]) deps.push_back(Dn[c]);
+            const int2* blocks = p->gblocks + p->goff[t];
+            const int32_t* seg = s->d_cseg;
+            const int32_t* src = s->d_csrc;
+            const int32_t* col = s->d_col;
+            void* args[] = {(void*)&dev, (void*)&blocks, (void*)&mp, (void*)&ring, (void*)&seg, (void*)&src, (void*)&col};
+            add(&Gn[t], (const void*)ring_gather_kernel<L>, (unsigned)(p->goff[t + 1] - p->goff[t]), 256, 0, args, deps);
+            all.push_back(Gn[t]);
+        }
+    }
+    if (!r) {
+        char* rc = reinterpret_cast<char*>(p->ring);
+        int64_t lines = (int64_t)(p->ring_bytes / 128);
+        void* args[] = {(void*)&rc, (void*)&lines};
+        cudaGraphNode_t dn;
+        add(&dn, (const void*)ring_discard_kernel, (unsigned)std::min<int64_t>((lines + 255) / 256, 1216), 256, 0, args, all);
+    }
+    if (!r && cudaGraphInstantiate(&p->exec[VAR], g, 0) != cudaSuccess) r = fail(OCMP_ERR_CUDA, "element ring: cudaGraphInstantiate");
+    cudaGraphDestroy(g);
+    if (!r) p->nodes[VAR] = nodes;
+    return r;
 }
 
 template <int D, int L, int VAR>
 int ring_launch(ocmp_matrix_s* m, const FormArgs& a, cudaStream_t st) {
     ocmp_space_s* s = m->space;
     RingPlan* p = s->ring;
-    if (!p->grid) {
-        int dev = 0, sms = 0, per = 0;
-        OCMP_CUDA(cudaGetDevice(&dev));
-        OCMP_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-        OCMP_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, ring_assemble_kernel<D, L, VAR>, kRingThreads, 0));
-        p->grid = std::max(1, per) * sms;
+    if (!p->exec[VAR]) {
+        constexpr int LL = L * L;
+        OCMP_CUDA(cudaFuncSetAttribute(ring_elem_kernel<D, L, VAR>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)(sizeof(float2) * (size_t)kGenElems * (LL | 1))));
+        const int r = ring_graph<D, L, VAR>(s, p);
+        if (r) return r;
     }
-    RingArgs g;
-    g.ne = s->mesh->ne;
-    g.geo = s->d_geo_ff;
-    g.conn = s->mesh->dconn;
-    g.a = a;
-    g.ring = p->ring;
-    g.ce_shift = p->ce_shift;
-    g.rmask = p->R - 1;
-    g.nchunk = p->nchunk;
-    g.nitems = p->nitems;
-    g.items = p->items;
-    g.tile_row = p->tile_row;
-    g.tile_wait = p->tile_wait;
-    g.chunk_wait = p->chunk_wait;
-    g.rowptr = s->d_rowptr;
-    g.col = s->d_col;
-    g.inc_ptr = s->d_inc_ptr;
-    g.inc = s->d_inc;
-    g.seg = s->d_cseg;
-    g.con = p->con;
-    g.freed = s->d_free;
-    g.sell_off = (m->flags & OCMP_MAT_SELL32) ? s->d_sell_off : nullptr;
-    g.vals = m->vals;
-    g.vals32 = m->vals32;
-    g.svals64 = m->svals64;
-    g.svals32 = m->svals32;
-    g.dinv = m->dinv;
-    g.dinv32 = m->dinv32;
-    g.cnt = p->cnt;
-    g.need = p->need;
-    OCMP_CUDA(cudaMemsetAsync(p->cnt, 0, sizeof(unsigned) * (2 + 3 * (size_t)p->nchunk), st));
-    OCMP_LAUNCH(ring_assemble_kernel<D, L, VAR><<<p->grid, kRingThreads, 0, st>>>(g));
-    const int64_t lines = (int64_t)(p->ring_bytes / 128);
-    OCMP_LAUNCH(ring_discard_kernel<<<(unsigned)std::min<int64_t>(nblk(lines, 256), 1184), 256, 0, st>>>(
-        reinterpret_cast<char*>(p->ring), lines));
+    RingDev v;
+    v.a = a;
+    v.vals = m->vals;
+    v.vals32 = m->vals32;
+    v.svals64 = m->svals64;
+    v.svals32 = m->svals32;
+    v.spos = (m->flags & OCMP_MAT_SELL32) ? s->d_sell_pos : nullptr;
+    v.dinv = m->dinv;
+    v.dinv32 = m->dinv32;
+    OCMP_LAUNCH(ring_args_kernel<<<1, 1, 0, st>>>(p->dev, v));
+    OCMP_CUDA(cudaGraphLaunch(p->exec[VAR], st));
+    ::ocmp::g_launches.fetch_add(p->nodes[VAR], std::memory_order_relaxed);
     OCMP_CUDA(cudaGetLastError());
     return OCMP_OK;
 }
