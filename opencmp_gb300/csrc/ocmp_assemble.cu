@@ -1760,7 +1760,7 @@ int assemble_impl(ocmp_matrix_s* m, const ocmp_form_t* f, cudaStream_t st) {
         if constexpr (GenTerms<D, L, 0>::value && GenTerms<D, L, 1>::value) {
             // element-only forms: the pipelined element ring, where the numbering allows it
             const uint32_t bm = f->outflow_mask | f->wn_mask;
-            if (s->kind == OCMP_H1 && !(bm != 0 && s->nbf > 0) && !(m->flags & OCMP_MAT_TWO_PASS)) {
+            if (s->kind == OCMP_H1 && !(bm != 0 && s->nbf > 0) && (m->flags & OCMP_MAT_RING)) {
                 if (s->ring_state == 0) {
                     const int r = ring_plan<L>(s, st);
                     if (r) return r;

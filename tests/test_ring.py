@@ -1,10 +1,10 @@
 """The pipelined element-ring assembly against the two-pass assembly and the oracle.
 
-Element-only forms on H1 spaces assembled in double-float run as one persistent launch (element
-tiles write their matrices into a ring of chunk slots held in L2; diagonal and row tiles sum them
-into the CSR entries once every element a row needs is written). Its sums are the two-pass
+Element-only forms on H1 spaces assembled in double-float with OCMP_MAT_RING run through the
+element ring (element matrices of consecutive chunks in a ring of slots held in L2, summed into the
+CSR entries once every element a row needs is written). Its sums are the two-pass
 assembly's, term for term and in the same order, so every output must agree bit for bit with the
-two-pass assembly (OCMP_MAT_TWO_PASS): FP64 values, FP32 copy, Jacobi-scaled values in CSR and
+two-pass assembly (the default): FP64 values, FP32 copy, Jacobi-scaled values in CSR and
 SELL-32 order, and the inverse diagonal. The meshes are large enough for many chunks and for the
 ring to wrap around (unit cube 24^3 x 6: 82,944 tetrahedra in 2,048-element chunks). Against the
 oracle the tolerance is the parity suite's: 1e-12 relative to the largest entry.
@@ -64,8 +64,8 @@ def test_ring_matches_two_pass_bit_for_bit(gpu_lib, name, mk, order):
     sp = fem.Space(m, 'H1', order, m.bc_names)
     layouts = [dict(jacobi32=True, sell=True), dict(fp32=True, jacobi64=True, jacobi32=True)]
     for lay in layouts:
-        ring = fem.Matrix(sp, dfloat=True, **lay)
-        two = fem.Matrix(sp, dfloat=True, two_pass=True, **lay)
+        ring = fem.Matrix(sp, dfloat=True, ring=True, **lay)
+        two = fem.Matrix(sp, dfloat=True, **lay)
         # several forms in a row: the ring, its counters and the diagonal are reused every time
         for _, f in _forms(fem, m):
             ring.assemble(f)
@@ -82,8 +82,8 @@ def test_ring_with_scattered_numbering(gpu_lib):
     perm = np.random.default_rng(3).permutation(m.ne)
     mp = M.Mesh(m.coords, np.ascontiguousarray(m.elements[perm]), m.bfacets, m.blabels, list(m.bc_names))
     sp = fem.Space(mp, 'H1', 2, mp.bc_names)
-    ring = fem.Matrix(sp, dfloat=True, jacobi32=True, sell=True)
-    two = fem.Matrix(sp, dfloat=True, jacobi32=True, sell=True, two_pass=True)
+    ring = fem.Matrix(sp, dfloat=True, jacobi32=True, sell=True, ring=True)
+    two = fem.Matrix(sp, dfloat=True, jacobi32=True, sell=True)
     f = _forms(fem, mp)[1][1]
     ring.assemble(f)
     two.assemble(f)
@@ -98,7 +98,7 @@ def test_ring_matches_oracle(gpu_lib, oracle):
     sp = fem.Space(m, 'H1', 2, m.bc_names)
     o = oracle.Space(m, oracle.H1, 2, m.label_mask(m.bc_names))
     kw = dict(mass=1.0, diff=1e-2, dt=1e-3, wind=(1.0, 0.5, 0.25))
-    A = fem.Matrix(sp, dfloat=True, fp32=True, jacobi32=True)
+    A = fem.Matrix(sp, dfloat=True, fp32=True, jacobi32=True, ring=True)
     A.assemble(fem.make_form(**kw))
     ao = o.assemble(oracle.make_form(**kw))
     v = A.values()
