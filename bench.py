@@ -149,7 +149,7 @@ def run_ours(args):
     # each path assembles the Krylov matrix it iterates with (A D^-1 in FP64, or in FP32) in the same
     # pass as the FP64 values used for the residuals
     mats = {'fp64': fem.Matrix(space, jacobi64=True),
-            'mixed': fem.Matrix(space, jacobi32=True, dfloat=True, sell=not args.csr32, ring=args.ring)}
+            'mixed': fem.Matrix(space, jacobi32=True, dfloat=True, sell=not args.csr32)}
     form = fem.make_form(mass=1.0, diff=EPS, dt=DT, wind=WIND)
     u0 = torch.as_tensor(fem.interpolate_p2(space, gaussian), device='cuda')
     b = torch.zeros(ndof, dtype=torch.float64, device='cuda')
@@ -1013,7 +1013,6 @@ def main():
     ap.add_argument('--check-every-mixed', type=int, default=6, help='mixed-precision paths')
     ap.add_argument('--no-cpu', action='store_true')
     ap.add_argument('--csr32', action='store_true', help='FP32 Krylov matrix in CSR order instead of SELL-32')
-    ap.add_argument('--ring', action='store_true', help='optimised paths assemble through the element ring')
     ap.add_argument('--config', default='transient3d', choices=['transient3d', 'batched', 'ins', 'dg2d'])
     ap.add_argument('--n-dg', type=int, default=256)
     ap.add_argument('--dg-cpu-n', type=int, default=128, help='mesh of the dg2d cpu_baseline sample')

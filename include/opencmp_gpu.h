@@ -186,19 +186,8 @@ enum {
     OCMP_MAT_JACOBI64 = 2,
     OCMP_MAT_JACOBI32 = 4,
     OCMP_MAT_DFLOAT = 8,
-    OCMP_MAT_SELL32 = 16,
-    OCMP_MAT_RING = 32
+    OCMP_MAT_SELL32 = 16
 };
-/* OCMP_MAT_RING (with OCMP_MAT_DFLOAT; element-only forms on H1 spaces with generated element code:
- * P1/P2 tetrahedra, P1..P3 triangles) assembles through the element ring instead of the two-pass
- * assembly (all element matrices to memory, then the sorted segmented gather): element matrices of
- * consecutive element chunks go into a ring of chunk slots sized to stay in L2 and are summed into
- * the CSR entries (and the diagonal) once every element a row needs is written, so they do not
- * round-trip through DRAM. The values are identical, bit for bit, to the two-pass assembly's. The
- * ring is planned on the first such assembly from the dof numbering; where the numbering spreads a
- * row's elements too widely for the ring, the two-pass assembly runs instead. The ring, like the
- * element-matrix buffer, is per space: assemblies of matrices on one space must not overlap on the
- * GPU. */
 /* OCMP_MAT_SELL32 (with OCMP_MAT_JACOBI32, single matrices): the FP32 Jacobi-scaled values are
  * written in the space's SELL-32 order instead of CSR order (slices of 32 rows, each row padded to
  * its slice's width in 4-entry chunks, chunk-major within a slice, zero padding), the layout the

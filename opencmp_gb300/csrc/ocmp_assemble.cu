@@ -20,7 +20,6 @@
 // integrands (max(w.n, 0)) are not polynomial.
 #include <cuda_runtime.h>
 
-#include <algorithm>
 #include <cmath>
 #include <vector>
 
@@ -953,279 +952,6 @@ __global__ void __launch_bounds__(256) csr_gather_kernel(int64_t nnz, const int3
 }
 
 // Element right-hand sides: dt (f, phi_i) + mass (u_prev, phi_i) + boundary data.
-// ---------------------------------------------------------------------------------------------
-// Element ring: pipelined assembly of element-only forms in double-float (H1 spaces with generated
-// element code), one persistent launch. The elements are cut into chunks of CE consecutive
-// elements, the rows into tiles of up to 256 consecutive rows, and the work into three queues:
-//   E  element tiles (128 elements of one chunk) write their element matrices into ring slot
-//      chunk mod R, structure of arrays (entry (i, j) of element e at slot + (i L + j) CE + e mod CE:
-//      consecutive lanes, consecutive addresses);
-//   D  row tiles, by D stage (the last chunk their rows' elements lie in): per row the sum of its
-//      incidences' K_e[i][i] from the ring, then D^-1 in FP64 and FP32;
-//   G  row tiles, by G stage (the last D stage among their rows' columns): per CSR entry the sum of
-//      its element-matrix entries from the ring in the two-pass gather's order (four entries per
-//      thread at a time), then the FP64 value, the FP32 copies and A D^-1.
-// A tile is ready when every tile it reads from is done: per queue a watermark counts the leading
-// stages whose tiles are all done (advanced by the block that completes a stage, with a
-// compare-and-swap chain over the stages behind it). D needs the E chunks up to its stage, G the E
-// chunks up to its D stage and the D stages up to its own, E(c) every D and G stage that reads
-// chunk c - R (the slot it overwrites). A block takes the first ready tile of G, then D, then E
-// (compare-and-swap on the queue head after the readiness check) and never waits while holding a
-// tile; with R at least the widest stage distance + 2 some tile is always ready or running, so the
-// launch finishes (a block that finds nothing ready for about a second sets an error flag and
-// leaves). The ring (R CE L^2 float pairs, at most half of L2) is stored and read with an L2
-// evict-last policy and dropped from L2 afterwards: element matrices do not round-trip through
-// DRAM. The sums are the two-pass assembly's, term for term and in the same order.
-constexpr int kRingThreads = 256;
-constexpr int kRingElems = 128;   // elements per element tile (two threads each)
-constexpr int kRingRows = 256;    // rows per row tile (at most)
-constexpr unsigned kRingSpin = 1u << 21;  // empty polls before a block gives up (about a second)
-
-struct RingArgs {
-    int64_t ne;
-    const float2* geo;
-    const int32_t* conn;
-    FormArgs a;
-    float2* ring;
-    int ce_shift, rmask;            // CE = 1 << ce_shift elements per chunk, R = rmask + 1 slots
-    int nchunk;
-    int nq[3];                      // tiles per queue: E, D, G
-    const int32_t* eq;              // E queue: first element of each tile (chunk = element >> ce_shift)
-    const int4* rq[2];              // D, G queues: {first row, end row, D stage, G stage}
-    const int32_t* last;            // per chunk: the last stage (D or G) that reads it
-    const int32_t* need;            // tiles per stage: E, D, G (nchunk each)
-    unsigned* ctl;                  // [0..2] queue heads, [3] error flag, [4..6] done-stage watermarks,
-                                    // then done tiles per stage: E, D, G (nchunk each)
-    const int32_t* rowptr;
-    const int32_t* col;
-    const int32_t* inc_ptr;
-    const int32_t* inc;
-    const int32_t* seg;             // per CSR entry, its run in src
-    const int32_t* src;             // per contribution, (e L + i) L + j
-    const uint8_t* freed;
-    const int32_t* spos;            // SELL-32 position of each CSR entry for svals32, or null (CSR order)
-    double* vals;
-    float* vals32;
-    double* svals64;
-    float* svals32;
-    double* dinv;
-    float* dinv32;
-};
-
-__device__ __forceinline__ unsigned ld_acquire_u32(const unsigned* p) {
-    unsigned v;
-    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
-    return v;
-}
-__device__ __forceinline__ uint64_t l2_evict_last_policy() {
-    uint64_t p;
-    asm volatile("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;" : "=l"(p));
-    return p;
-}
-__device__ __forceinline__ void st_ring(float2* p, float2 v, uint64_t pol) {
-    asm volatile("st.global.L2::cache_hint.v2.f32 [%0], {%1, %2}, %3;" ::"l"(p), "f"(v.x), "f"(v.y), "l"(pol)
-                 : "memory");
-}
-// ring entries are written by other blocks of the same launch: read through L2 (.cg), never L1
-__device__ __forceinline__ float2 ld_ring(const float2* p, uint64_t pol) {
-    float2 v;
-    asm volatile("ld.global.cg.L2::cache_hint.v2.f32 {%0, %1}, [%2], %3;" : "=f"(v.x), "=f"(v.y) : "l"(p), "l"(pol)
-                 : "memory");
-    return v;
-}
-template <int L>
-__device__ __forceinline__ const float2* ring_at(const RingArgs& g, int32_t e, int idx) {
-    const int64_t slot = (e >> g.ce_shift) & g.rmask;
-    return g.ring + ((slot * (L * L) + idx) << g.ce_shift) + (e & ((1 << g.ce_shift) - 1));
-}
-
-// One block (thread 0) marks a tile of queue q and stage s done; the block that completes a stage
-// moves the queue's watermark over every leading stage now complete.
-__device__ void ring_done(const RingArgs& g, int q, int s) {
-    unsigned* cnt = g.ctl + 7 + (int64_t)q * g.nchunk;
-    const int32_t* need = g.need + (int64_t)q * g.nchunk;
-    __threadfence();
-    const unsigned c = atomicAdd(cnt + s, 1u) + 1u;
-    __threadfence();
-    if (c != (unsigned)__ldg(need + s)) return;
-    unsigned* wm = g.ctl + 4 + q;
-    unsigned p = ld_acquire_u32(wm);
-    while (p < (unsigned)g.nchunk && ld_acquire_u32(cnt + p) >= (unsigned)__ldg(need + p)) {
-        __threadfence();
-        const unsigned o = atomicCAS(wm, p, p + 1);
-        p = o == p ? p + 1 : o;
-    }
-}
-
-// Thread 0: claims the first ready tile (kind 0 E, 1 D, 2 G; index), or returns kind -1 when every
-// queue is empty (or the wait gave up).
-__device__ int2 ring_claim(const RingArgs& g) {
-    unsigned spins = 0;
-    for (;;) {
-        if (ld_acquire_u32(g.ctl + 3)) return make_int2(-1, 0);
-        const unsigned wE = ld_acquire_u32(g.ctl + 4), wD = ld_acquire_u32(g.ctl + 5), wG = ld_acquire_u32(g.ctl + 6);
-        bool left = false;
-        for (int q = 2; q >= 0; q--) {
-            const unsigned h = ld_acquire_u32(g.ctl + q);
-            if (h >= (unsigned)g.nq[q]) continue;
-            left = true;
-            bool ready;
-            if (q == 0) {
-                const int j = (__ldg(g.eq + h) >> g.ce_shift) - (g.rmask + 1);
-                ready = j < 0 || (wD > (unsigned)__ldg(g.last + j) && wG > (unsigned)__ldg(g.last + j));
-            } else {
-                const int4 t = __ldg(g.rq[q - 1] + h);
-                ready = q == 1 ? wE > (unsigned)t.z : (wE > (unsigned)t.z && wD > (unsigned)t.w);
-            }
-            if (!ready) continue;
-            if (atomicCAS(g.ctl + q, h, h + 1) == h) {
-                __threadfence();
-                return make_int2(q, (int)h);
-            }
-            q++;  // lost the race: look at this queue again
-        }
-        if (!left) return make_int2(-1, 0);
-        if (++spins >= kRingSpin) {
-            atomicOr(g.ctl + 3, 1u);
-            return make_int2(-1, 0);
-        }
-        __nanosleep(spins < 32 ? 64 : 256);
-    }
-}
-
-template <int D, int L, int VAR>
-__global__ void __launch_bounds__(kRingThreads, 2) ring_assemble_kernel(RingArgs g) {
-    using GT = GenTerms<D, L, VAR>;
-    __shared__ int2 s_w;
-    const int tid = threadIdx.x;
-    const uint64_t pol = l2_evict_last_policy();
-    for (;;) {
-        if (tid == 0) s_w = ring_claim(g);
-        __syncthreads();
-        const int2 w = s_w;
-        if (w.x < 0) return;
-        int stage;
-        if (w.x == 0) {
-            // element tile: warp v holds elements (v / 2) * 32 + lane, half (v % 2) of the slots
-            const int32_t e0 = __ldg(g.eq + w.y);
-            stage = e0 >> g.ce_shift;
-            const int v = tid >> 5, lane = tid & 31;
-            const int64_t e = (int64_t)e0 + (v >> 1) * 32 + lane;
-            if (e < g.ne && (e >> g.ce_shift) == stage) {
-                float2 F[GT::NG];
-                gen_factors<D, L, VAR>(e, g.ne, g.geo, g.conn, g.a, F);
-                float2* slot = g.ring + (((int64_t)(stage & g.rmask) * (L * L)) << g.ce_shift) +
-                               (e & ((1 << g.ce_shift) - 1));
-                const int sh = g.ce_shift;
-                auto st = [slot, sh, pol](int idx, float2 x) { st_ring(slot + ((int64_t)idx << sh), x, pol); };
-                if ((v & 1) == 0) {
-                    GT::run0(F, st);
-                    GT::run1(F, st);
-                } else {
-                    GT::run2(F, st);
-                    GT::run3(F, st);
-                }
-            }
-        } else if (w.x == 1) {
-            // diagonal tile: one thread per row, incidences four at a time
-            const int4 t = __ldg(g.rq[0] + w.y);
-            stage = t.z;
-            const int32_t r = t.x + tid;
-            if (r < t.y && g.dinv) {
-                float h = 0.f, l = 0.f;
-                const int32_t k0 = __ldg(g.inc_ptr + r), k1 = __ldg(g.inc_ptr + r + 1);
-                for (int32_t k = k0; k < k1; k += 4) {
-                    int32_t fl[4];
-                    float2 x[4];
-#pragma unroll
-                    for (int u = 0; u < 4; u++) fl[u] = k + u < k1 ? __ldg(g.inc + k + u) : -1;
-#pragma unroll
-                    for (int u = 0; u < 4; u++) {
-                        x[u] = make_float2(0.f, 0.f);
-                        if (fl[u] >= 0) {
-                            const int32_t e = fl[u] / L, i = fl[u] - e * L;
-                            x[u] = ld_ring(ring_at<L>(g, e, i * (L + 1)), pol);
-                        }
-                    }
-#pragma unroll
-                    for (int u = 0; u < 4; u++)
-                        if (fl[u] >= 0) ff_add(h, l, x[u].x, x[u].y);
-                }
-                const double d = ff_to_double(h, l);
-                const double di = (__ldg(g.freed + r) && d != 0.0) ? 1.0 / d : 0.0;
-                g.dinv[r] = di;
-                if (g.dinv32) g.dinv32[r] = (float)di;
-            }
-        } else {
-            // row tile: one thread per CSR entry, four entries (256 apart) at a time, each with its
-            // contributions four at a time
-            const int4 t = __ldg(g.rq[1] + w.y);
-            stage = t.w;
-            const int32_t kb = __ldg(g.rowptr + t.x), ke = __ldg(g.rowptr + t.y);
-            for (int32_t k0 = kb + tid; k0 < ke; k0 += 4 * kRingThreads) {
-                int32_t c0[4], c1[4];
-#pragma unroll
-                for (int u = 0; u < 4; u++) {
-                    const int32_t k = k0 + u * kRingThreads;
-                    c0[u] = k < ke ? __ldcs(g.seg + k) : 0;
-                    c1[u] = k < ke ? __ldcs(g.seg + k + 1) : 0;
-                }
-                float h[4] = {0.f, 0.f, 0.f, 0.f}, l[4] = {0.f, 0.f, 0.f, 0.f};
-                for (int b = 0;; b += 4) {
-                    int32_t ix[4][4];
-                    float2 x[4][4];
-                    bool more = false;
-#pragma unroll
-                    for (int u = 0; u < 4; u++)
-#pragma unroll
-                        for (int q = 0; q < 4; q++) ix[u][q] = c0[u] + b + q < c1[u] ? __ldcs(g.src + c0[u] + b + q) : -1;
-#pragma unroll
-                    for (int u = 0; u < 4; u++)
-#pragma unroll
-                        for (int q = 0; q < 4; q++) {
-                            x[u][q] = make_float2(0.f, 0.f);
-                            if (ix[u][q] >= 0) {
-                                const int32_t ei = ix[u][q] / L, e = ei / L;
-                                x[u][q] = ld_ring(ring_at<L>(g, e, (ei - e * L) * L + (ix[u][q] - ei * L)), pol);
-                            }
-                        }
-#pragma unroll
-                    for (int u = 0; u < 4; u++) {
-#pragma unroll
-                        for (int q = 0; q < 4; q++)
-                            if (ix[u][q] >= 0) ff_add(h[u], l[u], x[u][q].x, x[u][q].y);
-                        more |= c0[u] + b + 4 < c1[u];
-                    }
-                    if (!more) break;
-                }
-#pragma unroll
-                for (int u = 0; u < 4; u++) {
-                    const int32_t k = k0 + u * kRingThreads;
-                    if (k >= ke) continue;
-                    const double vv = ff_to_double(h[u], l[u]);
-                    __stcs(g.vals + k, vv);
-                    const float v32 = __fadd_rn(h[u], l[u]);
-                    if (g.vals32) __stcs(g.vals32 + k, v32);
-                    if (g.svals64 || g.svals32) {
-                        const int32_t ck = __ldcs(g.col + k);
-                        if (g.svals64) __stcs(g.svals64 + k, vv * __ldcg(g.dinv + ck));
-                        if (g.svals32) __stcs(g.svals32 + (g.spos ? __ldcs(g.spos + k) : k), v32 * __ldcg(g.dinv32 + ck));
-                    }
-                }
-            }
-        }
-        __syncthreads();
-        if (tid == 0) ring_done(g, w.x, stage);
-    }
-}
-
-// Drops the ring's lines from L2 without writing them back (their contents are dead after the
-// assembly), so they do not hold L2 under the evict-last policy afterwards.
-__global__ void ring_discard_kernel(char* ring, int64_t lines) {
-    for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < lines; q += (int64_t)gridDim.x * blockDim.x)
-        asm volatile("discard.global.L2 [%0], 128;" ::"l"(ring + q * 128) : "memory");
-}
-
 template <int D, int L>
 __global__ void rhs_elem_kernel(int64_t ne, const double* __restrict__ X, const int32_t* __restrict__ conn,
                                 const int32_t* __restrict__ dofs, FormArgs a, double dt, int src_kind, double src_const,
@@ -1494,9 +1220,8 @@ FormArgs make_args(const ocmp_space_s* s, const ocmp_form_t* f) {
 
 inline unsigned nblk(int64_t n, int t) { return (unsigned)((n + t - 1) / t); }
 
-// The sorted segmented reduction's lists (once per space, and again if the element ring released
-// the element indices): per CSR entry its run start (d_cseg), per contribution its flat
-// element-matrix index (d_csrc).
+// The sorted segmented reduction's lists, built once per space: per CSR entry its run start
+// (d_cseg), per contribution its flat element-matrix index (d_csrc).
 template <int L>
 int ensure_contrib(ocmp_space_s* s, cudaStream_t st) {
     if (s->d_cseg && s->d_csrc) return OCMP_OK;
@@ -1515,229 +1240,6 @@ int ensure_contrib(ocmp_space_s* s, cudaStream_t st) {
     OCMP_CUDA(cudaStreamSynchronize(st));
     return OCMP_OK;
 }
-
-}  // namespace
-// ---------------------------------------------------------------------------------------------
-// Element ring: the plan (host, once per space) and the launch.
-struct RingPlan {
-    int ce_shift = 0, R = 0, nchunk = 0, grid = 0;
-    int nq[3] = {0, 0, 0};
-    size_t ring_bytes = 0;
-    float2* ring = nullptr;
-    int32_t* eq = nullptr;
-    int4* rq[2] = {nullptr, nullptr};
-    int32_t* last = nullptr;
-    int32_t* need = nullptr;
-    unsigned* ctl = nullptr;
-};
-
-void ring_destroy(RingPlan* p) {
-    if (!p) return;
-    void* ps[] = {p->ring, p->eq, p->rq[0], p->rq[1], p->last, p->need, p->ctl};
-    for (void* q : ps)
-        if (q) cudaFree(q);
-    delete p;
-}
-
-namespace {
-
-template <class T>
-int ring_upload(T** d, const std::vector<T>& h) {
-    if (cudaMalloc((void**)d, sizeof(T) * std::max<size_t>(1, h.size())) != cudaSuccess)
-        return fail(OCMP_ERR_NOMEM, "element ring: cudaMalloc");
-    if (!h.empty() && cudaMemcpy(*d, h.data(), sizeof(T) * h.size(), cudaMemcpyHostToDevice) != cudaSuccess)
-        return fail(OCMP_ERR_CUDA, "element ring: cudaMemcpy");
-    return OCMP_OK;
-}
-
-// The queues for chunks of 1 << ce_shift elements. Returns false when the ring they need exceeds
-// `budget` bytes.
-struct RingSchedule {
-    int R = 0, nchunk = 0;
-    size_t ring_bytes = 0;
-    std::vector<int32_t> eq, last, need;
-    std::vector<int4> dq, gq;
-};
-
-bool ring_schedule(const ocmp_space_s* s, int L, const std::vector<int32_t>& inc_ptr,
-                   const std::vector<int32_t>& inc, int ce_shift, size_t budget, RingSchedule& S) {
-    const int64_t ne = s->mesh->ne, nd = s->ndof;
-    const int64_t CE = (int64_t)1 << ce_shift;
-    const int nchunk = (int)((ne + CE - 1) / CE);
-    // the chunks a row's elements lie in
-    std::vector<int32_t> cmin(nd, INT32_MAX), cmax(nd, -1);
-    for (int64_t r = 0; r < nd; r++)
-        for (int32_t k = inc_ptr[r]; k < inc_ptr[r + 1]; k++) {
-            const int32_t c = (int32_t)((inc[k] / L) >> ce_shift);
-            cmin[r] = std::min(cmin[r], c);
-            cmax[r] = std::max(cmax[r], c);
-        }
-    // row tiles: up to kRingRows consecutive rows, not across the space's row ranges (vertex rows,
-    // then the rest: each range runs through the mesh on its own)
-    std::vector<int32_t> trow;
-    for (size_t q = 0; q + 1 < s->row_ranges.size(); q++)
-        for (int64_t r = s->row_ranges[q]; r < s->row_ranges[q + 1]; r += kRingRows) trow.push_back((int32_t)r);
-    trow.push_back((int32_t)nd);
-    const int nt = (int)trow.size() - 1;
-    std::vector<int32_t> elo(nt), dst(nt), gst(nt), dst_row(nd);
-    for (int b = 0; b < nt; b++) {
-        int32_t lo = INT32_MAX, hi = -1;
-        for (int32_t r = trow[b]; r < trow[b + 1]; r++) {
-            lo = std::min(lo, cmin[r]);
-            hi = std::max(hi, cmax[r]);
-        }
-        if (hi < 0) return false;  // a row without elements
-        elo[b] = lo;
-        dst[b] = hi;
-        for (int32_t r = trow[b]; r < trow[b + 1]; r++) dst_row[r] = hi;
-    }
-    for (int b = 0; b < nt; b++) {
-        int32_t hi = -1;
-        for (int64_t k = s->rowptr[trow[b]]; k < s->rowptr[trow[b + 1]]; k++) hi = std::max(hi, dst_row[s->col[k]]);
-        gst[b] = hi;
-    }
-    // the last stage reading each chunk; the ring outlasts the widest distance by two chunks
-    std::vector<int32_t> last(nchunk, -1);
-    for (int b = 0; b < nt; b++)
-        for (int32_t j = elo[b]; j <= dst[b]; j++) last[j] = std::max(last[j], gst[b]);
-    int lag = 0;
-    for (int j = 0; j < nchunk; j++) lag = std::max(lag, last[j] - j);
-    int R = 2;
-    while (R < lag + 2) R *= 2;
-    const size_t bytes = (size_t)R * (size_t)CE * L * L * sizeof(float2);
-    if (bytes > budget) return false;
-    S.R = R;
-    S.nchunk = nchunk;
-    S.ring_bytes = bytes;
-    S.last = last;
-    S.need.assign((size_t)3 * nchunk, 0);
-    for (int c = 0; c < nchunk; c++)
-        for (int64_t e = (int64_t)c * CE; e < std::min(ne, (int64_t)(c + 1) * CE); e += kRingElems) {
-            S.eq.push_back((int32_t)e);
-            S.need[c]++;
-        }
-    std::vector<int32_t> order(nt);
-    for (int b = 0; b < nt; b++) order[b] = b;
-    std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return dst[a] < dst[b]; });
-    for (int b : order) {
-        S.dq.push_back(make_int4(trow[b], trow[b + 1], dst[b], gst[b]));
-        S.need[nchunk + dst[b]]++;
-    }
-    std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return gst[a] < gst[b]; });
-    for (int b : order) {
-        S.gq.push_back(make_int4(trow[b], trow[b + 1], dst[b], gst[b]));
-        S.need[2 * nchunk + gst[b]]++;
-    }
-    return true;
-}
-
-// Plans the ring for space s (first use): on success s->ring holds the ring and the queues, else
-// the space is marked for the two-pass assembly.
-template <int L>
-int ring_plan(ocmp_space_s* s, cudaStream_t st) {
-    s->ring_state = -1;
-    const int64_t ne = s->mesh->ne, nd = s->ndof;
-    if (ne * (int64_t)L * L >= INT32_MAX) return OCMP_OK;
-    // the incidence lists, in the order the space stores them (ascending element)
-    std::vector<int32_t> inc_ptr(nd + 1, 0), inc((size_t)ne * L);
-    for (int64_t i = 0; i < ne * L; i++) inc_ptr[s->dofs[i] + 1]++;
-    for (int64_t i = 0; i < nd; i++) inc_ptr[i + 1] += inc_ptr[i];
-    {
-        std::vector<int32_t> fill(inc_ptr.begin(), inc_ptr.end() - 1);
-        for (int64_t i = 0; i < ne * L; i++) inc[fill[s->dofs[i]]++] = (int32_t)i;
-    }
-    int dev = 0, l2 = 0;
-    OCMP_CUDA(cudaGetDevice(&dev));
-    OCMP_CUDA(cudaDeviceGetAttribute(&l2, cudaDevAttrL2CacheSize, dev));
-    const size_t budget = (size_t)l2 / 2;
-    RingSchedule S;
-    int shift = -1;
-    for (int sh : {12, 11, 10, 9})
-        if (ring_schedule(s, L, inc_ptr, inc, sh, budget, S)) {
-            shift = sh;
-            break;
-        }
-    if (shift < 0) return OCMP_OK;
-    {
-        const int r = ensure_contrib<L>(s, st);
-        if (r) return r;
-    }
-    auto* p = new RingPlan();
-    p->ce_shift = shift;
-    p->R = S.R;
-    p->nchunk = S.nchunk;
-    p->ring_bytes = S.ring_bytes;
-    p->nq[0] = (int)S.eq.size();
-    p->nq[1] = (int)S.dq.size();
-    p->nq[2] = (int)S.gq.size();
-    int r = OCMP_OK;
-    if (cudaMalloc((void**)&p->ring, S.ring_bytes) != cudaSuccess) r = fail(OCMP_ERR_NOMEM, "element ring: cudaMalloc");
-    if (!r) r = ring_upload(&p->eq, S.eq);
-    if (!r) r = ring_upload(&p->rq[0], S.dq);
-    if (!r) r = ring_upload(&p->rq[1], S.gq);
-    if (!r) r = ring_upload(&p->last, S.last);
-    if (!r) r = ring_upload(&p->need, S.need);
-    if (!r && cudaMalloc((void**)&p->ctl, sizeof(unsigned) * (7 + 3 * (size_t)S.nchunk)) != cudaSuccess)
-        r = fail(OCMP_ERR_NOMEM, "element ring: cudaMalloc");
-    if (r) {
-        ring_destroy(p);
-        return r;
-    }
-    s->ring = p;
-    s->ring_state = 1;
-    return OCMP_OK;
-}
-
-template <int D, int L, int VAR>
-int ring_launch(ocmp_matrix_s* m, const FormArgs& a, cudaStream_t st) {
-    ocmp_space_s* s = m->space;
-    RingPlan* p = s->ring;
-    if (!p->grid) {
-        int dev = 0, sms = 0, per = 0;
-        OCMP_CUDA(cudaGetDevice(&dev));
-        OCMP_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-        OCMP_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, ring_assemble_kernel<D, L, VAR>, kRingThreads, 0));
-        p->grid = std::max(1, per) * sms;
-    }
-    RingArgs g;
-    g.ne = s->mesh->ne;
-    g.geo = s->d_geo_ff;
-    g.conn = s->mesh->dconn;
-    g.a = a;
-    g.ring = p->ring;
-    g.ce_shift = p->ce_shift;
-    g.rmask = p->R - 1;
-    g.nchunk = p->nchunk;
-    for (int q = 0; q < 3; q++) g.nq[q] = p->nq[q];
-    g.eq = p->eq;
-    g.rq[0] = p->rq[0];
-    g.rq[1] = p->rq[1];
-    g.last = p->last;
-    g.need = p->need;
-    g.ctl = p->ctl;
-    g.rowptr = s->d_rowptr;
-    g.col = s->d_col;
-    g.inc_ptr = s->d_inc_ptr;
-    g.inc = s->d_inc;
-    g.seg = s->d_cseg;
-    g.src = s->d_csrc;
-    g.freed = s->d_free;
-    g.spos = (m->flags & OCMP_MAT_SELL32) ? s->d_sell_pos : nullptr;
-    g.vals = m->vals;
-    g.vals32 = m->vals32;
-    g.svals64 = m->svals64;
-    g.svals32 = m->svals32;
-    g.dinv = m->dinv;
-    g.dinv32 = m->dinv32;
-    OCMP_CUDA(cudaMemsetAsync(p->ctl, 0, sizeof(unsigned) * (7 + 3 * (size_t)p->nchunk), st));
-    OCMP_LAUNCH(ring_assemble_kernel<D, L, VAR><<<p->grid, kRingThreads, 0, st>>>(g));
-    const int64_t lines = (int64_t)(p->ring_bytes / 128);
-    OCMP_LAUNCH(ring_discard_kernel<<<(unsigned)std::min<int64_t>(nblk(lines, 256), 1216), 256, 0, st>>>(
-        reinterpret_cast<char*>(p->ring), lines));
-    OCMP_CUDA(cudaGetLastError());
-    return OCMP_OK;
-}
-
 
 template <int D, int L>
 int assemble_impl(ocmp_matrix_s* m, const ocmp_form_t* f, cudaStream_t st) {
@@ -1765,15 +1267,6 @@ int assemble_impl(ocmp_matrix_s* m, const ocmp_form_t* f, cudaStream_t st) {
         }
         bool done = false;
         if constexpr (GenTerms<D, L, 0>::value && GenTerms<D, L, 1>::value) {
-            // element-only forms: the pipelined element ring, where the numbering allows it
-            const uint32_t bm = f->outflow_mask | f->wn_mask;
-            if (s->kind == OCMP_H1 && !(bm != 0 && s->nbf > 0) && (m->flags & OCMP_MAT_RING)) {
-                if (s->ring_state == 0) {
-                    const int r = ring_plan<L>(s, st);
-                    if (r) return r;
-                }
-                if (s->ring_state == 1) return var == 0 ? ring_launch<D, L, 0>(m, a, st) : ring_launch<D, L, 1>(m, a, st);
-            }
             if (s->kind == OCMP_H1) {
                 const size_t gsm = sizeof(float2) * (size_t)kGenElems * ((L * L) | 1);
                 if (!s->d_Kd) OCMP_CUDA(cudaMalloc((void**)&s->d_Kd, sizeof(float2) * (size_t)ne * L));

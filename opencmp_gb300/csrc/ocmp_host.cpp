@@ -565,8 +565,6 @@ static void free_space_device(ocmp_space_s* s) {
                   s->d_lift_ptr, s->d_lift_pos, s->d_Rm_ff, s->d_geo_ff, s->d_tpos, s->d_cseg, s->d_csrc, s->d_u2, s->d_Kd,
                   s->d_sell_off, s->d_sell_col, s->d_sell_pos};
     for (void* p : ps) dfree(p);
-    ocmp::ring_destroy(s->ring);
-    s->ring = nullptr;
 }
 
 int ocmp_space_create(ocmp_mesh_t mesh, int32_t kind, int32_t order, uint32_t dirichlet_mask, ocmp_space_t* out) {

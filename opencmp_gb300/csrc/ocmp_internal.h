@@ -65,11 +65,6 @@ struct ocmp_mesh_s {
     int32_t* dconn = nullptr;
 };
 
-namespace ocmp {
-struct RingPlan;
-void ring_destroy(RingPlan* p);
-}  // namespace ocmp
-
 // Reference-element tables of one space (host copies; device copies in ocmp_space_s).
 struct ocmp_tables {
     int nloc = 0, nq = 0, nfq = 0, ng_const = 0, ng_vtx = 0;
@@ -161,10 +156,6 @@ struct ocmp_space_s {
     int32_t* d_sell_off = nullptr;  // slices + 1
     int32_t* d_sell_col = nullptr;  // sell_nent columns (padding: the row itself, or 0 past the last row)
     int32_t* d_sell_pos = nullptr;  // nnz: the SELL position of each CSR entry
-    // pipelined element-ring assembly (ocmp_assemble.cu), planned on first use: 0 not planned yet,
-    // 1 planned, -1 not applicable (the numbering's element window is too wide for the ring)
-    int ring_state = 0;
-    ocmp::RingPlan* ring = nullptr;
 };
 
 // Matrix outputs selected at creation (ocmp_matrix_create's flags): the FP64 values always; an FP32

@@ -193,23 +193,21 @@ def make_rhs(dt=1.0, src_const=None, src_qp: Optional[torch.Tensor] = None, mass
     return r
 
 
-MAT_FP32, MAT_JACOBI64, MAT_JACOBI32, MAT_DFLOAT, MAT_SELL32, MAT_RING = 1, 2, 4, 8, 16, 32
+MAT_FP32, MAT_JACOBI64, MAT_JACOBI32, MAT_DFLOAT, MAT_SELL32 = 1, 2, 4, 8, 16
 
 
 class Matrix:
     """Assembled sparse matrix in the space's CSR pattern: FP64 values, and optionally an FP32 copy
     (``fp32``) and the Jacobi-scaled Krylov matrices A D^-1 in FP64 / FP32 (``jacobi64`` /
     ``jacobi32``) written by the same assembly pass. ``dfloat`` assembles in double-float arithmetic
-    on the FP32 pipes (about 1e-14 relative to the native FP64 assembly); with ``ring`` element-only
-    forms on H1 spaces assemble through the element ring instead of the two-pass assembly (the same
-    values, bit for bit)."""
+    on the FP32 pipes (about 1e-14 relative to the native FP64 assembly)."""
 
     def __init__(self, space: Space, fp32: bool = False, jacobi64: bool = False, jacobi32: bool = False,
-                 dfloat: bool = False, batch: int = 1, sell: bool = False, ring: bool = False):
+                 dfloat: bool = False, batch: int = 1, sell: bool = False):
         self.space = space
         h = C.c_void_p()
         flags = (MAT_FP32 if fp32 else 0) | (MAT_JACOBI64 if jacobi64 else 0) | (MAT_JACOBI32 if jacobi32 else 0) \
-            | (MAT_DFLOAT if dfloat else 0) | (MAT_SELL32 if sell else 0) | (MAT_RING if ring else 0)
+            | (MAT_DFLOAT if dfloat else 0) | (MAT_SELL32 if sell else 0)
         self.batch = batch
         LB.call('ocmp_matrix_create_batch', space.h, batch, flags, C.byref(h))
         self.h = h
