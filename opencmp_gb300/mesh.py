@@ -39,6 +39,14 @@ class Mesh:
         """Boundary names, like netgen's ``Mesh.GetBoundaries``."""
         return list(self.bc_names)
 
+    def Refine(self) -> 'Mesh':
+        """Uniform refinement in place, as netgen's ``Mesh.Refine()`` that OpenCMP's h-convergence test
+        calls (``opencmp/post_processing/error_analysis.py:84``): every triangle into four, every
+        tetrahedron into eight (:func:`refine_uniform`)."""
+        r = refine_uniform(self)
+        self.coords, self.elements, self.bfacets, self.blabels = r.coords, r.elements, r.bfacets, r.blabels
+        return self
+
     def label_mask(self, names) -> int:
         """Bit mask of the labels named in ``names`` (a list or a '|'-separated string)."""
         if isinstance(names, str):
@@ -48,6 +56,92 @@ class Mesh:
             if n in self.bc_names:
                 m |= 1 << self.bc_names.index(n)
         return m
+
+
+def _midpoints(coords: np.ndarray, pairs: np.ndarray):
+    """Unique edges of the (k, 2) vertex pairs and, per pair, the index of its midpoint vertex
+    (appended after the existing vertices, edges in ascending (lower, upper) order)."""
+    lo = np.minimum(pairs[:, 0], pairs[:, 1]).astype(np.int64)
+    hi = np.maximum(pairs[:, 0], pairs[:, 1]).astype(np.int64)
+    nv = coords.shape[0]
+    key = lo * nv + hi
+    uniq, inv = np.unique(key, return_inverse=True)
+    ea, eb = uniq // nv, uniq % nv
+    mid = 0.5 * (coords[ea] + coords[eb])
+    return np.concatenate([coords, mid]), (nv + inv).astype(np.int64)
+
+
+def refine_uniform(mesh: Mesh) -> Mesh:
+    """One level of uniform (red) refinement of a straight-sided simplicial mesh.
+
+    Triangles: the three corner triangles and the middle one of the edge midpoints. Tetrahedra: the
+    four corner tetrahedra and the inner octahedron cut into four along its shortest diagonal
+    (the diagonal choice keeps the element shapes from degrading over repeated refinements).
+    Boundary facets are split the same way (edges into two, triangles into four) and keep their
+    labels. Midpoint vertices are numbered after the old vertices in ascending edge order."""
+    X, E = mesh.coords, mesh.elements.astype(np.int64)
+    D = mesh.dim
+    ne = E.shape[0]
+    if D == 2:
+        loc = [(0, 1), (1, 2), (0, 2)]
+    else:
+        loc = [(0, 1), (0, 2), (0, 3), (1, 2), (1, 3), (2, 3)]
+    pairs = np.concatenate([E[:, [a, b]] for a, b in loc])
+    Xn, mids = _midpoints(X, pairs)
+    M = mids.reshape(len(loc), ne).T                     # M[e, k] = midpoint of local edge k
+    if D == 2:
+        v0, v1, v2 = E[:, 0], E[:, 1], E[:, 2]
+        m01, m12, m02 = M[:, 0], M[:, 1], M[:, 2]
+        kids = [(v0, m01, m02), (v1, m12, m01), (v2, m02, m12), (m01, m12, m02)]
+    else:
+        v0, v1, v2, v3 = E.T
+        m = {k: M[:, i] for i, k in enumerate(loc)}
+        kids = [(v0, m[0, 1], m[0, 2], m[0, 3]), (v1, m[0, 1], m[1, 2], m[1, 3]),
+                (v2, m[0, 2], m[1, 2], m[2, 3]), (v3, m[0, 3], m[1, 3], m[2, 3])]
+        # octahedron of the six midpoints: its three diagonals join midpoints of opposite edges;
+        # the four faces around a diagonal run through the other four midpoints in the cycle in
+        # which neighbours share an element vertex
+        diag = [((0, 1), (2, 3), [(0, 2), (1, 2), (1, 3), (0, 3)]),
+                ((0, 2), (1, 3), [(0, 1), (1, 2), (2, 3), (0, 3)]),
+                ((0, 3), (1, 2), [(0, 1), (1, 3), (2, 3), (0, 2)])]
+        length = np.stack([np.linalg.norm(Xn[m[a]] - Xn[m[b]], axis=1) for a, b, _ in diag], 1)
+        pick = np.argmin(length, axis=1)
+        inner = np.zeros((ne, 4, 4), np.int64)
+        for d, (a, b, cyc) in enumerate(diag):
+            sel = pick == d
+            for q in range(4):
+                c0, c1 = cyc[q], cyc[(q + 1) % 4]
+                inner[sel, q] = np.stack([m[a][sel], m[b][sel], m[c0][sel], m[c1][sel]], 1)
+        kids += [tuple(inner[:, q, i] for i in range(4)) for q in range(4)]
+    En = np.sort(np.concatenate([np.stack(k, 1) for k in kids]), axis=1).astype(np.int32)
+    # boundary facets: their edge midpoints are midpoints of element edges (same vertex pairs)
+    F = mesh.bfacets.astype(np.int64)
+    nv = X.shape[0]
+    lo = np.minimum(pairs[:, 0], pairs[:, 1])
+    hi = np.maximum(pairs[:, 0], pairs[:, 1])
+    keys = lo * nv + hi
+    order = np.argsort(keys, kind='stable')
+    ks = keys[order]
+
+    def mid_of(a, b):
+        k = np.minimum(a, b) * nv + np.maximum(a, b)
+        pos = np.searchsorted(ks, k)
+        if np.any(pos >= ks.size) or np.any(ks[np.minimum(pos, ks.size - 1)] != k):
+            raise ValueError('refine_uniform: a boundary facet is not a face of an element')
+        return mids[order[pos]]
+    if D == 2:
+        a, b = F[:, 0], F[:, 1]
+        mab = mid_of(a, b)
+        Fn = np.concatenate([np.stack([a, mab], 1), np.stack([mab, b], 1)])
+        Ln = np.concatenate([mesh.blabels, mesh.blabels])
+    else:
+        a, b, c = F[:, 0], F[:, 1], F[:, 2]
+        mab, mbc, mac = mid_of(a, b), mid_of(b, c), mid_of(a, c)
+        Fn = np.concatenate([np.stack([a, mab, mac], 1), np.stack([b, mbc, mab], 1),
+                             np.stack([c, mac, mbc], 1), np.stack([mab, mbc, mac], 1)])
+        Ln = np.concatenate([mesh.blabels] * 4)
+    return Mesh(np.ascontiguousarray(Xn), np.ascontiguousarray(En), np.ascontiguousarray(Fn.astype(np.int32)),
+                np.ascontiguousarray(Ln.astype(np.int32)), list(mesh.bc_names))
 
 
 def unit_square(n: int) -> Mesh:

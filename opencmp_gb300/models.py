@@ -237,7 +237,9 @@ class Model:
     def __init__(self, config: ConfigParser):
         self.config = config
         self.run_dir = config.get_item(['OTHER', 'run_dir'], str)
-        self.mesh = load_mesh(config.get_item(['MESH', 'filename'], str))
+        # the h-convergence test (post_processing.py) solves again on refined copies of the mesh
+        refined = getattr(config, 'refined_mesh', None)
+        self.mesh = refined if refined is not None else load_mesh(config.get_item(['MESH', 'filename'], str))
         self.gmesh = fem.GPUMesh(self.mesh)
         self.DG = config.get_item(['DG', 'DG'], bool)
         self.ipc = config.get_item(['DG', 'interior_penalty_coefficient'], float)
@@ -372,6 +374,17 @@ class Model:
         for name, v in self.vars.items():
             v.project(self.ic.get(name, {}).get('all', 0.0), 0.0)
 
+    def l2_error_of(self, name: str, t: float) -> float:
+        """|| u_h - u_ref ||_L2 of one model variable against its reference solution at time t
+        (``norm('l2_norm', ...)``, opencmp/helpers/error.py:75-128)."""
+        v = self.vars[name]
+        ref = self.ref_sol.get(name, 0.0)
+        c = _scalar_at(ref, t)
+        if c is not None:
+            return v.space.l2_error(v.u, c)
+        fq = torch.as_tensor(_at(ref, v.quad_points(), t).reshape(self.mesh.ne, -1), device='cuda')
+        return v.space.l2_error(v.u, fq)
+
     def errors(self, t: float) -> List[str]:
         """``L2 norm in <var>: <value>`` lines, as opencmp/helpers/error.py:238-301 prints them."""
         lines = []
@@ -379,15 +392,7 @@ class Model:
             if metric.lower() != 'l2_norm':
                 raise NotImplementedError('{} is not on the GPU path'.format(metric))
             for name in names:
-                v = self.vars[name]
-                ref = self.ref_sol.get(name, 0.0)
-                c = _scalar_at(ref, t)
-                if c is not None:
-                    err = v.space.l2_error(v.u, c)
-                else:
-                    fq = torch.as_tensor(_at(ref, v.quad_points(), t).reshape(self.mesh.ne, -1), device='cuda')
-                    err = v.space.l2_error(v.u, fq)
-                lines.append('{0} in {1}: {2}'.format(metric.replace('_', ' '), name, err))
+                lines.append('{0} in {1}: {2}'.format(metric.replace('_', ' '), name, self.l2_error_of(name, t)))
         return lines
 
 
@@ -679,27 +684,29 @@ class INS(Model):
         b = X[:, 2] - X[:, 0]
         return 0.5 * np.abs(a[:, 0] * b[:, 1] - a[:, 1] * b[:, 0]).sum()
 
+    def l2_error_of(self, name: str, t: float) -> float:
+        th = self.th
+        if name == 'u':
+            ref = self.ref_sol.get('u')
+            rq = None if ref is None else torch.as_tensor(_vec_at(ref, self.quad_points(), t), device='cuda')
+            return th.errors(self.u, rq)[0]
+        if name == 'p':
+            ref = self.ref_sol.get('p', 0.0)
+            c = _scalar_at(ref, t)
+            pv = th.component(self.u, 2)
+            if c is not None:
+                return th.Q.l2_error(pv, c)
+            Xq = th.Q.quad_points()
+            return th.Q.l2_error(pv, torch.as_tensor(_at(ref, Xq, t).reshape(self.mesh.ne, -1), device='cuda'))
+        raise NotImplementedError('L2 error of {} is not on the GPU path'.format(name))
+
     def errors(self, t: float) -> List[str]:
         lines = []
         th = self.th
         for metric, names in self.metrics.items():
             for name in names:
-                if metric.lower() == 'l2_norm' and name == 'u':
-                    ref = self.ref_sol.get('u')
-                    rq = None if ref is None else torch.as_tensor(_vec_at(ref, self.quad_points(), t), device='cuda')
-                    err, _ = th.errors(self.u, rq)
-                    lines.append('L2 norm in u: {}'.format(err))
-                elif metric.lower() == 'l2_norm' and name == 'p':
-                    ref = self.ref_sol.get('p', 0.0)
-                    c = _scalar_at(ref, t)
-                    pv = th.component(self.u, 2)
-                    if c is not None:
-                        err = th.Q.l2_error(pv, c)
-                    else:
-                        Xq = th.Q.quad_points()
-                        err = th.Q.l2_error(pv, torch.as_tensor(_at(ref, Xq, t).reshape(self.mesh.ne, -1),
-                                                                device='cuda'))
-                    lines.append('L2 norm in p: {}'.format(err))
+                if metric.lower() == 'l2_norm' and name in ('u', 'p'):
+                    lines.append('L2 norm in {}: {}'.format(name, self.l2_error_of(name, t)))
                 elif metric == 'divergence' and name == 'u':
                     _, dv = th.errors(self.u)
                     lines.append('divergence of u: {}'.format(dv))

@@ -1,13 +1,14 @@
 """``run(config_file_path, config_parser=None)``: OpenCMP's entry point (``opencmp/run.py:30-71``)
 on the GPU path. Loads the configuration, looks up the model and solver classes, solves, and then
-prints the error metrics as OpenCMP's post-processing does
-(``opencmp/post_processing/__init__.py:28-43``)."""
+runs OpenCMP's post-processing (``opencmp/post_processing/__init__.py:28-43``): the error metrics and
+the h / p convergence tests."""
 from __future__ import annotations
 
 from typing import Optional
 
 from .config import ConfigParser
 from .models import get_model_class
+from .post_processing import run_post_processing
 from .solvers import get_solver_class
 
 
@@ -22,6 +23,5 @@ def run(config_file_path: str, config_parser: Optional[ConfigParser] = None):
     solver_class = get_solver_class(config_parser)
     solver = solver_class(model_class, config_parser)
     sol = solver.solve()
-    if config_parser.get_item(['ERROR ANALYSIS', 'check_error'], bool):
-        solver.report()
+    run_post_processing(config_parser, solver, sol)
     return solver, sol
