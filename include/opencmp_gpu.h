@@ -84,6 +84,9 @@ typedef struct {
                                 keeps them in the time-coefficient form, always implicit, while the
                                 other operator terms are theta-weighted: time_integration_schemes.py) */
     double skeleton_dt;
+    uint32_t robin_mask;     /* labels with a Robin term  dt robin[l] (u, v)_l: OpenCMP's
+                                -dt dc r (u, v) on the marker, robin[l] = -dc r (poisson.py:93-97)   */
+    double robin[32];        /* per label: the coefficient of the Robin facet mass term             */
 } ocmp_form_t;
 
 /* Linear form  L(v) = dt (f, v) + mass (u_prev, v) + dt * sum_l bval[l] <v>_l + DG Dirichlet data */

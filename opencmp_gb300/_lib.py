@@ -33,7 +33,8 @@ class Form(C.Structure):
     _fields_ = [('mass', C.c_double), ('diff', C.c_double), ('dt', C.c_double), ('wind_kind', C.c_int32),
                 ('wind', C.c_double * 3), ('wind_vtx', C.c_void_p), ('ipc', C.c_double), ('dg', C.c_int32),
                 ('outflow_mask', C.c_uint32), ('wn_mask', C.c_uint32), ('nitsche_mask', C.c_uint32),
-                ('skeleton_own_dt', C.c_int32), ('skeleton_dt', C.c_double)]
+                ('skeleton_own_dt', C.c_int32), ('skeleton_dt', C.c_double),
+                ('robin_mask', C.c_uint32), ('robin', C.c_double * 32)]
 
 
 class Rhs(C.Structure):

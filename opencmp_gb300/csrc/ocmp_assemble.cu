@@ -79,8 +79,9 @@ struct FormArgs {
     double mass, diff, dt, dt_skel, ipc, w0, w1, w2;
     const double* wind_vtx;
     int wind_kind;
-    uint32_t outflow, wn, nitsche;
+    uint32_t outflow, wn, nitsche, robin;
     int dg, order;
+    double robin_c[32];
 };
 
 // Facet geometry on local facet lf of element e: outward unit normal, measure factor (length in
@@ -244,7 +245,8 @@ __global__ void boundary_facet_kernel(int64_t nbf, const double* __restrict__ X,
     for (int j = 0; j < L; j++) row[j] = 0;
     const uint32_t bit = (lab >= 0 && lab < 32) ? (1u << lab) : 0u;
     const bool has_out = a.outflow & bit, has_wn = a.wn & bit, has_nit = is_l2 && (a.nitsche & bit);
-    if (has_out || has_wn || has_nit) {
+    const bool has_rob = a.robin & bit;
+    if (has_out || has_wn || has_nit || has_rob) {
         Geo g;
         double x0[3];
         element_geo<D>(X, conn, e, g, x0);
@@ -280,6 +282,7 @@ __global__ void boundary_facet_kernel(int64_t nbf, const double* __restrict__ X,
                 if (has_out) tt += vi * vj * fmax(wn, 0.0);
                 if (has_wn) tt += vi * vj * wn;
                 if (has_nit) tt += a.diff * (alpha * vi * vj - vi * dnj - vj * dni) + vi * vj * fmax(wn, 0.0);
+                if (has_rob) tt += a.robin_c[lab] * vi * vj;
                 row[j] += wq * tt;
             }
         }
@@ -1213,6 +1216,8 @@ FormArgs make_args(const ocmp_space_s* s, const ocmp_form_t* f) {
     a.outflow = f->outflow_mask;
     a.wn = f->wn_mask;
     a.nitsche = f->nitsche_mask;
+    a.robin = f->robin_mask;
+    for (int l = 0; l < 32; l++) a.robin_c[l] = (f->robin_mask >> l) & 1u ? f->robin[l] : 0.0;
     a.dg = f->dg;
     a.order = s->order;
     return a;
@@ -1295,7 +1300,7 @@ int assemble_impl(ocmp_matrix_s* m, const ocmp_form_t* f, cudaStream_t st) {
     // facet matrices
     const bool is_l2 = s->kind == OCMP_L2;
     const bool interior = is_l2 && f->dg && s->nif > 0;
-    const uint32_t bmask = f->outflow_mask | f->wn_mask | (is_l2 ? f->nitsche_mask : 0u);
+    const uint32_t bmask = f->outflow_mask | f->wn_mask | f->robin_mask | (is_l2 ? f->nitsche_mask : 0u);
     const bool boundary = bmask != 0 && s->nbf > 0;
     const bool use_facets = interior || boundary;
     double* Ki = s->d_facetK;

@@ -150,10 +150,15 @@ class Space:
 
 
 def make_form(mass=0.0, diff=0.0, dt=1.0, wind=None, wind_vtx: Optional[torch.Tensor] = None, ipc=10.0, dg=False,
-              outflow_mask=0, wn_mask=0, nitsche_mask=0) -> LB.Form:
+              outflow_mask=0, wn_mask=0, nitsche_mask=0, robin: Optional[Dict[int, float]] = None) -> LB.Form:
+    """The bilinear form; ``robin`` maps boundary labels to the coefficient c of a Robin facet term
+    dt c (u, v) on them (OpenCMP's -dt dc r (u, v), so c = -dc r)."""
     f = LB.Form()
     f.mass, f.diff, f.dt, f.ipc, f.dg = mass, diff, dt, ipc, int(dg)
     f.outflow_mask, f.wn_mask, f.nitsche_mask = outflow_mask, wn_mask, nitsche_mask
+    for lab, c in (robin or {}).items():
+        f.robin_mask |= 1 << lab
+        f.robin[lab] = c
     f.wind_kind = LB.WIND_NONE
     if wind_vtx is not None:
         f.wind_kind = LB.WIND_VERTEX

@@ -33,8 +33,27 @@ from .mesh import load_mesh
 from .saddle import SaddleSolver
 
 
+class _RobinData:
+    """-r q of a Robin marker's [r, q] (the linear form's data, poisson.py:153-157)."""
+
+    def __init__(self, v):
+        self.v = v
+        self.depends_on_space = isinstance(v, Expr) and v.depends_on_space
+
+    def __call__(self, X, t):
+        if isinstance(self.v, Expr):
+            pts = None if X is None else np.asarray(X).reshape(-1, np.asarray(X).shape[-1])
+            rq = np.asarray(self.v(pts, t), float).reshape(-1, 2)
+        else:
+            rq = np.asarray(self.v, float).reshape(-1, 2)
+        out = -rq[:, 0] * rq[:, 1]
+        return float(out[0]) if X is None else out.reshape(np.asarray(X).shape[:-1])
+
+
 def _scalar_at(v, t) -> Optional[float]:
     """The value as a float when it does not depend on x, y, z (None otherwise)."""
+    if isinstance(v, _RobinData):
+        return None if v.depends_on_space else v(None, t)
     if isinstance(v, Expr):
         if v.depends_on_space:
             return None
@@ -46,7 +65,7 @@ def _scalar_at(v, t) -> Optional[float]:
 
 def _at(v, X, t):
     """A parsed config value at the points X (..., dim) and time t."""
-    if isinstance(v, Expr):
+    if isinstance(v, (Expr, _RobinData)):
         return v(X, t)
     return np.full(X.shape[:-1], float(v))
 
@@ -72,10 +91,13 @@ class Variable:
         self.dirichlet = bc.get('dirichlet', {}).get(name, {})
         self.neumann = bc.get('neumann', {}).get(name, {})
         self.total_flux = bc.get('total_flux', {}).get(name, {})
-        if bc.get('robin', {}).get(name) or bc.get('surface_rxn', {}).get(name):
-            raise NotImplementedError('Robin and surface-reaction boundary conditions are not on the GPU path')
+        self.robin = bc.get('robin', {}).get(name, {})
+        if self.robin and not isinstance(model, Poisson):
+            raise NotImplementedError('Robin boundary conditions are on the GPU path for the Poisson model')
+        if bc.get('surface_rxn', {}).get(name):
+            raise NotImplementedError('surface-reaction boundary conditions are not on the GPU path')
         names = set(model.mesh.bc_names)
-        for d in (self.dirichlet, self.neumann, self.total_flux):
+        for d in (self.dirichlet, self.neumann, self.total_flux, self.robin):
             for marker in d:
                 if marker not in names:
                     raise ValueError('boundary {!r} is not a label of the mesh ({})'.format(marker, sorted(names)))
@@ -406,16 +428,39 @@ class Poisson(Model):
         if self.dc is None:
             raise NotImplementedError('a space-dependent diffusion coefficient is not on the GPU path')
 
+    def robin_r(self, var, t: float) -> Dict[int, float]:
+        """Per Robin label, the coefficient of its facet mass term, -dc r (poisson.py:93-97); r is
+        the first entry of the marker's [r, q] and may vary in time, not in space."""
+        out = {}
+        for marker, v in var.robin.items():
+            if isinstance(v, Expr) and v.depends_on_space:
+                X, labs = var._facets()
+                rq = np.asarray(v(X[labs == var.lab(marker)].reshape(-1, X.shape[-1]), t), float).reshape(-1, 2)
+                if rq.size and np.ptp(rq[:, 0]) > 1e-14 * max(1.0, np.abs(rq[:, 0]).max()):
+                    raise NotImplementedError('a space-dependent Robin coefficient r is not on the GPU path')
+                r = float(rq[0, 0]) if rq.size else 0.0
+            else:
+                r = float(np.asarray(v(None, t) if isinstance(v, Expr) else v, float).reshape(-1)[0])
+            out[var.lab(marker)] = -self.dc * r
+        return out
+
     def operator(self, var):
-        return dict(diff=self.dc, ipc=self.ipc, dg=self.DG, nitsche_mask=var.mask(var.dirichlet) if self.DG else 0)
+        op = dict(diff=self.dc, ipc=self.ipc, dg=self.DG, nitsche_mask=var.mask(var.dirichlet) if self.DG else 0)
+        if var.robin:
+            op['robin'] = self.robin_r(var, getattr(self, 't_form', 0.0))
+        return op
 
     def boundary_rhs(self, var, t):
-        neu = var.facet_data(var.neumann, t, self.dc)
+        # Neumann data dc h, and the Robin markers' -dc r q (poisson.py:148-157)
+        data = dict(var.neumann)
+        for marker, v in var.robin.items():
+            data[marker] = _RobinData(v)
+        neu = var.facet_data(data, t, self.dc)
         dir_ = var.facet_data(var.dirichlet, t) if self.DG else ({}, None)
         return neu, dir_
 
     def boundary_mask(self, var):
-        return var.mask(var.neumann)
+        return var.mask(list(var.neumann) + list(var.robin))
 
 
 class MultiComponentINS(Model):

@@ -88,6 +88,7 @@ class Solver:
         mass = 1.0 if transient else 0.0
         # _assemble (base_solver.py:368-377): the bilinear and linear forms of this step, then the
         # preconditioner update
+        m.t_form = t_new                    # time of the step's time-dependent form data (Robin r)
         form = m.form(v, mass, theta * dt, dt)
         r, keep = m.rhs(v, t_new, theta * dt, mass=mass, uprev=uprev)
         v.a.form = form

@@ -621,7 +621,8 @@ static void bfacet_matrix(const or_sp* s, const or_form* f, int64_t e, int lf, i
     memset(K, 0, sizeof(double) * n * n);
     uint32_t bit = 1u << lab;
     int has_out = (f->outflow_mask & bit) != 0, has_wn = (f->wn_mask & bit) != 0, has_nit = (f->nitsche_mask & bit) != 0;
-    if (!has_out && !has_wn && !has_nit) return;
+    int has_rob = (f->robin_mask & bit) != 0;
+    if (!has_out && !has_wn && !has_nit && !has_rob) return;
     geo g;
     elem_geo(s, e, &g);
     double h = pow(g.adet, 1.0 / D);
@@ -646,6 +647,8 @@ static void bfacet_matrix(const or_sp* s, const or_form* f, int64_t e, int lf, i
                 if (has_wn) t += val[i] * val[j] * wn;
                 if (has_nit)
                     t += f->diff * (alpha * val[i] * val[j] - val[i] * dnj - val[j] * dni) + val[i] * val[j] * (wn > 0 ? wn : 0.0);
+                /* Robin term of poisson.py:93-97, -dt dc r u v, with robin[lab] = -dc r */
+                if (has_rob) t += f->robin[lab] * val[i] * val[j];
                 K[i * n + j] += wq * t;
             }
         }
@@ -754,7 +757,7 @@ int or_assemble_matrix(void* sp, const or_form* f, double* vals) {
         int lab = s->bfac[3 * b + 2];
         if (lab < 0 || lab >= 32) continue;
         uint32_t bit = 1u << lab;
-        if (!((f->outflow_mask | f->wn_mask | (s->kind == OR_L2 ? f->nitsche_mask : 0u)) & bit)) continue;
+        if (!((f->outflow_mask | f->wn_mask | f->robin_mask | (s->kind == OR_L2 ? f->nitsche_mask : 0u)) & bit)) continue;
         or_form ff = *f;
         if (s->kind != OR_L2) ff.nitsche_mask = 0;
         bfacet_matrix(s, &ff, s->bfac[3 * b], s->bfac[3 * b + 1], lab, B);

@@ -45,6 +45,8 @@ typedef struct {
     uint32_t wn_mask;       /* boundary labels carrying  dt * r c (w.n)   (MCINS Neumann half)    */
     uint32_t nitsche_mask;  /* DG Dirichlet labels: dt*diff*(alpha r c - r dc/dn - c dr/dn)
                                + dt*r c max(w.n,0)                                                */
+    uint32_t robin_mask;    /* Robin labels: dt * robin[l] * r c  (poisson.py:93-97: -dt dc r u v) */
+    double robin[32];
 } or_form;
 
 typedef struct {

@@ -34,7 +34,8 @@ def build(force: bool = False) -> str:
 class Form(C.Structure):
     _fields_ = [('mass', C.c_double), ('diff', C.c_double), ('dt', C.c_double), ('wind_kind', C.c_int),
                 ('wind', C.c_double * 3), ('wind_vtx', C.c_void_p), ('ipc', C.c_double), ('dg', C.c_int),
-                ('outflow_mask', C.c_uint32), ('wn_mask', C.c_uint32), ('nitsche_mask', C.c_uint32)]
+                ('outflow_mask', C.c_uint32), ('wn_mask', C.c_uint32), ('nitsche_mask', C.c_uint32),
+                ('robin_mask', C.c_uint32), ('robin', C.c_double * 32)]
 
 
 class Rhs(C.Structure):
@@ -88,10 +89,13 @@ def _p(a):
 
 
 def make_form(mass=0.0, diff=0.0, dt=1.0, wind=None, wind_vtx=None, ipc=10.0, dg=False,
-              outflow_mask=0, wn_mask=0, nitsche_mask=0):
+              outflow_mask=0, wn_mask=0, nitsche_mask=0, robin=None):
     f = Form()
     f.mass, f.diff, f.dt, f.ipc, f.dg = mass, diff, dt, ipc, int(dg)
     f.outflow_mask, f.wn_mask, f.nitsche_mask = outflow_mask, wn_mask, nitsche_mask
+    for lab, c in (robin or {}).items():
+        f.robin_mask |= 1 << lab
+        f.robin[lab] = c
     f._keep = None
     if wind_vtx is not None:
         wv = np.ascontiguousarray(wind_vtx, np.float64)
