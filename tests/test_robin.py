@@ -1,12 +1,13 @@
 """Robin boundary conditions of the Poisson model (opencmp/models/poisson.py:93-97, 153-157):
-eta n.grad u = r (u - q) on a marker, i.e. -dt dc r (u, v) in the bilinear form and -dt dc r q (v)
-in the linear form, the marker's value being [r, q].
+-dt dc r (u, v) in the bilinear form and -dt dc r q (v) in the linear form on a marker whose value
+is [r, q]. With the weak form's boundary term dc (n.grad u, v) these impose n.grad u = r (u - q),
+as the Neumann data h of the same forms is n.grad u (poisson.py:148-151).
 
 CPU: the linear-form data -r q of constant and space-dependent [r, q]. GPU: matrix entries with
 Robin terms on two labels against the oracle (1e-12 relative to the largest entry, FP64 and
 double-float assembly, continuous and DG spaces); and a manufactured solution through run():
 u = sin(pi x) cos(pi y) with eta = 0.5, the reference's h-convergence problem with the left
-boundary turned into a Robin boundary (r = -2, q = u - eta n.grad u / r), refined three times:
+boundary turned into a Robin boundary (r = -2, q = u - n.grad u / r), refined three times:
 the L2 error falls at the order-4 rate of P3.
 """
 import math
@@ -62,13 +63,13 @@ def test_robin_manufactured_solution_through_run(gpu_lib, tmp_path, capsys, dg):
     from opencmp_gb300.run import run
     run_dir = os.path.join(str(tmp_path), 'robin')
     shutil.copytree(os.path.join(FIX, 'poisson_h_convergence'), run_dir)
-    # left boundary (x = 0, n = (-1, 0)): eta n.grad u = -eta pi cos(pi y), u = 0, so with r = -2
-    # q = u - eta n.grad u / r = -(pi / 4) cos(pi y)
+    # left boundary (x = 0, n = (-1, 0)): n.grad u = -pi cos(pi y), u = 0, so with r = -2
+    # q = u - n.grad u / r = -(pi / 2) cos(pi y)
     with open(os.path.join(run_dir, 'bc_dir', 'bc_config'), 'w') as fh:
         fh.write('[DIRICHLET]\nu = right  ->  sin(pi * x) * cos(pi * y)\n\n'
                  '[NEUMANN]\nu = top    ->  -pi * sin(pi * x) * sin(pi * y)\n'
                  '    bottom ->  pi * sin(pi * x) * sin(pi * y)\n\n'
-                 '[ROBIN]\nu = left   ->  [-2, -pi / 4 * cos(pi * y)]\n')
+                 '[ROBIN]\nu = left   ->  [-2, -pi / 2 * cos(pi * y)]\n')
     cfg = ConfigParser(os.path.join(run_dir, 'config'))
     cfg['MESH']['filename'] = os.path.join(GOLDEN, 'unit_square_coarse.npz')
     cfg['OTHER']['run_dir'] = run_dir
