@@ -50,6 +50,12 @@ TRAFFIC_PER_NNZ = {'gm_spmv_float': 8.615, 'gm_spmv_sell': 9.768}
 ASSEMBLY_TRAFFIC_RATIO = 2168.0 / 227.0
 
 
+def workload_config(n, restart, ndof, nnz, world=1):
+    """The bench line's `config`: the problem both arms solve (the path each takes is in `path`)."""
+    return {'workload': WORKLOAD.format(n, restart), 'ndof': ndof, 'nnz': nnz,
+            'parallelism': 'replicas' if world > 1 else 'single GPU', 'l2': 'inputs larger than L2 (no flush)'}
+
+
 def gaussian(X):
     c = np.asarray(GAUSS['c'])
     return np.exp(-((X - c) ** 2).sum(-1) / (2 * GAUSS['s'] ** 2))
@@ -332,10 +338,9 @@ def run_ours(args):
         'metric': METRIC, 'value': value, 'unit': 'DOF/s', 'n_gpus': world, 'steps': args.steps, 'warmup': args.warmup,
         'ms_per_step': ms_opt / args.steps, 'higher_is_better': True, 'scaling': 'weak', 'vs_baseline': None,
         'dtype': 'f64+f32', 'data': 'synthetic (generated structured mesh, Gaussian initial condition)',
-        'config': {'workload': WORKLOAD.format(n, args.restart) + ', optimised path: double-float assembly, '
-                               'learned initial guess under its judge, FP32 inner GMRES + FP64 refinement',
-                   'ndof': ndof, 'nnz': nnz, 'parallelism': 'replicas' if world > 1 else 'single GPU',
-                   'l2': 'inputs larger than L2 (no flush)'},
+        'config': workload_config(n, args.restart, ndof, nnz, world),
+        'path': 'optimised: double-float assembly, learned initial guess under its judge, FP32 inner GMRES + FP64 '
+                'refinement',
         'plain_fp64': {'value': plain, 'unit': 'DOF/s', 'ms_per_step': ms_plain / args.steps,
                        'relres0_per_step': plain_relres0[0],
                        'iters_per_step': float(np.mean([s[0] for s in st_plain]))},
@@ -927,8 +932,8 @@ def dg2d_cpu_baseline(n_cpu):
                       'dofs), relres {2:.1e}'.format(n_cpu, o.ndof, o.relres(A, bo, x))}
 
 
-def cpu_steps(n_cpu, warmup, steps):
-    """The oracle's implicit-Euler step (full reassembly + GMRES(30)/Jacobi to 1e-8 from the
+def cpu_steps(n_cpu, warmup, steps, restart=30):
+    """The oracle's implicit-Euler step (full reassembly + GMRES(restart)/Jacobi to 1e-8 from the
     previous-step guess, OpenCMP's start) on the n_cpu^3 x 6 mesh, all host threads: `warmup`
     untimed steps from the Gaussian start, then `steps` timed ones."""
     from oracle import oracle as O
@@ -946,7 +951,7 @@ def cpu_steps(n_cpu, warmup, steps):
         A = s.assemble(f)
         b = s.rhs(f, O.make_rhs(dt=DT, mass=1.0, uprev=u))
         x = u.copy()
-        it, _ = s.gmres(A, b, x, restart=30, precond=1, tol=1e-8, maxit=2000)
+        it, _ = s.gmres(A, b, x, restart=restart, precond=1, tol=1e-8, maxit=2000)
         iters.append(it)
         return x
 
@@ -957,7 +962,7 @@ def cpu_steps(n_cpu, warmup, steps):
     for _ in range(steps):
         u = one(u)
     dt = time.perf_counter() - t0
-    return s.ndof, dt, threads, float(np.mean(iters)) if iters else 0.0
+    return s.ndof, dt, threads, float(np.mean(iters)) if iters else 0.0, s.nnz
 
 
 def _interp_p2_oracle(s, m):
@@ -966,7 +971,7 @@ def _interp_p2_oracle(s, m):
 
 
 def cpu_baseline(n_cpu, warmup=1, steps=2):
-    ndof, dt, threads, its = cpu_steps(n_cpu, warmup, steps)
+    ndof, dt, threads, its, _ = cpu_steps(n_cpu, warmup, steps)
     return {'value': ndof * steps / dt, 'unit': 'DOF/s', 'cores': threads, 'kind': 'port',
             'sample': 'implicit-Euler steps {}..{} from the Gaussian start (full reassembly + GMRES(30)/Jacobi to '
                       '1e-8 from the previous-step guess, {:.1f} iterations per step) on the {}^3 x 6 tet mesh ({} '
@@ -981,14 +986,15 @@ def run_reference(args):
     if rank != 0:
         return
     steps = max(1, args.steps)
-    ndof, dt, threads, its = cpu_steps(args.n, args.warmup, steps)
+    ndof, dt, threads, its, nnz = cpu_steps(args.n, args.warmup, steps, args.restart)
     v = ndof * steps / dt
     line = {'metric': METRIC, 'value': v, 'unit': 'DOF/s', 'n_gpus': 0, 'steps': steps, 'warmup': args.warmup,
             'ms_per_step': dt / steps * 1e3, 'higher_is_better': True, 'scaling': 'weak', 'vs_baseline': None,
             'dtype': 'f64', 'data': 'synthetic (generated structured mesh, Gaussian initial condition)',
             'impl': 'reference',
-            'config': {'workload': WORKLOAD.format(args.n, 30) + ', previous-step guess',
-                       'ndof': ndof, 'l2': 'inputs larger than L2 (no flush)'},
+            'config': workload_config(args.n, args.restart, ndof, nnz),
+            'path': "OpenCMP's algorithm for the step (FP64 assembly, GMRES({}) + Jacobi from the previous-step "
+                    "guess) restated by the oracle in C with OpenMP".format(args.restart),
             'cpu_baseline': {'value': v, 'unit': 'DOF/s', 'cores': threads, 'kind': 'port',
                              'sample': 'steps {}..{} from the Gaussian start on {} dofs, {:.1f} GMRES iterations per '
                                        'step, C oracle with OpenMP'.format(args.warmup + 1, args.warmup + steps,
