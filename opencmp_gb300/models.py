@@ -19,6 +19,7 @@ and ``skeleton_dt`` the interior-facet terms.
 """
 from __future__ import annotations
 
+import ctypes as C
 import math
 from typing import Dict, List, Optional
 
@@ -479,20 +480,51 @@ class MultiComponentINS(Model):
             self._wind_vtx = torch.as_tensor(np.ascontiguousarray(W(self.mesh.coords, 0.0)), device='cuda')
         elif W is not None:
             self._wind_const = tuple(np.ravel(W(None, 0.0) if isinstance(W, Expr) else [float(W)]))
+        # Oseen (the default) keeps the convection implicit; IMEX moves it to the linear form at the
+        # previous step's concentration (multi_component_ins.py:390-430, euler_IMEX in
+        # time_integration_schemes.py:193-250)
+        self.linearize = config.get_item(['SOLVER', 'linearization_method'], str)
+        if self.linearize == 'IMEX':
+            if self.DG:
+                raise NotImplementedError('the IMEX linearisation of MultiComponentINS is on the GPU path for '
+                                          'continuous spaces')
+            if any(self.bc.get('total_flux', {}).get(c) for c in self.components):
+                raise ValueError('Cannot specify total flux for IMEX schemes since convection term is fully explicit.')
 
     def symmetric(self, var):
+        if self.linearize == 'IMEX':
+            return True                       # mass and diffusion only
         if self._wind_vtx is not None:
             return False
         return self._wind_const is None or not any(self._wind_const)
 
     def operator(self, var):
-        flux = set(self.mesh.bc_names) - set(var.dirichlet) - set(var.neumann)
         if var.neumann and self.D[var.name] == 0:
             raise ValueError('Trying to apply a neuman boundary condition for purely advective flow '
                              '(diffusion coefficient is 0).')
+        if self.linearize == 'IMEX':
+            return dict(diff=self.D[var.name], ipc=self.ipc, dg=self.DG)
+        flux = set(self.mesh.bc_names) - set(var.dirichlet) - set(var.neumann)
         return dict(diff=self.D[var.name], wind=self._wind_const, wind_vtx=self._wind_vtx, ipc=self.ipc, dg=self.DG,
                     outflow_mask=var.mask(flux), wn_mask=var.mask(var.neumann),
                     nitsche_mask=var.mask(var.dirichlet) if self.DG else 0)
+
+    def imex_explicit(self, var, dt: float, t_new: float, uprev: torch.Tensor):
+        """The explicit part of the IMEX linear form, added to var.b (multi_component_ins.py:390-430):
+        dt (c^n, w . grad r) = -dt K_w c^n, K_w the convection matrix, and -dt (h, r) on the Neumann
+        markers (a second time: OpenCMP's explicit part repeats the linear form's Neumann half)."""
+        if self._wind_const is not None or self._wind_vtx is not None:
+            conv = fem.make_form(wind=self._wind_const, wind_vtx=self._wind_vtx)
+            if getattr(var, 'opx', None) is None:
+                var.opx = fem.Matrix(var.space)
+            var.opx.assemble(conv)
+            LB.call('ocmp_spmv_axpby', var.opx.h, -dt, C.c_void_p(uprev.data_ptr()), 1.0,
+                    C.c_void_p(var.b.data_ptr()), C.c_void_p(torch.cuda.current_stream().cuda_stream))
+        if var.neumann:
+            consts, fq = var.facet_data(var.neumann, t_new, -1.0)
+            r = fem.make_rhs(dt=dt, bval=consts, bval_fq=fq, bval_mask=var.mask(var.neumann))
+            r.accumulate = 1
+            fem.assemble_rhs(var.space, fem.make_form(), r, var.b)
 
     def boundary_rhs(self, var, t):
         d = dict(var.neumann)

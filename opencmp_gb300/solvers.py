@@ -106,6 +106,8 @@ class Solver:
             v.op.assemble(op_form)
             LB.call('ocmp_spmv_axpby', v.op.h, -(1.0 - theta) * dt, _ptr(uprev), 1.0, _ptr(v.b), _stream(None))
             del keep0
+        if transient and getattr(m, 'linearize', None) == 'IMEX' and hasattr(m, 'imex_explicit'):
+            m.imex_explicit(v, dt, t_new, uprev)
         info = v.solve(u_to)
         del keep
         if g is not None:
@@ -187,6 +189,9 @@ class TransientMultiStepSolver(Solver):
         self.t = self.t_range[0]
         self._next_dt = None
         order = IMEX.get(self.scheme, 1)
+        if order > 1 and not hasattr(self.model, 'startup_step'):
+            raise NotImplementedError('{!r} is on the GPU path for the INS model; other models take euler IMEX'.format(
+                self.scheme))
         if order > 1:
             # start-up (transient_multistep.py:51-100): order - 1 implicit-Euler steps of dt = 1e-10;
             # the first step of the scheme itself also takes 1e-10 (its dt is reset after the step)

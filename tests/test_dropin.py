@@ -49,8 +49,9 @@ def _cases():
         dg = cfg.get_item(['DG', 'DG'], bool)
         if scheme not in SUPPORTED:
             marks = [pytest.mark.skip(reason='time scheme {!r} is not on the GPU path'.format(scheme))]
-        elif scheme in ('euler IMEX', 'CNLF', 'SBDF') and model != 'INS':
-            marks = [pytest.mark.skip(reason='IMEX linearisation is on the GPU path for INS only')]
+        elif scheme in ('euler IMEX', 'CNLF', 'SBDF') and model != 'INS' and (scheme != 'euler IMEX' or dg):
+            marks = [pytest.mark.skip(reason='IMEX linearisation is on the GPU path for INS, and for the other '
+                                             'models as euler IMEX on continuous spaces')]
         elif model == 'INS' and (dg or scheme not in ('implicit euler', 'euler IMEX', 'CNLF', 'SBDF')):
             marks = [pytest.mark.skip(reason='INS runs on the GPU path as continuous Taylor-Hood with implicit '
                                              'Euler (Oseen) or the IMEX schemes')]
