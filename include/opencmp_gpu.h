@@ -295,6 +295,7 @@ typedef struct {
     int32_t schulz_strips;   /* of those, interface inverses by Newton-Schulz from the previous one */
     int32_t schulz_iterations; /* Newton-Schulz steps in total                                      */
     int32_t schulz_fallbacks;  /* Newton-Schulz attempts that fell back to Gauss-Jordan             */
+    double gemm_bytes;       /* algorithmic bytes of the dense products (operands once, C out/in)   */
 } ocmp_strip_stats_t;
 int ocmp_solver_strip_stats(ocmp_solver_t solver, ocmp_strip_stats_t* out);
 /* time every dense product of the next factorisations with CUDA events (measurement) */

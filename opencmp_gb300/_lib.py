@@ -76,7 +76,7 @@ class StripStats(C.Structure):
                 ('gemm_ms', C.c_double), ('gemm_flops', C.c_double), ('singular_tiles', C.c_int32),
                 ('gemm_kind', C.c_int32), ('tile_ms', C.c_double), ('panel_ms', C.c_double),
                 ('fast_strips', C.c_int32), ('schulz_strips', C.c_int32), ('schulz_iterations', C.c_int32),
-                ('schulz_fallbacks', C.c_int32)]
+                ('schulz_fallbacks', C.c_int32), ('gemm_bytes', C.c_double)]
 
 
 P = C.c_void_p

@@ -119,7 +119,7 @@ struct Strip {
     std::vector<int> ev_tag;            // per event pair: 0 product, 1 tile inversion, 2 panels
     double part_ms[3] = {0, 0, 0};
     cudaEvent_t fev[2] = {nullptr, nullptr};
-    double factor_ms = 0, gemm_ms = 0, gemm_flops = 0, gemm_flops_pending = 0;
+    double factor_ms = 0, gemm_ms = 0, gemm_flops = 0, gemm_flops_pending = 0, gemm_bytes = 0, gemm_bytes_pending = 0;
     int singular = 0;
     int gemm_kind = 0;               // 0: FP32 SIMT, 1: tensor cores (3xTF32)
     // Newton-Schulz path (strips whose N dofs form small independent groups, e.g. the elements of a
@@ -821,6 +821,8 @@ int gemm(Strip* p, int M, int N, int K, const float* A, int64_t lda, const float
     }
     if (t && tend(p, st, 0)) return OCMP_ERR_CUDA;
     p->gemm_flops_pending += 2.0 * M * N * (double)K;
+    // operands read once, C written (and read when beta != 0): the product's algorithmic bytes
+    p->gemm_bytes_pending += 4.0 * ((double)M * K + (double)N * K + (beta != 0.f ? 2.0 : 1.0) * M * (double)N);
     return OCMP_OK;
 }
 
@@ -1417,6 +1419,7 @@ int strip_factor(Strip* p, const ocmp_space_s* s, const double* vals, cudaStream
     p->ev_used = 0;
     p->ev_tag.clear();
     p->gemm_flops_pending = 0;
+    p->gemm_bytes_pending = 0;
     p->ns_iters = p->ns_strips = p->ns_fallbacks = 0;
     for (int& h : p->h_n) h = 0;
     OCMP_CUDA(cudaEventRecord(p->fev[0], st));
@@ -1482,6 +1485,7 @@ int strip_factor(Strip* p, const ocmp_space_s* s, const double* vals, cudaStream
     p->singular = flags[0];
     if (flags[1]) return fail(OCMP_TIMEOUT, "strip preconditioner: a tensor-core product gave up a bounded wait");
     p->gemm_flops = p->gemm_flops_pending;
+    p->gemm_bytes = p->gemm_bytes_pending;
     p->gemm_ms = 0;
     for (double& x : p->part_ms) x = 0;
     for (size_t q = 0; q + 1 < p->ev_used; q += 2) {
@@ -1571,6 +1575,7 @@ void strip_stats(const Strip* p, ocmp_strip_stats_t* o) {
     o->factor_ms = p->factor_ms;
     o->gemm_ms = p->gemm_ms;
     o->gemm_flops = p->gemm_flops;
+    o->gemm_bytes = p->gemm_bytes;
     o->singular_tiles = p->singular;
     o->gemm_kind = p->gemm_kind;
     o->tile_ms = p->part_ms[1];
