@@ -701,12 +701,39 @@ class INS(Model):
         """One time step: implicit Euler with Oseen Picard iterations, or one of the IMEX schemes
         (Euler IMEX, CNLF, SBDF of time_integration_schemes.py); the stationary solve when not
         transient."""
-        if theta != 1.0:
-            raise NotImplementedError('INS runs on the GPU path with implicit Euler, Euler IMEX, CNLF or SBDF')
+        if theta != 1.0 and not (theta == 0.5 and transient and self.linearize == 'Oseen'):
+            raise NotImplementedError('INS runs on the GPU path with implicit Euler, Crank-Nicolson (Oseen), '
+                                      'Euler IMEX, CNLF or SBDF')
         th = self.th
         uprev = self.u.clone() if transient else None
         mass = 1.0 if transient else 0.0
         f, fq = self.source(t_new)
+        if theta == 0.5:
+            # Crank-Nicolson with Oseen Picard iterations (time_integration_schemes.py:135-190): the
+            # pressure / divergence terms implicit with the full dt, the viscous and linearised
+            # convection terms halved, their old-time half moved to the linear form with the wind u^n
+            # (ins.py:136-161: at the previous step the wind is that step's velocity):
+            #   (M + coef(dt) + 1/2 ODE(.; W)) u = M u^n + dt/2 (f^{n+1} + f^n) - 1/2 ODE(u^n; u^n) u^n
+            f0, fq0 = self.source(t_old)
+            if self.Kv is None:
+                self.Kv = th.matrix()
+            th.assemble(self.Kv, mass=0.0, nu=self.kv, dt=dt, wind=uprev, tcoef=0.0)
+            area = float(self.mesh_area())
+            for it in range(self.max_picard):
+                self.set_dirichlet(t_new)
+                th.assemble(self.A, mass=1.0, nu=self.kv, dt=0.5 * dt, wind=self.W, tcoef=dt)
+                th.assemble_rhs(self.b, dt=0.5 * dt, src=f, src_qp=fq, mass=1.0, uprev=uprev)
+                th.assemble_rhs(self.b, dt=0.5 * dt, src=f0, src_qp=fq0, accumulate=True)
+                LB.call('ocmp_spmv_axpby', self.Kv.h, -0.5, fem._ptr(uprev), 1.0, fem._ptr(self.b), None)
+                infos.append(self._solve(1.0, 0.5 * dt, dt))
+                d = self.u - self.W
+                err, _ = th.errors(d)
+                unorm, _ = th.errors(self.u)
+                self.W.copy_(self.u)
+                if err < self.abs_tol + self.rel_tol * unorm / math.sqrt(area):
+                    break
+            self._push()
+            return
         if self.linearize == 'IMEX' and self.scheme == 'CNLF':
             # (2 coef + ODE + M) u = M u^{n-1} + L(t^{n-1}) - ODE(u^{n-1}) + 2 N(u^n)
             u1 = self.hist[1]
