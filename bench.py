@@ -898,25 +898,21 @@ def run_dg2d(args):
             'factorisation': gem,
             'e2e': {'value': nd / (ms_e2e * 1e-3), 'unit': 'DOF/s', 'h2d_bytes_per_step': 8 * fq.numel(),
                     'd2h_bytes_per_step': 8 * nd},
-            # the products of the factorisation are mostly rank-128 updates (K = 128): their intensity
-            # (FP32-equivalent flops per algorithmic byte) sits below the tensor/HBM ridge, so HBM is the
-            # bound they are measured against; the tensor figure stands beside it
-            'roofline': ({'bound': 'hbm', 'kernel': 'tc_gemm_nt_kernel (tcgen05 kind::tf32, 3xTF32, TMA-staged)',
-                          'achieved': tc['gbs'], 'peak': hbm_peak, 'peak_kind': hbm_kind, 'unit': 'GB/s',
-                          'frac': tc['gbs'] / hbm_peak if tc['gbs'] else None,
-                          'intensity_flop_per_byte': tc['gemm_flops'] / tc['gemm_bytes'],
-                          'ridge_flop_per_byte': peak * 1e12 / (hbm_peak * 1e9),
-                          'bytes': 'per product A and B read once, C written (and read when beta != 0)',
-                          'traffic': None}
-                         if tc['gemm_bytes'] and tc['gemm_flops'] / tc['gemm_bytes'] < peak * 1e12 / (hbm_peak * 1e9)
-                         else {'bound': 'tensor', 'kernel': 'tc_gemm_nt_kernel (tcgen05 kind::tf32, 3xTF32, TMA-staged)',
-                               'achieved': tc['tflops'], 'peak': peak, 'peak_kind': peak_kind + ' bf16 dense (burst)',
-                               'unit': 'TFLOP/s', 'frac': tc['tflops'] / peak if tc['tflops'] else None,
-                               'traffic': None}),
-            'roofline_tensor': {'achieved': tc['tflops'], 'peak': peak, 'peak_kind': peak_kind + ' bf16 dense (burst)',
-                                'unit': 'TFLOP/s', 'frac': tc['tflops'] / peak if tc['tflops'] else None,
-                                'flops': 'FP32-equivalent 2 M N K per product (the three TF32 products of the '
-                                         'split are not counted)'},
+            # the 3xTF32 split issues three TF32 products per FP32-equivalent product and TF32 runs at
+            # 1.1 / 2.25 of the BF16 rate (nominal dense figures), so the products' own peak is the
+            # measured BF16 rate x (1.1 / 2.25) / 3; their intensity (FP32-equivalent flops per
+            # algorithmic byte) is above that peak's ridge against HBM, so they are tensor-bound
+            'roofline': {'bound': 'tensor', 'kernel': 'tc_gemm_nt_kernel (tcgen05 kind::tf32, 3xTF32, TMA-staged)',
+                         'achieved': tc['tflops'], 'peak': peak * (1.1 / 2.25) / 3.0,
+                         'peak_kind': peak_kind + ' bf16 dense (burst) x nominal TF32/BF16 rate (1.1/2.25) / 3 '
+                                                  '(three TF32 products per FP32-equivalent product)',
+                         'unit': 'TFLOP/s', 'frac': tc['tflops'] / (peak * (1.1 / 2.25) / 3.0) if tc['tflops'] else None,
+                         'flops': 'FP32-equivalent 2 M N K per product',
+                         'intensity_flop_per_byte': tc['gemm_flops'] / tc['gemm_bytes'] if tc['gemm_bytes'] else None,
+                         'ridge_flop_per_byte': peak * (1.1 / 2.25) / 3.0 * 1e12 / (hbm_peak * 1e9),
+                         'achieved_gbs': tc['gbs'], 'traffic': None},
+            'roofline_bf16': {'achieved': tc['tflops'], 'peak': peak, 'peak_kind': peak_kind + ' bf16 dense (burst)',
+                              'unit': 'TFLOP/s', 'frac': tc['tflops'] / peak if tc['tflops'] else None},
             'gpu_launches': res['tensor_fp64']['launches']}
     if not args.no_cpu:
         line['cpu_baseline'] = dg2d_cpu_baseline(args.dg_cpu_n)
