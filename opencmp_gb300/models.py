@@ -782,6 +782,25 @@ class INS(Model):
                 break
         self._push()
 
+    # ---------------------------------------------------------------- adaptive time stepping
+    def adaptive_state(self):
+        """What one step changes (solution, Picard wind, step history), for an attempt to be undone."""
+        return self.u.clone(), self.W.clone(), [h.clone() for h in self.hist]
+
+    def adaptive_restore(self, st):
+        u, W, hist = st
+        self.u.copy_(u)
+        self.W.copy_(W)
+        for h, h0 in zip(self.hist, hist):
+            h.copy_(h0)
+
+    def local_errors(self, kept, other):
+        """[(|| kept - other ||, || kept ||)] over the components in OpenCMP's local error: the velocity
+        only (ins.py:67-69)."""
+        d, _ = self.th.errors(kept - other)
+        n, _ = self.th.errors(kept)
+        return [(d or 1e-10, n or 1e-10)]
+
     def mesh_area(self):
         X = self.mesh.coords[self.mesh.elements]
         a = X[:, 1] - X[:, 0]

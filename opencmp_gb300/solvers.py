@@ -239,7 +239,7 @@ class AdaptiveSolver(TransientMultiStepSolver):
 
     def __init__(self, model_class, config):
         Solver.__init__(self, model_class, config)
-        if hasattr(self.model, 'step'):
+        if hasattr(self.model, 'step') and not hasattr(self.model, 'adaptive_state'):
             raise NotImplementedError('adaptive time stepping is not on the GPU path for this model')
         self.scheme = config.get_item(['TRANSIENT', 'scheme'], str)
         self.t_range = config.get_list(['TRANSIENT', 'time_range'], float)
@@ -275,15 +275,42 @@ class AdaptiveSolver(TransientMultiStepSolver):
                 out[v.name] = (short, long_)
         return out
 
+    def _attempt_model(self, dt, t_old):
+        """Both solutions of an attempt for a model that steps itself (INS): the kept one stays in the
+        model; returns (state before the attempt, kept, other)."""
+        m = self.model
+        t_new = t_old + dt
+        st0 = m.adaptive_state()
+        if self.scheme == 'adaptive two step':
+            m.step(0.5, dt, t_new, t_old, True, self.infos)
+            other = m.u.clone()
+            m.adaptive_restore(st0)
+            m.step(1.0, dt, t_new, t_old, True, self.infos)
+        else:
+            m.step(1.0, dt, t_new, t_old, True, self.infos)
+            other = m.u.clone()
+            m.adaptive_restore(st0)
+            m.step(1.0, dt / 2, t_old + dt / 2, t_old, True, self.infos)
+            m.step(1.0, dt / 2, t_new, t_old + dt / 2, True, self.infos)
+        return st0, m.u.clone(), other
+
     def solve(self):
         t1 = self.t_range[1]
         rejects = 0
         if self.saver is not None:
             self.saver.save(self.t)
+        whole = hasattr(self.model, 'step')
         while self.t < t1 and not np.isclose(self.t, t1):
             dt = min(self.dt, t1 - self.t)
-            sols = self._attempt(dt, self.t)
             errs, norms = [], []
+            if whole:
+                st0, kept, other = self._attempt_model(dt, self.t)
+                for e, nrm in self.model.local_errors(kept, other):
+                    errs.append(e)
+                    norms.append(nrm)
+                sols = {}
+            else:
+                sols = self._attempt(dt, self.t)
             for name, (kept, other) in sols.items():
                 v = self.model.vars[name]
                 errs.append(v.space.l2_error(kept - other) or 1e-10)
@@ -307,6 +334,8 @@ class AdaptiveSolver(TransientMultiStepSolver):
                 if self.check_error:
                     self.report()
             else:
+                if whole:
+                    self.model.adaptive_restore(st0)
                 rejects += 1
                 if rejects > self.max_rejects:
                     raise RuntimeError('At t = {} the maximum number of rejected time steps has been exceeded.'

@@ -52,8 +52,8 @@ def _cases():
         elif scheme in ('euler IMEX', 'CNLF', 'SBDF') and model != 'INS' and (scheme != 'euler IMEX' or dg):
             marks = [pytest.mark.skip(reason='IMEX linearisation is on the GPU path for INS, and for the other '
                                              'models as euler IMEX on continuous spaces')]
-        elif model == 'INS' and (dg or scheme not in ('implicit euler', 'crank nicolson', 'euler IMEX', 'CNLF',
-                                                      'SBDF')):
+        elif model == 'INS' and (dg or scheme not in ('implicit euler', 'crank nicolson', 'adaptive two step',
+                                                      'adaptive three step', 'euler IMEX', 'CNLF', 'SBDF')):
             marks = [pytest.mark.skip(reason='INS runs on the GPU path as continuous Taylor-Hood with implicit '
                                              'Euler or Crank-Nicolson (Oseen) or the IMEX schemes')]
         elif t['id'] in UNSTABLE:
