@@ -68,6 +68,53 @@ def _sgn(a, eps=1e-12):
     return np.where(a < -eps, -1.0, np.where(a > eps, 1.0, 0.0))
 
 
+# IMPORT(name) (opencmp/config_functions/parse_arithmetic.py:105, 238-256): the function `name` of
+# the run directory's import_functions.py, called as OpenCMP calls it, f(t_param, new_variables,
+# mesh, time_step), with t_param the list [t]. OpenCMP's functions return NGSolve coefficient
+# functions; here the result is a number, an array over the points, or a callable f(X) or f(X, t)
+# evaluated at the points X (N x dim). The run directory is the one whose configuration is being
+# read (set_import_dir).
+_IMPORT_DIR: Optional[str] = None
+_IMPORTED: Dict[str, Any] = {}
+
+
+def set_import_dir(path: Optional[str]) -> None:
+    """Directory whose import_functions.py IMPORT(...) expressions read (the run directory)."""
+    global _IMPORT_DIR
+    _IMPORT_DIR = path
+
+
+def _imported(name: str, import_dir: Optional[str]):
+    if import_dir is None:
+        raise ValueError('IMPORT({}): no run directory to import from'.format(name))
+    path = os.path.join(import_dir, 'import_functions.py')
+    mod = _IMPORTED.get(path)
+    if mod is None:
+        import importlib.util
+        spec = importlib.util.spec_from_file_location('import_functions_{}'.format(len(_IMPORTED)), path)
+        if spec is None or not os.path.isfile(path):
+            raise FileNotFoundError('IMPORT({}): {} not found'.format(name, path))
+        mod = importlib.util.module_from_spec(spec)
+        spec.loader.exec_module(mod)
+        _IMPORTED[path] = mod
+    fn = getattr(mod, name)
+    if not callable(fn):
+        raise TypeError('IMPORT({}): not a function'.format(name))
+    return fn
+
+
+def _import_value(fn, X, t):
+    v = fn([t], [{}], None, None)
+    if callable(v):
+        import inspect
+        try:
+            nargs = len(inspect.signature(v).parameters)
+        except (TypeError, ValueError):
+            nargs = 2
+        v = v(X, t) if nargs >= 2 else v(X)
+    return v
+
+
 FUNCS = {'sin': np.sin, 'cos': np.cos, 'tan': np.tan, 'exp': np.exp, 'tanh': _tanh, 'sig': _sig, 'H': _heaviside,
          'abs': np.abs, 'trunc': np.trunc, 'round': np.round, 'sqrt': np.sqrt, 'sgn': _sgn, 'ramp': _ramp}
 CONSTS = {'pi': math.pi, 'e': math.e}
@@ -81,6 +128,7 @@ class Expr:
         self.text = text.strip()
         self._toks = [(m.group(1), m.group(2), m.group(3)) for m in _TOKEN.finditer(self.text) if any(m.groups())]
         self._pos = 0
+        self._imports: List[Any] = []
         self.ast = self._expr()
         if self._pos != len(self._toks):
             raise ValueError('cannot parse expression: {!r}'.format(text))
@@ -145,6 +193,15 @@ class Expr:
         if op == '[':
             return ('vec', self._args(']'))
         if name is not None:
+            if name == 'IMPORT' and self._peek()[2] == '(':
+                self._take()
+                _, fname, _ = self._take()
+                self._take(')')
+                if fname is None:
+                    raise ValueError('IMPORT takes the name of a function: {!r}'.format(self.text))
+                fn = _imported(fname, _IMPORT_DIR)
+                self._imports.append(fn)
+                return ('import', fn)
             if self._peek()[2] == '(':
                 self._take()
                 args = self._args(')')
@@ -171,6 +228,8 @@ class Expr:
             return X[..., c] if X is not None and c < X.shape[-1] else 0.0
         if k == 'neg':
             return -self._eval(node[1], X, t)
+        if k == 'import':
+            return _import_value(node[1], X, t)
         if k == 'call':
             return FUNCS[node[1]](*[self._eval(a, X, t) for a in node[2]])
         if k == 'vec':
@@ -184,7 +243,10 @@ class Expr:
 
     @property
     def depends_on_space(self) -> bool:
-        return re.search(r'\b[xyz]\b', self.text) is not None
+        if re.search(r'\b[xyz]\b', self.text) is not None:
+            return True
+        # an imported function depends on space unless it returns a number
+        return any(not np.isscalar(fn([0.0], [{}], None, None)) for fn in self._imports)
 
     def __call__(self, X=None, t=0.0):
         v = self._eval(self.ast, X, t)

@@ -29,7 +29,7 @@ import torch
 from . import _lib as LB
 from . import fem
 from . import forms
-from .config import ConfigParser, Expr, load_sub_config, parse, value_map
+from .config import ConfigParser, Expr, load_sub_config, parse, set_import_dir, value_map
 from .mesh import load_mesh
 from .saddle import SaddleSolver
 
@@ -268,6 +268,7 @@ class Model:
         self.ipc = config.get_item(['DG', 'interior_penalty_coefficient'], float)
         self.interp_ord = config.get_item(['FINITE ELEMENT SPACE', 'interpolant_order'], int)
         self.elements = config.get_dict(['FINITE ELEMENT SPACE', 'elements'], all_str=True)
+        set_import_dir(self.run_dir)        # IMPORT(...) in the sub-configurations reads this run's functions
         bc = load_sub_config(self.run_dir, 'bc')
         self.bc = {k.lower(): value_map(bc, k) for k in (bc.sections() if bc else [])}
         ic = load_sub_config(self.run_dir, 'ic')
