@@ -129,6 +129,7 @@ class Expr:
         self._toks = [(m.group(1), m.group(2), m.group(3)) for m in _TOKEN.finditer(self.text) if any(m.groups())]
         self._pos = 0
         self._imports: List[Any] = []
+        self.mvars: set = set()
         self.ast = self._expr()
         if self._pos != len(self._toks):
             raise ValueError('cannot parse expression: {!r}'.format(text))
@@ -214,27 +215,34 @@ class Expr:
                 return ('var', name)
             if name in CONSTS:
                 return ('num', CONSTS[name])
-            raise ValueError('unknown name {!r} in {!r}'.format(name, self.text))
+            # any other name is a model variable (a component of the model's solution, e.g. the
+            # concentration `a` in a reaction source `-1*a`): its value is supplied at evaluation
+            self.mvars.add(name)
+            return ('mvar', name)
         raise ValueError('cannot parse expression: {!r}'.format(self.text))
 
-    def _eval(self, node, X, t):
+    def _eval(self, node, X, t, vals=None):
         k = node[0]
         if k == 'num':
             return node[1]
+        if k == 'mvar':
+            if vals is None or node[1] not in vals:
+                raise ValueError('{!r} reads the model variable {!r}, which has no value here'.format(self.text, node[1]))
+            return vals[node[1]]
         if k == 'var':
             if node[1] == 't':
                 return t
             c = 'xyz'.index(node[1])
             return X[..., c] if X is not None and c < X.shape[-1] else 0.0
         if k == 'neg':
-            return -self._eval(node[1], X, t)
+            return -self._eval(node[1], X, t, vals)
         if k == 'import':
             return _import_value(node[1], X, t)
         if k == 'call':
-            return FUNCS[node[1]](*[self._eval(a, X, t) for a in node[2]])
+            return FUNCS[node[1]](*[self._eval(a, X, t, vals) for a in node[2]])
         if k == 'vec':
-            return [self._eval(a, X, t) for a in node[1]]
-        a, b = self._eval(node[1], X, t), self._eval(node[2], X, t)
+            return [self._eval(a, X, t, vals) for a in node[1]]
+        a, b = self._eval(node[1], X, t, vals), self._eval(node[2], X, t, vals)
         return {'+': np.add, '-': np.subtract, '*': np.multiply, '/': np.divide, '^': np.power}[k](a, b)
 
     @property
@@ -248,8 +256,10 @@ class Expr:
         # an imported function depends on space unless it returns a number
         return any(not np.isscalar(fn([0.0], [{}], None, None)) for fn in self._imports)
 
-    def __call__(self, X=None, t=0.0):
-        v = self._eval(self.ast, X, t)
+    def __call__(self, X=None, t=0.0, vals=None):
+        """The value at the points X (N x dim, or None) and time t; `vals` gives the model
+        variables the expression reads ({name: value})."""
+        v = self._eval(self.ast, X, t, vals)
         if isinstance(v, list):
             n = X.shape[0] if X is not None else 1
             return np.stack([np.broadcast_to(np.asarray(c, np.float64), (n,)) for c in v], axis=-1)

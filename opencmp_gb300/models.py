@@ -71,6 +71,39 @@ def _at(v, X, t):
     return np.full(X.shape[:-1], float(v))
 
 
+def affine_parts(v, names: List[str], X, t: float):
+    """A source that reads model variables, split as f = f0 + sum_j k_j c_j: f0 at the points X
+    (c = 0) and the coefficients k_j, which must not vary in space; anything but an affine
+    dependence on the variables is refused. OpenCMP puts the part that reads the unknowns into the
+    bilinear form (multi_component_ins.py:243-257)."""
+    used = [n for n in names if isinstance(v, Expr) and n in v.mvars]
+    other = set(v.mvars) - set(names) if isinstance(v, Expr) else set()
+    if other:
+        raise NotImplementedError('expression {!r} reads {} (not model variables of the GPU path)'.format(
+            v.text, sorted(other)))
+    zero = {n: 0.0 for n in names}
+    f0 = np.asarray(v(X, t, zero), float)
+    ks = {}
+    for n in used:
+        one = dict(zero)
+        one[n] = 1.0
+        k = np.asarray(v(X, t, one), float) - f0
+        two = dict(zero)
+        two[n] = 2.0
+        k2 = np.asarray(v(X, t, two), float) - f0
+        if np.abs(k2 - 2 * k).max() > 1e-12 * max(1.0, np.abs(k).max()) or np.ptp(k) > 1e-12 * max(1.0, np.abs(k).max()):
+            raise NotImplementedError('source {!r}: only constant-coefficient linear terms in the model variables '
+                                      'are on the GPU path'.format(v.text))
+        ks[n] = float(k.reshape(-1)[0])
+    for i, a in enumerate(used):
+        for b in used[i + 1:]:
+            both = dict(zero)
+            both[a] = both[b] = 1.0
+            if np.abs(np.asarray(v(X, t, both), float) - f0 - ks[a] - ks[b]).max() > 1e-12 * max(1.0, abs(ks[a]) + abs(ks[b])):
+                raise NotImplementedError('source {!r}: products of model variables are not on the GPU path'.format(v.text))
+    return f0, ks
+
+
 def checked_solve(solver, b, x, accept: float):
     """Solve; a stop at the iteration cap is accepted when the FP64 relative residual reached
     `accept` (the round-off floor of an ill-conditioned system), otherwise it raises."""
@@ -245,6 +278,16 @@ class Variable:
         f = fs.get(self.name, fs.get('all'))
         if f is None:
             return None, None
+        if isinstance(f, Expr) and f.mvars:
+            # the part that does not read the model variables (the rest is the reaction terms of
+            # Model.reaction)
+            names = list(self.model.vars) or list(self.model.components)
+            X = self.quad_points()
+            f0, _ = affine_parts(f, names, X, t)
+            if np.ptp(f0) == 0.0:
+                c0 = float(f0.reshape(-1)[0])
+                return (c0 if c0 != 0.0 else None), None
+            return None, torch.as_tensor(np.ascontiguousarray(f0.reshape(self.model.mesh.ne, -1)), device='cuda')
         c = _scalar_at(f, t)
         if c is not None:
             return (c if c != 0.0 else None), None
@@ -378,8 +421,37 @@ class Model:
         raise NotImplementedError
 
     # ---------------------------------------------------------------- forms
+    def reaction(self, var: Variable, t: float) -> Dict[str, float]:
+        """{variable: k} of the variable's source terms that read the model's variables (f = f0 +
+        sum_j k_j c_j); empty when the source reads none."""
+        fs = self.functions.get('source', {})
+        f = fs.get(var.name, fs.get('all'))
+        if not (isinstance(f, Expr) and f.mvars):
+            return {}
+        _, ks = affine_parts(f, list(self.vars), var.quad_points()[:1], t)
+        return ks
+
+    def coupled(self) -> bool:
+        """Whether a source reads another variable than its own (the variables' systems couple)."""
+        return any(n != v.name for v in self.vars.values() for n in self.reaction(v, 0.0))
+
+    def coupling_rhs(self, var: Variable, theta: float, dt: float, olds, cur):
+        """The cross-variable reaction terms of a segregated sweep in the linear form:
+        theta dt k_j (c_j, r) at the sweep's current c_j plus (1 - theta) dt k_j (c_j^n, r)."""
+        for name, k in self.reaction(var, getattr(self, 't_form', 0.0)).items():
+            if name == var.name or k == 0.0:
+                continue
+            for coef, vec in ((theta * dt * k, cur[name]), ((1.0 - theta) * dt * k, olds[name])):
+                if coef != 0.0:
+                    r = fem.make_rhs(mass=coef, uprev=vec)
+                    r.accumulate = 1
+                    fem.assemble_rhs(var.space, fem.make_form(), r, var.b)
+
     def form(self, var: Variable, mass: float, dt: float, skeleton_dt: float) -> LB.Form:
-        f = fem.make_form(mass=mass, dt=dt, **self.operator(var))
+        # a source term k c that reads the variable itself goes into the bilinear form as
+        # -dt k (c, r), with the operator's dt (multi_component_ins.py:243-257)
+        k_own = self.reaction(var, getattr(self, 't_form', 0.0)).get(var.name, 0.0)
+        f = fem.make_form(mass=mass - dt * k_own, dt=dt, **self.operator(var))
         f.skeleton_own_dt, f.skeleton_dt = 1, skeleton_dt
         return f
 

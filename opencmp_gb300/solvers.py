@@ -108,6 +108,9 @@ class Solver:
             del keep0
         if transient and getattr(m, 'linearize', None) == 'IMEX' and hasattr(m, 'imex_explicit'):
             m.imex_explicit(v, dt, t_new, uprev)
+        if getattr(self, '_coupling', None) is not None:
+            olds, cur = self._coupling
+            m.coupling_rhs(v, theta if transient else 1.0, dt if transient else 1.0, olds, cur)
         info = v.solve(u_to)
         del keep
         if g is not None:
@@ -149,12 +152,48 @@ class Solver:
             v.guess_dt = dt
         return g
 
+    def _solve_all(self, theta: float, dt: float, t_new: float, t_old: float, transient: bool, src=None, dst=None):
+        """One step of every variable from src into dst ({name: tensor}; None: in place). Where a
+        source reads another variable (coupled reactions, which OpenCMP solves as one compound
+        system), segregated sweeps over the variables repeat, each with the others' latest values
+        and the step's start values, until no variable changes by more than 1e-12 relative: the
+        compound system's solution."""
+        m = self.model
+        names = list(m.vars)
+        src = src or {n: m.vars[n].u for n in names}
+        dst = dst or {n: m.vars[n].u for n in names}
+        if not m.coupled():
+            for n in names:
+                self._solve_var(m.vars[n], theta, dt, t_new, t_old, transient, u_from=src[n], u_to=dst[n])
+            return
+        if self.guess_mode != 'previous':
+            raise NotImplementedError('coupled reactions run with the previous-step initial guess')
+        olds = {n: src[n].clone() for n in names}
+        for n in names:
+            if dst[n].data_ptr() != src[n].data_ptr():
+                dst[n].copy_(src[n])
+        self._coupling = (olds, dst)
+        try:
+            for sweep in range(self.max_sweeps):
+                before = {n: dst[n].clone() for n in names}
+                for n in names:
+                    self._solve_var(m.vars[n], theta, dt, t_new, t_old, transient, u_from=olds[n], u_to=dst[n])
+                change = max(float(torch.linalg.vector_norm(dst[n] - before[n]) /
+                                   max(float(torch.linalg.vector_norm(dst[n])), 1e-300)) for n in names)
+                if sweep > 0 and change <= 1e-12:
+                    return
+        finally:
+            self._coupling = None
+        raise RuntimeError('coupled reactions: the segregated sweeps did not converge in {} sweeps'.format(
+            self.max_sweeps))
+
+    max_sweeps = 200
+
     def _step(self, theta: float, dt: float, t_new: float, t_old: float, transient: bool):
         if hasattr(self.model, 'step'):
             self.model.step(theta, dt, t_new, t_old, transient, self.infos)
             return
-        for v in self.model.vars.values():
-            self._solve_var(v, theta, dt, t_new, t_old, transient)
+        self._solve_all(theta, dt, t_new, t_old, transient)
 
     def solve(self):
         raise NotImplementedError
@@ -259,21 +298,18 @@ class AdaptiveSolver(TransientMultiStepSolver):
 
     def _attempt(self, dt, t_old):
         """Both solutions of every variable for one attempt; returns {name: (kept, other)}."""
-        out = {}
         t_new = t_old + dt
-        for v in self.model.vars.values():
-            if self.scheme == 'adaptive two step':
-                pred, corr = self._buf(v, 'a'), self._buf(v, 'b')
-                self._solve_var(v, 0.5, dt, t_new, t_old, True, u_from=v.u, u_to=pred)
-                self._solve_var(v, 1.0, dt, t_new, t_old, True, u_from=v.u, u_to=corr)
-                out[v.name] = (corr, pred)
-            else:
-                long_, half, short = self._buf(v, 'a'), self._buf(v, 'b'), self._buf(v, 'c')
-                self._solve_var(v, 1.0, dt, t_new, t_old, True, u_from=v.u, u_to=long_)
-                self._solve_var(v, 1.0, dt / 2, t_old + dt / 2, t_old, True, u_from=v.u, u_to=half)
-                self._solve_var(v, 1.0, dt / 2, t_new, t_old + dt / 2, True, u_from=half, u_to=short)
-                out[v.name] = (short, long_)
-        return out
+        vs = self.model.vars
+        cur = {n: v.u for n, v in vs.items()}
+        buf = {k: {n: self._buf(v, k) for n, v in vs.items()} for k in 'abc'}
+        if self.scheme == 'adaptive two step':
+            self._solve_all(0.5, dt, t_new, t_old, True, src=cur, dst=buf['a'])
+            self._solve_all(1.0, dt, t_new, t_old, True, src=cur, dst=buf['b'])
+            return {n: (buf['b'][n], buf['a'][n]) for n in vs}
+        self._solve_all(1.0, dt, t_new, t_old, True, src=cur, dst=buf['a'])
+        self._solve_all(1.0, dt / 2, t_old + dt / 2, t_old, True, src=cur, dst=buf['b'])
+        self._solve_all(1.0, dt / 2, t_new, t_old + dt / 2, True, src=buf['b'], dst=buf['c'])
+        return {n: (buf['c'][n], buf['a'][n]) for n in vs}
 
     def _attempt_model(self, dt, t_old):
         """Both solutions of an attempt for a model that steps itself (INS): the kept one stays in the

@@ -31,7 +31,8 @@ from opencmp_gb300.mesh import load_mesh  # noqa: E402
 
 
 FIXTURES = ['poisson/transient_coarse', 'poisson/h_convergence', 'mcins/diffusion', 'mcins/diffusion_convection',
-            'mcins/purely_convective', 'ins/sinusoidal_transient', 'restart/transient_poisson']
+            'mcins/purely_convective', 'mcins/0th_rxn', 'mcins/1st_rxn', 'mcins/1st_rxn_coupled',
+            'ins/sinusoidal_transient', 'restart/transient_poisson']
 MESHES = ['unit_square_coarse.vol', 'square.msh', 'coarse_large_square_4bcs.vol']
 
 

@@ -50,3 +50,24 @@ def test_import_errors(tmp_path):
         set_import_dir(None)
     with pytest.raises(ValueError):
         parse('IMPORT(source)')          # no run directory
+
+
+def test_model_variables_in_expressions():
+    """A source such as `-5*a + 0.9*5*b` reads the model's variables: parsed as such, evaluated
+    with their values, and split into the part without them and constant coefficients
+    (OpenCMP puts the part that reads the unknowns into the bilinear form)."""
+    from opencmp_gb300.models import affine_parts
+    e = parse('-5*a + 0.9*5*b + 2*x')
+    assert e.mvars == {'a', 'b'}
+    X = np.array([[0.5, 0.0], [0.25, 1.0]])
+    assert np.allclose(e(X, 0.0, {'a': 1.0, 'b': 2.0}), -5 + 9 + 2 * X[:, 0])
+    with pytest.raises(ValueError):
+        e(X, 0.0)                                      # no values for a, b
+    f0, ks = affine_parts(e, ['a', 'b', 'c'], X, 0.0)
+    assert np.allclose(f0, 2 * X[:, 0]) and ks == pytest.approx({'a': -5.0, 'b': 4.5})
+    with pytest.raises(NotImplementedError):
+        affine_parts(parse('a*b'), ['a', 'b'], X, 0.0)  # not affine
+    with pytest.raises(NotImplementedError):
+        affine_parts(parse('x*a'), ['a'], X, 0.0)       # coefficient varies in space
+    with pytest.raises(NotImplementedError):
+        affine_parts(parse('q + 1'), ['a'], X, 0.0)     # not a model variable here
