@@ -106,9 +106,12 @@ def affine_parts(v, names: List[str], X, t: float):
 
 def checked_solve(solver, b, x, accept: float):
     """Solve; a stop at the iteration cap is accepted when the FP64 relative residual reached
-    `accept` (the round-off floor of an ill-conditioned system), otherwise it raises."""
+    `accept` (the round-off floor of an ill-conditioned system), or fell by 1e-12 from the initial
+    residual (NGSolve's Krylov criterion; it decides where the right-hand side cancels to round-off,
+    as when the solution reaches zero), otherwise it raises."""
     info = solver.solve(b, x, raise_on_fail=False)
-    if info.status == LB.NOT_CONVERGED and np.isfinite(info.relres) and info.relres <= accept:
+    if info.status == LB.NOT_CONVERGED and np.isfinite(info.relres) and (
+            info.relres <= accept or (np.isfinite(info.relres0) and info.relres <= 1e-12 * info.relres0)):
         return info
     LB.check(info.status)
     return info
