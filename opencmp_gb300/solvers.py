@@ -281,6 +281,11 @@ class AdaptiveSolver(TransientMultiStepSolver):
         Solver.__init__(self, model_class, config)
         if hasattr(self.model, 'step') and not hasattr(self.model, 'adaptive_state'):
             raise NotImplementedError('adaptive time stepping is not on the GPU path for this model')
+        if not hasattr(self.model, 'step') and self.model.coupled():
+            # the segregated sweeps contract by about (k_ab k_ba dt^2) / ((1 + k_aa dt)(1 + k_bb dt)),
+            # which tends to a constant near 1 as the adaptive step grows
+            raise NotImplementedError('coupled reactions with adaptive time steps are not on the GPU path (the '
+                                      'segregated sweeps slow down as the step grows)')
         self.scheme = config.get_item(['TRANSIENT', 'scheme'], str)
         self.t_range = config.get_list(['TRANSIENT', 'time_range'], float)
         self.dt = config.get_item(['TRANSIENT', 'dt'], float)
