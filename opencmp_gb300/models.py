@@ -104,15 +104,33 @@ def affine_parts(v, names: List[str], X, t: float):
     return f0, ks
 
 
+def _accepted(info, accept: float) -> bool:
+    return info.status == LB.OK or (info.status == LB.NOT_CONVERGED and np.isfinite(info.relres) and (
+        info.relres <= accept or (np.isfinite(info.relres0) and info.relres <= 1e-12 * info.relres0)))
+
+
 def checked_solve(solver, b, x, accept: float):
     """Solve; a stop at the iteration cap is accepted when the FP64 relative residual reached
     `accept` (the round-off floor of an ill-conditioned system), or fell by 1e-12 from the initial
     residual (NGSolve's Krylov criterion; it decides where the right-hand side cancels to round-off,
-    as when the solution reaches zero), otherwise it raises."""
+    as when the solution reaches zero), otherwise it raises.
+
+    A solve that fails from an initial guess whose residual is larger than the right-hand side
+    (relres0 > 1: the right-hand side cancelled far below the guess's residual, as when the solution
+    reaches zero in one step) is repeated once from zero on the free dofs: the round-off of cancelling
+    the guess, eps |A| |x0|, is what kept the first attempt from the tolerance."""
     info = solver.solve(b, x, raise_on_fail=False)
-    if info.status == LB.NOT_CONVERGED and np.isfinite(info.relres) and (
-            info.relres <= accept or (np.isfinite(info.relres0) and info.relres <= 1e-12 * info.relres0)):
+    if _accepted(info, accept):
         return info
+    space = getattr(getattr(solver, 'mat', None), 'space', None)
+    if (info.status == LB.NOT_CONVERGED and np.isfinite(info.relres0) and info.relres0 > 1.0
+            and hasattr(space, 'FreeDofs')):
+        free = space.FreeDofs()
+        if free.shape[0] == x.numel():
+            x[torch.from_numpy(free).to(x.device)] = 0.0
+            info = solver.solve(b, x, raise_on_fail=False)
+            if _accepted(info, accept):
+                return info
     LB.check(info.status)
     return info
 

@@ -23,10 +23,6 @@ SUPPORTED = ('explicit euler', 'implicit euler', 'crank nicolson', 'euler IMEX',
 # Explicit Euler on the order-3 DG Poisson forms of the coarse fixture amplifies by 5.0 per step
 # (test_explicit_dg_poisson_is_unstable): every run of it, the oracle's included, overflows.
 UNSTABLE = {'test_poisson.py::TestTransient::test_explicit_euler_dg'}
-# Known failure on the GPU path: on the DG zero-order reaction case the adaptive step grows to about
-# 3 and the CG solve of the next step's Crank-Nicolson predictor stops at its iteration cap (the
-# continuous-space variant passes); not yet explained.
-KNOWN_FAILING = {'test_mcins.py::TestZeroOrderRxn::test_adaptive_2_step_dg'}
 
 
 def _load(case) -> ConfigParser:
@@ -64,8 +60,6 @@ def _cases():
             marks = [pytest.mark.skip(reason='the scheme is unstable on these forms (amplification 5.0 per step)')]
         elif t['fixture'] == 'mcins_1st_rxn_coupled' and scheme.startswith('adaptive'):
             marks = [pytest.mark.skip(reason='coupled reactions with adaptive time steps are not on the GPU path')]
-        elif t['id'] in KNOWN_FAILING:
-            marks = [pytest.mark.skip(reason='known failure on the GPU path (see KNOWN_FAILING)')]
         else:
             marks = []
         out.append(pytest.param(t, id=t['id'].split('::', 1)[1].replace('::', '-'), marks=marks))
