@@ -58,8 +58,6 @@ def _cases():
                                              'Euler or Crank-Nicolson (Oseen) or the IMEX schemes')]
         elif t['id'] in UNSTABLE:
             marks = [pytest.mark.skip(reason='the scheme is unstable on these forms (amplification 5.0 per step)')]
-        elif t['fixture'] == 'mcins_1st_rxn_coupled' and scheme.startswith('adaptive'):
-            marks = [pytest.mark.skip(reason='coupled reactions with adaptive time steps are not on the GPU path')]
         else:
             marks = []
         out.append(pytest.param(t, id=t['id'].split('::', 1)[1].replace('::', '-'), marks=marks))
